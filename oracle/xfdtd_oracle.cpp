@@ -1,0 +1,1563 @@
+// xfdtd_oracle.cpp -- TEST INFRASTRUCTURE ONLY (the checker, never the product).
+//
+// Plain C++17 FP64 restatement of the reference XFDTD step loop and its setup,
+// following the reference sources line by line (citations are paths inside
+// the reference project).  It keeps the reference's data layout: one array
+// per field component and one per-cell FP64 array per update coefficient, in
+// the component shapes of src/simulation/simulation_init.cpp:28-35 and
+// src/fdtd_basic_coff/fdtd_basic_coff.cpp:313-339, row-major with z fastest.
+//
+// Build with -ffp-contract=off so that every product and sum rounds the way
+// the reference's plain C++ does.  The OpenMP pragmas only split independent
+// per-cell loops; results do not depend on the thread count.
+//
+// Where the reference reads memory it never initialised (PML psi arrays on
+// the XP/YP faces, perfect_match_layer.cpp:159-175,212-230; VoltageMonitor
+// value, voltage_monitor.cpp:61,72; the TFSF 1-D arrays, tfsf_3d.cpp:58-65),
+// this restatement uses zero, the evident intent.  Where the reference's
+// Y-axis lumped-element setup assigns _da twice and never _db
+// (current_source.cpp:86-87, resistor.cpp:51-52, capacitor.cpp:52-53,
+// inductor.cpp:48-49) or tests `YN || YN` (voltage_source.cpp:80), the
+// intended assignment is used; the reference path there is not well defined.
+
+#include "xfdtd_oracle.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+using cplx = std::complex<double>;
+
+// src/include/util/constant.h:10-29
+constexpr double PI = M_PI;
+constexpr double EPSILON_0 = 8.854187817e-12;
+constexpr double MU_0 = 4 * PI * 1e-7;
+constexpr double SQUARED_C_0 = 1 / (EPSILON_0 * MU_0);
+const double ETA_0 = std::sqrt(MU_0 / EPSILON_0);
+const double C_0 = std::sqrt(SQUARED_C_0);
+constexpr double TOLERABLE_EPSILON = 10 * std::numeric_limits<double>::epsilon();
+
+thread_local std::string g_error;
+
+// src/include/util/float_compare.h:9-24
+bool isLessOrEqual(double a, double b, double eps = TOLERABLE_EPSILON) {
+  return (std::abs(a - b) < eps) ? true : (a < b);
+}
+bool isGreaterOrEqual(double a, double b, double eps = TOLERABLE_EPSILON) {
+  return (std::abs(a - b) < eps) ? true : (a > b);
+}
+
+struct A3 {
+  size_t n0 = 0, n1 = 0, n2 = 0;
+  std::vector<double> v;
+  void init(size_t a, size_t b, size_t c, double fill = 0.0) {
+    n0 = a; n1 = b; n2 = c;
+    v.assign(a * b * c, fill);
+  }
+  double &operator()(size_t i, size_t j, size_t k) { return v[(i * n1 + j) * n2 + k]; }
+  double operator()(size_t i, size_t j, size_t k) const { return v[(i * n1 + j) * n2 + k]; }
+};
+
+struct C3 {
+  size_t n0 = 0, n1 = 0, n2 = 0;
+  std::vector<cplx> v;
+  void init(size_t a, size_t b, size_t c) {
+    n0 = a; n1 = b; n2 = c;
+    v.assign(a * b * c, cplx(0.0, 0.0));
+  }
+  cplx &operator()(size_t i, size_t j, size_t k) { return v[(i * n1 + j) * n2 + k]; }
+};
+
+// ---------------------------------------------------------------- shapes ---
+struct Box {  // Cube(point, size): src/include/shape/cube.h:35-49
+  double p[3], s[3];
+  double mn(int a) const { return p[a]; }
+  double mx(int a) const { return p[a] + s[a]; }
+};
+
+struct Shape {
+  xfdtd_shape_desc d;
+  // getWrappedBox: sphere.cpp:32-36, cube.cpp:39-41, cylinder.cpp:45-66
+  Box wrapped() const {
+    Box b{};
+    if (d.kind == XFDTD_SHAPE_CUBE) {
+      for (int a = 0; a < 3; ++a) { b.p[a] = d.point[a]; b.s[a] = d.size[a]; }
+    } else if (d.kind == XFDTD_SHAPE_SPHERE) {
+      for (int a = 0; a < 3; ++a) { b.p[a] = d.point[a] - d.radius; b.s[a] = 2 * d.radius; }
+    } else {
+      for (int a = 0; a < 3; ++a) {
+        if (a == d.axis) { b.p[a] = d.point[a] - d.height / 2; b.s[a] = d.height; }
+        else { b.p[a] = d.point[a] - d.radius; b.s[a] = 2 * d.radius; }
+      }
+    }
+    return b;
+  }
+  static bool cubeInside(const Box &b, const double *q) {  // cube.cpp:27-37
+    return isLessOrEqual(b.p[0], q[0]) && isLessOrEqual(b.p[1], q[1]) &&
+           isLessOrEqual(b.p[2], q[2]) && isGreaterOrEqual(b.p[0] + b.s[0], q[0]) &&
+           isGreaterOrEqual(b.p[1] + b.s[1], q[1]) && isGreaterOrEqual(b.p[2] + b.s[2], q[2]);
+  }
+  bool inside(const double *q) const {
+    if (d.kind == XFDTD_SHAPE_CUBE) {
+      Box b = wrapped();
+      return cubeInside(b, q);
+    }
+    if (d.kind == XFDTD_SHAPE_SPHERE) {  // sphere.cpp:27-30 (xt::norm_l2)
+      double dx = q[0] - d.point[0], dy = q[1] - d.point[1], dz = q[2] - d.point[2];
+      double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
+      return isLessOrEqual(dist, d.radius);
+    }
+    // cylinder.cpp:26-43
+    if (!cubeInside(wrapped(), q)) return false;
+    int a0 = d.axis == 0 ? 1 : 0;
+    int a1 = d.axis == 2 ? 1 : 2;
+    double dis = std::sqrt(std::pow(q[a0] - d.point[a0], 2) + std::pow(q[a1] - d.point[a1], 2));
+    return isLessOrEqual(dis, d.radius);
+  }
+};
+
+// ------------------------------------------------------------- GridSpace ---
+struct GridBox {  // src/grid/grid_box.cpp:5-105
+  size_t o[3], n[3];
+  size_t start(int a) const { return o[a]; }
+  size_t end(int a) const { return o[a] + n[a]; }
+};
+
+struct GridSpace {  // src/grid/grid_space.cpp (uniform construction only)
+  double base[3];
+  double mn[3], mx[3];
+  size_t n[3] = {0, 0, 0};
+  bool ready = false;
+  std::vector<double> ec[3], hc[3], es[3], hs[3];
+
+  explicit GridSpace(double dl) {  // grid_space.cpp:14-27
+    for (int a = 0; a < 3; ++a) {
+      base[a] = dl;
+      mn[a] = std::numeric_limits<double>::max();
+      mx[a] = std::numeric_limits<double>::min();  // smallest positive normal, as there
+    }
+  }
+  void resizeSpaceSize(const double *nmn, const double *nmx) {  // :576-618
+    for (int a = 0; a < 3; ++a) {
+      if (mn[a] > nmn[a]) mn[a] = nmn[a];
+      if (mx[a] < nmx[a]) mx[a] = nmx[a];
+    }
+    size_t nn[3];
+    for (int a = 0; a < 3; ++a) {
+      nn[a] = static_cast<size_t>(std::round((mx[a] - mn[a]) / base[a]));
+      if (mx[a] < mn[a]) nn[a] = 1;
+    }
+    for (int a = 0; a < 3; ++a) n[a] = std::max(n[a], nn[a]);
+  }
+  void calculateSpaceSize(const Box &b) {  // :351-362, :620-623
+    if (ready) throw std::runtime_error("GridSpace is ready");
+    double a[3], c[3];
+    for (int q = 0; q < 3; ++q) { a[q] = b.mn(q); c[q] = b.mx(q); }
+    resizeSpaceSize(a, c);
+  }
+  void extendBoundary(int ori, double size) {  // :364-464
+    if (ready) throw std::runtime_error("GridSpace is ready");
+    int axis = ori / 2;
+    if (n[axis] <= 1) throw std::runtime_error("GridSpace is not extended");
+    if (size < 0) throw std::runtime_error("size is less than 0");
+    double a[3] = {mn[0], mn[1], mn[2]}, c[3] = {mx[0], mx[1], mx[2]};
+    if (ori % 2 == 0) a[axis] = mn[axis] - size; else c[axis] = mx[axis] + size;
+    resizeSpaceSize(a, c);
+  }
+  void generateUniformGridSpace() {  // :501-536, :625-638, :679-689, :737-757
+    if (ready) throw std::runtime_error("GridSpace is ready");
+    for (int a = 0; a < 3; ++a) n[a] = std::max<size_t>(n[a], 1);
+    if (!(n[0] > 1 && n[1] > 1 && n[2] > 1))
+      throw std::runtime_error("only three-dimensional grids are restated");
+    for (int a = 0; a < 3; ++a) {
+      ec[a].resize(n[a] + 1);
+      for (size_t i = 0; i <= n[a]; ++i) ec[a][i] = mn[a] + static_cast<double>(i) * base[a];
+      hc[a].resize(n[a]);
+      for (size_t i = 0; i < n[a]; ++i) hc[a][i] = (ec[a][i] + ec[a][i + 1]) / 2;
+      std::vector<double> virt(n[a] + 2);
+      virt[0] = hc[a].front() - base[a];
+      for (size_t i = 0; i < n[a]; ++i) virt[i + 1] = hc[a][i];
+      virt[n[a] + 1] = hc[a].back() + base[a];
+      hs[a].resize(n[a] + 1);
+      for (size_t i = 0; i <= n[a]; ++i) hs[a][i] = virt[i + 1] - virt[i];
+      es[a].resize(n[a]);
+      for (size_t i = 0; i < n[a]; ++i) es[a][i] = ec[a][i + 1] - ec[a][i];
+      n[a] = hc[a].size();
+    }
+  }
+  size_t handleTransform(int a, double x) const {  // :551-574 (argmin, first minimum)
+    if (x < mn[a]) throw std::out_of_range("coordinate is out of range");
+    size_t best = 0;
+    double bd = std::abs(ec[a][0] - x);
+    for (size_t i = 1; i < ec[a].size(); ++i) {
+      double d = std::abs(ec[a][i] - x);
+      if (d < bd) { bd = d; best = i; }
+    }
+    return best;
+  }
+  GridBox getGridBox(const Shape &s) const {  // :306-329
+    Box b = s.wrapped();
+    GridBox g{};
+    for (int a = 0; a < 3; ++a) {
+      size_t st = handleTransform(a, b.mn(a));
+      size_t en = handleTransform(a, b.mx(a));
+      if (en < st) throw std::range_error("end < start");
+      g.o[a] = st;
+      g.n[a] = en - st;
+    }
+    return g;
+  }
+  GridBox getGridBox(const double *p, const double *sz) const {
+    Shape s{};
+    s.d.kind = XFDTD_SHAPE_CUBE;
+    for (int a = 0; a < 3; ++a) { s.d.point[a] = p[a]; s.d.size[a] = sz[a]; }
+    return getGridBox(s);
+  }
+};
+
+// -------------------------------------------------------------- waveform ---
+struct Waveform {  // src/waveform/*.cpp
+  xfdtd_waveform_desc d;
+  double amplitude;
+  std::vector<double> value;
+  double f(double t) const {  // getValueByTime without the amplitude
+    switch (d.kind) {
+      case XFDTD_WAVE_GAUSSIAN:  // gaussian_waveform.cpp:18-24
+        return std::exp(-std::pow((t - d.t0) / d.tau, 2));
+      case XFDTD_WAVE_COS_GAUSSIAN:  // cosine_modulated_gaussian_waveform.cpp:24-35
+        return std::cos(2 * PI * d.frequency * (t - d.t0)) * std::exp(-std::pow((t - d.t0) / d.tau, 2));
+      case XFDTD_WAVE_SINUSOIDAL:  // sinusoidal_waveform.cpp
+        return std::sin(2 * PI * d.frequency * t + d.phase);
+      default:  // custom_waveform.cpp:13-23
+        return d.fn(t, d.ctx);
+    }
+  }
+  void init(const std::vector<double> &times) {
+    value.resize(times.size());
+    for (size_t i = 0; i < times.size(); ++i) {
+      if (d.kind == XFDTD_WAVE_GAUSSIAN)
+        value[i] = amplitude * std::exp(-std::pow((times[i] - d.t0) / d.tau, 2));
+      else if (d.kind == XFDTD_WAVE_COS_GAUSSIAN)
+        value[i] = amplitude * std::cos(2 * PI * d.frequency * (times[i] - d.t0)) *
+                   std::exp(-std::pow((times[i] - d.t0) / d.tau, 2));
+      else if (d.kind == XFDTD_WAVE_SINUSOIDAL)
+        value[i] = amplitude * std::sin(2 * PI * d.frequency * times[i] + d.phase);
+      else
+        value[i] = amplitude * d.fn(times[i], d.ctx);
+    }
+  }
+};
+
+// xt::linspace(start, stop, num) with endpoint: start + i * step, step = (stop-start)/(num-1)
+std::vector<double> linspace(double start, double stop, size_t num) {
+  std::vector<double> v(num);
+  if (num == 1) { v[0] = start; return v; }
+  double step = (stop - start) / static_cast<double>(num - 1);
+  for (size_t i = 0; i < num; ++i) v[i] = start + static_cast<double>(i) * step;
+  return v;
+}
+
+// ------------------------------------------------------------------- PML ---
+struct PML {  // src/boundary/perfect_match_layer.cpp
+  xfdtd_pml_desc d;
+  double dl = 0, dt = 0;
+  size_t start = 0;
+  int na = 0, nb = 0;
+  int axis = 0, aa = 0, ab = 0;  // normal axis and the a/b axes
+  std::vector<double> kappa_e, kappa_m, a_e, b_e, a_m, b_m;
+  A3 psi_ea, psi_eb, psi_ha, psi_hb, c_ea, c_eb, c_ha, c_hb;
+  bool positive() const { return d.orientation % 2 == 1; }
+};
+
+// -------------------------------------------------------------- lumped ----
+struct Lumped {
+  xfdtd_lumped_desc d;
+  size_t s[3] = {0, 0, 0}, e[3] = {0, 0, 0};
+  int comp = 0;  // 0 x, 1 y, 2 z
+  Waveform wave;
+  std::vector<double> da, db, dc, beta, coff;  // over the box, row-major
+  std::vector<double> cecjc, cjcec, jcur;      // inductor
+  double factor = 0, amp_factor = 0;
+};
+
+struct Monitor {
+  xfdtd_monitor_desc d;
+  size_t s[3] = {0, 0, 0}, e[3] = {0, 0, 0};
+  std::vector<double> coff, da, db;
+  double positive = 1;
+  std::vector<double> value;
+};
+
+struct Sim;
+
+}  // namespace
+
+struct oracle_sim {
+  // scene
+  double cell = 0;
+  float cfl = 0.99f;
+  std::vector<xfdtd_object_desc> objects;
+  std::vector<PML> pmls;
+  std::vector<Lumped> lumped;
+  std::vector<Monitor> monitors;
+  bool has_tfsf = false, has_nffft = false;
+  xfdtd_tfsf_desc tfsf_d{};
+  std::vector<xfdtd_material_desc> voxel_mats;
+  std::vector<uint16_t> voxel_idx;
+  int64_t voxel_shape[3] = {0, 0, 0};
+
+  std::unique_ptr<GridSpace> gs;
+  size_t nx = 0, ny = 0, nz = 0;
+  double dt = 0;
+  size_t total = 0, cur = 0;
+
+  A3 eps[3], mu[3], sig[3], sigm[3];
+  A3 cexe, cexhy, cexhz, ceye, ceyhz, ceyhx, ceze, cezhx, cezhy;
+  A3 chxh, chxey, chxez, chyh, chyez, chyex, chzh, chzex, chzey;
+  A3 ex, ey, ez, hx, hy, hz;
+
+  // TFSF3D (src/tfsf/tfsf_3d.cpp)
+  struct {
+    size_t dist[3];
+    double e0, theta, phi, psi;
+    double k[3], te[3], th[3];
+    size_t L = 0;
+    size_t li, ri, lj, rj, lk, rk;
+    std::vector<double> e_inc, h_inc, exi, eyi, ezi, hxi, hyi, hzi;
+    std::vector<double> px_f, py_f, pz_f, px_h, py_h, pz_h;
+    double scaled_dl, ceie = 1.0, ceihi, chih = 1.0, chiei;
+    double a = 0, b = 0;
+    Waveform wave;
+  } tf;
+
+  // NffftFd (src/nffft/nffft_fd.cpp)
+  struct {
+    size_t dist[3];
+    size_t li, ri, lj, rj, lk, rk, bx, by, bz;
+    std::vector<double> freq, k, theta, phi;
+    std::vector<C3> acc;             // 24 arrays, order documented in the header
+    std::vector<cplx> tj, tm;        // [nf][total]
+    bool ff_valid = false;
+    size_t ff_step = 0;
+    std::vector<cplx> out[8];
+    std::vector<double> power[2];
+  } nf;
+
+  A3 &field(int c) {
+    switch (c) {
+      case 0: return ex; case 1: return ey; case 2: return ez;
+      case 3: return hx; case 4: return hy; default: return hz;
+    }
+  }
+  A3 &coeff(int w) {
+    A3 *t[18] = {&cexe, &cexhy, &cexhz, &ceye, &ceyhz, &ceyhx, &ceze, &cezhx, &cezhy,
+                 &chxh, &chxey, &chxez, &chyh, &chyez, &chyex, &chzh, &chzex, &chzey};
+    return *t[w];
+  }
+
+  void init();
+  void initObjects();
+  void initCoff();
+  void initThinWire(const xfdtd_object_desc &o);
+  void initTFSF();
+  void initNFFFT();
+  void initLumpedElement(Lumped &l);
+  void correctCoffLumped(Lumped &l);
+  void initPML(PML &p);
+  void initMonitor(Monitor &m);
+  void step();
+  void updateE();
+  void updateH();
+  void pmlE(PML &p);
+  void pmlH(PML &p);
+  void tfsfIncident(size_t t);
+  void tfsfE();
+  void tfsfH();
+  void lumpedE(Lumped &l);
+  void nffftUpdate();
+  void monitorUpdate(Monitor &m);
+  void farField();
+};
+
+namespace {
+// Maps (normal, a, b) coordinates to (i, j, k).
+inline void nab2ijk(int axis, int aa, int ab, size_t vn, size_t va, size_t vb, size_t *ijk) {
+  ijk[axis] = vn;
+  ijk[aa] = va;
+  ijk[ab] = vb;
+}
+}  // namespace
+
+// ------------------------------------------------------------------ init ---
+void oracle_sim::init() {
+  // initGridSpace, src/simulation/simulation_init.cpp:105-146
+  gs.reset(new GridSpace(cell));
+  for (auto &o : objects) {
+    Shape s{};
+    s.d = o.shape;
+    gs->calculateSpaceSize(s.wrapped());
+  }
+  for (auto &p : pmls) gs->extendBoundary(p.d.orientation, p.d.thickness * gs->base[p.d.orientation / 2]);
+  gs->generateUniformGridSpace();
+  gs->ready = true;
+  nx = gs->n[0]; ny = gs->n[1]; nz = gs->n[2];
+
+  // FDTDBasicCoff::init, fdtd_basic_coff.cpp:11-29, :313-354
+  double cfl_d = static_cast<double>(cfl);
+  dt = cfl_d / (C_0 * std::sqrt(1.0 / (gs->base[0] * gs->base[0]) + 1.0 / (gs->base[1] * gs->base[1]) +
+                                 1.0 / (gs->base[2] * gs->base[2])));
+  eps[0].init(nx, ny + 1, nz + 1, EPSILON_0);
+  eps[1].init(nx + 1, ny, nz + 1, EPSILON_0);
+  eps[2].init(nx + 1, ny + 1, nz, EPSILON_0);
+  mu[0].init(nx + 1, ny, nz, MU_0);
+  mu[1].init(nx, ny + 1, nz, MU_0);
+  mu[2].init(nx, ny, nz + 1, MU_0);
+  sig[0].init(nx, ny + 1, nz + 1);
+  sig[1].init(nx + 1, ny, nz + 1);
+  sig[2].init(nx + 1, ny + 1, nz);
+  sigm[0].init(nx + 1, ny, nz);
+  sigm[1].init(nx, ny + 1, nz);
+  sigm[2].init(nx, ny, nz + 1);
+
+  // initEMInstance, simulation_init.cpp:28-35
+  ex.init(nx, ny + 1, nz + 1);
+  ey.init(nx + 1, ny, nz + 1);
+  ez.init(nx + 1, ny + 1, nz);
+  hx.init(nx + 1, ny, nz);
+  hy.init(nx, ny + 1, nz);
+  hz.init(nx, ny, nz + 1);
+
+  initObjects();
+  if (has_tfsf) initTFSF();
+  if (has_nffft) initNFFFT();
+  for (auto &l : lumped) initLumpedElement(l);
+  // initUpdateCoefficient, simulation_init.cpp:82-91
+  initCoff();
+  for (auto &o : objects)
+    if (o.kind == XFDTD_OBJECT_THIN_WIRE) initThinWire(o);
+  for (auto &l : lumped) correctCoffLumped(l);
+  // initBoundaryCondition, :93-97
+  for (auto &p : pmls) initPML(p);
+  for (auto &m : monitors) initMonitor(m);
+  // the per-cell material arrays are no longer read after this point
+  for (int a = 0; a < 3; ++a) {
+    mu[a] = A3(); sigm[a] = A3();
+  }
+}
+
+void oracle_sim::initObjects() {
+  // Object::init, src/object/object.cpp:53-73; mask from cell centres,
+  // grid_space.cpp:274-283.  xt::filter(arr, mask) writes arr(i,j,k) for
+  // every masked cell (i,j,k) of the (nx,ny,nz) mask.
+  for (auto &o : objects) {
+    if (o.kind == XFDTD_OBJECT_THIN_WIRE) {
+      // ThinWire::init only checks the shape (thin_wire.cpp:17-37)
+      if (o.shape.kind != XFDTD_SHAPE_CYLINDER) throw std::runtime_error("ThinWire only support Cylinder shape");
+      double r = o.shape.radius;
+      bool thin = false;
+      if (o.shape.axis == 0) thin = r < gs->base[1] / 2 && r < gs->base[2] / 2;
+      if (o.shape.axis == 1) thin = r < gs->base[0] / 2 && r < gs->base[2] / 2;
+      if (o.shape.axis == 2) thin = r < gs->base[0] / 2 && r < gs->base[1] / 2;
+      if (!thin) throw std::runtime_error("ThinWire is not enough thin");
+      continue;
+    }
+    Shape s{};
+    s.d = o.shape;
+    gs->getGridBox(s);  // Object::init computes (and discards) the grid box; it can throw
+    double e = static_cast<double>(o.material.eps_r) * EPSILON_0;  // material.cpp:7-16
+    double m = static_cast<double>(o.material.mu_r) * MU_0;
+    double se = o.material.sigma_e, sm = o.material.sigma_m;
+#pragma omp parallel for schedule(static)
+    for (long long ii = 0; ii < static_cast<long long>(nx); ++ii) {
+      size_t i = static_cast<size_t>(ii);
+      double q[3];
+      q[0] = gs->hc[0][i];
+      for (size_t j = 0; j < ny; ++j) {
+        q[1] = gs->hc[1][j];
+        for (size_t k = 0; k < nz; ++k) {
+          q[2] = gs->hc[2][k];
+          if (!s.inside(q)) continue;
+          for (int a = 0; a < 3; ++a) {
+            eps[a](i, j, k) = e; mu[a](i, j, k) = m;
+            sig[a](i, j, k) = se; sigm[a](i, j, k) = sm;
+          }
+        }
+      }
+    }
+  }
+  // Voxel raster: one 1-cell cube object per voxel, after all objects.
+  if (!voxel_idx.empty()) {
+    if (voxel_shape[0] != static_cast<int64_t>(nx) || voxel_shape[1] != static_cast<int64_t>(ny) ||
+        voxel_shape[2] != static_cast<int64_t>(nz))
+      throw std::runtime_error("voxel raster shape does not match the grid");
+#pragma omp parallel for schedule(static)
+    for (long long ii = 0; ii < static_cast<long long>(nx); ++ii) {
+      size_t i = static_cast<size_t>(ii);
+      for (size_t j = 0; j < ny; ++j)
+        for (size_t k = 0; k < nz; ++k) {
+          const xfdtd_material_desc &md = voxel_mats[voxel_idx[(i * ny + j) * nz + k]];
+          double e = static_cast<double>(md.eps_r) * EPSILON_0;
+          double m = static_cast<double>(md.mu_r) * MU_0;
+          for (int a = 0; a < 3; ++a) {
+            eps[a](i, j, k) = e; mu[a](i, j, k) = m;
+            sig[a](i, j, k) = md.sigma_e; sigm[a](i, j, k) = md.sigma_m;
+          }
+        }
+    }
+  }
+}
+
+void oracle_sim::initCoff() {
+  // FDTDBasicCoff::initCoff, fdtd_basic_coff.cpp:66-121.  Node sizes come
+  // from the coordinate differences of the GridSpace, as there.
+  const auto &esx = gs->es[0], &esy = gs->es[1], &esz = gs->es[2];
+  const auto &hsx = gs->hs[0], &hsy = gs->hs[1], &hsz = gs->hs[2];
+  auto ce = [&](double da, double db, double eps_, double sigma, double &cece, double &cecha, double &cechb) {
+    cece = (2 * eps_ - dt * sigma) / (2 * eps_ + dt * sigma);
+    cecha = -(2 * dt / db) / (2 * eps_ + sigma * dt);
+    cechb = (2 * dt / da) / (2 * eps_ + sigma * dt);
+  };
+  auto ch = [&](double da, double db, double mu_, double sm, double &chch, double &chcea, double &chceb) {
+    chch = (2 * mu_ - dt * sm) / (2 * mu_ + dt * sm);
+    chcea = (2 * dt / db) / (2 * mu_ + sm * dt);
+    chceb = -(2 * dt / da) / (2 * mu_ + sm * dt);
+  };
+  cexe.init(nx, ny + 1, nz + 1); cexhy.init(nx, ny + 1, nz + 1); cexhz.init(nx, ny + 1, nz + 1);
+  ceye.init(nx + 1, ny, nz + 1); ceyhz.init(nx + 1, ny, nz + 1); ceyhx.init(nx + 1, ny, nz + 1);
+  ceze.init(nx + 1, ny + 1, nz); cezhx.init(nx + 1, ny + 1, nz); cezhy.init(nx + 1, ny + 1, nz);
+  chxh.init(nx + 1, ny, nz); chxey.init(nx + 1, ny, nz); chxez.init(nx + 1, ny, nz);
+  chyh.init(nx, ny + 1, nz); chyez.init(nx, ny + 1, nz); chyex.init(nx, ny + 1, nz);
+  chzh.init(nx, ny, nz + 1); chzex.init(nx, ny, nz + 1); chzey.init(nx, ny, nz + 1);
+  // Ex: meshgrid(e_x, h_y, h_z); da = h_y, db = h_z
+  for (size_t i = 0; i < nx; ++i)
+    for (size_t j = 0; j <= ny; ++j)
+      for (size_t k = 0; k <= nz; ++k)
+        ce(hsy[j], hsz[k], eps[0](i, j, k), sig[0](i, j, k), cexe(i, j, k), cexhy(i, j, k), cexhz(i, j, k));
+  // Ey: meshgrid(h_x, e_y, h_z); da = h_z, db = h_x
+  for (size_t i = 0; i <= nx; ++i)
+    for (size_t j = 0; j < ny; ++j)
+      for (size_t k = 0; k <= nz; ++k)
+        ce(hsz[k], hsx[i], eps[1](i, j, k), sig[1](i, j, k), ceye(i, j, k), ceyhz(i, j, k), ceyhx(i, j, k));
+  // Ez: meshgrid(h_x, h_y, e_z); da = h_x, db = h_y
+  for (size_t i = 0; i <= nx; ++i)
+    for (size_t j = 0; j <= ny; ++j)
+      for (size_t k = 0; k < nz; ++k)
+        ce(hsx[i], hsy[j], eps[2](i, j, k), sig[2](i, j, k), ceze(i, j, k), cezhx(i, j, k), cezhy(i, j, k));
+  // Hx: meshgrid(h_x, e_y, e_z); da = e_y, db = e_z
+  for (size_t i = 0; i <= nx; ++i)
+    for (size_t j = 0; j < ny; ++j)
+      for (size_t k = 0; k < nz; ++k)
+        ch(esy[j], esz[k], mu[0](i, j, k), sigm[0](i, j, k), chxh(i, j, k), chxey(i, j, k), chxez(i, j, k));
+  // Hy: meshgrid(e_x, h_y, e_z); da = e_z, db = e_x
+  for (size_t i = 0; i < nx; ++i)
+    for (size_t j = 0; j <= ny; ++j)
+      for (size_t k = 0; k < nz; ++k)
+        ch(esz[k], esx[i], mu[1](i, j, k), sigm[1](i, j, k), chyh(i, j, k), chyez(i, j, k), chyex(i, j, k));
+  // Hz: meshgrid(e_x, e_y, h_z); da = e_x, db = e_y
+  for (size_t i = 0; i < nx; ++i)
+    for (size_t j = 0; j < ny; ++j)
+      for (size_t k = 0; k <= nz; ++k)
+        ch(esx[i], esy[j], mu[2](i, j, k), sigm[2](i, j, k), chzh(i, j, k), chzex(i, j, k), chzey(i, j, k));
+}
+
+void oracle_sim::initThinWire(const xfdtd_object_desc &o) {
+  // ThinWire::correctFDTDCoff, src/object/thin_wire.cpp:39-129
+  Shape s{};
+  s.d = o.shape;
+  GridBox g = gs->getGridBox(s);
+  size_t is = g.start(0), ie = g.end(0), js = g.start(1), je = g.end(1), ks = g.start(2), ke = g.end(2);
+  double dx = gs->base[0], dy = gs->base[1], dz = gs->base[2];
+  double r = o.shape.radius;
+  if (o.shape.axis == XFDTD_AXIS_X) {
+    for (size_t i = is; i < ie; ++i) { cexe(i, js, ks) = 0.0; cexhy(i, js, ks) = 0.0; cexhz(i, js, ks) = 0.0; }
+    double khy = dz * std::atan(dy / dy) / dy;
+    double khz = dy * std::atan(dz / dy) / dz;
+    for (size_t i = is; i < ie; ++i)
+      for (size_t k = ks - 1; k < ks + 1; ++k) chyex(i, js, k) = khy * 2 * chyex(i, js, k) / std::log(dz / r);
+    for (size_t i = is; i < ie; ++i)
+      for (size_t j = js - 1; j < js + 1; ++j) chzex(i, j, ks) = khz * 2 * chzex(i, j, ks) / std::log(dy / r);
+  } else if (o.shape.axis == XFDTD_AXIS_Y) {
+    // the E coefficients are left alone on this axis (commented out there)
+    double khz = dx * std::atan(dz / dx) / dz;
+    double khx = dz * std::atan(dx / dz) / dx;
+    for (size_t i = is - 1; i < is + 1; ++i)
+      for (size_t j = js; j < je; ++j) chzey(i, j, ks) = khz * 2 * chzey(i, j, ks) / std::log(dx / r);
+    for (size_t j = js; j < je; ++j)
+      for (size_t k = ks - 1; k < ks + 1; ++k) chxey(is, j, k) = khx * 2 * chxey(is, j, k) / std::log(dz / r);
+  } else {
+    for (size_t k = ks; k < ke; ++k) { ceze(is, js, k) = 0.0; cezhx(is, js, k) = 0.0; cezhy(is, js, k) = 0.0; }
+    double khx = dy * std::atan(dx / dy) / dx;
+    double khy = dx * std::atan(dy / dx) / dy;
+    for (size_t j = js - 1; j < js + 1; ++j)
+      for (size_t k = ks; k < ke; ++k) chxez(is, j, k) = khx * 2 * chxez(is, j, k) / std::log(dy / r);
+    for (size_t i = is - 1; i < is + 1; ++i)
+      for (size_t k = ks; k < ke; ++k) chyez(i, js, k) = khy * 2 * chyez(i, js, k) / std::log(dx / r);
+  }
+}
+
+void oracle_sim::initTFSF() {
+  auto &t = tf;
+  // TFSF ctor, src/tfsf/tfsf.cpp:15-33
+  double st = std::sin(t.theta), ct = std::cos(t.theta), sp = std::sin(t.phi), cp = std::cos(t.phi);
+  double sps = std::sin(t.psi), cps = std::cos(t.psi);
+  t.k[0] = st * cp; t.k[1] = st * sp; t.k[2] = ct;
+  // TFSF3D ctor, tfsf_3d.cpp:18-31: transform_e = U . (sin psi, cos psi, 0),
+  // transform_h = k x transform_e
+  double u[3][3] = {{-sp, ct * cp, st * cp}, {cp, ct * sp, st * sp}, {0, -st, ct}};
+  double ke[3] = {sps, cps, 0};
+  for (int r = 0; r < 3; ++r) t.te[r] = u[r][0] * ke[0] + u[r][1] * ke[1] + u[r][2] * ke[2];
+  t.th[0] = t.k[1] * t.te[2] - t.k[2] * t.te[1];
+  t.th[1] = t.k[2] * t.te[0] - t.k[0] * t.te[2];
+  t.th[2] = t.k[0] * t.te[1] - t.k[1] * t.te[0];
+  // defaultInitTFSF, tfsf.cpp:35-53
+  size_t n[3] = {nx, ny, nz};
+  size_t bn[3];
+  for (int a = 0; a < 3; ++a) bn[a] = n[a] - 2 * t.dist[a];
+  t.li = t.dist[0]; t.ri = t.dist[0] + bn[0];
+  t.lj = t.dist[1]; t.rj = t.dist[1] + bn[1];
+  t.lk = t.dist[2]; t.rk = t.dist[2] + bn[2];
+  std::vector<double> times(total);
+  for (size_t i = 0; i < total; ++i) times[i] = static_cast<double>(i) * dt;
+  t.wave.init(times);
+  // TFSF3D::init, tfsf_3d.cpp:33-151
+  double ratio_delta = 1 / std::sqrt(std::pow(std::sin(t.theta), 4) *
+                                         (std::pow(std::cos(t.phi), 4) + std::pow(std::sin(t.phi), 4)) +
+                                     std::pow(std::cos(t.theta), 4));
+  double diagonal_length = std::sqrt(std::pow(bn[0], 2) + std::pow(bn[1], 2) + std::pow(bn[2], 2)) * ratio_delta;
+  t.L = static_cast<size_t>(std::ceil(diagonal_length)) + 4 + 1;
+  t.e_inc.assign(t.L, 0.0); t.exi.assign(t.L, 0.0); t.eyi.assign(t.L, 0.0); t.ezi.assign(t.L, 0.0);
+  t.h_inc.assign(t.L - 1, 0.0); t.hxi.assign(t.L - 1, 0.0); t.hyi.assign(t.L - 1, 0.0); t.hzi.assign(t.L - 1, 0.0);
+  double extra[3];
+  for (int a = 0; a < 3; ++a) extra[a] = 2 * t.k[a] / ratio_delta;
+  double lo[3] = {static_cast<double>(t.li), static_cast<double>(t.lj), static_cast<double>(t.lk)};
+  double hi[3] = {static_cast<double>(t.ri), static_cast<double>(t.rj), static_cast<double>(t.rk)};
+  double orig[3];
+  for (int a = 0; a < 3; ++a) orig[a] = (t.k[a] >= 0 ? lo[a] : hi[a]) - extra[a];
+  size_t start[3] = {t.li, t.lj, t.lk};
+  std::vector<double> *full[3] = {&t.px_f, &t.py_f, &t.pz_f};
+  std::vector<double> *half[3] = {&t.px_h, &t.py_h, &t.pz_h};
+  for (int a = 0; a < 3; ++a) {
+    full[a]->assign(bn[a] + 1, 0.0);
+    half[a]->assign(bn[a] + 2, 0.0);
+    for (size_t i = 0; i < bn[a] + 1; ++i) (*full[a])[i] = ((i + start[a]) - orig[a]) * t.k[a] * ratio_delta;
+    for (size_t i = 0; i < bn[a] + 2; ++i)
+      (*half[a])[i] = ((i + start[a]) - orig[a] - 0.5) * t.k[a] * ratio_delta;
+  }
+  t.scaled_dl = gs->base[0] / ratio_delta;
+  t.ceihi = -(dt / (EPSILON_0 * t.scaled_dl));
+  t.chiei = -(dt / (MU_0 * t.scaled_dl));
+}
+
+void oracle_sim::initNFFFT() {
+  auto &f = nf;
+  // NFFFT::defaultInit, src/nffft/nffft.cpp:22-34
+  size_t bn[3] = {nx - 2 * f.dist[0], ny - 2 * f.dist[1], nz - 2 * f.dist[2]};
+  f.li = f.dist[0]; f.ri = f.li + bn[0];
+  f.lj = f.dist[1]; f.rj = f.lj + bn[1];
+  f.lk = f.dist[2]; f.rk = f.lk + bn[2];
+  f.bx = bn[0]; f.by = bn[1]; f.bz = bn[2];
+  size_t nfq = f.freq.size();
+  // NffftFd::init, nffft_fd.cpp:17-89
+  f.acc.resize(24);
+  for (int q = 0; q < 8; ++q) {
+    f.acc[q].init(nfq, f.by, f.bz);        // X faces
+    f.acc[8 + q].init(nfq, f.bz, f.bx);    // Y faces
+    f.acc[16 + q].init(nfq, f.bx, f.by);   // Z faces
+  }
+  // initDFT, nffft_fd.cpp:91-106
+  using namespace std::complex_literals;
+  f.tj.assign(nfq * total, cplx(0, 0));
+  f.tm.assign(nfq * total, cplx(0, 0));
+  for (size_t n = 0; n < nfq; ++n)
+    for (size_t t = 0; t < total; ++t) {
+      f.tj[n * total + t] = dt * std::exp(-1i * 2.0 * PI * (f.freq[n] * (t + 0.5) * dt));
+      f.tm[n * total + t] = dt * std::exp(-1i * 2.0 * PI * (f.freq[n] * t * dt));
+    }
+  f.k.resize(nfq);
+  for (size_t n = 0; n < nfq; ++n) f.k[n] = 2 * PI * f.freq[n] / C_0;  // nffft_fd.h:45
+}
+
+void oracle_sim::initLumpedElement(Lumped &l) {
+  // {Current,Voltage}Source / Resistor / Capacitor / Inductor ::init
+  GridBox g = gs->getGridBox(l.d.point, l.d.size);
+  for (int a = 0; a < 3; ++a) { l.s[a] = g.start(a); l.e[a] = g.end(a); }
+  bool source = l.d.kind == XFDTD_LUMPED_CURRENT_SOURCE || l.d.kind == XFDTD_LUMPED_VOLTAGE_SOURCE;
+  int comp = source ? l.d.orientation / 2 : l.d.orientation;
+  l.comp = comp;
+  double nI = static_cast<double>(l.e[0] - l.s[0]), nJ = static_cast<double>(l.e[1] - l.s[1]),
+         nK = static_cast<double>(l.e[2] - l.s[2]);
+  // na x nb transverse, nc along the element
+  double nc = comp == 0 ? nI : (comp == 1 ? nJ : nK);
+  double na_nb = comp == 0 ? nK * nJ : (comp == 1 ? nK * nI : nI * nJ);
+  size_t cnt = (l.e[0] - l.s[0]) * (l.e[1] - l.s[1]) * (l.e[2] - l.s[2]);
+  l.da.resize(cnt); l.db.resize(cnt); l.dc.resize(cnt);
+  size_t c = 0;
+  for (size_t i = l.s[0]; i < l.e[0]; ++i)
+    for (size_t j = l.s[1]; j < l.e[1]; ++j)
+      for (size_t k = l.s[2]; k < l.e[2]; ++k, ++c) {
+        if (comp == 0) { l.da[c] = gs->hs[1][j]; l.db[c] = gs->hs[2][k]; l.dc[c] = gs->es[0][i]; }
+        else if (comp == 1) { l.da[c] = gs->hs[2][k]; l.db[c] = gs->hs[0][i]; l.dc[c] = gs->es[1][j]; }
+        else { l.da[c] = gs->hs[0][i]; l.db[c] = gs->hs[1][j]; l.dc[c] = gs->es[2][k]; }
+      }
+  double R = l.d.value;
+  l.beta.resize(cnt);
+  if (l.d.kind == XFDTD_LUMPED_CURRENT_SOURCE) {  // current_source.cpp:34-116
+    if (R == 0) R = 1e-20;  // :12-15
+    // resistance_factor = R * (transverse cells) / (cells along)
+    if (comp == 0) l.factor = R * nK * nJ / nI;
+    else if (comp == 1) l.factor = R * nK * nI / nJ;
+    else l.factor = R * nI * nJ / nK;
+    l.amp_factor = l.d.waveform.amplitude / na_nb;
+    if (l.d.orientation % 2 == 0) l.amp_factor *= -1;
+    for (size_t q = 0; q < cnt; ++q) l.beta[q] = (dt * l.dc[q]) / (l.factor * l.da[q] * l.db[q]);
+    l.wave.d = l.d.waveform;
+    l.wave.amplitude = l.amp_factor;
+    l.wave.init(linspace(0.5 * dt, (total - 0.5) * dt, total));
+  } else if (l.d.kind == XFDTD_LUMPED_VOLTAGE_SOURCE) {  // voltage_source.cpp:44-130
+    if (R == 0) R = 1e-20;
+    if (comp == 0) l.factor = R * nJ * nK / nI;
+    else if (comp == 1) l.factor = R * nI * nK / nJ;
+    else l.factor = R * nI * nJ / nK;
+    l.amp_factor = l.d.waveform.amplitude / nc;
+    if (l.d.orientation % 2 == 0) l.amp_factor *= -1;
+    l.coff.resize(cnt);  // alpha, kept in coff until correctFDTDCoff
+    for (size_t q = 0; q < cnt; ++q) {
+      double alpha = l.da[q] * l.db[q] * l.factor;
+      l.coff[q] = alpha;
+      l.beta[q] = dt * l.dc[q] / alpha;
+    }
+    l.wave.d = l.d.waveform;
+    l.wave.amplitude = l.amp_factor;
+    l.wave.init(linspace(dt * 0.5, (total - 0.5) * dt, total));
+  } else if (l.d.kind == XFDTD_LUMPED_RESISTOR) {  // resistor.cpp:10-67
+    if (comp == 0) l.factor = R * nJ * nK / nI;
+    else if (comp == 1) l.factor = R * nI * nK / nJ;
+    else l.factor = R * nI * nJ / nK;
+    for (size_t q = 0; q < cnt; ++q) l.beta[q] = dt * l.dc[q] / (l.factor * l.da[q] * l.db[q]);
+  } else if (l.d.kind == XFDTD_LUMPED_CAPACITOR) {  // capacitor.cpp:11-72
+    double C = l.d.value;
+    if (comp == 0) l.factor = C * nI / (nJ * nK);
+    else if (comp == 1) l.factor = C * nJ / (nI * nK);
+    else l.factor = C * nK / (nI * nJ);
+    for (size_t q = 0; q < cnt; ++q) l.beta[q] = 2 * l.factor * l.dc[q] / (l.da[q] * l.db[q]);
+  } else {  // inductor.cpp:10-66
+    double L = l.d.value;
+    if (comp == 0) l.factor = L * nJ * nK / nI;
+    else if (comp == 1) l.factor = L * nI * nK / nJ;
+    else l.factor = L * nI * nJ / nK;
+    l.cjcec.resize(cnt);
+    for (size_t q = 0; q < cnt; ++q) l.cjcec[q] = dt * l.dc[q] / (l.factor * l.da[q] * l.db[q]);
+  }
+}
+
+void oracle_sim::correctCoffLumped(Lumped &l) {
+  A3 *cece, *cecha, *cechb;
+  if (l.comp == 0) { cece = &cexe; cecha = &cexhy; cechb = &cexhz; }
+  else if (l.comp == 1) { cece = &ceye; cecha = &ceyhz; cechb = &ceyhx; }
+  else { cece = &ceze; cecha = &cezhx; cechb = &cezhy; }
+  A3 &e = eps[l.comp], &s = sig[l.comp];
+  size_t c = 0;
+  if (l.d.kind == XFDTD_LUMPED_INDUCTOR) {  // inductor.cpp:68-100
+    l.cecjc.resize(l.cjcec.size());
+    for (size_t i = l.s[0]; i < l.e[0]; ++i)
+      for (size_t j = l.s[1]; j < l.e[1]; ++j)
+        for (size_t k = l.s[2]; k < l.e[2]; ++k, ++c)
+          l.cecjc[c] = -(2 * dt) / (2 * e(i, j, k) + dt * s(i, j, k));
+    l.jcur.assign(l.cjcec.size(), 0.0);
+    return;
+  }
+  if (l.d.kind != XFDTD_LUMPED_VOLTAGE_SOURCE) l.coff.resize(l.beta.size());
+  for (size_t i = l.s[0]; i < l.e[0]; ++i)
+    for (size_t j = l.s[1]; j < l.e[1]; ++j)
+      for (size_t k = l.s[2]; k < l.e[2]; ++k, ++c) {
+        double ev = e(i, j, k), sv = s(i, j, k), b = l.beta[c];
+        if (l.d.kind == XFDTD_LUMPED_CAPACITOR) {  // capacitor.cpp:100-120
+          (*cece)(i, j, k) = (2 * ev - dt * sv + b) / (2 * ev + dt * sv + b);
+          (*cecha)(i, j, k) = -(2 * dt) / ((2 * ev + dt * sv + b) * l.db[c]);
+          (*cechb)(i, j, k) = (2 * dt) / ((2 * ev + dt * sv + b) * l.da[c]);
+          continue;
+        }
+        // current_source.cpp:167-187, voltage_source.cpp:151-169, resistor.cpp:94-112
+        (*cece)(i, j, k) = (2 * ev - dt * sv - b) / (2 * ev + dt * sv + b);
+        (*cecha)(i, j, k) = -2 * dt / ((2 * ev + dt * sv + b) * l.db[c]);
+        (*cechb)(i, j, k) = 2 * dt / ((2 * ev + dt * sv + b) * l.da[c]);
+        if (l.d.kind == XFDTD_LUMPED_CURRENT_SOURCE)
+          l.coff[c] = -2 * dt / ((2 * ev + dt * sv + b) * (l.db[c] * l.da[c]));
+        else if (l.d.kind == XFDTD_LUMPED_VOLTAGE_SOURCE)
+          l.coff[c] = -2 * dt / ((2 * ev + dt * sv + b) * l.coff[c]);
+      }
+}
+
+void oracle_sim::initPML(PML &p) {
+  // PML::init(emf, ...), perfect_match_layer.cpp:49-96
+  int ori = p.d.orientation;
+  p.axis = ori / 2;
+  if (p.axis == 0) { p.aa = 1; p.ab = 2; }
+  else if (p.axis == 1) { p.aa = 2; p.ab = 0; }
+  else { p.aa = 0; p.ab = 1; }
+  size_t n[3] = {nx, ny, nz};
+  p.dl = gs->base[p.axis];
+  p.dt = dt;
+  int T = p.d.thickness;
+  p.start = p.positive() ? n[p.axis] - static_cast<size_t>(T) : 0;
+  p.na = static_cast<int>(n[p.aa]);
+  p.nb = static_cast<int>(n[p.ab]);
+  A3 *ceahb, *cebha, *chaeb, *chbea;
+  if (p.axis == 0) { ceahb = &ceyhz; cebha = &cezhy; chaeb = &chyez; chbea = &chzey; }
+  else if (p.axis == 1) { ceahb = &cezhx; cebha = &cexhz; chaeb = &chzex; chbea = &chxez; }
+  else { ceahb = &cexhy; cebha = &ceyhx; chaeb = &chxey; chbea = &chyex; }
+  // initP / initN profiles, :133-155 and :302-325
+  double e2m = MU_0 / EPSILON_0;
+  double sigma_max = p.d.sigma_ratio * (p.d.order + 1) / (150.0 * PI * p.dl);
+  p.kappa_e.resize(T); p.kappa_m.resize(T); p.a_e.resize(T); p.b_e.resize(T); p.a_m.resize(T); p.b_m.resize(T);
+  for (int i = 0; i < T; ++i) {
+    double rho_e, rho_m;
+    if (p.positive()) {
+      rho_e = (i + 1 - 0.75) / static_cast<double>(T);
+      rho_m = (i + 1 - 0.25) / static_cast<double>(T);
+    } else {
+      rho_e = (T - i - 0.75) / static_cast<double>(T);
+      rho_m = (T - i - 0.25) / static_cast<double>(T);
+    }
+    double sigma_e = sigma_max * std::pow(rho_e, p.d.order);
+    double sigma_m = sigma_max * std::pow(rho_m, p.d.order);
+    sigma_m = sigma_m * e2m;
+    double kappa_e = 1 + (p.d.kappa_max - 1) * std::pow(rho_e, p.d.order);
+    double kappa_m = 1 + (p.d.kappa_max - 1) * std::pow(rho_m, p.d.order);
+    double alpha_e = p.d.alpha_min + (p.d.alpha_max - p.d.alpha_min) * (1 - rho_e);
+    double alpha_m = p.d.alpha_min + (p.d.alpha_max - p.d.alpha_min) * (1 - rho_m);
+    alpha_m = alpha_m * e2m;
+    p.kappa_e[i] = kappa_e;
+    p.kappa_m[i] = kappa_m;
+    p.b_e[i] = std::exp((-p.dt / EPSILON_0) * (sigma_e / kappa_e + alpha_e));
+    p.a_e[i] = (1 / p.dl) * (p.b_e[i] - 1) * sigma_e / (kappa_e * (sigma_e + kappa_e * alpha_e));
+    p.b_m[i] = std::exp((-p.dt / MU_0) * (sigma_m / kappa_m + alpha_m));
+    p.a_m[i] = (1 / p.dl) * (p.b_m[i] - 1) * sigma_m / (kappa_m * (sigma_m + kappa_m * alpha_m));
+  }
+  // psi and c_psi arrays (all zero-initialised here), :157-299 and :327-431.
+  // Internal layout (layer, a, b); the reference permutes it per face,
+  // which does not change any value.
+  p.psi_ea.init(T, p.na, p.nb + 1); p.psi_hb.init(T, p.na, p.nb + 1);
+  p.c_ea.init(T, p.na, p.nb + 1); p.c_hb.init(T, p.na, p.nb + 1);
+  p.psi_eb.init(T, p.na + 1, p.nb); p.psi_ha.init(T, p.na + 1, p.nb);
+  p.c_eb.init(T, p.na + 1, p.nb); p.c_ha.init(T, p.na + 1, p.nb);
+  size_t off_e = p.positive() ? 0 : 1;  // N side updates E at start+i+1
+  size_t ijk[3];
+  for (int l = 0; l < T; ++l) {
+    for (int a = 0; a < p.na; ++a)
+      for (int b = 0; b < p.nb + 1; ++b) {
+        nab2ijk(p.axis, p.aa, p.ab, p.start + l + off_e, a, b, ijk);
+        p.c_ea(l, a, b) = (*ceahb)(ijk[0], ijk[1], ijk[2]) * p.dl;
+        (*ceahb)(ijk[0], ijk[1], ijk[2]) = (*ceahb)(ijk[0], ijk[1], ijk[2]) / p.kappa_e[l];
+        nab2ijk(p.axis, p.aa, p.ab, p.start + l, a, b, ijk);
+        p.c_hb(l, a, b) = (*chbea)(ijk[0], ijk[1], ijk[2]) * p.dl;
+        (*chbea)(ijk[0], ijk[1], ijk[2]) = (*chbea)(ijk[0], ijk[1], ijk[2]) / p.kappa_m[l];
+      }
+    for (int a = 0; a < p.na + 1; ++a)
+      for (int b = 0; b < p.nb; ++b) {
+        nab2ijk(p.axis, p.aa, p.ab, p.start + l + off_e, a, b, ijk);
+        p.c_eb(l, a, b) = (*cebha)(ijk[0], ijk[1], ijk[2]) * p.dl;
+        (*cebha)(ijk[0], ijk[1], ijk[2]) = (*cebha)(ijk[0], ijk[1], ijk[2]) / p.kappa_e[l];
+        nab2ijk(p.axis, p.aa, p.ab, p.start + l, a, b, ijk);
+        p.c_ha(l, a, b) = (*chaeb)(ijk[0], ijk[1], ijk[2]) * p.dl;
+        (*chaeb)(ijk[0], ijk[1], ijk[2]) = (*chaeb)(ijk[0], ijk[1], ijk[2]) / p.kappa_m[l];
+      }
+  }
+}
+
+void oracle_sim::initMonitor(Monitor &m) {
+  GridBox g = gs->getGridBox(m.d.point, m.d.size);
+  for (int a = 0; a < 3; ++a) { m.s[a] = g.start(a); m.e[a] = g.end(a); }
+  int axis = m.d.orientation / 2;
+  bool neg = m.d.orientation % 2 == 0;
+  if (m.d.kind == XFDTD_MONITOR_VOLTAGE) {  // voltage_monitor.cpp:25-62
+    double other = axis == 0 ? static_cast<double>((m.e[1] - m.s[1]) * (m.e[2] - m.s[2]))
+                   : axis == 1 ? static_cast<double>((m.e[0] - m.s[0]) * (m.e[2] - m.s[2]))
+                               : static_cast<double>((m.e[0] - m.s[0]) * (m.e[1] - m.s[1]));
+    for (size_t q = m.s[axis]; q < m.e[axis]; ++q) {
+      double c = -gs->hs[axis][q] / other;
+      if (neg) c *= -1;
+      m.coff.push_back(c);
+    }
+  } else {  // current_monitor.cpp:23-68
+    int aa = axis == 0 ? 1 : (axis == 1 ? 2 : 0);
+    int ab = axis == 0 ? 2 : (axis == 1 ? 0 : 1);
+    for (size_t q = m.s[aa]; q < m.e[aa] + 1; ++q) m.da.push_back(gs->es[aa][q]);
+    for (size_t q = m.s[ab]; q < m.e[ab] + 1; ++q) m.db.push_back(gs->es[ab][q]);
+    m.positive = neg ? -1 : 1;
+  }
+  m.value.assign(total, 0.0);
+}
+
+// ------------------------------------------------------------ time loop ---
+void oracle_sim::updateE() {  // Simulation::updateE, simulation_update.cpp:170-196
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < static_cast<long long>(nx); ++ii) {
+    size_t i = static_cast<size_t>(ii);
+    for (size_t j = 1; j < ny; ++j)
+      for (size_t k = 1; k < nz; ++k)
+        ex(i, j, k) = cexe(i, j, k) * ex(i, j, k) + cexhy(i, j, k) * (hy(i, j, k) - hy(i, j, k - 1)) +
+                      cexhz(i, j, k) * (hz(i, j, k) - hz(i, j - 1, k));
+  }
+#pragma omp parallel for schedule(static)
+  for (long long jj = 0; jj < static_cast<long long>(ny); ++jj) {
+    size_t j = static_cast<size_t>(jj);
+    for (size_t k = 1; k < nz; ++k)
+      for (size_t i = 1; i < nx; ++i)
+        ey(i, j, k) = ceye(i, j, k) * ey(i, j, k) + ceyhx(i, j, k) * (hx(i, j, k) - hx(i, j, k - 1)) +
+                      ceyhz(i, j, k) * (hz(i, j, k) - hz(i - 1, j, k));
+  }
+#pragma omp parallel for schedule(static)
+  for (long long kk = 0; kk < static_cast<long long>(nz); ++kk) {
+    size_t k = static_cast<size_t>(kk);
+    for (size_t i = 1; i < nx; ++i)
+      for (size_t j = 1; j < ny; ++j)
+        ez(i, j, k) = ceze(i, j, k) * ez(i, j, k) + cezhx(i, j, k) * (hx(i, j, k) - hx(i, j - 1, k)) +
+                      cezhy(i, j, k) * (hy(i, j, k) - hy(i - 1, j, k));
+  }
+}
+
+void oracle_sim::updateH() {  // Simulation::updateH, simulation_update.cpp:84-100
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < static_cast<long long>(nx); ++ii) {
+    size_t i = static_cast<size_t>(ii);
+    for (size_t j = 0; j < ny; ++j)
+      for (size_t k = 0; k < nz; ++k) {
+        hx(i, j, k) = chxh(i, j, k) * hx(i, j, k) + chxey(i, j, k) * (ey(i, j, k + 1) - ey(i, j, k)) +
+                      chxez(i, j, k) * (ez(i, j + 1, k) - ez(i, j, k));
+        hy(i, j, k) = chyh(i, j, k) * hy(i, j, k) + chyez(i, j, k) * (ez(i + 1, j, k) - ez(i, j, k)) +
+                      chyex(i, j, k) * (ex(i, j, k + 1) - ex(i, j, k));
+        hz(i, j, k) = chzh(i, j, k) * hz(i, j, k) + chzex(i, j, k) * (ex(i, j + 1, k) - ex(i, j, k)) +
+                      chzey(i, j, k) * (ey(i + 1, j, k) - ey(i, j, k));
+      }
+  }
+}
+
+void oracle_sim::pmlE(PML &p) {  // PML::updateE, perfect_match_layer.cpp:574-718
+  A3 *ea, *eb, *ha, *hb;
+  if (p.axis == 0) { ea = &ey; eb = &ez; ha = &hy; hb = &hz; }
+  else if (p.axis == 1) { ea = &ez; eb = &ex; ha = &hz; hb = &hx; }
+  else { ea = &ex; eb = &ey; ha = &hx; hb = &hy; }
+  const int T = p.d.thickness;
+  const bool pos = p.positive();
+#pragma omp parallel for schedule(static)
+  for (int l = 0; l < T; ++l) {
+    size_t en = pos ? p.start + l : p.start + l + 1;  // E index on the normal axis
+    size_t h1 = en, h0 = en - 1;                        // H(en) - H(en-1) in both cases
+    size_t a1[3], a0[3], ae[3];
+    for (int a = 0; a < p.na; ++a)
+      for (int b = 0; b < p.nb + 1; ++b) {
+        nab2ijk(p.axis, p.aa, p.ab, h1, a, b, a1);
+        nab2ijk(p.axis, p.aa, p.ab, h0, a, b, a0);
+        nab2ijk(p.axis, p.aa, p.ab, en, a, b, ae);
+        p.psi_ea(l, a, b) = p.b_e[l] * p.psi_ea(l, a, b) +
+                            p.a_e[l] * ((*hb)(a1[0], a1[1], a1[2]) - (*hb)(a0[0], a0[1], a0[2]));
+        (*ea)(ae[0], ae[1], ae[2]) = (*ea)(ae[0], ae[1], ae[2]) + p.c_ea(l, a, b) * p.psi_ea(l, a, b);
+      }
+    for (int a = 0; a < p.na + 1; ++a)
+      for (int b = 0; b < p.nb; ++b) {
+        nab2ijk(p.axis, p.aa, p.ab, h1, a, b, a1);
+        nab2ijk(p.axis, p.aa, p.ab, h0, a, b, a0);
+        nab2ijk(p.axis, p.aa, p.ab, en, a, b, ae);
+        p.psi_eb(l, a, b) = p.b_e[l] * p.psi_eb(l, a, b) +
+                            p.a_e[l] * ((*ha)(a1[0], a1[1], a1[2]) - (*ha)(a0[0], a0[1], a0[2]));
+        (*eb)(ae[0], ae[1], ae[2]) = (*eb)(ae[0], ae[1], ae[2]) + p.c_eb(l, a, b) * p.psi_eb(l, a, b);
+      }
+  }
+}
+
+void oracle_sim::pmlH(PML &p) {  // PML::updateH, perfect_match_layer.cpp:434-572
+  A3 *ea, *eb, *ha, *hb;
+  if (p.axis == 0) { ea = &ey; eb = &ez; ha = &hy; hb = &hz; }
+  else if (p.axis == 1) { ea = &ez; eb = &ex; ha = &hz; hb = &hx; }
+  else { ea = &ex; eb = &ey; ha = &hx; hb = &hy; }
+  const int T = p.d.thickness;
+#pragma omp parallel for schedule(static)
+  for (int l = 0; l < T; ++l) {
+    size_t hn = p.start + l;
+    size_t e1[3], e0[3], ah[3];
+    for (int a = 0; a < p.na; ++a)
+      for (int b = 0; b < p.nb + 1; ++b) {
+        nab2ijk(p.axis, p.aa, p.ab, hn + 1, a, b, e1);
+        nab2ijk(p.axis, p.aa, p.ab, hn, a, b, e0);
+        nab2ijk(p.axis, p.aa, p.ab, hn, a, b, ah);
+        p.psi_hb(l, a, b) = p.b_m[l] * p.psi_hb(l, a, b) +
+                            p.a_m[l] * ((*ea)(e1[0], e1[1], e1[2]) - (*ea)(e0[0], e0[1], e0[2]));
+        (*hb)(ah[0], ah[1], ah[2]) = (*hb)(ah[0], ah[1], ah[2]) + p.c_hb(l, a, b) * p.psi_hb(l, a, b);
+      }
+    for (int a = 0; a < p.na + 1; ++a)
+      for (int b = 0; b < p.nb; ++b) {
+        nab2ijk(p.axis, p.aa, p.ab, hn + 1, a, b, e1);
+        nab2ijk(p.axis, p.aa, p.ab, hn, a, b, e0);
+        nab2ijk(p.axis, p.aa, p.ab, hn, a, b, ah);
+        p.psi_ha(l, a, b) = p.b_m[l] * p.psi_ha(l, a, b) +
+                            p.a_m[l] * ((*eb)(e1[0], e1[1], e1[2]) - (*eb)(e0[0], e0[1], e0[2]));
+        (*ha)(ah[0], ah[1], ah[2]) = (*ha)(ah[0], ah[1], ah[2]) + p.c_ha(l, a, b) * p.psi_ha(l, a, b);
+      }
+  }
+}
+
+void oracle_sim::tfsfIncident(size_t t) {  // TFSF3D::updateIncidentField, tfsf_3d.cpp:153-183
+  auto &f = tf;
+  double e0w = f.e0 * f.wave.value[t];  // getIncidentWaveValueByTimeStep, tfsf.cpp:80-82
+  f.e_inc[0] = e0w;
+  double x = f.e_inc[f.L - 2];
+  double y = f.e_inc[f.L - 1];
+  for (size_t i = 1; i < f.L - 1; ++i) f.e_inc[i] = f.ceie * f.e_inc[i] + f.ceihi * (f.h_inc[i] - f.h_inc[i - 1]);
+  double coff_1 = (C_0 * dt - f.scaled_dl) / (C_0 * dt + f.scaled_dl);
+  double coff_2 = 2 * f.scaled_dl / (C_0 * dt + f.scaled_dl);
+  f.e_inc[f.L - 1] = -f.a + coff_1 * (f.e_inc[f.L - 2] + f.b) + coff_2 * (x + y);
+  f.a = x;
+  f.b = y;
+  for (size_t i = 0; i < f.L - 1; ++i) f.h_inc[i] = f.chih * f.h_inc[i] + f.chiei * (f.e_inc[i + 1] - f.e_inc[i]);
+  for (size_t i = 0; i < f.L; ++i) {
+    f.exi[i] = f.te[0] * f.e_inc[i];
+    f.eyi[i] = f.te[1] * f.e_inc[i];
+    f.ezi[i] = f.te[2] * f.e_inc[i];
+  }
+  for (size_t i = 0; i < f.L - 1; ++i) {
+    f.hxi[i] = f.th[0] * f.h_inc[i];
+    f.hyi[i] = f.th[1] * f.h_inc[i];
+    f.hzi[i] = f.th[2] * f.h_inc[i];
+  }
+}
+
+namespace {
+inline double interp(const std::vector<double> &v, double projection) {  // tfsf_3d.cpp:413-483
+  size_t index = static_cast<size_t>(projection);
+  double weight = projection - index;
+  return (1 - weight) * v[index] + weight * v[index + 1];
+}
+}  // namespace
+
+void oracle_sim::tfsfH() {  // TFSF3D::updateH, tfsf_3d.cpp:185-297
+  auto &f = tf;
+  const size_t li = f.li, ri = f.ri, lj = f.lj, rj = f.rj, lk = f.lk, rk = f.rk;
+  double cbx = dt / (MU_0 * gs->base[0]), cby = dt / (MU_0 * gs->base[1]), cbz = dt / (MU_0 * gs->base[2]);
+  auto Ex = [&](size_t i, size_t j, size_t k) {
+    return interp(f.exi, f.px_h[i - li + 1] + f.py_f[j - lj] + f.pz_f[k - lk]);
+  };
+  auto Ey = [&](size_t i, size_t j, size_t k) {
+    return interp(f.eyi, f.px_f[i - li] + f.py_h[j - lj + 1] + f.pz_f[k - lk]);
+  };
+  auto Ez = [&](size_t i, size_t j, size_t k) {
+    return interp(f.ezi, f.px_f[i - li] + f.py_f[j - lj] + f.pz_h[k - lk + 1]);
+  };
+  for (size_t j = lj; j < rj; ++j)
+    for (size_t k = lk; k < rk + 1; ++k) hz(li - 1, j, k) += cbx * Ey(li, j, k);
+  for (size_t j = lj; j < rj + 1; ++j)
+    for (size_t k = lk; k < rk; ++k) hy(li - 1, j, k) -= cbx * Ez(li, j, k);
+  for (size_t j = lj; j < rj; ++j)
+    for (size_t k = lk; k < rk + 1; ++k) hz(ri, j, k) -= cbx * Ey(ri, j, k);
+  for (size_t j = lj; j < rj + 1; ++j)
+    for (size_t k = lk; k < rk; ++k) hy(ri, j, k) += cbx * Ez(ri, j, k);
+  for (size_t k = lk; k < rk; ++k)
+    for (size_t i = li; i < ri + 1; ++i) hx(i, lj - 1, k) += cby * Ez(i, lj, k);
+  for (size_t k = lk; k < rk + 1; ++k)
+    for (size_t i = li; i < ri; ++i) hz(i, lj - 1, k) -= cby * Ex(i, lj, k);
+  for (size_t k = lk; k < rk; ++k)
+    for (size_t i = li; i < ri + 1; ++i) hx(i, rj, k) -= cby * Ez(i, rj, k);
+  for (size_t k = lk; k < rk + 1; ++k)
+    for (size_t i = li; i < ri; ++i) hz(i, rj, k) += cby * Ex(i, rj, k);
+  for (size_t i = li; i < ri; ++i)
+    for (size_t j = lj; j < rj + 1; ++j) hy(i, j, lk - 1) += cbz * Ex(i, j, lk);
+  for (size_t i = li; i < ri + 1; ++i)
+    for (size_t j = lj; j < rj; ++j) hx(i, j, lk - 1) -= cbz * Ey(i, j, lk);
+  for (size_t i = li; i < ri; ++i)
+    for (size_t j = lj; j < rj + 1; ++j) hy(i, j, rk) -= cbz * Ex(i, j, rk);
+  for (size_t i = li; i < ri + 1; ++i)
+    for (size_t j = lj; j < rj; ++j) hx(i, j, rk) += cbz * Ey(i, j, rk);
+}
+
+void oracle_sim::tfsfE() {  // TFSF3D::updateE, tfsf_3d.cpp:299-411
+  auto &f = tf;
+  const size_t li = f.li, ri = f.ri, lj = f.lj, rj = f.rj, lk = f.lk, rk = f.rk;
+  double cax = dt / (EPSILON_0 * gs->base[0]), cay = dt / (EPSILON_0 * gs->base[1]),
+         caz = dt / (EPSILON_0 * gs->base[2]);
+  auto Hx = [&](size_t i, size_t j, size_t k) {
+    return interp(f.hxi, f.px_f[i - li] + f.py_h[j - lj + 1] + f.pz_h[k - lk + 1] - 0.5);
+  };
+  auto Hy = [&](size_t i, size_t j, size_t k) {
+    return interp(f.hyi, f.px_h[i - li + 1] + f.py_f[j - lj] + f.pz_h[k - lk + 1] - 0.5);
+  };
+  auto Hz = [&](size_t i, size_t j, size_t k) {
+    return interp(f.hzi, f.px_h[i - li + 1] + f.py_h[j - lj + 1] + f.pz_f[k - lk] - 0.5);
+  };
+  for (size_t j = lj; j < rj; ++j)
+    for (size_t k = lk; k < rk + 1; ++k) ey(li, j, k) += cax * Hz(li - 1, j, k);
+  for (size_t j = lj; j < rj + 1; ++j)
+    for (size_t k = lk; k < rk; ++k) ez(li, j, k) -= cax * Hy(li - 1, j, k);
+  for (size_t j = lj; j < rj; ++j)
+    for (size_t k = lk; k < rk + 1; ++k) ey(ri, j, k) -= cax * Hz(ri, j, k);
+  for (size_t j = lj; j < rj + 1; ++j)
+    for (size_t k = lk; k < rk; ++k) ez(ri, j, k) += cax * Hy(ri, j, k);
+  for (size_t k = lk; k < rk; ++k)
+    for (size_t i = li; i < ri + 1; ++i) ez(i, lj, k) += cay * Hx(i, lj - 1, k);
+  for (size_t k = lk; k < rk + 1; ++k)
+    for (size_t i = li; i < ri; ++i) ex(i, lj, k) -= cay * Hz(i, lj - 1, k);
+  for (size_t k = lk; k < rk; ++k)
+    for (size_t i = li; i < ri + 1; ++i) ez(i, rj, k) -= cay * Hx(i, rj, k);
+  for (size_t k = lk; k < rk + 1; ++k)
+    for (size_t i = li; i < ri; ++i) ex(i, rj, k) += cay * Hz(i, rj, k);
+  for (size_t i = li; i < ri; ++i)
+    for (size_t j = lj; j < rj + 1; ++j) ex(i, j, lk) += caz * Hy(i, j, lk - 1);
+  for (size_t i = li; i < ri + 1; ++i)
+    for (size_t j = lj; j < rj; ++j) ey(i, j, lk) -= caz * Hx(i, j, lk - 1);
+  for (size_t i = li; i < ri; ++i)
+    for (size_t j = lj; j < rj + 1; ++j) ex(i, j, rk) -= caz * Hy(i, j, rk);
+  for (size_t i = li; i < ri + 1; ++i)
+    for (size_t j = lj; j < rj; ++j) ey(i, j, rk) += caz * Hx(i, j, rk);
+}
+
+void oracle_sim::lumpedE(Lumped &l) {
+  A3 &e = field(l.comp);
+  size_t c = 0;
+  if (l.d.kind == XFDTD_LUMPED_CURRENT_SOURCE || l.d.kind == XFDTD_LUMPED_VOLTAGE_SOURCE) {
+    // current_source.cpp:140-163, voltage_source.cpp:171-194
+    double w = l.wave.value[cur];
+    for (size_t i = l.s[0]; i < l.e[0]; ++i)
+      for (size_t j = l.s[1]; j < l.e[1]; ++j)
+        for (size_t k = l.s[2]; k < l.e[2]; ++k, ++c) e(i, j, k) += l.coff[c] * w;
+  } else if (l.d.kind == XFDTD_LUMPED_INDUCTOR) {  // inductor.cpp:102-143
+    for (size_t i = l.s[0]; i < l.e[0]; ++i)
+      for (size_t j = l.s[1]; j < l.e[1]; ++j)
+        for (size_t k = l.s[2]; k < l.e[2]; ++k, ++c) {
+          e(i, j, k) += l.cecjc[c] * l.jcur[c];
+          l.jcur[c] = (l.cjcec[c] * e(i, j, k) + l.jcur[c]);
+        }
+  }
+}
+
+void oracle_sim::nffftUpdate() {  // NffftFd::update, nffft_fd.cpp:108-203
+  auto &f = nf;
+  const size_t li = f.li, ri = f.ri, lj = f.lj, rj = f.rj, lk = f.lk, rk = f.rk, nt = cur;
+  const size_t nfq = f.freq.size();
+  // face-centre interpolations, linear_interpolation_emf.cpp:286-421
+  auto EyFX = [&](size_t i, size_t j, size_t k) { return 0.5 * (ey(i, j, k) + ey(i, j, k + 1)); };
+  auto EzFX = [&](size_t i, size_t j, size_t k) { return 0.5 * (ez(i, j, k) + ez(i, j + 1, k)); };
+  auto HyFX = [&](size_t i, size_t j, size_t k) {
+    return 0.25 * (hy(i, j, k) + hy(i, j + 1, k) + hy(i - 1, j, k) + hy(i - 1, j + 1, k));
+  };
+  auto HzFX = [&](size_t i, size_t j, size_t k) {
+    return 0.25 * (hz(i, j, k) + hz(i, j, k + 1) + hz(i - 1, j, k) + hz(i - 1, j, k + 1));
+  };
+  auto ExFY = [&](size_t i, size_t j, size_t k) { return 0.5 * (ex(i, j, k) + ex(i, j + 1, k)); };
+  auto EzFY = [&](size_t i, size_t j, size_t k) { return 0.5 * (ez(i, j, k) + ez(i + 1, j, k)); };
+  auto HxFY = [&](size_t i, size_t j, size_t k) {
+    return 0.25 * (hx(i + 1, j, k) + hx(i, j, k) + hx(i + 1, j - 1, k) + hx(i, j - 1, k));
+  };
+  auto HzFY = [&](size_t i, size_t j, size_t k) {
+    return 0.25 * (hz(i, j, k) + hz(i, j, k + 1) + hz(i, j - 1, k) + hz(i, j - 1, k + 1));
+  };
+  auto ExFZ = [&](size_t i, size_t j, size_t k) { return 0.5 * (ex(i, j, k) + ex(i, j, k + 1)); };
+  auto EyFZ = [&](size_t i, size_t j, size_t k) { return 0.5 * (ey(i, j, k) + ey(i + 1, j, k)); };
+  auto HxFZ = [&](size_t i, size_t j, size_t k) {
+    return 0.25 * (hx(i + 1, j, k) + hx(i, j, k) + hx(i + 1, j, k - 1) + hx(i, j, k - 1));
+  };
+  auto HyFZ = [&](size_t i, size_t j, size_t k) {
+    return 0.25 * (hy(i, j, k) + hy(i, j + 1, k) + hy(i, j, k - 1) + hy(i, j + 1, k - 1));
+  };
+  auto add = [&](int which, size_t a, size_t b, double v, bool is_j) {
+    const std::vector<cplx> &tr = is_j ? f.tj : f.tm;
+    for (size_t n = 0; n < nfq; ++n) f.acc[which](n, a, b) += v * tr[n * total + nt];
+  };
+  // X faces: jy, jz, my, mz
+  for (size_t j = lj; j < rj; ++j)
+    for (size_t k = lk; k < rk; ++k) {
+      double my_xn = -1 * EzFX(li, j, k), mz_xn = EyFX(li, j, k);
+      double jy_xn = HzFX(li, j, k), jz_xn = -1 * HyFX(li, j, k);
+      double my_xp = EzFX(ri, j, k), mz_xp = -1 * EyFX(ri, j, k);
+      double jy_xp = -1 * HzFX(ri, j, k), jz_xp = HyFX(ri, j, k);
+      size_t a = j - lj, b = k - lk;
+      add(2, a, b, my_xn, false); add(3, a, b, mz_xn, false);
+      add(0, a, b, jy_xn, true); add(1, a, b, jz_xn, true);
+      add(6, a, b, my_xp, false); add(7, a, b, mz_xp, false);
+      add(4, a, b, jy_xp, true); add(5, a, b, jz_xp, true);
+    }
+  // Y faces: jz, jx, mz, mx
+  for (size_t k = lk; k < rk; ++k)
+    for (size_t i = li; i < ri; ++i) {
+      double mz_yn = -1 * ExFY(i, lj, k), mx_yn = EzFY(i, lj, k);
+      double jz_yn = HxFY(i, lj, k), jx_yn = -1 * HzFY(i, lj, k);
+      double mz_yp = ExFY(i, rj, k), mx_yp = -1 * EzFY(i, rj, k);
+      double jz_yp = -1 * HxFY(i, rj, k), jx_yp = HzFY(i, rj, k);
+      size_t a = k - lk, b = i - li;
+      add(10, a, b, mz_yn, false); add(11, a, b, mx_yn, false);
+      add(8, a, b, jz_yn, true); add(9, a, b, jx_yn, true);
+      add(14, a, b, mz_yp, false); add(15, a, b, mx_yp, false);
+      add(12, a, b, jz_yp, true); add(13, a, b, jx_yp, true);
+    }
+  // Z faces: jx, jy, mx, my
+  for (size_t i = li; i < ri; ++i)
+    for (size_t j = lj; j < rj; ++j) {
+      double mx_zn = -1 * EyFZ(i, j, lk), my_zn = ExFZ(i, j, lk);
+      double jx_zn = HyFZ(i, j, lk), jy_zn = -1 * HxFZ(i, j, lk);
+      double mx_zp = EyFZ(i, j, rk), my_zp = -1 * ExFZ(i, j, rk);
+      double jx_zp = -1 * HyFZ(i, j, rk), jy_zp = HxFZ(i, j, rk);
+      size_t a = i - li, b = j - lj;
+      add(18, a, b, mx_zn, false); add(19, a, b, my_zn, false);
+      add(16, a, b, jx_zn, true); add(17, a, b, jy_zn, true);
+      add(22, a, b, mx_zp, false); add(23, a, b, my_zp, false);
+      add(20, a, b, jx_zp, true); add(21, a, b, jy_zp, true);
+    }
+}
+
+void oracle_sim::monitorUpdate(Monitor &m) {
+  size_t t = cur;
+  int axis = m.d.orientation / 2;
+  if (m.d.kind == XFDTD_MONITOR_VOLTAGE) {  // voltage_monitor.cpp:64-97
+    A3 &e = field(axis);
+    for (size_t i = m.s[0]; i < m.e[0]; ++i)
+      for (size_t j = m.s[1]; j < m.e[1]; ++j)
+        for (size_t k = m.s[2]; k < m.e[2]; ++k) {
+          size_t q = axis == 0 ? i - m.s[0] : (axis == 1 ? j - m.s[1] : k - m.s[2]);
+          m.value[t] += m.coff[q] * e(i, j, k);
+        }
+    return;
+  }
+  // current_monitor.cpp:70-115
+  const size_t is = m.s[0], ie = m.e[0], js = m.s[1], je = m.e[1], ks = m.s[2], ke = m.e[2];
+  double ix = 0, iy = 0, iz = 0;
+  if (axis == 0) {
+    for (size_t j = js; j <= je; ++j) iy += (hy(is, j, ks - 1) - hy(is, j, ke)) * m.da[j - js];
+    for (size_t k = ks; k <= ke; ++k) iz += (hz(is, je, k) - hz(is, js - 1, k)) * m.db[k - ks];
+    m.value[t] = m.positive * (iz + iy);
+  } else if (axis == 1) {
+    for (size_t k = ks; k <= ke; ++k) iz += (hz(is - 1, js, k) - hz(ie, js, k)) * m.da[k - ks];
+    for (size_t i = is; i <= ie; ++i) ix += (hx(i, js, ke) - hx(i, js, ks - 1)) * m.db[i - is];
+    m.value[t] = m.positive * (iz + ix);
+  } else {
+    for (size_t i = is; i <= ie; ++i) ix += (hx(i, js - 1, ks) - hx(i, je, ks)) * m.da[i - is];
+    for (size_t j = js; j <= je; ++j) iy += (hy(ie, j, ks) - hy(is - 1, j, ks)) * m.db[j - js];
+    m.value[t] = m.positive * (ix + iy);
+  }
+}
+
+void oracle_sim::step() {  // loop body of Simulation::run, simulation_update.cpp:13-35
+  if (cur >= total) throw std::runtime_error("all time steps have been run");
+  updateE();
+  for (auto &l : lumped) lumpedE(l);  // correctE, :282-290
+  if (has_tfsf) tfsfE();
+  for (auto &p : pmls) pmlE(p);       // updateBoundaryE
+  updateH();
+  if (has_tfsf) tfsfIncident(cur);    // updateTFSFIncidentField
+  if (has_tfsf) tfsfH();              // correctH (lumped correctH are all empty)
+  for (auto &p : pmls) pmlH(p);       // updateBoundaryH
+  if (has_nffft) nffftUpdate();
+  for (auto &m : monitors) monitorUpdate(m);
+  ++cur;
+}
+
+void oracle_sim::farField() {  // NffftFd::calculateFarfield{,X,Y,Z}, nffft_fd.cpp:379-556
+  using namespace std::complex_literals;
+  auto &f = nf;
+  size_t NF = f.freq.size(), NT = f.theta.size(), NP = f.phi.size();
+  size_t tot = NF * NT * NP;
+  std::vector<cplx> ax(tot), ay(tot), az(tot), fx(tot), fy(tot), fz(tot);
+  std::vector<cplx> a_theta(tot), a_phi(tot), f_theta(tot), f_phi(tot);
+  const size_t li = f.li, lj = f.lj, lk = f.lk, ri = f.ri, rj = f.rj, rk = f.rk;
+  const double dx = gs->base[0], dy = gs->base[1], dz = gs->base[2];
+#pragma omp parallel for schedule(dynamic)
+  for (long long qq = 0; qq < static_cast<long long>(tot); ++qq) {
+    size_t q = static_cast<size_t>(qq);
+    size_t n = q / (NT * NP), t = (q / NP) % NT, p = q % NP;
+    double cos_t = std::cos(f.theta[t]), sin_t = std::sin(f.theta[t]);
+    double cos_p = std::cos(f.phi[p]), sin_p = std::sin(f.phi[p]);
+    double stcp = sin_t * cos_p, stsp = sin_t * sin_p;
+    {  // X, :423-465
+      const double dx_k = dx * f.k[n];
+      const double dy_dz = dy * dz;
+      cplx sjy(0, 0), sjz(0, 0), smy(0, 0), smz(0, 0);
+      for (size_t j = lj; j < rj; ++j)
+        for (size_t k = lk; k < rk; ++k) {
+          double dn = dx_k * ((li - 0) * stcp + (j - 0 + 0.5) * stsp + (k - 0 + 0.5) * cos_t);
+          cplx pn = std::exp(1i * dn);
+          double dp = dx_k * ((ri - 0) * stcp + (j - 0 + 0.5) * stsp + (k - 0 + 0.5) * cos_t);
+          cplx pp = std::exp(1i * dp);
+          size_t a = j - lj, b = k - lk;
+          sjy += f.acc[0](n, a, b) * pn + f.acc[4](n, a, b) * pp;
+          sjz += f.acc[1](n, a, b) * pn + f.acc[5](n, a, b) * pp;
+          smy += f.acc[2](n, a, b) * pn + f.acc[6](n, a, b) * pp;
+          smz += f.acc[3](n, a, b) * pn + f.acc[7](n, a, b) * pp;
+        }
+      ay[q] += sjy * dy_dz; az[q] += sjz * dy_dz; fy[q] += smy * dy_dz; fz[q] += smz * dy_dz;
+    }
+    {  // Y, :467-510
+      const double dy_k = dy * f.k[n];
+      const double dz_dx = dz * dx;
+      cplx sjz(0, 0), sjx(0, 0), smz(0, 0), smx(0, 0);
+      for (size_t k = lk; k < rk; ++k)
+        for (size_t i = li; i < ri; ++i) {
+          double dn = dy_k * ((i - 0 + 0.5) * stcp + (lj - 0) * stsp + (k - 0 + 0.5) * cos_t);
+          cplx pn = std::exp(1i * dn);
+          double dp = dy_k * ((i - 0 + 0.5) * stcp + (rj - 0) * stsp + (k - 0 + 0.5) * cos_t);
+          cplx pp = std::exp(1i * dp);
+          size_t a = k - lk, b = i - li;
+          sjz += f.acc[8](n, a, b) * pn + f.acc[12](n, a, b) * pp;
+          sjx += f.acc[9](n, a, b) * pn + f.acc[13](n, a, b) * pp;
+          smz += f.acc[10](n, a, b) * pn + f.acc[14](n, a, b) * pp;
+          smx += f.acc[11](n, a, b) * pn + f.acc[15](n, a, b) * pp;
+        }
+      az[q] += sjz * dz_dx; ax[q] += sjx * dz_dx; fz[q] += smz * dz_dx; fx[q] += smx * dz_dx;
+    }
+    {  // Z, :512-556
+      const double dz_k = dz * f.k[n];
+      const double dx_dy = dx * dy;
+      cplx sjx(0, 0), sjy(0, 0), smx(0, 0), smy(0, 0);
+      for (size_t j = lj; j < rj; ++j)
+        for (size_t i = li; i < ri; ++i) {
+          double dn = dz_k * ((i - 0 + 0.5) * stcp + (j - 0 + 0.5) * stsp + (lk - 0) * cos_t);
+          cplx pn = std::exp(1i * dn);
+          double dp = dz_k * ((i - 0 + 0.5) * stcp + (j - 0 + 0.5) * stsp + (rk - 0) * cos_t);
+          cplx pp = std::exp(1i * dp);
+          size_t a = i - li, b = j - lj;
+          sjx += f.acc[16](n, a, b) * pn + f.acc[20](n, a, b) * pp;
+          sjy += f.acc[17](n, a, b) * pn + f.acc[21](n, a, b) * pp;
+          smx += f.acc[18](n, a, b) * pn + f.acc[22](n, a, b) * pp;
+          smy += f.acc[19](n, a, b) * pn + f.acc[23](n, a, b) * pp;
+        }
+      ax[q] += sjx * dx_dy; ay[q] += sjy * dx_dy; fx[q] += smx * dx_dy; fy[q] += smy * dx_dy;
+    }
+    double ctcp = cos_t * cos_p, ctsp = cos_t * sin_p;
+    a_theta[q] = ctcp * ax[q] + ctsp * ay[q] - sin_t * az[q];
+    a_phi[q] = -sin_p * ax[q] + cos_p * ay[q];
+    f_theta[q] = ctcp * fx[q] + ctsp * fy[q] - sin_t * fz[q];
+    f_phi[q] = -sin_p * fx[q] + cos_p * fy[q];
+  }
+  for (int w = 0; w < 8; ++w) f.out[w].assign(tot, cplx(0, 0));
+  f.power[0].assign(tot, 0.0);
+  f.power[1].assign(tot, 0.0);
+  for (size_t q = 0; q < tot; ++q) {
+    size_t n = q / (NT * NP);
+    double k = f.k[n];
+    double coff = std::pow(k, 2) / (32 * PI * PI * ETA_0);
+    f.out[0][q] = (-1i * k) * (ETA_0 * a_theta[q] + f_phi[q]) / (4 * PI);
+    f.out[1][q] = (1i * k) * (-ETA_0 * a_phi[q] + f_theta[q]) / (4 * PI);
+    f.out[2][q] = (1i * k) * (a_phi[q] - f_theta[q] / ETA_0) / (4 * PI);
+    f.out[3][q] = (-1i * k) * (a_theta[q] + f_phi[q] / ETA_0) / (4 * PI);
+    f.out[4][q] = a_theta[q];
+    f.out[5][q] = a_phi[q];
+    f.out[6][q] = f_theta[q];
+    f.out[7][q] = f_phi[q];
+    f.power[0][q] = coff * std::pow(std::abs(ETA_0 * a_theta[q] + f_phi[q]), 2);
+    f.power[1][q] = coff * std::pow(std::abs(-ETA_0 * a_phi[q] + f_theta[q]), 2);
+  }
+  f.ff_valid = true;
+  f.ff_step = cur;
+}
+
+// ---------------------------------------------------------------- C API ---
+namespace {
+template <class F>
+int guarded(F &&fn) {
+  try {
+    fn();
+    return 0;
+  } catch (const std::exception &e) {
+    g_error = e.what();
+    return 1;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+const char *oracle_last_error(void) { return g_error.c_str(); }
+
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n > 0 ? n : 1);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
+int oracle_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, oracle_sim **out) {
+  return guarded([&] {
+    if (!sc || !out) throw std::invalid_argument("null argument");
+    if (total_steps <= 0) throw std::invalid_argument("total_steps must be positive");
+    std::unique_ptr<oracle_sim> s(new oracle_sim());
+    s->cell = sc->cell_size;
+    s->cfl = sc->cfl;
+    s->total = static_cast<size_t>(total_steps);
+    for (int i = 0; i < sc->n_objects; ++i) s->objects.push_back(sc->objects[i]);
+    for (int i = 0; i < sc->n_pml; ++i) {
+      PML p;
+      p.d = sc->pml[i];
+      s->pmls.push_back(p);
+    }
+    for (int i = 0; i < sc->n_lumped; ++i) {
+      Lumped l;
+      l.d = sc->lumped[i];
+      s->lumped.push_back(l);
+    }
+    for (int i = 0; i < sc->n_monitors; ++i) {
+      Monitor m;
+      m.d = sc->monitors[i];
+      s->monitors.push_back(m);
+    }
+    if (sc->tfsf.enabled) {
+      s->has_tfsf = true;
+      s->tfsf_d = sc->tfsf;
+      for (int a = 0; a < 3; ++a) s->tf.dist[a] = static_cast<size_t>(sc->tfsf.distance[a]);
+      s->tf.e0 = sc->tfsf.e0;
+      s->tf.theta = sc->tfsf.theta;
+      s->tf.phi = sc->tfsf.phi;
+      s->tf.psi = sc->tfsf.psi;
+      s->tf.wave.d = sc->tfsf.waveform;
+      s->tf.wave.amplitude = sc->tfsf.waveform.amplitude;
+    }
+    if (sc->nffft.enabled) {
+      s->has_nffft = true;
+      for (int a = 0; a < 3; ++a) s->nf.dist[a] = static_cast<size_t>(sc->nffft.distance[a]);
+      s->nf.freq.assign(sc->nffft.frequencies, sc->nffft.frequencies + sc->nffft.n_freq);
+      s->nf.theta.assign(sc->nffft.theta, sc->nffft.theta + sc->nffft.n_theta);
+      s->nf.phi.assign(sc->nffft.phi, sc->nffft.phi + sc->nffft.n_phi);
+    }
+    if (sc->voxel_index) {
+      s->voxel_mats.assign(sc->voxel_materials, sc->voxel_materials + sc->n_voxel_materials);
+      size_t cnt = static_cast<size_t>(sc->voxel_shape[0] * sc->voxel_shape[1] * sc->voxel_shape[2]);
+      s->voxel_idx.assign(sc->voxel_index, sc->voxel_index + cnt);
+      for (int a = 0; a < 3; ++a) s->voxel_shape[a] = sc->voxel_shape[a];
+      for (uint16_t v : s->voxel_idx)
+        if (v >= sc->n_voxel_materials) throw std::invalid_argument("voxel index out of range");
+    }
+    s->init();
+    *out = s.release();
+  });
+}
+
+int oracle_sim_step(oracle_sim *s, int64_t n) {
+  return guarded([&] {
+    for (int64_t i = 0; i < n; ++i) s->step();
+  });
+}
+
+int oracle_sim_info(oracle_sim *s, int64_t out_n[3], double *out_dt, int64_t *out_step) {
+  return guarded([&] {
+    if (out_n) { out_n[0] = s->nx; out_n[1] = s->ny; out_n[2] = s->nz; }
+    if (out_dt) *out_dt = s->dt;
+    if (out_step) *out_step = static_cast<int64_t>(s->cur);
+  });
+}
+
+int oracle_sim_read_field(oracle_sim *s, int comp, double *out, int64_t len) {
+  return guarded([&] {
+    if (comp < 0 || comp > 5) throw std::invalid_argument("bad component");
+    A3 &a = s->field(comp);
+    if (static_cast<size_t>(len) != a.v.size()) throw std::invalid_argument("length mismatch");
+    std::memcpy(out, a.v.data(), a.v.size() * sizeof(double));
+  });
+}
+
+int oracle_sim_write_field(oracle_sim *s, int comp, const double *in, int64_t len) {
+  return guarded([&] {
+    if (comp < 0 || comp > 5) throw std::invalid_argument("bad component");
+    A3 &a = s->field(comp);
+    if (static_cast<size_t>(len) != a.v.size()) throw std::invalid_argument("length mismatch");
+    std::memcpy(a.v.data(), in, a.v.size() * sizeof(double));
+  });
+}
+
+int oracle_sim_read_monitor(oracle_sim *s, int index, double *out, int64_t len) {
+  return guarded([&] {
+    if (index < 0 || index >= static_cast<int>(s->monitors.size())) throw std::invalid_argument("bad monitor");
+    auto &v = s->monitors[index].value;
+    if (static_cast<size_t>(len) != v.size()) throw std::invalid_argument("length mismatch");
+    std::memcpy(out, v.data(), v.size() * sizeof(double));
+  });
+}
+
+int oracle_sim_read_nffft(oracle_sim *s, int which, double *out, int64_t len) {
+  return guarded([&] {
+    if (!s->has_nffft) throw std::invalid_argument("no NFFFT");
+    if (which < 0 || which >= 24) throw std::invalid_argument("bad accumulator");
+    auto &a = s->nf.acc[which].v;
+    if (static_cast<size_t>(len) != 2 * a.size()) throw std::invalid_argument("length mismatch");
+    std::memcpy(out, a.data(), a.size() * sizeof(cplx));
+  });
+}
+
+int oracle_sim_far_field(oracle_sim *s, int which, double *out, int64_t len) {
+  return guarded([&] {
+    if (!s->has_nffft) throw std::invalid_argument("no NFFFT");
+    if (!s->nf.ff_valid || s->nf.ff_step != s->cur) s->farField();
+    if (which >= 0 && which < 8) {
+      auto &v = s->nf.out[which];
+      if (static_cast<size_t>(len) != 2 * v.size()) throw std::invalid_argument("length mismatch");
+      std::memcpy(out, v.data(), v.size() * sizeof(cplx));
+    } else if (which == 8 || which == 9) {
+      auto &v = s->nf.power[which - 8];
+      if (static_cast<size_t>(len) != v.size()) throw std::invalid_argument("length mismatch");
+      std::memcpy(out, v.data(), v.size() * sizeof(double));
+    } else {
+      throw std::invalid_argument("bad far-field output");
+    }
+  });
+}
+
+int oracle_sim_incident_dft(oracle_sim *s, const double *freqs, int n, double *out) {
+  return guarded([&] {
+    if (!s->has_tfsf) throw std::invalid_argument("no TFSF");
+    using namespace std::complex_literals;
+    for (int i = 0; i < n; ++i) {  // util/dft.h:11-27
+      cplx sum(0.0, 0.0);
+      for (size_t j = 0; j < s->total; ++j) {
+        double t = j * s->dt;
+        sum += (s->tf.e0 * s->tf.wave.value[j]) * std::exp(-2.0 * 1i * PI * freqs[i] * t);
+      }
+      cplx r = sum * s->dt;
+      out[2 * i] = r.real();
+      out[2 * i + 1] = r.imag();
+    }
+  });
+}
+
+int oracle_sim_read_coeff(oracle_sim *s, int which, double *out, int64_t len) {
+  return guarded([&] {
+    if (which < 0 || which >= 18) throw std::invalid_argument("bad coefficient");
+    A3 &a = s->coeff(which);
+    if (static_cast<size_t>(len) != a.v.size()) throw std::invalid_argument("length mismatch");
+    std::memcpy(out, a.v.data(), a.v.size() * sizeof(double));
+  });
+}
+
+void oracle_sim_destroy(oracle_sim *s) { delete s; }
+
+int oracle_grid_from_cube(const double point[3], const double size[3], double dl, int64_t out_n[3],
+                          double *out_sizes, int64_t len) {
+  return guarded([&] {
+    GridSpace g(dl);
+    Box b{};
+    for (int a = 0; a < 3; ++a) { b.p[a] = point[a]; b.s[a] = size[a]; }
+    g.calculateSpaceSize(b);
+    g.generateUniformGridSpace();
+    g.ready = true;
+    for (int a = 0; a < 3; ++a) out_n[a] = static_cast<int64_t>(g.n[a]);
+    size_t need = 0;
+    for (int a = 0; a < 3; ++a) need += g.es[a].size() + g.hs[a].size();
+    if (static_cast<size_t>(len) < need) throw std::invalid_argument("output too small");
+    size_t o = 0;
+    for (int a = 0; a < 3; ++a)
+      for (double v : g.es[a]) out_sizes[o++] = v;
+    for (int a = 0; a < 3; ++a)
+      for (double v : g.hs[a]) out_sizes[o++] = v;
+  });
+}
+
+}  // extern "C"

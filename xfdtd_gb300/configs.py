@@ -1,0 +1,120 @@
+"""Seeded synthetic scenes with the shapes of the benchmark configurations.
+
+Every builder returns (Scene, total_steps).  `scale` shrinks the interior
+(cell counts are divided by it, CPML and TFSF / NF-FF offsets are kept) so
+that the same scene family can be run at sizes a CPU checker finishes in
+seconds.
+
+  pec_sphere_rcs      3-D PEC sphere bistatic RCS: 40^3 interior + 8-cell
+                      CPML (56^3), dx = 5 mm, sphere r = 10 cells, TFSF 4
+                      cells inside the CPML, x-polarised +z Gaussian
+                      (tau = 30 dt, t0 = 4.5 tau), dt = 0.98 x CFL, 800
+                      steps, NF-FF 2 cells inside the TFSF box at 1 GHz,
+                      361 angles over the phi = 0 great circle.
+  dielectric_sphere   256^3 interior + 12-cell CPML (280^3), dx = 2 mm,
+                      eps_r = 4 sphere of radius 60 cells, tau = 40 dt,
+                      2000 steps, NF-FF at 1, 2, 3 GHz, 181 angles in the
+                      phi = 0 and phi = 90 deg planes.
+  heterogeneous       512x512x384 + 10-cell CPML, dx = 1 mm, per-voxel
+                      material from a 256-entry table (eps_r U[1,6] as
+                      float, sigma U[0, 0.01] S/m; seeds 1001/1002), soft
+                      z-directed point current source at the centre
+                      (Gaussian-modulated sine, f0 = 10 GHz, 5 GHz
+                      bandwidth), 64 Ez probes at seeded cells (seed 1003),
+                      1000 steps.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import scene as S
+
+
+def cfl_dt(dl: float, cfl: float) -> float:
+    """dt of FDTDBasicCoff::calculateDeltaT (fdtd_basic_coff.cpp:342-346) for
+    a cubic cell; cfl passes through float as in Simulation(..., float cfl)."""
+    c = float(np.float32(cfl))
+    return c / (S.C_0 * math.sqrt(3.0 / (dl * dl)))
+
+
+def _six_pml(t: int):
+    return [S.PML(o, t) for o in (S.XN, S.XP, S.YN, S.YP, S.ZN, S.ZP)]
+
+
+def pec_sphere_rcs(scale: int = 1, steps: int = 800):
+    dl = 5e-3
+    half = 20 // scale
+    cpml = 8
+    objects = [
+        S.Object("domain", S.Cube([-half * dl] * 3, [2 * half * dl] * 3), S.Material("air", 1, 1, 0, 0)),
+        S.Object("scatter", S.Sphere([0, 0, 0], (10 // scale) * dl), S.Material("pec", 1, 1, 1e10, 0)),
+    ]
+    dt = cfl_dt(dl, 0.98)
+    tau = 30 * dt
+    t0 = 4.5 * tau
+    d_tfsf = cpml + 4
+    tfsf = S.TFSF3D(d_tfsf, d_tfsf, d_tfsf, 1.0, 0.0, 0.0, 0.0, S.GaussianWaveform(1.0, tau, t0))
+    theta = np.linspace(0.0, 2 * math.pi, 361)
+    nffft = S.NffftFd(d_tfsf + 2, d_tfsf + 2, d_tfsf + 2, [1e9], theta, [0.0], "pec_sphere_rcs")
+    sc = S.Scene(dl, objects, _six_pml(cpml), tfsf=tfsf, nffft=nffft, cfl=0.98)
+    return sc, steps
+
+
+def dielectric_sphere(scale: int = 1, steps: int = 2000, n_theta: int = 181):
+    dl = 2e-3
+    half = 128 // scale
+    cpml = 12
+    objects = [
+        S.Object("domain", S.Cube([-half * dl] * 3, [2 * half * dl] * 3), S.Material("air", 1, 1, 0, 0)),
+        S.Object("sphere", S.Sphere([0, 0, 0], (60 // scale) * dl), S.Material("dielectric", 4.0, 1, 0, 0)),
+    ]
+    dt = cfl_dt(dl, 0.98)
+    tau = 40 * dt
+    t0 = 4.5 * tau
+    d_tfsf = cpml + 4
+    tfsf = S.TFSF3D(d_tfsf, d_tfsf, d_tfsf, 1.0, 0.0, 0.0, 0.0, S.GaussianWaveform(1.0, tau, t0))
+    theta = np.linspace(0.0, math.pi, n_theta)
+    nffft = S.NffftFd(d_tfsf + 2, d_tfsf + 2, d_tfsf + 2, [1e9, 2e9, 3e9], theta, [0.0, math.pi / 2],
+                      "dielectric_sphere")
+    sc = S.Scene(dl, objects, _six_pml(cpml), tfsf=tfsf, nffft=nffft, cfl=0.98)
+    return sc, steps
+
+
+def heterogeneous(scale: int = 1, steps: int = 1000, n_probes: int = 64):
+    dl = 1e-3
+    cpml = 10
+    interior = (512 // scale, 512 // scale, 384 // scale)
+    n = tuple(v + 2 * cpml for v in interior)
+    objects = [S.Object("domain", S.Cube([0.0, 0.0, 0.0], [v * dl for v in interior]),
+                        S.Material("air", 1, 1, 0, 0))]
+    rng_t = np.random.default_rng(1001)
+    eps = rng_t.uniform(1.0, 6.0, 256).astype(np.float32)
+    sig = rng_t.uniform(0.0, 0.01, 256)
+    mats = [S.Material(f"m{i}", float(eps[i]), 1.0, float(sig[i]), 0.0) for i in range(256)]
+    rng_v = np.random.default_rng(1002)
+    voxel = rng_v.integers(0, 256, size=n, dtype=np.uint16)
+    dt = cfl_dt(dl, 0.99)
+    f0 = 10e9
+    tau = 2.0 / (math.pi * 5e9)
+    t0 = 4.5 * tau
+    src_cell = [v // 2 for v in interior]
+    src = S.CurrentSource(S.Cube([c * dl for c in src_cell], [dl, dl, dl]), S.ZP, 1e30,
+                          S.CustomWaveform(1.0, S.gaussian_modulated_sine(f0, tau, t0)))
+    rng_p = np.random.default_rng(1003)
+    probes = []
+    for _ in range(n_probes):
+        c = [int(rng_p.integers(0, v)) for v in interior]
+        probes.append(S.VoltageMonitor(S.Cube([q * dl for q in c], [dl, dl, dl]), S.ZP))
+    sc = S.Scene(dl, objects, _six_pml(cpml), lumped_elements=[src], monitors=probes, cfl=0.99,
+                 voxel_materials=mats, voxel_index=voxel)
+    del dt
+    return sc, steps
+
+
+CONFIGS = {
+    "pec_sphere_rcs": pec_sphere_rcs,
+    "dielectric_sphere": dielectric_sphere,
+    "heterogeneous": heterogeneous,
+}
