@@ -1,0 +1,212 @@
+/*
+ * xfdtd_cuda.h -- C-ABI of the GB300 FDTD engine (libxfdtd_cuda.so).
+ *
+ * The engine runs the loop body of the reference's Simulation::run
+ * (src/simulation/simulation_update.cpp:9-36) on one GPU:
+ *
+ *   updateE (:130-197) -> correctE: lumped (:282-290), TFSF3D::updateE
+ *   (src/tfsf/tfsf_3d.cpp:299-411) -> PML::updateE
+ *   (src/boundary/perfect_match_layer.cpp:574-718) -> updateH (:50-108) ->
+ *   TFSF3D::updateIncidentField (tfsf_3d.cpp:153-183) -> TFSF3D::updateH
+ *   (:185-297) -> PML::updateH (perfect_match_layer.cpp:434-572) ->
+ *   NffftFd::update (src/nffft/nffft_fd.cpp:108-203) -> Monitor::update
+ *   (src/monitor/voltage_monitor.cpp:64-97, current_monitor.cpp:70-115)
+ *
+ * and the far-field integration of NffftFd::calculateFarfield
+ * (nffft_fd.cpp:379-556) at the end.  The reference has no FFI; these
+ * entry points replace the virtual hooks Simulation calls per step
+ * (Boundary::updateE/H, TFSF::updateIncidentField/updateE/updateH,
+ * NFFFT::update, LumpedElement::correctE, Monitor::update -- declared in
+ * src/include/{boundary/boundary.h:28-52, tfsf/tfsf.h:80-90,
+ * nffft/nffft.h:71-75, lumped_element/lumped_element.h:22-30,
+ * monitor/monitor.h:31-37}) with one plan built once on the host.
+ *
+ * The plan is what the reference's init() computes
+ * (src/simulation/simulation_init.cpp:10-22), in a compact form: a per-cell
+ * material index into a table of the 18 update coefficients of
+ * FDTDBasicCoff::initCoff (src/fdtd_basic_coff/fdtd_basic_coff.cpp:77-121)
+ * instead of 18 full per-cell arrays; 1-D CPML profiles instead of the
+ * per-face c_psi slabs; the TFSF projection tables; the NF-FF phase tables.
+ *
+ * Conventions.  Grid cells nx, ny, nz include the CPML.  Every field,
+ * material-index and coefficient array uses the reference's (i, j, k)
+ * indexing, row-major with k fastest.  The handle owns all device memory;
+ * host arrays passed in are copied and not retained.  Calls on one handle
+ * must be serialised by the caller; distinct handles are independent.
+ * Every function returns XFDTD_OK (0) or an XFDTD_ERR_* status, and
+ * xfdtd_last_error() gives the message of the last failure on that handle.
+ */
+#ifndef XFDTD_CUDA_H_
+#define XFDTD_CUDA_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  XFDTD_OK = 0,
+  XFDTD_ERR_INVALID_PLAN = 1,   /* rejected on the host before any GPU work */
+  XFDTD_ERR_CUDA = 2,           /* a CUDA runtime call failed               */
+  XFDTD_ERR_OOM = 3,            /* device allocation failed                 */
+  XFDTD_ERR_TIMEOUT = 4,        /* a bounded device wait gave up            */
+  XFDTD_ERR_NAN = 5,            /* non-finite value found by xfdtd_check_finite */
+  XFDTD_ERR_DEVICE_CHECK = 6,   /* a device-side bounds check fired          */
+  XFDTD_ERR_STATE = 7           /* call not valid in the handle's state     */
+};
+
+enum { XFDTD_FP64 = 0, XFDTD_FP32 = 1 };
+
+/* Plan flags. */
+enum {
+  XFDTD_FLAG_GRAPH = 1,      /* replay the step loop from a captured CUDA graph */
+  XFDTD_FLAG_PROFILE = 2     /* time every kernel launch with CUDA events        */
+};
+
+/* The 18 coefficients of one table entry, in this order (the reference's
+ * names, fdtd_basic_coff.h): cexe cexhy cexhz ceye ceyhz ceyhx ceze cezhx
+ * cezhy chxh chxey chxez chyh chyez chyex chzh chzex chzey.  Values are
+ * those before the CPML's kappa division (perfect_match_layer.cpp:190-206);
+ * the engine applies 1/kappa from the CPML profiles. */
+#define XFDTD_N_COEFF 18
+
+/* CPML along one axis: the union of its N and P slabs.  For an E-located
+ * index I (0..n) slot_e[I] is the psi layer (0..n_layers-1) or -1 outside
+ * the slabs; slot_h likewise for H-located indices.  b/a are the CPML
+ * recursion coefficients and rk = 1/kappa of the layer (1 outside). */
+typedef struct xfdtd_cpml_axis {
+  int32_t n_layers;
+  int32_t reserved;
+  const int32_t *slot_e, *slot_h;          /* [n+1] */
+  const double *b_e, *a_e, *rk_e;          /* [n+1] */
+  const double *b_m, *a_m, *rk_m;          /* [n+1] */
+} xfdtd_cpml_axis;
+
+/* TFSF3D by the 1-D incident-field array (tfsf_3d.cpp:33-183). */
+typedef struct xfdtd_tfsf_plan {
+  int32_t enabled;
+  int32_t aux_len;                 /* L = ceil(diagonal * ratio_delta) + 5      */
+  int64_t lo[3], hi[3];            /* li lj lk, ri rj rk                        */
+  const double *proj_full[3];      /* [box_n + 1]                               */
+  const double *proj_half[3];      /* [box_n + 2]                               */
+  double transform_e[3], transform_h[3];
+  double ceihi, chiei;             /* 1-D free-space update coefficients        */
+  double mur_c1, mur_c2;           /* second-order Mur ABC at the far end       */
+  double ca[3], cb[3];             /* dt/(eps0 d), dt/(mu0 d) per axis          */
+  const double *source;            /* [total_steps] e0 * w(t dt)                */
+} xfdtd_tfsf_plan;
+
+/* NffftFd (nffft_fd.cpp:17-203, 379-556). */
+typedef struct xfdtd_nffft_plan {
+  int32_t enabled;
+  int32_t n_freq;
+  int64_t lo[3], hi[3];
+  const double *phase_j;           /* [n_freq * total_steps] (re, im) pairs    */
+  const double *phase_m;           /* [n_freq * total_steps] (re, im) pairs    */
+  const double *wave_number;       /* [n_freq]                                 */
+  int32_t n_theta, n_phi;
+  const double *theta, *phi;
+} xfdtd_nffft_plan;
+
+/* E(comp)[i,j,k] += coff * waveform[w][t]  (CurrentSource / VoltageSource
+ * ::correctE, current_source.cpp:140-163, voltage_source.cpp:171-194). */
+typedef struct xfdtd_injection {
+  int32_t comp, waveform;
+  int64_t i, j, k;
+  double coff;
+} xfdtd_injection;
+
+/* E += cecjc * J; J = cjcec * E + J  (Inductor::correctE, inductor.cpp:102-143). */
+typedef struct xfdtd_inductor_cell {
+  int32_t comp, reserved;
+  int64_t i, j, k;
+  double cecjc, cjcec;
+} xfdtd_inductor_cell;
+
+/* value[probe][t] = sum over the probe's terms of weight * F(comp)[i,j,k]
+ * (VoltageMonitor / CurrentMonitor as linear functionals).  Terms of one
+ * probe are contiguous and summed in order. */
+typedef struct xfdtd_probe_term {
+  int32_t probe, comp;
+  int64_t i, j, k;
+  double weight;
+} xfdtd_probe_term;
+
+typedef struct xfdtd_plan_desc {
+  int32_t nx, ny, nz;
+  int32_t precision;               /* XFDTD_FP64 or XFDTD_FP32 (fields, psi)    */
+  double dt;
+  double dl[3];
+  int64_t total_steps;
+  int32_t flags;                   /* XFDTD_FLAG_*                             */
+  int32_t index_bytes;             /* 1 or 2                                   */
+  int32_t n_materials;
+  int32_t reserved;
+  const void *material_index;      /* [(nx+1)*(ny+1)*(nz+1)]                   */
+  const double *coeff_table;       /* [n_materials * XFDTD_N_COEFF]            */
+  xfdtd_cpml_axis cpml[3];
+  xfdtd_tfsf_plan tfsf;
+  xfdtd_nffft_plan nffft;
+  int32_t n_waveforms;
+  int32_t n_injections;
+  const double *waveforms;         /* [n_waveforms * total_steps]              */
+  const xfdtd_injection *injections;
+  int32_t n_inductor_cells;
+  int32_t n_probes;
+  const xfdtd_inductor_cell *inductor_cells;
+  int32_t n_probe_terms;
+  int32_t reserved2;
+  const xfdtd_probe_term *probe_terms;
+} xfdtd_plan_desc;
+
+typedef struct xfdtd_handle xfdtd_handle;
+
+/* Validates the plan, allocates and uploads everything.  Replaces the
+ * per-component init hooks (Boundary::init, TFSF::init, NFFFT::init, ...). */
+int xfdtd_create(const xfdtd_plan_desc *plan, xfdtd_handle **out);
+/* Enqueues n steps of the loop body on the handle's stream (asynchronous). */
+int xfdtd_step(xfdtd_handle *h, int64_t n);
+/* Waits for the handle's stream and reports any device-side status. */
+int xfdtd_synchronize(xfdtd_handle *h);
+/* Enqueues n steps and returns their device time in milliseconds, measured
+ * with CUDA events on the handle's stream. */
+int xfdtd_step_timed(xfdtd_handle *h, int64_t n, double *ms);
+/* Current step index (steps completed). */
+int xfdtd_current_step(xfdtd_handle *h, int64_t *step);
+/* Field component c (0..5: Ex Ey Ez Hx Hy Hz) in the reference's component
+ * shape (Ex (nx,ny+1,nz+1) ... Hz (nx,ny,nz+1)), converted to FP64. */
+int xfdtd_read_field(xfdtd_handle *h, int comp, double *out, int64_t len);
+int xfdtd_write_field(xfdtd_handle *h, int comp, const double *in, int64_t len);
+/* Probe time series [n_probes * total_steps]. */
+int xfdtd_read_probes(xfdtd_handle *h, double *out, int64_t len);
+/* NF-FF accumulator `which` = face*4 + q (faces XN XP YN YP ZN ZP; X faces
+ * jy jz my mz over (ny_box, nz_box); Y faces jz jx mz mx over (nz_box,
+ * nx_box); Z faces jx jy mx my over (nx_box, ny_box)), [n_freq][a][b] (re, im). */
+int xfdtd_read_nffft(xfdtd_handle *h, int which, double *out, int64_t len);
+/* Far field over (n_freq, n_theta, n_phi): which 0 e_theta 1 e_phi 2 h_theta
+ * 3 h_phi 4 n_theta 5 n_phi 6 l_theta 7 l_phi (complex pairs), 8 power_theta
+ * 9 power_phi (real) -- the arrays NffftFd::outputData writes. */
+int xfdtd_far_field(xfdtd_handle *h, int which, double *out, int64_t len);
+/* Scans all fields for NaN / Inf (XFDTD_ERR_NAN if any). */
+int xfdtd_check_finite(xfdtd_handle *h);
+/* Per-kernel device time accumulated under XFDTD_FLAG_PROFILE:
+ * names[i] (static strings), total milliseconds and launch counts. */
+int xfdtd_profile(xfdtd_handle *h, int max, const char **names, double *ms, int64_t *launches, int *count);
+int xfdtd_profile_reset(xfdtd_handle *h);
+/* Kernel launches the engine enqueues per step for this plan. */
+int xfdtd_launches_per_step(xfdtd_handle *h, int *n);
+/* Device bytes held by the handle. */
+int xfdtd_device_bytes(xfdtd_handle *h, int64_t *bytes);
+const char *xfdtd_last_error(xfdtd_handle *h);
+void xfdtd_destroy(xfdtd_handle *h);
+
+/* Version string of the engine build. */
+const char *xfdtd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XFDTD_CUDA_H_ */

@@ -1,0 +1,57 @@
+/*
+ * xfdtd_sim.h -- scene-level C-ABI of libxfdtd.so (the C++ Simulation API
+ * behind plain C entry points), for callers in other languages.
+ *
+ * The reference has no FFI; a binding of its C++ API would construct
+ * Object / PML / TFSF3D / NffftFd / lumped elements / monitors and call
+ * Simulation::run (src/simulation/simulation_update.cpp:5-40).  These entry
+ * points do exactly that from an xfdtd_scene_desc (xfdtd_scene.h) and then
+ * expose what the reference writes at the end of a run: field snapshots
+ * (EMF getters), monitor time series (Monitor::outputData), the NF-FF
+ * accumulators and far field (NffftFd::outputData) and the incident-wave
+ * DFT (TFSF::getIncidentWaveFourierTransform, src/tfsf/tfsf.cpp:63-66).
+ *
+ * Status codes are those of xfdtd_cuda.h; setup errors the reference throws
+ * as std::runtime_error / std::out_of_range come back as
+ * XFDTD_ERR_INVALID_PLAN with the message in xfdtd_sim_last_error().
+ */
+#ifndef XFDTD_SIM_H_
+#define XFDTD_SIM_H_
+
+#include <stdint.h>
+
+#include "xfdtd_cuda.h"
+#include "xfdtd_scene.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct xfdtd_sim xfdtd_sim;
+
+/* Builds the Simulation and its engine plan for total_steps steps.
+ * precision: XFDTD_FP64 or XFDTD_FP32; flags: XFDTD_FLAG_*.  On failure *out
+ * is still set (when non-null) so that xfdtd_sim_last_error can be read; it
+ * must then be destroyed. */
+int xfdtd_sim_create(const xfdtd_scene_desc *scene, int64_t total_steps, int precision, int flags, xfdtd_sim **out);
+int xfdtd_sim_step(xfdtd_sim *s, int64_t n);
+int xfdtd_sim_info(xfdtd_sim *s, int64_t out_n[3], double *out_dt, int64_t *out_step);
+int xfdtd_sim_read_field(xfdtd_sim *s, int comp, double *out, int64_t len);
+int xfdtd_sim_write_field(xfdtd_sim *s, int comp, const double *in, int64_t len);
+int xfdtd_sim_read_monitor(xfdtd_sim *s, int index, double *out, int64_t len);
+int xfdtd_sim_read_nffft(xfdtd_sim *s, int which, double *out, int64_t len);
+int xfdtd_sim_far_field(xfdtd_sim *s, int which, double *out, int64_t len);
+int xfdtd_sim_incident_dft(xfdtd_sim *s, const double *freqs, int n, double *out);
+/* Writes the reference's .npy outputs (NF-FF into its output directory,
+ * monitors into theirs). */
+int xfdtd_sim_output(xfdtd_sim *s);
+/* The engine handle behind the simulation (for timing and profiling). */
+xfdtd_handle *xfdtd_sim_engine(xfdtd_sim *s);
+const char *xfdtd_sim_last_error(xfdtd_sim *s);
+void xfdtd_sim_destroy(xfdtd_sim *s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XFDTD_SIM_H_ */

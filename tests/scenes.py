@@ -1,0 +1,124 @@
+"""Small seeded scenes shared by the CPU and GPU tests (test utility).
+
+Each builder returns (Scene, steps) at a size the CPU oracle runs in seconds.
+"""
+import math
+
+import numpy as np
+
+from xfdtd_gb300 import configs
+from xfdtd_gb300 import scene as S
+
+
+def pec_sphere(scale=2, steps=300):
+    return configs.pec_sphere_rcs(scale=scale, steps=steps)
+
+
+def dielectric(scale=8, steps=300):
+    return configs.dielectric_sphere(scale=scale, steps=steps, n_theta=19)
+
+
+def heterogeneous(scale=16, steps=150, n_probes=8):
+    return configs.heterogeneous(scale=scale, steps=steps, n_probes=n_probes)
+
+
+def oblique(steps=250):
+    """Dielectric sphere lit by an oblique plane wave (theta 30, phi 45, psi 60 deg)."""
+    dl = 5e-3
+    half = 12
+    objects = [
+        S.Object("domain", S.Cube([-half * dl] * 3, [2 * half * dl] * 3), S.Material("air", 1, 1, 0, 0)),
+        S.Object("ball", S.Sphere([0.3 * dl, -0.2 * dl, 0.1 * dl], 5.5 * dl), S.Material("d", 3.5, 1.0, 0.02, 0.0)),
+    ]
+    dt = configs.cfl_dt(dl, 0.98)
+    tau = 20 * dt
+    tfsf = S.TFSF3D(10, 10, 10, 2.0, math.pi / 6, math.pi / 4, math.pi / 3,
+                    S.GaussianWaveform(1.0, tau, 4.5 * tau))
+    nffft = S.NffftFd(12, 12, 12, [2e9, 5e9], np.linspace(0, math.pi, 13), [0.0, 1.0], "oblique")
+    boundaries = [S.PML(o, 6) for o in (S.XN, S.XP, S.YN, S.YP, S.ZN, S.ZP)]
+    return S.Scene(dl, objects, boundaries, tfsf=tfsf, nffft=nffft, cfl=0.98), steps
+
+
+def partial_pml(steps=200):
+    """CPML on three faces only (the others stay PEC walls), asymmetric grid,
+    cube and cylinder objects, non-default CPML parameters."""
+    dl = 4e-3
+    objects = [
+        S.Object("domain", S.Cube([0, 0, 0], [20 * dl, 26 * dl, 17 * dl]), S.Material("air", 1, 1, 0, 0)),
+        S.Object("block", S.Cube([5 * dl, 6 * dl, 4 * dl], [4 * dl, 7 * dl, 5 * dl]), S.Material("b", 2.2, 1.3, 0.05, 10.0)),
+        S.Object("rod", S.Cylinder(S.AXIS_Y, [12 * dl, 13 * dl, 9 * dl], 2.6 * dl, 14 * dl),
+                 S.Material("r", 5.0, 1.0, 0.0, 0.0)),
+    ]
+    boundaries = [S.PML(S.XN, 5, 3, 0.8, 0.01, 0.1, 6.0), S.PML(S.YP, 7), S.PML(S.ZN, 4, 2, 1.2, 0.0, 0.03, 12.0)]
+    src = S.CurrentSource(S.Cube([10 * dl, 12 * dl, 8 * dl], [dl, dl, dl]), S.ZP, 50.0,
+                          S.CosineModulatedGaussianWaveform(1e-3, 40e-12, 160e-12, 6e9))
+    mons = [S.VoltageMonitor(S.Cube([14 * dl, 15 * dl, 6 * dl], [dl, dl, 3 * dl]), S.ZP),
+            S.VoltageMonitor(S.Cube([8 * dl, 18 * dl, 10 * dl], [2 * dl, dl, dl]), S.XN)]
+    return S.Scene(dl, objects, boundaries, lumped_elements=[src], monitors=mons, cfl=0.95), steps
+
+
+def lumped(steps=300):
+    """Voltage source, resistor, capacitor, inductor and current source in a
+    CPML box, with voltage and current monitors."""
+    dl = 1e-3
+    objects = [S.Object("domain", S.Cube([0, 0, 0], [24 * dl, 24 * dl, 24 * dl]), S.Material("air", 1, 1, 0, 0))]
+    boundaries = [S.PML(o, 6) for o in (S.XN, S.XP, S.YN, S.YP, S.ZN, S.ZP)]
+    tau = 30e-12
+    le = [
+        S.VoltageSource(S.Cube([10 * dl, 10 * dl, 10 * dl], [dl, dl, 2 * dl]), S.ZP, 50.0,
+                        S.GaussianWaveform(1.0, tau, 4.5 * tau)),
+        S.Resistor(S.Cube([14 * dl, 10 * dl, 10 * dl], [dl, dl, 2 * dl]), S.AXIS_Z, 100.0),
+        S.Capacitor(S.Cube([10 * dl, 14 * dl, 10 * dl], [2 * dl, dl, dl]), S.AXIS_X, 1e-12),
+        S.Inductor(S.Cube([13 * dl, 14 * dl, 12 * dl], [dl, dl, 2 * dl]), S.AXIS_Z, 2e-9),
+        S.CurrentSource(S.Cube([6 * dl, 16 * dl, 8 * dl], [2 * dl, 2 * dl, dl]), S.ZN, 1e3,
+                        S.SinusoidalWaveform(1e-3, 8e9, 0.3)),
+    ]
+    mons = [
+        S.VoltageMonitor(S.Cube([10 * dl, 10 * dl, 10 * dl], [dl, dl, 2 * dl]), S.ZP),
+        S.VoltageMonitor(S.Cube([14 * dl, 10 * dl, 10 * dl], [dl, dl, 2 * dl]), S.ZN),
+        S.CurrentMonitor(S.Cube([10 * dl, 10 * dl, 11 * dl], [dl, dl, 0]), S.ZP),
+        S.CurrentMonitor(S.Cube([13 * dl, 14 * dl, 13 * dl], [dl, dl, 0]), S.ZN),
+        S.CurrentMonitor(S.Cube([11 * dl, 14 * dl, 10 * dl], [0, dl, dl]), S.XP),
+    ]
+    return S.Scene(dl, objects, boundaries, lumped_elements=le, monitors=mons, cfl=0.99), steps
+
+
+def thin_wire(steps=300):
+    """A z-directed half-wave-style thin-wire dipole fed by a voltage source
+    across its gap (the reference's examples/thin_wire.cpp layout), plus x-
+    and y-directed wires (ThinWire, src/object/thin_wire.cpp)."""
+    dl = 2e-3
+    objects = [
+        S.Object("domain", S.Cube([-12 * dl] * 3, [24 * dl] * 3), S.Material("air", 1, 1, 0, 0)),
+        S.ThinWire("arm0", S.Cylinder(S.AXIS_Z, [0, 0, 4.5 * dl], 0.1 * dl, 7 * dl)),
+        S.ThinWire("arm1", S.Cylinder(S.AXIS_Z, [0, 0, -4.5 * dl], 0.1 * dl, 7 * dl)),
+        S.ThinWire("wx", S.Cylinder(S.AXIS_X, [0, 5 * dl, 5 * dl], 0.2 * dl, 8 * dl)),
+        S.ThinWire("wy", S.Cylinder(S.AXIS_Y, [-5 * dl, 0, -4 * dl], 0.15 * dl, 6 * dl)),
+    ]
+    boundaries = [S.PML(o, 6) for o in (S.XN, S.XP, S.YN, S.YP, S.ZN, S.ZP)]
+    tau = 40e-12
+    le = [S.VoltageSource(S.Cube([0, 0, -dl], [dl, dl, 2 * dl]), S.ZP, 50.0, S.GaussianWaveform(1.0, tau, 4.5 * tau))]
+    mons = [S.VoltageMonitor(S.Cube([0, 0, -dl], [dl, dl, 2 * dl]), S.ZP),
+            S.CurrentMonitor(S.Cube([0, 0, 0], [dl, dl, dl]), S.ZP)]
+    return S.Scene(dl, objects, boundaries, lumped_elements=le, monitors=mons, cfl=0.99), steps
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b| (0 when both vanish)."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    scale = np.abs(b).max()
+    if scale == 0:
+        return float(np.abs(a).max())
+    return float(np.abs(a - b).max() / scale)
+
+
+SCENES = {
+    "pec_sphere": pec_sphere,
+    "dielectric": dielectric,
+    "heterogeneous": heterogeneous,
+    "oblique": oblique,
+    "partial_pml": partial_pml,
+    "lumped": lumped,
+    "thin_wire": thin_wire,
+}

@@ -1,0 +1,154 @@
+"""Pins the CPU oracle (FP64 restatement of the reference) before it is
+trusted as the GPU engine's checker.
+
+* test/test_grid.cpp of the reference, restated: uniform GridSpace counts
+  and node sizes for seeded random cubes.
+* Analytic facts of the reference's algorithm: exact TFSF cancellation for
+  normal incidence, CPML absorption, and the PEC-sphere bistatic RCS against
+  a Mie series within the ~1 dB the reference's readme reports
+  (readme.md: "average error of 1dB").
+* Committed golden vectors (tests/golden, made by make_golden.py).
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+import mie
+import oracle as O
+import scenes
+from xfdtd_gb300 import configs
+from xfdtd_gb300 import scene as S
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _threads():
+    O.set_threads(min(8, os.cpu_count() or 1))
+
+
+def test_grid_space_matches_reference_test_grid():
+    """test/test_grid.cpp:12-91: for random cubes with dl = size/20 the grid
+    has 20 cells per axis and every node size equals dl within 10 eps."""
+    rng = np.random.default_rng(20240)
+    for _ in range(10):
+        origin = rng.uniform(0, 1, 3)
+        size_x = rng.uniform(0, 1)
+        dl = size_x / 20.0
+        n, sizes = O.grid_from_cube(origin, [size_x] * 3, dl)
+        assert n == (20, 20, 20)
+        for key in ("esx", "esy", "esz"):
+            assert np.all(np.abs(sizes[key] - dl) <= 10 * np.finfo(float).eps), key
+        for key in ("hsx", "hsy", "hsz"):
+            assert sizes[key].shape == (21,)
+            assert np.all(np.abs(sizes[key] - dl) <= 10 * np.finfo(float).eps), key
+
+
+def test_tfsf_normal_incidence_cancels_outside_box():
+    sc, _ = configs.pec_sphere_rcs(scale=2, steps=260)
+    sc.objects = sc.objects[:1]
+    o = O.OracleSim(sc, 260)
+    inside = outside = 0.0
+    d = sc.tfsf.distance_x
+    for _ in range(13):
+        o.step(20)
+        ex = o.read_field(S.EX)
+        inside = max(inside, np.abs(ex[d + 1:-d - 1, d + 1:-d - 1, d + 1:-d - 1]).max())
+        m = ex.copy()
+        m[d - 1:-d + 1, d - 1:-d + 1, d - 1:-d + 1] = 0
+        outside = max(outside, np.abs(m).max())
+    assert inside > 0.99
+    assert outside < 1e-12 * inside
+
+
+def test_tfsf_oblique_incidence_leakage_small():
+    sc, st = scenes.oblique(steps=220)
+    sc.objects = sc.objects[:1]
+    o = O.OracleSim(sc, st)
+    o.step(st)
+    ey = o.read_field(S.EY)
+    d = sc.tfsf.distance_x
+    m = ey.copy()
+    m[d - 1:-d + 1, d - 1:-d + 1, d - 1:-d + 1] = 0
+    # the 1-D auxiliary grid does not match the 3-D grid's dispersion exactly:
+    # a leakage of a few percent of the incident amplitude is the method's own
+    assert np.abs(m).max() < 0.05 * sc.tfsf.e_0
+
+
+def test_cpml_absorbs_outgoing_wave():
+    """A soft point source radiates in a box with a CPML of T cells 12 cells
+    away; a probe 8 cells out is compared with the same probe in a box 40
+    cells wide, over the window before that box's own walls answer.  The
+    reflection falls with T (about -21, -30, -41 dB for T = 6, 10, 16 with
+    the reference's default CPML parameters)."""
+    def run(half, t_pml, steps=150):
+        dl = 1e-3
+        objects = [S.Object("air", S.Cube([-half * dl] * 3, [2 * half * dl] * 3), S.Material("air", 1, 1, 0, 0))]
+        src = S.CurrentSource(S.Cube([0, 0, 0], [dl, dl, dl]), S.ZP, 1e30,
+                              S.CustomWaveform(1.0, S.gaussian_modulated_sine(30e9, 15e-12, 60e-12)))
+        mon = S.VoltageMonitor(S.Cube([8 * dl, 0, 0], [dl, dl, dl]), S.ZP)
+        sc = S.Scene(dl, objects, [S.PML(o_, t_pml) for o_ in range(6)], lumped_elements=[src], monitors=[mon])
+        o = O.OracleSim(sc, steps)
+        o.step(steps)
+        return o.read_monitor(0)
+    big = run(40, 10)
+    refl = {}
+    for t_pml in (6, 10, 16):
+        small = run(12, t_pml)
+        refl[t_pml] = 20 * math.log10(np.abs(small - big).max() / np.abs(big).max())
+    assert refl[10] < -25
+    assert refl[16] < refl[10] < refl[6]
+    assert refl[6] - refl[16] > 15
+
+
+def test_pec_sphere_rcs_against_mie():
+    sc, st = configs.pec_sphere_rcs()
+    o = O.OracleSim(sc, st)
+    o.step(st)
+    rcs = o.rcs_db()[0, :, 0]
+    theta = np.linspace(0, 2 * np.pi, 361)
+    th = np.where(theta > np.pi, 2 * np.pi - theta, theta)
+    se, _ = mie.pec_sphere_rcs(0.05, 1e9, th)
+    err = np.abs(rcs - 10 * np.log10(se))
+    assert err.mean() < 1.5, err.mean()   # the reference reports ~1 dB on average
+    assert err.max() < 3.0
+
+
+@pytest.mark.parametrize("name", sorted(scenes.SCENES))
+def test_oracle_matches_golden(name):
+    path = os.path.join(GOLDEN, f"{name}.npz")
+    g = np.load(path)
+    sc, _ = scenes.SCENES[name]()
+    steps = int(g["steps"])
+    o = O.OracleSim(sc, steps)
+    o.step(steps)
+    for c in range(6):
+        f = o.read_field(c)
+        np.testing.assert_allclose(f.sum(axis=(1, 2)), g[f"f{c}_xsum"], rtol=1e-12, atol=1e-300)
+        np.testing.assert_allclose(f[f.shape[0] // 2], g[f"f{c}_slice"], rtol=1e-12, atol=1e-30)
+    for m in range(len(sc.monitors)):
+        np.testing.assert_allclose(o.read_monitor(m), g[f"m{m}"], rtol=1e-12, atol=1e-30)
+    if sc.nffft is not None:
+        for w in (0, 1, 8):
+            np.testing.assert_allclose(o.far_field(w), g[f"ff{w}"], rtol=1e-10, atol=1e-30)
+
+
+def test_scene_description_round_trip():
+    sc, st = scenes.lumped(steps=3)
+    d = sc.desc()
+    assert d.n_objects == 1 and d.n_pml == 6 and d.n_lumped == 5 and d.n_monitors == 5
+    assert abs(d.cfl - 0.99) < 1e-7
+    o = O.OracleSim(sc, st)
+    assert o.n == (36, 36, 36)
+
+
+def test_oracle_rejects_bad_scenes():
+    sc, st = scenes.pec_sphere()
+    sc.objects.append(S.ThinWire("fat", S.Cylinder(S.AXIS_Z, [0, 0, 0], 0.01, 0.05)))
+    with pytest.raises(RuntimeError, match="not enough thin"):
+        O.OracleSim(sc, st)
+    sc2, _ = scenes.pec_sphere()
+    with pytest.raises(RuntimeError):
+        O.OracleSim(sc2, 0)

@@ -1,0 +1,239 @@
+"""xfdtd_gb300 -- GB300-native engine for the XFDTD (Mrwatermolen/XFDTD)
+time-stepping hot path: Yee E/H with CPML, TFSF plane-wave injection, the
+NF-FF running DFT and far-field integration, lumped elements, thin wires and
+probes, as hand-written CUDA for sm_103a behind a C-ABI.
+
+Python binding of the scene-level C-ABI (include/xfdtd_sim.h) and of the
+engine's timing / profiling entry points (include/xfdtd_cuda.h).  There is
+no CPU fallback: if the native libraries are missing or no GPU is present,
+every call that would run the engine raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import scene
+from .scene import (  # noqa: F401  (re-exported: the reference's scene API)
+    AXIS_X, AXIS_Y, AXIS_Z, EX, EY, EZ, HX, HY, HZ, XN, XP, YN, YP, ZN, ZP,
+    Capacitor, CosineModulatedGaussianWaveform, CurrentMonitor, CurrentSource, Cube,
+    CustomWaveform, Cylinder, GaussianWaveform, Inductor, Material, NffftFd, Object, PML,
+    Resistor, Scene, SinusoidalWaveform, Sphere, TFSF3D, ThinWire, VoltageMonitor,
+    VoltageSource,
+)
+
+FP64, FP32 = 0, 1
+FLAG_GRAPH, FLAG_PROFILE = 1, 2
+STATUS = {0: "ok", 1: "invalid plan", 2: "CUDA error", 3: "out of device memory", 4: "timeout",
+          5: "non-finite value", 6: "device check", 7: "bad state"}
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_DIR = os.path.join(_HERE, "_lib")
+_cuda = None
+_host = None
+
+
+class EngineError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+def build(force: bool = False) -> None:
+    """Compiles the native libraries in-tree (see native_build.py)."""
+    from . import native_build
+    native_build.build(force=force)
+
+
+def libs():
+    """Loads libxfdtd_cuda.so and libxfdtd.so (raises if they are not built)."""
+    global _cuda, _host
+    if _host is None:
+        cuda_path = os.path.join(_LIB_DIR, "libxfdtd_cuda.so")
+        host_path = os.path.join(_LIB_DIR, "libxfdtd.so")
+        if not (os.path.exists(cuda_path) and os.path.exists(host_path)):
+            raise ImportError("xfdtd_gb300 native libraries are not built; run xfdtd_gb300.build()")
+        cu = C.CDLL(cuda_path, mode=C.RTLD_GLOBAL)
+        ho = C.CDLL(host_path)
+        P = C.POINTER
+        dp = P(C.c_double)
+        ho.xfdtd_sim_create.argtypes = [P(scene.SceneDesc), C.c_int64, C.c_int, C.c_int, P(C.c_void_p)]
+        ho.xfdtd_sim_step.argtypes = [C.c_void_p, C.c_int64]
+        ho.xfdtd_sim_info.argtypes = [C.c_void_p, P(C.c_int64), dp, P(C.c_int64)]
+        for fn in ("xfdtd_sim_read_field", "xfdtd_sim_read_monitor", "xfdtd_sim_read_nffft", "xfdtd_sim_far_field"):
+            getattr(ho, fn).argtypes = [C.c_void_p, C.c_int, dp, C.c_int64]
+        ho.xfdtd_sim_write_field.argtypes = [C.c_void_p, C.c_int, dp, C.c_int64]
+        ho.xfdtd_sim_incident_dft.argtypes = [C.c_void_p, dp, C.c_int, dp]
+        ho.xfdtd_sim_output.argtypes = [C.c_void_p]
+        ho.xfdtd_sim_engine.argtypes = [C.c_void_p]
+        ho.xfdtd_sim_engine.restype = C.c_void_p
+        ho.xfdtd_sim_last_error.argtypes = [C.c_void_p]
+        ho.xfdtd_sim_last_error.restype = C.c_char_p
+        ho.xfdtd_sim_destroy.argtypes = [C.c_void_p]
+        cu.xfdtd_step_timed.argtypes = [C.c_void_p, C.c_int64, dp]
+        cu.xfdtd_step.argtypes = [C.c_void_p, C.c_int64]
+        cu.xfdtd_synchronize.argtypes = [C.c_void_p]
+        cu.xfdtd_check_finite.argtypes = [C.c_void_p]
+        cu.xfdtd_profile.argtypes = [C.c_void_p, C.c_int, P(C.c_char_p), dp, P(C.c_int64), P(C.c_int)]
+        cu.xfdtd_profile_reset.argtypes = [C.c_void_p]
+        cu.xfdtd_launches_per_step.argtypes = [C.c_void_p, P(C.c_int)]
+        cu.xfdtd_device_bytes.argtypes = [C.c_void_p, P(C.c_int64)]
+        cu.xfdtd_last_error.argtypes = [C.c_void_p]
+        cu.xfdtd_last_error.restype = C.c_char_p
+        cu.xfdtd_version.restype = C.c_char_p
+        _cuda, _host = cu, ho
+    return _cuda, _host
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Simulation:
+    """One simulation on the GPU engine, built from a `scene.Scene`.
+
+    precision: "fp64" (the reference's arithmetic) or "fp32" (fields and CPML
+    state in FP32; TFSF 1-D grid, NF-FF accumulation and far-field
+    integration stay FP64).
+    """
+
+    def __init__(self, sc: "scene.Scene", total_steps: int, precision: str = "fp64", graph: bool = True,
+                 profile: bool = False):
+        self.scene = sc
+        self.total_steps = int(total_steps)
+        self.precision = precision
+        cu, ho = libs()
+        self._desc = sc.desc()
+        prec = FP64 if precision == "fp64" else FP32
+        flags = (FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0)
+        h = C.c_void_p()
+        rc = ho.xfdtd_sim_create(C.byref(self._desc), self.total_steps, prec, flags, C.byref(h))
+        self.h = h
+        if rc != 0:
+            msg = ho.xfdtd_sim_last_error(h).decode() if h.value else "no handle"
+            ho.xfdtd_sim_destroy(h)
+            self.h = None
+            raise EngineError(rc, msg)
+        n = (C.c_int64 * 3)()
+        dt = C.c_double()
+        ho.xfdtd_sim_info(self.h, n, C.byref(dt), None)
+        self.n = tuple(int(v) for v in n)
+        self.dt = dt.value
+        self.engine = C.c_void_p(ho.xfdtd_sim_engine(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            libs()[1].xfdtd_sim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise EngineError(rc, libs()[1].xfdtd_sim_last_error(self.h).decode())
+
+    def _check_engine(self, rc: int):
+        if rc != 0:
+            raise EngineError(rc, libs()[0].xfdtd_last_error(self.engine).decode())
+
+    @property
+    def step_index(self) -> int:
+        st = C.c_int64()
+        libs()[1].xfdtd_sim_info(self.h, None, None, C.byref(st))
+        return st.value
+
+    def step(self, n: int = 1):
+        self._check(libs()[1].xfdtd_sim_step(self.h, int(n)))
+
+    def step_timed(self, n: int) -> float:
+        """Enqueues n steps; returns their device time in ms (CUDA events)."""
+        ms = C.c_double()
+        self._check_engine(libs()[0].xfdtd_step_timed(self.engine, int(n), C.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        self._check_engine(libs()[0].xfdtd_synchronize(self.engine))
+
+    def check_finite(self):
+        self._check_engine(libs()[0].xfdtd_check_finite(self.engine))
+
+    def read_field(self, comp: int) -> np.ndarray:
+        out = np.empty(scene.field_shape(comp, self.n), dtype=np.float64)
+        self._check(libs()[1].xfdtd_sim_read_field(self.h, comp, _dp(out), out.size))
+        return out
+
+    def write_field(self, comp: int, a: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        self._check(libs()[1].xfdtd_sim_write_field(self.h, comp, _dp(a), a.size))
+
+    def read_monitor(self, index: int) -> np.ndarray:
+        out = np.empty(self.total_steps, dtype=np.float64)
+        self._check(libs()[1].xfdtd_sim_read_monitor(self.h, index, _dp(out), out.size))
+        return out
+
+    def nffft_box(self):
+        nf = self.scene.nffft
+        return (self.n[0] - 2 * nf.distance_x, self.n[1] - 2 * nf.distance_y, self.n[2] - 2 * nf.distance_z)
+
+    def read_nffft(self, which: int) -> np.ndarray:
+        nfreq = len(np.atleast_1d(self.scene.nffft.frequencies))
+        shp = (nfreq,) + scene.nffft_face_shape(which, self.nffft_box())
+        out = np.empty(shp + (2,), dtype=np.float64)
+        self._check(libs()[1].xfdtd_sim_read_nffft(self.h, which, _dp(out), out.size))
+        return out[..., 0] + 1j * out[..., 1]
+
+    def far_field(self, which: int) -> np.ndarray:
+        f, t, p = self.scene.nffft.arrays()
+        shp = (len(f), len(t), len(p))
+        if which < 8:
+            out = np.empty(shp + (2,), dtype=np.float64)
+            self._check(libs()[1].xfdtd_sim_far_field(self.h, which, _dp(out), out.size))
+            return out[..., 0] + 1j * out[..., 1]
+        out = np.empty(shp, dtype=np.float64)
+        self._check(libs()[1].xfdtd_sim_far_field(self.h, which, _dp(out), out.size))
+        return out
+
+    def incident_dft(self, freqs) -> np.ndarray:
+        f = np.ascontiguousarray(np.atleast_1d(freqs), dtype=np.float64)
+        out = np.empty((len(f), 2), dtype=np.float64)
+        self._check(libs()[1].xfdtd_sim_incident_dft(self.h, _dp(f), len(f), _dp(out)))
+        return out[:, 0] + 1j * out[:, 1]
+
+    def rcs_db(self) -> np.ndarray:
+        et, ep = self.far_field(0), self.far_field(1)
+        f, _, _ = self.scene.nffft.arrays()
+        inc = self.incident_dft(f)
+        sigma = 4 * np.pi * (np.abs(et) ** 2 + np.abs(ep) ** 2) / (np.abs(inc)[:, None, None] ** 2)
+        return 10 * np.log10(sigma)
+
+    def output(self):
+        self._check(libs()[1].xfdtd_sim_output(self.h))
+
+    def profile(self) -> dict:
+        """Per-kernel device time (ms) and launches recorded under profile=True."""
+        names = (C.c_char_p * 16)()
+        ms = (C.c_double * 16)()
+        cnt = (C.c_int64 * 16)()
+        n = C.c_int()
+        self._check_engine(libs()[0].xfdtd_profile(self.engine, 16, names, ms, cnt, C.byref(n)))
+        return {names[i].decode(): (ms[i], int(cnt[i])) for i in range(n.value)}
+
+    def profile_reset(self):
+        self._check_engine(libs()[0].xfdtd_profile_reset(self.engine))
+
+    def launches_per_step(self) -> int:
+        n = C.c_int()
+        self._check_engine(libs()[0].xfdtd_launches_per_step(self.engine, C.byref(n)))
+        return n.value
+
+    def device_bytes(self) -> int:
+        b = C.c_int64()
+        self._check_engine(libs()[0].xfdtd_device_bytes(self.engine, C.byref(b)))
+        return b.value
+
+
+def version() -> str:
+    return libs()[0].xfdtd_version().decode()

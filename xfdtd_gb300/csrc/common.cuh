@@ -1,0 +1,74 @@
+// common.cuh -- device-side data layout shared by the engine's kernels.
+//
+// Fields live in one uniform padded box per component: (nx+1) x (ny+1) x NZP
+// with NZP = nz+1 rounded up to 32, i.e. index (i*(ny+1) + j)*NZP + k.  Every
+// component of the reference (Ex (nx,ny+1,nz+1) ... Hz (nx,ny,nz+1),
+// src/simulation/simulation_init.cpp:28-35) fits in that box at the same
+// (i, j, k); the cells a component does not have stay zero and are never
+// written.  k is the contiguous axis, so a warp reads 128 contiguous bytes
+// (FP32) of one row.
+#pragma once
+
+#include <cstdint>
+
+namespace xg {
+
+struct Dims {
+  int nx, ny, nz;
+  int nzp;            // padded row length
+  long long sj, si;   // strides of j and i
+  long long cells;    // (nx+1)*(ny+1)*nzp
+};
+
+// CPML profile along one axis (device copy of xfdtd_cpml_axis).
+template <typename T>
+struct CpmlAxis {
+  int n_layers;
+  const int *slot_e, *slot_h;
+  const T *b_e, *a_e, *rk_e;
+  const T *b_m, *a_m, *rk_m;
+};
+
+// TFSF surface data.  inc holds two buffers (step parity) of the projected
+// incident arrays ex, ey, ez (aux_len each) and hx, hy, hz (aux_len-1 each,
+// stored with stride aux_len).
+struct TfsfDev {
+  int enabled;
+  int L;
+  int lo[3], hi[3];
+  const double *pf[3], *ph[3];
+  double ca[3], cb[3];
+  const double *inc;   // [2][6][L]
+};
+
+// psi storage: axis X (L, ny+1, nzp), axis Y (nx+1, L, nzp), axis Z (nx+1, ny+1, L).
+template <typename T>
+struct Psi {
+  T *ex_y, *ex_z, *ey_x, *ey_z, *ez_x, *ez_y;   // E recursions
+  T *hx_y, *hx_z, *hy_x, *hy_z, *hz_x, *hz_y;   // H recursions
+};
+
+template <typename T, typename I>
+struct VolParams {
+  Dims d;
+  T *E[3];
+  T *H[3];
+  const I *idx;
+  const T *table;      // [n_mat][18], reference coefficient order
+  int n_mat;
+  CpmlAxis<T> cp[3];
+  Psi<T> psi;
+  T dl[3];
+  TfsfDev tf;
+  const long long *step;
+  int chunk;           // planes of i per block
+};
+
+__device__ __forceinline__ double tfsf_interp(const double *v, double projection) {
+  // TFSF3D::getIncident*, src/tfsf/tfsf_3d.cpp:413-483
+  const unsigned long long index = static_cast<unsigned long long>(projection);
+  const double weight = projection - static_cast<double>(index);
+  return (1 - weight) * v[index] + weight * v[index + 1];
+}
+
+}  // namespace xg

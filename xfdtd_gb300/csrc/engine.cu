@@ -1,0 +1,917 @@
+// engine.cu -- C-ABI of the GB300 FDTD engine (include/xfdtd_cuda.h).
+//
+// One handle = one simulation = one CUDA stream.  xfdtd_create validates the
+// plan on the host, allocates every device buffer once and uploads the
+// tables; xfdtd_step enqueues the per-step kernel sequence
+//
+//   k_tfsf_aux (1 block)  -> k_update_e (Yee E + TFSF E + CPML E)
+//   -> k_lumped_e (sparse) -> k_update_h (Yee H + TFSF H + CPML H)
+//   -> k_nffft (surface)  -> k_probes -> k_advance
+//
+// which is the order of the reference's loop body
+// (src/simulation/simulation_update.cpp:13-35).  The step index lives on the
+// device (k_advance bumps it), so a captured CUDA graph of G steps replays
+// for any starting step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/xfdtd_cuda.h"
+#include "common.cuh"
+#include "surface.cuh"
+#include "volume.cuh"
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kEps0 = 8.854187817e-12;
+constexpr double kMu0 = 4 * kPi * 1e-7;
+
+struct Err {
+  int code;
+  std::string msg;
+};
+
+#define XCHECK(call)                                                                    \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      throw Err{e_ == cudaErrorMemoryAllocation ? XFDTD_ERR_OOM : XFDTD_ERR_CUDA,       \
+                std::string(#call) + ": " + cudaGetErrorString(e_)};                    \
+  } while (0)
+
+const char *kKernelNames[] = {"tfsf_aux", "update_e", "lumped_e", "update_h", "nffft", "probes", "advance"};
+constexpr int kNumKernels = 7;
+
+}  // namespace
+
+struct xfdtd_handle {
+  std::string err;
+  int precision = XFDTD_FP64;
+  int idx_bytes = 1;
+  int flags = 0;
+  xg::Dims d{};
+  long long total = 0;
+  long long host_step = 0;   // steps enqueued so far
+  size_t esize = 8;
+  double dl[3] = {0, 0, 0};
+  double dt = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<void *> allocs;
+  size_t bytes = 0;
+
+  void *F[6] = {};
+  void *idx = nullptr;
+  void *table = nullptr;
+  int n_mat = 0;
+  bool smem_table = false;
+  size_t smem_bytes = 0;
+
+  // CPML
+  int L[3] = {0, 0, 0};
+  int *slot_e[3] = {}, *slot_h[3] = {};
+  void *prof[3][6] = {};   // b_e a_e rk_e b_m a_m rk_m (precision T)
+  void *psi[12] = {};      // ex_y ex_z ey_x ey_z ez_x ez_y hx_y hx_z hy_x hy_z hz_x hz_y
+
+  // TFSF
+  bool tfsf = false;
+  int aux_len = 0;
+  int tf_lo[3] = {}, tf_hi[3] = {};
+  double *tf_pf[3] = {}, *tf_ph[3] = {};
+  double *tf_state = nullptr, *tf_inc = nullptr, *tf_src = nullptr;
+  double tf_ca[3] = {}, tf_cb[3] = {}, tf_te[3] = {}, tf_th[3] = {};
+  double tf_ceihi = 0, tf_chiei = 0, tf_c1 = 0, tf_c2 = 0;
+
+  // NF-FF
+  bool nffft = false;
+  int nf = 0, nt = 0, np = 0;
+  int nf_lo[3] = {}, nf_hi[3] = {};
+  double2 *acc[24] = {};
+  long long acc_len[24] = {};
+  double2 *phase_j = nullptr, *phase_m = nullptr;
+  double *ff_theta = nullptr, *ff_phi = nullptr, *ff_k = nullptr;
+  double2 *ff_out[8] = {};
+  double *ff_power[2] = {};
+  long long ff_step = -1;
+
+  // sparse
+  int n_inj = 0, n_ind = 0, n_probes = 0, n_waveforms = 0;
+  xfdtd_injection *inj = nullptr;
+  xfdtd_inductor_cell *ind = nullptr;
+  double *ind_j = nullptr;
+  double *waveforms = nullptr;
+  xfdtd_probe_term *terms = nullptr;
+  int *probe_off = nullptr;
+  double *probe_out = nullptr;
+
+  long long *d_step = nullptr;
+  int *d_status = nullptr;
+  int *d_flag = nullptr;
+
+  // graph replay
+  cudaGraphExec_t gexec = nullptr;
+  int graph_steps = 0;
+
+  // profiling
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, int>> ev_pending;   // (kernel id, event index of start)
+  double prof_ms[kNumKernels] = {};
+  long long prof_n[kNumKernels] = {};
+
+  template <class P>
+  P *alloc(size_t count) {
+    void *p = nullptr;
+    size_t nb = std::max<size_t>(count * sizeof(P), 16);
+    XCHECK(cudaMalloc(&p, nb));
+    allocs.push_back(p);
+    bytes += nb;
+    XCHECK(cudaMemsetAsync(p, 0, nb, stream));
+    return static_cast<P *>(p);
+  }
+  void *alloc_bytes(size_t nb) {
+    void *p = nullptr;
+    nb = std::max<size_t>(nb, 16);
+    XCHECK(cudaMalloc(&p, nb));
+    allocs.push_back(p);
+    bytes += nb;
+    XCHECK(cudaMemsetAsync(p, 0, nb, stream));
+    return p;
+  }
+  template <class P>
+  P *upload(const P *src, size_t count) {
+    P *p = alloc<P>(count);
+    if (count) XCHECK(cudaMemcpyAsync(p, src, count * sizeof(P), cudaMemcpyHostToDevice, stream));
+    return p;
+  }
+  // upload doubles, converting to the field precision
+  void *upload_real(const double *src, size_t count) {
+    if (precision == XFDTD_FP64) return upload<double>(src, count);
+    std::vector<float> tmp(count);
+    for (size_t q = 0; q < count; ++q) tmp[q] = static_cast<float>(src[q]);
+    return upload<float>(tmp.data(), count);
+  }
+  ~xfdtd_handle() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    for (auto e : ev_pool) cudaEventDestroy(e);
+    for (void *p : allocs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+template <class F>
+int guarded(xfdtd_handle *h, F &&fn) {
+  try {
+    fn();
+    return XFDTD_OK;
+  } catch (const Err &e) {
+    if (h) h->err = e.msg;
+    return e.code;
+  } catch (const std::exception &e) {
+    if (h) h->err = e.what();
+    return XFDTD_ERR_INVALID_PLAN;
+  }
+}
+
+void invalid(const std::string &m) { throw Err{XFDTD_ERR_INVALID_PLAN, m}; }
+
+// ------------------------------------------------------------ launches ---
+void prof_begin(xfdtd_handle *h, int id) {
+  if (!(h->flags & XFDTD_FLAG_PROFILE)) return;
+  size_t need = h->ev_pending.size() * 2 + 2;
+  while (h->ev_pool.size() < need) {
+    cudaEvent_t e;
+    XCHECK(cudaEventCreate(&e));
+    h->ev_pool.push_back(e);
+  }
+  int s = static_cast<int>(h->ev_pending.size() * 2);
+  XCHECK(cudaEventRecord(h->ev_pool[s], h->stream));
+  h->ev_pending.push_back({id, s});
+}
+void prof_end(xfdtd_handle *h) {
+  if (!(h->flags & XFDTD_FLAG_PROFILE)) return;
+  int s = h->ev_pending.back().second;
+  XCHECK(cudaEventRecord(h->ev_pool[s + 1], h->stream));
+}
+void prof_collect(xfdtd_handle *h) {
+  if (h->ev_pending.empty()) return;
+  XCHECK(cudaStreamSynchronize(h->stream));
+  for (auto &pr : h->ev_pending) {
+    float ms = 0;
+    XCHECK(cudaEventElapsedTime(&ms, h->ev_pool[pr.second], h->ev_pool[pr.second + 1]));
+    h->prof_ms[pr.first] += ms;
+    h->prof_n[pr.first] += 1;
+  }
+  h->ev_pending.clear();
+}
+
+template <typename T, typename I>
+xg::VolParams<T, I> vol_params(xfdtd_handle *h) {
+  xg::VolParams<T, I> p{};
+  p.d = h->d;
+  for (int c = 0; c < 3; ++c) {
+    p.E[c] = static_cast<T *>(h->F[c]);
+    p.H[c] = static_cast<T *>(h->F[3 + c]);
+  }
+  p.idx = static_cast<const I *>(h->idx);
+  p.table = static_cast<const T *>(h->table);
+  p.n_mat = h->n_mat;
+  for (int a = 0; a < 3; ++a) {
+    p.cp[a].n_layers = h->L[a];
+    p.cp[a].slot_e = h->slot_e[a];
+    p.cp[a].slot_h = h->slot_h[a];
+    p.cp[a].b_e = static_cast<const T *>(h->prof[a][0]);
+    p.cp[a].a_e = static_cast<const T *>(h->prof[a][1]);
+    p.cp[a].rk_e = static_cast<const T *>(h->prof[a][2]);
+    p.cp[a].b_m = static_cast<const T *>(h->prof[a][3]);
+    p.cp[a].a_m = static_cast<const T *>(h->prof[a][4]);
+    p.cp[a].rk_m = static_cast<const T *>(h->prof[a][5]);
+    p.dl[a] = static_cast<T>(h->dl[a]);
+  }
+  T **ps = reinterpret_cast<T **>(&p.psi);
+  for (int q = 0; q < 12; ++q) ps[q] = static_cast<T *>(h->psi[q]);
+  p.tf.enabled = h->tfsf ? 1 : 0;
+  p.tf.L = h->aux_len;
+  for (int a = 0; a < 3; ++a) {
+    p.tf.lo[a] = h->tf_lo[a];
+    p.tf.hi[a] = h->tf_hi[a];
+    p.tf.pf[a] = h->tf_pf[a];
+    p.tf.ph[a] = h->tf_ph[a];
+    p.tf.ca[a] = h->tf_ca[a];
+    p.tf.cb[a] = h->tf_cb[a];
+  }
+  p.tf.inc = h->tf_inc;
+  p.step = h->d_step;
+  return p;
+}
+
+constexpr int kBlockX = 32, kBlockY = 8;
+
+int chunk_planes(const xfdtd_handle *h) {
+  // Enough (j,k) columns x i-chunks to keep >= 4 blocks per SM resident.
+  long long cols = static_cast<long long>((h->d.nz + kBlockX) / kBlockX) * ((h->d.ny + kBlockY) / kBlockY);
+  long long target_blocks = 152LL * 8;
+  long long nchunks = std::max<long long>(1, (target_blocks + cols - 1) / cols);
+  int chunk = static_cast<int>((h->d.nx + 1 + nchunks - 1) / nchunks);
+  return std::max(chunk, 8);
+}
+
+template <typename T, typename I>
+void launch_volume(xfdtd_handle *h, bool e_side) {
+  auto p = vol_params<T, I>(h);
+  p.chunk = chunk_planes(h);
+  dim3 block(kBlockX, kBlockY, 1);
+  dim3 grid((h->d.nz + kBlockX) / kBlockX, (h->d.ny + kBlockY) / kBlockY, (h->d.nx + 1 + p.chunk - 1) / p.chunk);
+  if (h->smem_table) {
+    if (e_side) xg::k_update_e<T, I, true><<<grid, block, h->smem_bytes, h->stream>>>(p);
+    else xg::k_update_h<T, I, true><<<grid, block, h->smem_bytes, h->stream>>>(p);
+  } else {
+    if (e_side) xg::k_update_e<T, I, false><<<grid, block, 0, h->stream>>>(p);
+    else xg::k_update_h<T, I, false><<<grid, block, 0, h->stream>>>(p);
+  }
+  XCHECK(cudaGetLastError());
+}
+
+template <typename T>
+xg::SparseParams<T> sparse_params(xfdtd_handle *h) {
+  xg::SparseParams<T> p{};
+  p.d = h->d;
+  for (int c = 0; c < 6; ++c) p.F[c] = static_cast<T *>(h->F[c]);
+  p.inj = h->inj;
+  p.n_inj = h->n_inj;
+  p.waveforms = h->waveforms;
+  p.ind = h->ind;
+  p.ind_j = h->ind_j;
+  p.n_ind = h->n_ind;
+  p.terms = h->terms;
+  p.probe_off = h->probe_off;
+  p.n_probes = h->n_probes;
+  p.probe_out = h->probe_out;
+  p.total = h->total;
+  p.step = h->d_step;
+  return p;
+}
+
+template <typename T>
+void launch_nffft(xfdtd_handle *h) {
+  xg::NfParams<T> p{};
+  p.d = h->d;
+  for (int c = 0; c < 3; ++c) {
+    p.E[c] = static_cast<const T *>(h->F[c]);
+    p.H[c] = static_cast<const T *>(h->F[3 + c]);
+  }
+  for (int a = 0; a < 3; ++a) {
+    p.lo[a] = h->nf_lo[a];
+    p.hi[a] = h->nf_hi[a];
+  }
+  p.nf = h->nf;
+  for (int q = 0; q < 24; ++q) p.acc[q] = h->acc[q];
+  p.pj = h->phase_j;
+  p.pm = h->phase_m;
+  p.total = h->total;
+  p.step = h->d_step;
+  int bx = h->nf_hi[0] - h->nf_lo[0], by = h->nf_hi[1] - h->nf_lo[1], bz = h->nf_hi[2] - h->nf_lo[2];
+  int u = std::max(bz, by), v = std::max(by, bx);
+  dim3 block(32, 8, 1);
+  dim3 grid((u + 31) / 32, (v + 7) / 8, 3);
+  xg::k_nffft<T><<<grid, block, 0, h->stream>>>(p);
+  XCHECK(cudaGetLastError());
+}
+
+template <typename T, typename I>
+void enqueue_step_t(xfdtd_handle *h) {
+  if (h->tfsf) {
+    xg::AuxParams a{};
+    a.L = h->aux_len;
+    a.state = h->tf_state;
+    a.inc = h->tf_inc;
+    a.source = h->tf_src;
+    a.ceihi = h->tf_ceihi;
+    a.chiei = h->tf_chiei;
+    a.c1 = h->tf_c1;
+    a.c2 = h->tf_c2;
+    for (int q = 0; q < 3; ++q) { a.te[q] = h->tf_te[q]; a.th[q] = h->tf_th[q]; }
+    a.step = h->d_step;
+    a.total = h->total;
+    a.status = h->d_status;
+    prof_begin(h, 0);
+    xg::k_tfsf_aux<<<1, 512, 0, h->stream>>>(a);
+    XCHECK(cudaGetLastError());
+    prof_end(h);
+  }
+  prof_begin(h, 1);
+  launch_volume<T, I>(h, true);
+  prof_end(h);
+  if (h->n_inj || h->n_ind) {
+    auto sp = sparse_params<T>(h);
+    int n = std::max(h->n_inj, h->n_ind);
+    prof_begin(h, 2);
+    xg::k_lumped_e<T><<<(n + 127) / 128, 128, 0, h->stream>>>(sp);
+    XCHECK(cudaGetLastError());
+    prof_end(h);
+  }
+  prof_begin(h, 3);
+  launch_volume<T, I>(h, false);
+  prof_end(h);
+  if (h->nffft) {
+    prof_begin(h, 4);
+    launch_nffft<T>(h);
+    prof_end(h);
+  }
+  if (h->n_probes) {
+    auto sp = sparse_params<T>(h);
+    prof_begin(h, 5);
+    xg::k_probes<T><<<(h->n_probes + 127) / 128, 128, 0, h->stream>>>(sp);
+    XCHECK(cudaGetLastError());
+    prof_end(h);
+  }
+  prof_begin(h, 6);
+  xg::k_advance<<<1, 1, 0, h->stream>>>(h->d_step);
+  XCHECK(cudaGetLastError());
+  prof_end(h);
+}
+
+void enqueue_step(xfdtd_handle *h) {
+  if (h->precision == XFDTD_FP64) {
+    if (h->idx_bytes == 1) enqueue_step_t<double, uint8_t>(h);
+    else enqueue_step_t<double, uint16_t>(h);
+  } else {
+    if (h->idx_bytes == 1) enqueue_step_t<float, uint8_t>(h);
+    else enqueue_step_t<float, uint16_t>(h);
+  }
+}
+
+int launches_per_step(const xfdtd_handle *h) {
+  return (h->tfsf ? 1 : 0) + 2 + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
+}
+
+void build_graph(xfdtd_handle *h, int g) {
+  cudaGraph_t graph;
+  XCHECK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  for (int s = 0; s < g; ++s) enqueue_step(h);
+  XCHECK(cudaStreamEndCapture(h->stream, &graph));
+  cudaError_t e = cudaGraphInstantiate(&h->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  XCHECK(e);
+  h->graph_steps = g;
+}
+
+void check_status(xfdtd_handle *h) {
+  int st = 0;
+  XCHECK(cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  XCHECK(cudaStreamSynchronize(h->stream));
+  if (st != 0) throw Err{XFDTD_ERR_DEVICE_CHECK, "device status " + std::to_string(st) + " (step index past the plan)"};
+}
+
+// component shapes of the reference (simulation_init.cpp:28-35)
+void comp_shape(const xfdtd_handle *h, int c, long long s[3]) {
+  long long nx = h->d.nx, ny = h->d.ny, nz = h->d.nz;
+  const long long t[6][3] = {{nx, ny + 1, nz + 1}, {nx + 1, ny, nz + 1}, {nx + 1, ny + 1, nz},
+                             {nx + 1, ny, nz},     {nx, ny + 1, nz},     {nx, ny, nz + 1}};
+  for (int a = 0; a < 3; ++a) s[a] = t[c][a];
+}
+
+// ----------------------------------------------------------- creation ---
+void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
+  if (pl->nx < 2 || pl->ny < 2 || pl->nz < 2) invalid("grid must have at least 2 cells per axis");
+  if (pl->precision != XFDTD_FP64 && pl->precision != XFDTD_FP32) invalid("precision must be FP64 or FP32");
+  if (pl->index_bytes != 1 && pl->index_bytes != 2) invalid("index_bytes must be 1 or 2");
+  if (pl->n_materials < 1 || pl->n_materials > (pl->index_bytes == 1 ? 256 : 65536))
+    invalid("material count does not fit the index width");
+  if (!pl->material_index || !pl->coeff_table) invalid("material index and coefficient table are required");
+  if (pl->total_steps < 1) invalid("total_steps must be positive");
+  if (!(pl->dt > 0)) invalid("dt must be positive");
+  h->precision = pl->precision;
+  h->idx_bytes = pl->index_bytes;
+  h->flags = pl->flags;
+  h->esize = pl->precision == XFDTD_FP64 ? 8 : 4;
+  h->total = pl->total_steps;
+  h->dt = pl->dt;
+  for (int a = 0; a < 3; ++a) h->dl[a] = pl->dl[a];
+  xg::Dims &d = h->d;
+  d.nx = pl->nx;
+  d.ny = pl->ny;
+  d.nz = pl->nz;
+  d.nzp = ((pl->nz + 1) + 31) / 32 * 32;
+  d.sj = d.nzp;
+  d.si = static_cast<long long>(pl->ny + 1) * d.nzp;
+  d.cells = static_cast<long long>(pl->nx + 1) * d.si;
+  const long long NX1 = pl->nx + 1, NY1 = pl->ny + 1, NZ1 = pl->nz + 1;
+
+  XCHECK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  for (int c = 0; c < 6; ++c) h->F[c] = h->alloc_bytes(d.cells * h->esize);
+
+  // material index, repacked into the padded layout
+  {
+    std::vector<uint8_t> buf(d.cells * pl->index_bytes, 0);
+    const uint8_t *src = static_cast<const uint8_t *>(pl->material_index);
+    for (long long i = 0; i < NX1; ++i)
+      for (long long j = 0; j < NY1; ++j) {
+        const uint8_t *row = src + ((i * NY1 + j) * NZ1) * pl->index_bytes;
+        if (pl->index_bytes == 2) {
+          const uint16_t *r16 = reinterpret_cast<const uint16_t *>(row);
+          for (long long k = 0; k < NZ1; ++k)
+            if (r16[k] >= pl->n_materials) invalid("material index out of range");
+        } else {
+          for (long long k = 0; k < NZ1; ++k)
+            if (row[k] >= pl->n_materials) invalid("material index out of range");
+        }
+        std::memcpy(buf.data() + (i * d.si + j * d.sj) * pl->index_bytes, row, NZ1 * pl->index_bytes);
+      }
+    h->idx = h->upload<uint8_t>(buf.data(), buf.size());
+  }
+  h->n_mat = pl->n_materials;
+  h->table = h->upload_real(pl->coeff_table, static_cast<size_t>(pl->n_materials) * XFDTD_N_COEFF);
+  h->smem_bytes = static_cast<size_t>(pl->n_materials) * 9 * h->esize;
+  h->smem_table = h->smem_bytes <= 96 * 1024;
+  if (h->smem_table && h->smem_bytes > 48 * 1024) {
+    // opt in to more than 48 KB of dynamic shared memory for the table
+    int bytes = static_cast<int>(h->smem_bytes);
+    if (h->precision == XFDTD_FP64) {
+      XCHECK(cudaFuncSetAttribute(xg::k_update_e<double, uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+      XCHECK(cudaFuncSetAttribute(xg::k_update_h<double, uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+      XCHECK(cudaFuncSetAttribute(xg::k_update_e<double, uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+      XCHECK(cudaFuncSetAttribute(xg::k_update_h<double, uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    } else {
+      XCHECK(cudaFuncSetAttribute(xg::k_update_e<float, uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+      XCHECK(cudaFuncSetAttribute(xg::k_update_h<float, uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+      XCHECK(cudaFuncSetAttribute(xg::k_update_e<float, uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+      XCHECK(cudaFuncSetAttribute(xg::k_update_h<float, uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    }
+  }
+
+  // CPML profiles
+  const int n_axis[3] = {pl->nx, pl->ny, pl->nz};
+  for (int a = 0; a < 3; ++a) {
+    const xfdtd_cpml_axis &ca = pl->cpml[a];
+    if (ca.n_layers < 0) invalid("negative CPML layer count");
+    h->L[a] = ca.n_layers;
+    if (ca.n_layers == 0) continue;
+    const int n1 = n_axis[a] + 1;
+    if (!ca.slot_e || !ca.slot_h || !ca.b_e || !ca.a_e || !ca.rk_e || !ca.b_m || !ca.a_m || !ca.rk_m)
+      invalid("CPML axis is missing a profile array");
+    for (int q = 0; q < n1; ++q) {
+      if (ca.slot_e[q] >= ca.n_layers || ca.slot_h[q] >= ca.n_layers) invalid("CPML slot out of range");
+      if (ca.slot_e[q] >= 0 && (q < 1 || q > n_axis[a] - 1)) invalid("CPML E slot on an outer wall");
+      if (ca.slot_h[q] >= 0 && q > n_axis[a] - 1) invalid("CPML H slot on the last index");
+    }
+    h->slot_e[a] = h->upload<int>(ca.slot_e, n1);
+    h->slot_h[a] = h->upload<int>(ca.slot_h, n1);
+    const double *src[6] = {ca.b_e, ca.a_e, ca.rk_e, ca.b_m, ca.a_m, ca.rk_m};
+    for (int q = 0; q < 6; ++q) h->prof[a][q] = h->upload_real(src[q], n1);
+  }
+  // psi arrays: axis X (L, ny+1, nzp), Y (nx+1, L, nzp), Z (nx+1, ny+1, L)
+  {
+    const size_t sx = static_cast<size_t>(h->L[0]) * NY1 * d.nzp;
+    const size_t sy = static_cast<size_t>(NX1) * h->L[1] * d.nzp;
+    const size_t sz = static_cast<size_t>(NX1) * NY1 * h->L[2];
+    // order: ex_y ex_z ey_x ey_z ez_x ez_y hx_y hx_z hy_x hy_z hz_x hz_y
+    const size_t sizes[12] = {sy, sz, sx, sz, sx, sy, sy, sz, sx, sz, sx, sy};
+    for (int q = 0; q < 12; ++q) h->psi[q] = sizes[q] ? h->alloc_bytes(sizes[q] * h->esize) : nullptr;
+  }
+
+  // TFSF
+  const xfdtd_tfsf_plan &tp = pl->tfsf;
+  if (tp.enabled) {
+    h->tfsf = true;
+    if (tp.aux_len < 6) invalid("TFSF auxiliary grid too short");
+    h->aux_len = tp.aux_len;
+    for (int a = 0; a < 3; ++a) {
+      if (tp.lo[a] < 1 || tp.hi[a] <= tp.lo[a] || tp.hi[a] > n_axis[a] - 1) invalid("TFSF box outside the grid");
+      h->tf_lo[a] = static_cast<int>(tp.lo[a]);
+      h->tf_hi[a] = static_cast<int>(tp.hi[a]);
+      const long long bn = tp.hi[a] - tp.lo[a];
+      if (!tp.proj_full[a] || !tp.proj_half[a]) invalid("TFSF projection tables are required");
+      h->tf_pf[a] = h->upload<double>(tp.proj_full[a], bn + 1);
+      h->tf_ph[a] = h->upload<double>(tp.proj_half[a], bn + 2);
+      h->tf_ca[a] = tp.ca[a];
+      h->tf_cb[a] = tp.cb[a];
+      h->tf_te[a] = tp.transform_e[a];
+      h->tf_th[a] = tp.transform_h[a];
+    }
+    // Every interpolation index (a sum of one entry per axis, minus 0.5 for
+    // H) must stay inside the 1-D arrays: e_inc has L entries, h_inc L-1.
+    double lo_sum = 0, hi_sum = 0;
+    for (int a = 0; a < 3; ++a) {
+      const long long bn = tp.hi[a] - tp.lo[a];
+      double mn = tp.proj_full[a][0], mx = mn;
+      for (long long q = 0; q < bn + 1; ++q) { mn = std::min(mn, tp.proj_full[a][q]); mx = std::max(mx, tp.proj_full[a][q]); }
+      for (long long q = 0; q < bn + 2; ++q) { mn = std::min(mn, tp.proj_half[a][q]); mx = std::max(mx, tp.proj_half[a][q]); }
+      if (!std::isfinite(mn) || !std::isfinite(mx)) invalid("TFSF projection is not finite");
+      lo_sum += mn;
+      hi_sum += mx;
+    }
+    if (lo_sum - 0.5 < 0 || std::floor(hi_sum) + 1 > tp.aux_len - 2) invalid("TFSF box does not fit the auxiliary grid");
+    h->tf_ceihi = tp.ceihi;
+    h->tf_chiei = tp.chiei;
+    h->tf_c1 = tp.mur_c1;
+    h->tf_c2 = tp.mur_c2;
+    if (!tp.source) invalid("TFSF source samples are required");
+    h->tf_src = h->upload<double>(tp.source, pl->total_steps);
+    h->tf_state = h->alloc<double>(2 * static_cast<size_t>(tp.aux_len) + 1);
+    h->tf_inc = h->alloc<double>(2 * 6 * static_cast<size_t>(tp.aux_len));
+  }
+
+  // NF-FF
+  const xfdtd_nffft_plan &np = pl->nffft;
+  if (np.enabled) {
+    h->nffft = true;
+    if (np.n_freq < 1) invalid("NF-FF needs at least one frequency");
+    h->nf = np.n_freq;
+    h->nt = np.n_theta;
+    h->np = np.n_phi;
+    for (int a = 0; a < 3; ++a) {
+      if (np.lo[a] < 1 || np.hi[a] <= np.lo[a] || np.hi[a] > n_axis[a] - 1) invalid("NF-FF box outside the grid");
+      h->nf_lo[a] = static_cast<int>(np.lo[a]);
+      h->nf_hi[a] = static_cast<int>(np.hi[a]);
+    }
+    const long long bx = np.hi[0] - np.lo[0], by = np.hi[1] - np.lo[1], bz = np.hi[2] - np.lo[2];
+    const long long face[3] = {by * bz, bz * bx, bx * by};
+    for (int q = 0; q < 24; ++q) {
+      h->acc_len[q] = np.n_freq * face[q / 8];
+      h->acc[q] = h->alloc<double2>(h->acc_len[q]);
+    }
+    if (!np.phase_j || !np.phase_m || !np.wave_number) invalid("NF-FF phase tables are required");
+    h->phase_j = h->upload<double2>(reinterpret_cast<const double2 *>(np.phase_j), np.n_freq * pl->total_steps);
+    h->phase_m = h->upload<double2>(reinterpret_cast<const double2 *>(np.phase_m), np.n_freq * pl->total_steps);
+    h->ff_k = h->upload<double>(np.wave_number, np.n_freq);
+    if (np.n_theta > 0 && np.n_phi > 0) {
+      h->ff_theta = h->upload<double>(np.theta, np.n_theta);
+      h->ff_phi = h->upload<double>(np.phi, np.n_phi);
+      const size_t dirs = static_cast<size_t>(np.n_freq) * np.n_theta * np.n_phi;
+      for (int q = 0; q < 8; ++q) h->ff_out[q] = h->alloc<double2>(dirs);
+      for (int q = 0; q < 2; ++q) h->ff_power[q] = h->alloc<double>(dirs);
+    }
+  }
+
+  // sparse work
+  h->n_waveforms = pl->n_waveforms;
+  if (pl->n_waveforms) h->waveforms = h->upload<double>(pl->waveforms, static_cast<size_t>(pl->n_waveforms) * pl->total_steps);
+  auto check_cell = [&](int comp, long long i, long long j, long long k) {
+    if (comp < 0 || comp > 5) invalid("bad field component in a sparse entry");
+    long long s[3];
+    comp_shape(h, comp, s);
+    if (i < 0 || j < 0 || k < 0 || i >= s[0] || j >= s[1] || k >= s[2]) invalid("sparse entry outside its component");
+  };
+  h->n_inj = pl->n_injections;
+  if (pl->n_injections) {
+    for (int q = 0; q < pl->n_injections; ++q) {
+      const auto &c = pl->injections[q];
+      check_cell(c.comp, c.i, c.j, c.k);
+      if (c.comp > 2) invalid("injections act on E components");
+      if (c.waveform < 0 || c.waveform >= pl->n_waveforms) invalid("injection waveform out of range");
+    }
+    h->inj = h->upload<xfdtd_injection>(pl->injections, pl->n_injections);
+  }
+  h->n_ind = pl->n_inductor_cells;
+  if (pl->n_inductor_cells) {
+    for (int q = 0; q < pl->n_inductor_cells; ++q) {
+      const auto &c = pl->inductor_cells[q];
+      check_cell(c.comp, c.i, c.j, c.k);
+      if (c.comp > 2) invalid("inductors act on E components");
+    }
+    h->ind = h->upload<xfdtd_inductor_cell>(pl->inductor_cells, pl->n_inductor_cells);
+    h->ind_j = h->alloc<double>(pl->n_inductor_cells);
+  }
+  h->n_probes = pl->n_probes;
+  if (pl->n_probes) {
+    std::vector<int> off(pl->n_probes + 1, 0);
+    int last = -1;
+    for (int q = 0; q < pl->n_probe_terms; ++q) {
+      const auto &c = pl->probe_terms[q];
+      check_cell(c.comp, c.i, c.j, c.k);
+      if (c.probe < last || c.probe >= pl->n_probes) invalid("probe terms must be grouped by probe in order");
+      last = c.probe;
+      off[c.probe + 1] += 1;
+    }
+    for (int q = 0; q < pl->n_probes; ++q) off[q + 1] += off[q];
+    h->terms = h->upload<xfdtd_probe_term>(pl->probe_terms, std::max(1, pl->n_probe_terms));
+    h->probe_off = h->upload<int>(off.data(), off.size());
+    h->probe_out = h->alloc<double>(static_cast<size_t>(pl->n_probes) * pl->total_steps);
+  }
+
+  h->d_step = h->alloc<long long>(1);
+  h->d_status = h->alloc<int>(1);
+  h->d_flag = h->alloc<int>(1);
+  XCHECK(cudaStreamSynchronize(h->stream));
+}
+
+template <typename T>
+void read_comp(xfdtd_handle *h, int comp, double *out, long long len) {
+  long long s[3];
+  comp_shape(h, comp, s);
+  if (len != s[0] * s[1] * s[2]) invalid("length does not match the component shape");
+  std::vector<T> buf(h->d.cells);
+  XCHECK(cudaMemcpyAsync(buf.data(), h->F[comp], h->d.cells * sizeof(T), cudaMemcpyDeviceToHost, h->stream));
+  XCHECK(cudaStreamSynchronize(h->stream));
+  long long o = 0;
+  for (long long i = 0; i < s[0]; ++i)
+    for (long long j = 0; j < s[1]; ++j)
+      for (long long k = 0; k < s[2]; ++k) out[o++] = static_cast<double>(buf[i * h->d.si + j * h->d.sj + k]);
+}
+
+template <typename T>
+void write_comp(xfdtd_handle *h, int comp, const double *in, long long len) {
+  long long s[3];
+  comp_shape(h, comp, s);
+  if (len != s[0] * s[1] * s[2]) invalid("length does not match the component shape");
+  std::vector<T> buf(h->d.cells, T(0));
+  long long o = 0;
+  for (long long i = 0; i < s[0]; ++i)
+    for (long long j = 0; j < s[1]; ++j)
+      for (long long k = 0; k < s[2]; ++k) buf[i * h->d.si + j * h->d.sj + k] = static_cast<T>(in[o++]);
+  XCHECK(cudaMemcpyAsync(h->F[comp], buf.data(), h->d.cells * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+  XCHECK(cudaStreamSynchronize(h->stream));
+}
+
+void run_far_field(xfdtd_handle *h) {
+  if (!h->nffft) throw Err{XFDTD_ERR_STATE, "the plan has no NF-FF box"};
+  if (!h->ff_theta) throw Err{XFDTD_ERR_STATE, "the plan has no far-field directions"};
+  if (h->ff_step == h->host_step) return;
+  xg::FarParams p{};
+  for (int a = 0; a < 3; ++a) {
+    p.lo[a] = h->nf_lo[a];
+    p.hi[a] = h->nf_hi[a];
+    p.dl[a] = h->dl[a];
+  }
+  p.nf = h->nf;
+  p.nt = h->nt;
+  p.np = h->np;
+  for (int q = 0; q < 24; ++q) p.acc[q] = h->acc[q];
+  p.theta = h->ff_theta;
+  p.phi = h->ff_phi;
+  p.k = h->ff_k;
+  p.eta0 = std::sqrt(kMu0 / kEps0);
+  p.pi = kPi;
+  for (int q = 0; q < 8; ++q) p.out[q] = h->ff_out[q];
+  for (int q = 0; q < 2; ++q) p.power[q] = h->ff_power[q];
+  xg::k_far_field<<<h->nf * h->nt * h->np, 256, 0, h->stream>>>(p);
+  XCHECK(cudaGetLastError());
+  XCHECK(cudaStreamSynchronize(h->stream));
+  h->ff_step = h->host_step;
+}
+
+void do_steps(xfdtd_handle *h, long long n) {
+  if (n < 0) invalid("negative step count");
+  if (h->host_step + n > h->total) throw Err{XFDTD_ERR_STATE, "stepping past the plan's total_steps"};
+  const bool graph = (h->flags & XFDTD_FLAG_GRAPH) && !(h->flags & XFDTD_FLAG_PROFILE);
+  long long left = n;
+  if (graph && n >= 2) {
+    if (!h->gexec) build_graph(h, static_cast<int>(std::min<long long>(n, 64)));
+    while (left >= h->graph_steps) {
+      XCHECK(cudaGraphLaunch(h->gexec, h->stream));
+      left -= h->graph_steps;
+    }
+  }
+  for (long long s = 0; s < left; ++s) enqueue_step(h);
+  h->host_step += n;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *xfdtd_version(void) { return "xfdtd_gb300 engine 0.1 (sm_103a)"; }
+
+int xfdtd_create(const xfdtd_plan_desc *plan, xfdtd_handle **out) {
+  if (!plan || !out) return XFDTD_ERR_INVALID_PLAN;
+  std::unique_ptr<xfdtd_handle> h(new xfdtd_handle());
+  int rc = guarded(h.get(), [&] { create(plan, h.get()); });
+  if (rc != XFDTD_OK) {
+    // keep the handle so that the caller can read the message; it holds no work
+    *out = h.release();
+    return rc;
+  }
+  *out = h.release();
+  return XFDTD_OK;
+}
+
+int xfdtd_step(xfdtd_handle *h, int64_t n) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    do_steps(h, n);
+    prof_collect(h);
+  });
+}
+
+int xfdtd_synchronize(xfdtd_handle *h) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    XCHECK(cudaStreamSynchronize(h->stream));
+    check_status(h);
+  });
+}
+
+int xfdtd_step_timed(xfdtd_handle *h, int64_t n, double *ms) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    cudaEvent_t a, b;
+    XCHECK(cudaEventCreate(&a));
+    XCHECK(cudaEventCreate(&b));
+    XCHECK(cudaEventRecord(a, h->stream));
+    do_steps(h, n);
+    XCHECK(cudaEventRecord(b, h->stream));
+    XCHECK(cudaEventSynchronize(b));
+    float f = 0;
+    XCHECK(cudaEventElapsedTime(&f, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    prof_collect(h);
+    if (ms) *ms = f;
+  });
+}
+
+int xfdtd_current_step(xfdtd_handle *h, int64_t *step) {
+  if (!h || !step) return XFDTD_ERR_STATE;
+  *step = h->host_step;
+  return XFDTD_OK;
+}
+
+int xfdtd_read_field(xfdtd_handle *h, int comp, double *out, int64_t len) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    if (comp < 0 || comp > 5) invalid("component must be 0..5");
+    if (h->precision == XFDTD_FP64) read_comp<double>(h, comp, out, len);
+    else read_comp<float>(h, comp, out, len);
+  });
+}
+
+int xfdtd_write_field(xfdtd_handle *h, int comp, const double *in, int64_t len) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    if (comp < 0 || comp > 5) invalid("component must be 0..5");
+    if (h->precision == XFDTD_FP64) write_comp<double>(h, comp, in, len);
+    else write_comp<float>(h, comp, in, len);
+  });
+}
+
+int xfdtd_read_probes(xfdtd_handle *h, double *out, int64_t len) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    if (len != static_cast<int64_t>(h->n_probes) * h->total) invalid("length must be n_probes * total_steps");
+    if (!len) return;
+    XCHECK(cudaMemcpyAsync(out, h->probe_out, len * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    XCHECK(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int xfdtd_read_nffft(xfdtd_handle *h, int which, double *out, int64_t len) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    if (!h->nffft) throw Err{XFDTD_ERR_STATE, "the plan has no NF-FF box"};
+    if (which < 0 || which >= 24) invalid("accumulator index must be 0..23");
+    if (len != 2 * h->acc_len[which]) invalid("length must be 2 * n_freq * face cells");
+    std::vector<double2> buf(h->acc_len[which]);
+    XCHECK(cudaMemcpyAsync(buf.data(), h->acc[which], buf.size() * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    XCHECK(cudaStreamSynchronize(h->stream));
+    if (which / 8 == 1) {  // Y faces: device [n][i][k] -> reference [n][k][i]
+      const long long bx = h->nf_hi[0] - h->nf_lo[0], bz = h->nf_hi[2] - h->nf_lo[2];
+      for (long long n = 0; n < h->nf; ++n)
+        for (long long i = 0; i < bx; ++i)
+          for (long long k = 0; k < bz; ++k) {
+            const double2 v = buf[(n * bx + i) * bz + k];
+            const long long o = (n * bz + k) * bx + i;
+            out[2 * o] = v.x;
+            out[2 * o + 1] = v.y;
+          }
+    } else {
+      for (size_t q = 0; q < buf.size(); ++q) {
+        out[2 * q] = buf[q].x;
+        out[2 * q + 1] = buf[q].y;
+      }
+    }
+  });
+}
+
+int xfdtd_far_field(xfdtd_handle *h, int which, double *out, int64_t len) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    run_far_field(h);
+    const long long dirs = static_cast<long long>(h->nf) * h->nt * h->np;
+    if (which >= 0 && which < 8) {
+      if (len != 2 * dirs) invalid("length must be 2 * n_freq * n_theta * n_phi");
+      XCHECK(cudaMemcpyAsync(out, h->ff_out[which], dirs * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    } else if (which == 8 || which == 9) {
+      if (len != dirs) invalid("length must be n_freq * n_theta * n_phi");
+      XCHECK(cudaMemcpyAsync(out, h->ff_power[which - 8], dirs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    } else {
+      invalid("far-field output must be 0..9");
+    }
+    XCHECK(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int xfdtd_check_finite(xfdtd_handle *h) {
+  if (!h) return XFDTD_ERR_STATE;
+  int rc = guarded(h, [&] {
+    XCHECK(cudaMemsetAsync(h->d_flag, 0, sizeof(int), h->stream));
+    for (int c = 0; c < 6; ++c) {
+      if (h->precision == XFDTD_FP64)
+        xg::k_finite<double><<<304, 256, 0, h->stream>>>(static_cast<const double *>(h->F[c]), h->d.cells, h->d_flag);
+      else
+        xg::k_finite<float><<<304, 256, 0, h->stream>>>(static_cast<const float *>(h->F[c]), h->d.cells, h->d_flag);
+      XCHECK(cudaGetLastError());
+    }
+    int flag = 0;
+    XCHECK(cudaMemcpyAsync(&flag, h->d_flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    XCHECK(cudaStreamSynchronize(h->stream));
+    if (flag) throw Err{XFDTD_ERR_NAN, "non-finite field value"};
+  });
+  return rc;
+}
+
+int xfdtd_profile(xfdtd_handle *h, int max, const char **names, double *ms, int64_t *launches, int *count) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    prof_collect(h);
+    int c = 0;
+    for (int q = 0; q < kNumKernels && c < max; ++q) {
+      if (!h->prof_n[q]) continue;
+      if (names) names[c] = kKernelNames[q];
+      if (ms) ms[c] = h->prof_ms[q];
+      if (launches) launches[c] = h->prof_n[q];
+      ++c;
+    }
+    if (count) *count = c;
+  });
+}
+
+int xfdtd_profile_reset(xfdtd_handle *h) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    prof_collect(h);
+    for (int q = 0; q < kNumKernels; ++q) {
+      h->prof_ms[q] = 0;
+      h->prof_n[q] = 0;
+    }
+  });
+}
+
+int xfdtd_launches_per_step(xfdtd_handle *h, int *n) {
+  if (!h || !n) return XFDTD_ERR_STATE;
+  *n = launches_per_step(h);
+  return XFDTD_OK;
+}
+
+int xfdtd_device_bytes(xfdtd_handle *h, int64_t *bytes) {
+  if (!h || !bytes) return XFDTD_ERR_STATE;
+  *bytes = static_cast<int64_t>(h->bytes);
+  return XFDTD_OK;
+}
+
+const char *xfdtd_last_error(xfdtd_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+void xfdtd_destroy(xfdtd_handle *h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  delete h;
+}
+
+}  // extern "C"

@@ -1,0 +1,376 @@
+// surface.cuh -- TFSF 1-D auxiliary grid, NF-FF running DFT, far-field
+// integration, sparse lumped-element and probe kernels, step counter.
+#pragma once
+
+#include "common.cuh"
+
+namespace xg {
+
+// ------------------------------------------------------------------------
+// TFSF3D::updateIncidentField (src/tfsf/tfsf_3d.cpp:153-183) for one step,
+// in one block.  state = [e_inc (L) | h_inc (L-1) | a | b].  The projected
+// arrays of this step go to buffer (t & 1) of `inc`.
+struct AuxParams {
+  int L;
+  double *state;
+  double *inc;
+  const double *source;    // e0 * w(t dt)
+  double ceihi, chiei, c1, c2;
+  double te[3], th[3];
+  const long long *step;
+  long long total;
+  int *status;
+};
+
+__global__ void k_tfsf_aux(AuxParams p) {
+  const long long t = *p.step;
+  if (t >= p.total) {
+    if (threadIdx.x == 0) atomicExch(p.status, 6);
+    return;
+  }
+  const int L = p.L;
+  double *e = p.state;
+  double *h = p.state + L;
+  double *ab = p.state + 2 * L - 1;
+  __shared__ double xy[2];
+  if (threadIdx.x == 0) {
+    e[0] = p.source[t];
+    xy[0] = e[L - 2];
+    xy[1] = e[L - 1];
+  }
+  __syncthreads();
+  for (int i = 1 + threadIdx.x; i < L - 1; i += blockDim.x) e[i] = 1.0 * e[i] + p.ceihi * (h[i] - h[i - 1]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double x = xy[0], y = xy[1];
+    e[L - 1] = -ab[0] + p.c1 * (e[L - 2] + ab[1]) + p.c2 * (x + y);
+    ab[0] = x;
+    ab[1] = y;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < L - 1; i += blockDim.x) h[i] = 1.0 * h[i] + p.chiei * (e[i + 1] - e[i]);
+  __syncthreads();
+  double *out = p.inc + (t & 1) * 6 * L;
+  for (int i = threadIdx.x; i < L; i += blockDim.x) {
+    const double ev = e[i];
+    out[0 * L + i] = p.te[0] * ev;
+    out[1 * L + i] = p.te[1] * ev;
+    out[2 * L + i] = p.te[2] * ev;
+    if (i < L - 1) {
+      const double hv = h[i];
+      out[3 * L + i] = p.th[0] * hv;
+      out[4 * L + i] = p.th[1] * hv;
+      out[5 * L + i] = p.th[2] * hv;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// NffftFd::update (src/nffft/nffft_fd.cpp:108-203) with the face-centre
+// interpolations of EMF (src/electromagnetic_field/linear_interpolation_emf.cpp:286-421).
+// blockIdx.z selects the face pair (0: x, 1: y, 2: z).  Accumulators are
+// complex FP64 in both precisions.  Device layout: X faces [n][j][k],
+// Y faces [n][i][k] (k contiguous; the reference's order is [n][k][i]),
+// Z faces [n][i][j].
+template <typename T>
+struct NfParams {
+  Dims d;
+  const T *E[3];
+  const T *H[3];
+  int lo[3], hi[3];
+  int nf;
+  double2 *acc[24];
+  const double2 *pj, *pm;   // [nf][total]
+  long long total;
+  const long long *step;
+};
+
+template <typename T>
+__global__ void k_nffft(NfParams<T> p) {
+  const long long t = *p.step;
+  if (t >= p.total) return;
+  const int li = p.lo[0], lj = p.lo[1], lk = p.lo[2], ri = p.hi[0], rj = p.hi[1], rk = p.hi[2];
+  const long long si = p.d.si, sj = p.d.sj;
+  const T *ex = p.E[0], *ey = p.E[1], *ez = p.E[2], *hx = p.H[0], *hy = p.H[1], *hz = p.H[2];
+  auto at = [&](const T *f, int i, int j, int k) -> double {
+    return static_cast<double>(f[static_cast<long long>(i) * si + static_cast<long long>(j) * sj + k]);
+  };
+  const int face = blockIdx.z;
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;   // fastest face axis
+  const int v = blockIdx.y * blockDim.y + threadIdx.y;
+  double val[8];
+  long long cell, plane;
+  int base;
+  if (face == 0) {  // X faces: j in [lj, rj), k in [lk, rk); jy, jz, my, mz
+    const int k = lk + u, j = lj + v;
+    if (k >= rk || j >= rj) return;
+    // M = -/+ E face centres, J = +/- H face centres
+    val[2] = -1 * (0.5 * (at(ez, li, j, k) + at(ez, li, j + 1, k)));            // my_xn
+    val[3] = 0.5 * (at(ey, li, j, k) + at(ey, li, j, k + 1));                   // mz_xn
+    val[0] = 0.25 * (at(hz, li, j, k) + at(hz, li, j, k + 1) + at(hz, li - 1, j, k) + at(hz, li - 1, j, k + 1));
+    val[1] = -1 * (0.25 * (at(hy, li, j, k) + at(hy, li, j + 1, k) + at(hy, li - 1, j, k) + at(hy, li - 1, j + 1, k)));
+    val[6] = 0.5 * (at(ez, ri, j, k) + at(ez, ri, j + 1, k));                   // my_xp
+    val[7] = -1 * (0.5 * (at(ey, ri, j, k) + at(ey, ri, j, k + 1)));            // mz_xp
+    val[4] = -1 * (0.25 * (at(hz, ri, j, k) + at(hz, ri, j, k + 1) + at(hz, ri - 1, j, k) + at(hz, ri - 1, j, k + 1)));
+    val[5] = 0.25 * (at(hy, ri, j, k) + at(hy, ri, j + 1, k) + at(hy, ri - 1, j, k) + at(hy, ri - 1, j + 1, k));
+    cell = static_cast<long long>(j - lj) * (rk - lk) + (k - lk);
+    plane = static_cast<long long>(rj - lj) * (rk - lk);
+    base = 0;
+  } else if (face == 1) {  // Y faces: k in [lk, rk), i in [li, ri); jz, jx, mz, mx
+    const int k = lk + u, i = li + v;
+    if (k >= rk || i >= ri) return;
+    val[2] = -1 * (0.5 * (at(ex, i, lj, k) + at(ex, i, lj + 1, k)));            // mz_yn
+    val[3] = 0.5 * (at(ez, i, lj, k) + at(ez, i + 1, lj, k));                   // mx_yn
+    val[0] = 0.25 * (at(hx, i + 1, lj, k) + at(hx, i, lj, k) + at(hx, i + 1, lj - 1, k) + at(hx, i, lj - 1, k));
+    val[1] = -1 * (0.25 * (at(hz, i, lj, k) + at(hz, i, lj, k + 1) + at(hz, i, lj - 1, k) + at(hz, i, lj - 1, k + 1)));
+    val[6] = 0.5 * (at(ex, i, rj, k) + at(ex, i, rj + 1, k));                   // mz_yp
+    val[7] = -1 * (0.5 * (at(ez, i, rj, k) + at(ez, i + 1, rj, k)));            // mx_yp
+    val[4] = -1 * (0.25 * (at(hx, i + 1, rj, k) + at(hx, i, rj, k) + at(hx, i + 1, rj - 1, k) + at(hx, i, rj - 1, k)));
+    val[5] = 0.25 * (at(hz, i, rj, k) + at(hz, i, rj, k + 1) + at(hz, i, rj - 1, k) + at(hz, i, rj - 1, k + 1));
+    cell = static_cast<long long>(i - li) * (rk - lk) + (k - lk);
+    plane = static_cast<long long>(ri - li) * (rk - lk);
+    base = 8;
+  } else {  // Z faces: i in [li, ri), j in [lj, rj); jx, jy, mx, my
+    const int j = lj + u, i = li + v;
+    if (j >= rj || i >= ri) return;
+    val[2] = -1 * (0.5 * (at(ey, i, j, lk) + at(ey, i + 1, j, lk)));            // mx_zn
+    val[3] = 0.5 * (at(ex, i, j, lk) + at(ex, i, j, lk + 1));                   // my_zn
+    val[0] = 0.25 * (at(hy, i, j, lk) + at(hy, i, j + 1, lk) + at(hy, i, j, lk - 1) + at(hy, i, j + 1, lk - 1));
+    val[1] = -1 * (0.25 * (at(hx, i + 1, j, lk) + at(hx, i, j, lk) + at(hx, i + 1, j, lk - 1) + at(hx, i, j, lk - 1)));
+    val[6] = 0.5 * (at(ey, i, j, rk) + at(ey, i + 1, j, rk));                   // mx_zp
+    val[7] = -1 * (0.5 * (at(ex, i, j, rk) + at(ex, i, j, rk + 1)));            // my_zp
+    val[4] = -1 * (0.25 * (at(hy, i, j, rk) + at(hy, i, j + 1, rk) + at(hy, i, j, rk - 1) + at(hy, i, j + 1, rk - 1)));
+    val[5] = 0.25 * (at(hx, i + 1, j, rk) + at(hx, i, j, rk) + at(hx, i + 1, j, rk - 1) + at(hx, i, j, rk - 1));
+    cell = static_cast<long long>(i - li) * (rj - lj) + (j - lj);
+    plane = static_cast<long long>(ri - li) * (rj - lj);
+    base = 16;
+  }
+  for (int n = 0; n < p.nf; ++n) {
+    const double2 tj = p.pj[n * p.total + t], tm = p.pm[n * p.total + t];
+    const long long o = n * plane + cell;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const double2 ph = (q % 4) < 2 ? tj : tm;   // J terms use the (t+1/2) phase, M terms t
+      double2 *a = p.acc[base + q] + o;
+      double2 r = *a;
+      r.x += val[q] * ph.x;
+      r.y += val[q] * ph.y;
+      *a = r;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// NffftFd::calculateFarfield{,X,Y,Z} (src/nffft/nffft_fd.cpp:379-556): one
+// block per (frequency, theta, phi).  Each thread sums a strided share of
+// the surface, the block reduces with warp shuffles, thread 0 projects and
+// writes E/H theta/phi, N/L theta/phi and the power pattern.
+struct FarParams {
+  int lo[3], hi[3];
+  int nf, nt, np;
+  const double2 *acc[24];
+  const double *theta, *phi, *k;
+  double dl[3];
+  double eta0, pi;
+  double2 *out[8];
+  double *power[2];
+};
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+
+__global__ void __launch_bounds__(256) k_far_field(FarParams p) {
+  const int q = blockIdx.x;
+  const int n = q / (p.nt * p.np), t = (q / p.np) % p.nt, pp = q % p.np;
+  const double cos_t = cos(p.theta[t]), sin_t = sin(p.theta[t]);
+  const double cos_p = cos(p.phi[pp]), sin_p = sin(p.phi[pp]);
+  const double stcp = sin_t * cos_p, stsp = sin_t * sin_p;
+  const int li = p.lo[0], lj = p.lo[1], lk = p.lo[2], ri = p.hi[0], rj = p.hi[1], rk = p.hi[2];
+  const int bx = ri - li, by = rj - lj, bz = rk - lk;
+  // s[0..3]: X faces jy jz my mz; s[4..7]: Y faces jz jx mz mx; s[8..11]: Z faces jx jy mx my
+  double2 s[12];
+#pragma unroll
+  for (int r = 0; r < 12; ++r) s[r] = make_double2(0.0, 0.0);
+  {
+    const double dk = p.dl[0] * p.k[n];
+    const long long cnt = static_cast<long long>(by) * bz;
+    for (long long c = threadIdx.x; c < cnt; c += blockDim.x) {
+      const int a = static_cast<int>(c / bz), b = static_cast<int>(c % bz);
+      const int j = lj + a, k = lk + b;
+      double sn, cn, sp, cp;
+      sincos(dk * (li * stcp + (j + 0.5) * stsp + (k + 0.5) * cos_t), &sn, &cn);
+      sincos(dk * (ri * stcp + (j + 0.5) * stsp + (k + 0.5) * cos_t), &sp, &cp);
+      const double2 pn = make_double2(cn, sn), pq = make_double2(cp, sp);
+      const long long o = static_cast<long long>(n) * cnt + c;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) s[r] = cadd(s[r], cadd(cmul(p.acc[r][o], pn), cmul(p.acc[4 + r][o], pq)));
+    }
+  }
+  {
+    const double dk = p.dl[1] * p.k[n];
+    const long long cnt = static_cast<long long>(bz) * bx;
+    for (long long c = threadIdx.x; c < cnt; c += blockDim.x) {
+      const int a = static_cast<int>(c / bz), b = static_cast<int>(c % bz);   // device layout [i][k]
+      const int i = li + a, k = lk + b;
+      double sn, cn, sp, cp;
+      sincos(dk * ((i + 0.5) * stcp + lj * stsp + (k + 0.5) * cos_t), &sn, &cn);
+      sincos(dk * ((i + 0.5) * stcp + rj * stsp + (k + 0.5) * cos_t), &sp, &cp);
+      const double2 pn = make_double2(cn, sn), pq = make_double2(cp, sp);
+      const long long o = static_cast<long long>(n) * cnt + c;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) s[4 + r] = cadd(s[4 + r], cadd(cmul(p.acc[8 + r][o], pn), cmul(p.acc[12 + r][o], pq)));
+    }
+  }
+  {
+    const double dk = p.dl[2] * p.k[n];
+    const long long cnt = static_cast<long long>(bx) * by;
+    for (long long c = threadIdx.x; c < cnt; c += blockDim.x) {
+      const int a = static_cast<int>(c / by), b = static_cast<int>(c % by);
+      const int i = li + a, j = lj + b;
+      double sn, cn, sp, cp;
+      sincos(dk * ((i + 0.5) * stcp + (j + 0.5) * stsp + lk * cos_t), &sn, &cn);
+      sincos(dk * ((i + 0.5) * stcp + (j + 0.5) * stsp + rk * cos_t), &sp, &cp);
+      const double2 pn = make_double2(cn, sn), pq = make_double2(cp, sp);
+      const long long o = static_cast<long long>(n) * cnt + c;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) s[8 + r] = cadd(s[8 + r], cadd(cmul(p.acc[16 + r][o], pn), cmul(p.acc[20 + r][o], pq)));
+    }
+  }
+  // block reduction of the 24 doubles
+  __shared__ double red[8][24];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int r = 0; r < 12; ++r) {
+    double x = s[r].x, y = s[r].y;
+    for (int off = 16; off > 0; off >>= 1) {
+      x += __shfl_down_sync(0xffffffffu, x, off);
+      y += __shfl_down_sync(0xffffffffu, y, off);
+    }
+    if (lane == 0) { red[warp][2 * r] = x; red[warp][2 * r + 1] = y; }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const int nw = blockDim.x / 32;
+  double tot[24];
+  for (int r = 0; r < 24; ++r) {
+    double acc = 0;
+    for (int w = 0; w < nw; ++w) acc += red[w][r];
+    tot[r] = acc;
+  }
+  auto S = [&](int r) { return make_double2(tot[2 * r], tot[2 * r + 1]); };
+  const double dy_dz = p.dl[1] * p.dl[2], dz_dx = p.dl[2] * p.dl[0], dx_dy = p.dl[0] * p.dl[1];
+  double2 zero = make_double2(0.0, 0.0);
+  // X adds a_y a_z f_y f_z; Y adds a_z a_x f_z f_x; Z adds a_x a_y f_x f_y (that order)
+  double2 a_x = zero, a_y = zero, a_z = zero, f_x = zero, f_y = zero, f_z = zero;
+  a_y = cadd(a_y, cscale(S(0), dy_dz)); a_z = cadd(a_z, cscale(S(1), dy_dz));
+  f_y = cadd(f_y, cscale(S(2), dy_dz)); f_z = cadd(f_z, cscale(S(3), dy_dz));
+  a_z = cadd(a_z, cscale(S(4), dz_dx)); a_x = cadd(a_x, cscale(S(5), dz_dx));
+  f_z = cadd(f_z, cscale(S(6), dz_dx)); f_x = cadd(f_x, cscale(S(7), dz_dx));
+  a_x = cadd(a_x, cscale(S(8), dx_dy)); a_y = cadd(a_y, cscale(S(9), dx_dy));
+  f_x = cadd(f_x, cscale(S(10), dx_dy)); f_y = cadd(f_y, cscale(S(11), dx_dy));
+  const double ctcp = cos_t * cos_p, ctsp = cos_t * sin_p;
+  const double2 a_th = cadd(cadd(cscale(a_x, ctcp), cscale(a_y, ctsp)), cscale(a_z, -sin_t));
+  const double2 a_ph = cadd(cscale(a_x, -sin_p), cscale(a_y, cos_p));
+  const double2 f_th = cadd(cadd(cscale(f_x, ctcp), cscale(f_y, ctsp)), cscale(f_z, -sin_t));
+  const double2 f_ph = cadd(cscale(f_x, -sin_p), cscale(f_y, cos_p));
+  const double k = p.k[n], eta = p.eta0, fp = 4 * p.pi;
+  const double coff = (k * k) / (32 * p.pi * p.pi * eta);
+  // e_theta = (-i k)(eta a_th + f_ph)/(4 pi), e_phi = (i k)(-eta a_ph + f_th)/(4 pi),
+  // h_theta = (i k)(a_ph - f_th/eta)/(4 pi), h_phi = (-i k)(a_th + f_ph/eta)/(4 pi)
+  const double2 u1 = cadd(cscale(a_th, eta), f_ph);
+  const double2 u2 = cadd(cscale(a_ph, -eta), f_th);
+  const double2 u3 = make_double2(a_ph.x - f_th.x / eta, a_ph.y - f_th.y / eta);
+  const double2 u4 = make_double2(a_th.x + f_ph.x / eta, a_th.y + f_ph.y / eta);
+  const double2 mik = make_double2(-0.0, -k), pik = make_double2(0.0, k);
+  auto div = [](double2 a, double s) { return make_double2(a.x / s, a.y / s); };
+  p.out[0][q] = div(cmul(mik, u1), fp);
+  p.out[1][q] = div(cmul(pik, u2), fp);
+  p.out[2][q] = div(cmul(pik, u3), fp);
+  p.out[3][q] = div(cmul(mik, u4), fp);
+  p.out[4][q] = a_th;
+  p.out[5][q] = a_ph;
+  p.out[6][q] = f_th;
+  p.out[7][q] = f_ph;
+  const double m1 = hypot(u1.x, u1.y), m2 = hypot(u2.x, u2.y);
+  p.power[0][q] = coff * (m1 * m1);
+  p.power[1][q] = coff * (m2 * m2);
+}
+
+// ------------------------------------------------------------------------
+// Sparse per-step work.
+template <typename T>
+struct SparseParams {
+  Dims d;
+  T *F[6];
+  const xfdtd_injection *inj;
+  int n_inj;
+  const double *waveforms;   // [n_waveforms][total]
+  xfdtd_inductor_cell *ind;
+  double *ind_j;
+  int n_ind;
+  const xfdtd_probe_term *terms;
+  const int *probe_off;       // [n_probes + 1]
+  int n_probes;
+  double *probe_out;          // [n_probes][total]
+  long long total;
+  const long long *step;
+};
+
+template <typename T>
+__device__ __forceinline__ long long sp_index(const Dims &d, long long i, long long j, long long k) {
+  return i * d.si + j * d.sj + k;
+}
+
+// CurrentSource / VoltageSource ::correctE and Inductor::correctE, in list order.
+template <typename T>
+__global__ void k_lumped_e(SparseParams<T> p) {
+  const long long t = *p.step;
+  if (t >= p.total) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < p.n_inj) {
+    const xfdtd_injection &c = p.inj[q];
+    T &e = p.F[c.comp][sp_index<T>(p.d, c.i, c.j, c.k)];
+    e = static_cast<T>(static_cast<double>(e) + c.coff * p.waveforms[c.waveform * p.total + t]);
+  }
+  if (q < p.n_ind) {
+    const xfdtd_inductor_cell &c = p.ind[q];
+    T &e = p.F[c.comp][sp_index<T>(p.d, c.i, c.j, c.k)];
+    double ev = static_cast<double>(e) + c.cecjc * p.ind_j[q];
+    e = static_cast<T>(ev);
+    p.ind_j[q] = c.cjcec * static_cast<double>(e) + p.ind_j[q];
+  }
+}
+
+// Monitor::update as a linear functional per probe (one thread per probe).
+template <typename T>
+__global__ void k_probes(SparseParams<T> p) {
+  const long long t = *p.step;
+  if (t >= p.total) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= p.n_probes) return;
+  double acc = 0.0;
+  for (int r = p.probe_off[q]; r < p.probe_off[q + 1]; ++r) {
+    const xfdtd_probe_term &c = p.terms[r];
+    acc += c.weight * static_cast<double>(p.F[c.comp][sp_index<T>(p.d, c.i, c.j, c.k)]);
+  }
+  p.probe_out[static_cast<long long>(q) * p.total + t] = acc;
+}
+
+__global__ void k_advance(long long *step) { *step += 1; }
+
+// Non-finite scan: sets *flag when any value is NaN or Inf.
+template <typename T>
+__global__ void k_finite(const T *f, long long n, int *flag) {
+  for (long long q = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; q < n;
+       q += static_cast<long long>(gridDim.x) * blockDim.x) {
+    if (!isfinite(static_cast<double>(f[q]))) {
+      atomicExch(flag, 1);
+      return;
+    }
+  }
+}
+
+}  // namespace xg

@@ -1,0 +1,599 @@
+// xfdtd.h -- the reference XFDTD C++ scene API (Mrwatermolen/XFDTD), kept
+// class for class so that a program written against the reference builds
+// against this library, plus the GB300 engine underneath it.
+//
+// Kept: class names, constructor signatures, argument order and defaults of
+//   Simulation       src/include/simulation/simulation.h:27-66
+//   Object, ThinWire src/include/object/object.h:17-20, thin_wire.h
+//   Shape, Cube, Sphere, Cylinder   src/include/shape/*.h
+//   Material         src/include/material/material.h:14-78
+//   Boundary, PML    src/include/boundary/{boundary.h,perfect_match_layer.h}
+//   Waveform family  src/include/waveform/*.h
+//   TFSF, TFSF3D     src/include/tfsf/{tfsf.h,tfsf_3d.h}
+//   NFFFT, NffftFd   src/include/nffft/{nffft.h,nffft_fd.h}
+//   LumpedElement, CurrentSource, VoltageSource, Resistor, Capacitor,
+//   Inductor         src/include/lumped_element/*.h
+//   Monitor, VoltageMonitor, CurrentMonitor   src/include/monitor/*.h
+// and the .npy outputs of NffftFd::outputData / Monitor::outputData.
+//
+// Changed: xtensor types in signatures become std::vector<double> /
+// std::array; PointVector is std::array<double, 3>.  The per-step virtual
+// hooks (Boundary::updateE/H, TFSF::updateE/H, NFFFT::update, Monitor::update,
+// LumpedElement::correctE/H) are not called per step: Simulation lowers the
+// whole scene to one plan and the GPU engine runs the loop.  A user subclass
+// that overrides those hooks is therefore not supported.
+#pragma once
+
+#include <array>
+#include <cmath>
+#include <complex>
+#include <cstddef>
+#include <cstdint>
+#include <functional>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <string_view>
+#include <tuple>
+#include <vector>
+
+struct xfdtd_handle;
+
+namespace xfdtd {
+
+// src/include/util/constant.h:10-29
+namespace constant {
+inline constexpr double PI{3.14159265358979323846};
+inline constexpr double EPSILON_0{8.854187817e-12};
+inline constexpr double MU_0{4 * PI * 1e-7};
+inline constexpr double SQUARED_C_0{1 / (EPSILON_0 * MU_0)};
+inline const double ETA_0{std::sqrt(MU_0 / EPSILON_0)};
+inline const double C_0{std::sqrt(SQUARED_C_0)};
+inline constexpr double TOLERABLE_EPSILON{10 * std::numeric_limits<double>::epsilon()};
+}  // namespace constant
+
+using PointVector = std::array<double, 3>;
+using SpatialIndex = size_t;
+enum class Orientation { XN, XP, YN, YP, ZN, ZP };
+enum class Axis { X, Y, Z };
+
+// GB300 engine precision (extension).
+enum class Precision { FP64, FP32 };
+
+// ----------------------------------------------------------------- shapes
+class Cube;
+class Shape {
+ public:
+  virtual ~Shape() = default;
+  virtual bool isPointInside(const PointVector &point) const = 0;
+  virtual std::unique_ptr<Shape> getWrappedBox() const = 0;
+  virtual std::unique_ptr<Shape> clone() const = 0;
+};
+
+class Cube : public Shape {
+ public:
+  Cube(PointVector point, PointVector size) : _point{point}, _size{size} {}
+  bool isPointInside(const PointVector &point) const override;
+  std::unique_ptr<Shape> getWrappedBox() const override { return std::make_unique<Cube>(_point, _size); }
+  std::unique_ptr<Shape> clone() const override { return std::make_unique<Cube>(*this); }
+  double getXmin() const { return _point[0]; }
+  double getXmax() const { return _point[0] + _size[0]; }
+  double getYmin() const { return _point[1]; }
+  double getYmax() const { return _point[1] + _size[1]; }
+  double getZmin() const { return _point[2]; }
+  double getZmax() const { return _point[2] + _size[2]; }
+  PointVector getSize() const { return _size; }
+  PointVector getPoint() const { return _point; }
+
+ private:
+  PointVector _point, _size;
+};
+
+class Sphere : public Shape {
+ public:
+  Sphere(PointVector center, double radius) : _center{center}, _radius{radius} {}
+  bool isPointInside(const PointVector &point) const override;
+  std::unique_ptr<Shape> getWrappedBox() const override;
+  std::unique_ptr<Shape> clone() const override { return std::make_unique<Sphere>(*this); }
+  double getRadius() const { return _radius; }
+  PointVector getCenter() const { return _center; }
+
+ private:
+  PointVector _center;
+  double _radius;
+};
+
+class Cylinder : public Shape {
+ public:
+  Cylinder(Axis axis, PointVector center, double radius, double height)
+      : _axis{axis}, _center{center}, _radius{radius}, _height{height} {}
+  bool isPointInside(const PointVector &point) const override;
+  std::unique_ptr<Shape> getWrappedBox() const override;
+  std::unique_ptr<Shape> clone() const override { return std::make_unique<Cylinder>(*this); }
+  Axis getAxis() const { return _axis; }
+  double getRadius() const { return _radius; }
+  double getHeight() const { return _height; }
+  PointVector getCenter() const { return _center; }
+
+ private:
+  Axis _axis;
+  PointVector _center;
+  double _radius, _height;
+};
+
+// --------------------------------------------------------------- material
+class Material {
+ public:
+  Material(std::string_view name, float eps_r, float mu_r, double sigma_e, double sigma_m,
+           bool is_dispersion = false);
+  static std::unique_ptr<Material> createAir(const std::string &name = "XFDTD_AIR");
+  static std::unique_ptr<Material> createPEC();
+  static std::unique_ptr<Material> createPMC();
+  double getPermittivityE() const { return _eps; }
+  double getPermeabilityM() const { return _mu; }
+  double getElectricalConductivity() const { return _sigma_e; }
+  double getMagneticConductivity() const { return _sigma_m; }
+  std::tuple<double, double, double, double> getElectromagneticProperties() const {
+    return {_eps, _mu, _sigma_e, _sigma_m};
+  }
+  bool isDispersion() const { return _is_dispersion; }
+  float getEpsR() const { return _eps_r; }
+  float getMuR() const { return _mu_r; }
+  const std::string &getName() const { return _name; }
+
+ private:
+  std::string _name;
+  float _eps_r, _mu_r;
+  double _eps, _mu, _sigma_e, _sigma_m;
+  bool _is_dispersion;
+};
+
+// ----------------------------------------------------------------- object
+class Object {
+ public:
+  Object(std::string_view name, std::unique_ptr<Shape> shape, std::unique_ptr<Material> material);
+  Object(std::string_view name, std::unique_ptr<Shape> shape, Material material);
+  Object(const Object &other);
+  Object &operator=(const Object &other);
+  Object(Object &&) noexcept = default;
+  Object &operator=(Object &&) noexcept = default;
+  virtual ~Object() = default;
+  std::unique_ptr<Shape> getWrappedBox() const { return _shape->getWrappedBox(); }
+  std::unique_ptr<Shape> getShape() const { return _shape->clone(); }
+  const Shape &shape() const { return *_shape; }
+  const Material &material() const { return *_material; }
+  bool isDispersion() const { return _material->isDispersion(); }
+  virtual bool isThinWire() const { return false; }
+  const std::string &getName() const { return _name; }
+
+ private:
+  std::string _name;
+  std::unique_ptr<Shape> _shape;
+  std::unique_ptr<Material> _material;
+};
+
+class ThinWire : public Object {
+ public:
+  ThinWire(const std::string &name, std::unique_ptr<Cylinder> shape);
+  bool isThinWire() const override { return true; }
+};
+
+// --------------------------------------------------------------- boundary
+class Boundary {
+ public:
+  virtual ~Boundary() = default;
+  virtual Orientation getOrientation() const = 0;
+  virtual int getSize() const = 0;
+};
+
+class PML : public Boundary {
+ public:
+  PML(Orientation orientation, int thickness, int order = 4, double sigma_ratio = 1, double alpha_min = 0,
+      double alpha_max = 0.05, double kappa_max = 10)
+      : _orientation{orientation}, _thickness{thickness}, _order{order}, _sigma_ratio{sigma_ratio},
+        _alpha_min{alpha_min}, _alpha_max{alpha_max}, _kappa_max{kappa_max} {}
+  Orientation getOrientation() const override { return _orientation; }
+  int getSize() const override { return _thickness; }
+  int getOrder() const { return _order; }
+  double getSigmaRatio() const { return _sigma_ratio; }
+  double getAlphaMin() const { return _alpha_min; }
+  double getAlphaMax() const { return _alpha_max; }
+  double getKappaMax() const { return _kappa_max; }
+
+ private:
+  Orientation _orientation;
+  int _thickness, _order;
+  double _sigma_ratio, _alpha_min, _alpha_max, _kappa_max;
+};
+
+// --------------------------------------------------------------- waveform
+class Waveform {
+ public:
+  explicit Waveform(double amplitude) : _amplitude{amplitude} {}
+  Waveform() = default;
+  virtual ~Waveform() = default;
+  virtual std::unique_ptr<Waveform> clone() const = 0;
+  // Samples amplitude * f(t) at the given times (Waveform::init).
+  virtual void init(const std::vector<double> &time_array);
+  virtual double getValueByTime(double time) const = 0;
+  const std::vector<double> &getValue() const { return _value; }
+  double operator()(size_t i) const { return _value.at(i); }
+  double getAmplitude() const { return _amplitude; }
+  void setAmplitude(double a) { _amplitude = a; }
+  std::vector<std::complex<double>> getFourierTransform(const std::vector<double> &frequencies, double dt) const;
+
+ protected:
+  void setValue(std::vector<double> v) { _value = std::move(v); }
+
+ private:
+  double _amplitude{1.0};
+  std::vector<double> _value;
+};
+
+class GaussianWaveform : public Waveform {
+ public:
+  GaussianWaveform(double amplitude, double tau, double t_0) : Waveform{amplitude}, _tau{tau}, _t_0{t_0} {}
+  GaussianWaveform(double tau, double t_0) : _tau{tau}, _t_0{t_0} {}
+  std::unique_ptr<Waveform> clone() const override { return std::make_unique<GaussianWaveform>(*this); }
+  double getValueByTime(double t) const override;
+  void init(const std::vector<double> &time_array) override;
+
+ private:
+  double _tau, _t_0;
+};
+
+class CosineModulatedGaussianWaveform : public Waveform {
+ public:
+  CosineModulatedGaussianWaveform(double amplitude, double tau, double t_0, double modulation_frequency)
+      : Waveform{amplitude}, _tau{tau}, _t_0{t_0}, _f{modulation_frequency} {}
+  CosineModulatedGaussianWaveform(double tau, double t_0, double modulation_frequency)
+      : _tau{tau}, _t_0{t_0}, _f{modulation_frequency} {}
+  std::unique_ptr<Waveform> clone() const override {
+    return std::make_unique<CosineModulatedGaussianWaveform>(*this);
+  }
+  double getValueByTime(double t) const override;
+  void init(const std::vector<double> &time_array) override;
+
+ private:
+  double _tau, _t_0, _f;
+};
+
+class SinusoidalWaveform : public Waveform {
+ public:
+  SinusoidalWaveform(double amplitude, double frequency, double phase)
+      : Waveform(amplitude), _frequency(frequency), _phase(phase) {}
+  SinusoidalWaveform(double frequency, double phase) : _frequency(frequency), _phase(phase) {}
+  std::unique_ptr<Waveform> clone() const override { return std::make_unique<SinusoidalWaveform>(*this); }
+  double getValueByTime(double t) const override;
+  void init(const std::vector<double> &time_array) override;
+
+ private:
+  double _frequency, _phase;
+};
+
+class CustomWaveform : public Waveform {
+ public:
+  CustomWaveform(double amplitude, std::function<double(double)> f) : Waveform(amplitude), _f(std::move(f)) {}
+  std::unique_ptr<Waveform> clone() const override { return std::make_unique<CustomWaveform>(*this); }
+  double getValueByTime(double t) const override { return getAmplitude() * _f(t); }
+
+ private:
+  std::function<double(double)> _f;
+};
+
+// ------------------------------------------------------------------- TFSF
+class TFSF {
+ public:
+  TFSF(SpatialIndex distance_x, SpatialIndex distance_y, SpatialIndex distance_z, double e_0, double theta_inc,
+       double phi_inc, double psi, std::shared_ptr<Waveform> waveform);
+  virtual ~TFSF() = default;
+  std::tuple<SpatialIndex, SpatialIndex, SpatialIndex> getDistance() const {
+    return {_distance_x, _distance_y, _distance_z};
+  }
+  double getIncidentFieldAmplitude() const { return _e_0; }
+  double getIncidentTheta() const { return _theta_inc; }
+  double getIncidentPhi() const { return _phi_inc; }
+  double getIncidentPsi() const { return _psi; }
+  PointVector getKVector() const { return _k; }
+  Waveform &waveform() const { return *_waveform; }
+  // dt * sum_t e0 w[t] exp(-i 2 pi f t dt) over the sampled incident wave
+  // (TFSF::getIncidentWaveFourierTransform, tfsf.cpp:63-66; valid after run/init).
+  std::vector<std::complex<double>> getIncidentWaveFourierTransform(const std::vector<double> &frequencies) const;
+  void bindTimeStep(double dt) { _dt = dt; }
+
+ private:
+  SpatialIndex _distance_x, _distance_y, _distance_z;
+  double _e_0, _theta_inc, _phi_inc, _psi;
+  PointVector _k;
+  std::shared_ptr<Waveform> _waveform;
+  double _dt{0};
+};
+
+class TFSF3D : public TFSF {
+ public:
+  TFSF3D(SpatialIndex distance_x, SpatialIndex distance_y, SpatialIndex distance_z, double e_0, double theta_inc,
+         double phi_inc, double psi, std::shared_ptr<Waveform> waveform)
+      : TFSF(distance_x, distance_y, distance_z, e_0, theta_inc, phi_inc, psi, std::move(waveform)) {}
+};
+
+// ------------------------------------------------------------------ NF-FF
+class NFFFT {
+ public:
+  NFFFT(SpatialIndex distance_x, SpatialIndex distance_y, SpatialIndex distance_z, std::string output_dir_path)
+      : _distance_x{distance_x}, _distance_y{distance_y}, _distance_z{distance_z},
+        _output_dir_path{std::move(output_dir_path)} {}
+  virtual ~NFFFT() = default;
+  std::tuple<SpatialIndex, SpatialIndex, SpatialIndex> getDistance() const {
+    return {_distance_x, _distance_y, _distance_z};
+  }
+  const std::string &getOutputDirPath() const { return _output_dir_path; }
+
+ private:
+  SpatialIndex _distance_x, _distance_y, _distance_z;
+  std::string _output_dir_path;
+};
+
+class NffftFd : public NFFFT {
+ public:
+  NffftFd(SpatialIndex distance_x, SpatialIndex distance_y, SpatialIndex distance_z, std::vector<double> frequencies,
+          std::vector<double> theta, std::vector<double> phi, std::string output_dir_path)
+      : NFFFT(distance_x, distance_y, distance_z, std::move(output_dir_path)), _frequencies{std::move(frequencies)},
+        _theta{std::move(theta)}, _phi{std::move(phi)} {}
+  NffftFd(SpatialIndex distance_x, SpatialIndex distance_y, SpatialIndex distance_z, double frequency,
+          std::vector<double> theta, std::vector<double> phi, std::string output_dir_path)
+      : NffftFd(distance_x, distance_y, distance_z, std::vector<double>{frequency}, std::move(theta), std::move(phi),
+                std::move(output_dir_path)) {}
+  const std::vector<double> &getFrequencies() const { return _frequencies; }
+  const std::vector<double> &getTheta() const { return _theta; }
+  const std::vector<double> &getPhi() const { return _phi; }
+
+ private:
+  std::vector<double> _frequencies, _theta, _phi;
+};
+
+// ---------------------------------------------------------- lumped element
+class LumpedElement {
+ public:
+  explicit LumpedElement(std::unique_ptr<Cube> cube) : _cube{std::move(cube)} {}
+  LumpedElement(const LumpedElement &o) : _cube{std::make_unique<Cube>(*o._cube)} {}
+  virtual ~LumpedElement() = default;
+  const Cube &cube() const { return *_cube; }
+
+ private:
+  std::unique_ptr<Cube> _cube;
+};
+
+class CurrentSource : public LumpedElement {
+ public:
+  CurrentSource(std::unique_ptr<Cube> cube, Orientation orientation, double resistance,
+                std::unique_ptr<Waveform> waveform);
+  CurrentSource(const CurrentSource &o);
+  Orientation getOrientation() const { return _orientation; }
+  double getResistance() const { return _resistance; }
+  Waveform &waveform() const { return *_waveform; }
+
+ private:
+  Orientation _orientation;
+  double _resistance;
+  std::unique_ptr<Waveform> _waveform;
+};
+
+class VoltageSource : public LumpedElement {
+ public:
+  VoltageSource(std::unique_ptr<Cube> cube, Orientation orientation, double resistance,
+                std::unique_ptr<Waveform> waveform);
+  VoltageSource(const VoltageSource &o);
+  Orientation getOrientation() const { return _orientation; }
+  double getResistance() const { return _resistance; }
+  Waveform &waveform() const { return *_waveform; }
+
+ private:
+  Orientation _orientation;
+  double _resistance;
+  std::unique_ptr<Waveform> _waveform;
+};
+
+class Resistor : public LumpedElement {
+ public:
+  Resistor(std::unique_ptr<Cube> cube, Axis axis, double resistance)
+      : LumpedElement{std::move(cube)}, _axis{axis}, _resistance{resistance} {}
+  Axis getAxis() const { return _axis; }
+  double getResistance() const { return _resistance; }
+
+ private:
+  Axis _axis;
+  double _resistance;
+};
+
+class Capacitor : public LumpedElement {
+ public:
+  Capacitor(std::unique_ptr<Cube> cube, Axis axis, double capacitance)
+      : LumpedElement{std::move(cube)}, _axis{axis}, _capacitance{capacitance} {}
+  Axis getAxis() const { return _axis; }
+  double getCapacitance() const { return _capacitance; }
+
+ private:
+  Axis _axis;
+  double _capacitance;
+};
+
+class Inductor : public LumpedElement {
+ public:
+  Inductor(std::unique_ptr<Cube> cube, Axis axis, double inductance)
+      : LumpedElement{std::move(cube)}, _axis{axis}, _inductance{inductance} {}
+  Axis getAxis() const { return _axis; }
+  double getInductance() const { return _inductance; }
+
+ private:
+  Axis _axis;
+  double _inductance;
+};
+
+// ----------------------------------------------------------------- monitor
+class Monitor {
+ public:
+  Monitor(std::unique_ptr<Cube> cube, std::string output_dir_path, std::string output_file_name)
+      : _cube{std::move(cube)}, _dir{std::move(output_dir_path)}, _file{std::move(output_file_name)} {}
+  Monitor(const Monitor &o) : _cube{std::make_unique<Cube>(*o._cube)}, _dir{o._dir}, _file{o._file} {}
+  virtual ~Monitor() = default;
+  const Cube &cube() const { return *_cube; }
+  const std::string &getOutputPath() const { return _dir; }
+  const std::string &getOutputFileName() const { return _file; }
+  void setOutputDirPath(const std::string &d) { _dir = d; }
+  void setOutputFileName(const std::string &f) { _file = f; }
+  // Time series recorded by the last run (one value per step).
+  const std::vector<double> &getValue() const { return _value; }
+  double getValue(size_t i) const { return _value.at(i); }
+  void setValue(std::vector<double> v) { _value = std::move(v); }
+
+ private:
+  std::unique_ptr<Cube> _cube;
+  std::string _dir, _file;
+  std::vector<double> _value;
+};
+
+class VoltageMonitor : public Monitor {
+ public:
+  VoltageMonitor(std::unique_ptr<Cube> shape, Orientation orientation, std::string output_dir_path,
+                 std::string output_file_name)
+      : Monitor{std::move(shape), std::move(output_dir_path), std::move(output_file_name)},
+        _orientation{orientation} {}
+  Orientation getOrientation() const { return _orientation; }
+
+ private:
+  Orientation _orientation;
+};
+
+class CurrentMonitor : public Monitor {
+ public:
+  CurrentMonitor(std::unique_ptr<Cube> shape, Orientation orientation, std::string output_dir_path,
+                 std::string output_file_name)
+      : Monitor{std::move(shape), std::move(output_dir_path), std::move(output_file_name)},
+        _orientation{orientation} {}
+  Orientation getOrientation() const { return _orientation; }
+
+ private:
+  Orientation _orientation;
+};
+
+// -------------------------------------------------------------- grid space
+// Uniform GridSpace (src/grid/grid_space.cpp:14-757, uniform path only).
+class GridSpace {
+ public:
+  explicit GridSpace(double dl);
+  void calculateSpaceSize(const Cube &box);
+  void extendBoundary(Orientation o, double size);
+  void generateUniformGridSpace();
+  size_t n(int axis) const { return _n[axis]; }
+  double base(int axis) const { return _base[axis]; }
+  double eNode(int axis, size_t i) const { return _ec[axis][i]; }
+  double hNode(int axis, size_t i) const { return _hc[axis][i]; }
+  const std::vector<double> &eNodes(int axis) const { return _ec[axis]; }
+  const std::vector<double> &hNodes(int axis) const { return _hc[axis]; }
+  // nearest E node (handleTransform*, grid_space.cpp:551-574)
+  size_t nearest(int axis, double x) const;
+  // [start, end) index box of a shape's wrapped cube (getGridBox, :306-329)
+  std::array<size_t, 6> gridBox(const Shape &shape) const;
+
+ private:
+  double _base[3];
+  double _mn[3], _mx[3];
+  size_t _n[3] = {0, 0, 0};
+  bool _ready = false;
+  std::vector<double> _ec[3], _hc[3];
+  void resize(const double *mn, const double *mx);
+};
+
+// --------------------------------------------------------------- simulation
+class Simulation {
+ public:
+  inline static constexpr float DEFAULT_CFL{0.99};
+
+  explicit Simulation(double cell_size, float cfl = DEFAULT_CFL);
+  Simulation(double cell_size, std::vector<std::shared_ptr<Object>> objects,
+             std::vector<std::shared_ptr<Boundary>> boundaries, std::unique_ptr<TFSF> tfsf, float cfl = DEFAULT_CFL);
+  Simulation(double cell_size, std::vector<std::shared_ptr<Object>> objects,
+             std::vector<std::shared_ptr<Boundary>> boundaries, std::unique_ptr<TFSF> tfsf,
+             std::unique_ptr<NFFFT> nffft, float cfl = DEFAULT_CFL);
+  Simulation(double cell_size, std::vector<std::shared_ptr<Object>> objects,
+             std::vector<std::shared_ptr<LumpedElement>> lumped_elements,
+             std::vector<std::shared_ptr<Boundary>> boundaries = {}, std::vector<std::shared_ptr<Monitor>> monitor = {},
+             float cfl = DEFAULT_CFL);
+  Simulation(double cell_size, std::vector<std::shared_ptr<Object>> objects,
+             std::vector<std::shared_ptr<Monitor>> monitors = {}, float cfl = DEFAULT_CFL);
+  ~Simulation();
+  Simulation(const Simulation &) = delete;
+  Simulation &operator=(const Simulation &) = delete;
+
+  void addObject(std::shared_ptr<Object> object);
+  void addBoundary(std::shared_ptr<Boundary> boundary);
+  void addLumpedElement(std::shared_ptr<LumpedElement> lumped_element);
+  void addTFSFSource(std::shared_ptr<TFSF> tfsf);
+  void addNFFFT(std::shared_ptr<NFFFT> nffft);
+  void addMonitor(std::shared_ptr<Monitor> monitor);
+
+  // Simulation::run (simulation_update.cpp:5-40): init, the loop, outputData.
+  void run(size_t total_time_steps);
+  // Builds the grid and the plan only and writes the counts
+  // (Simulation::checkRun, simulation.cpp:98-113).
+  void checkRun(size_t total_time_steps);
+
+  // ---- GB300 extensions -------------------------------------------------
+  void setPrecision(Precision p) { _precision = p; }
+  Precision getPrecision() const { return _precision; }
+  void setUseGraph(bool g) { _use_graph = g; }
+  void setProfile(bool p) { _profile = p; }
+  // One material per cell, applied after all objects (see xfdtd_scene.h).
+  void setVoxelMaterials(std::vector<Material> materials, std::vector<uint16_t> index, std::array<size_t, 3> shape);
+  // Split run(): init once, step in pieces, read state, output at the end.
+  void init(size_t total_time_steps);
+  void step(size_t n);
+  void outputData();
+  size_t getCurrentTimeStep() const;
+  size_t getTotalTimeSteps() const { return _total; }
+  // Field component c (0 Ex .. 5 Hz) in the reference's component shape.
+  std::vector<double> readField(int comp) const;
+  void writeField(int comp, const std::vector<double> &values);
+  // Far-field array `which` (0 e_theta .. 7 l_phi complex, 8/9 power).
+  std::vector<std::complex<double>> farField(int which) const;
+  std::vector<double> farFieldPower(int which) const;
+  std::vector<std::complex<double>> nffftAccumulator(int which) const;
+  // Bistatic RCS in dB over (frequency, theta, phi):
+  // 10 log10(4 pi (|E_theta|^2 + |E_phi|^2) / |E_inc(f)|^2).
+  std::vector<double> rcsDb() const;
+  xfdtd_handle *engine() const { return _engine; }
+
+  double getDt() const { return _dt; }
+  SpatialIndex getNx() const { return _nx; }
+  SpatialIndex getNy() const { return _ny; }
+  SpatialIndex getNz() const { return _nz; }
+
+ private:
+  double _cell_size;
+  float _cfl;
+  std::vector<std::shared_ptr<Object>> _objects;
+  std::vector<std::shared_ptr<Boundary>> _boundaries;
+  std::vector<std::shared_ptr<LumpedElement>> _lumped_elements;
+  std::vector<std::shared_ptr<Monitor>> _monitors;
+  std::shared_ptr<TFSF> _tfsf;
+  std::shared_ptr<NFFFT> _nffft;
+  std::vector<Material> _voxel_materials;
+  std::vector<uint16_t> _voxel_index;
+  std::array<size_t, 3> _voxel_shape{0, 0, 0};
+
+  Precision _precision{Precision::FP64};
+  bool _use_graph{true};
+  bool _profile{false};
+  size_t _total{0};
+  size_t _nx{0}, _ny{0}, _nz{0};
+  double _dt{0};
+  xfdtd_handle *_engine{nullptr};
+  std::vector<size_t> _monitor_probe;   // probe index of each monitor
+  void release();
+};
+
+// Throws std::runtime_error with the engine's message on a non-zero status.
+void checkEngine(int status, xfdtd_handle *h);
+
+}  // namespace xfdtd

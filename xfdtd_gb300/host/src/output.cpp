@@ -1,0 +1,113 @@
+// output.cpp -- .npy outputs of the reference (NffftFd::outputData,
+// src/nffft/nffft_fd.cpp:579-634; VoltageMonitor / CurrentMonitor ::outputData,
+// src/monitor/voltage_monitor.cpp:99-120, current_monitor.cpp:117-140) and
+// Simulation::checkRun (src/simulation/simulation.cpp:98-113).
+#include <cstdio>
+#include <filesystem>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+
+#include "../../../include/xfdtd_cuda.h"
+#include "xfdtd/xfdtd.h"
+
+namespace xfdtd {
+
+namespace {
+
+// Minimal .npy (format 1.0) writer: little-endian '<f8' or '<c16', C order.
+void writeNpy(const std::filesystem::path &path, const void *data, size_t elem_bytes, const char *descr,
+              const std::vector<size_t> &shape) {
+  std::ostringstream hdr;
+  hdr << "{'descr': '" << descr << "', 'fortran_order': False, 'shape': (";
+  for (size_t q = 0; q < shape.size(); ++q) hdr << shape[q] << (shape.size() == 1 || q + 1 < shape.size() ? ", " : "");
+  hdr << "), }";
+  std::string h = hdr.str();
+  const size_t total = 10 + h.size() + 1;
+  const size_t pad = (64 - total % 64) % 64;
+  h.append(pad, ' ');
+  h.push_back('\n');
+  std::ofstream f(path, std::ios::binary);
+  if (!f) throw std::runtime_error("cannot write " + path.string());
+  const char magic[] = {'\x93', 'N', 'U', 'M', 'P', 'Y', 1, 0};
+  f.write(magic, 8);
+  const uint16_t len = static_cast<uint16_t>(h.size());
+  const unsigned char l2[2] = {static_cast<unsigned char>(len & 0xff), static_cast<unsigned char>(len >> 8)};
+  f.write(reinterpret_cast<const char *>(l2), 2);
+  f.write(h.data(), static_cast<std::streamsize>(h.size()));
+  size_t n = 1;
+  for (size_t s : shape) n *= s;
+  f.write(static_cast<const char *>(data), static_cast<std::streamsize>(n * elem_bytes));
+}
+
+bool ensureDir(const std::filesystem::path &p) {
+  if (p.empty()) return true;
+  if (std::filesystem::exists(p)) return true;
+  try {
+    std::filesystem::create_directories(p);
+  } catch (const std::exception &) {
+    std::cerr << "Error: cannot create directory " << p.string() << '\n';
+    return false;
+  }
+  return true;
+}
+
+std::vector<double> linspace(double a, double b, size_t n) {
+  std::vector<double> v(n);
+  const double step = n > 1 ? (b - a) / static_cast<double>(n - 1) : 0.0;
+  for (size_t i = 0; i < n; ++i) v[i] = a + static_cast<double>(i) * step;
+  return v;
+}
+
+}  // namespace
+
+void Simulation::outputData() {
+  if (!_engine) throw std::runtime_error("Simulation::init has not been called");
+  // monitors: stack(time, value) -> (2, N)
+  if (!_monitors.empty()) {
+    std::vector<double> all(_monitors.size() * _total);
+    checkEngine(xfdtd_read_probes(_engine, all.data(), static_cast<int64_t>(all.size())), _engine);
+    for (size_t m = 0; m < _monitors.size(); ++m) {
+      std::vector<double> v(all.begin() + m * _total, all.begin() + (m + 1) * _total);
+      _monitors[m]->setValue(v);
+      const std::string &dir = _monitors[m]->getOutputPath();
+      if (dir.empty()) continue;
+      const bool current = dynamic_cast<const CurrentMonitor *>(_monitors[m].get()) != nullptr;
+      auto t = current ? linspace(0.5 * _dt, (_total + 0.5) * _dt, _total) : linspace(0.0, _total * _dt, _total);
+      if (!ensureDir(dir)) continue;
+      std::vector<double> st(2 * _total);
+      std::copy(t.begin(), t.end(), st.begin());
+      std::copy(v.begin(), v.end(), st.begin() + _total);
+      writeNpy(std::filesystem::path(dir) / _monitors[m]->getOutputFileName(), st.data(), 8, "<f8", {2, _total});
+    }
+  }
+  const NffftFd *nfd = dynamic_cast<const NffftFd *>(_nffft.get());
+  if (nfd && !nfd->getOutputDirPath().empty() && !nfd->getTheta().empty() && !nfd->getPhi().empty()) {
+    const std::filesystem::path out{nfd->getOutputDirPath()};
+    if (!ensureDir(out)) return;
+    const std::vector<size_t> shp{nfd->getFrequencies().size(), nfd->getTheta().size(), nfd->getPhi().size()};
+    writeNpy(out / "frequencies.npy", nfd->getFrequencies().data(), 8, "<f8", {nfd->getFrequencies().size()});
+    writeNpy(out / "theta.npy", nfd->getTheta().data(), 8, "<f8", {nfd->getTheta().size()});
+    writeNpy(out / "phi.npy", nfd->getPhi().data(), 8, "<f8", {nfd->getPhi().size()});
+    const char *names[8] = {"e_theta", "e_phi", "h_theta", "h_phi", "n_theta", "n_phi", "l_theta", "l_phi"};
+    for (int w = 0; w < 8; ++w) {
+      auto v = farField(w);
+      writeNpy(out / (std::string(names[w]) + ".npy"), v.data(), 16, "<c16", shp);
+    }
+    auto p0 = farFieldPower(0), p1 = farFieldPower(1);
+    writeNpy(out / "power_theta.npy", p0.data(), 8, "<f8", shp);
+    writeNpy(out / "power_phi.npy", p1.data(), 8, "<f8", shp);
+  }
+}
+
+void Simulation::checkRun(size_t total_time_steps) {
+  init(total_time_steps);
+  std::ofstream ofs{"simulation_check", std::ios::out};
+  ofs << "nx:" << _nx << " ny:" << _ny << " nz:" << _nz << '\n';
+  ofs << "Total size:" << _nx * _ny * _nz << '\n';
+  std::ofstream object_ofs{"simulation_object_check", std::ios::out};
+  object_ofs << "Object:" << '\n';
+  for (auto &o : _objects) object_ofs << "Object: " << o->getName() << '\n';
+}
+
+}  // namespace xfdtd
