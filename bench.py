@@ -1,0 +1,372 @@
+"""Benchmark of the FDTD step loop on GB300: Mcell-updates/s and the HBM
+roofline fraction of the dominant kernel, beside the CPU oracle.
+
+Workload: the dielectric-sphere scattering configuration -- 256^3 interior
+plus a 12-cell CPML per face (280^3 = 21,952,000 cells), dx = 2 mm, eps_r = 4
+sphere of radius 60 cells, TFSF x-polarised +z Gaussian plane wave
+(tau = 40 dt), NF-FF running DFT at 1, 2 and 3 GHz, 2000 steps -- in the FP32
+form (fields and CPML in FP32; TFSF 1-D grid, NF-FF accumulators and
+far-field integration in FP64).  Synthetic inputs of that shape (there is no
+dataset).  The fields (6 x 87.8 MB) are far larger than the 129 MB L2, so no
+flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one time step of the loop body over the whole grid.  value =
+(cells x steps x ranks) / max-over-ranks device time of the K timed steps
+(CUDA events on the engine's stream).  e2e = the same metric over one whole
+job through the public API (host scene -> plan -> upload, K steps, far field
+and RCS copied back), wall clock.  With --gpus N > 1 (torchrun), every rank
+runs an independent replica of the workload (the path has no exchange).
+
+--impl reference times the reference's algorithm on the host cores: the
+reference cannot be built here (xtensor, xtensor-blas, xtensor-fftw, FFTW3,
+BLAS and LAPACK are absent), so its line restates it -- the FP64 CPU oracle
+(oracle/), all host threads, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from xfdtd_gb300 import configs  # noqa: E402
+
+CONFIG_NAME = "dielectric_sphere"
+METRIC = "Mcell-updates/s"
+UNIT = "Mcell-updates/s"
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class _Group:
+    """torch.distributed plumbing for N > 1 (barrier and max-reduce only)."""
+
+    def __init__(self, world, local):
+        self.world = world
+        self.torch = None
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+            self.torch = torch
+            self.dist = dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            if torch.cuda.is_available():
+                torch.cuda.set_device(local)
+                dist.init_process_group("nccl")
+                self.dev = torch.device("cuda", local)
+            else:
+                dist.init_process_group("gloo")
+                self.dev = torch.device("cpu")
+
+    def barrier(self):
+        if self.torch is not None:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.torch is None:
+            return v
+        t = self.torch.tensor([v], dtype=self.torch.float64, device=self.dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.torch is not None:
+            self.dist.destroy_process_group()
+
+
+def aggregate_value(cells: int, steps: int, world: int, max_ms: float) -> float:
+    """Whole-job Mcell-updates/s: every rank advances its own replica."""
+    return cells * steps * world / (max_ms / 1e3) / 1e6
+
+
+# ----------------------------------------------------------------- clocks ---
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            import tempfile
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in rows for q in range(4) if r[3][q].lower() == "active"})
+        loaded = [r for r in rows if r[2] > 300] or rows
+        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": reasons}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------- roofline ---
+def algorithmic_bytes(n, slab_layers, precision: str, kernel: str) -> float:
+    """Bytes one launch of the E (or H) kernel must move at least: read the
+    3 own components and the 3 curl components, write the 3 own components,
+    read the 1-byte material index; inside CPML slabs read and write one psi
+    per (component, slab axis) pair (2 per slab axis)."""
+    nx, ny, nz = n
+    cells = nx * ny * nz
+    w = 8 if precision == "fp64" else 4
+    per_cell = 9 * w + 1
+    slab_cells = (slab_layers[0] * ny * nz + slab_layers[1] * nx * nz + slab_layers[2] * nx * ny)
+    return cells * per_cell + slab_cells * 2 * 2 * w
+
+
+def _slab_layers(sc):
+    lay = [0, 0, 0]
+    for b in sc.boundaries:
+        lay[b.orientation // 2] += b.thickness
+    return lay
+
+
+# -------------------------------------------------------------------- arms ---
+def run_cpu_oracle(threads: int, sample_steps: int, scale: int = 1):
+    """FP64 CPU oracle on the same workload: init untimed, `sample_steps`
+    steps timed.  Returns (Mcell-updates/s, cores, sample description)."""
+    import oracle
+    oracle.build()
+    cores = oracle.set_threads(threads)
+    sc, _ = configs.dielectric_sphere(scale=scale)
+    o = oracle.OracleSim(sc, sample_steps + 1)
+    o.step(1)   # first touch
+    t0 = time.perf_counter()
+    o.step(sample_steps)
+    dt = time.perf_counter() - t0
+    cells = o.n[0] * o.n[1] * o.n[2]
+    del o
+    return cells * sample_steps / dt / 1e6, cores, f"{sample_steps} steps of the {o_n(sc)} grid, {cores} thread(s), {dt:.1f} s"
+
+
+def o_n(sc):
+    return "x".join(str(v) for v in _grid_n(sc))
+
+
+def _grid_n(sc):
+    half = round(sc.objects[0].shape.size[0] / sc.cell_size)
+    t = sc.boundaries[0].thickness
+    return (half + 2 * t,) * 3
+
+
+def reference_arm(args, world, rank):
+    base = {"metric": METRIC, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "dielectric sphere, 280^3 cells incl. 12-cell CPML, TFSF, NF-FF 3 freq",
+                       "cells": 280 ** 3}}
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    import oracle
+    oracle.build()
+    cores = oracle.set_threads(threads)
+    # Each bench step is one oracle time step of the same scene family on a
+    # grid sized so that the whole --warmup W --steps K run stays within
+    # about args.ref_budget seconds (calibrated on the 1/4-scale grid).
+    cal, _ = configs.dielectric_sphere(scale=4)
+    oc = oracle.OracleSim(cal, 6)
+    oc.step(1)
+    t0 = time.perf_counter()
+    oc.step(4)
+    per_cell = (time.perf_counter() - t0) / 4 / (oc.n[0] * oc.n[1] * oc.n[2])
+    del oc
+    budget_step = args.ref_budget / (args.warmup + args.steps)
+    scale = 1
+    for s in (1, 2, 4):
+        scale = s
+        if _grid_n(configs.dielectric_sphere(scale=s)[0])[0] ** 3 * per_cell <= budget_step:
+            break
+    sc, _ = configs.dielectric_sphere(scale=scale)
+    o = oracle.OracleSim(sc, args.warmup + args.steps + 1)
+    cells = o.n[0] * o.n[1] * o.n[2]
+    o.step(1)
+    o.step(args.warmup)
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    tot = time.perf_counter() - t0
+    v = cells * args.steps / tot / 1e6
+    line = dict(base)
+    line["config"] = dict(base["config"], sample_grid=list(o.n), sample_scale=scale)
+    line.update({"value": v, "ms_per_step": 1e3 * tot / args.steps,
+                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                  "sample": f"{args.steps} oracle steps of the {'x'.join(map(str, o.n))} grid "
+                                            f"(scale 1/{scale} of the workload), {cores} threads"},
+                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                 "note": "the reference does not build here; its FP64 algorithm is restated in oracle/"})
+    print(json.dumps(line), flush=True)
+
+
+def ours_arm(args, world, rank, local, grp):
+    import xfdtd_gb300 as X
+    X.build()
+    sc, _ = configs.dielectric_sphere()
+    total = args.warmup + args.steps
+    sim = X.Simulation(sc, total, precision=args.precision, graph=False, profile=True, device=local)
+    n = sim.n
+    cells = n[0] * n[1] * n[2]
+    sim.step(args.warmup)
+    sim.synchronize()
+    sim.profile_reset()
+    clock = ClockSampler(local)
+    clock.start()
+    grp.barrier()
+    ms = sim.step_timed(args.steps)
+    sim.synchronize()
+    grp.barrier()
+    clocks = clock.stop()
+    max_ms = grp.max(ms)
+    prof = sim.profile()
+    launches = sim.launches_per_step() * args.steps
+    sim.check_finite()
+    value = aggregate_value(cells, args.steps, world, max_ms)
+
+    # roofline of the dominant kernel (largest share of device time)
+    peak, peak_kind = _peaks()
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    slabs = _slab_layers(sc)
+    alg = algorithmic_bytes(n, slabs, args.precision, dom)
+    achieved = alg / (dom_ms / dom_n / 1e3) / 1e9
+    total_prof = sum(v[0] for v in prof.values())
+    shares = {k: round(v[0] / total_prof, 4) for k, v in prof.items()}
+    del sim
+
+    # e2e: one whole job through the public API, host scene to host results
+    grp.barrier()
+    t0 = time.perf_counter()
+    job = X.Simulation(sc, args.steps, precision=args.precision, graph=True, device=local)
+    job.step(args.steps)
+    rcs = job.rcs_db()
+    t1 = time.perf_counter()
+    h2d, d2h = job.transfer_bytes()
+    assert np.isfinite(rcs).all()
+    e2e_s = grp.max(t1 - t0)
+    del job
+
+    # FP64 form on the same workload (fewer steps)
+    fp64 = None
+    if args.fp64_steps > 0 and rank == 0:
+        s64 = X.Simulation(sc, args.warmup + args.fp64_steps, precision="fp64", graph=False, profile=True, device=local)
+        s64.step(args.warmup)
+        s64.profile_reset()
+        ms64 = s64.step_timed(args.fp64_steps)
+        p64 = s64.profile()
+        d64 = max(p64, key=lambda k: p64[k][0])
+        a64 = algorithmic_bytes(n, slabs, "fp64", d64) / (p64[d64][0] / p64[d64][1] / 1e3) / 1e9
+        fp64 = {"value": cells * args.fp64_steps / (ms64 / 1e3) / 1e6, "unit": UNIT, "steps": args.fp64_steps,
+                "ms_per_step": ms64 / args.fp64_steps, "dominant_kernel": d64,
+                "dominant_kernel_GBs": a64, "note": "GB300 FP64 is ~1/64 rate: this form is compute-bound"}
+        del s64
+
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_sample > 0:
+        v, cores, sample = run_cpu_oracle(1, args.cpu_sample)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
+        "data": "synthetic",
+        "config": {"workload": "dielectric sphere scattering: 256^3 interior + 12-cell CPML (280^3 cells), "
+                               "dx 2 mm, eps_r 4 sphere r=60 cells, TFSF x-pol +z Gaussian, NF-FF 1/2/3 GHz",
+                   "cells": cells, "grid": list(n), "precision_form": args.precision,
+                   "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (cells * (4 if args.precision == 'fp32' else 8) / 1e6),
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": alg, "launch_ms": dom_ms / dom_n},
+        "kernel_shares": shares,
+        "e2e": {"value": cells * args.steps * world / e2e_s / 1e6, "unit": UNIT,
+                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+                "wall_s": e2e_s, "scope": "scene lowering + upload + steps + far field + RCS readback"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+        "fp64_form": fp64,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--fp64-steps", type=int, default=200)
+    ap.add_argument("--cpu-sample", type=int, default=8, help="oracle steps timed for cpu_baseline (0: skip)")
+    ap.add_argument("--ref-budget", type=float, default=120.0, help="seconds of oracle work for --impl reference")
+    args = ap.parse_args()
+    world, rank, local = _dist()
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args, world, rank)
+        return
+    grp = _Group(world, local)
+    try:
+        ours_arm(args, world, rank, local, grp)
+    finally:
+        grp.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -143,7 +143,7 @@ typedef struct xfdtd_plan_desc {
   int32_t flags;                   /* XFDTD_FLAG_*                             */
   int32_t index_bytes;             /* 1 or 2                                   */
   int32_t n_materials;
-  int32_t reserved;
+  int32_t device;                  /* CUDA device ordinal the handle runs on   */
   const void *material_index;      /* [(nx+1)*(ny+1)*(nz+1)]                   */
   const double *coeff_table;       /* [n_materials * XFDTD_N_COEFF]            */
   xfdtd_cpml_axis cpml[3];
@@ -197,6 +197,8 @@ int xfdtd_profile(xfdtd_handle *h, int max, const char **names, double *ms, int6
 int xfdtd_profile_reset(xfdtd_handle *h);
 /* Kernel launches the engine enqueues per step for this plan. */
 int xfdtd_launches_per_step(xfdtd_handle *h, int *n);
+/* Bytes copied host->device and device->host by the handle so far. */
+int xfdtd_transfer_bytes(xfdtd_handle *h, int64_t *h2d, int64_t *d2h);
 /* Device bytes held by the handle. */
 int xfdtd_device_bytes(xfdtd_handle *h, int64_t *bytes);
 const char *xfdtd_last_error(xfdtd_handle *h);

@@ -19,9 +19,9 @@
  *                                          src/include/nffft/nffft_fd.h:39-50
  *   CurrentSource / VoltageSource(Cube, Orientation, R, Waveform),
  *   Resistor / Capacitor / Inductor(Cube, Axis, value)
- *                                          src/include/lumped_element/*.h
+ *                                          src/include/lumped_element/ (all)
  *   VoltageMonitor / CurrentMonitor(Cube, Orientation, dir, file)
- *                                          src/include/monitor/*.h
+ *                                          src/include/monitor/ (all)
  *   Simulation(cell_size, ..., float cfl)  src/include/simulation/simulation.h:27-66
  *
  * One addition has no reference counterpart: a voxel material raster

@@ -29,10 +29,14 @@ extern "C" {
 
 typedef struct xfdtd_sim xfdtd_sim;
 
+/* Bits 8..15 of the flags of xfdtd_sim_create carry the CUDA device ordinal. */
+#define XFDTD_SIM_DEVICE_SHIFT 8
+
 /* Builds the Simulation and its engine plan for total_steps steps.
- * precision: XFDTD_FP64 or XFDTD_FP32; flags: XFDTD_FLAG_*.  On failure *out
- * is still set (when non-null) so that xfdtd_sim_last_error can be read; it
- * must then be destroyed. */
+ * precision: XFDTD_FP64 or XFDTD_FP32; flags: XFDTD_FLAG_* |
+ * (device << XFDTD_SIM_DEVICE_SHIFT).  On failure *out is still set (when
+ * non-null) so that xfdtd_sim_last_error can be read; it must then be
+ * destroyed. */
 int xfdtd_sim_create(const xfdtd_scene_desc *scene, int64_t total_steps, int precision, int flags, xfdtd_sim **out);
 int xfdtd_sim_step(xfdtd_sim *s, int64_t n);
 int xfdtd_sim_info(xfdtd_sim *s, int64_t out_n[3], double *out_dt, int64_t *out_step);

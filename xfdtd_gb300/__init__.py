@@ -80,6 +80,7 @@ def libs():
         cu.xfdtd_profile_reset.argtypes = [C.c_void_p]
         cu.xfdtd_launches_per_step.argtypes = [C.c_void_p, P(C.c_int)]
         cu.xfdtd_device_bytes.argtypes = [C.c_void_p, P(C.c_int64)]
+        cu.xfdtd_transfer_bytes.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64)]
         cu.xfdtd_last_error.argtypes = [C.c_void_p]
         cu.xfdtd_last_error.restype = C.c_char_p
         cu.xfdtd_version.restype = C.c_char_p
@@ -100,14 +101,14 @@ class Simulation:
     """
 
     def __init__(self, sc: "scene.Scene", total_steps: int, precision: str = "fp64", graph: bool = True,
-                 profile: bool = False):
+                 profile: bool = False, device: int = 0):
         self.scene = sc
         self.total_steps = int(total_steps)
         self.precision = precision
         cu, ho = libs()
         self._desc = sc.desc()
         prec = FP64 if precision == "fp64" else FP32
-        flags = (FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0)
+        flags = (FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0) | (int(device) << 8)
         h = C.c_void_p()
         rc = ho.xfdtd_sim_create(C.byref(self._desc), self.total_steps, prec, flags, C.byref(h))
         self.h = h
@@ -228,6 +229,12 @@ class Simulation:
         n = C.c_int()
         self._check_engine(libs()[0].xfdtd_launches_per_step(self.engine, C.byref(n)))
         return n.value
+
+    def transfer_bytes(self):
+        """(host->device, device->host) bytes the engine has copied so far."""
+        a, b = C.c_int64(), C.c_int64()
+        self._check_engine(libs()[0].xfdtd_transfer_bytes(self.engine, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def device_bytes(self) -> int:
         b = C.c_int64()

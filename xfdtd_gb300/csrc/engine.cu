@@ -53,6 +53,7 @@ constexpr int kNumKernels = 7;
 
 struct xfdtd_handle {
   std::string err;
+  int device = 0;
   int precision = XFDTD_FP64;
   int idx_bytes = 1;
   int flags = 0;
@@ -65,6 +66,7 @@ struct xfdtd_handle {
   cudaStream_t stream = nullptr;
   std::vector<void *> allocs;
   size_t bytes = 0;
+  long long h2d = 0, d2h = 0;   // bytes copied host<->device
 
   void *F[6] = {};
   void *idx = nullptr;
@@ -147,6 +149,7 @@ struct xfdtd_handle {
   P *upload(const P *src, size_t count) {
     P *p = alloc<P>(count);
     if (count) XCHECK(cudaMemcpyAsync(p, src, count * sizeof(P), cudaMemcpyHostToDevice, stream));
+    h2d += static_cast<long long>(count * sizeof(P));
     return p;
   }
   // upload doubles, converting to the field precision
@@ -169,6 +172,7 @@ namespace {
 template <class F>
 int guarded(xfdtd_handle *h, F &&fn) {
   try {
+    if (h && h->stream) XCHECK(cudaSetDevice(h->device));
     fn();
     return XFDTD_OK;
   } catch (const Err &e) {
@@ -428,6 +432,9 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   if (!pl->material_index || !pl->coeff_table) invalid("material index and coefficient table are required");
   if (pl->total_steps < 1) invalid("total_steps must be positive");
   if (!(pl->dt > 0)) invalid("dt must be positive");
+  if (pl->device < 0) invalid("device ordinal must be >= 0");
+  h->device = pl->device;
+  XCHECK(cudaSetDevice(pl->device));
   h->precision = pl->precision;
   h->idx_bytes = pl->index_bytes;
   h->flags = pl->flags;
@@ -650,6 +657,7 @@ void read_comp(xfdtd_handle *h, int comp, double *out, long long len) {
   if (len != s[0] * s[1] * s[2]) invalid("length does not match the component shape");
   std::vector<T> buf(h->d.cells);
   XCHECK(cudaMemcpyAsync(buf.data(), h->F[comp], h->d.cells * sizeof(T), cudaMemcpyDeviceToHost, h->stream));
+  h->d2h += h->d.cells * static_cast<long long>(sizeof(T));
   XCHECK(cudaStreamSynchronize(h->stream));
   long long o = 0;
   for (long long i = 0; i < s[0]; ++i)
@@ -668,6 +676,7 @@ void write_comp(xfdtd_handle *h, int comp, const double *in, long long len) {
     for (long long j = 0; j < s[1]; ++j)
       for (long long k = 0; k < s[2]; ++k) buf[i * h->d.si + j * h->d.sj + k] = static_cast<T>(in[o++]);
   XCHECK(cudaMemcpyAsync(h->F[comp], buf.data(), h->d.cells * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+  h->h2d += h->d.cells * static_cast<long long>(sizeof(T));
   XCHECK(cudaStreamSynchronize(h->stream));
 }
 
@@ -798,6 +807,7 @@ int xfdtd_read_probes(xfdtd_handle *h, double *out, int64_t len) {
     if (len != static_cast<int64_t>(h->n_probes) * h->total) invalid("length must be n_probes * total_steps");
     if (!len) return;
     XCHECK(cudaMemcpyAsync(out, h->probe_out, len * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    h->d2h += len * static_cast<long long>(sizeof(double));
     XCHECK(cudaStreamSynchronize(h->stream));
   });
 }
@@ -810,6 +820,7 @@ int xfdtd_read_nffft(xfdtd_handle *h, int which, double *out, int64_t len) {
     if (len != 2 * h->acc_len[which]) invalid("length must be 2 * n_freq * face cells");
     std::vector<double2> buf(h->acc_len[which]);
     XCHECK(cudaMemcpyAsync(buf.data(), h->acc[which], buf.size() * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    h->d2h += static_cast<long long>(buf.size() * sizeof(double2));
     XCHECK(cudaStreamSynchronize(h->stream));
     if (which / 8 == 1) {  // Y faces: device [n][i][k] -> reference [n][k][i]
       const long long bx = h->nf_hi[0] - h->nf_lo[0], bz = h->nf_hi[2] - h->nf_lo[2];
@@ -838,9 +849,11 @@ int xfdtd_far_field(xfdtd_handle *h, int which, double *out, int64_t len) {
     if (which >= 0 && which < 8) {
       if (len != 2 * dirs) invalid("length must be 2 * n_freq * n_theta * n_phi");
       XCHECK(cudaMemcpyAsync(out, h->ff_out[which], dirs * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+      h->d2h += dirs * static_cast<long long>(sizeof(double2));
     } else if (which == 8 || which == 9) {
       if (len != dirs) invalid("length must be n_freq * n_theta * n_phi");
       XCHECK(cudaMemcpyAsync(out, h->ff_power[which - 8], dirs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      h->d2h += dirs * static_cast<long long>(sizeof(double));
     } else {
       invalid("far-field output must be 0..9");
     }
@@ -900,6 +913,13 @@ int xfdtd_launches_per_step(xfdtd_handle *h, int *n) {
   return XFDTD_OK;
 }
 
+int xfdtd_transfer_bytes(xfdtd_handle *h, int64_t *h2d, int64_t *d2h) {
+  if (!h) return XFDTD_ERR_STATE;
+  if (h2d) *h2d = h->h2d;
+  if (d2h) *d2h = h->d2h;
+  return XFDTD_OK;
+}
+
 int xfdtd_device_bytes(xfdtd_handle *h, int64_t *bytes) {
   if (!h || !bytes) return XFDTD_ERR_STATE;
   *bytes = static_cast<int64_t>(h->bytes);
@@ -910,7 +930,10 @@ const char *xfdtd_last_error(xfdtd_handle *h) { return h ? h->err.c_str() : "nul
 
 void xfdtd_destroy(xfdtd_handle *h) {
   if (!h) return;
-  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->stream) {
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+  }
   delete h;
 }
 

@@ -544,6 +544,7 @@ class Simulation {
   Precision getPrecision() const { return _precision; }
   void setUseGraph(bool g) { _use_graph = g; }
   void setProfile(bool p) { _profile = p; }
+  void setDevice(int d) { _device = d; }
   // One material per cell, applied after all objects (see xfdtd_scene.h).
   void setVoxelMaterials(std::vector<Material> materials, std::vector<uint16_t> index, std::array<size_t, 3> shape);
   // Split run(): init once, step in pieces, read state, output at the end.
@@ -585,6 +586,7 @@ class Simulation {
   Precision _precision{Precision::FP64};
   bool _use_graph{true};
   bool _profile{false};
+  int _device{0};
   size_t _total{0};
   size_t _nx{0}, _ny{0}, _nz{0};
   double _dt{0};

@@ -451,6 +451,7 @@ void Simulation::init(size_t total_time_steps) {
   plan.total_steps = static_cast<int64_t>(_total);
   plan.flags = (_use_graph ? XFDTD_FLAG_GRAPH : 0) | (_profile ? XFDTD_FLAG_PROFILE : 0);
   plan.index_bytes = index_bytes;
+  plan.device = _device;
   plan.n_materials = static_cast<int32_t>(table.size());
   plan.material_index = idx_bytes.data();
   plan.coeff_table = coeff.data();

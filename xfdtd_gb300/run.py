@@ -1,0 +1,50 @@
+"""Command-line runner for the built-in configurations.
+
+    python -m xfdtd_gb300.run --config dielectric_sphere --steps 20 --precision fp32
+    python -m xfdtd_gb300.run --config pec_sphere_rcs --steps 800 --out out_dir
+
+Builds the scene, runs it on the GPU engine and prints one JSON line with
+the grid, the device time per step and Mcell-updates/s; with --out it also
+writes the reference's .npy outputs (far field, monitors).  It is also the
+small driver that profilers wrap.
+"""
+import argparse
+import json
+import os
+import time
+
+from . import Simulation, build, configs
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", default="dielectric_sphere", choices=sorted(configs.CONFIGS))
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--scale", type=int, default=1)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--out", default=None)
+    args = ap.parse_args()
+    build()
+    sc, steps = configs.CONFIGS[args.config](scale=args.scale)
+    if args.steps is not None:
+        steps = args.steps
+    if args.out and sc.nffft is not None:
+        sc.nffft.output_dir_path = args.out
+    t0 = time.perf_counter()
+    sim = Simulation(sc, steps, precision=args.precision, graph=not args.no_graph)
+    t1 = time.perf_counter()
+    ms = sim.step_timed(steps)
+    sim.synchronize()
+    cells = sim.n[0] * sim.n[1] * sim.n[2]
+    res = {"config": args.config, "grid": sim.n, "steps": steps, "precision": args.precision,
+           "setup_s": t1 - t0, "ms_per_step": ms / steps, "Mcell_updates_per_s": cells * steps / ms / 1e3,
+           "device_bytes": sim.device_bytes()}
+    if args.out:
+        os.makedirs(args.out, exist_ok=True)
+        sim.output()
+    print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()
