@@ -271,6 +271,7 @@ def ours_arm(args, world, rank, local, grp):
     clocks = clock.stop()
     max_ms = grp.max(ms)
     prof = sim.profile()
+    variants = sim.kernel_variants()
     launches = sim.launches_per_step() * args.steps
     sim.check_finite()
     value = aggregate_value(cells, args.steps, world, max_ms)
@@ -334,6 +335,9 @@ def ours_arm(args, world, rank, local, grp):
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
                      "algorithmic_bytes_per_launch": alg, "launch_ms": dom_ms / dom_n},
         "kernel_shares": shares,
+        "autotuned_variants": {"update_e": variants["e"], "update_h": variants["h"],
+                               "trial_ms_e": [round(v, 4) for v in variants["trials_e"]],
+                               "trial_ms_h": [round(v, 4) for v in variants["trials_h"]]},
         "e2e": {"value": cells * args.steps * world / e2e_s / 1e6, "unit": UNIT,
                 "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
                 "wall_s": e2e_s, "scope": "scene lowering + upload + steps + far field + RCS readback"},

@@ -62,7 +62,8 @@ enum { XFDTD_FP64 = 0, XFDTD_FP32 = 1 };
 /* Plan flags. */
 enum {
   XFDTD_FLAG_GRAPH = 1,      /* replay the step loop from a captured CUDA graph */
-  XFDTD_FLAG_PROFILE = 2     /* time every kernel launch with CUDA events        */
+  XFDTD_FLAG_PROFILE = 2,    /* time every kernel launch with CUDA events        */
+  XFDTD_FLAG_AUTOTUNE = 4    /* pick the volume-kernel variants by timing at create */
 };
 
 /* The 18 coefficients of one table entry, in this order (the reference's
@@ -195,6 +196,15 @@ int xfdtd_check_finite(xfdtd_handle *h);
  * names[i] (static strings), total milliseconds and launch counts. */
 int xfdtd_profile(xfdtd_handle *h, int max, const char **names, double *ms, int64_t *launches, int *count);
 int xfdtd_profile_reset(xfdtd_handle *h);
+/* Times every variant (register cap x block shape) of the E and H volume
+ * kernels and keeps the fastest for each.  Only before the first step: the
+ * trials run on the all-zero initial state and leave it unchanged.  All
+ * variants compute bitwise-identical results. */
+int xfdtd_autotune(xfdtd_handle *h, int trials);
+/* Number of variants, the ones in use, and the last trial times
+ * (trial_ms[2*v] for E, [2*v+1] for H; 0 where not tried). */
+int xfdtd_kernel_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h, double *trial_ms);
+int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant);
 /* Kernel launches the engine enqueues per step for this plan. */
 int xfdtd_launches_per_step(xfdtd_handle *h, int *n);
 /* Bytes copied host->device and device->host by the handle so far. */

@@ -160,3 +160,38 @@ def test_invalid_plans_rejected():
     sc2.tfsf.distance_x = 40   # larger than half the grid: empty box
     with pytest.raises(X.EngineError):
         X.Simulation(sc2, st2)
+
+
+def test_every_kernel_variant_is_bitwise_identical():
+    """The autotuner's variants (register caps x block shapes) change only
+    scheduling: fields after the same steps are bitwise equal."""
+    for precision in ("fp64", "fp32"):
+        sc, st = scenes.oblique(steps=60)
+        ref = X.Simulation(sc, st, precision=precision, autotune=False)
+        ref.step(st)
+        want = [ref.read_field(c) for c in range(6)]
+        info = ref.kernel_variants()
+        tried = 0
+        for v in range(info["n"]):
+            g = X.Simulation(sc, st, precision=precision, autotune=False)
+            try:
+                g.set_kernel_variant(v, v)
+            except X.EngineError:
+                continue   # not offered for this precision
+            tried += 1
+            g.step(st)
+            for c in range(6):
+                assert np.array_equal(g.read_field(c), want[c]), (precision, v, c)
+        assert tried >= 4
+
+
+def test_autotune_leaves_state_unchanged():
+    sc, st = scenes.pec_sphere(steps=40)
+    a = X.Simulation(sc, st, autotune=True)
+    b = X.Simulation(sc, st, autotune=False)
+    a.step(st)
+    b.step(st)
+    for c in range(6):
+        assert np.array_equal(a.read_field(c), b.read_field(c))
+    t = a.kernel_variants()
+    assert max(t["trials_e"]) > 0 and max(t["trials_h"]) > 0

@@ -25,7 +25,7 @@ from .scene import (  # noqa: F401  (re-exported: the reference's scene API)
 )
 
 FP64, FP32 = 0, 1
-FLAG_GRAPH, FLAG_PROFILE = 1, 2
+FLAG_GRAPH, FLAG_PROFILE, FLAG_AUTOTUNE = 1, 2, 4
 STATUS = {0: "ok", 1: "invalid plan", 2: "CUDA error", 3: "out of device memory", 4: "timeout",
           5: "non-finite value", 6: "device check", 7: "bad state"}
 
@@ -81,6 +81,9 @@ def libs():
         cu.xfdtd_launches_per_step.argtypes = [C.c_void_p, P(C.c_int)]
         cu.xfdtd_device_bytes.argtypes = [C.c_void_p, P(C.c_int64)]
         cu.xfdtd_transfer_bytes.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64)]
+        cu.xfdtd_autotune.argtypes = [C.c_void_p, C.c_int]
+        cu.xfdtd_kernel_variants.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int), dp]
+        cu.xfdtd_set_kernel_variant.argtypes = [C.c_void_p, C.c_int, C.c_int]
         cu.xfdtd_last_error.argtypes = [C.c_void_p]
         cu.xfdtd_last_error.restype = C.c_char_p
         cu.xfdtd_version.restype = C.c_char_p
@@ -101,14 +104,15 @@ class Simulation:
     """
 
     def __init__(self, sc: "scene.Scene", total_steps: int, precision: str = "fp64", graph: bool = True,
-                 profile: bool = False, device: int = 0):
+                 profile: bool = False, device: int = 0, autotune: bool = True):
         self.scene = sc
         self.total_steps = int(total_steps)
         self.precision = precision
         cu, ho = libs()
         self._desc = sc.desc()
         prec = FP64 if precision == "fp64" else FP32
-        flags = (FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0) | (int(device) << 8)
+        flags = ((FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0)
+                 | (FLAG_AUTOTUNE if autotune else 0) | (int(device) << 8))
         h = C.c_void_p()
         rc = ho.xfdtd_sim_create(C.byref(self._desc), self.total_steps, prec, flags, C.byref(h))
         self.h = h
@@ -229,6 +233,18 @@ class Simulation:
         n = C.c_int()
         self._check_engine(libs()[0].xfdtd_launches_per_step(self.engine, C.byref(n)))
         return n.value
+
+    def kernel_variants(self) -> dict:
+        """Volume-kernel variant in use for E and H and the autotuner's trial
+        times (ms per launch; 0 = not tried for this precision)."""
+        n, ce, ch = C.c_int(), C.c_int(), C.c_int()
+        ms = (C.c_double * 64)()
+        self._check_engine(libs()[0].xfdtd_kernel_variants(self.engine, C.byref(n), C.byref(ce), C.byref(ch), ms))
+        return {"e": ce.value, "h": ch.value, "n": n.value,
+                "trials_e": [ms[2 * v] for v in range(n.value)], "trials_h": [ms[2 * v + 1] for v in range(n.value)]}
+
+    def set_kernel_variant(self, e_variant: int, h_variant: int):
+        self._check_engine(libs()[0].xfdtd_set_kernel_variant(self.engine, int(e_variant), int(h_variant)))
 
     def transfer_bytes(self):
         """(host->device, device->host) bytes the engine has copied so far."""

@@ -61,7 +61,6 @@ struct VolParams {
   T dl[3];
   TfsfDev tf;
   const long long *step;
-  int chunk;           // planes of i per block
 };
 
 __device__ __forceinline__ double tfsf_interp(const double *v, double projection) {

@@ -116,6 +116,10 @@ struct xfdtd_handle {
   int *d_status = nullptr;
   int *d_flag = nullptr;
 
+  // volume-kernel variants (autotuned)
+  int var_e = 0, var_h = 0;
+  float tune_ms[2][16] = {};
+
   // graph replay
   cudaGraphExec_t gexec = nullptr;
   int graph_steps = 0;
@@ -256,31 +260,117 @@ xg::VolParams<T, I> vol_params(xfdtd_handle *h) {
   return p;
 }
 
-constexpr int kBlockX = 32, kBlockY = 8;
+// Volume-kernel variants the autotuner chooses from: a register cap (the
+// minimum number of resident 256-thread blocks per SM asked of the register
+// allocator) and a block shape (k fastest; 32 or 64 along k for full
+// 128-byte rows).  Every variant computes the same per-cell arithmetic.
+struct Variant {
+  int minb;
+  int bx, by, bz;
+};
+constexpr Variant kVariants[] = {
+    {1, 32, 4, 2}, {1, 32, 8, 1}, {1, 64, 2, 2}, {4, 32, 4, 2}, {4, 32, 8, 1},
+    {5, 32, 4, 2}, {5, 64, 4, 1}, {2, 32, 4, 2}, {3, 32, 4, 2},
+};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-int chunk_planes(const xfdtd_handle *h) {
-  // Enough (j,k) columns x i-chunks to keep >= 4 blocks per SM resident.
-  long long cols = static_cast<long long>((h->d.nz + kBlockX) / kBlockX) * ((h->d.ny + kBlockY) / kBlockY);
-  long long target_blocks = 152LL * 8;
-  long long nchunks = std::max<long long>(1, (target_blocks + cols - 1) / cols);
-  int chunk = static_cast<int>((h->d.nx + 1 + nchunks - 1) / nchunks);
-  return std::max(chunk, 8);
+// FP32 kernels try register caps of 4 or 5 blocks per SM, FP64 kernels
+// (more registers per thread) 2 or 3; both try the uncapped build.
+bool variant_allowed(const Variant &v, bool fp64) {
+  if (v.minb == 1) return true;
+  return fp64 ? (v.minb == 2 || v.minb == 3) : (v.minb == 4 || v.minb == 5);
+}
+
+template <typename T, typename I, int MB>
+void smem_attr_mb(int bytes) {
+  XCHECK(cudaFuncSetAttribute(xg::k_update_e<T, I, true, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_update_h<T, I, true, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+}
+
+// Opts every shared-memory-table instantiation in to `bytes` of dynamic
+// shared memory (needed above 48 KB).
+template <typename T, typename I>
+void smem_attr(int bytes) {
+  smem_attr_mb<T, I, 1>(bytes);
+  smem_attr_mb<T, I, 2>(bytes);
+  smem_attr_mb<T, I, 3>(bytes);
+  smem_attr_mb<T, I, 4>(bytes);
+  smem_attr_mb<T, I, 5>(bytes);
+}
+
+template <typename T, typename I, bool S, int MB>
+void launch_vol_mb(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, dim3 grid, dim3 block) {
+  const size_t smem = S ? h->smem_bytes : 0;
+  if (e_side) xg::k_update_e<T, I, S, MB><<<grid, block, smem, h->stream>>>(p);
+  else xg::k_update_h<T, I, S, MB><<<grid, block, smem, h->stream>>>(p);
+}
+
+template <typename T, typename I, bool S>
+void launch_vol_s(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, int var) {
+  const Variant &v = kVariants[var];
+  dim3 block(v.bx, v.by, v.bz);
+  dim3 grid((h->d.nz + v.bx) / v.bx, (h->d.ny + v.by) / v.by, (h->d.nx + v.bz) / v.bz);
+  switch (v.minb) {
+    case 1: launch_vol_mb<T, I, S, 1>(h, p, e_side, grid, block); break;
+    case 2: launch_vol_mb<T, I, S, 2>(h, p, e_side, grid, block); break;
+    case 3: launch_vol_mb<T, I, S, 3>(h, p, e_side, grid, block); break;
+    case 4: launch_vol_mb<T, I, S, 4>(h, p, e_side, grid, block); break;
+    default: launch_vol_mb<T, I, S, 5>(h, p, e_side, grid, block); break;
+  }
 }
 
 template <typename T, typename I>
-void launch_volume(xfdtd_handle *h, bool e_side) {
+void launch_volume(xfdtd_handle *h, bool e_side, int var = -1) {
   auto p = vol_params<T, I>(h);
-  p.chunk = chunk_planes(h);
-  dim3 block(kBlockX, kBlockY, 1);
-  dim3 grid((h->d.nz + kBlockX) / kBlockX, (h->d.ny + kBlockY) / kBlockY, (h->d.nx + 1 + p.chunk - 1) / p.chunk);
-  if (h->smem_table) {
-    if (e_side) xg::k_update_e<T, I, true><<<grid, block, h->smem_bytes, h->stream>>>(p);
-    else xg::k_update_h<T, I, true><<<grid, block, h->smem_bytes, h->stream>>>(p);
-  } else {
-    if (e_side) xg::k_update_e<T, I, false><<<grid, block, 0, h->stream>>>(p);
-    else xg::k_update_h<T, I, false><<<grid, block, 0, h->stream>>>(p);
-  }
+  if (var < 0) var = e_side ? h->var_e : h->var_h;
+  if (h->smem_table) launch_vol_s<T, I, true>(h, p, e_side, var);
+  else launch_vol_s<T, I, false>(h, p, e_side, var);
   XCHECK(cudaGetLastError());
+}
+
+// Times every variant of the E and H kernels on the handle's current state
+// and keeps the fastest.  Run before the first step, when every field and
+// psi is zero: the volume kernels then write zeros back (the TFSF buffers
+// they read are zero too), so the trials leave the simulation unchanged.
+template <typename T, typename I>
+void autotune_t(xfdtd_handle *h, int trials) {
+  cudaEvent_t a, b;
+  XCHECK(cudaEventCreate(&a));
+  XCHECK(cudaEventCreate(&b));
+  for (int side = 0; side < 2; ++side) {
+    float best = 1e30f;
+    int best_v = 0;
+    for (int v = 0; v < kNumVariants; ++v) {
+      if (!variant_allowed(kVariants[v], sizeof(T) == 8)) continue;
+      launch_volume<T, I>(h, side == 0, v);   // warm-up / module load
+      XCHECK(cudaEventRecord(a, h->stream));
+      for (int r = 0; r < trials; ++r) launch_volume<T, I>(h, side == 0, v);
+      XCHECK(cudaEventRecord(b, h->stream));
+      XCHECK(cudaEventSynchronize(b));
+      float ms = 0;
+      XCHECK(cudaEventElapsedTime(&ms, a, b));
+      h->tune_ms[side][v] = ms / trials;
+      if (ms < best) {
+        best = ms;
+        best_v = v;
+      }
+    }
+    if (side == 0) h->var_e = best_v;
+    else h->var_h = best_v;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+}
+
+void autotune(xfdtd_handle *h, int trials) {
+  if (h->host_step != 0) throw Err{XFDTD_ERR_STATE, "autotuning runs before the first step only"};
+  if (h->precision == XFDTD_FP64) {
+    if (h->idx_bytes == 1) autotune_t<double, uint8_t>(h, trials);
+    else autotune_t<double, uint16_t>(h, trials);
+  } else {
+    if (h->idx_bytes == 1) autotune_t<float, uint8_t>(h, trials);
+    else autotune_t<float, uint16_t>(h, trials);
+  }
 }
 
 template <typename T>
@@ -482,15 +572,11 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     // opt in to more than 48 KB of dynamic shared memory for the table
     int bytes = static_cast<int>(h->smem_bytes);
     if (h->precision == XFDTD_FP64) {
-      XCHECK(cudaFuncSetAttribute(xg::k_update_e<double, uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-      XCHECK(cudaFuncSetAttribute(xg::k_update_h<double, uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-      XCHECK(cudaFuncSetAttribute(xg::k_update_e<double, uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-      XCHECK(cudaFuncSetAttribute(xg::k_update_h<double, uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+      if (h->idx_bytes == 1) smem_attr<double, uint8_t>(bytes);
+      else smem_attr<double, uint16_t>(bytes);
     } else {
-      XCHECK(cudaFuncSetAttribute(xg::k_update_e<float, uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-      XCHECK(cudaFuncSetAttribute(xg::k_update_h<float, uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-      XCHECK(cudaFuncSetAttribute(xg::k_update_e<float, uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-      XCHECK(cudaFuncSetAttribute(xg::k_update_h<float, uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+      if (h->idx_bytes == 1) smem_attr<float, uint8_t>(bytes);
+      else smem_attr<float, uint16_t>(bytes);
     }
   }
 
@@ -648,6 +734,7 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   h->d_status = h->alloc<int>(1);
   h->d_flag = h->alloc<int>(1);
   XCHECK(cudaStreamSynchronize(h->stream));
+  if (pl->flags & XFDTD_FLAG_AUTOTUNE) autotune(h, 3);
 }
 
 template <typename T>
@@ -903,6 +990,40 @@ int xfdtd_profile_reset(xfdtd_handle *h) {
     for (int q = 0; q < kNumKernels; ++q) {
       h->prof_ms[q] = 0;
       h->prof_n[q] = 0;
+    }
+  });
+}
+
+int xfdtd_autotune(xfdtd_handle *h, int trials) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] { autotune(h, trials > 0 ? trials : 3); });
+}
+
+int xfdtd_kernel_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h, double *trial_ms) {
+  if (!h) return XFDTD_ERR_STATE;
+  if (n) *n = kNumVariants;
+  if (current_e) *current_e = h->var_e;
+  if (current_h) *current_h = h->var_h;
+  if (trial_ms)
+    for (int v = 0; v < kNumVariants; ++v) {
+      trial_ms[2 * v] = h->tune_ms[0][v];
+      trial_ms[2 * v + 1] = h->tune_ms[1][v];
+    }
+  return XFDTD_OK;
+}
+
+int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    const bool fp64 = h->precision == XFDTD_FP64;
+    if (e_variant < 0 || e_variant >= kNumVariants || h_variant < 0 || h_variant >= kNumVariants ||
+        !variant_allowed(kVariants[e_variant], fp64) || !variant_allowed(kVariants[h_variant], fp64))
+      invalid("kernel variant not available for this precision");
+    h->var_e = e_variant;
+    h->var_h = h_variant;
+    if (h->gexec) {   // the captured graph holds the old launches
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
     }
   });
 }

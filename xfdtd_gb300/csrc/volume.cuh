@@ -1,9 +1,11 @@
 // volume.cuh -- the fused Yee E and H kernels.
 //
-// One thread owns one (j, k) column of a chunk of i-planes and marches along
-// i (the outermost, slowest axis of the row-major layout), carrying the
-// previous plane's H (E kernel) or the next plane's E (H kernel) in
-// registers.  Per cell it applies, in the reference's order:
+// One thread per cell (i, j, k) of the (nx+1)(ny+1)(nz+1) box, k on the
+// fastest thread axis so that a warp reads 32 contiguous values.  The
+// curl operands are read-only during the kernel (H in the E kernel, E in the
+// H kernel), so they go through the read-only data path; neighbours along
+// k and j hit L1, neighbours along i (another block) hit L2.  Per cell the
+// kernel applies, in the reference's order:
 //
 //   E:  updateE main update          src/simulation/simulation_update.cpp:170-196
 //       TFSF3D::updateE faces        src/tfsf/tfsf_3d.cpp:299-411
@@ -30,14 +32,17 @@ __device__ __forceinline__ void add_corr(T &v, double corr) {
   v = static_cast<T>(static_cast<double>(v) + corr);
 }
 
-template <typename T, typename I, bool SMEM_TABLE>
-__global__ void __launch_bounds__(256) k_update_e(VolParams<T, I> p) {
+// MINB: minimum resident blocks per SM requested from the register
+// allocator (1 = no cap); the autotuner in engine.cu picks it per plan.
+template <typename T, typename I, bool SMEM_TABLE, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_update_e(VolParams<T, I> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const T *tab = p.table;
   int ts = 18;
   if (SMEM_TABLE) {
     T *st = reinterpret_cast<T *>(smem_raw);
-    const int nt = blockDim.x * blockDim.y, tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nt = blockDim.x * blockDim.y * blockDim.z;
+    const int tid = (threadIdx.z * blockDim.y + threadIdx.y) * blockDim.x + threadIdx.x;
     for (int q = tid; q < p.n_mat * 9; q += nt) st[q] = p.table[(q / 9) * 18 + (q % 9)];
     __syncthreads();
     tab = st;
@@ -45,13 +50,15 @@ __global__ void __launch_bounds__(256) k_update_e(VolParams<T, I> p) {
   }
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = blockIdx.z * blockDim.z + threadIdx.z;
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
-  if (k > nz || j > ny) return;
+  if (k > nz || j > ny || i > nx) return;
   const long long si = p.d.si, sj = p.d.sj;
-  const int i0 = blockIdx.z * p.chunk;
-  const int i1 = min(i0 + p.chunk, nx + 1);
+  const T *__restrict__ Hx = p.H[0];
+  const T *__restrict__ Hy = p.H[1];
+  const T *__restrict__ Hz = p.H[2];
 
-  // Per-column CPML data for the y and z axes (E-located indices).
+  // CPML data for the y and z axes (E-located indices).
   const int ys = p.cp[1].n_layers ? p.cp[1].slot_e[j] : -1;
   const int zs = p.cp[2].n_layers ? p.cp[2].slot_e[k] : -1;
   T by = 0, ay = 0, rky = 1, bz = 0, az = 0, rkz = 1;
@@ -69,17 +76,16 @@ __global__ void __launch_bounds__(256) k_update_e(VolParams<T, I> p) {
     hinc = tf.inc + ((t + 1) & 1) * 6 * tf.L;   // incident H of the previous step
   }
 
-  long long b = static_cast<long long>(i0) * si + static_cast<long long>(j) * sj + k;
-  T hy_im1 = 0, hz_im1 = 0;
-  if (i0 > 0) { hy_im1 = p.H[1][b - si]; hz_im1 = p.H[2][b - si]; }
-
-  for (int i = i0; i < i1; ++i, b += si) {
-    const T hx = p.H[0][b], hy = p.H[1][b], hz = p.H[2][b];
-    const T hx_k = k > 0 ? p.H[0][b - 1] : T(0);
-    const T hy_k = k > 0 ? p.H[1][b - 1] : T(0);
-    const T hx_j = j > 0 ? p.H[0][b - sj] : T(0);
-    const T hz_j = j > 0 ? p.H[2][b - sj] : T(0);
-    const T *c = tab + static_cast<long long>(p.idx[b]) * ts;
+  const long long b = static_cast<long long>(i) * si + static_cast<long long>(j) * sj + k;
+  {
+    const T hx = __ldg(Hx + b), hy = __ldg(Hy + b), hz = __ldg(Hz + b);
+    const T hx_k = k > 0 ? __ldg(Hx + b - 1) : T(0);
+    const T hy_k = k > 0 ? __ldg(Hy + b - 1) : T(0);
+    const T hx_j = j > 0 ? __ldg(Hx + b - sj) : T(0);
+    const T hz_j = j > 0 ? __ldg(Hz + b - sj) : T(0);
+    const T hy_im1 = i > 0 ? __ldg(Hy + b - si) : T(0);
+    const T hz_im1 = i > 0 ? __ldg(Hz + b - si) : T(0);
+    const T *c = tab + static_cast<long long>(__ldg(p.idx + b)) * ts;
     const int xs = p.cp[0].n_layers ? p.cp[0].slot_e[i] : -1;
     T bx = 0, ax = 0, rkx = 1;
     if (xs >= 0) { bx = p.cp[0].b_e[i]; ax = p.cp[0].a_e[i]; rkx = p.cp[0].rk_e[i]; }
@@ -225,19 +231,18 @@ __global__ void __launch_bounds__(256) k_update_e(VolParams<T, I> p) {
       }
       if (w) p.E[2][b] = e;
     }
-    hy_im1 = hy;
-    hz_im1 = hz;
   }
 }
 
-template <typename T, typename I, bool SMEM_TABLE>
-__global__ void __launch_bounds__(256) k_update_h(VolParams<T, I> p) {
+template <typename T, typename I, bool SMEM_TABLE, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_update_h(VolParams<T, I> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const T *tab = p.table + 9;
   int ts = 18;
   if (SMEM_TABLE) {
     T *st = reinterpret_cast<T *>(smem_raw);
-    const int nt = blockDim.x * blockDim.y, tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nt = blockDim.x * blockDim.y * blockDim.z;
+    const int tid = (threadIdx.z * blockDim.y + threadIdx.y) * blockDim.x + threadIdx.x;
     for (int q = tid; q < p.n_mat * 9; q += nt) st[q] = p.table[(q / 9) * 18 + 9 + (q % 9)];
     __syncthreads();
     tab = st;
@@ -245,11 +250,13 @@ __global__ void __launch_bounds__(256) k_update_h(VolParams<T, I> p) {
   }
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = blockIdx.z * blockDim.z + threadIdx.z;
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
-  if (k > nz || j > ny) return;
+  if (k > nz || j > ny || i > nx) return;
   const long long si = p.d.si, sj = p.d.sj;
-  const int i0 = blockIdx.z * p.chunk;
-  const int i1 = min(i0 + p.chunk, nx + 1);
+  const T *__restrict__ Ex = p.E[0];
+  const T *__restrict__ Ey = p.E[1];
+  const T *__restrict__ Ez = p.E[2];
 
   const int ys = p.cp[1].n_layers ? p.cp[1].slot_h[j] : -1;
   const int zs = p.cp[2].n_layers ? p.cp[2].slot_h[k] : -1;
@@ -262,18 +269,16 @@ __global__ void __launch_bounds__(256) k_update_h(VolParams<T, I> p) {
   const double *einc = nullptr;
   if (tf.enabled) einc = tf.inc + ((*p.step) & 1) * 6 * tf.L;   // incident E of this step
 
-  long long b = static_cast<long long>(i0) * si + static_cast<long long>(j) * sj + k;
-  T ey_i = p.E[1][b], ez_i = p.E[2][b];
-
-  for (int i = i0; i < i1; ++i, b += si) {
-    const T ex = p.E[0][b];
-    const T ey_ip = i < nx ? p.E[1][b + si] : T(0);
-    const T ez_ip = i < nx ? p.E[2][b + si] : T(0);
-    const T ex_kp = k < nz ? p.E[0][b + 1] : T(0);
-    const T ey_kp = k < nz ? p.E[1][b + 1] : T(0);
-    const T ex_jp = j < ny ? p.E[0][b + sj] : T(0);
-    const T ez_jp = j < ny ? p.E[2][b + sj] : T(0);
-    const T *c = tab + static_cast<long long>(p.idx[b]) * ts;
+  const long long b = static_cast<long long>(i) * si + static_cast<long long>(j) * sj + k;
+  {
+    const T ex = __ldg(Ex + b), ey_i = __ldg(Ey + b), ez_i = __ldg(Ez + b);
+    const T ey_ip = i < nx ? __ldg(Ey + b + si) : T(0);
+    const T ez_ip = i < nx ? __ldg(Ez + b + si) : T(0);
+    const T ex_kp = k < nz ? __ldg(Ex + b + 1) : T(0);
+    const T ey_kp = k < nz ? __ldg(Ey + b + 1) : T(0);
+    const T ex_jp = j < ny ? __ldg(Ex + b + sj) : T(0);
+    const T ez_jp = j < ny ? __ldg(Ez + b + sj) : T(0);
+    const T *c = tab + static_cast<long long>(__ldg(p.idx + b)) * ts;
     const int xs = p.cp[0].n_layers ? p.cp[0].slot_h[i] : -1;
     T bx = 0, ax = 0, rkx = 1;
     if (xs >= 0) { bx = p.cp[0].b_m[i]; ax = p.cp[0].a_m[i]; rkx = p.cp[0].rk_m[i]; }
@@ -418,8 +423,6 @@ __global__ void __launch_bounds__(256) k_update_h(VolParams<T, I> p) {
       }
       if (w) p.H[2][b] = h;
     }
-    ey_i = ey_ip;
-    ez_i = ez_ip;
   }
 }
 

@@ -545,6 +545,8 @@ class Simulation {
   void setUseGraph(bool g) { _use_graph = g; }
   void setProfile(bool p) { _profile = p; }
   void setDevice(int d) { _device = d; }
+  // Time the volume-kernel variants at init and keep the fastest (default on).
+  void setAutotune(bool a) { _autotune = a; }
   // One material per cell, applied after all objects (see xfdtd_scene.h).
   void setVoxelMaterials(std::vector<Material> materials, std::vector<uint16_t> index, std::array<size_t, 3> shape);
   // Split run(): init once, step in pieces, read state, output at the end.
@@ -587,6 +589,7 @@ class Simulation {
   bool _use_graph{true};
   bool _profile{false};
   int _device{0};
+  bool _autotune{true};
   size_t _total{0};
   size_t _nx{0}, _ny{0}, _nz{0};
   double _dt{0};
