@@ -61,7 +61,14 @@ struct VolParams {
   T dl[3];
   TfsfDev tf;
   const long long *step;
+  const uint8_t *flags[3];   // per-axis index flags (kSpecialE / kSpecialH)
 };
+
+// Index flags: an index needs the general per-cell path of the E (H) kernel
+// when it is an outer wall, lies in a CPML slab or on a TFSF face plane of
+// that side; a cell whose three indices carry no flag takes the fast path.
+constexpr uint8_t kSpecialE = 1;
+constexpr uint8_t kSpecialH = 2;
 
 __device__ __forceinline__ double tfsf_interp(const double *v, double projection) {
   // TFSF3D::getIncident*, src/tfsf/tfsf_3d.cpp:413-483

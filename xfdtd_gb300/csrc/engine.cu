@@ -46,8 +46,9 @@ struct Err {
                 std::string(#call) + ": " + cudaGetErrorString(e_)};                    \
   } while (0)
 
-const char *kKernelNames[] = {"tfsf_aux", "update_e", "lumped_e", "update_h", "nffft", "probes", "advance"};
-constexpr int kNumKernels = 7;
+const char *kKernelNames[] = {"tfsf_aux", "update_e", "lumped_e", "update_h", "nffft",
+                              "probes",   "advance",  "tfsf_e",   "tfsf_h"};
+constexpr int kNumKernels = 9;
 
 }  // namespace
 
@@ -78,6 +79,7 @@ struct xfdtd_handle {
   // CPML
   int L[3] = {0, 0, 0};
   int *slot_e[3] = {}, *slot_h[3] = {};
+  uint8_t *axis_flags[3] = {};  // per-axis fast-path flags
   void *prof[3][6] = {};   // b_e a_e rk_e b_m a_m rk_m (precision T)
   void *psi[12] = {};      // ex_y ex_z ey_x ey_z ez_x ez_y hx_y hx_z hy_x hy_z hz_x hz_y
 
@@ -257,6 +259,7 @@ xg::VolParams<T, I> vol_params(xfdtd_handle *h) {
   }
   p.tf.inc = h->tf_inc;
   p.step = h->d_step;
+  for (int a = 0; a < 3; ++a) p.flags[a] = h->axis_flags[a];
   return p;
 }
 
@@ -269,16 +272,16 @@ struct Variant {
   int bx, by, bz;
 };
 constexpr Variant kVariants[] = {
-    {1, 32, 4, 2}, {1, 32, 8, 1}, {1, 64, 2, 2}, {4, 32, 4, 2}, {4, 32, 8, 1},
-    {5, 32, 4, 2}, {5, 64, 4, 1}, {2, 32, 4, 2}, {3, 32, 4, 2},
+    {1, 32, 4, 2}, {1, 32, 8, 1}, {1, 64, 2, 2}, {6, 32, 4, 2},
+    {6, 32, 8, 1}, {8, 32, 4, 2}, {8, 32, 8, 1}, {8, 64, 4, 1},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-// FP32 kernels try register caps of 4 or 5 blocks per SM, FP64 kernels
-// (more registers per thread) 2 or 3; both try the uncapped build.
+// Every variant is offered in both precisions: uncapped, and capped for 6
+// or 8 resident blocks (75% / 100% thread occupancy).
 bool variant_allowed(const Variant &v, bool fp64) {
-  if (v.minb == 1) return true;
-  return fp64 ? (v.minb == 2 || v.minb == 3) : (v.minb == 4 || v.minb == 5);
+  (void)fp64;
+  return v.minb == 1 || v.minb == 6 || v.minb == 8;
 }
 
 template <typename T, typename I, int MB>
@@ -292,10 +295,8 @@ void smem_attr_mb(int bytes) {
 template <typename T, typename I>
 void smem_attr(int bytes) {
   smem_attr_mb<T, I, 1>(bytes);
-  smem_attr_mb<T, I, 2>(bytes);
-  smem_attr_mb<T, I, 3>(bytes);
-  smem_attr_mb<T, I, 4>(bytes);
-  smem_attr_mb<T, I, 5>(bytes);
+  smem_attr_mb<T, I, 6>(bytes);
+  smem_attr_mb<T, I, 8>(bytes);
 }
 
 template <typename T, typename I, bool S, int MB>
@@ -312,10 +313,8 @@ void launch_vol_s(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, in
   dim3 grid((h->d.nz + v.bx) / v.bx, (h->d.ny + v.by) / v.by, (h->d.nx + v.bz) / v.bz);
   switch (v.minb) {
     case 1: launch_vol_mb<T, I, S, 1>(h, p, e_side, grid, block); break;
-    case 2: launch_vol_mb<T, I, S, 2>(h, p, e_side, grid, block); break;
-    case 3: launch_vol_mb<T, I, S, 3>(h, p, e_side, grid, block); break;
-    case 4: launch_vol_mb<T, I, S, 4>(h, p, e_side, grid, block); break;
-    default: launch_vol_mb<T, I, S, 5>(h, p, e_side, grid, block); break;
+    case 6: launch_vol_mb<T, I, S, 6>(h, p, e_side, grid, block); break;
+    default: launch_vol_mb<T, I, S, 8>(h, p, e_side, grid, block); break;
   }
 }
 
@@ -419,6 +418,26 @@ void launch_nffft(xfdtd_handle *h) {
   XCHECK(cudaGetLastError());
 }
 
+template <typename T>
+xg::TfsfSurfParams<T> tfsf_surf_params(xfdtd_handle *h) {
+  xg::TfsfSurfParams<T> p{};
+  p.d = h->d;
+  for (int c = 0; c < 6; ++c) p.F[c] = static_cast<T *>(h->F[c]);
+  p.tf.enabled = 1;
+  p.tf.L = h->aux_len;
+  for (int a = 0; a < 3; ++a) {
+    p.tf.lo[a] = h->tf_lo[a];
+    p.tf.hi[a] = h->tf_hi[a];
+    p.tf.pf[a] = h->tf_pf[a];
+    p.tf.ph[a] = h->tf_ph[a];
+    p.tf.ca[a] = h->tf_ca[a];
+    p.tf.cb[a] = h->tf_cb[a];
+  }
+  p.tf.inc = h->tf_inc;
+  p.step = h->d_step;
+  return p;
+}
+
 template <typename T, typename I>
 void enqueue_step_t(xfdtd_handle *h) {
   if (h->tfsf) {
@@ -451,9 +470,26 @@ void enqueue_step_t(xfdtd_handle *h) {
     XCHECK(cudaGetLastError());
     prof_end(h);
   }
+  if (h->tfsf) {
+    const auto sp = tfsf_surf_params<T>(h);
+    const long long n = xg::surface_count(h->tf_lo[0], h->tf_hi[0], h->tf_lo[1], h->tf_hi[1], h->tf_lo[2], h->tf_hi[2]);
+    prof_begin(h, 7);
+    xg::k_tfsf_e<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, h->stream>>>(sp);
+    XCHECK(cudaGetLastError());
+    prof_end(h);
+  }
   prof_begin(h, 3);
   launch_volume<T, I>(h, false);
   prof_end(h);
+  if (h->tfsf) {
+    const auto sp = tfsf_surf_params<T>(h);
+    const long long n = xg::surface_count(h->tf_lo[0] - 1, h->tf_hi[0], h->tf_lo[1] - 1, h->tf_hi[1],
+                                          h->tf_lo[2] - 1, h->tf_hi[2]);
+    prof_begin(h, 8);
+    xg::k_tfsf_h<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, h->stream>>>(sp);
+    XCHECK(cudaGetLastError());
+    prof_end(h);
+  }
   if (h->nffft) {
     prof_begin(h, 4);
     launch_nffft<T>(h);
@@ -483,7 +519,7 @@ void enqueue_step(xfdtd_handle *h) {
 }
 
 int launches_per_step(const xfdtd_handle *h) {
-  return (h->tfsf ? 1 : 0) + 2 + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
+  return (h->tfsf ? 3 : 0) + 2 + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
 }
 
 void build_graph(xfdtd_handle *h, int g) {
@@ -728,6 +764,19 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     h->terms = h->upload<xfdtd_probe_term>(pl->probe_terms, std::max(1, pl->n_probe_terms));
     h->probe_off = h->upload<int>(off.data(), off.size());
     h->probe_out = h->alloc<double>(static_cast<size_t>(pl->n_probes) * pl->total_steps);
+  }
+
+  // per-axis index flags for the volume kernels' fast path
+  for (int a = 0; a < 3; ++a) {
+    const int n = n_axis[a];
+    std::vector<uint8_t> fl(n + 1, 0);
+    for (int q = 0; q <= n; ++q) {
+      const bool slab_e = pl->cpml[a].n_layers && pl->cpml[a].slot_e[q] >= 0;
+      const bool slab_h = pl->cpml[a].n_layers && pl->cpml[a].slot_h[q] >= 0;
+      if (q == 0 || q == n || slab_e) fl[q] |= xg::kSpecialE;
+      if (q == n || slab_h) fl[q] |= xg::kSpecialH;
+    }
+    h->axis_flags[a] = h->upload<uint8_t>(fl.data(), fl.size());
   }
 
   h->d_step = h->alloc<long long>(1);

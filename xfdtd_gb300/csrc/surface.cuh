@@ -300,6 +300,211 @@ __global__ void __launch_bounds__(256) k_far_field(FarParams p) {
 }
 
 // ------------------------------------------------------------------------
+// TFSF3D::updateE / updateH face corrections (src/tfsf/tfsf_3d.cpp:185-411).
+// One thread per cell of the surface of the face box ([lo, hi] on every axis
+// for E, [lo-1, hi] for H), split into six disjoint parts (the two x planes
+// whole, the two y planes without their x edges, the two z planes without
+// their x and y edges).  A thread applies every face correction its cell
+// receives, per component, in the reference's face order (x, then y, then z).
+template <typename T>
+struct TfsfSurfParams {
+  Dims d;
+  T *F[6];
+  TfsfDev tf;
+  const long long *step;
+};
+
+template <typename T>
+__device__ __forceinline__ void add_corr(T &v, double corr) {
+  v = static_cast<T>(static_cast<double>(v) + corr);
+}
+
+// Maps a linear surface index to (i, j, k) on the surface of [a0,a1]x[b0,b1]x[c0,c1].
+__device__ __forceinline__ bool surface_cell(long long q, int a0, int a1, int b0, int b1, int c0, int c1, int &i,
+                                             int &j, int &k) {
+  const long long nb = b1 - b0 + 1, nc = c1 - c0 + 1, na_in = a1 - a0 - 1, nb_in = b1 - b0 - 1;
+  const long long px = nb * nc, py = (na_in > 0 ? na_in : 0) * nc, pz = (na_in > 0 ? na_in : 0) * (nb_in > 0 ? nb_in : 0);
+  if (q < 2 * px) {
+    i = q < px ? a0 : a1;
+    const long long r = q % px;
+    j = b0 + static_cast<int>(r / nc);
+    k = c0 + static_cast<int>(r % nc);
+    return true;
+  }
+  q -= 2 * px;
+  if (q < 2 * py) {
+    j = q < py ? b0 : b1;
+    const long long r = q % py;
+    i = a0 + 1 + static_cast<int>(r / nc);
+    k = c0 + static_cast<int>(r % nc);
+    return true;
+  }
+  q -= 2 * py;
+  if (q < 2 * pz) {
+    k = q < pz ? c0 : c1;
+    const long long r = q % pz;
+    i = a0 + 1 + static_cast<int>(r / nb_in);
+    j = b0 + 1 + static_cast<int>(r % nb_in);
+    return true;
+  }
+  return false;
+}
+
+template <typename T>
+__global__ void k_tfsf_e(TfsfSurfParams<T> p) {
+  const TfsfDev &tf = p.tf;
+  const int li = tf.lo[0], ri = tf.hi[0], lj = tf.lo[1], rj = tf.hi[1], lk = tf.lo[2], rk = tf.hi[2];
+  int i, j, k;
+  const long long q = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (!surface_cell(q, li, ri, lj, rj, lk, rk, i, j, k)) return;
+  const double *hinc = tf.inc + (((*p.step) + 1) & 1) * 6 * tf.L;   // incident H of the previous step
+  const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
+  // Ex: y faces (j = lj: -= cay Hz_inc(i, lj-1, k); j = rj: += cay Hz_inc(i, rj, k)),
+  //     z faces (k = lk: += caz Hy_inc(i, j, lk-1); k = rk: -= caz Hy_inc(i, j, rk))
+  {
+    T e = p.F[0][b];
+    bool w = false;
+    if ((j == lj || j == rj) && k >= lk && k <= rk && i >= li && i < ri) {
+      const int jj = j == lj ? lj - 1 : rj;
+      const double pr = tf.ph[0][i - li + 1] + tf.ph[1][jj - lj + 1] + tf.pf[2][k - lk] - 0.5;
+      const double v = tf.ca[1] * tfsf_interp(hinc + 5 * tf.L, pr);
+      add_corr(e, j == lj ? -v : v);
+      w = true;
+    }
+    if ((k == lk || k == rk) && i >= li && i < ri && j >= lj && j <= rj) {
+      const int kk = k == lk ? lk - 1 : rk;
+      const double pr = tf.ph[0][i - li + 1] + tf.pf[1][j - lj] + tf.ph[2][kk - lk + 1] - 0.5;
+      const double v = tf.ca[2] * tfsf_interp(hinc + 4 * tf.L, pr);
+      add_corr(e, k == lk ? v : -v);
+      w = true;
+    }
+    if (w) p.F[0][b] = e;
+  }
+  // Ey: x faces (i = li: += cax Hz_inc(li-1, j, k); i = ri: -= cax Hz_inc(ri, j, k)),
+  //     z faces (k = lk: -= caz Hx_inc(i, j, lk-1); k = rk: += caz Hx_inc(i, j, rk))
+  {
+    T e = p.F[1][b];
+    bool w = false;
+    if ((i == li || i == ri) && j >= lj && j < rj && k >= lk && k <= rk) {
+      const int ii = i == li ? li - 1 : ri;
+      const double pr = tf.ph[0][ii - li + 1] + tf.ph[1][j - lj + 1] + tf.pf[2][k - lk] - 0.5;
+      const double v = tf.ca[0] * tfsf_interp(hinc + 5 * tf.L, pr);
+      add_corr(e, i == li ? v : -v);
+      w = true;
+    }
+    if ((k == lk || k == rk) && i >= li && i <= ri && j >= lj && j < rj) {
+      const int kk = k == lk ? lk - 1 : rk;
+      const double pr = tf.pf[0][i - li] + tf.ph[1][j - lj + 1] + tf.ph[2][kk - lk + 1] - 0.5;
+      const double v = tf.ca[2] * tfsf_interp(hinc + 3 * tf.L, pr);
+      add_corr(e, k == lk ? -v : v);
+      w = true;
+    }
+    if (w) p.F[1][b] = e;
+  }
+  // Ez: x faces (i = li: -= cax Hy_inc(li-1, j, k); i = ri: += cax Hy_inc(ri, j, k)),
+  //     y faces (j = lj: += cay Hx_inc(i, lj-1, k); j = rj: -= cay Hx_inc(i, rj, k))
+  {
+    T e = p.F[2][b];
+    bool w = false;
+    if ((i == li || i == ri) && j >= lj && j <= rj && k >= lk && k < rk) {
+      const int ii = i == li ? li - 1 : ri;
+      const double pr = tf.ph[0][ii - li + 1] + tf.pf[1][j - lj] + tf.ph[2][k - lk + 1] - 0.5;
+      const double v = tf.ca[0] * tfsf_interp(hinc + 4 * tf.L, pr);
+      add_corr(e, i == li ? -v : v);
+      w = true;
+    }
+    if ((j == lj || j == rj) && k >= lk && k < rk && i >= li && i <= ri) {
+      const int jj = j == lj ? lj - 1 : rj;
+      const double pr = tf.pf[0][i - li] + tf.ph[1][jj - lj + 1] + tf.ph[2][k - lk + 1] - 0.5;
+      const double v = tf.ca[1] * tfsf_interp(hinc + 3 * tf.L, pr);
+      add_corr(e, j == lj ? v : -v);
+      w = true;
+    }
+    if (w) p.F[2][b] = e;
+  }
+}
+
+template <typename T>
+__global__ void k_tfsf_h(TfsfSurfParams<T> p) {
+  const TfsfDev &tf = p.tf;
+  const int li = tf.lo[0], ri = tf.hi[0], lj = tf.lo[1], rj = tf.hi[1], lk = tf.lo[2], rk = tf.hi[2];
+  int i, j, k;
+  const long long q = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (!surface_cell(q, li - 1, ri, lj - 1, rj, lk - 1, rk, i, j, k)) return;
+  const double *einc = tf.inc + ((*p.step) & 1) * 6 * tf.L;   // incident E of this step
+  const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
+  // Hx: y faces (j = lj-1: += cby Ez_inc(i, lj, k); j = rj: -= cby Ez_inc(i, rj, k)),
+  //     z faces (k = lk-1: -= cbz Ey_inc(i, j, lk); k = rk: += cbz Ey_inc(i, j, rk))
+  {
+    T h = p.F[3][b];
+    bool w = false;
+    if ((j == lj - 1 || j == rj) && k >= lk && k < rk && i >= li && i <= ri) {
+      const int jj = j == rj ? rj : lj;
+      const double pr = tf.pf[0][i - li] + tf.pf[1][jj - lj] + tf.ph[2][k - lk + 1];
+      const double v = tf.cb[1] * tfsf_interp(einc + 2 * tf.L, pr);
+      add_corr(h, j == rj ? -v : v);
+      w = true;
+    }
+    if ((k == lk - 1 || k == rk) && i >= li && i <= ri && j >= lj && j < rj) {
+      const int kk = k == rk ? rk : lk;
+      const double pr = tf.pf[0][i - li] + tf.ph[1][j - lj + 1] + tf.pf[2][kk - lk];
+      const double v = tf.cb[2] * tfsf_interp(einc + 1 * tf.L, pr);
+      add_corr(h, k == rk ? v : -v);
+      w = true;
+    }
+    if (w) p.F[3][b] = h;
+  }
+  // Hy: x faces (i = li-1: -= cbx Ez_inc(li, j, k); i = ri: += cbx Ez_inc(ri, j, k)),
+  //     z faces (k = lk-1: += cbz Ex_inc(i, j, lk); k = rk: -= cbz Ex_inc(i, j, rk))
+  {
+    T h = p.F[4][b];
+    bool w = false;
+    if ((i == li - 1 || i == ri) && j >= lj && j <= rj && k >= lk && k < rk) {
+      const int ii = i == ri ? ri : li;
+      const double pr = tf.pf[0][ii - li] + tf.pf[1][j - lj] + tf.ph[2][k - lk + 1];
+      const double v = tf.cb[0] * tfsf_interp(einc + 2 * tf.L, pr);
+      add_corr(h, i == ri ? v : -v);
+      w = true;
+    }
+    if ((k == lk - 1 || k == rk) && i >= li && i < ri && j >= lj && j <= rj) {
+      const int kk = k == rk ? rk : lk;
+      const double pr = tf.ph[0][i - li + 1] + tf.pf[1][j - lj] + tf.pf[2][kk - lk];
+      const double v = tf.cb[2] * tfsf_interp(einc + 0 * tf.L, pr);
+      add_corr(h, k == rk ? -v : v);
+      w = true;
+    }
+    if (w) p.F[4][b] = h;
+  }
+  // Hz: x faces (i = li-1: += cbx Ey_inc(li, j, k); i = ri: -= cbx Ey_inc(ri, j, k)),
+  //     y faces (j = lj-1: -= cby Ex_inc(i, lj, k); j = rj: += cby Ex_inc(i, rj, k))
+  {
+    T h = p.F[5][b];
+    bool w = false;
+    if ((i == li - 1 || i == ri) && j >= lj && j < rj && k >= lk && k <= rk) {
+      const int ii = i == ri ? ri : li;
+      const double pr = tf.pf[0][ii - li] + tf.ph[1][j - lj + 1] + tf.pf[2][k - lk];
+      const double v = tf.cb[0] * tfsf_interp(einc + 1 * tf.L, pr);
+      add_corr(h, i == ri ? -v : v);
+      w = true;
+    }
+    if ((j == lj - 1 || j == rj) && k >= lk && k <= rk && i >= li && i < ri) {
+      const int jj = j == rj ? rj : lj;
+      const double pr = tf.ph[0][i - li + 1] + tf.pf[1][jj - lj] + tf.pf[2][k - lk];
+      const double v = tf.cb[1] * tfsf_interp(einc + 0 * tf.L, pr);
+      add_corr(h, j == rj ? v : -v);
+      w = true;
+    }
+    if (w) p.F[5][b] = h;
+  }
+}
+
+// Number of cells on the surface of [a0,a1]x[b0,b1]x[c0,c1] (surface_cell's range).
+inline long long surface_count(int a0, int a1, int b0, int b1, int c0, int c1) {
+  const long long nb = b1 - b0 + 1, nc = c1 - c0 + 1, na_in = a1 - a0 - 1, nb_in = b1 - b0 - 1;
+  return 2 * nb * nc + 2 * (na_in > 0 ? na_in : 0) * nc + 2 * (na_in > 0 ? na_in : 0) * (nb_in > 0 ? nb_in : 0);
+}
+
+// ------------------------------------------------------------------------
 // Sparse per-step work.
 template <typename T>
 struct SparseParams {
