@@ -205,6 +205,8 @@ int xfdtd_autotune(xfdtd_handle *h, int trials);
  * (trial_ms[2*v] for E, [2*v+1] for H; 0 where not tried). */
 int xfdtd_kernel_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h, double *trial_ms);
 int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant);
+/* Per-step kernel launches enqueued so far (graph replays included). */
+int xfdtd_launch_count(xfdtd_handle *h, int64_t *n);
 /* Kernel launches the engine enqueues per step for this plan. */
 int xfdtd_launches_per_step(xfdtd_handle *h, int *n);
 /* Bytes copied host->device and device->host by the handle so far. */

@@ -195,3 +195,28 @@ def test_autotune_leaves_state_unchanged():
         assert np.array_equal(a.read_field(c), b.read_field(c))
     t = a.kernel_variants()
     assert max(t["trials_e"]) > 0 and max(t["trials_h"]) > 0
+
+
+def test_nffft_batches_flush_mid_run():
+    """Reading the NF-FF accumulators between batch boundaries folds the
+    pending steps; later steps continue from there (graph and plain replay)."""
+    sc, st = scenes.dielectric(steps=90)
+    o = O.OracleSim(sc, st)
+    for graph in (True, False):
+        g = X.Simulation(sc, st, graph=graph)
+        done = 0
+        for chunk in (13, 37, 40):
+            g.step(chunk)
+            done += chunk
+            if not graph:
+                o.step(chunk)
+            for w in (0, 11, 22):
+                ref = o.read_nffft(w) if not graph else None
+                got = g.read_nffft(w)
+                if ref is not None:
+                    assert scenes.rel_err(got, ref) <= TOL, (done, w)
+        if graph:
+            plain = X.Simulation(sc, st, graph=False)
+            plain.step(st)
+            for w in range(24):
+                assert np.array_equal(g.read_nffft(w), plain.read_nffft(w))

@@ -81,6 +81,7 @@ def libs():
         cu.xfdtd_launches_per_step.argtypes = [C.c_void_p, P(C.c_int)]
         cu.xfdtd_device_bytes.argtypes = [C.c_void_p, P(C.c_int64)]
         cu.xfdtd_transfer_bytes.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64)]
+        cu.xfdtd_launch_count.argtypes = [C.c_void_p, P(C.c_int64)]
         cu.xfdtd_autotune.argtypes = [C.c_void_p, C.c_int]
         cu.xfdtd_kernel_variants.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int), dp]
         cu.xfdtd_set_kernel_variant.argtypes = [C.c_void_p, C.c_int, C.c_int]
@@ -228,6 +229,12 @@ class Simulation:
 
     def profile_reset(self):
         self._check_engine(libs()[0].xfdtd_profile_reset(self.engine))
+
+    def launch_count(self) -> int:
+        """Per-step kernel launches the engine has enqueued so far."""
+        n = C.c_int64()
+        self._check_engine(libs()[0].xfdtd_launch_count(self.engine, C.byref(n)))
+        return n.value
 
     def launches_per_step(self) -> int:
         n = C.c_int()

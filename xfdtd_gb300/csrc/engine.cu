@@ -47,8 +47,8 @@ struct Err {
   } while (0)
 
 const char *kKernelNames[] = {"tfsf_aux", "update_e", "lumped_e", "update_h", "nffft",
-                              "probes",   "advance",  "tfsf_e",   "tfsf_h"};
-constexpr int kNumKernels = 9;
+                              "probes",   "advance",  "tfsf_e",   "tfsf_h",   "nffft_acc"};
+constexpr int kNumKernels = 10;
 
 }  // namespace
 
@@ -125,6 +125,14 @@ struct xfdtd_handle {
   // graph replay
   cudaGraphExec_t gexec = nullptr;
   int graph_steps = 0;
+  long long graph_launches = 0;
+  long long launch_count = 0;   // per-step kernels enqueued so far
+
+  // NF-FF batching: surface values of up to nf_batch steps are buffered and
+  // folded into the accumulators together
+  int nf_batch = 8;
+  long long nf_done = 0;        // steps already folded
+  void *nf_buf[3] = {};
 
   // profiling
   std::vector<cudaEvent_t> ev_pool;
@@ -194,6 +202,7 @@ void invalid(const std::string &m) { throw Err{XFDTD_ERR_INVALID_PLAN, m}; }
 
 // ------------------------------------------------------------ launches ---
 void prof_begin(xfdtd_handle *h, int id) {
+  h->launch_count += 1;   // every per-step kernel launch passes here
   if (!(h->flags & XFDTD_FLAG_PROFILE)) return;
   size_t need = h->ev_pending.size() * 2 + 2;
   while (h->ev_pool.size() < need) {
@@ -410,12 +419,50 @@ void launch_nffft(xfdtd_handle *h) {
   p.pm = h->phase_m;
   p.total = h->total;
   p.step = h->d_step;
+  for (int g = 0; g < 3; ++g) p.buf[g] = static_cast<T *>(h->nf_buf[g]);
+  p.batch = h->nf_batch;
   int bx = h->nf_hi[0] - h->nf_lo[0], by = h->nf_hi[1] - h->nf_lo[1], bz = h->nf_hi[2] - h->nf_lo[2];
   int u = std::max(bz, by), v = std::max(by, bx);
   dim3 block(32, 8, 1);
   dim3 grid((u + 31) / 32, (v + 7) / 8, 3);
   xg::k_nffft<T><<<grid, block, 0, h->stream>>>(p);
   XCHECK(cudaGetLastError());
+}
+
+// Folds `count` buffered NF-FF steps into the accumulators; `lag` = 0 inside
+// a step (the device step counter points at the last sampled step), 1 after
+// it (the counter has advanced past it).
+template <typename T>
+void launch_nffft_accumulate(xfdtd_handle *h, int count, int lag) {
+  xg::NfParams<T> p{};
+  for (int a = 0; a < 3; ++a) {
+    p.lo[a] = h->nf_lo[a];
+    p.hi[a] = h->nf_hi[a];
+  }
+  p.nf = h->nf;
+  for (int q = 0; q < 24; ++q) p.acc[q] = h->acc[q];
+  p.pj = h->phase_j;
+  p.pm = h->phase_m;
+  p.total = h->total;
+  p.step = h->d_step;
+  for (int g = 0; g < 3; ++g) p.buf[g] = static_cast<T *>(h->nf_buf[g]);
+  p.batch = h->nf_batch;
+  const long long bx = h->nf_hi[0] - h->nf_lo[0], by = h->nf_hi[1] - h->nf_lo[1], bz = h->nf_hi[2] - h->nf_lo[2];
+  const long long most = std::max(by * bz, std::max(bx * bz, bx * by));
+  dim3 grid(static_cast<unsigned>((most + 255) / 256), 1, 3);
+  xg::k_nffft_accumulate<T><<<grid, 256, 0, h->stream>>>(p, count, lag);
+  XCHECK(cudaGetLastError());
+}
+
+// Accumulates the NF-FF steps sampled since the last fold (before any read
+// of the accumulators or the far field).
+void nffft_flush(xfdtd_handle *h) {
+  if (!h->nffft) return;
+  const long long pending = h->host_step - h->nf_done;
+  if (pending <= 0) return;
+  if (h->precision == XFDTD_FP64) launch_nffft_accumulate<double>(h, static_cast<int>(pending), 1);
+  else launch_nffft_accumulate<float>(h, static_cast<int>(pending), 1);
+  h->nf_done = h->host_step;
 }
 
 template <typename T>
@@ -439,7 +486,7 @@ xg::TfsfSurfParams<T> tfsf_surf_params(xfdtd_handle *h) {
 }
 
 template <typename T, typename I>
-void enqueue_step_t(xfdtd_handle *h) {
+void enqueue_step_t(xfdtd_handle *h, long long s) {
   if (h->tfsf) {
     xg::AuxParams a{};
     a.L = h->aux_len;
@@ -494,6 +541,12 @@ void enqueue_step_t(xfdtd_handle *h) {
     prof_begin(h, 4);
     launch_nffft<T>(h);
     prof_end(h);
+    if ((s + 1) % h->nf_batch == 0) {   // the batch is full: fold it
+      prof_begin(h, 9);
+      launch_nffft_accumulate<T>(h, static_cast<int>(s + 1 - h->nf_done), 0);
+      prof_end(h);
+      h->nf_done = s + 1;
+    }
   }
   if (h->n_probes) {
     auto sp = sparse_params<T>(h);
@@ -508,13 +561,14 @@ void enqueue_step_t(xfdtd_handle *h) {
   prof_end(h);
 }
 
-void enqueue_step(xfdtd_handle *h) {
+// Enqueues the kernels of step s (s = the step's index, known on the host).
+void enqueue_step(xfdtd_handle *h, long long s) {
   if (h->precision == XFDTD_FP64) {
-    if (h->idx_bytes == 1) enqueue_step_t<double, uint8_t>(h);
-    else enqueue_step_t<double, uint16_t>(h);
+    if (h->idx_bytes == 1) enqueue_step_t<double, uint8_t>(h, s);
+    else enqueue_step_t<double, uint16_t>(h, s);
   } else {
-    if (h->idx_bytes == 1) enqueue_step_t<float, uint8_t>(h);
-    else enqueue_step_t<float, uint16_t>(h);
+    if (h->idx_bytes == 1) enqueue_step_t<float, uint8_t>(h, s);
+    else enqueue_step_t<float, uint16_t>(h, s);
   }
 }
 
@@ -522,11 +576,18 @@ int launches_per_step(const xfdtd_handle *h) {
   return (h->tfsf ? 3 : 0) + 2 + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
 }
 
+// Captures g steps starting at a step index that is a multiple of the NF-FF
+// batch (g is one too), so that the captured kernel sequence -- including
+// the batch folds -- is the same for every replay.
 void build_graph(xfdtd_handle *h, int g) {
   cudaGraph_t graph;
+  const long long nf_done = h->nf_done, launches = h->launch_count;
   XCHECK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  for (int s = 0; s < g; ++s) enqueue_step(h);
+  for (int s = 0; s < g; ++s) enqueue_step(h, h->host_step + s);
   XCHECK(cudaStreamEndCapture(h->stream, &graph));
+  h->graph_launches = h->launch_count - launches;
+  h->nf_done = nf_done;   // capture only recorded the launches
+  h->launch_count = launches;
   cudaError_t e = cudaGraphInstantiate(&h->gexec, graph, 0);
   cudaGraphDestroy(graph);
   XCHECK(e);
@@ -707,6 +768,7 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
       h->acc_len[q] = np.n_freq * face[q / 8];
       h->acc[q] = h->alloc<double2>(h->acc_len[q]);
     }
+    for (int g = 0; g < 3; ++g) h->nf_buf[g] = h->alloc_bytes(static_cast<size_t>(h->nf_batch) * 8 * face[g] * h->esize);
     if (!np.phase_j || !np.phase_m || !np.wave_number) invalid("NF-FF phase tables are required");
     h->phase_j = h->upload<double2>(reinterpret_cast<const double2 *>(np.phase_j), np.n_freq * pl->total_steps);
     h->phase_m = h->upload<double2>(reinterpret_cast<const double2 *>(np.phase_m), np.n_freq * pl->total_steps);
@@ -820,6 +882,7 @@ void run_far_field(xfdtd_handle *h) {
   if (!h->nffft) throw Err{XFDTD_ERR_STATE, "the plan has no NF-FF box"};
   if (!h->ff_theta) throw Err{XFDTD_ERR_STATE, "the plan has no far-field directions"};
   if (h->ff_step == h->host_step) return;
+  nffft_flush(h);
   xg::FarParams p{};
   for (int a = 0; a < 3; ++a) {
     p.lo[a] = h->nf_lo[a];
@@ -847,16 +910,23 @@ void do_steps(xfdtd_handle *h, long long n) {
   if (n < 0) invalid("negative step count");
   if (h->host_step + n > h->total) throw Err{XFDTD_ERR_STATE, "stepping past the plan's total_steps"};
   const bool graph = (h->flags & XFDTD_FLAG_GRAPH) && !(h->flags & XFDTD_FLAG_PROFILE);
-  long long left = n;
-  if (graph && n >= 2) {
-    if (!h->gexec) build_graph(h, static_cast<int>(std::min<long long>(n, 64)));
-    while (left >= h->graph_steps) {
+  const long long end = h->host_step + n;
+  const int B = h->nf_batch;
+  // single steps up to a batch boundary, whole graphs, then single steps
+  while (h->host_step < end) {
+    const bool aligned = h->host_step % B == 0 && (!h->nffft || h->nf_done == h->host_step);
+    const long long graph_len = h->gexec ? h->graph_steps : 4 * B;
+    if (graph && aligned && end - h->host_step >= graph_len) {
+      if (!h->gexec) build_graph(h, static_cast<int>(graph_len));
       XCHECK(cudaGraphLaunch(h->gexec, h->stream));
-      left -= h->graph_steps;
+      h->host_step += h->graph_steps;
+      h->launch_count += h->graph_launches;
+      if (h->nffft) h->nf_done = h->host_step;
+      continue;
     }
+    enqueue_step(h, h->host_step);
+    h->host_step += 1;
   }
-  for (long long s = 0; s < left; ++s) enqueue_step(h);
-  h->host_step += n;
 }
 
 }  // namespace
@@ -954,6 +1024,7 @@ int xfdtd_read_nffft(xfdtd_handle *h, int which, double *out, int64_t len) {
     if (!h->nffft) throw Err{XFDTD_ERR_STATE, "the plan has no NF-FF box"};
     if (which < 0 || which >= 24) invalid("accumulator index must be 0..23");
     if (len != 2 * h->acc_len[which]) invalid("length must be 2 * n_freq * face cells");
+    nffft_flush(h);
     std::vector<double2> buf(h->acc_len[which]);
     XCHECK(cudaMemcpyAsync(buf.data(), h->acc[which], buf.size() * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
     h->d2h += static_cast<long long>(buf.size() * sizeof(double2));
@@ -1075,6 +1146,12 @@ int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant) {
       h->gexec = nullptr;
     }
   });
+}
+
+int xfdtd_launch_count(xfdtd_handle *h, int64_t *n) {
+  if (!h || !n) return XFDTD_ERR_STATE;
+  *n = h->launch_count;
+  return XFDTD_OK;
 }
 
 int xfdtd_launches_per_step(xfdtd_handle *h, int *n) {

@@ -83,6 +83,8 @@ struct NfParams {
   const double2 *pj, *pm;   // [nf][total]
   long long total;
   const long long *step;
+  T *buf[3];                // per face pair: [batch][8][face cells] surface values
+  int batch;
 };
 
 template <typename T>
@@ -145,16 +147,40 @@ __global__ void k_nffft(NfParams<T> p) {
     plane = static_cast<long long>(ri - li) * (rj - lj);
     base = 16;
   }
-  for (int n = 0; n < p.nf; ++n) {
-    const double2 tj = p.pj[n * p.total + t], tm = p.pm[n * p.total + t];
-    const long long o = n * plane + cell;
+  // store the step's surface values in slot t % batch; k_nffft_accumulate
+  // folds a whole batch into the FP64 accumulators
+  T *buf = p.buf[base / 8] + (static_cast<long long>(t % p.batch) * 8) * plane + cell;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const double2 ph = (q % 4) < 2 ? tj : tm;   // J terms use the (t+1/2) phase, M terms t
-      double2 *a = p.acc[base + q] + o;
+  for (int q = 0; q < 8; ++q) buf[q * plane] = static_cast<T>(val[q]);
+}
+
+// acc[n] += v[s] * phase[n][t0 + s] for the `count` buffered steps ending at
+// step *step - lag, added one step at a time in step order: the same
+// additions, in the same order, as accumulating every step (nffft_fd.cpp:117-203).
+template <typename T>
+__global__ void k_nffft_accumulate(NfParams<T> p, int count, int lag) {
+  const int group = blockIdx.z;
+  const int lo_a = group == 0 ? p.lo[1] : p.lo[0], hi_a = group == 0 ? p.hi[1] : p.hi[0];
+  const int lo_b = group == 2 ? p.lo[1] : p.lo[2], hi_b = group == 2 ? p.hi[1] : p.hi[2];
+  const long long plane = static_cast<long long>(hi_a - lo_a) * (hi_b - lo_b);
+  const long long cell = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (cell >= plane) return;
+  const long long t_last = *p.step - lag;
+  const long long t0 = t_last - count + 1;
+  if (t0 < 0 || t_last >= p.total) return;
+  const T *buf = p.buf[group] + cell;
+  for (int q = 0; q < 8; ++q) {
+    const double2 *ph = (q % 4) < 2 ? p.pj : p.pm;   // J terms use the (t+1/2) phase, M terms t
+    for (int n = 0; n < p.nf; ++n) {
+      double2 *a = p.acc[group * 8 + q] + n * plane + cell;
       double2 r = *a;
-      r.x += val[q] * ph.x;
-      r.y += val[q] * ph.y;
+      for (int s = 0; s < count; ++s) {
+        const long long t = t0 + s;
+        const double v = static_cast<double>(buf[(static_cast<long long>(t % p.batch) * 8 + q) * plane]);
+        const double2 f = ph[n * p.total + t];
+        r.x += v * f.x;
+        r.y += v * f.y;
+      }
       *a = r;
     }
   }
