@@ -210,11 +210,15 @@ def test_nffft_batches_flush_mid_run():
             done += chunk
             if not graph:
                 o.step(chunk)
-            for w in (0, 11, 22):
-                ref = o.read_nffft(w) if not graph else None
-                got = g.read_nffft(w)
-                if ref is not None:
-                    assert scenes.rel_err(got, ref) <= TOL, (done, w)
+                # some accumulators hold only rounding noise early on (the
+                # incident plane wave has no Hz): compare on the common scale
+                refs = [o.read_nffft(w) for w in range(24)]
+                scale = max(np.abs(r).max() for r in refs)
+                for w in range(24):
+                    got = g.read_nffft(w)
+                    assert np.abs(got - refs[w]).max() <= TOL * scale, (done, w)
+            else:
+                g.read_nffft(0)   # folds the pending steps mid-batch
         if graph:
             plain = X.Simulation(sc, st, graph=False)
             plain.step(st)

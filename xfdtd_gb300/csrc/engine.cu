@@ -119,7 +119,7 @@ struct xfdtd_handle {
   int *d_flag = nullptr;
 
   // volume-kernel variants (autotuned)
-  int var_e = 0, var_h = 0;
+  int var_e = 1, var_h = 1;   // L1-table variant: valid for every plan
   float tune_ms[2][16] = {};
 
   // graph replay
@@ -272,68 +272,66 @@ xg::VolParams<T, I> vol_params(xfdtd_handle *h) {
   return p;
 }
 
-// Volume-kernel variants the autotuner chooses from: a register cap (the
-// minimum number of resident 256-thread blocks per SM asked of the register
-// allocator) and a block shape (k fastest; 32 or 64 along k for full
-// 128-byte rows).  Every variant computes the same per-cell arithmetic.
+// Volume-kernel variants the autotuner chooses from.  A variant fixes the
+// register cap (the minimum number of resident 256-thread blocks per SM
+// asked of the register allocator; 1 = none), the block shape (k fastest,
+// 32..128 along k for 128..512-byte rows), the cells per thread along i
+// (1 or 2) and where the coefficient table lives (shared memory, filled per
+// block behind a barrier, or read through L1).  Every variant computes the
+// same per-cell arithmetic, so all give identical bits.
 struct Variant {
   int minb;
   int bx, by, bz;
+  int nc;
+  bool smem;
 };
 constexpr Variant kVariants[] = {
-    {1, 32, 4, 2}, {1, 32, 8, 1}, {1, 64, 2, 2}, {6, 32, 4, 2},
-    {6, 32, 8, 1}, {8, 32, 4, 2}, {8, 32, 8, 1}, {8, 64, 4, 1},
+    {8, 32, 4, 2, 1, true},   {8, 32, 4, 2, 1, false},  {8, 32, 8, 1, 1, false}, {8, 64, 4, 1, 1, false},
+    {8, 128, 2, 1, 1, false}, {6, 32, 4, 2, 2, false},  {6, 32, 8, 1, 2, false}, {6, 64, 4, 1, 2, false},
+    {1, 32, 4, 2, 2, false},  {1, 32, 4, 2, 1, false},  {8, 32, 4, 2, 2, false}, {6, 32, 4, 2, 1, true},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-// Every variant is offered in both precisions: uncapped, and capped for 6
-// or 8 resident blocks (75% / 100% thread occupancy).
-bool variant_allowed(const Variant &v, bool fp64) {
-  (void)fp64;
-  return v.minb == 1 || v.minb == 6 || v.minb == 8;
-}
+// A shared-memory-table variant needs the table to fit (smem_table).
+bool variant_allowed(const xfdtd_handle *h, const Variant &v) { return !v.smem || h->smem_table; }
 
-template <typename T, typename I, int MB>
-void smem_attr_mb(int bytes) {
-  XCHECK(cudaFuncSetAttribute(xg::k_update_e<T, I, true, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  XCHECK(cudaFuncSetAttribute(xg::k_update_h<T, I, true, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-}
-
-// Opts every shared-memory-table instantiation in to `bytes` of dynamic
-// shared memory (needed above 48 KB).
-template <typename T, typename I>
-void smem_attr(int bytes) {
-  smem_attr_mb<T, I, 1>(bytes);
-  smem_attr_mb<T, I, 6>(bytes);
-  smem_attr_mb<T, I, 8>(bytes);
-}
-
-template <typename T, typename I, bool S, int MB>
-void launch_vol_mb(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, dim3 grid, dim3 block) {
-  const size_t smem = S ? h->smem_bytes : 0;
-  if (e_side) xg::k_update_e<T, I, S, MB><<<grid, block, smem, h->stream>>>(p);
-  else xg::k_update_h<T, I, S, MB><<<grid, block, smem, h->stream>>>(p);
-}
-
-template <typename T, typename I, bool S>
-void launch_vol_s(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, int var) {
-  const Variant &v = kVariants[var];
+template <typename T, typename I, bool S, int MB, int NC>
+void launch_vol_v(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, const Variant &v) {
   dim3 block(v.bx, v.by, v.bz);
-  dim3 grid((h->d.nz + v.bx) / v.bx, (h->d.ny + v.by) / v.by, (h->d.nx + v.bz) / v.bz);
-  switch (v.minb) {
-    case 1: launch_vol_mb<T, I, S, 1>(h, p, e_side, grid, block); break;
-    case 6: launch_vol_mb<T, I, S, 6>(h, p, e_side, grid, block); break;
-    default: launch_vol_mb<T, I, S, 8>(h, p, e_side, grid, block); break;
-  }
+  const int zc = v.bz * NC;
+  dim3 grid((h->d.nz + v.bx) / v.bx, (h->d.ny + v.by) / v.by, (h->d.nx + zc) / zc);
+  const size_t smem = S ? h->smem_bytes : 0;
+  if (e_side) xg::k_update_e<T, I, S, MB, NC><<<grid, block, smem, h->stream>>>(p);
+  else xg::k_update_h<T, I, S, MB, NC><<<grid, block, smem, h->stream>>>(p);
 }
 
 template <typename T, typename I>
 void launch_volume(xfdtd_handle *h, bool e_side, int var = -1) {
   auto p = vol_params<T, I>(h);
   if (var < 0) var = e_side ? h->var_e : h->var_h;
-  if (h->smem_table) launch_vol_s<T, I, true>(h, p, e_side, var);
-  else launch_vol_s<T, I, false>(h, p, e_side, var);
+  const Variant &v = kVariants[var];
+  const int key = v.minb * 100 + v.nc * 10 + (v.smem ? 1 : 0);
+  switch (key) {
+    case 811: launch_vol_v<T, I, true, 8, 1>(h, p, e_side, v); break;
+    case 810: launch_vol_v<T, I, false, 8, 1>(h, p, e_side, v); break;
+    case 820: launch_vol_v<T, I, false, 8, 2>(h, p, e_side, v); break;
+    case 620: launch_vol_v<T, I, false, 6, 2>(h, p, e_side, v); break;
+    case 611: launch_vol_v<T, I, true, 6, 1>(h, p, e_side, v); break;
+    case 120: launch_vol_v<T, I, false, 1, 2>(h, p, e_side, v); break;
+    case 110: launch_vol_v<T, I, false, 1, 1>(h, p, e_side, v); break;
+    default: throw Err{XFDTD_ERR_STATE, "volume-kernel variant without an instantiation"};
+  }
   XCHECK(cudaGetLastError());
+}
+
+// Opts the shared-memory-table instantiations in to `bytes` of dynamic
+// shared memory (needed above 48 KB).
+template <typename T, typename I>
+void smem_attr(int bytes) {
+  XCHECK(cudaFuncSetAttribute(xg::k_update_e<T, I, true, 8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_update_h<T, I, true, 8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_update_e<T, I, true, 6, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_update_h<T, I, true, 6, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
 }
 
 // Times every variant of the E and H kernels on the handle's current state
@@ -349,7 +347,7 @@ void autotune_t(xfdtd_handle *h, int trials) {
     float best = 1e30f;
     int best_v = 0;
     for (int v = 0; v < kNumVariants; ++v) {
-      if (!variant_allowed(kVariants[v], sizeof(T) == 8)) continue;
+      if (!variant_allowed(h, kVariants[v])) continue;
       launch_volume<T, I>(h, side == 0, v);   // warm-up / module load
       XCHECK(cudaEventRecord(a, h->stream));
       for (int r = 0; r < trials; ++r) launch_volume<T, I>(h, side == 0, v);
@@ -1135,9 +1133,8 @@ int xfdtd_kernel_variants(xfdtd_handle *h, int *n, int *current_e, int *current_
 int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant) {
   if (!h) return XFDTD_ERR_STATE;
   return guarded(h, [&] {
-    const bool fp64 = h->precision == XFDTD_FP64;
     if (e_variant < 0 || e_variant >= kNumVariants || h_variant < 0 || h_variant >= kNumVariants ||
-        !variant_allowed(kVariants[e_variant], fp64) || !variant_allowed(kVariants[h_variant], fp64))
+        !variant_allowed(h, kVariants[e_variant]) || !variant_allowed(h, kVariants[h_variant]))
       invalid("kernel variant not available for this precision");
     h->var_e = e_variant;
     h->var_h = h_variant;

@@ -47,17 +47,11 @@ __device__ __forceinline__ const T *load_table(const VolParams<T, I> &p, int hal
   return st;
 }
 
-// MINB: minimum resident blocks per SM requested from the register
-// allocator (1 = no cap); the autotuner in engine.cu picks it per plan.
-template <typename T, typename I, bool SMEM_TABLE, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_update_e(VolParams<T, I> p) {
-  int ts;
-  const T *tab = load_table<T, I, SMEM_TABLE>(p, 0, ts);
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int i = blockIdx.z * blockDim.z + threadIdx.z;
+// E update of one cell (fast path when the cell is plain, else the general
+// path with walls and CPML).
+template <typename T, typename I>
+__device__ __forceinline__ void e_cell(const VolParams<T, I> &p, const T *tab, int ts, int i, int j, int k) {
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
-  if (k > nz || j > ny || i > nx) return;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
   const T *__restrict__ Hx = p.H[0];
@@ -187,15 +181,74 @@ __global__ void __launch_bounds__(256, MINB) k_update_e(VolParams<T, I> p) {
   }
 }
 
-template <typename T, typename I, bool SMEM_TABLE, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_update_h(VolParams<T, I> p) {
+// NC plain cells (i0 .. i0+NC-1) of one (j, k) column: every load is issued
+// before any store, and the H at i-1 of cell c+1 is cell c's own.
+template <typename T, typename I, int NC>
+__device__ __forceinline__ void e_fast(const VolParams<T, I> &p, const T *tab, int ts, int i0, int j, int k) {
+  const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
+  const unsigned b0 = static_cast<unsigned>(i0) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
+  const T *__restrict__ Hx = p.H[0];
+  const T *__restrict__ Hy = p.H[1];
+  const T *__restrict__ Hz = p.H[2];
+  T *__restrict__ Ex = p.E[0];
+  T *__restrict__ Ey = p.E[1];
+  T *__restrict__ Ez = p.E[2];
+  T hx[NC], hy[NC + 1], hz[NC + 1], hx_k[NC], hy_k[NC], hx_j[NC], hz_j[NC], ex[NC], ey[NC], ez[NC];
+  const T *c[NC];
+  hy[0] = __ldg(Hy + b0 - usi);
+  hz[0] = __ldg(Hz + b0 - usi);
+#pragma unroll
+  for (int q = 0; q < NC; ++q) {
+    const unsigned b = b0 + q * usi;
+    hx[q] = __ldg(Hx + b);
+    hy[q + 1] = __ldg(Hy + b);
+    hz[q + 1] = __ldg(Hz + b);
+    hx_k[q] = __ldg(Hx + b - 1);
+    hy_k[q] = __ldg(Hy + b - 1);
+    hx_j[q] = __ldg(Hx + b - usj);
+    hz_j[q] = __ldg(Hz + b - usj);
+    c[q] = tab + static_cast<unsigned>(__ldg(p.idx + b)) * ts;
+    ex[q] = Ex[b];
+    ey[q] = Ey[b];
+    ez[q] = Ez[b];
+  }
+#pragma unroll
+  for (int q = 0; q < NC; ++q) {
+    const unsigned b = b0 + q * usi;
+    const T *cc = c[q];
+    Ex[b] = cc[0] * ex[q] + cc[1] * (hy[q + 1] - hy_k[q]) + cc[2] * (hz[q + 1] - hz_j[q]);
+    Ey[b] = cc[3] * ey[q] + cc[5] * (hx[q] - hx_k[q]) + cc[4] * (hz[q + 1] - hz[q]);
+    Ez[b] = cc[6] * ez[q] + cc[7] * (hx[q] - hx_j[q]) + cc[8] * (hy[q + 1] - hy[q]);
+  }
+}
+
+// MINB: minimum resident blocks per SM requested from the register
+// allocator (1 = no cap); NC: cells per thread along i.  The autotuner in
+// engine.cu picks both (and the block shape) per plan.
+template <typename T, typename I, bool SMEM_TABLE, int MINB, int NC>
+__global__ void __launch_bounds__(256, MINB) k_update_e(VolParams<T, I> p) {
   int ts;
-  const T *tab = load_table<T, I, SMEM_TABLE>(p, 1, ts);
+  const T *tab = load_table<T, I, SMEM_TABLE>(p, 0, ts);
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int i = blockIdx.z * blockDim.z + threadIdx.z;
+  const int i0 = (blockIdx.z * blockDim.z + threadIdx.z) * NC;
+  if (k > p.d.nz || j > p.d.ny || i0 > p.d.nx) return;
+  bool plain = !((__ldg(p.flags[1] + j) | __ldg(p.flags[2] + k)) & kSpecialE) && i0 + NC - 1 <= p.d.nx;
+#pragma unroll
+  for (int q = 0; q < NC; ++q) plain = plain && !(__ldg(p.flags[0] + min(i0 + q, p.d.nx)) & kSpecialE);
+  if (plain) {
+    e_fast<T, I, NC>(p, tab, ts, i0, j, k);
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < NC; ++q)
+    if (i0 + q <= p.d.nx) e_cell<T, I>(p, tab, ts, i0 + q, j, k);
+}
+
+// H update of one cell (fast path when the cell is plain).
+template <typename T, typename I>
+__device__ __forceinline__ void h_cell(const VolParams<T, I> &p, const T *tab, int ts, int i, int j, int k) {
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
-  if (k > nz || j > ny || i > nx) return;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
   const T *__restrict__ Ex = p.E[0];
@@ -322,6 +375,66 @@ __global__ void __launch_bounds__(256, MINB) k_update_h(VolParams<T, I> p) {
     }
     if (w) Hz[b] = h;
   }
+}
+
+// NC plain cells of one column for H: the E at i+1 of cell c is cell c+1's own.
+template <typename T, typename I, int NC>
+__device__ __forceinline__ void h_fast(const VolParams<T, I> &p, const T *tab, int ts, int i0, int j, int k) {
+  const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
+  const unsigned b0 = static_cast<unsigned>(i0) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
+  const T *__restrict__ Ex = p.E[0];
+  const T *__restrict__ Ey = p.E[1];
+  const T *__restrict__ Ez = p.E[2];
+  T *__restrict__ Hx = p.H[0];
+  T *__restrict__ Hy = p.H[1];
+  T *__restrict__ Hz = p.H[2];
+  T ex[NC], ey[NC + 1], ez[NC + 1], ex_kp[NC], ey_kp[NC], ex_jp[NC], ez_jp[NC], hx[NC], hy[NC], hz[NC];
+  const T *c[NC];
+#pragma unroll
+  for (int q = 0; q < NC; ++q) {
+    const unsigned b = b0 + q * usi;
+    ex[q] = __ldg(Ex + b);
+    ey[q] = __ldg(Ey + b);
+    ez[q] = __ldg(Ez + b);
+    ex_kp[q] = __ldg(Ex + b + 1);
+    ey_kp[q] = __ldg(Ey + b + 1);
+    ex_jp[q] = __ldg(Ex + b + usj);
+    ez_jp[q] = __ldg(Ez + b + usj);
+    c[q] = tab + static_cast<unsigned>(__ldg(p.idx + b)) * ts;
+    hx[q] = Hx[b];
+    hy[q] = Hy[b];
+    hz[q] = Hz[b];
+  }
+  ey[NC] = __ldg(Ey + b0 + NC * usi);
+  ez[NC] = __ldg(Ez + b0 + NC * usi);
+#pragma unroll
+  for (int q = 0; q < NC; ++q) {
+    const unsigned b = b0 + q * usi;
+    const T *cc = c[q];
+    Hx[b] = cc[0] * hx[q] + cc[1] * (ey_kp[q] - ey[q]) + cc[2] * (ez_jp[q] - ez[q]);
+    Hy[b] = cc[3] * hy[q] + cc[4] * (ez[q + 1] - ez[q]) + cc[5] * (ex_kp[q] - ex[q]);
+    Hz[b] = cc[6] * hz[q] + cc[7] * (ex_jp[q] - ex[q]) + cc[8] * (ey[q + 1] - ey[q]);
+  }
+}
+
+template <typename T, typename I, bool SMEM_TABLE, int MINB, int NC>
+__global__ void __launch_bounds__(256, MINB) k_update_h(VolParams<T, I> p) {
+  int ts;
+  const T *tab = load_table<T, I, SMEM_TABLE>(p, 1, ts);
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i0 = (blockIdx.z * blockDim.z + threadIdx.z) * NC;
+  if (k > p.d.nz || j > p.d.ny || i0 > p.d.nx) return;
+  bool plain = !((__ldg(p.flags[1] + j) | __ldg(p.flags[2] + k)) & kSpecialH) && i0 + NC - 1 <= p.d.nx;
+#pragma unroll
+  for (int q = 0; q < NC; ++q) plain = plain && !(__ldg(p.flags[0] + min(i0 + q, p.d.nx)) & kSpecialH);
+  if (plain) {
+    h_fast<T, I, NC>(p, tab, ts, i0, j, k);
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < NC; ++q)
+    if (i0 + q <= p.d.nx) h_cell<T, I>(p, tab, ts, i0 + q, j, k);
 }
 
 }  // namespace xg
