@@ -155,6 +155,12 @@ def _peaks():
 
 
 # --------------------------------------------------------------- roofline ---
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
+# from an ncu --set full capture of that kernel on this workload
+# (python -m xfdtd_gb300.run --config dielectric_sphere --steps 24 --precision fp32 --no-graph).
+NCU_TRAFFIC = {("update_e", "fp32", (280, 280, 280)): 621.793024e6 + 318.648320e6}
+
+
 def algorithmic_bytes(n, slab_layers, precision: str, kernel: str) -> float:
     """Bytes one launch of the E (or H) kernel must move at least: read the
     3 own components and the 3 curl components, write the 3 own components,
@@ -333,7 +339,8 @@ def ours_arm(args, world, rank, local, grp):
                    "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (cells * (4 if args.precision == 'fp32' else 8) / 1e6),
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": NCU_TRAFFIC.get((dom, args.precision, tuple(n))),
                      "algorithmic_bytes_per_launch": alg, "launch_ms": dom_ms / dom_n},
         "kernel_shares": shares,
         "autotuned_variants": {"update_e": variants["e"], "update_h": variants["h"],

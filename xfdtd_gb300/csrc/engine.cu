@@ -4,14 +4,22 @@
 // plan on the host, allocates every device buffer once and uploads the
 // tables; xfdtd_step enqueues the per-step kernel sequence
 //
-//   k_tfsf_aux (1 block)  -> k_update_e (Yee E + TFSF E + CPML E)
-//   -> k_lumped_e (sparse) -> k_update_h (Yee H + TFSF H + CPML H)
-//   -> k_nffft (surface)  -> k_probes -> k_advance
+//   k_tfsf_aux (1 block: 1-D incident line)
+//   -> k_update_e (Yee E + CPML E, one thread per cell)
+//   -> k_lumped_e (sparse) -> k_tfsf_e (TFSF surface E corrections)
+//   -> k_update_h (Yee H + CPML H) -> k_tfsf_h (TFSF surface H corrections)
+//   -> k_nffft (surface samples into the batch buffer)
+//   -> k_nffft_accumulate (every nf_batch steps: DFT fold of the batch)
+//   -> k_probes -> k_advance
 //
 // which is the order of the reference's loop body
-// (src/simulation/simulation_update.cpp:13-35).  The step index lives on the
-// device (k_advance bumps it), so a captured CUDA graph of G steps replays
-// for any starting step.
+// (src/simulation/simulation_update.cpp:13-35), except that the CPML terms
+// are added inside the volume kernels, before the lumped and TFSF
+// corrections rather than after them.  The two only meet on cells where a
+// TFSF face or a lumped element lies inside a CPML slab, where the same
+// terms are added in another order.  The step index lives on the device (k_advance bumps it), so a
+// captured CUDA graph of G steps (G a multiple of the NF-FF batch) replays
+// for any starting step on a batch boundary.
 #include <cuda_runtime.h>
 
 #include <algorithm>
