@@ -219,6 +219,51 @@ void xfdtd_destroy(xfdtd_handle *h);
 /* Version string of the engine build. */
 const char *xfdtd_version(void);
 
+/* ---------------------------------------------------------------------
+ * Allocation-free NF-FF running DFT.  No counterpart in the reference: it
+ * is NffftFd::update (nffft_fd.cpp:108-203) as a stand-alone operator on
+ * caller-owned device arrays for callers that may not allocate device
+ * memory during a run (runtimes that own every device allocation,
+ * fixed-memory solvers).  The sample batch lives in a static 64 MiB device
+ * array (xfdtd_nffft_noalloc_max_bytes()); the functions make no device
+ * allocation and call no allocating library.
+ *
+ * Call xfdtd_nffft_noalloc_setup(device) once per device before the first
+ * operator call and before any stream capture begins: it makes the device
+ * current and looks up the scratch address.  Each operator call samples
+ * step `step` (fields as they stand after that step's H update) into slot
+ * step % batch and, if fold_count > 0, folds steps step-fold_count+1 ..
+ * step (all sampled earlier through this operator on this device) into
+ * acc[].  The accumulators must start at zero.  The scratch is shared by
+ * all calls on a device: calls that overlap in time race on it.  A batch
+ * larger than the scratch (batch * 24 * largest face * element size) is
+ * rejected with XFDTD_ERR_INVALID_PLAN.  Launches are asynchronous on
+ * `stream`; errors: xfdtd_nffft_noalloc_last_error(). */
+typedef struct xfdtd_nffft_operator {
+  int32_t precision;        /* XFDTD_FP64 or XFDTD_FP32: element type of fields */
+  int32_t device;           /* CUDA device ordinal the pointers live on         */
+  int64_t nx, ny, nz;       /* cells per axis                                   */
+  const void *fields[6];    /* Ex Ey Ez Hx Hy Hz, reference component shapes,
+                               k contiguous (Ex (nx,ny+1,nz+1) ... Hz (nx,ny,nz+1)) */
+  int64_t lo[3], hi[3];     /* NF-FF box: cells [lo, hi) per axis, lo >= 1      */
+  int32_t n_freq;
+  int32_t batch;            /* sample slots (1..), fold_count <= batch          */
+  int64_t total_steps;      /* length of the phase tables                        */
+  int64_t step;             /* step being sampled, 0 <= step < total_steps       */
+  int32_t fold_count;       /* steps to fold after sampling (0 = none)          */
+  int32_t reserved;
+  const double *phase_j;    /* [n_freq][total_steps] (re, im): dt e^{-j w (t+1/2) dt} */
+  const double *phase_m;    /* [n_freq][total_steps] (re, im): dt e^{-j w t dt}       */
+  double *acc[24];          /* [n_freq][a][b] (re, im), layout of xfdtd_read_nffft;
+                               16-byte aligned, like the phase tables       */
+  void *stream;             /* cudaStream_t (NULL: legacy default stream)       */
+} xfdtd_nffft_operator;
+
+int xfdtd_nffft_noalloc_setup(int device);
+int xfdtd_nffft_dft_noalloc(const xfdtd_nffft_operator *op);
+int64_t xfdtd_nffft_noalloc_max_bytes(void);
+const char *xfdtd_nffft_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

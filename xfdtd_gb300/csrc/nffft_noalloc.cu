@@ -1,0 +1,254 @@
+// nffft_noalloc.cu -- the batched NF-FF running DFT as a stand-alone operator
+// that allocates no device memory (xfdtd_nffft_dft_noalloc, xfdtd_cuda.h).
+//
+// Some callers cannot allocate device memory when they call in: a host
+// runtime whose memory manager owns every device allocation (a JVM, Go or
+// .NET binding that reserves the GPU up front), a solver that budgets its
+// device memory before the run and must not grow it mid-run, or a loop
+// where cudaMalloc's implicit device synchronisation is not acceptable.  For
+// them the batch of buffered surface samples lives in a fixed file-scope
+// device array (kScratchBytes, 64 MiB) instead of memory the engine
+// allocates per handle; the array is resident on every GPU that loads this
+// library until the process exits.  A plan whose batch does not fit
+// (batch x 24 x largest face x element size) is rejected with
+// XFDTD_ERR_INVALID_PLAN before any GPU work.
+//
+// The operator follows NffftFd::update (src/nffft/nffft_fd.cpp:108-203)
+// with the face-centre interpolations of EMF
+// (src/electromagnetic_field/linear_interpolation_emf.cpp:286-421): each call
+// samples the 24 surface currents of one step into slot (step mod batch) of
+// the scratch array and, when asked, folds the last `fold_count` sampled
+// steps into the caller's FP64 accumulators one step at a time, in step
+// order.  The accumulators must start at zero (the caller owns and clears
+// them); the scratch needs no clearing, because every slot is written by a
+// sample before a fold reads it.  One scratch array serves all calls on a
+// device, so calls that overlap in time on that device (different streams
+// or threads) race on it: callers serialise them.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/xfdtd_cuda.h"
+
+namespace {
+
+// 64 MiB: a batch of 8 steps fits a largest NF-FF face of 87,381 cells in
+// FP32 (295 x 295) or 43,690 cells in FP64 (209 x 209).
+constexpr size_t kScratchBytes = 64ull << 20;
+
+static __device__ __align__(256) unsigned char g_nffft_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+void *g_scratch_ptr[kMaxDevices] = {};
+std::mutex g_scratch_mu;
+thread_local char g_err[256];
+
+int fail(int code, const char *msg) {
+  std::strncpy(g_err, msg, sizeof(g_err) - 1);
+  g_err[sizeof(g_err) - 1] = '\0';
+  return code;
+}
+
+// Device address of the scratch array on `dev`, looked up once per device
+// with that device current (host code must not use the symbol itself: on
+// the host it is only a stand-in).
+int scratch_on_device(int dev, void **out) {
+  if (dev < 0 || dev >= kMaxDevices) return fail(XFDTD_ERR_INVALID_PLAN, "device ordinal out of range");
+  if (cudaSetDevice(dev) != cudaSuccess) return fail(XFDTD_ERR_CUDA, "cudaSetDevice failed");
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_ptr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_nffft_scratch);
+    if (e != cudaSuccess || !p) return fail(XFDTD_ERR_CUDA, "cudaGetSymbolAddress of the NF-FF scratch failed");
+    g_scratch_ptr[dev] = p;
+  }
+  *out = g_scratch_ptr[dev];
+  return XFDTD_OK;
+}
+
+template <typename T>
+struct OpParams {
+  const T *f[6];
+  long long si[6], sj[6];
+  int lo[3], hi[3];
+  int nf;
+  const double2 *pj, *pm;
+  long long total;
+  int batch;
+  T *buf;                // [batch][24][max_plane]: the scratch array
+  long long plane[3];    // X (ny_box*nz_box), Y (nz_box*nx_box), Z (nx_box*ny_box)
+  long long max_plane;
+  long long step;
+  double2 *acc[24];
+};
+
+template <typename T>
+__device__ __forceinline__ double at(const OpParams<T> &p, int c, int i, int j, int k) {
+  return static_cast<double>(p.f[c][static_cast<long long>(i) * p.si[c] + static_cast<long long>(j) * p.sj[c] + k]);
+}
+
+// Samples the 24 surface currents of step p.step (reference accumulator
+// layout: X faces [j][k], Y faces [k][i], Z faces [i][j]).
+template <typename T>
+__global__ void k_sample(OpParams<T> p) {
+  const long long t = p.step;
+  const int li = p.lo[0], lj = p.lo[1], lk = p.lo[2], ri = p.hi[0], rj = p.hi[1], rk = p.hi[2];
+  const int face = blockIdx.z;
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = blockIdx.y * blockDim.y + threadIdx.y;
+  double val[8];
+  long long cell;
+  if (face == 0) {   // j in [lj, rj), k in [lk, rk): jy jz my mz (xn), then xp
+    const int k = lk + u, j = lj + v;
+    if (k >= rk || j >= rj) return;
+    val[2] = -1 * (0.5 * (at(p, 2, li, j, k) + at(p, 2, li, j + 1, k)));
+    val[3] = 0.5 * (at(p, 1, li, j, k) + at(p, 1, li, j, k + 1));
+    val[0] = 0.25 * (at(p, 5, li, j, k) + at(p, 5, li, j, k + 1) + at(p, 5, li - 1, j, k) + at(p, 5, li - 1, j, k + 1));
+    val[1] = -1 * (0.25 * (at(p, 4, li, j, k) + at(p, 4, li, j + 1, k) + at(p, 4, li - 1, j, k) + at(p, 4, li - 1, j + 1, k)));
+    val[6] = 0.5 * (at(p, 2, ri, j, k) + at(p, 2, ri, j + 1, k));
+    val[7] = -1 * (0.5 * (at(p, 1, ri, j, k) + at(p, 1, ri, j, k + 1)));
+    val[4] = -1 * (0.25 * (at(p, 5, ri, j, k) + at(p, 5, ri, j, k + 1) + at(p, 5, ri - 1, j, k) + at(p, 5, ri - 1, j, k + 1)));
+    val[5] = 0.25 * (at(p, 4, ri, j, k) + at(p, 4, ri, j + 1, k) + at(p, 4, ri - 1, j, k) + at(p, 4, ri - 1, j + 1, k));
+    cell = static_cast<long long>(j - lj) * (rk - lk) + (k - lk);
+  } else if (face == 1) {   // k in [lk, rk), i in [li, ri): jz jx mz mx (yn), then yp
+    const int i = li + u, k = lk + v;
+    if (i >= ri || k >= rk) return;
+    val[2] = -1 * (0.5 * (at(p, 0, i, lj, k) + at(p, 0, i, lj + 1, k)));
+    val[3] = 0.5 * (at(p, 2, i, lj, k) + at(p, 2, i + 1, lj, k));
+    val[0] = 0.25 * (at(p, 3, i + 1, lj, k) + at(p, 3, i, lj, k) + at(p, 3, i + 1, lj - 1, k) + at(p, 3, i, lj - 1, k));
+    val[1] = -1 * (0.25 * (at(p, 5, i, lj, k) + at(p, 5, i, lj, k + 1) + at(p, 5, i, lj - 1, k) + at(p, 5, i, lj - 1, k + 1)));
+    val[6] = 0.5 * (at(p, 0, i, rj, k) + at(p, 0, i, rj + 1, k));
+    val[7] = -1 * (0.5 * (at(p, 2, i, rj, k) + at(p, 2, i + 1, rj, k)));
+    val[4] = -1 * (0.25 * (at(p, 3, i + 1, rj, k) + at(p, 3, i, rj, k) + at(p, 3, i + 1, rj - 1, k) + at(p, 3, i, rj - 1, k)));
+    val[5] = 0.25 * (at(p, 5, i, rj, k) + at(p, 5, i, rj, k + 1) + at(p, 5, i, rj - 1, k) + at(p, 5, i, rj - 1, k + 1));
+    cell = static_cast<long long>(k - lk) * (ri - li) + (i - li);
+  } else {   // i in [li, ri), j in [lj, rj): jx jy mx my (zn), then zp
+    const int j = lj + u, i = li + v;
+    if (j >= rj || i >= ri) return;
+    val[2] = -1 * (0.5 * (at(p, 1, i, j, lk) + at(p, 1, i + 1, j, lk)));
+    val[3] = 0.5 * (at(p, 0, i, j, lk) + at(p, 0, i, j, lk + 1));
+    val[0] = 0.25 * (at(p, 4, i, j, lk) + at(p, 4, i, j + 1, lk) + at(p, 4, i, j, lk - 1) + at(p, 4, i, j + 1, lk - 1));
+    val[1] = -1 * (0.25 * (at(p, 3, i + 1, j, lk) + at(p, 3, i, j, lk) + at(p, 3, i + 1, j, lk - 1) + at(p, 3, i, j, lk - 1)));
+    val[6] = 0.5 * (at(p, 1, i, j, rk) + at(p, 1, i + 1, j, rk));
+    val[7] = -1 * (0.5 * (at(p, 0, i, j, rk) + at(p, 0, i, j, rk + 1)));
+    val[4] = -1 * (0.25 * (at(p, 4, i, j, rk) + at(p, 4, i, j + 1, rk) + at(p, 4, i, j, rk - 1) + at(p, 4, i, j + 1, rk - 1)));
+    val[5] = 0.25 * (at(p, 3, i + 1, j, rk) + at(p, 3, i, j, rk) + at(p, 3, i + 1, j, rk - 1) + at(p, 3, i, j, rk - 1));
+    cell = static_cast<long long>(i - li) * (rj - lj) + (j - lj);
+  }
+  T *b = p.buf + (static_cast<long long>(t % p.batch) * 24 + face * 8) * p.max_plane + cell;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) b[q * p.max_plane] = static_cast<T>(val[q]);
+}
+
+// acc += v[s] * phase[t0 + s] for the `count` steps ending at p.step, one
+// step at a time in step order.
+template <typename T>
+__global__ void k_fold(OpParams<T> p, int count) {
+  const int face = blockIdx.z;
+  const long long cell = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (cell >= p.plane[face]) return;
+  const long long t_last = p.step, t0 = t_last - count + 1;
+  for (int q = 0; q < 8; ++q) {
+    const double2 *ph = (q % 4) < 2 ? p.pj : p.pm;   // J terms at (t+1/2) dt, M terms at t dt
+    for (int n = 0; n < p.nf; ++n) {
+      double2 *a = p.acc[face * 8 + q] + n * p.plane[face] + cell;
+      double2 r = *a;
+      for (int s = 0; s < count; ++s) {
+        const long long t = t0 + s;
+        const double v = static_cast<double>(p.buf[(static_cast<long long>(t % p.batch) * 24 + face * 8 + q) * p.max_plane + cell]);
+        const double2 f = ph[n * p.total + t];
+        r.x += v * f.x;
+        r.y += v * f.y;
+      }
+      *a = r;
+    }
+  }
+}
+
+// Validates the description on the host (no device call before it passes),
+// then looks up the scratch and launches.
+template <typename T>
+int run(const xfdtd_nffft_operator *op) {
+  OpParams<T> p{};
+  const long long n[3] = {op->nx, op->ny, op->nz};
+  for (int a = 0; a < 3; ++a) {
+    if (op->lo[a] < 1 || op->hi[a] <= op->lo[a] || op->hi[a] > n[a] - 1)
+      return fail(XFDTD_ERR_INVALID_PLAN, "NF-FF box outside the grid");
+    p.lo[a] = static_cast<int>(op->lo[a]);
+    p.hi[a] = static_cast<int>(op->hi[a]);
+  }
+  // reference component shapes (simulation_init.cpp:28-35), k contiguous
+  const long long shp[6][3] = {{n[0], n[1] + 1, n[2] + 1}, {n[0] + 1, n[1], n[2] + 1}, {n[0] + 1, n[1] + 1, n[2]},
+                               {n[0] + 1, n[1], n[2]},     {n[0], n[1] + 1, n[2]},     {n[0], n[1], n[2] + 1}};
+  for (int c = 0; c < 6; ++c) {
+    if (!op->fields[c]) return fail(XFDTD_ERR_INVALID_PLAN, "a field pointer is null");
+    p.f[c] = static_cast<const T *>(op->fields[c]);
+    p.sj[c] = shp[c][2];
+    p.si[c] = shp[c][1] * shp[c][2];
+  }
+  const long long bx = p.hi[0] - p.lo[0], by = p.hi[1] - p.lo[1], bz = p.hi[2] - p.lo[2];
+  p.plane[0] = by * bz;
+  p.plane[1] = bz * bx;
+  p.plane[2] = bx * by;
+  p.max_plane = p.plane[0] > p.plane[1] ? p.plane[0] : p.plane[1];
+  if (p.plane[2] > p.max_plane) p.max_plane = p.plane[2];
+  if (op->batch < 1 || op->n_freq < 1 || op->total_steps < 1 || op->step < 0 || op->step >= op->total_steps)
+    return fail(XFDTD_ERR_INVALID_PLAN, "batch, n_freq, total_steps and step must be positive and in range");
+  if (op->fold_count < 0 || op->fold_count > op->batch || op->fold_count > op->step + 1)
+    return fail(XFDTD_ERR_INVALID_PLAN, "fold_count must be within the batch and the steps taken");
+  const unsigned long long need = static_cast<unsigned long long>(op->batch) * 24ull * p.max_plane * sizeof(T);
+  if (need > kScratchBytes)
+    return fail(XFDTD_ERR_INVALID_PLAN, "NF-FF batch exceeds the 64 MiB allocation-free scratch (batch x 24 x face cells)");
+  if (!op->phase_j || !op->phase_m) return fail(XFDTD_ERR_INVALID_PLAN, "phase tables are required");
+  for (int q = 0; q < 24; ++q) {
+    if (!op->acc[q]) return fail(XFDTD_ERR_INVALID_PLAN, "an accumulator pointer is null");
+    p.acc[q] = reinterpret_cast<double2 *>(op->acc[q]);
+  }
+  p.nf = op->n_freq;
+  p.pj = reinterpret_cast<const double2 *>(op->phase_j);
+  p.pm = reinterpret_cast<const double2 *>(op->phase_m);
+  p.total = op->total_steps;
+  p.batch = op->batch;
+  p.step = op->step;
+  void *scratch = nullptr;
+  const int rc = scratch_on_device(op->device, &scratch);
+  if (rc != XFDTD_OK) return rc;
+  p.buf = static_cast<T *>(scratch);
+  cudaStream_t st = static_cast<cudaStream_t>(op->stream);
+  // face 0 spans (k, j), face 1 (i, k), face 2 (j, i): cover the longest edge on both grid axes
+  const long long m = bx > by ? (bx > bz ? bx : bz) : (by > bz ? by : bz);
+  dim3 block(32, 8, 1);
+  dim3 grid(static_cast<unsigned>((m + 31) / 32), static_cast<unsigned>((m + 7) / 8), 3);
+  k_sample<T><<<grid, block, 0, st>>>(p);
+  if (cudaGetLastError() != cudaSuccess) return fail(XFDTD_ERR_CUDA, "NF-FF sample launch failed");
+  if (op->fold_count > 0) {
+    dim3 g2(static_cast<unsigned>((p.max_plane + 255) / 256), 1, 3);
+    k_fold<T><<<g2, 256, 0, st>>>(p, op->fold_count);
+    if (cudaGetLastError() != cudaSuccess) return fail(XFDTD_ERR_CUDA, "NF-FF fold launch failed");
+  }
+  return XFDTD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xfdtd_nffft_noalloc_setup(int device) {
+  void *scratch = nullptr;
+  return scratch_on_device(device, &scratch);
+}
+
+int xfdtd_nffft_dft_noalloc(const xfdtd_nffft_operator *op) {
+  if (!op) return fail(XFDTD_ERR_INVALID_PLAN, "null operator description");
+  if (op->precision != XFDTD_FP64 && op->precision != XFDTD_FP32)
+    return fail(XFDTD_ERR_INVALID_PLAN, "precision must be FP64 or FP32");
+  return op->precision == XFDTD_FP64 ? run<double>(op) : run<float>(op);
+}
+
+int64_t xfdtd_nffft_noalloc_max_bytes(void) { return static_cast<int64_t>(kScratchBytes); }
+
+const char *xfdtd_nffft_noalloc_last_error(void) { return g_err; }
+
+}  // extern "C"

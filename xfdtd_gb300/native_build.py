@@ -34,9 +34,9 @@ def _nvcc() -> str:
 
 
 def cuda_cmd(out: str = CUDA_LIB, extra=()) -> list:
-    src = os.path.join(HERE, "csrc", "engine.cu")
+    srcs = [os.path.join(HERE, "csrc", f) for f in ("engine.cu", "nffft_noalloc.cu")]
     return [_nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-            *extra, "-o", out, src]
+            *extra, "-o", out, *srcs]
 
 
 def host_cmd() -> list:
