@@ -155,6 +155,8 @@ def _peaks():
 
 
 # --------------------------------------------------------------- roofline ---
+SIDE_STREAM_KERNELS = ("tfsf_aux",)
+
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
 # from an ncu --set full capture of that kernel on this workload
 # (python -m xfdtd_gb300.run --config dielectric_sphere --steps 24 --precision fp32 --no-graph).
@@ -290,8 +292,12 @@ def ours_arm(args, world, rank, local, grp):
     slabs = _slab_layers(sc)
     alg = algorithmic_bytes(n, slabs, args.precision, dom)
     achieved = alg / (dom_ms / dom_n / 1e3) / 1e9
+    # the TFSF 1-D line runs on a side stream beside update_e: its event time
+    # overlaps the main stream's and is reported apart from the shares
+    side = {k: prof.pop(k) for k in SIDE_STREAM_KERNELS if k in prof}
     total_prof = sum(v[0] for v in prof.values())
     shares = {k: round(v[0] / total_prof, 4) for k, v in prof.items()}
+    shares.update({f"{k} (concurrent)": round(v[0] / total_prof, 4) for k, v in side.items()})
     del sim
 
     # e2e: one whole job through the public API, host scene to host results

@@ -17,9 +17,9 @@
 // are added inside the volume kernels, before the lumped and TFSF
 // corrections rather than after them.  The two only meet on cells where a
 // TFSF face or a lumped element lies inside a CPML slab, where the same
-// terms are added in another order.  The step index lives on the device (k_advance bumps it), so a
-// captured CUDA graph of G steps (G a multiple of the NF-FF batch) replays
-// for any starting step on a batch boundary.
+// terms are added in another order.  The step index lives on the device
+// (k_advance bumps it), so a captured CUDA graph of G steps (G a multiple of
+// the NF-FF batch) replays for any starting step on a batch boundary.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -73,6 +73,8 @@ struct xfdtd_handle {
   double dl[3] = {0, 0, 0};
   double dt = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;            // the TFSF 1-D line runs here, forked and joined per step
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<void *> allocs;
   size_t bytes = 0;
   long long h2d = 0, d2h = 0;   // bytes copied host<->device
@@ -107,6 +109,7 @@ struct xfdtd_handle {
   double2 *acc[24] = {};
   long long acc_len[24] = {};
   double2 *phase_j = nullptr, *phase_m = nullptr;
+  float2 *phase_jf = nullptr, *phase_mf = nullptr;
   double *ff_theta = nullptr, *ff_phi = nullptr, *ff_k = nullptr;
   double2 *ff_out[8] = {};
   double *ff_power[2] = {};
@@ -185,6 +188,9 @@ struct xfdtd_handle {
     if (gexec) cudaGraphExecDestroy(gexec);
     for (auto e : ev_pool) cudaEventDestroy(e);
     for (void *p : allocs) cudaFree(p);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -209,7 +215,7 @@ int guarded(xfdtd_handle *h, F &&fn) {
 void invalid(const std::string &m) { throw Err{XFDTD_ERR_INVALID_PLAN, m}; }
 
 // ------------------------------------------------------------ launches ---
-void prof_begin(xfdtd_handle *h, int id) {
+void prof_begin(xfdtd_handle *h, int id, cudaStream_t st = nullptr) {
   h->launch_count += 1;   // every per-step kernel launch passes here
   if (!(h->flags & XFDTD_FLAG_PROFILE)) return;
   size_t need = h->ev_pending.size() * 2 + 2;
@@ -219,13 +225,13 @@ void prof_begin(xfdtd_handle *h, int id) {
     h->ev_pool.push_back(e);
   }
   int s = static_cast<int>(h->ev_pending.size() * 2);
-  XCHECK(cudaEventRecord(h->ev_pool[s], h->stream));
+  XCHECK(cudaEventRecord(h->ev_pool[s], st ? st : h->stream));
   h->ev_pending.push_back({id, s});
 }
-void prof_end(xfdtd_handle *h) {
+void prof_end(xfdtd_handle *h, cudaStream_t st = nullptr) {
   if (!(h->flags & XFDTD_FLAG_PROFILE)) return;
   int s = h->ev_pending.back().second;
-  XCHECK(cudaEventRecord(h->ev_pool[s + 1], h->stream));
+  XCHECK(cudaEventRecord(h->ev_pool[s + 1], st ? st : h->stream));
 }
 void prof_collect(xfdtd_handle *h) {
   if (h->ev_pending.empty()) return;
@@ -423,6 +429,8 @@ void launch_nffft(xfdtd_handle *h) {
   for (int q = 0; q < 24; ++q) p.acc[q] = h->acc[q];
   p.pj = h->phase_j;
   p.pm = h->phase_m;
+  p.pjf = h->phase_jf;
+  p.pmf = h->phase_mf;
   p.total = h->total;
   p.step = h->d_step;
   for (int g = 0; g < 3; ++g) p.buf[g] = static_cast<T *>(h->nf_buf[g]);
@@ -449,6 +457,8 @@ void launch_nffft_accumulate(xfdtd_handle *h, int count, int lag) {
   for (int q = 0; q < 24; ++q) p.acc[q] = h->acc[q];
   p.pj = h->phase_j;
   p.pm = h->phase_m;
+  p.pjf = h->phase_jf;
+  p.pmf = h->phase_mf;
   p.total = h->total;
   p.step = h->d_step;
   for (int g = 0; g < 3; ++g) p.buf[g] = static_cast<T *>(h->nf_buf[g]);
@@ -507,10 +517,16 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     a.step = h->d_step;
     a.total = h->total;
     a.status = h->d_status;
-    prof_begin(h, 0);
-    xg::k_tfsf_aux<<<1, 512, 0, h->stream>>>(a);
+    // The 1-D line of step t runs on a side stream, beside the E update: it
+    // must follow the E corrections of step t-1 (which read the buffer it
+    // writes) and precede the H corrections of step t (joined there).
+    XCHECK(cudaEventRecord(h->ev_fork, h->stream));
+    XCHECK(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
+    prof_begin(h, 0, h->side);
+    xg::k_tfsf_aux<<<1, 512, 0, h->side>>>(a);
     XCHECK(cudaGetLastError());
-    prof_end(h);
+    prof_end(h, h->side);
+    XCHECK(cudaEventRecord(h->ev_join, h->side));
   }
   prof_begin(h, 1);
   launch_volume<T, I>(h, true);
@@ -535,6 +551,7 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
   launch_volume<T, I>(h, false);
   prof_end(h);
   if (h->tfsf) {
+    XCHECK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
     const auto sp = tfsf_surf_params<T>(h);
     const long long n = xg::surface_count(h->tf_lo[0] - 1, h->tf_hi[0], h->tf_lo[1] - 1, h->tf_hi[1],
                                           h->tf_lo[2] - 1, h->tf_hi[2]);
@@ -646,6 +663,9 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   const long long NX1 = pl->nx + 1, NY1 = pl->ny + 1, NZ1 = pl->nz + 1;
 
   XCHECK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  XCHECK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+  XCHECK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+  XCHECK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
   for (int c = 0; c < 6; ++c) h->F[c] = h->alloc_bytes(d.cells * h->esize);
 
   // material index, repacked into the padded layout
@@ -778,6 +798,16 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     if (!np.phase_j || !np.phase_m || !np.wave_number) invalid("NF-FF phase tables are required");
     h->phase_j = h->upload<double2>(reinterpret_cast<const double2 *>(np.phase_j), np.n_freq * pl->total_steps);
     h->phase_m = h->upload<double2>(reinterpret_cast<const double2 *>(np.phase_m), np.n_freq * pl->total_steps);
+    if (h->precision == XFDTD_FP32) {   // FP32 copies for the FP32 form's batch partial sums
+      const size_t n2 = static_cast<size_t>(np.n_freq) * pl->total_steps * 2;
+      std::vector<float> fj(n2), fm(n2);
+      for (size_t q = 0; q < n2; ++q) {
+        fj[q] = static_cast<float>(np.phase_j[q]);
+        fm[q] = static_cast<float>(np.phase_m[q]);
+      }
+      h->phase_jf = h->upload<float2>(reinterpret_cast<const float2 *>(fj.data()), n2 / 2);
+      h->phase_mf = h->upload<float2>(reinterpret_cast<const float2 *>(fm.data()), n2 / 2);
+    }
     h->ff_k = h->upload<double>(np.wave_number, np.n_freq);
     if (np.n_theta > 0 && np.n_phi > 0) {
       h->ff_theta = h->upload<double>(np.theta, np.n_theta);

@@ -84,9 +84,12 @@ struct OpParams {
   double2 *acc[24];
 };
 
+// Face-centre averages are taken in the field precision (FP64 as the
+// reference does; FP32 for FP32 fields, whose samples are stored as FP32),
+// as the engine's own NF-FF kernel does.
 template <typename T>
-__device__ __forceinline__ double at(const OpParams<T> &p, int c, int i, int j, int k) {
-  return static_cast<double>(p.f[c][static_cast<long long>(i) * p.si[c] + static_cast<long long>(j) * p.sj[c] + k]);
+__device__ __forceinline__ T at(const OpParams<T> &p, int c, int i, int j, int k) {
+  return p.f[c][static_cast<long long>(i) * p.si[c] + static_cast<long long>(j) * p.sj[c] + k];
 }
 
 // Samples the 24 surface currents of step p.step (reference accumulator
@@ -98,52 +101,56 @@ __global__ void k_sample(OpParams<T> p) {
   const int face = blockIdx.z;
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   const int v = blockIdx.y * blockDim.y + threadIdx.y;
-  double val[8];
+  T val[8];
+  const T half = T(0.5), quarter = T(0.25), neg = T(-1);
   long long cell;
   if (face == 0) {   // j in [lj, rj), k in [lk, rk): jy jz my mz (xn), then xp
     const int k = lk + u, j = lj + v;
     if (k >= rk || j >= rj) return;
-    val[2] = -1 * (0.5 * (at(p, 2, li, j, k) + at(p, 2, li, j + 1, k)));
-    val[3] = 0.5 * (at(p, 1, li, j, k) + at(p, 1, li, j, k + 1));
-    val[0] = 0.25 * (at(p, 5, li, j, k) + at(p, 5, li, j, k + 1) + at(p, 5, li - 1, j, k) + at(p, 5, li - 1, j, k + 1));
-    val[1] = -1 * (0.25 * (at(p, 4, li, j, k) + at(p, 4, li, j + 1, k) + at(p, 4, li - 1, j, k) + at(p, 4, li - 1, j + 1, k)));
-    val[6] = 0.5 * (at(p, 2, ri, j, k) + at(p, 2, ri, j + 1, k));
-    val[7] = -1 * (0.5 * (at(p, 1, ri, j, k) + at(p, 1, ri, j, k + 1)));
-    val[4] = -1 * (0.25 * (at(p, 5, ri, j, k) + at(p, 5, ri, j, k + 1) + at(p, 5, ri - 1, j, k) + at(p, 5, ri - 1, j, k + 1)));
-    val[5] = 0.25 * (at(p, 4, ri, j, k) + at(p, 4, ri, j + 1, k) + at(p, 4, ri - 1, j, k) + at(p, 4, ri - 1, j + 1, k));
+    val[2] = neg * (half * (at(p, 2, li, j, k) + at(p, 2, li, j + 1, k)));
+    val[3] = half * (at(p, 1, li, j, k) + at(p, 1, li, j, k + 1));
+    val[0] = quarter * (at(p, 5, li, j, k) + at(p, 5, li, j, k + 1) + at(p, 5, li - 1, j, k) + at(p, 5, li - 1, j, k + 1));
+    val[1] = neg * (quarter * (at(p, 4, li, j, k) + at(p, 4, li, j + 1, k) + at(p, 4, li - 1, j, k) + at(p, 4, li - 1, j + 1, k)));
+    val[6] = half * (at(p, 2, ri, j, k) + at(p, 2, ri, j + 1, k));
+    val[7] = neg * (half * (at(p, 1, ri, j, k) + at(p, 1, ri, j, k + 1)));
+    val[4] = neg * (quarter * (at(p, 5, ri, j, k) + at(p, 5, ri, j, k + 1) + at(p, 5, ri - 1, j, k) + at(p, 5, ri - 1, j, k + 1)));
+    val[5] = quarter * (at(p, 4, ri, j, k) + at(p, 4, ri, j + 1, k) + at(p, 4, ri - 1, j, k) + at(p, 4, ri - 1, j + 1, k));
     cell = static_cast<long long>(j - lj) * (rk - lk) + (k - lk);
   } else if (face == 1) {   // k in [lk, rk), i in [li, ri): jz jx mz mx (yn), then yp
     const int i = li + u, k = lk + v;
     if (i >= ri || k >= rk) return;
-    val[2] = -1 * (0.5 * (at(p, 0, i, lj, k) + at(p, 0, i, lj + 1, k)));
-    val[3] = 0.5 * (at(p, 2, i, lj, k) + at(p, 2, i + 1, lj, k));
-    val[0] = 0.25 * (at(p, 3, i + 1, lj, k) + at(p, 3, i, lj, k) + at(p, 3, i + 1, lj - 1, k) + at(p, 3, i, lj - 1, k));
-    val[1] = -1 * (0.25 * (at(p, 5, i, lj, k) + at(p, 5, i, lj, k + 1) + at(p, 5, i, lj - 1, k) + at(p, 5, i, lj - 1, k + 1)));
-    val[6] = 0.5 * (at(p, 0, i, rj, k) + at(p, 0, i, rj + 1, k));
-    val[7] = -1 * (0.5 * (at(p, 2, i, rj, k) + at(p, 2, i + 1, rj, k)));
-    val[4] = -1 * (0.25 * (at(p, 3, i + 1, rj, k) + at(p, 3, i, rj, k) + at(p, 3, i + 1, rj - 1, k) + at(p, 3, i, rj - 1, k)));
-    val[5] = 0.25 * (at(p, 5, i, rj, k) + at(p, 5, i, rj, k + 1) + at(p, 5, i, rj - 1, k) + at(p, 5, i, rj - 1, k + 1));
+    val[2] = neg * (half * (at(p, 0, i, lj, k) + at(p, 0, i, lj + 1, k)));
+    val[3] = half * (at(p, 2, i, lj, k) + at(p, 2, i + 1, lj, k));
+    val[0] = quarter * (at(p, 3, i + 1, lj, k) + at(p, 3, i, lj, k) + at(p, 3, i + 1, lj - 1, k) + at(p, 3, i, lj - 1, k));
+    val[1] = neg * (quarter * (at(p, 5, i, lj, k) + at(p, 5, i, lj, k + 1) + at(p, 5, i, lj - 1, k) + at(p, 5, i, lj - 1, k + 1)));
+    val[6] = half * (at(p, 0, i, rj, k) + at(p, 0, i, rj + 1, k));
+    val[7] = neg * (half * (at(p, 2, i, rj, k) + at(p, 2, i + 1, rj, k)));
+    val[4] = neg * (quarter * (at(p, 3, i + 1, rj, k) + at(p, 3, i, rj, k) + at(p, 3, i + 1, rj - 1, k) + at(p, 3, i, rj - 1, k)));
+    val[5] = quarter * (at(p, 5, i, rj, k) + at(p, 5, i, rj, k + 1) + at(p, 5, i, rj - 1, k) + at(p, 5, i, rj - 1, k + 1));
     cell = static_cast<long long>(k - lk) * (ri - li) + (i - li);
   } else {   // i in [li, ri), j in [lj, rj): jx jy mx my (zn), then zp
     const int j = lj + u, i = li + v;
     if (j >= rj || i >= ri) return;
-    val[2] = -1 * (0.5 * (at(p, 1, i, j, lk) + at(p, 1, i + 1, j, lk)));
-    val[3] = 0.5 * (at(p, 0, i, j, lk) + at(p, 0, i, j, lk + 1));
-    val[0] = 0.25 * (at(p, 4, i, j, lk) + at(p, 4, i, j + 1, lk) + at(p, 4, i, j, lk - 1) + at(p, 4, i, j + 1, lk - 1));
-    val[1] = -1 * (0.25 * (at(p, 3, i + 1, j, lk) + at(p, 3, i, j, lk) + at(p, 3, i + 1, j, lk - 1) + at(p, 3, i, j, lk - 1)));
-    val[6] = 0.5 * (at(p, 1, i, j, rk) + at(p, 1, i + 1, j, rk));
-    val[7] = -1 * (0.5 * (at(p, 0, i, j, rk) + at(p, 0, i, j, rk + 1)));
-    val[4] = -1 * (0.25 * (at(p, 4, i, j, rk) + at(p, 4, i, j + 1, rk) + at(p, 4, i, j, rk - 1) + at(p, 4, i, j + 1, rk - 1)));
-    val[5] = 0.25 * (at(p, 3, i + 1, j, rk) + at(p, 3, i, j, rk) + at(p, 3, i + 1, j, rk - 1) + at(p, 3, i, j, rk - 1));
+    val[2] = neg * (half * (at(p, 1, i, j, lk) + at(p, 1, i + 1, j, lk)));
+    val[3] = half * (at(p, 0, i, j, lk) + at(p, 0, i, j, lk + 1));
+    val[0] = quarter * (at(p, 4, i, j, lk) + at(p, 4, i, j + 1, lk) + at(p, 4, i, j, lk - 1) + at(p, 4, i, j + 1, lk - 1));
+    val[1] = neg * (quarter * (at(p, 3, i + 1, j, lk) + at(p, 3, i, j, lk) + at(p, 3, i + 1, j, lk - 1) + at(p, 3, i, j, lk - 1)));
+    val[6] = half * (at(p, 1, i, j, rk) + at(p, 1, i + 1, j, rk));
+    val[7] = neg * (half * (at(p, 0, i, j, rk) + at(p, 0, i, j, rk + 1)));
+    val[4] = neg * (quarter * (at(p, 4, i, j, rk) + at(p, 4, i, j + 1, rk) + at(p, 4, i, j, rk - 1) + at(p, 4, i, j + 1, rk - 1)));
+    val[5] = quarter * (at(p, 3, i + 1, j, rk) + at(p, 3, i, j, rk) + at(p, 3, i + 1, j, rk - 1) + at(p, 3, i, j, rk - 1));
     cell = static_cast<long long>(i - li) * (rj - lj) + (j - lj);
   }
   T *b = p.buf + (static_cast<long long>(t % p.batch) * 24 + face * 8) * p.max_plane + cell;
 #pragma unroll
-  for (int q = 0; q < 8; ++q) b[q * p.max_plane] = static_cast<T>(val[q]);
+  for (int q = 0; q < 8; ++q) b[q * p.max_plane] = val[q];
 }
 
-// acc += v[s] * phase[t0 + s] for the `count` steps ending at p.step, one
-// step at a time in step order.
+// acc += v[s] * phase[t0 + s] for the `count` steps ending at p.step, the
+// engine's fold (k_nffft_accumulate): FP64 samples are added one step at a
+// time in step order; FP32 samples are summed over the batch in FP32, with
+// the phases rounded to FP32, and the partial sum goes to the FP64
+// accumulator.
 template <typename T>
 __global__ void k_fold(OpParams<T> p, int count) {
   const int face = blockIdx.z;
@@ -151,16 +158,26 @@ __global__ void k_fold(OpParams<T> p, int count) {
   if (cell >= p.plane[face]) return;
   const long long t_last = p.step, t0 = t_last - count + 1;
   for (int q = 0; q < 8; ++q) {
-    const double2 *ph = (q % 4) < 2 ? p.pj : p.pm;   // J terms at (t+1/2) dt, M terms at t dt
+    const double2 *ph = ((q % 4) < 2 ? p.pj : p.pm) + t0;   // J terms at (t+1/2) dt, M terms at t dt
     for (int n = 0; n < p.nf; ++n) {
       double2 *a = p.acc[face * 8 + q] + n * p.plane[face] + cell;
       double2 r = *a;
+      float2 part = make_float2(0.f, 0.f);
       for (int s = 0; s < count; ++s) {
         const long long t = t0 + s;
-        const double v = static_cast<double>(p.buf[(static_cast<long long>(t % p.batch) * 24 + face * 8 + q) * p.max_plane + cell]);
-        const double2 f = ph[n * p.total + t];
-        r.x += v * f.x;
-        r.y += v * f.y;
+        const T v = p.buf[(static_cast<long long>(t % p.batch) * 24 + face * 8 + q) * p.max_plane + cell];
+        const double2 f = ph[n * p.total + s];
+        if constexpr (sizeof(T) == 8) {
+          r.x = fma(v, f.x, r.x);
+          r.y = fma(v, f.y, r.y);
+        } else {
+          part.x = fmaf(v, static_cast<float>(f.x), part.x);
+          part.y = fmaf(v, static_cast<float>(f.y), part.y);
+        }
+      }
+      if constexpr (sizeof(T) == 4) {
+        r.x += static_cast<double>(part.x);
+        r.y += static_cast<double>(part.y);
       }
       *a = r;
     }

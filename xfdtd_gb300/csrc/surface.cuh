@@ -81,6 +81,7 @@ struct NfParams {
   int nf;
   double2 *acc[24];
   const double2 *pj, *pm;   // [nf][total]
+  const float2 *pjf, *pmf;  // the same tables rounded to FP32 (FP32 form only)
   long long total;
   const long long *step;
   T *buf[3];                // per face pair: [batch][8][face cells] surface values
@@ -94,55 +95,58 @@ __global__ void k_nffft(NfParams<T> p) {
   const int li = p.lo[0], lj = p.lo[1], lk = p.lo[2], ri = p.hi[0], rj = p.hi[1], rk = p.hi[2];
   const long long si = p.d.si, sj = p.d.sj;
   const T *ex = p.E[0], *ey = p.E[1], *ez = p.E[2], *hx = p.H[0], *hy = p.H[1], *hz = p.H[2];
-  auto at = [&](const T *f, int i, int j, int k) -> double {
-    return static_cast<double>(f[static_cast<long long>(i) * si + static_cast<long long>(j) * sj + k]);
+  // the face-centre averages are taken in the field precision: FP64 as the
+  // reference does; FP32 in the FP32 form, whose samples are stored as FP32
+  auto at = [&](const T *f, int i, int j, int k) -> T {
+    return f[static_cast<long long>(i) * si + static_cast<long long>(j) * sj + k];
   };
+  const T half = T(0.5), quarter = T(0.25), neg = T(-1);
   const int face = blockIdx.z;
   const int u = blockIdx.x * blockDim.x + threadIdx.x;   // fastest face axis
   const int v = blockIdx.y * blockDim.y + threadIdx.y;
-  double val[8];
+  T val[8];
   long long cell, plane;
   int base;
   if (face == 0) {  // X faces: j in [lj, rj), k in [lk, rk); jy, jz, my, mz
     const int k = lk + u, j = lj + v;
     if (k >= rk || j >= rj) return;
     // M = -/+ E face centres, J = +/- H face centres
-    val[2] = -1 * (0.5 * (at(ez, li, j, k) + at(ez, li, j + 1, k)));            // my_xn
-    val[3] = 0.5 * (at(ey, li, j, k) + at(ey, li, j, k + 1));                   // mz_xn
-    val[0] = 0.25 * (at(hz, li, j, k) + at(hz, li, j, k + 1) + at(hz, li - 1, j, k) + at(hz, li - 1, j, k + 1));
-    val[1] = -1 * (0.25 * (at(hy, li, j, k) + at(hy, li, j + 1, k) + at(hy, li - 1, j, k) + at(hy, li - 1, j + 1, k)));
-    val[6] = 0.5 * (at(ez, ri, j, k) + at(ez, ri, j + 1, k));                   // my_xp
-    val[7] = -1 * (0.5 * (at(ey, ri, j, k) + at(ey, ri, j, k + 1)));            // mz_xp
-    val[4] = -1 * (0.25 * (at(hz, ri, j, k) + at(hz, ri, j, k + 1) + at(hz, ri - 1, j, k) + at(hz, ri - 1, j, k + 1)));
-    val[5] = 0.25 * (at(hy, ri, j, k) + at(hy, ri, j + 1, k) + at(hy, ri - 1, j, k) + at(hy, ri - 1, j + 1, k));
+    val[2] = neg * (half * (at(ez, li, j, k) + at(ez, li, j + 1, k)));            // my_xn
+    val[3] = half * (at(ey, li, j, k) + at(ey, li, j, k + 1));                   // mz_xn
+    val[0] = quarter * (at(hz, li, j, k) + at(hz, li, j, k + 1) + at(hz, li - 1, j, k) + at(hz, li - 1, j, k + 1));
+    val[1] = neg * (quarter * (at(hy, li, j, k) + at(hy, li, j + 1, k) + at(hy, li - 1, j, k) + at(hy, li - 1, j + 1, k)));
+    val[6] = half * (at(ez, ri, j, k) + at(ez, ri, j + 1, k));                   // my_xp
+    val[7] = neg * (half * (at(ey, ri, j, k) + at(ey, ri, j, k + 1)));            // mz_xp
+    val[4] = neg * (quarter * (at(hz, ri, j, k) + at(hz, ri, j, k + 1) + at(hz, ri - 1, j, k) + at(hz, ri - 1, j, k + 1)));
+    val[5] = quarter * (at(hy, ri, j, k) + at(hy, ri, j + 1, k) + at(hy, ri - 1, j, k) + at(hy, ri - 1, j + 1, k));
     cell = static_cast<long long>(j - lj) * (rk - lk) + (k - lk);
     plane = static_cast<long long>(rj - lj) * (rk - lk);
     base = 0;
   } else if (face == 1) {  // Y faces: k in [lk, rk), i in [li, ri); jz, jx, mz, mx
     const int k = lk + u, i = li + v;
     if (k >= rk || i >= ri) return;
-    val[2] = -1 * (0.5 * (at(ex, i, lj, k) + at(ex, i, lj + 1, k)));            // mz_yn
-    val[3] = 0.5 * (at(ez, i, lj, k) + at(ez, i + 1, lj, k));                   // mx_yn
-    val[0] = 0.25 * (at(hx, i + 1, lj, k) + at(hx, i, lj, k) + at(hx, i + 1, lj - 1, k) + at(hx, i, lj - 1, k));
-    val[1] = -1 * (0.25 * (at(hz, i, lj, k) + at(hz, i, lj, k + 1) + at(hz, i, lj - 1, k) + at(hz, i, lj - 1, k + 1)));
-    val[6] = 0.5 * (at(ex, i, rj, k) + at(ex, i, rj + 1, k));                   // mz_yp
-    val[7] = -1 * (0.5 * (at(ez, i, rj, k) + at(ez, i + 1, rj, k)));            // mx_yp
-    val[4] = -1 * (0.25 * (at(hx, i + 1, rj, k) + at(hx, i, rj, k) + at(hx, i + 1, rj - 1, k) + at(hx, i, rj - 1, k)));
-    val[5] = 0.25 * (at(hz, i, rj, k) + at(hz, i, rj, k + 1) + at(hz, i, rj - 1, k) + at(hz, i, rj - 1, k + 1));
+    val[2] = neg * (half * (at(ex, i, lj, k) + at(ex, i, lj + 1, k)));            // mz_yn
+    val[3] = half * (at(ez, i, lj, k) + at(ez, i + 1, lj, k));                   // mx_yn
+    val[0] = quarter * (at(hx, i + 1, lj, k) + at(hx, i, lj, k) + at(hx, i + 1, lj - 1, k) + at(hx, i, lj - 1, k));
+    val[1] = neg * (quarter * (at(hz, i, lj, k) + at(hz, i, lj, k + 1) + at(hz, i, lj - 1, k) + at(hz, i, lj - 1, k + 1)));
+    val[6] = half * (at(ex, i, rj, k) + at(ex, i, rj + 1, k));                   // mz_yp
+    val[7] = neg * (half * (at(ez, i, rj, k) + at(ez, i + 1, rj, k)));            // mx_yp
+    val[4] = neg * (quarter * (at(hx, i + 1, rj, k) + at(hx, i, rj, k) + at(hx, i + 1, rj - 1, k) + at(hx, i, rj - 1, k)));
+    val[5] = quarter * (at(hz, i, rj, k) + at(hz, i, rj, k + 1) + at(hz, i, rj - 1, k) + at(hz, i, rj - 1, k + 1));
     cell = static_cast<long long>(i - li) * (rk - lk) + (k - lk);
     plane = static_cast<long long>(ri - li) * (rk - lk);
     base = 8;
   } else {  // Z faces: i in [li, ri), j in [lj, rj); jx, jy, mx, my
     const int j = lj + u, i = li + v;
     if (j >= rj || i >= ri) return;
-    val[2] = -1 * (0.5 * (at(ey, i, j, lk) + at(ey, i + 1, j, lk)));            // mx_zn
-    val[3] = 0.5 * (at(ex, i, j, lk) + at(ex, i, j, lk + 1));                   // my_zn
-    val[0] = 0.25 * (at(hy, i, j, lk) + at(hy, i, j + 1, lk) + at(hy, i, j, lk - 1) + at(hy, i, j + 1, lk - 1));
-    val[1] = -1 * (0.25 * (at(hx, i + 1, j, lk) + at(hx, i, j, lk) + at(hx, i + 1, j, lk - 1) + at(hx, i, j, lk - 1)));
-    val[6] = 0.5 * (at(ey, i, j, rk) + at(ey, i + 1, j, rk));                   // mx_zp
-    val[7] = -1 * (0.5 * (at(ex, i, j, rk) + at(ex, i, j, rk + 1)));            // my_zp
-    val[4] = -1 * (0.25 * (at(hy, i, j, rk) + at(hy, i, j + 1, rk) + at(hy, i, j, rk - 1) + at(hy, i, j + 1, rk - 1)));
-    val[5] = 0.25 * (at(hx, i + 1, j, rk) + at(hx, i, j, rk) + at(hx, i + 1, j, rk - 1) + at(hx, i, j, rk - 1));
+    val[2] = neg * (half * (at(ey, i, j, lk) + at(ey, i + 1, j, lk)));            // mx_zn
+    val[3] = half * (at(ex, i, j, lk) + at(ex, i, j, lk + 1));                   // my_zn
+    val[0] = quarter * (at(hy, i, j, lk) + at(hy, i, j + 1, lk) + at(hy, i, j, lk - 1) + at(hy, i, j + 1, lk - 1));
+    val[1] = neg * (quarter * (at(hx, i + 1, j, lk) + at(hx, i, j, lk) + at(hx, i + 1, j, lk - 1) + at(hx, i, j, lk - 1)));
+    val[6] = half * (at(ey, i, j, rk) + at(ey, i + 1, j, rk));                   // mx_zp
+    val[7] = neg * (half * (at(ex, i, j, rk) + at(ex, i, j, rk + 1)));            // my_zp
+    val[4] = neg * (quarter * (at(hy, i, j, rk) + at(hy, i, j + 1, rk) + at(hy, i, j, rk - 1) + at(hy, i, j + 1, rk - 1)));
+    val[5] = quarter * (at(hx, i + 1, j, rk) + at(hx, i, j, rk) + at(hx, i + 1, j, rk - 1) + at(hx, i, j, rk - 1));
     cell = static_cast<long long>(i - li) * (rj - lj) + (j - lj);
     plane = static_cast<long long>(ri - li) * (rj - lj);
     base = 16;
@@ -151,12 +155,17 @@ __global__ void k_nffft(NfParams<T> p) {
   // folds a whole batch into the FP64 accumulators
   T *buf = p.buf[base / 8] + (static_cast<long long>(t % p.batch) * 8) * plane + cell;
 #pragma unroll
-  for (int q = 0; q < 8; ++q) buf[q * plane] = static_cast<T>(val[q]);
+  for (int q = 0; q < 8; ++q) buf[q * plane] = val[q];
 }
 
-// acc[n] += v[s] * phase[n][t0 + s] for the `count` buffered steps ending at
-// step *step - lag, added one step at a time in step order: the same
-// additions, in the same order, as accumulating every step (nffft_fd.cpp:117-203).
+// acc[n] += v[s] * phase[n][t0 + s] for the `count` (<= 8) buffered steps
+// ending at step *step - lag.  FP64 form: added one step at a time in step
+// order, the same additions in the same order as accumulating every step
+// (nffft_fd.cpp:117-203).  FP32 form: the batch's products are summed in FP32
+// (the samples are FP32 already) and the partial sum is added to the FP64
+// running sum, which carries the thousands-of-steps accumulation.
+constexpr int kMaxNfBatch = 8;
+
 template <typename T>
 __global__ void k_nffft_accumulate(NfParams<T> p, int count, int lag) {
   const int group = blockIdx.z;
@@ -167,19 +176,38 @@ __global__ void k_nffft_accumulate(NfParams<T> p, int count, int lag) {
   if (cell >= plane) return;
   const long long t_last = *p.step - lag;
   const long long t0 = t_last - count + 1;
-  if (t0 < 0 || t_last >= p.total) return;
+  if (t0 < 0 || t_last >= p.total || count > kMaxNfBatch) return;
   const T *buf = p.buf[group] + cell;
   for (int q = 0; q < 8; ++q) {
-    const double2 *ph = (q % 4) < 2 ? p.pj : p.pm;   // J terms use the (t+1/2) phase, M terms t
+    T v[kMaxNfBatch];
+#pragma unroll
+    for (int s = 0; s < kMaxNfBatch; ++s)
+      v[s] = s < count ? buf[(static_cast<long long>((t0 + s) % p.batch) * 8 + q) * plane] : T(0);
+    const bool j_term = (q % 4) < 2;   // J terms use the (t+1/2) phase, M terms t
     for (int n = 0; n < p.nf; ++n) {
       double2 *a = p.acc[group * 8 + q] + n * plane + cell;
       double2 r = *a;
-      for (int s = 0; s < count; ++s) {
-        const long long t = t0 + s;
-        const double v = static_cast<double>(buf[(static_cast<long long>(t % p.batch) * 8 + q) * plane]);
-        const double2 f = ph[n * p.total + t];
-        r.x += v * f.x;
-        r.y += v * f.y;
+      if constexpr (sizeof(T) == 8) {
+        const double2 *ph = (j_term ? p.pj : p.pm) + n * p.total + t0;
+#pragma unroll
+        for (int s = 0; s < kMaxNfBatch; ++s)
+          if (s < count) {
+            const double2 f = ph[s];
+            r.x = fma(static_cast<double>(v[s]), f.x, r.x);
+            r.y = fma(static_cast<double>(v[s]), f.y, r.y);
+          }
+      } else {
+        const float2 *ph = (j_term ? p.pjf : p.pmf) + n * p.total + t0;
+        float2 part = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int s = 0; s < kMaxNfBatch; ++s)
+          if (s < count) {
+            const float2 f = ph[s];
+            part.x = fmaf(static_cast<float>(v[s]), f.x, part.x);
+            part.y = fmaf(static_cast<float>(v[s]), f.y, part.y);
+          }
+        r.x += static_cast<double>(part.x);
+        r.y += static_cast<double>(part.y);
       }
       *a = r;
     }
@@ -345,32 +373,33 @@ __device__ __forceinline__ void add_corr(T &v, double corr) {
   v = static_cast<T>(static_cast<double>(v) + corr);
 }
 
-// Maps a linear surface index to (i, j, k) on the surface of [a0,a1]x[b0,b1]x[c0,c1].
-__device__ __forceinline__ bool surface_cell(long long q, int a0, int a1, int b0, int b1, int c0, int c1, int &i,
-                                             int &j, int &k) {
-  const long long nb = b1 - b0 + 1, nc = c1 - c0 + 1, na_in = a1 - a0 - 1, nb_in = b1 - b0 - 1;
-  const long long px = nb * nc, py = (na_in > 0 ? na_in : 0) * nc, pz = (na_in > 0 ? na_in : 0) * (nb_in > 0 ? nb_in : 0);
+// Maps a linear surface index to (i, j, k) on the surface of [a0,a1]x[b0,b1]x[c0,c1]
+// (32-bit arithmetic: a surface holds far fewer than 2^31 cells).
+__device__ __forceinline__ bool surface_cell(int q, int a0, int a1, int b0, int b1, int c0, int c1, int &i, int &j,
+                                             int &k) {
+  const int nb = b1 - b0 + 1, nc = c1 - c0 + 1, na_in = max(a1 - a0 - 1, 0), nb_in = max(b1 - b0 - 1, 0);
+  const int px = nb * nc, py = na_in * nc, pz = na_in * nb_in;
   if (q < 2 * px) {
     i = q < px ? a0 : a1;
-    const long long r = q % px;
-    j = b0 + static_cast<int>(r / nc);
-    k = c0 + static_cast<int>(r % nc);
+    const int r = q < px ? q : q - px;
+    j = b0 + r / nc;
+    k = c0 + r % nc;
     return true;
   }
   q -= 2 * px;
   if (q < 2 * py) {
     j = q < py ? b0 : b1;
-    const long long r = q % py;
-    i = a0 + 1 + static_cast<int>(r / nc);
-    k = c0 + static_cast<int>(r % nc);
+    const int r = q < py ? q : q - py;
+    i = a0 + 1 + r / nc;
+    k = c0 + r % nc;
     return true;
   }
   q -= 2 * py;
   if (q < 2 * pz) {
     k = q < pz ? c0 : c1;
-    const long long r = q % pz;
-    i = a0 + 1 + static_cast<int>(r / nb_in);
-    j = b0 + 1 + static_cast<int>(r % nb_in);
+    const int r = q < pz ? q : q - pz;
+    i = a0 + 1 + r / nb_in;
+    j = b0 + 1 + r % nb_in;
     return true;
   }
   return false;
@@ -381,72 +410,75 @@ __global__ void k_tfsf_e(TfsfSurfParams<T> p) {
   const TfsfDev &tf = p.tf;
   const int li = tf.lo[0], ri = tf.hi[0], lj = tf.lo[1], rj = tf.hi[1], lk = tf.lo[2], rk = tf.hi[2];
   int i, j, k;
-  const long long q = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (!surface_cell(q, li, ri, lj, rj, lk, rk, i, j, k)) return;
   const double *hinc = tf.inc + (((*p.step) + 1) & 1) * 6 * tf.L;   // incident H of the previous step
   const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
   // Ex: y faces (j = lj: -= cay Hz_inc(i, lj-1, k); j = rj: += cay Hz_inc(i, rj, k)),
   //     z faces (k = lk: += caz Hy_inc(i, j, lk-1); k = rk: -= caz Hy_inc(i, j, rk))
   {
-    T e = p.F[0][b];
-    bool w = false;
-    if ((j == lj || j == rj) && k >= lk && k <= rk && i >= li && i < ri) {
-      const int jj = j == lj ? lj - 1 : rj;
-      const double pr = tf.ph[0][i - li + 1] + tf.ph[1][jj - lj + 1] + tf.pf[2][k - lk] - 0.5;
-      const double v = tf.ca[1] * tfsf_interp(hinc + 5 * tf.L, pr);
-      add_corr(e, j == lj ? -v : v);
-      w = true;
+    const bool w1 = (j == lj || j == rj) && k >= lk && k <= rk && i >= li && i < ri;
+    const bool w2 = (k == lk || k == rk) && i >= li && i < ri && j >= lj && j <= rj;
+    if (w1 || w2) {
+      T e = p.F[0][b];
+      if (w1) {
+        const int jj = j == lj ? lj - 1 : rj;
+        const double pr = tf.ph[0][i - li + 1] + tf.ph[1][jj - lj + 1] + tf.pf[2][k - lk] - 0.5;
+        const double v = tf.ca[1] * tfsf_interp(hinc + 5 * tf.L, pr);
+        add_corr(e, j == lj ? -v : v);
+      }
+      if (w2) {
+        const int kk = k == lk ? lk - 1 : rk;
+        const double pr = tf.ph[0][i - li + 1] + tf.pf[1][j - lj] + tf.ph[2][kk - lk + 1] - 0.5;
+        const double v = tf.ca[2] * tfsf_interp(hinc + 4 * tf.L, pr);
+        add_corr(e, k == lk ? v : -v);
+      }
+      p.F[0][b] = e;
     }
-    if ((k == lk || k == rk) && i >= li && i < ri && j >= lj && j <= rj) {
-      const int kk = k == lk ? lk - 1 : rk;
-      const double pr = tf.ph[0][i - li + 1] + tf.pf[1][j - lj] + tf.ph[2][kk - lk + 1] - 0.5;
-      const double v = tf.ca[2] * tfsf_interp(hinc + 4 * tf.L, pr);
-      add_corr(e, k == lk ? v : -v);
-      w = true;
-    }
-    if (w) p.F[0][b] = e;
   }
   // Ey: x faces (i = li: += cax Hz_inc(li-1, j, k); i = ri: -= cax Hz_inc(ri, j, k)),
   //     z faces (k = lk: -= caz Hx_inc(i, j, lk-1); k = rk: += caz Hx_inc(i, j, rk))
   {
-    T e = p.F[1][b];
-    bool w = false;
-    if ((i == li || i == ri) && j >= lj && j < rj && k >= lk && k <= rk) {
-      const int ii = i == li ? li - 1 : ri;
-      const double pr = tf.ph[0][ii - li + 1] + tf.ph[1][j - lj + 1] + tf.pf[2][k - lk] - 0.5;
-      const double v = tf.ca[0] * tfsf_interp(hinc + 5 * tf.L, pr);
-      add_corr(e, i == li ? v : -v);
-      w = true;
+    const bool w1 = (i == li || i == ri) && j >= lj && j < rj && k >= lk && k <= rk;
+    const bool w2 = (k == lk || k == rk) && i >= li && i <= ri && j >= lj && j < rj;
+    if (w1 || w2) {
+      T e = p.F[1][b];
+      if (w1) {
+        const int ii = i == li ? li - 1 : ri;
+        const double pr = tf.ph[0][ii - li + 1] + tf.ph[1][j - lj + 1] + tf.pf[2][k - lk] - 0.5;
+        const double v = tf.ca[0] * tfsf_interp(hinc + 5 * tf.L, pr);
+        add_corr(e, i == li ? v : -v);
+      }
+      if (w2) {
+        const int kk = k == lk ? lk - 1 : rk;
+        const double pr = tf.pf[0][i - li] + tf.ph[1][j - lj + 1] + tf.ph[2][kk - lk + 1] - 0.5;
+        const double v = tf.ca[2] * tfsf_interp(hinc + 3 * tf.L, pr);
+        add_corr(e, k == lk ? -v : v);
+      }
+      p.F[1][b] = e;
     }
-    if ((k == lk || k == rk) && i >= li && i <= ri && j >= lj && j < rj) {
-      const int kk = k == lk ? lk - 1 : rk;
-      const double pr = tf.pf[0][i - li] + tf.ph[1][j - lj + 1] + tf.ph[2][kk - lk + 1] - 0.5;
-      const double v = tf.ca[2] * tfsf_interp(hinc + 3 * tf.L, pr);
-      add_corr(e, k == lk ? -v : v);
-      w = true;
-    }
-    if (w) p.F[1][b] = e;
   }
   // Ez: x faces (i = li: -= cax Hy_inc(li-1, j, k); i = ri: += cax Hy_inc(ri, j, k)),
   //     y faces (j = lj: += cay Hx_inc(i, lj-1, k); j = rj: -= cay Hx_inc(i, rj, k))
   {
-    T e = p.F[2][b];
-    bool w = false;
-    if ((i == li || i == ri) && j >= lj && j <= rj && k >= lk && k < rk) {
-      const int ii = i == li ? li - 1 : ri;
-      const double pr = tf.ph[0][ii - li + 1] + tf.pf[1][j - lj] + tf.ph[2][k - lk + 1] - 0.5;
-      const double v = tf.ca[0] * tfsf_interp(hinc + 4 * tf.L, pr);
-      add_corr(e, i == li ? -v : v);
-      w = true;
+    const bool w1 = (i == li || i == ri) && j >= lj && j <= rj && k >= lk && k < rk;
+    const bool w2 = (j == lj || j == rj) && k >= lk && k < rk && i >= li && i <= ri;
+    if (w1 || w2) {
+      T e = p.F[2][b];
+      if (w1) {
+        const int ii = i == li ? li - 1 : ri;
+        const double pr = tf.ph[0][ii - li + 1] + tf.pf[1][j - lj] + tf.ph[2][k - lk + 1] - 0.5;
+        const double v = tf.ca[0] * tfsf_interp(hinc + 4 * tf.L, pr);
+        add_corr(e, i == li ? -v : v);
+      }
+      if (w2) {
+        const int jj = j == lj ? lj - 1 : rj;
+        const double pr = tf.pf[0][i - li] + tf.ph[1][jj - lj + 1] + tf.ph[2][k - lk + 1] - 0.5;
+        const double v = tf.ca[1] * tfsf_interp(hinc + 3 * tf.L, pr);
+        add_corr(e, j == lj ? v : -v);
+      }
+      p.F[2][b] = e;
     }
-    if ((j == lj || j == rj) && k >= lk && k < rk && i >= li && i <= ri) {
-      const int jj = j == lj ? lj - 1 : rj;
-      const double pr = tf.pf[0][i - li] + tf.ph[1][jj - lj + 1] + tf.ph[2][k - lk + 1] - 0.5;
-      const double v = tf.ca[1] * tfsf_interp(hinc + 3 * tf.L, pr);
-      add_corr(e, j == lj ? v : -v);
-      w = true;
-    }
-    if (w) p.F[2][b] = e;
   }
 }
 
@@ -455,72 +487,75 @@ __global__ void k_tfsf_h(TfsfSurfParams<T> p) {
   const TfsfDev &tf = p.tf;
   const int li = tf.lo[0], ri = tf.hi[0], lj = tf.lo[1], rj = tf.hi[1], lk = tf.lo[2], rk = tf.hi[2];
   int i, j, k;
-  const long long q = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (!surface_cell(q, li - 1, ri, lj - 1, rj, lk - 1, rk, i, j, k)) return;
   const double *einc = tf.inc + ((*p.step) & 1) * 6 * tf.L;   // incident E of this step
   const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
   // Hx: y faces (j = lj-1: += cby Ez_inc(i, lj, k); j = rj: -= cby Ez_inc(i, rj, k)),
   //     z faces (k = lk-1: -= cbz Ey_inc(i, j, lk); k = rk: += cbz Ey_inc(i, j, rk))
   {
-    T h = p.F[3][b];
-    bool w = false;
-    if ((j == lj - 1 || j == rj) && k >= lk && k < rk && i >= li && i <= ri) {
-      const int jj = j == rj ? rj : lj;
-      const double pr = tf.pf[0][i - li] + tf.pf[1][jj - lj] + tf.ph[2][k - lk + 1];
-      const double v = tf.cb[1] * tfsf_interp(einc + 2 * tf.L, pr);
-      add_corr(h, j == rj ? -v : v);
-      w = true;
+    const bool w1 = (j == lj - 1 || j == rj) && k >= lk && k < rk && i >= li && i <= ri;
+    const bool w2 = (k == lk - 1 || k == rk) && i >= li && i <= ri && j >= lj && j < rj;
+    if (w1 || w2) {
+      T h = p.F[3][b];
+      if (w1) {
+        const int jj = j == rj ? rj : lj;
+        const double pr = tf.pf[0][i - li] + tf.pf[1][jj - lj] + tf.ph[2][k - lk + 1];
+        const double v = tf.cb[1] * tfsf_interp(einc + 2 * tf.L, pr);
+        add_corr(h, j == rj ? -v : v);
+      }
+      if (w2) {
+        const int kk = k == rk ? rk : lk;
+        const double pr = tf.pf[0][i - li] + tf.ph[1][j - lj + 1] + tf.pf[2][kk - lk];
+        const double v = tf.cb[2] * tfsf_interp(einc + 1 * tf.L, pr);
+        add_corr(h, k == rk ? v : -v);
+      }
+      p.F[3][b] = h;
     }
-    if ((k == lk - 1 || k == rk) && i >= li && i <= ri && j >= lj && j < rj) {
-      const int kk = k == rk ? rk : lk;
-      const double pr = tf.pf[0][i - li] + tf.ph[1][j - lj + 1] + tf.pf[2][kk - lk];
-      const double v = tf.cb[2] * tfsf_interp(einc + 1 * tf.L, pr);
-      add_corr(h, k == rk ? v : -v);
-      w = true;
-    }
-    if (w) p.F[3][b] = h;
   }
   // Hy: x faces (i = li-1: -= cbx Ez_inc(li, j, k); i = ri: += cbx Ez_inc(ri, j, k)),
   //     z faces (k = lk-1: += cbz Ex_inc(i, j, lk); k = rk: -= cbz Ex_inc(i, j, rk))
   {
-    T h = p.F[4][b];
-    bool w = false;
-    if ((i == li - 1 || i == ri) && j >= lj && j <= rj && k >= lk && k < rk) {
-      const int ii = i == ri ? ri : li;
-      const double pr = tf.pf[0][ii - li] + tf.pf[1][j - lj] + tf.ph[2][k - lk + 1];
-      const double v = tf.cb[0] * tfsf_interp(einc + 2 * tf.L, pr);
-      add_corr(h, i == ri ? v : -v);
-      w = true;
+    const bool w1 = (i == li - 1 || i == ri) && j >= lj && j <= rj && k >= lk && k < rk;
+    const bool w2 = (k == lk - 1 || k == rk) && i >= li && i < ri && j >= lj && j <= rj;
+    if (w1 || w2) {
+      T h = p.F[4][b];
+      if (w1) {
+        const int ii = i == ri ? ri : li;
+        const double pr = tf.pf[0][ii - li] + tf.pf[1][j - lj] + tf.ph[2][k - lk + 1];
+        const double v = tf.cb[0] * tfsf_interp(einc + 2 * tf.L, pr);
+        add_corr(h, i == ri ? v : -v);
+      }
+      if (w2) {
+        const int kk = k == rk ? rk : lk;
+        const double pr = tf.ph[0][i - li + 1] + tf.pf[1][j - lj] + tf.pf[2][kk - lk];
+        const double v = tf.cb[2] * tfsf_interp(einc + 0 * tf.L, pr);
+        add_corr(h, k == rk ? -v : v);
+      }
+      p.F[4][b] = h;
     }
-    if ((k == lk - 1 || k == rk) && i >= li && i < ri && j >= lj && j <= rj) {
-      const int kk = k == rk ? rk : lk;
-      const double pr = tf.ph[0][i - li + 1] + tf.pf[1][j - lj] + tf.pf[2][kk - lk];
-      const double v = tf.cb[2] * tfsf_interp(einc + 0 * tf.L, pr);
-      add_corr(h, k == rk ? -v : v);
-      w = true;
-    }
-    if (w) p.F[4][b] = h;
   }
   // Hz: x faces (i = li-1: += cbx Ey_inc(li, j, k); i = ri: -= cbx Ey_inc(ri, j, k)),
   //     y faces (j = lj-1: -= cby Ex_inc(i, lj, k); j = rj: += cby Ex_inc(i, rj, k))
   {
-    T h = p.F[5][b];
-    bool w = false;
-    if ((i == li - 1 || i == ri) && j >= lj && j < rj && k >= lk && k <= rk) {
-      const int ii = i == ri ? ri : li;
-      const double pr = tf.pf[0][ii - li] + tf.ph[1][j - lj + 1] + tf.pf[2][k - lk];
-      const double v = tf.cb[0] * tfsf_interp(einc + 1 * tf.L, pr);
-      add_corr(h, i == ri ? -v : v);
-      w = true;
+    const bool w1 = (i == li - 1 || i == ri) && j >= lj && j < rj && k >= lk && k <= rk;
+    const bool w2 = (j == lj - 1 || j == rj) && k >= lk && k <= rk && i >= li && i < ri;
+    if (w1 || w2) {
+      T h = p.F[5][b];
+      if (w1) {
+        const int ii = i == ri ? ri : li;
+        const double pr = tf.pf[0][ii - li] + tf.ph[1][j - lj + 1] + tf.pf[2][k - lk];
+        const double v = tf.cb[0] * tfsf_interp(einc + 1 * tf.L, pr);
+        add_corr(h, i == ri ? -v : v);
+      }
+      if (w2) {
+        const int jj = j == rj ? rj : lj;
+        const double pr = tf.ph[0][i - li + 1] + tf.pf[1][jj - lj] + tf.pf[2][k - lk];
+        const double v = tf.cb[1] * tfsf_interp(einc + 0 * tf.L, pr);
+        add_corr(h, j == rj ? v : -v);
+      }
+      p.F[5][b] = h;
     }
-    if ((j == lj - 1 || j == rj) && k >= lk && k <= rk && i >= li && i < ri) {
-      const int jj = j == rj ? rj : lj;
-      const double pr = tf.ph[0][i - li + 1] + tf.pf[1][jj - lj] + tf.pf[2][k - lk];
-      const double v = tf.cb[1] * tfsf_interp(einc + 0 * tf.L, pr);
-      add_corr(h, j == rj ? v : -v);
-      w = true;
-    }
-    if (w) p.F[5][b] = h;
   }
 }
 
