@@ -164,16 +164,19 @@ NCU_TRAFFIC = {("update_e", "fp32", (280, 280, 280)): 621.793024e6 + 318.648320e
 
 
 def algorithmic_bytes(n, slab_layers, precision: str, kernel: str) -> float:
-    """Bytes one launch of the E (or H) kernel must move at least: read the
-    3 own components and the 3 curl components, write the 3 own components,
-    read the 1-byte material index; inside CPML slabs read and write one psi
-    per (component, slab axis) pair (2 per slab axis)."""
+    """Bytes one launch of a volume kernel must move at least.  Split E (or
+    H) kernel: read the 3 own components and the 3 curl components, write
+    the 3 own components, read the 1-byte material index; inside CPML slabs
+    read and write one psi per (component, slab axis) pair (2 per slab
+    axis).  Fused sweep (E and H of one step): read and write all 6
+    components once and the index once; psi traffic of both halves."""
     nx, ny, nz = n
     cells = nx * ny * nz
     w = 8 if precision == "fp64" else 4
-    per_cell = 9 * w + 1
     slab_cells = (slab_layers[0] * ny * nz + slab_layers[1] * nx * nz + slab_layers[2] * nx * ny)
-    return cells * per_cell + slab_cells * 2 * 2 * w
+    if kernel == "sweep_eh":
+        return cells * (12 * w + 1) + slab_cells * 2 * 2 * w * 2
+    return cells * (9 * w + 1) + slab_cells * 2 * 2 * w
 
 
 def _slab_layers(sc):

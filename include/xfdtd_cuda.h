@@ -63,7 +63,12 @@ enum { XFDTD_FP64 = 0, XFDTD_FP32 = 1 };
 enum {
   XFDTD_FLAG_GRAPH = 1,      /* replay the step loop from a captured CUDA graph */
   XFDTD_FLAG_PROFILE = 2,    /* time every kernel launch with CUDA events        */
-  XFDTD_FLAG_AUTOTUNE = 4    /* pick the volume-kernel variants by timing at create */
+  XFDTD_FLAG_AUTOTUNE = 4,   /* pick the volume kernels and their variants by timing at create */
+  XFDTD_FLAG_SPLIT_EH = 8,   /* always the separate in-place E and H kernels            */
+  XFDTD_FLAG_FUSED_EH = 16   /* always the fused E/H sweep (unless the plan has lumped
+                                elements, which run the split kernels).  With neither
+                                flag the autotuner picks the faster of the two, and
+                                without autotuning the split kernels run. */
 };
 
 /* The 18 coefficients of one table entry, in this order (the reference's
@@ -196,13 +201,17 @@ int xfdtd_check_finite(xfdtd_handle *h);
  * names[i] (static strings), total milliseconds and launch counts. */
 int xfdtd_profile(xfdtd_handle *h, int max, const char **names, double *ms, int64_t *launches, int *count);
 int xfdtd_profile_reset(xfdtd_handle *h);
-/* Times every variant (register cap x block shape) of the E and H volume
- * kernels and keeps the fastest for each.  Only before the first step: the
- * trials run on the all-zero initial state and leave it unchanged.  All
- * variants compute bitwise-identical results. */
+/* Times every variant of the volume kernels and keeps the fastest: of the
+ * fused E/H sweep (register cap x planes per block), or with
+ * XFDTD_FLAG_SPLIT_EH of the E and H kernels separately (register cap x
+ * block shape x cells per thread x table placement).  Only before the first
+ * step: the trials run on the all-zero initial state and leave it unchanged.
+ * All variants compute bitwise-identical results. */
 int xfdtd_autotune(xfdtd_handle *h, int trials);
 /* Number of variants, the ones in use, and the last trial times
- * (trial_ms[2*v] for E, [2*v+1] for H; 0 where not tried). */
+ * (trial_ms[2*v] for E, [2*v+1] for H; 0 where not tried).  For the fused
+ * sweep both sides report the sweep's variant and time, and
+ * xfdtd_set_kernel_variant takes the same variant for both. */
 int xfdtd_kernel_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h, double *trial_ms);
 int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant);
 /* Per-step kernel launches enqueued so far (graph replays included). */

@@ -163,17 +163,19 @@ def test_invalid_plans_rejected():
 
 
 def test_every_kernel_variant_is_bitwise_identical():
-    """The autotuner's variants (register caps x block shapes) change only
-    scheduling: fields after the same steps are bitwise equal."""
-    for precision in ("fp64", "fp32"):
+    """The autotuner's variants (split kernels: register caps x block shapes
+    x cells per thread x table placement; fused sweep: register caps x
+    planes per block) change only scheduling: fields after the same steps
+    are bitwise equal."""
+    for precision, fused in (("fp64", False), ("fp32", False), ("fp64", True), ("fp32", True)):
         sc, st = scenes.oblique(steps=60)
-        ref = X.Simulation(sc, st, precision=precision, autotune=False)
+        ref = X.Simulation(sc, st, precision=precision, autotune=False, fused=fused)
         ref.step(st)
         want = [ref.read_field(c) for c in range(6)]
         info = ref.kernel_variants()
         tried = 0
         for v in range(info["n"]):
-            g = X.Simulation(sc, st, precision=precision, autotune=False)
+            g = X.Simulation(sc, st, precision=precision, autotune=False, fused=fused)
             try:
                 g.set_kernel_variant(v, v)
             except X.EngineError:
@@ -183,6 +185,46 @@ def test_every_kernel_variant_is_bitwise_identical():
             for c in range(6):
                 assert np.array_equal(g.read_field(c), want[c]), (precision, v, c)
         assert tried >= 4
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("name", ["pec_sphere", "oblique", "dielectric"])
+def test_fused_sweep_matches_split_kernels(name, precision):
+    """The fused E/H sweep (two buffer sets, recomputed halos, TFSF E
+    corrections inside the sweep) gives the split kernels' bits: fields and
+    NF-FF accumulators after the same steps, graph replay on both."""
+    sc, st = scenes.SCENES[name]()
+    st = min(st, 70)
+    a = X.Simulation(sc, st, precision=precision, fused=True)
+    b = X.Simulation(sc, st, precision=precision, fused=False)
+    assert a.launches_per_step() < b.launches_per_step()
+    a.step(st)
+    b.step(st)
+    for c in range(6):
+        assert np.array_equal(a.read_field(c), b.read_field(c)), (name, precision, c)
+    if sc.nffft is not None:
+        for w in (0, 7, 13, 22):
+            assert np.array_equal(a.read_nffft(w), b.read_nffft(w)), (name, precision, w)
+
+
+def test_fused_sweep_from_random_fields_all_cells():
+    """Random state everywhere (walls, CPML, TFSF faces): one and two sweeps
+    equal the split kernels, including cells no update touches (the sweep
+    copies them into the other buffer set)."""
+    sc, _ = scenes.oblique(steps=6)
+    rng = np.random.default_rng(3)
+    sims = [X.Simulation(sc, 6, precision=pr, fused=f, graph=False) for pr in ("fp64", "fp32") for f in (True, False)]
+    n = sims[0].n
+    vals = [rng.standard_normal(S.field_shape(c, n)) for c in range(6)]
+    for g in sims:
+        for c in range(6):
+            g.write_field(c, vals[c])
+    for steps in (1, 1, 3):
+        for g in sims:
+            g.step(steps)
+        for pair in ((sims[0], sims[1]), (sims[2], sims[3])):
+            for c in range(6):
+                assert np.array_equal(pair[0].read_field(c), pair[1].read_field(c)), (steps, c)
 
 
 def test_autotune_leaves_state_unchanged():

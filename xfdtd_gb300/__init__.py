@@ -25,7 +25,7 @@ from .scene import (  # noqa: F401  (re-exported: the reference's scene API)
 )
 
 FP64, FP32 = 0, 1
-FLAG_GRAPH, FLAG_PROFILE, FLAG_AUTOTUNE = 1, 2, 4
+FLAG_GRAPH, FLAG_PROFILE, FLAG_AUTOTUNE, FLAG_SPLIT_EH, FLAG_FUSED_EH = 1, 2, 4, 8, 16
 STATUS = {0: "ok", 1: "invalid plan", 2: "CUDA error", 3: "out of device memory", 4: "timeout",
           5: "non-finite value", 6: "device check", 7: "bad state"}
 
@@ -101,11 +101,13 @@ class Simulation:
 
     precision: "fp64" (the reference's arithmetic) or "fp32" (fields and CPML
     state in FP32; TFSF 1-D grid, NF-FF accumulation and far-field
-    integration stay FP64).
+    integration stay FP64).  fused: True = one E/H sweep kernel per step,
+    False = separate E and H kernels, None = the autotuner picks the faster;
+    all give identical bits.
     """
 
     def __init__(self, sc: "scene.Scene", total_steps: int, precision: str = "fp64", graph: bool = True,
-                 profile: bool = False, device: int = 0, autotune: bool = True):
+                 profile: bool = False, device: int = 0, autotune: bool = True, fused=None):
         self.scene = sc
         self.total_steps = int(total_steps)
         self.precision = precision
@@ -113,7 +115,7 @@ class Simulation:
         self._desc = sc.desc()
         prec = FP64 if precision == "fp64" else FP32
         flags = ((FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0)
-                 | (FLAG_AUTOTUNE if autotune else 0) | (int(device) << 8))
+                 | (FLAG_AUTOTUNE if autotune else 0) | ({True: FLAG_FUSED_EH, False: FLAG_SPLIT_EH, None: 0}[fused]) | (int(device) << 8))
         h = C.c_void_p()
         rc = ho.xfdtd_sim_create(C.byref(self._desc), self.total_steps, prec, flags, C.byref(h))
         self.h = h

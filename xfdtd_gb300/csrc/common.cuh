@@ -69,6 +69,9 @@ struct VolParams {
 // that side; a cell whose three indices carry no flag takes the fast path.
 constexpr uint8_t kSpecialE = 1;
 constexpr uint8_t kSpecialH = 2;
+// An index on a TFSF face plane (lo or hi of that axis): the fused sweep
+// applies the TFSF E corrections to cells with this flag on any axis.
+constexpr uint8_t kTfsfE = 4;
 
 __device__ __forceinline__ double tfsf_interp(const double *v, double projection) {
   // TFSF3D::getIncident*, src/tfsf/tfsf_3d.cpp:413-483

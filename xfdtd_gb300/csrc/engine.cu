@@ -33,6 +33,7 @@
 #include "../../include/xfdtd_cuda.h"
 #include "common.cuh"
 #include "surface.cuh"
+#include "sweep.cuh"
 #include "volume.cuh"
 
 namespace {
@@ -54,9 +55,9 @@ struct Err {
                 std::string(#call) + ": " + cudaGetErrorString(e_)};                    \
   } while (0)
 
-const char *kKernelNames[] = {"tfsf_aux", "update_e", "lumped_e", "update_h", "nffft",
-                              "probes",   "advance",  "tfsf_e",   "tfsf_h",   "nffft_acc"};
-constexpr int kNumKernels = 10;
+const char *kKernelNames[] = {"tfsf_aux", "update_e", "lumped_e", "update_h",  "nffft",   "probes",
+                              "advance",  "tfsf_e",   "tfsf_h",   "nffft_acc", "sweep_eh"};
+constexpr int kNumKernels = 11;
 
 }  // namespace
 
@@ -132,6 +133,15 @@ struct xfdtd_handle {
   // volume-kernel variants (autotuned)
   int var_e = 1, var_h = 1;   // L1-table variant: valid for every plan
   float tune_ms[2][16] = {};
+
+  // fused E/H sweep (sweep.cuh): the state of step t+1 goes to the second
+  // buffer set, swapped with the first after each step
+  bool sweep_ok = false;   // the plan allows the sweep (buffers allocated)
+  bool sweep = false;      // the sweep runs
+  void *F2[6] = {};
+  void *psi2[6] = {};         // E psi of the second set (order of psi[0..5])
+  int var_s = 1;
+  float sweep_ms[8] = {};
 
   // graph replay
   cudaGraphExec_t gexec = nullptr;
@@ -319,6 +329,47 @@ void launch_vol_v(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, co
   else xg::k_update_h<T, I, S, MB, NC><<<grid, block, smem, h->stream>>>(p);
 }
 
+// Fused-sweep variants: register cap (minimum resident 256-thread blocks
+// per SM) and planes per block along i.
+struct SweepVariant {
+  int minb;
+  int chunk;
+};
+constexpr SweepVariant kSweepVariants[] = {{1, 32}, {2, 32}, {3, 32}, {4, 32}, {5, 32}, {6, 32}, {4, 16}, {4, 64}};
+constexpr int kNumSweepVariants = sizeof(kSweepVariants) / sizeof(kSweepVariants[0]);
+
+template <typename T, typename I>
+void launch_sweep(xfdtd_handle *h, int var = -1) {
+  if (var < 0) var = h->var_s;
+  const SweepVariant &v = kSweepVariants[var];
+  xg::SweepParams<T, I> f{};
+  f.v = vol_params<T, I>(h);
+  for (int c = 0; c < 3; ++c) {
+    f.E2[c] = static_cast<T *>(h->F2[c]);
+    f.H2[c] = static_cast<T *>(h->F2[3 + c]);
+  }
+  T **ps = reinterpret_cast<T **>(&f.psi2);
+  for (int q = 0; q < 6; ++q) ps[q] = static_cast<T *>(h->psi2[q]);
+  f.chunk = v.chunk;
+  dim3 block(xg::kSwK, xg::kSwJ, 1);
+  dim3 grid((h->d.nz + xg::kSwK) / xg::kSwK, (h->d.ny + xg::kSwJ) / xg::kSwJ, (h->d.nx + v.chunk) / v.chunk);
+  switch (v.minb) {
+    case 1: xg::k_sweep<T, I, 1><<<grid, block, 0, h->stream>>>(f); break;
+    case 2: xg::k_sweep<T, I, 2><<<grid, block, 0, h->stream>>>(f); break;
+    case 3: xg::k_sweep<T, I, 3><<<grid, block, 0, h->stream>>>(f); break;
+    case 4: xg::k_sweep<T, I, 4><<<grid, block, 0, h->stream>>>(f); break;
+    case 5: xg::k_sweep<T, I, 5><<<grid, block, 0, h->stream>>>(f); break;
+    default: xg::k_sweep<T, I, 6><<<grid, block, 0, h->stream>>>(f); break;
+  }
+  XCHECK(cudaGetLastError());
+}
+
+// After a sweep the second buffer set holds step t+1: make it current.
+void swap_state(xfdtd_handle *h) {
+  for (int c = 0; c < 6; ++c) std::swap(h->F[c], h->F2[c]);
+  for (int q = 0; q < 6; ++q) std::swap(h->psi[q], h->psi2[q]);
+}
+
 template <typename T, typename I>
 void launch_volume(xfdtd_handle *h, bool e_side, int var = -1) {
   auto p = vol_params<T, I>(h);
@@ -357,7 +408,28 @@ void autotune_t(xfdtd_handle *h, int trials) {
   cudaEvent_t a, b;
   XCHECK(cudaEventCreate(&a));
   XCHECK(cudaEventCreate(&b));
-  for (int side = 0; side < 2; ++side) {
+  // an update of the all-zero state writes zeros: the trials change nothing
+  float best_sweep = 1e30f, best_split = 0.f;
+  if (h->sweep_ok) {
+    float best = 1e30f;
+    for (int v = 0; v < kNumSweepVariants; ++v) {
+      launch_sweep<T, I>(h, v);
+      XCHECK(cudaEventRecord(a, h->stream));
+      for (int r = 0; r < trials; ++r) launch_sweep<T, I>(h, v);
+      XCHECK(cudaEventRecord(b, h->stream));
+      XCHECK(cudaEventSynchronize(b));
+      float ms = 0;
+      XCHECK(cudaEventElapsedTime(&ms, a, b));
+      h->sweep_ms[v] = ms / trials;
+      if (ms < best) {
+        best = ms;
+        h->var_s = v;
+      }
+    }
+    best_sweep = best / trials;
+  }
+  const bool forced = h->sweep && (h->flags & XFDTD_FLAG_FUSED_EH);
+  for (int side = 0; side < 2 && !forced; ++side) {
     float best = 1e30f;
     int best_v = 0;
     for (int v = 0; v < kNumVariants; ++v) {
@@ -377,7 +449,10 @@ void autotune_t(xfdtd_handle *h, int trials) {
     }
     if (side == 0) h->var_e = best_v;
     else h->var_h = best_v;
+    best_split += best / trials;
   }
+  // without a forcing flag, the faster of the sweep and the split pair
+  if (h->sweep_ok && !forced) h->sweep = best_sweep < best_split;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
 }
@@ -528,28 +603,35 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     prof_end(h, h->side);
     XCHECK(cudaEventRecord(h->ev_join, h->side));
   }
-  prof_begin(h, 1);
-  launch_volume<T, I>(h, true);
-  prof_end(h);
-  if (h->n_inj || h->n_ind) {
-    auto sp = sparse_params<T>(h);
-    int n = std::max(h->n_inj, h->n_ind);
-    prof_begin(h, 2);
-    xg::k_lumped_e<T><<<(n + 127) / 128, 128, 0, h->stream>>>(sp);
-    XCHECK(cudaGetLastError());
+  if (h->sweep) {
+    prof_begin(h, 10);
+    launch_sweep<T, I>(h);
+    prof_end(h);
+    swap_state(h);
+  } else {
+    prof_begin(h, 1);
+    launch_volume<T, I>(h, true);
+    prof_end(h);
+    if (h->n_inj || h->n_ind) {
+      auto sp = sparse_params<T>(h);
+      int n = std::max(h->n_inj, h->n_ind);
+      prof_begin(h, 2);
+      xg::k_lumped_e<T><<<(n + 127) / 128, 128, 0, h->stream>>>(sp);
+      XCHECK(cudaGetLastError());
+      prof_end(h);
+    }
+    if (h->tfsf) {
+      const auto sp = tfsf_surf_params<T>(h);
+      const long long n = xg::surface_count(h->tf_lo[0], h->tf_hi[0], h->tf_lo[1], h->tf_hi[1], h->tf_lo[2], h->tf_hi[2]);
+      prof_begin(h, 7);
+      xg::k_tfsf_e<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, h->stream>>>(sp);
+      XCHECK(cudaGetLastError());
+      prof_end(h);
+    }
+    prof_begin(h, 3);
+    launch_volume<T, I>(h, false);
     prof_end(h);
   }
-  if (h->tfsf) {
-    const auto sp = tfsf_surf_params<T>(h);
-    const long long n = xg::surface_count(h->tf_lo[0], h->tf_hi[0], h->tf_lo[1], h->tf_hi[1], h->tf_lo[2], h->tf_hi[2]);
-    prof_begin(h, 7);
-    xg::k_tfsf_e<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, h->stream>>>(sp);
-    XCHECK(cudaGetLastError());
-    prof_end(h);
-  }
-  prof_begin(h, 3);
-  launch_volume<T, I>(h, false);
-  prof_end(h);
   if (h->tfsf) {
     XCHECK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
     const auto sp = tfsf_surf_params<T>(h);
@@ -596,6 +678,7 @@ void enqueue_step(xfdtd_handle *h, long long s) {
 }
 
 int launches_per_step(const xfdtd_handle *h) {
+  if (h->sweep) return (h->tfsf ? 2 : 0) + 1 + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
   return (h->tfsf ? 3 : 0) + 2 + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
 }
 
@@ -731,6 +814,14 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     // order: ex_y ex_z ey_x ey_z ez_x ez_y hx_y hx_z hy_x hy_z hz_x hz_y
     const size_t sizes[12] = {sy, sz, sx, sz, sx, sy, sy, sz, sx, sz, sx, sy};
     for (int q = 0; q < 12; ++q) h->psi[q] = sizes[q] ? h->alloc_bytes(sizes[q] * h->esize) : nullptr;
+    // the fused sweep, unless the plan asks for the split kernels or has
+    // lumped elements (whose E corrections run between the E and H updates)
+    h->sweep_ok = !(pl->flags & XFDTD_FLAG_SPLIT_EH) && pl->n_injections == 0 && pl->n_inductor_cells == 0;
+    h->sweep = h->sweep_ok && (pl->flags & XFDTD_FLAG_FUSED_EH);
+    if (h->sweep_ok) {
+      for (int c = 0; c < 6; ++c) h->F2[c] = h->alloc_bytes(d.cells * h->esize);
+      for (int q = 0; q < 6; ++q) h->psi2[q] = sizes[q] ? h->alloc_bytes(sizes[q] * h->esize) : nullptr;
+    }
   }
 
   // TFSF
@@ -873,6 +964,7 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
       const bool slab_h = pl->cpml[a].n_layers && pl->cpml[a].slot_h[q] >= 0;
       if (q == 0 || q == n || slab_e) fl[q] |= xg::kSpecialE;
       if (q == n || slab_h) fl[q] |= xg::kSpecialH;
+      if (h->tfsf && (q == h->tf_lo[a] || q == h->tf_hi[a])) fl[q] |= xg::kTfsfE;
     }
     h->axis_flags[a] = h->upload<uint8_t>(fl.data(), fl.size());
   }
@@ -1157,6 +1249,14 @@ int xfdtd_autotune(xfdtd_handle *h, int trials) {
 
 int xfdtd_kernel_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h, double *trial_ms) {
   if (!h) return XFDTD_ERR_STATE;
+  if (h->sweep) {   // one fused kernel: its variants stand for both sides
+    if (n) *n = kNumSweepVariants;
+    if (current_e) *current_e = h->var_s;
+    if (current_h) *current_h = h->var_s;
+    if (trial_ms)
+      for (int v = 0; v < kNumSweepVariants; ++v) trial_ms[2 * v] = trial_ms[2 * v + 1] = h->sweep_ms[v];
+    return XFDTD_OK;
+  }
   if (n) *n = kNumVariants;
   if (current_e) *current_e = h->var_e;
   if (current_h) *current_h = h->var_h;
@@ -1171,6 +1271,16 @@ int xfdtd_kernel_variants(xfdtd_handle *h, int *n, int *current_e, int *current_
 int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant) {
   if (!h) return XFDTD_ERR_STATE;
   return guarded(h, [&] {
+    if (h->sweep) {
+      if (e_variant < 0 || e_variant >= kNumSweepVariants || h_variant != e_variant)
+        invalid("fused-sweep variant out of range (E and H variants must be equal)");
+      h->var_s = e_variant;
+      if (h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+      }
+      return;
+    }
     if (e_variant < 0 || e_variant >= kNumVariants || h_variant < 0 || h_variant >= kNumVariants ||
         !variant_allowed(h, kVariants[e_variant]) || !variant_allowed(h, kVariants[h_variant]))
       invalid("kernel variant not available for this precision");

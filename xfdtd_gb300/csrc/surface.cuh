@@ -405,81 +405,98 @@ __device__ __forceinline__ bool surface_cell(int q, int a0, int a1, int b0, int 
   return false;
 }
 
+// TFSF3D::updateE (src/tfsf/tfsf_3d.cpp:299-411) for one cell and one E
+// component C: which of the component's two face corrections apply at
+// (i, j, k) (bit 0: the first face pair, bit 1: the second) ...
+template <int C>
+__device__ __forceinline__ int tfsf_e_terms(const TfsfDev &tf, int i, int j, int k) {
+  const int li = tf.lo[0], ri = tf.hi[0], lj = tf.lo[1], rj = tf.hi[1], lk = tf.lo[2], rk = tf.hi[2];
+  if (C == 0)   // Ex: y faces, z faces
+    return (((j == lj || j == rj) && k >= lk && k <= rk && i >= li && i < ri) ? 1 : 0) |
+           (((k == lk || k == rk) && i >= li && i < ri && j >= lj && j <= rj) ? 2 : 0);
+  if (C == 1)   // Ey: x faces, z faces
+    return (((i == li || i == ri) && j >= lj && j < rj && k >= lk && k <= rk) ? 1 : 0) |
+           (((k == lk || k == rk) && i >= li && i <= ri && j >= lj && j < rj) ? 2 : 0);
+  // Ez: x faces, y faces
+  return (((i == li || i == ri) && j >= lj && j <= rj && k >= lk && k < rk) ? 1 : 0) |
+         (((j == lj || j == rj) && k >= lk && k < rk && i >= li && i <= ri) ? 2 : 0);
+}
+
+// ... and adds them to e, first face pair first.  hinc: the incident H
+// arrays of the previous step.
+template <int C, typename T>
+__device__ __forceinline__ void tfsf_e_add(const TfsfDev &tf, const double *hinc, int i, int j, int k, int terms,
+                                           T &e) {
+  const int li = tf.lo[0], ri = tf.hi[0], lj = tf.lo[1], rj = tf.hi[1], lk = tf.lo[2], rk = tf.hi[2];
+  if (C == 0) {
+    // Ex: y faces (j = lj: -= cay Hz_inc(i, lj-1, k); j = rj: += cay Hz_inc(i, rj, k)),
+    //     z faces (k = lk: += caz Hy_inc(i, j, lk-1); k = rk: -= caz Hy_inc(i, j, rk))
+    if (terms & 1) {
+      const int jj = j == lj ? lj - 1 : rj;
+      const double pr = tf.ph[0][i - li + 1] + tf.ph[1][jj - lj + 1] + tf.pf[2][k - lk] - 0.5;
+      const double v = tf.ca[1] * tfsf_interp(hinc + 5 * tf.L, pr);
+      add_corr(e, j == lj ? -v : v);
+    }
+    if (terms & 2) {
+      const int kk = k == lk ? lk - 1 : rk;
+      const double pr = tf.ph[0][i - li + 1] + tf.pf[1][j - lj] + tf.ph[2][kk - lk + 1] - 0.5;
+      const double v = tf.ca[2] * tfsf_interp(hinc + 4 * tf.L, pr);
+      add_corr(e, k == lk ? v : -v);
+    }
+  } else if (C == 1) {
+    // Ey: x faces (i = li: += cax Hz_inc(li-1, j, k); i = ri: -= cax Hz_inc(ri, j, k)),
+    //     z faces (k = lk: -= caz Hx_inc(i, j, lk-1); k = rk: += caz Hx_inc(i, j, rk))
+    if (terms & 1) {
+      const int ii = i == li ? li - 1 : ri;
+      const double pr = tf.ph[0][ii - li + 1] + tf.ph[1][j - lj + 1] + tf.pf[2][k - lk] - 0.5;
+      const double v = tf.ca[0] * tfsf_interp(hinc + 5 * tf.L, pr);
+      add_corr(e, i == li ? v : -v);
+    }
+    if (terms & 2) {
+      const int kk = k == lk ? lk - 1 : rk;
+      const double pr = tf.pf[0][i - li] + tf.ph[1][j - lj + 1] + tf.ph[2][kk - lk + 1] - 0.5;
+      const double v = tf.ca[2] * tfsf_interp(hinc + 3 * tf.L, pr);
+      add_corr(e, k == lk ? -v : v);
+    }
+  } else {
+    // Ez: x faces (i = li: -= cax Hy_inc(li-1, j, k); i = ri: += cax Hy_inc(ri, j, k)),
+    //     y faces (j = lj: += cay Hx_inc(i, lj-1, k); j = rj: -= cay Hx_inc(i, rj, k))
+    if (terms & 1) {
+      const int ii = i == li ? li - 1 : ri;
+      const double pr = tf.ph[0][ii - li + 1] + tf.pf[1][j - lj] + tf.ph[2][k - lk + 1] - 0.5;
+      const double v = tf.ca[0] * tfsf_interp(hinc + 4 * tf.L, pr);
+      add_corr(e, i == li ? -v : v);
+    }
+    if (terms & 2) {
+      const int jj = j == lj ? lj - 1 : rj;
+      const double pr = tf.pf[0][i - li] + tf.ph[1][jj - lj + 1] + tf.ph[2][k - lk + 1] - 0.5;
+      const double v = tf.ca[1] * tfsf_interp(hinc + 3 * tf.L, pr);
+      add_corr(e, j == lj ? v : -v);
+    }
+  }
+}
+
+template <int C, typename T>
+__device__ __forceinline__ void tfsf_e_component(const TfsfSurfParams<T> &p, const double *hinc, int i, int j, int k,
+                                                 long long b) {
+  const int terms = tfsf_e_terms<C>(p.tf, i, j, k);
+  if (!terms) return;
+  T e = p.F[C][b];
+  tfsf_e_add<C>(p.tf, hinc, i, j, k, terms, e);
+  p.F[C][b] = e;
+}
+
 template <typename T>
 __global__ void k_tfsf_e(TfsfSurfParams<T> p) {
   const TfsfDev &tf = p.tf;
-  const int li = tf.lo[0], ri = tf.hi[0], lj = tf.lo[1], rj = tf.hi[1], lk = tf.lo[2], rk = tf.hi[2];
   int i, j, k;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!surface_cell(q, li, ri, lj, rj, lk, rk, i, j, k)) return;
+  if (!surface_cell(q, tf.lo[0], tf.hi[0], tf.lo[1], tf.hi[1], tf.lo[2], tf.hi[2], i, j, k)) return;
   const double *hinc = tf.inc + (((*p.step) + 1) & 1) * 6 * tf.L;   // incident H of the previous step
   const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
-  // Ex: y faces (j = lj: -= cay Hz_inc(i, lj-1, k); j = rj: += cay Hz_inc(i, rj, k)),
-  //     z faces (k = lk: += caz Hy_inc(i, j, lk-1); k = rk: -= caz Hy_inc(i, j, rk))
-  {
-    const bool w1 = (j == lj || j == rj) && k >= lk && k <= rk && i >= li && i < ri;
-    const bool w2 = (k == lk || k == rk) && i >= li && i < ri && j >= lj && j <= rj;
-    if (w1 || w2) {
-      T e = p.F[0][b];
-      if (w1) {
-        const int jj = j == lj ? lj - 1 : rj;
-        const double pr = tf.ph[0][i - li + 1] + tf.ph[1][jj - lj + 1] + tf.pf[2][k - lk] - 0.5;
-        const double v = tf.ca[1] * tfsf_interp(hinc + 5 * tf.L, pr);
-        add_corr(e, j == lj ? -v : v);
-      }
-      if (w2) {
-        const int kk = k == lk ? lk - 1 : rk;
-        const double pr = tf.ph[0][i - li + 1] + tf.pf[1][j - lj] + tf.ph[2][kk - lk + 1] - 0.5;
-        const double v = tf.ca[2] * tfsf_interp(hinc + 4 * tf.L, pr);
-        add_corr(e, k == lk ? v : -v);
-      }
-      p.F[0][b] = e;
-    }
-  }
-  // Ey: x faces (i = li: += cax Hz_inc(li-1, j, k); i = ri: -= cax Hz_inc(ri, j, k)),
-  //     z faces (k = lk: -= caz Hx_inc(i, j, lk-1); k = rk: += caz Hx_inc(i, j, rk))
-  {
-    const bool w1 = (i == li || i == ri) && j >= lj && j < rj && k >= lk && k <= rk;
-    const bool w2 = (k == lk || k == rk) && i >= li && i <= ri && j >= lj && j < rj;
-    if (w1 || w2) {
-      T e = p.F[1][b];
-      if (w1) {
-        const int ii = i == li ? li - 1 : ri;
-        const double pr = tf.ph[0][ii - li + 1] + tf.ph[1][j - lj + 1] + tf.pf[2][k - lk] - 0.5;
-        const double v = tf.ca[0] * tfsf_interp(hinc + 5 * tf.L, pr);
-        add_corr(e, i == li ? v : -v);
-      }
-      if (w2) {
-        const int kk = k == lk ? lk - 1 : rk;
-        const double pr = tf.pf[0][i - li] + tf.ph[1][j - lj + 1] + tf.ph[2][kk - lk + 1] - 0.5;
-        const double v = tf.ca[2] * tfsf_interp(hinc + 3 * tf.L, pr);
-        add_corr(e, k == lk ? -v : v);
-      }
-      p.F[1][b] = e;
-    }
-  }
-  // Ez: x faces (i = li: -= cax Hy_inc(li-1, j, k); i = ri: += cax Hy_inc(ri, j, k)),
-  //     y faces (j = lj: += cay Hx_inc(i, lj-1, k); j = rj: -= cay Hx_inc(i, rj, k))
-  {
-    const bool w1 = (i == li || i == ri) && j >= lj && j <= rj && k >= lk && k < rk;
-    const bool w2 = (j == lj || j == rj) && k >= lk && k < rk && i >= li && i <= ri;
-    if (w1 || w2) {
-      T e = p.F[2][b];
-      if (w1) {
-        const int ii = i == li ? li - 1 : ri;
-        const double pr = tf.ph[0][ii - li + 1] + tf.pf[1][j - lj] + tf.ph[2][k - lk + 1] - 0.5;
-        const double v = tf.ca[0] * tfsf_interp(hinc + 4 * tf.L, pr);
-        add_corr(e, i == li ? -v : v);
-      }
-      if (w2) {
-        const int jj = j == lj ? lj - 1 : rj;
-        const double pr = tf.pf[0][i - li] + tf.ph[1][jj - lj + 1] + tf.ph[2][k - lk + 1] - 0.5;
-        const double v = tf.ca[1] * tfsf_interp(hinc + 3 * tf.L, pr);
-        add_corr(e, j == lj ? v : -v);
-      }
-      p.F[2][b] = e;
-    }
-  }
+  tfsf_e_component<0>(p, hinc, i, j, k, b);
+  tfsf_e_component<1>(p, hinc, i, j, k, b);
+  tfsf_e_component<2>(p, hinc, i, j, k, b);
 }
 
 template <typename T>

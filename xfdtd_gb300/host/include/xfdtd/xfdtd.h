@@ -547,6 +547,10 @@ class Simulation {
   void setDevice(int d) { _device = d; }
   // Time the volume-kernel variants at init and keep the fastest (default on).
   void setAutotune(bool a) { _autotune = a; }
+  // Volume kernels: 1 = always the fused E/H sweep, 0 = always separate
+  // in-place E and H kernels, -1 (default) = the autotuner picks the faster.
+  // Plans with lumped elements always run the split kernels.
+  void setFusedSweep(int mode) { _fused = mode; }
   // One material per cell, applied after all objects (see xfdtd_scene.h).
   void setVoxelMaterials(std::vector<Material> materials, std::vector<uint16_t> index, std::array<size_t, 3> shape);
   // Split run(): init once, step in pieces, read state, output at the end.
@@ -589,6 +593,7 @@ class Simulation {
   bool _use_graph{true};
   bool _profile{false};
   int _device{0};
+  int _fused{-1};
   bool _autotune{true};
   size_t _total{0};
   size_t _nx{0}, _ny{0}, _nz{0};

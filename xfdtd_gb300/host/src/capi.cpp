@@ -162,6 +162,7 @@ int xfdtd_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, int precis
     sim->setUseGraph((flags & XFDTD_FLAG_GRAPH) != 0);
     sim->setProfile((flags & XFDTD_FLAG_PROFILE) != 0);
     sim->setAutotune((flags & XFDTD_FLAG_AUTOTUNE) != 0);
+    sim->setFusedSweep((flags & XFDTD_FLAG_FUSED_EH) ? 1 : (flags & XFDTD_FLAG_SPLIT_EH) ? 0 : -1);
     sim->setDevice((flags >> XFDTD_SIM_DEVICE_SHIFT) & 0xff);
     if (total_steps <= 0) throw std::invalid_argument("total_steps must be positive");
     sim->init(static_cast<size_t>(total_steps));

@@ -450,7 +450,8 @@ void Simulation::init(size_t total_time_steps) {
   for (int a = 0; a < 3; ++a) plan.dl[a] = d[a];
   plan.total_steps = static_cast<int64_t>(_total);
   plan.flags = (_use_graph ? XFDTD_FLAG_GRAPH : 0) | (_profile ? XFDTD_FLAG_PROFILE : 0) |
-               (_autotune ? XFDTD_FLAG_AUTOTUNE : 0);
+               (_autotune ? XFDTD_FLAG_AUTOTUNE : 0) | (_fused == 0 ? XFDTD_FLAG_SPLIT_EH : 0) |
+               (_fused == 1 ? XFDTD_FLAG_FUSED_EH : 0);
   plan.index_bytes = index_bytes;
   plan.device = _device;
   plan.n_materials = static_cast<int32_t>(table.size());
