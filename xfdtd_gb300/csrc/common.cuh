@@ -39,7 +39,31 @@ struct TfsfDev {
   const double *pf[3], *ph[3];
   double ca[3], cb[3];
   const double *inc;   // [2][6][L]
+  // the same tables in FP32 (FP32 form): projections, coefficients and the
+  // incident arrays (written by the 1-D line beside the FP64 ones)
+  const float *pff[3], *phf[3];
+  float caf[3], cbf[3];
+  const float *incf;   // [2][6][L]
 };
+
+// The TFSF tables in the arithmetic of the field precision T: FP64 (the
+// reference's) for FP64 fields, FP32 for the FP32 form.
+template <typename R>
+struct TfsfView {
+  const R *pf[3], *ph[3];
+  R ca[3], cb[3];
+  const R *inc;
+};
+template <typename T>
+__device__ __forceinline__ auto tfsf_view(const TfsfDev &tf) {
+  if constexpr (sizeof(T) == 8) {
+    return TfsfView<double>{{tf.pf[0], tf.pf[1], tf.pf[2]}, {tf.ph[0], tf.ph[1], tf.ph[2]},
+                            {tf.ca[0], tf.ca[1], tf.ca[2]}, {tf.cb[0], tf.cb[1], tf.cb[2]}, tf.inc};
+  } else {
+    return TfsfView<float>{{tf.pff[0], tf.pff[1], tf.pff[2]}, {tf.phf[0], tf.phf[1], tf.phf[2]},
+                           {tf.caf[0], tf.caf[1], tf.caf[2]}, {tf.cbf[0], tf.cbf[1], tf.cbf[2]}, tf.incf};
+  }
+}
 
 // psi storage: axis X (L, ny+1, nzp), axis Y (nx+1, L, nzp), axis Z (nx+1, ny+1, L).
 template <typename T>
@@ -77,6 +101,11 @@ __device__ __forceinline__ double tfsf_interp(const double *v, double projection
   // TFSF3D::getIncident*, src/tfsf/tfsf_3d.cpp:413-483
   const unsigned long long index = static_cast<unsigned long long>(projection);
   const double weight = projection - static_cast<double>(index);
+  return (1 - weight) * v[index] + weight * v[index + 1];
+}
+__device__ __forceinline__ float tfsf_interp(const float *v, float projection) {
+  const int index = static_cast<int>(projection);
+  const float weight = projection - static_cast<float>(index);
   return (1 - weight) * v[index] + weight * v[index + 1];
 }
 

@@ -20,6 +20,8 @@
 // terms are added in another order.  The step index lives on the device
 // (k_advance bumps it), so a captured CUDA graph of G steps (G a multiple of
 // the NF-FF batch) replays for any starting step on a batch boundary.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -100,6 +102,7 @@ struct xfdtd_handle {
   int tf_lo[3] = {}, tf_hi[3] = {};
   double *tf_pf[3] = {}, *tf_ph[3] = {};
   double *tf_state = nullptr, *tf_inc = nullptr, *tf_src = nullptr;
+  float *tf_pff[3] = {}, *tf_phf[3] = {}, *tf_incf = nullptr;   // FP32 copies (FP32 form)
   double tf_ca[3] = {}, tf_cb[3] = {}, tf_te[3] = {}, tf_th[3] = {};
   double tf_ceihi = 0, tf_chiei = 0, tf_c1 = 0, tf_c2 = 0;
 
@@ -138,6 +141,8 @@ struct xfdtd_handle {
   // buffer set, swapped with the first after each step
   bool sweep_ok = false;   // the plan allows the sweep (buffers allocated)
   bool sweep = false;      // the sweep runs
+  int cur_set = 0;         // which buffer set (0: allocated as F, 1: as F2) is current
+  CUtensorMap tm_h[2][3], tm_e[2][3], tm_idx;   // TMA maps of both sets and the index
   void *F2[6] = {};
   void *psi2[6] = {};         // E psi of the second set (order of psi[0..5])
   int var_s = 1;
@@ -289,8 +294,13 @@ xg::VolParams<T, I> vol_params(xfdtd_handle *h) {
     p.tf.ph[a] = h->tf_ph[a];
     p.tf.ca[a] = h->tf_ca[a];
     p.tf.cb[a] = h->tf_cb[a];
+    p.tf.pff[a] = h->tf_pff[a];
+    p.tf.phf[a] = h->tf_phf[a];
+    p.tf.caf[a] = static_cast<float>(h->tf_ca[a]);
+    p.tf.cbf[a] = static_cast<float>(h->tf_cb[a]);
   }
   p.tf.inc = h->tf_inc;
+  p.tf.incf = h->tf_incf;
   p.step = h->d_step;
   for (int a = 0; a < 3; ++a) p.flags[a] = h->axis_flags[a];
   return p;
@@ -335,11 +345,12 @@ struct SweepVariant {
   int minb;
   int chunk;
 };
-constexpr SweepVariant kSweepVariants[] = {{1, 32}, {2, 32}, {3, 32}, {4, 32}, {5, 32}, {6, 32}, {4, 16}, {4, 64}};
+constexpr SweepVariant kSweepVariants[] = {{1, 32}, {2, 32}, {3, 32}, {4, 32}, {2, 16}, {4, 16}, {2, 64}, {4, 64}};
 constexpr int kNumSweepVariants = sizeof(kSweepVariants) / sizeof(kSweepVariants[0]);
 
 template <typename T, typename I>
 void launch_sweep(xfdtd_handle *h, int var = -1) {
+  using G = xg::SweepTiles<T, I>;
   if (var < 0) var = h->var_s;
   const SweepVariant &v = kSweepVariants[var];
   xg::SweepParams<T, I> f{};
@@ -351,23 +362,82 @@ void launch_sweep(xfdtd_handle *h, int var = -1) {
   T **ps = reinterpret_cast<T **>(&f.psi2);
   for (int q = 0; q < 6; ++q) ps[q] = static_cast<T *>(h->psi2[q]);
   f.chunk = v.chunk;
+  f.status = h->d_status;
+  xg::SweepMaps m;
+  for (int c = 0; c < 3; ++c) {
+    m.h[c] = h->tm_h[h->cur_set][c];
+    m.e[c] = h->tm_e[h->cur_set][c];
+  }
+  m.idx = h->tm_idx;
   dim3 block(xg::kSwK, xg::kSwJ, 1);
   dim3 grid((h->d.nz + xg::kSwK) / xg::kSwK, (h->d.ny + xg::kSwJ) / xg::kSwJ, (h->d.nx + v.chunk) / v.chunk);
   switch (v.minb) {
-    case 1: xg::k_sweep<T, I, 1><<<grid, block, 0, h->stream>>>(f); break;
-    case 2: xg::k_sweep<T, I, 2><<<grid, block, 0, h->stream>>>(f); break;
-    case 3: xg::k_sweep<T, I, 3><<<grid, block, 0, h->stream>>>(f); break;
-    case 4: xg::k_sweep<T, I, 4><<<grid, block, 0, h->stream>>>(f); break;
-    case 5: xg::k_sweep<T, I, 5><<<grid, block, 0, h->stream>>>(f); break;
-    default: xg::k_sweep<T, I, 6><<<grid, block, 0, h->stream>>>(f); break;
+    case 1: xg::k_sweep<T, I, 1><<<grid, block, G::SMEM, h->stream>>>(m, f); break;
+    case 2: xg::k_sweep<T, I, 2><<<grid, block, G::SMEM, h->stream>>>(m, f); break;
+    case 3: xg::k_sweep<T, I, 3><<<grid, block, G::SMEM, h->stream>>>(m, f); break;
+    default: xg::k_sweep<T, I, 4><<<grid, block, G::SMEM, h->stream>>>(m, f); break;
   }
   XCHECK(cudaGetLastError());
+}
+
+template <typename T, typename I>
+void sweep_smem_attr() {
+  const int bytes = xg::SweepTiles<T, I>::SMEM;
+  XCHECK(cudaFuncSetAttribute(xg::k_sweep<T, I, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_sweep<T, I, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_sweep<T, I, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_sweep<T, I, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+}
+
+// cuTensorMapEncodeTiled, from the driver through the runtime (no link to libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    XCHECK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !ptr) throw Err{XFDTD_ERR_CUDA, "cuTensorMapEncodeTiled is not available"};
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+  }
+  return fn;
+}
+
+// A 3-D tiled map over one padded field (or index) array: dims (nzp, ny+1,
+// nx+1), box (box_x, box_y, 1); out-of-range box parts read as zero.
+void encode_map(xfdtd_handle *h, CUtensorMap *m, void *base, CUtensorMapDataType dt, size_t esize, unsigned box_x,
+                unsigned box_y) {
+  const cuuint64_t dims[3] = {static_cast<cuuint64_t>(h->d.nzp), static_cast<cuuint64_t>(h->d.ny + 1),
+                              static_cast<cuuint64_t>(h->d.nx + 1)};
+  const cuuint64_t strides[2] = {static_cast<cuuint64_t>(h->d.nzp) * esize,
+                                 static_cast<cuuint64_t>(h->d.nzp) * (h->d.ny + 1) * esize};
+  const cuuint32_t box[3] = {box_x, box_y, 1};
+  const cuuint32_t elem[3] = {1, 1, 1};
+  const CUresult r = tensor_map_encoder()(m, dt, 3, base, dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Err{XFDTD_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(static_cast<int>(r))};
+}
+
+template <typename T, typename I>
+void sweep_setup(xfdtd_handle *h) {
+  using G = xg::SweepTiles<T, I>;
+  const CUtensorMapDataType dt = sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  for (int c = 0; c < 3; ++c) {
+    encode_map(h, &h->tm_h[0][c], h->F[3 + c], dt, sizeof(T), G::HW, xg::kHJ);
+    encode_map(h, &h->tm_h[1][c], h->F2[3 + c], dt, sizeof(T), G::HW, xg::kHJ);
+    encode_map(h, &h->tm_e[0][c], h->F[c], dt, sizeof(T), G::EW, xg::kEJ);
+    encode_map(h, &h->tm_e[1][c], h->F2[c], dt, sizeof(T), G::EW, xg::kEJ);
+  }
+  encode_map(h, &h->tm_idx, h->idx, sizeof(I) == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16,
+             sizeof(I), G::IW, xg::kEJ);
+  sweep_smem_attr<T, I>();
 }
 
 // After a sweep the second buffer set holds step t+1: make it current.
 void swap_state(xfdtd_handle *h) {
   for (int c = 0; c < 6; ++c) std::swap(h->F[c], h->F2[c]);
   for (int q = 0; q < 6; ++q) std::swap(h->psi[q], h->psi2[q]);
+  h->cur_set ^= 1;
 }
 
 template <typename T, typename I>
@@ -570,8 +640,13 @@ xg::TfsfSurfParams<T> tfsf_surf_params(xfdtd_handle *h) {
     p.tf.ph[a] = h->tf_ph[a];
     p.tf.ca[a] = h->tf_ca[a];
     p.tf.cb[a] = h->tf_cb[a];
+    p.tf.pff[a] = h->tf_pff[a];
+    p.tf.phf[a] = h->tf_phf[a];
+    p.tf.caf[a] = static_cast<float>(h->tf_ca[a]);
+    p.tf.cbf[a] = static_cast<float>(h->tf_cb[a]);
   }
   p.tf.inc = h->tf_inc;
+  p.tf.incf = h->tf_incf;
   p.step = h->d_step;
   return p;
 }
@@ -583,6 +658,7 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     a.L = h->aux_len;
     a.state = h->tf_state;
     a.inc = h->tf_inc;
+    a.incf = h->tf_incf;
     a.source = h->tf_src;
     a.ceihi = h->tf_ceihi;
     a.chiei = h->tf_chiei;
@@ -704,6 +780,7 @@ void check_status(xfdtd_handle *h) {
   int st = 0;
   XCHECK(cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   XCHECK(cudaStreamSynchronize(h->stream));
+  if (st == XFDTD_ERR_TIMEOUT) throw Err{XFDTD_ERR_TIMEOUT, "a bounded wait of the fused sweep gave up"};
   if (st != 0) throw Err{XFDTD_ERR_DEVICE_CHECK, "device status " + std::to_string(st) + " (step index past the plan)"};
 }
 
@@ -838,6 +915,10 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
       if (!tp.proj_full[a] || !tp.proj_half[a]) invalid("TFSF projection tables are required");
       h->tf_pf[a] = h->upload<double>(tp.proj_full[a], bn + 1);
       h->tf_ph[a] = h->upload<double>(tp.proj_half[a], bn + 2);
+      if (pl->precision == XFDTD_FP32) {
+        h->tf_pff[a] = static_cast<float *>(h->upload_real(tp.proj_full[a], bn + 1));
+        h->tf_phf[a] = static_cast<float *>(h->upload_real(tp.proj_half[a], bn + 2));
+      }
       h->tf_ca[a] = tp.ca[a];
       h->tf_cb[a] = tp.cb[a];
       h->tf_te[a] = tp.transform_e[a];
@@ -864,6 +945,7 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     h->tf_src = h->upload<double>(tp.source, pl->total_steps);
     h->tf_state = h->alloc<double>(2 * static_cast<size_t>(tp.aux_len) + 1);
     h->tf_inc = h->alloc<double>(2 * 6 * static_cast<size_t>(tp.aux_len));
+    if (pl->precision == XFDTD_FP32) h->tf_incf = h->alloc<float>(2 * 6 * static_cast<size_t>(tp.aux_len));
   }
 
   // NF-FF
@@ -972,6 +1054,15 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   h->d_step = h->alloc<long long>(1);
   h->d_status = h->alloc<int>(1);
   h->d_flag = h->alloc<int>(1);
+  if (h->sweep_ok) {
+    if (h->precision == XFDTD_FP64) {
+      if (h->idx_bytes == 1) sweep_setup<double, uint8_t>(h);
+      else sweep_setup<double, uint16_t>(h);
+    } else {
+      if (h->idx_bytes == 1) sweep_setup<float, uint8_t>(h);
+      else sweep_setup<float, uint16_t>(h);
+    }
+  }
   XCHECK(cudaStreamSynchronize(h->stream));
   if (pl->flags & XFDTD_FLAG_AUTOTUNE) autotune(h, 3);
 }

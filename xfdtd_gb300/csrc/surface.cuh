@@ -2,6 +2,8 @@
 // integration, sparse lumped-element and probe kernels, step counter.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace xg {
@@ -14,6 +16,7 @@ struct AuxParams {
   int L;
   double *state;
   double *inc;
+  float *incf;             // FP32 copy of inc (FP32 form), or null
   const double *source;    // e0 * w(t dt)
   double ceihi, chiei, c1, c2;
   double te[3], th[3];
@@ -51,16 +54,20 @@ __global__ void k_tfsf_aux(AuxParams p) {
   for (int i = threadIdx.x; i < L - 1; i += blockDim.x) h[i] = 1.0 * h[i] + p.chiei * (e[i + 1] - e[i]);
   __syncthreads();
   double *out = p.inc + (t & 1) * 6 * L;
+  float *outf = p.incf ? p.incf + (t & 1) * 6 * L : nullptr;
   for (int i = threadIdx.x; i < L; i += blockDim.x) {
     const double ev = e[i];
-    out[0 * L + i] = p.te[0] * ev;
-    out[1 * L + i] = p.te[1] * ev;
-    out[2 * L + i] = p.te[2] * ev;
+    double o[6] = {p.te[0] * ev, p.te[1] * ev, p.te[2] * ev, 0, 0, 0};
     if (i < L - 1) {
       const double hv = h[i];
-      out[3 * L + i] = p.th[0] * hv;
-      out[4 * L + i] = p.th[1] * hv;
-      out[5 * L + i] = p.th[2] * hv;
+      o[3] = p.th[0] * hv;
+      o[4] = p.th[1] * hv;
+      o[5] = p.th[2] * hv;
+    }
+    const int nc = i < L - 1 ? 6 : 3;
+    for (int c = 0; c < nc; ++c) {
+      out[c * L + i] = o[c];
+      if (outf) outf[c * L + i] = static_cast<float>(o[c]);
     }
   }
 }
@@ -368,10 +375,8 @@ struct TfsfSurfParams {
   const long long *step;
 };
 
-template <typename T>
-__device__ __forceinline__ void add_corr(T &v, double corr) {
-  v = static_cast<T>(static_cast<double>(v) + corr);
-}
+__device__ __forceinline__ void add_corr(double &v, double corr) { v = v + corr; }
+__device__ __forceinline__ void add_corr(float &v, float corr) { v = v + corr; }
 
 // Maps a linear surface index to (i, j, k) on the surface of [a0,a1]x[b0,b1]x[c0,c1]
 // (32-bit arithmetic: a surface holds far fewer than 2^31 cells).
@@ -425,22 +430,24 @@ __device__ __forceinline__ int tfsf_e_terms(const TfsfDev &tf, int i, int j, int
 // ... and adds them to e, first face pair first.  hinc: the incident H
 // arrays of the previous step.
 template <int C, typename T>
-__device__ __forceinline__ void tfsf_e_add(const TfsfDev &tf, const double *hinc, int i, int j, int k, int terms,
-                                           T &e) {
+__device__ __forceinline__ void tfsf_e_add(const TfsfDev &tf, const decltype(tfsf_view<T>(tf).inc) hinc, int i, int j,
+                                           int k, int terms, T &e) {
+  const auto V = tfsf_view<T>(tf);
+  using R = typename std::remove_const<typename std::remove_pointer<decltype(V.inc)>::type>::type;
   const int li = tf.lo[0], ri = tf.hi[0], lj = tf.lo[1], rj = tf.hi[1], lk = tf.lo[2], rk = tf.hi[2];
   if (C == 0) {
     // Ex: y faces (j = lj: -= cay Hz_inc(i, lj-1, k); j = rj: += cay Hz_inc(i, rj, k)),
     //     z faces (k = lk: += caz Hy_inc(i, j, lk-1); k = rk: -= caz Hy_inc(i, j, rk))
     if (terms & 1) {
       const int jj = j == lj ? lj - 1 : rj;
-      const double pr = tf.ph[0][i - li + 1] + tf.ph[1][jj - lj + 1] + tf.pf[2][k - lk] - 0.5;
-      const double v = tf.ca[1] * tfsf_interp(hinc + 5 * tf.L, pr);
+      const R pr = V.ph[0][i - li + 1] + V.ph[1][jj - lj + 1] + V.pf[2][k - lk] - R(0.5);
+      const R v = V.ca[1] * tfsf_interp(hinc + 5 * tf.L, pr);
       add_corr(e, j == lj ? -v : v);
     }
     if (terms & 2) {
       const int kk = k == lk ? lk - 1 : rk;
-      const double pr = tf.ph[0][i - li + 1] + tf.pf[1][j - lj] + tf.ph[2][kk - lk + 1] - 0.5;
-      const double v = tf.ca[2] * tfsf_interp(hinc + 4 * tf.L, pr);
+      const R pr = V.ph[0][i - li + 1] + V.pf[1][j - lj] + V.ph[2][kk - lk + 1] - R(0.5);
+      const R v = V.ca[2] * tfsf_interp(hinc + 4 * tf.L, pr);
       add_corr(e, k == lk ? v : -v);
     }
   } else if (C == 1) {
@@ -448,14 +455,14 @@ __device__ __forceinline__ void tfsf_e_add(const TfsfDev &tf, const double *hinc
     //     z faces (k = lk: -= caz Hx_inc(i, j, lk-1); k = rk: += caz Hx_inc(i, j, rk))
     if (terms & 1) {
       const int ii = i == li ? li - 1 : ri;
-      const double pr = tf.ph[0][ii - li + 1] + tf.ph[1][j - lj + 1] + tf.pf[2][k - lk] - 0.5;
-      const double v = tf.ca[0] * tfsf_interp(hinc + 5 * tf.L, pr);
+      const R pr = V.ph[0][ii - li + 1] + V.ph[1][j - lj + 1] + V.pf[2][k - lk] - R(0.5);
+      const R v = V.ca[0] * tfsf_interp(hinc + 5 * tf.L, pr);
       add_corr(e, i == li ? v : -v);
     }
     if (terms & 2) {
       const int kk = k == lk ? lk - 1 : rk;
-      const double pr = tf.pf[0][i - li] + tf.ph[1][j - lj + 1] + tf.ph[2][kk - lk + 1] - 0.5;
-      const double v = tf.ca[2] * tfsf_interp(hinc + 3 * tf.L, pr);
+      const R pr = V.pf[0][i - li] + V.ph[1][j - lj + 1] + V.ph[2][kk - lk + 1] - R(0.5);
+      const R v = V.ca[2] * tfsf_interp(hinc + 3 * tf.L, pr);
       add_corr(e, k == lk ? -v : v);
     }
   } else {
@@ -463,22 +470,22 @@ __device__ __forceinline__ void tfsf_e_add(const TfsfDev &tf, const double *hinc
     //     y faces (j = lj: += cay Hx_inc(i, lj-1, k); j = rj: -= cay Hx_inc(i, rj, k))
     if (terms & 1) {
       const int ii = i == li ? li - 1 : ri;
-      const double pr = tf.ph[0][ii - li + 1] + tf.pf[1][j - lj] + tf.ph[2][k - lk + 1] - 0.5;
-      const double v = tf.ca[0] * tfsf_interp(hinc + 4 * tf.L, pr);
+      const R pr = V.ph[0][ii - li + 1] + V.pf[1][j - lj] + V.ph[2][k - lk + 1] - R(0.5);
+      const R v = V.ca[0] * tfsf_interp(hinc + 4 * tf.L, pr);
       add_corr(e, i == li ? -v : v);
     }
     if (terms & 2) {
       const int jj = j == lj ? lj - 1 : rj;
-      const double pr = tf.pf[0][i - li] + tf.ph[1][jj - lj + 1] + tf.ph[2][k - lk + 1] - 0.5;
-      const double v = tf.ca[1] * tfsf_interp(hinc + 3 * tf.L, pr);
+      const R pr = V.pf[0][i - li] + V.ph[1][jj - lj + 1] + V.ph[2][k - lk + 1] - R(0.5);
+      const R v = V.ca[1] * tfsf_interp(hinc + 3 * tf.L, pr);
       add_corr(e, j == lj ? v : -v);
     }
   }
 }
 
 template <int C, typename T>
-__device__ __forceinline__ void tfsf_e_component(const TfsfSurfParams<T> &p, const double *hinc, int i, int j, int k,
-                                                 long long b) {
+__device__ __forceinline__ void tfsf_e_component(const TfsfSurfParams<T> &p, const decltype(tfsf_view<T>(p.tf).inc) hinc,
+                                                 int i, int j, int k, long long b) {
   const int terms = tfsf_e_terms<C>(p.tf, i, j, k);
   if (!terms) return;
   T e = p.F[C][b];
@@ -492,7 +499,7 @@ __global__ void k_tfsf_e(TfsfSurfParams<T> p) {
   int i, j, k;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (!surface_cell(q, tf.lo[0], tf.hi[0], tf.lo[1], tf.hi[1], tf.lo[2], tf.hi[2], i, j, k)) return;
-  const double *hinc = tf.inc + (((*p.step) + 1) & 1) * 6 * tf.L;   // incident H of the previous step
+  const auto hinc = tfsf_view<T>(tf).inc + (((*p.step) + 1) & 1) * 6 * tf.L;   // incident H of the previous step
   const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
   tfsf_e_component<0>(p, hinc, i, j, k, b);
   tfsf_e_component<1>(p, hinc, i, j, k, b);
@@ -506,7 +513,9 @@ __global__ void k_tfsf_h(TfsfSurfParams<T> p) {
   int i, j, k;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (!surface_cell(q, li - 1, ri, lj - 1, rj, lk - 1, rk, i, j, k)) return;
-  const double *einc = tf.inc + ((*p.step) & 1) * 6 * tf.L;   // incident E of this step
+  const auto V = tfsf_view<T>(tf);
+  using R = typename std::remove_const<typename std::remove_pointer<decltype(V.inc)>::type>::type;
+  const R *einc = V.inc + ((*p.step) & 1) * 6 * tf.L;   // incident E of this step
   const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
   // Hx: y faces (j = lj-1: += cby Ez_inc(i, lj, k); j = rj: -= cby Ez_inc(i, rj, k)),
   //     z faces (k = lk-1: -= cbz Ey_inc(i, j, lk); k = rk: += cbz Ey_inc(i, j, rk))
@@ -517,14 +526,14 @@ __global__ void k_tfsf_h(TfsfSurfParams<T> p) {
       T h = p.F[3][b];
       if (w1) {
         const int jj = j == rj ? rj : lj;
-        const double pr = tf.pf[0][i - li] + tf.pf[1][jj - lj] + tf.ph[2][k - lk + 1];
-        const double v = tf.cb[1] * tfsf_interp(einc + 2 * tf.L, pr);
+        const R pr = V.pf[0][i - li] + V.pf[1][jj - lj] + V.ph[2][k - lk + 1];
+        const R v = V.cb[1] * tfsf_interp(einc + 2 * tf.L, pr);
         add_corr(h, j == rj ? -v : v);
       }
       if (w2) {
         const int kk = k == rk ? rk : lk;
-        const double pr = tf.pf[0][i - li] + tf.ph[1][j - lj + 1] + tf.pf[2][kk - lk];
-        const double v = tf.cb[2] * tfsf_interp(einc + 1 * tf.L, pr);
+        const R pr = V.pf[0][i - li] + V.ph[1][j - lj + 1] + V.pf[2][kk - lk];
+        const R v = V.cb[2] * tfsf_interp(einc + 1 * tf.L, pr);
         add_corr(h, k == rk ? v : -v);
       }
       p.F[3][b] = h;
@@ -539,14 +548,14 @@ __global__ void k_tfsf_h(TfsfSurfParams<T> p) {
       T h = p.F[4][b];
       if (w1) {
         const int ii = i == ri ? ri : li;
-        const double pr = tf.pf[0][ii - li] + tf.pf[1][j - lj] + tf.ph[2][k - lk + 1];
-        const double v = tf.cb[0] * tfsf_interp(einc + 2 * tf.L, pr);
+        const R pr = V.pf[0][ii - li] + V.pf[1][j - lj] + V.ph[2][k - lk + 1];
+        const R v = V.cb[0] * tfsf_interp(einc + 2 * tf.L, pr);
         add_corr(h, i == ri ? v : -v);
       }
       if (w2) {
         const int kk = k == rk ? rk : lk;
-        const double pr = tf.ph[0][i - li + 1] + tf.pf[1][j - lj] + tf.pf[2][kk - lk];
-        const double v = tf.cb[2] * tfsf_interp(einc + 0 * tf.L, pr);
+        const R pr = V.ph[0][i - li + 1] + V.pf[1][j - lj] + V.pf[2][kk - lk];
+        const R v = V.cb[2] * tfsf_interp(einc + 0 * tf.L, pr);
         add_corr(h, k == rk ? -v : v);
       }
       p.F[4][b] = h;
@@ -561,14 +570,14 @@ __global__ void k_tfsf_h(TfsfSurfParams<T> p) {
       T h = p.F[5][b];
       if (w1) {
         const int ii = i == ri ? ri : li;
-        const double pr = tf.pf[0][ii - li] + tf.ph[1][j - lj + 1] + tf.pf[2][k - lk];
-        const double v = tf.cb[0] * tfsf_interp(einc + 1 * tf.L, pr);
+        const R pr = V.pf[0][ii - li] + V.ph[1][j - lj + 1] + V.pf[2][k - lk];
+        const R v = V.cb[0] * tfsf_interp(einc + 1 * tf.L, pr);
         add_corr(h, i == ri ? -v : v);
       }
       if (w2) {
         const int jj = j == rj ? rj : lj;
-        const double pr = tf.ph[0][i - li + 1] + tf.pf[1][jj - lj] + tf.pf[2][k - lk];
-        const double v = tf.cb[1] * tfsf_interp(einc + 0 * tf.L, pr);
+        const R pr = V.ph[0][i - li + 1] + V.pf[1][jj - lj] + V.pf[2][k - lk];
+        const R v = V.cb[1] * tfsf_interp(einc + 0 * tf.L, pr);
         add_corr(h, j == rj ? v : -v);
       }
       p.F[5][b] = h;

@@ -28,8 +28,11 @@
 // here: plans with them run the split kernels.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "surface.cuh"
+#include "tma.cuh"
 #include "volume.cuh"
 
 namespace xg {
@@ -40,6 +43,7 @@ struct SweepParams {
   T *E2[3], *H2[3];    // E and H of step t+1
   Psi<T> psi2;         // E psi of step t+1 (the H members are unused)
   int chunk;           // planes along i per block
+  int *status;         // set to XFDTD_ERR_TIMEOUT if a stage wait gives up
 };
 
 constexpr int kSwK = 32;                         // owned tile: 32 cells along k
@@ -49,24 +53,54 @@ constexpr int kEK = kSwK + 1, kEJ = kSwJ + 1;    // E(t+1) tile: one halo cell o
 constexpr int kEHalo = kEK + kSwJ;               // halo E cells: row j0+8 (33) and column k0+32 (8)
 constexpr int kSwThreads = kSwK * kSwJ;
 
-// Per thread, the global values of one plane that the sweep needs: up to
-// two H(t) tile elements, E(t) and the material index of the thread's own
-// cell and (for the first kEHalo threads) of one halo cell.  Loaded one
-// plane ahead so that the loads of plane i+1 are in flight while plane i is
-// computed.
-template <typename T>
-struct SweepPlane {
-  T h0[3], h1[3];
-  T e[3], eh[3];
-  unsigned idx, idxh;
-  uint8_t fi;   // flags of plane i
+// Shared-memory staging.  For each plane the block needs H(t) on its tile
+// with a one-cell halo all round (rows j0-1 .. j0+8, columns k0-1 .. k0+32),
+// E(t) and the material index on the E tile (rows j0 .. j0+8, columns
+// k0 .. k0+32).  One elected thread fetches them with tiled TMA loads
+// (cp.async.bulk.tensor) into a ring of kStages plane stages, kStages-2
+// planes ahead of the plane being computed; an mbarrier per stage counts
+// the bytes in.  Tile rows start on 16-byte boundaries as TMA requires: the
+// H rows start at k0-4 (FP32) or k0-2 (FP64), the E and index rows at k0,
+// and the boxes are widened to whole 16-byte rows.  Out-of-range parts of a
+// box (j or k beyond the grid, plane -1) arrive as zeros.
+constexpr int kStages = 4;
+
+__host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128; }
+
+template <typename T, typename I>
+struct SweepTiles {
+  static constexpr int HW = sizeof(T) == 4 ? 40 : 36;    // H row: columns k0-HOFF-1 ..
+  static constexpr int HOFF = sizeof(T) == 4 ? 3 : 1;    // tile column of k0-1, minus 0
+  static constexpr int EW = sizeof(T) == 4 ? 36 : 34;    // E row: columns k0 ..
+  static constexpr int IW = sizeof(I) == 1 ? 48 : 40;    // index row: columns k0 ..
+  static constexpr int H_TILE = round128(kHJ * HW * int(sizeof(T)));
+  static constexpr int E_TILE = round128(kEJ * EW * int(sizeof(T)));
+  static constexpr int I_TILE = round128(kEJ * IW * int(sizeof(I)));
+  static constexpr int STAGE = 3 * H_TILE + 3 * E_TILE + I_TILE;
+  static constexpr int SE = round128(2 * 3 * kEJ * kEK * int(sizeof(T)));   // E(t+1) of planes i-1, i
+  static constexpr int SMEM = kStages * STAGE + SE + kStages * 8;
+  static constexpr unsigned H_BYTES = 3u * kHJ * HW * sizeof(T);
+  static constexpr unsigned FULL_BYTES = H_BYTES + 3u * kEJ * EW * sizeof(T) + unsigned(kEJ * IW * sizeof(I));
 };
 
+// The tensor maps of one launch: H(t) and E(t) components and the index.
+struct SweepMaps {
+  CUtensorMap h[3];
+  CUtensorMap e[3];
+  CUtensorMap idx;
+};
+
+// Polls of a stage barrier before the sweep gives up and reports
+// XFDTD_ERR_TIMEOUT through the status word.
+constexpr int kSweepWaitLimit = 1 << 22;
+
 template <typename T, typename I, int MINB>
-__global__ void __launch_bounds__(kSwThreads, MINB) k_sweep(SweepParams<T, I> f) {
+__global__ void __launch_bounds__(kSwThreads, MINB) k_sweep(const __grid_constant__ SweepMaps maps, SweepParams<T, I> f) {
+  using G = SweepTiles<T, I>;
   const VolParams<T, I> &p = f.v;
-  __shared__ T sH[3][3][kHJ][kHK];   // H(t) of planes i-2 .. i (ring of 3)
-  __shared__ T sE[3][3][kEJ][kEK];   // E(t+1) of planes i-2 .. i (ring of 3)
+  extern __shared__ __align__(128) unsigned char smem[];
+  T(*sE)[3][kEJ][kEK] = reinterpret_cast<T(*)[3][kEJ][kEK]>(smem + kStages * G::STAGE);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kStages * G::STAGE + G::SE);
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const int lane = threadIdx.x, row = threadIdx.y, tid = row * kSwK + lane;
@@ -74,16 +108,55 @@ __global__ void __launch_bounds__(kSwThreads, MINB) k_sweep(SweepParams<T, I> f)
   const int ia = blockIdx.z * f.chunk;
   if (ia > nx) return;
   const int ib = min(ia + f.chunk, nx + 1);   // owned planes [ia, ib)
-  const double *hinc = p.tf.enabled ? p.tf.inc + (((*p.step) + 1) & 1) * 6 * p.tf.L : nullptr;
+  const int last = min(ib, nx);               // last plane loaded
+  const auto hinc = p.tf.enabled ? tfsf_view<T>(p.tf).inc + (((*p.step) + 1) & 1) * 6 * p.tf.L : nullptr;
 
-  // this thread's H tile elements (tid and tid + 256 of the 10 x 34 tile)
-  const int hr0 = tid / kHK, hc0 = tid - hr0 * kHK;
-  const int e1 = tid + kSwThreads, hr1 = e1 / kHK, hc1 = e1 - hr1 * kHK;
-  const bool has1 = e1 < kHJ * kHK;
-  const int hj0 = j0 - 1 + hr0, hk0 = k0 - 1 + hc0, hj1 = j0 - 1 + hr1, hk1 = k0 - 1 + hc1;
-  const bool hin0 = hj0 >= 0 && hj0 <= ny && hk0 >= 0 && hk0 <= nz;
-  const bool hin1 = has1 && hj1 >= 0 && hj1 <= ny && hk1 >= 0 && hk1 <= nz;
-  // the thread's own cell and its halo cell of the E tile
+  // stage of plane q: planes ia-1 .. last in order, kStages in the ring
+  auto stage_of = [&](int q) { return (q - ia + 1) % kStages; };
+  auto h_tile = [&](int st, int c) { return reinterpret_cast<T *>(smem + st * G::STAGE + c * G::H_TILE); };
+  auto e_tile = [&](int st, int c) {
+    return reinterpret_cast<T *>(smem + st * G::STAGE + 3 * G::H_TILE + c * G::E_TILE);
+  };
+  auto i_tile = [&](int st) { return reinterpret_cast<I *>(smem + st * G::STAGE + 3 * G::H_TILE + 3 * G::E_TILE); };
+  // H(t) at H-tile cell (r, c), r = j - (j0-1), c = k - (k0-1)
+  auto hv = [&](int st, int comp, int r, int c) { return h_tile(st, comp)[r * G::HW + c + G::HOFF]; };
+
+  // thread 0: start the loads of plane q (H only for plane ia-1)
+  auto issue = [&](int q) {
+    const int st = stage_of(q);
+    const bool full = q >= ia;
+    mbar_arrive_expect_tx(&bar[st], full ? G::FULL_BYTES : G::H_BYTES);
+    for (int c = 0; c < 3; ++c) tma_load_3d(h_tile(st, c), &maps.h[c], k0 - G::HOFF - 1, j0 - 1, q, &bar[st]);
+    if (full) {
+      for (int c = 0; c < 3; ++c) tma_load_3d(e_tile(st, c), &maps.e[c], k0, j0, q, &bar[st]);
+      tma_load_3d(i_tile(st), &maps.idx, k0, j0, q, &bar[st]);
+    }
+  };
+
+  if (tid == 0) {
+    for (int q = 0; q < kStages; ++q) mbar_init(&bar[q], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (ia == 0) {   // plane -1: H(t) = 0, written here instead of loaded
+    for (int c = 0; c < 3; ++c)
+      for (int e = tid; e < kHJ * G::HW; e += kSwThreads) h_tile(0, c)[e] = T(0);
+  }
+  if (tid == 0) {
+    fence_proxy_async();
+    for (int q = max(ia - 1, 0); q <= min(ia + kStages - 2, last); ++q) issue(q);
+  }
+  unsigned phase = 0;   // bit s: parity of the next completion of stage s
+  bool timed_out = false;
+  auto wait_plane = [&](int q) {
+    const int st = stage_of(q);
+    if (!mbar_wait_bounded(&bar[st], (phase >> st) & 1u, kSweepWaitLimit)) timed_out = true;
+    phase ^= 1u << st;
+  };
+  if (ia > 0) wait_plane(ia - 1);
+  __syncthreads();   // the zeros of plane -1 are visible
+
+  // this thread's own cell and its halo cell of the E tile
   const int jm = j0 + row, km = k0 + lane;
   const bool min_ = jm <= ny && km <= nz;
   const bool has_h = tid < kEHalo;
@@ -93,49 +166,23 @@ __global__ void __launch_bounds__(kSwThreads, MINB) k_sweep(SweepParams<T, I> f)
   const uint8_t fjk = min_ ? (__ldg(p.flags[1] + jm) | __ldg(p.flags[2] + km)) : 0;
   const uint8_t fjkh = hin_ ? (__ldg(p.flags[1] + jh) | __ldg(p.flags[2] + kh)) : 0;
 
-  auto fetch = [&](int i, SweepPlane<T> &q) {
-    const bool pin = i >= 0 && i <= nx;
-    const unsigned bi = pin ? static_cast<unsigned>(i) * usi : 0u;
-    const unsigned b0 = bi + static_cast<unsigned>(hj0) * usj + hk0, b1 = bi + static_cast<unsigned>(hj1) * usj + hk1;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      q.h0[c] = pin && hin0 ? __ldg(p.H[c] + b0) : T(0);
-      q.h1[c] = pin && hin1 ? __ldg(p.H[c] + b1) : T(0);
-    }
-    const unsigned bm = bi + static_cast<unsigned>(jm) * usj + km, bh = bi + static_cast<unsigned>(jh) * usj + kh;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      q.e[c] = pin && min_ ? __ldg(p.E[c] + bm) : T(0);
-      q.eh[c] = pin && hin_ ? __ldg(p.E[c] + bh) : T(0);
-    }
-    q.idx = pin && min_ ? static_cast<unsigned>(__ldg(p.idx + bm)) : 0u;
-    q.idxh = pin && hin_ ? static_cast<unsigned>(__ldg(p.idx + bh)) : 0u;
-    q.fi = pin ? __ldg(p.flags[0] + i) : 0;
-  };
-  auto stash_h = [&](const SweepPlane<T> &q, int s) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      sH[s][c][hr0][hc0] = q.h0[c];
-      if (has1) sH[s][c][hr1][hc1] = q.h1[c];
-    }
-  };
-
-  // E(t+1) of plane i at tile cell (r, c) from E(t) = e; `own`: also store
-  // it (and its psi) as the new state
-  auto e_update = [&](int i, int r, int c, bool own, const T *eo, unsigned id, uint8_t fl) {
-    const int j = j0 + r, k = k0 + c, s = i % 3, sm = (i + 2) % 3;
-    T ex = eo[0], ey = eo[1], ez = eo[2];
-    const ECurl<T> h{sH[s][0][r + 1][c + 1], sH[s][1][r + 1][c + 1], sH[s][2][r + 1][c + 1],
-                     sH[s][0][r + 1][c],     sH[s][1][r + 1][c],     sH[s][0][r][c + 1],
-                     sH[s][2][r][c + 1],     sH[sm][1][r + 1][c + 1], sH[sm][2][r + 1][c + 1]};
-    const T *cf = p.table + id * 18;
-    if (!(fl & kSpecialE)) {
+  // E(t+1) of plane i at E-tile cell (r, c); `own`: also store it (and its
+  // psi) as the new state
+  auto e_update = [&](auto plain_tile, int i, int r, int c, bool own, uint8_t fl) {
+    constexpr bool kPlain = decltype(plain_tile)::value;
+    const int j = j0 + r, k = k0 + c, s = i & 1, st = stage_of(i), sm = stage_of(i - 1);
+    T ex = e_tile(st, 0)[r * G::EW + c], ey = e_tile(st, 1)[r * G::EW + c], ez = e_tile(st, 2)[r * G::EW + c];
+    const ECurl<T> h{hv(st, 0, r + 1, c + 1), hv(st, 1, r + 1, c + 1), hv(st, 2, r + 1, c + 1),
+                     hv(st, 0, r + 1, c),     hv(st, 1, r + 1, c),     hv(st, 0, r, c + 1),
+                     hv(st, 2, r, c + 1),     hv(sm, 1, r + 1, c + 1), hv(sm, 2, r + 1, c + 1)};
+    const T *cf = p.table + static_cast<unsigned>(i_tile(st)[r * G::IW + c]) * 18;
+    if (kPlain || !(fl & kSpecialE)) {
       e_plain(cf, h, ex, ey, ez);
     } else {
       bool w[3];
       e_general<T, I, true>(p, cf, i, j, k, h, p.psi, f.psi2, own, ex, ey, ez, w);
     }
-    if ((fl & kTfsfE) && hinc) {
+    if (!kPlain && (fl & kTfsfE) && hinc) {
       int t;
       if ((t = tfsf_e_terms<0>(p.tf, i, j, k))) tfsf_e_add<0>(p.tf, hinc, i, j, k, t, ex);
       if ((t = tfsf_e_terms<1>(p.tf, i, j, k))) tfsf_e_add<1>(p.tf, hinc, i, j, k, t, ey);
@@ -158,14 +205,15 @@ __global__ void __launch_bounds__(kSwThreads, MINB) k_sweep(SweepParams<T, I> f)
   };
 
   // H(t+1) of plane i at owned tile cell (r, c)
-  auto h_update = [&](int i, int r, int c, unsigned id, uint8_t fl) {
-    const int j = j0 + r, k = k0 + c, s = i % 3, sp = (i + 1) % 3;
+  auto h_update = [&](auto plain_tile, int i, int r, int c, uint8_t fl) {
+    constexpr bool kPlain = decltype(plain_tile)::value;
+    const int j = j0 + r, k = k0 + c, s = i & 1, sp = (i + 1) & 1, st = stage_of(i);
     const HCurl<T> e{sE[s][0][r][c],     sE[s][1][r][c],     sE[s][2][r][c],
                      sE[s][0][r][c + 1], sE[s][1][r][c + 1], sE[s][0][r + 1][c],
                      sE[s][2][r + 1][c], sE[sp][1][r][c],    sE[sp][2][r][c]};
-    T hx = sH[s][0][r + 1][c + 1], hy = sH[s][1][r + 1][c + 1], hz = sH[s][2][r + 1][c + 1];
-    const T *cf = p.table + id * 18 + 9;
-    if (!(fl & kSpecialH)) {
+    T hx = hv(st, 0, r + 1, c + 1), hy = hv(st, 1, r + 1, c + 1), hz = hv(st, 2, r + 1, c + 1);
+    const T *cf = p.table + static_cast<unsigned>(i_tile(st)[r * G::IW + c]) * 18 + 9;
+    if (kPlain || !(fl & kSpecialH)) {
       h_plain(cf, e, hx, hy, hz);
     } else {
       bool w[3];
@@ -177,34 +225,50 @@ __global__ void __launch_bounds__(kSwThreads, MINB) k_sweep(SweepParams<T, I> f)
     f.H2[2][b] = hz;
   };
 
-  SweepPlane<T> cur, nxt;
-  fetch(ia - 1, nxt);   // H(t) of plane ia-1 (zeros for ia = 0)
-  stash_h(nxt, (ia + 2) % 3);
-  fetch(ia, cur);
-  unsigned idx_prev = 0;   // material index of the own cell on plane i-1
-  uint8_t fi_prev = 0;
+  // Tiles whose rows and columns carry no wall, CPML or TFSF flag take the
+  // plain update on every plane that carries none either (same bits, no
+  // general-path code).
+  const std::integral_constant<bool, true> plain;
+  const std::integral_constant<bool, false> general;
+  const bool tile_plain_e = __syncthreads_and(!((fjk | fjkh) & (kSpecialE | kTfsfE)));
+  const bool tile_plain_h = __syncthreads_and(!(fjk & kSpecialH));
   for (int i = ia; i <= ib; ++i) {
-    const int s = i % 3;
-    stash_h(cur, s);
-    if (i < ib) fetch(i + 1, nxt);   // in flight while plane i is computed
-    __syncthreads();
+    const int s = i & 1;
     if (i <= nx) {
-      if (min_) e_update(i, row, lane, i < ib, cur.e, cur.idx, cur.fi | fjk);
-      else e_zero(s, row, lane);
-      if (has_h) {
-        if (hin_) e_update(i, rh, ch, false, cur.eh, cur.idxh, cur.fi | fjkh);
-        else e_zero(s, rh, ch);
+      wait_plane(i);
+      const uint8_t fi = __ldg(p.flags[0] + i);
+      if (tile_plain_e && !(fi & (kSpecialE | kTfsfE))) {
+        if (min_) e_update(plain, i, row, lane, i < ib, 0);
+        else e_zero(s, row, lane);
+        if (has_h) {
+          if (hin_) e_update(plain, i, rh, ch, false, 0);
+          else e_zero(s, rh, ch);
+        }
+      } else {
+        if (min_) e_update(general, i, row, lane, i < ib, fi | fjk);
+        else e_zero(s, row, lane);
+        if (has_h) {
+          if (hin_) e_update(general, i, rh, ch, false, fi | fjkh);
+          else e_zero(s, rh, ch);
+        }
       }
     } else {   // past the last plane: E(t+1) of plane nx+1 is zero
       T *z = &sE[s][0][0][0];
       for (int e = tid; e < 3 * kEJ * kEK; e += kSwThreads) z[e] = T(0);
     }
     __syncthreads();
-    if (i > ia && min_) h_update(i - 1, row, lane, idx_prev, fi_prev | fjk);
-    idx_prev = cur.idx;
-    fi_prev = cur.fi;
-    cur = nxt;
+    if (i > ia && min_) {
+      const uint8_t fi = __ldg(p.flags[0] + i - 1);
+      if (tile_plain_h && !(fi & kSpecialH)) h_update(plain, i - 1, row, lane, 0);
+      else h_update(general, i - 1, row, lane, fi | fjk);
+    }
+    __syncthreads();   // stage of plane i-1 and E(t+1) slot of plane i-1 are free
+    if (tid == 0 && i + kStages - 1 <= last) {
+      fence_proxy_async();
+      issue(i + kStages - 1);
+    }
   }
+  if (timed_out) atomicExch(f.status, static_cast<int>(4));   // XFDTD_ERR_TIMEOUT
 }
 
 }  // namespace xg
