@@ -262,6 +262,37 @@ def reference_arm(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_batched_form(args, local):
+    """The batched form: many uneven scatterer problems (interior 32 .. 160
+    cells per axis, 8-cell CPML, 500 .. 1500 steps each) advanced as one
+    batch, against the same problems run one after another with the plain
+    single-simulation kernels on the same GPU.  Both timed with CUDA events
+    over the step loops (set-up excluded), FP32."""
+    from xfdtd_gb300 import configs
+    probs = configs.batched_scatterers(n=args.batch_problems)
+    members = [X.Simulation(sc, st, precision="fp32", fused=False, autotune=False, device=local) for sc, st in probs]
+    cells = [m.n[0] * m.n[1] * m.n[2] for m in members]
+    work = sum(c * st for c, (_, st) in zip(cells, probs))
+    b = X.Batch(members, graph=True)
+    ms_b = b.step_timed(max(st for _, st in probs))
+    b.synchronize()
+    launches = b.status()["launches"]
+    for m in members:
+        m.check_finite()
+    del b, members
+    ms_s = 0.0
+    for sc, st in probs:   # sequential: each problem alone, plain split kernels, graph replay
+        s = X.Simulation(sc, st, precision="fp32", fused=False, autotune=False, device=local)
+        ms_s += s.step_timed(st)
+        del s
+    return {"problems": len(probs), "cells_total": sum(cells), "cell_updates": work,
+            "value": work / (ms_b / 1e3) / 1e6, "unit": UNIT, "ms": ms_b, "launches": launches,
+            "sequential_value": work / (ms_s / 1e3) / 1e6, "sequential_ms": ms_s,
+            "speedup_vs_sequential": ms_s / ms_b,
+            "workload": "64 dielectric-sphere problems, interior U{32..160}^3 + 8-cell CPML, "
+                        "steps U{500..1500}, seeds 4000+i"}
+
+
 def ours_arm(args, world, rank, local, grp):
     import xfdtd_gb300 as X
     X.build()
@@ -330,6 +361,8 @@ def ours_arm(args, world, rank, local, grp):
                 "dominant_kernel_GBs": a64, "note": "GB300 FP64 is ~1/64 rate: this form is compute-bound"}
         del s64
 
+    batched = run_batched_form(args, local) if (args.batch_problems > 0 and rank == 0) else None
+
     cpu = None
     if rank == 0 and world == 1 and args.cpu_sample > 0:
         v, cores, sample = run_cpu_oracle(1, args.cpu_sample)
@@ -362,6 +395,7 @@ def ours_arm(args, world, rank, local, grp):
         "clocks": clocks,
         "cpu_baseline": cpu,
         "fp64_form": fp64,
+        "batched_form": batched,
     }
     print(json.dumps(line), flush=True)
 
@@ -376,6 +410,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=200)
     ap.add_argument("--cpu-sample", type=int, default=8, help="oracle steps timed for cpu_baseline (0: skip)")
     ap.add_argument("--ref-budget", type=float, default=120.0, help="seconds of oracle work for --impl reference")
+    ap.add_argument("--batch-problems", type=int, default=64, help="problems of the batched form (0: skip)")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.impl == "reference":

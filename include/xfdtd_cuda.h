@@ -229,6 +229,33 @@ void xfdtd_destroy(xfdtd_handle *h);
 const char *xfdtd_version(void);
 
 /* ---------------------------------------------------------------------
+ * Batches: many independent simulations of different sizes advanced
+ * together.  The reference runs one Simulation at a time
+ * (simulation_update.cpp:5-40); a batch runs each phase of the loop body
+ * for all of its members in one launch over a (member, tile) work list,
+ * and replays the step loop from a CUDA graph (XFDTD_FLAG_GRAPH).  Members
+ * are ordinary handles from xfdtd_create -- same device, precision and
+ * material-index width, not yet stepped, without lumped elements or
+ * monitors; the batch does not own them.  Each member stops at its own
+ * total_steps.  A batched member gives the same bits as the same handle
+ * stepped alone with XFDTD_FLAG_SPLIT_EH.  After xfdtd_batch_synchronize
+ * the members are read with the ordinary entry points (xfdtd_read_field,
+ * xfdtd_read_nffft, xfdtd_far_field, ...); they must not be stepped on
+ * their own while in a batch. */
+typedef struct xfdtd_batch xfdtd_batch;
+
+int xfdtd_batch_create(xfdtd_handle *const *members, int n, int flags, xfdtd_batch **out);
+/* Advances every member that has steps left by up to n steps (asynchronous). */
+int xfdtd_batch_step(xfdtd_batch *b, int64_t n);
+/* The same, returning the device time of the n steps (CUDA events). */
+int xfdtd_batch_step_timed(xfdtd_batch *b, int64_t n, double *ms);
+int xfdtd_batch_synchronize(xfdtd_batch *b);
+/* Members with steps left, batch steps taken, kernel launches enqueued. */
+int xfdtd_batch_status(xfdtd_batch *b, int *n_running, int64_t *clock, int64_t *launches);
+const char *xfdtd_batch_last_error(xfdtd_batch *b);
+void xfdtd_batch_destroy(xfdtd_batch *b);
+
+/* ---------------------------------------------------------------------
  * Allocation-free NF-FF running DFT.  No counterpart in the reference: it
  * is NffftFd::update (nffft_fd.cpp:108-203) as a stand-alone operator on
  * caller-owned device arrays for callers that may not allocate device

@@ -91,3 +91,19 @@ int main(void) {
     mine = [C.sizeof(t) for t in (S.SceneDesc, S.ObjectDesc, S.WaveformDesc, S.PMLDesc, S.TFSFDesc,
                                   S.NFFFTDesc, S.LumpedDesc, S.MonitorDesc)]
     assert sizes == mine
+
+
+def test_batch_rejects_empty_member_list_on_the_host(libs):
+    cu, _ = libs
+    cu.xfdtd_batch_create.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+    cu.xfdtd_batch_last_error.argtypes = [C.c_void_p]
+    cu.xfdtd_batch_last_error.restype = C.c_char_p
+    cu.xfdtd_batch_destroy.argtypes = [C.c_void_p]
+    b = C.c_void_p()
+    assert cu.xfdtd_batch_create(None, 0, 0, C.byref(b)) == 1
+    assert b"at least one member" in cu.xfdtd_batch_last_error(b)
+    cu.xfdtd_batch_destroy(b)
+    members = (C.c_void_p * 2)(None, None)
+    assert cu.xfdtd_batch_create(members, 2, 0, C.byref(b)) == 1
+    assert b"not a created handle" in cu.xfdtd_batch_last_error(b)
+    cu.xfdtd_batch_destroy(b)

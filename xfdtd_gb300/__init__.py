@@ -88,6 +88,14 @@ def libs():
         cu.xfdtd_last_error.argtypes = [C.c_void_p]
         cu.xfdtd_last_error.restype = C.c_char_p
         cu.xfdtd_version.restype = C.c_char_p
+        cu.xfdtd_batch_create.argtypes = [P(C.c_void_p), C.c_int, C.c_int, P(C.c_void_p)]
+        cu.xfdtd_batch_step.argtypes = [C.c_void_p, C.c_int64]
+        cu.xfdtd_batch_step_timed.argtypes = [C.c_void_p, C.c_int64, dp]
+        cu.xfdtd_batch_synchronize.argtypes = [C.c_void_p]
+        cu.xfdtd_batch_status.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int64), P(C.c_int64)]
+        cu.xfdtd_batch_last_error.argtypes = [C.c_void_p]
+        cu.xfdtd_batch_last_error.restype = C.c_char_p
+        cu.xfdtd_batch_destroy.argtypes = [C.c_void_p]
         _cuda, _host = cu, ho
     return _cuda, _host
 
@@ -269,3 +277,50 @@ class Simulation:
 
 def version() -> str:
     return libs()[0].xfdtd_version().decode()
+
+
+class Batch:
+    """Several simulations of different sizes advanced together
+    (xfdtd_batch_*): one launch per phase over a work list of every member
+    still running, the step loop replayed from a CUDA graph.  Members are
+    `Simulation`s created with fused=False, not yet stepped, without lumped
+    elements or monitors; each stops at its own total_steps.  Read them with
+    their own methods after `synchronize()`."""
+
+    def __init__(self, members: list, graph: bool = True):
+        cu, _ = libs()
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.engine.value for m in self.members])
+        b = C.c_void_p()
+        rc = cu.xfdtd_batch_create(arr, len(self.members), FLAG_GRAPH if graph else 0, C.byref(b))
+        self.b = b
+        if rc != 0:
+            msg = cu.xfdtd_batch_last_error(b).decode()
+            cu.xfdtd_batch_destroy(b)
+            self.b = None
+            raise EngineError(rc, msg)
+
+    def _check(self, rc):
+        if rc != 0:
+            raise EngineError(rc, libs()[0].xfdtd_batch_last_error(self.b).decode())
+
+    def step(self, n: int):
+        self._check(libs()[0].xfdtd_batch_step(self.b, int(n)))
+
+    def step_timed(self, n: int) -> float:
+        ms = C.c_double()
+        self._check(libs()[0].xfdtd_batch_step_timed(self.b, int(n), C.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        self._check(libs()[0].xfdtd_batch_synchronize(self.b))
+
+    def status(self) -> dict:
+        r, clock, launches = C.c_int(), C.c_int64(), C.c_int64()
+        self._check(libs()[0].xfdtd_batch_status(self.b, C.byref(r), C.byref(clock), C.byref(launches)))
+        return {"running": r.value, "clock": clock.value, "launches": launches.value}
+
+    def __del__(self):
+        if getattr(self, "b", None) and _cuda is not None:
+            _cuda.xfdtd_batch_destroy(self.b)
+            self.b = None

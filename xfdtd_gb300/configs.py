@@ -22,6 +22,9 @@ seconds.
                       (Gaussian-modulated sine, f0 = 10 GHz, 5 GHz
                       bandwidth), 64 Ez probes at seeded cells (seed 1003),
                       1000 steps.
+  batched_scatterers  64 uneven dielectric-sphere problems (interior 32 ..
+                      160 cells per axis, 8-cell CPML, 500 .. 1500 steps),
+                      run together as one batch.
 """
 from __future__ import annotations
 
@@ -111,6 +114,37 @@ def heterogeneous(scale: int = 1, steps: int = 1000, n_probes: int = 64):
                  voxel_materials=mats, voxel_index=voxel)
     del dt
     return sc, steps
+
+
+def batched_scatterers(n: int = 64, scale: int = 1, seed0: int = 4000, n_theta: int = 19):
+    """`n` independent scatterer problems with uneven grids (problem i seeded
+    with seed0 + i): interior dims uniform in 32 .. 160 cells per axis,
+    8-cell CPML, dx = 2 mm, a dielectric sphere of radius 20-40 % of the
+    smallest dimension with eps_r uniform in [2, 8] (as float) at the
+    centre, TFSF 4 cells inside the CPML (x-polarised +z Gaussian, tau =
+    30 dt, t0 = 4.5 tau), NF-FF 6 cells inside the CPML at 1 GHz, steps
+    uniform in 500 .. 1500.  Returns a list of (Scene, total_steps); `scale`
+    divides the interior dims and the steps."""
+    dl = 2e-3
+    cpml = 8
+    out = []
+    for i in range(n):
+        rng = np.random.default_rng(seed0 + i)
+        dims = [int(v) // scale for v in rng.integers(32, 161, size=3)]
+        radius = float(rng.uniform(0.2, 0.4)) * min(dims)
+        eps = float(np.float32(rng.uniform(2.0, 8.0)))
+        steps = int(rng.integers(500, 1501)) // scale
+        objects = [
+            S.Object("domain", S.Cube([0.0, 0.0, 0.0], [v * dl for v in dims]), S.Material("air", 1, 1, 0, 0)),
+            S.Object("sphere", S.Sphere([v * dl / 2 for v in dims], radius * dl), S.Material("d", eps, 1, 0, 0)),
+        ]
+        dt = cfl_dt(dl, 0.98)
+        tau = 30 * dt
+        tfsf = S.TFSF3D(cpml + 4, cpml + 4, cpml + 4, 1.0, 0.0, 0.0, 0.0, S.GaussianWaveform(1.0, tau, 4.5 * tau))
+        nffft = S.NffftFd(cpml + 6, cpml + 6, cpml + 6, [1e9], np.linspace(0.0, math.pi, n_theta), [0.0],
+                          f"batched_{i}")
+        out.append((S.Scene(dl, objects, _six_pml(cpml), tfsf=tfsf, nffft=nffft, cfl=0.98), steps))
+    return out
 
 
 CONFIGS = {

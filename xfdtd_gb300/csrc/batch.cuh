@@ -1,0 +1,142 @@
+// batch.cuh -- kernels that advance many independent simulations at once.
+//
+// A batch (engine.cu, xfdtd_batch_*) drives several engine handles of
+// different grid sizes.  Each phase of a step is one launch over a work
+// list of (simulation, tile) items for all simulations still running.  The
+// volume phases run one block per item; the surface phases (few items per
+// simulation) have a fixed number of blocks, each walking a contiguous
+// range of the list and loading a simulation's parameters into shared
+// memory when its range crosses into the next simulation.
+// Per cell the work is that of the single-simulation split kernels
+// (e_plain / e_cell, h_plain / h_cell, tfsf_e_surface / tfsf_h_surface,
+// nffft_sample / nffft_fold, tfsf_aux_block), so a batched simulation gives
+// the same bits as the same simulation run alone.
+#pragma once
+
+#include "common.cuh"
+#include "surface.cuh"
+#include "volume.cuh"
+
+namespace xg {
+
+// One work item: simulation `sim`, tile `tile` of that simulation's launch
+// grid for the phase (a tile is one 256-thread block of the split kernel).
+struct WorkItem {
+  int sim;
+  int tile;
+};
+
+// Range of work items of this block: contiguous, equal shares.
+__device__ __forceinline__ void item_range(int n_items, int &lo, int &hi) {
+  const int per = (n_items + gridDim.x - 1) / gridDim.x;
+  lo = blockIdx.x * per;
+  hi = min(lo + per, n_items);
+}
+
+// Copies the parameter struct of simulation `sim` into shared memory (all
+// threads; returns after a barrier).
+template <typename P>
+__device__ __forceinline__ void load_params(P &dst, const P *all, int sim) {
+  __syncthreads();   // everyone is done with the previous simulation's copy
+  const int *src = reinterpret_cast<const int *>(all + sim);
+  int *d = reinterpret_cast<int *>(&dst);
+  for (int q = threadIdx.x; q < static_cast<int>(sizeof(P) / sizeof(int)); q += blockDim.x) d[q] = src[q];
+  __syncthreads();
+}
+
+// Volume update (E or H): one block per listed tile, a tile being 32 (k) x
+// 8 (j) cells of one plane i, packed as i << 16 | j-block << 8 | k-block.
+// The block reads its simulation's parameters from the array (the same
+// addresses for every thread: served by L1); per cell the update is that of
+// the split kernels.  (A persistent form -- a fixed grid walking the list,
+// one or two tiles per block at a time -- ran at 14-21 Gcell-updates/s on
+// GB300 against 25+ for one block per tile: fewer resident warps.)
+template <typename T, typename I, bool E_SIDE>
+__global__ void __launch_bounds__(256, 6) k_volume_batch(const VolParams<T, I> *__restrict__ all,
+                                                          const WorkItem *__restrict__ items) {
+  const WorkItem it = items[blockIdx.x];
+  const VolParams<T, I> &p = all[it.sim];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int i = it.tile >> 16, j = ((it.tile >> 8) & 0xff) * 8 + ty, k = (it.tile & 0xff) * 32 + tx;
+  if (k > p.d.nz || j > p.d.ny) return;
+  if (E_SIDE) e_cell<T, I>(p, p.table, 18, i, j, k);
+  else h_cell<T, I>(p, p.table + 9, 18, i, j, k);
+}
+
+// TFSF E or H corrections: tile = 256 consecutive surface cells.
+template <typename T, bool E_SIDE>
+__global__ void __launch_bounds__(256) k_tfsf_batch(const TfsfSurfParams<T> *__restrict__ all,
+                                                    const WorkItem *__restrict__ items, int n_items) {
+  __shared__ TfsfSurfParams<T> p;
+  int lo, hi;
+  item_range(n_items, lo, hi);
+  int cur = -1;
+  for (int w = lo; w < hi; ++w) {
+    const WorkItem it = items[w];
+    if (it.sim != cur) {
+      load_params(p, all, it.sim);
+      cur = it.sim;
+    }
+    const int q = it.tile * 256 + threadIdx.x;
+    if (E_SIDE) tfsf_e_surface(p, q);
+    else tfsf_h_surface(p, q);
+  }
+}
+
+// NF-FF surface samples: tile = (face, 32 x 8 face block), numbered
+// u-block fastest, then v-block, then face; the grid of a simulation is
+// that of k_nffft, given by gu x gv per face (ints 0, 1 of the tile).
+template <typename T>
+__global__ void __launch_bounds__(256) k_nffft_batch(const NfParams<T> *__restrict__ all, const int2 *__restrict__ grid,
+                                                     const WorkItem *__restrict__ items, int n_items) {
+  __shared__ NfParams<T> p;
+  int lo, hi;
+  item_range(n_items, lo, hi);
+  int cur = -1;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int w = lo; w < hi; ++w) {
+    const WorkItem it = items[w];
+    if (it.sim != cur) {
+      load_params(p, all, it.sim);
+      cur = it.sim;
+    }
+    const int2 g = grid[it.sim];
+    const int bu = it.tile % g.x, bv = (it.tile / g.x) % g.y, face = it.tile / (g.x * g.y);
+    nffft_sample(p, face, bu * 32 + tx, bv * 8 + ty);
+  }
+}
+
+// NF-FF fold of `count` buffered steps: tile = (group, 256 face cells),
+// numbered cell block fastest; per simulation nb blocks per group.
+template <typename T>
+__global__ void __launch_bounds__(256) k_nffft_fold_batch(const NfParams<T> *__restrict__ all, const int *__restrict__ nb,
+                                                          const WorkItem *__restrict__ items, int n_items, int count) {
+  __shared__ NfParams<T> p;
+  int lo, hi;
+  item_range(n_items, lo, hi);
+  int cur = -1;
+  for (int w = lo; w < hi; ++w) {
+    const WorkItem it = items[w];
+    if (it.sim != cur) {
+      load_params(p, all, it.sim);
+      cur = it.sim;
+    }
+    const int n = nb[it.sim];
+    nffft_fold(p, it.tile / n, static_cast<long long>(it.tile % n) * 256 + threadIdx.x, count, 0);
+  }
+}
+
+// The 1-D incident lines: one block per listed simulation.
+__global__ void __launch_bounds__(512) k_tfsf_aux_batch(const AuxParams *__restrict__ all, const int *__restrict__ sims) {
+  __shared__ AuxParams p;
+  load_params(p, all, sims[blockIdx.x]);
+  tfsf_aux_block(p);
+}
+
+// Step counters of the listed simulations.
+__global__ void k_advance_batch(long long *const *__restrict__ steps, int n) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) *steps[q] += 1;
+}
+
+}  // namespace xg

@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -34,6 +35,7 @@
 
 #include "../../include/xfdtd_cuda.h"
 #include "common.cuh"
+#include "batch.cuh"
 #include "surface.cuh"
 #include "sweep.cuh"
 #include "volume.cuh"
@@ -559,7 +561,7 @@ xg::SparseParams<T> sparse_params(xfdtd_handle *h) {
 }
 
 template <typename T>
-void launch_nffft(xfdtd_handle *h) {
+xg::NfParams<T> nf_params(xfdtd_handle *h) {
   xg::NfParams<T> p{};
   p.d = h->d;
   for (int c = 0; c < 3; ++c) {
@@ -580,11 +582,27 @@ void launch_nffft(xfdtd_handle *h) {
   p.step = h->d_step;
   for (int g = 0; g < 3; ++g) p.buf[g] = static_cast<T *>(h->nf_buf[g]);
   p.batch = h->nf_batch;
-  int bx = h->nf_hi[0] - h->nf_lo[0], by = h->nf_hi[1] - h->nf_lo[1], bz = h->nf_hi[2] - h->nf_lo[2];
-  int u = std::max(bz, by), v = std::max(by, bx);
-  dim3 block(32, 8, 1);
-  dim3 grid((u + 31) / 32, (v + 7) / 8, 3);
-  xg::k_nffft<T><<<grid, block, 0, h->stream>>>(p);
+  return p;
+}
+
+// Launch grid of the NF-FF sampling kernel (32 x 8 blocks, one z-slice per face pair).
+dim3 nffft_grid(const xfdtd_handle *h) {
+  const int bx = h->nf_hi[0] - h->nf_lo[0], by = h->nf_hi[1] - h->nf_lo[1], bz = h->nf_hi[2] - h->nf_lo[2];
+  const int u = std::max(bz, by), v = std::max(by, bx);
+  return dim3((u + 31) / 32, (v + 7) / 8, 3);
+}
+
+// Blocks of 256 face cells per face pair for the NF-FF fold.
+long long nffft_fold_blocks(const xfdtd_handle *h) {
+  const long long bx = h->nf_hi[0] - h->nf_lo[0], by = h->nf_hi[1] - h->nf_lo[1], bz = h->nf_hi[2] - h->nf_lo[2];
+  const long long most = std::max(by * bz, std::max(bx * bz, bx * by));
+  return (most + 255) / 256;
+}
+
+template <typename T>
+void launch_nffft(xfdtd_handle *h) {
+  const auto p = nf_params<T>(h);
+  xg::k_nffft<T><<<nffft_grid(h), dim3(32, 8, 1), 0, h->stream>>>(p);
   XCHECK(cudaGetLastError());
 }
 
@@ -593,24 +611,8 @@ void launch_nffft(xfdtd_handle *h) {
 // it (the counter has advanced past it).
 template <typename T>
 void launch_nffft_accumulate(xfdtd_handle *h, int count, int lag) {
-  xg::NfParams<T> p{};
-  for (int a = 0; a < 3; ++a) {
-    p.lo[a] = h->nf_lo[a];
-    p.hi[a] = h->nf_hi[a];
-  }
-  p.nf = h->nf;
-  for (int q = 0; q < 24; ++q) p.acc[q] = h->acc[q];
-  p.pj = h->phase_j;
-  p.pm = h->phase_m;
-  p.pjf = h->phase_jf;
-  p.pmf = h->phase_mf;
-  p.total = h->total;
-  p.step = h->d_step;
-  for (int g = 0; g < 3; ++g) p.buf[g] = static_cast<T *>(h->nf_buf[g]);
-  p.batch = h->nf_batch;
-  const long long bx = h->nf_hi[0] - h->nf_lo[0], by = h->nf_hi[1] - h->nf_lo[1], bz = h->nf_hi[2] - h->nf_lo[2];
-  const long long most = std::max(by * bz, std::max(bx * bz, bx * by));
-  dim3 grid(static_cast<unsigned>((most + 255) / 256), 1, 3);
+  const auto p = nf_params<T>(h);
+  dim3 grid(static_cast<unsigned>(nffft_fold_blocks(h)), 1, 3);
   xg::k_nffft_accumulate<T><<<grid, 256, 0, h->stream>>>(p, count, lag);
   XCHECK(cudaGetLastError());
 }
@@ -651,23 +653,31 @@ xg::TfsfSurfParams<T> tfsf_surf_params(xfdtd_handle *h) {
   return p;
 }
 
+xg::AuxParams aux_params(xfdtd_handle *h) {
+  xg::AuxParams a{};
+  a.L = h->aux_len;
+  a.state = h->tf_state;
+  a.inc = h->tf_inc;
+  a.incf = h->tf_incf;
+  a.source = h->tf_src;
+  a.ceihi = h->tf_ceihi;
+  a.chiei = h->tf_chiei;
+  a.c1 = h->tf_c1;
+  a.c2 = h->tf_c2;
+  for (int q = 0; q < 3; ++q) {
+    a.te[q] = h->tf_te[q];
+    a.th[q] = h->tf_th[q];
+  }
+  a.step = h->d_step;
+  a.total = h->total;
+  a.status = h->d_status;
+  return a;
+}
+
 template <typename T, typename I>
 void enqueue_step_t(xfdtd_handle *h, long long s) {
   if (h->tfsf) {
-    xg::AuxParams a{};
-    a.L = h->aux_len;
-    a.state = h->tf_state;
-    a.inc = h->tf_inc;
-    a.incf = h->tf_incf;
-    a.source = h->tf_src;
-    a.ceihi = h->tf_ceihi;
-    a.chiei = h->tf_chiei;
-    a.c1 = h->tf_c1;
-    a.c2 = h->tf_c2;
-    for (int q = 0; q < 3; ++q) { a.te[q] = h->tf_te[q]; a.th[q] = h->tf_th[q]; }
-    a.step = h->d_step;
-    a.total = h->total;
-    a.status = h->d_status;
+    const xg::AuxParams a = aux_params(h);
     // The 1-D line of step t runs on a side stream, beside the E update: it
     // must follow the E corrections of step t-1 (which read the buffer it
     // writes) and precede the H corrections of step t (joined there).
@@ -1418,6 +1428,376 @@ void xfdtd_destroy(xfdtd_handle *h) {
     cudaStreamSynchronize(h->stream);
   }
   delete h;
+}
+
+}  // extern "C"
+
+// ================================================================ batch ===
+// Many independent handles advanced together (batch.cuh): one launch per
+// phase over the (simulation, tile) work list of every member still
+// running, the step loop replayed from a CUDA graph per set of running
+// members.  Members keep their own buffers and are read through the
+// ordinary entry points once the batch has been synchronised.
+
+struct xfdtd_batch {
+  std::string err;
+  std::vector<xfdtd_handle *> m;
+  int device = 0, precision = XFDTD_FP64, idx_bytes = 1, flags = 0;
+  int n_sm = 152;
+  cudaStream_t stream = nullptr;
+  long long clock = 0;   // steps taken (every member started at step 0)
+  long long nf_done = 0;
+  long long launches = 0;
+  std::vector<void *> allocs;
+  // per-member parameter arrays (device), built once
+  void *vol = nullptr, *tsurf = nullptr, *nfp = nullptr, *aux = nullptr;
+  int2 *nf_grid = nullptr;
+  int *nf_nb = nullptr;
+  // work lists of the running members (device, sized for all members)
+  std::vector<int> running;
+  xg::WorkItem *it_vol = nullptr, *it_te = nullptr, *it_th = nullptr, *it_nf = nullptr, *it_fold = nullptr;
+  int n_vol = 0, n_te = 0, n_th = 0, n_nf = 0, n_fold = 0;
+  int *aux_list = nullptr;
+  int n_aux = 0;
+  long long **step_list = nullptr;
+  // graph of kGraphSteps steps for the current running set
+  cudaGraphExec_t gexec = nullptr;
+  long long graph_launches = 0;
+
+  template <class P>
+  P *alloc(size_t count) {
+    void *p = nullptr;
+    XCHECK(cudaMalloc(&p, std::max<size_t>(count * sizeof(P), 16)));
+    allocs.push_back(p);
+    return static_cast<P *>(p);
+  }
+  ~xfdtd_batch() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    for (void *p : allocs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+constexpr int kBatchGraphSteps = 32;   // a multiple of the NF-FF batch
+
+template <typename T, typename I>
+void batch_setup(xfdtd_batch *b) {
+  const int n = static_cast<int>(b->m.size());
+  std::vector<xg::VolParams<T, I>> vol(n);
+  std::vector<xg::TfsfSurfParams<T>> ts(n);
+  std::vector<xg::NfParams<T>> nf(n);
+  std::vector<xg::AuxParams> ax(n);
+  std::vector<int2> grid(n);
+  std::vector<int> nb(n);
+  for (int q = 0; q < n; ++q) {
+    xfdtd_handle *h = b->m[q];
+    vol[q] = vol_params<T, I>(h);
+    if (h->tfsf) {
+      ts[q] = tfsf_surf_params<T>(h);
+      ax[q] = aux_params(h);
+    }
+    if (h->nffft) {
+      nf[q] = nf_params<T>(h);
+      const dim3 g = nffft_grid(h);
+      grid[q] = make_int2(static_cast<int>(g.x), static_cast<int>(g.y));
+      nb[q] = static_cast<int>(nffft_fold_blocks(h));
+    }
+  }
+  auto up = [&](auto &v) {
+    using E = typename std::remove_reference<decltype(v)>::type::value_type;
+    E *d = b->alloc<E>(v.size());
+    XCHECK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice, b->stream));
+    return d;
+  };
+  b->vol = up(vol);
+  b->tsurf = up(ts);
+  b->nfp = up(nf);
+  b->aux = up(ax);
+  b->nf_grid = up(grid);
+  b->nf_nb = up(nb);
+  XCHECK(cudaStreamSynchronize(b->stream));   // the host vectors go out of scope
+}
+
+// Work lists of the members that have steps left.
+void batch_lists(xfdtd_batch *b) {
+  std::vector<int> run;
+  for (int q = 0; q < static_cast<int>(b->m.size()); ++q)
+    if (b->m[q]->host_step < b->m[q]->total) run.push_back(q);
+  if (run == b->running && b->it_vol) return;
+  b->running = run;
+  if (b->gexec) {
+    cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+  }
+  std::vector<xg::WorkItem> vol, te, th, nf, fold;
+  std::vector<int> aux;
+  std::vector<long long *> steps;
+  for (int q : run) {
+    xfdtd_handle *h = b->m[q];
+    const int gx = (h->d.nz + 32) / 32, gy = (h->d.ny + 8) / 8;
+    for (int i = 0; i <= h->d.nx; ++i)   // packed tiles: i << 16 | j-block << 8 | k-block
+      for (int by = 0; by < gy; ++by)
+        for (int bx = 0; bx < gx; ++bx) vol.push_back({q, (i << 16) | (by << 8) | bx});
+    if (h->tfsf) {
+      aux.push_back(q);
+      const long long ne = xg::surface_count(h->tf_lo[0], h->tf_hi[0], h->tf_lo[1], h->tf_hi[1], h->tf_lo[2], h->tf_hi[2]);
+      const long long nh = xg::surface_count(h->tf_lo[0] - 1, h->tf_hi[0], h->tf_lo[1] - 1, h->tf_hi[1],
+                                             h->tf_lo[2] - 1, h->tf_hi[2]);
+      for (long long t = 0; t < (ne + 255) / 256; ++t) te.push_back({q, static_cast<int>(t)});
+      for (long long t = 0; t < (nh + 255) / 256; ++t) th.push_back({q, static_cast<int>(t)});
+    }
+    if (h->nffft) {
+      const dim3 g = nffft_grid(h);
+      for (long long t = 0; t < static_cast<long long>(g.x) * g.y * 3; ++t) nf.push_back({q, static_cast<int>(t)});
+      for (long long t = 0; t < 3 * nffft_fold_blocks(h); ++t) fold.push_back({q, static_cast<int>(t)});
+    }
+    steps.push_back(h->d_step);
+  }
+  auto put = [&](auto &v, auto *&dst) {
+    using E = typename std::remove_reference<decltype(v)>::type::value_type;
+    if (!dst) {   // sized once, for the first (largest) running set
+      dst = b->alloc<E>(std::max<size_t>(v.size(), 1));
+    }
+    if (!v.empty()) XCHECK(cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice, b->stream));
+    return static_cast<int>(v.size());
+  };
+  b->n_vol = put(vol, b->it_vol);
+  b->n_te = put(te, b->it_te);
+  b->n_th = put(th, b->it_th);
+  b->n_nf = put(nf, b->it_nf);
+  b->n_fold = put(fold, b->it_fold);
+  b->n_aux = put(aux, b->aux_list);
+  put(steps, b->step_list);
+  XCHECK(cudaStreamSynchronize(b->stream));
+}
+
+unsigned persistent_grid(const xfdtd_batch *b, int items, int per_sm) {
+  return static_cast<unsigned>(std::max(1, std::min(items, b->n_sm * per_sm)));
+}
+
+template <typename T, typename I>
+void batch_enqueue_t(xfdtd_batch *b, long long s) {
+  cudaStream_t st = b->stream;
+  int launched = 0;
+  if (b->n_aux) {
+    xg::k_tfsf_aux_batch<<<b->n_aux, 512, 0, st>>>(static_cast<const xg::AuxParams *>(b->aux), b->aux_list);
+    ++launched;
+  }
+  const auto *vp = static_cast<const xg::VolParams<T, I> *>(b->vol);
+  xg::k_volume_batch<T, I, true><<<b->n_vol, 256, 0, st>>>(vp, b->it_vol);
+  ++launched;
+  const auto *tp = static_cast<const xg::TfsfSurfParams<T> *>(b->tsurf);
+  if (b->n_te) {
+    xg::k_tfsf_batch<T, true><<<persistent_grid(b, b->n_te, 8), 256, 0, st>>>(tp, b->it_te, b->n_te);
+    ++launched;
+  }
+  xg::k_volume_batch<T, I, false><<<b->n_vol, 256, 0, st>>>(vp, b->it_vol);
+  ++launched;
+  if (b->n_th) {
+    xg::k_tfsf_batch<T, false><<<persistent_grid(b, b->n_th, 8), 256, 0, st>>>(tp, b->it_th, b->n_th);
+    ++launched;
+  }
+  const auto *np = static_cast<const xg::NfParams<T> *>(b->nfp);
+  if (b->n_nf) {
+    xg::k_nffft_batch<T><<<persistent_grid(b, b->n_nf, 8), 256, 0, st>>>(np, b->nf_grid, b->it_nf, b->n_nf);
+    ++launched;
+    if ((s + 1) % xg::kMaxNfBatch == 0) {
+      xg::k_nffft_fold_batch<T><<<persistent_grid(b, b->n_fold, 8), 256, 0, st>>>(
+          np, b->nf_nb, b->it_fold, b->n_fold, static_cast<int>(s + 1 - b->nf_done));
+      ++launched;
+      b->nf_done = s + 1;
+    }
+  }
+  const int nr = static_cast<int>(b->running.size());
+  xg::k_advance_batch<<<(nr + 127) / 128, 128, 0, st>>>(b->step_list, nr);
+  ++launched;
+  XCHECK(cudaGetLastError());
+  b->launches += launched;
+}
+
+void batch_enqueue(xfdtd_batch *b, long long s) {
+  if (b->precision == XFDTD_FP64) {
+    if (b->idx_bytes == 1) batch_enqueue_t<double, uint8_t>(b, s);
+    else batch_enqueue_t<double, uint16_t>(b, s);
+  } else {
+    if (b->idx_bytes == 1) batch_enqueue_t<float, uint8_t>(b, s);
+    else batch_enqueue_t<float, uint16_t>(b, s);
+  }
+}
+
+// Host bookkeeping of the running members after `k` batch steps.
+void batch_advance_members(xfdtd_batch *b, long long k) {
+  b->clock += k;
+  for (int q : b->running) {
+    xfdtd_handle *h = b->m[q];
+    h->host_step += k;
+    if (h->nffft) h->nf_done = b->nf_done;
+  }
+}
+
+void batch_steps(xfdtd_batch *b, long long n) {
+  if (n < 0) invalid("negative step count");
+  const bool graph = (b->flags & XFDTD_FLAG_GRAPH) != 0;
+  while (n > 0) {
+    batch_lists(b);
+    if (b->running.empty()) return;
+    long long seg = n;   // up to the next member that finishes
+    for (int q : b->running) seg = std::min(seg, b->m[q]->total - b->m[q]->host_step);
+    const long long end = b->clock + seg;
+    while (b->clock < end) {
+      if (graph && b->clock % kBatchGraphSteps == 0 && end - b->clock >= kBatchGraphSteps) {
+        if (!b->gexec) {
+          cudaGraph_t g;
+          const long long nf_done = b->nf_done, launches = b->launches;
+          XCHECK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+          for (int s = 0; s < kBatchGraphSteps; ++s) batch_enqueue(b, b->clock + s);
+          XCHECK(cudaStreamEndCapture(b->stream, &g));
+          b->graph_launches = b->launches - launches;
+          b->launches = launches;
+          b->nf_done = nf_done;
+          const cudaError_t e = cudaGraphInstantiate(&b->gexec, g, 0);
+          cudaGraphDestroy(g);
+          XCHECK(e);
+        }
+        XCHECK(cudaGraphLaunch(b->gexec, b->stream));
+        b->launches += b->graph_launches;
+        b->nf_done = b->clock + kBatchGraphSteps;
+        batch_advance_members(b, kBatchGraphSteps);
+        continue;
+      }
+      batch_enqueue(b, b->clock);
+      batch_advance_members(b, 1);
+    }
+    n -= seg;
+  }
+}
+
+int batch_guarded(xfdtd_batch *b, const std::function<void()> &fn) {
+  try {
+    XCHECK(cudaSetDevice(b->device));
+    fn();
+    return XFDTD_OK;
+  } catch (const Err &e) {
+    b->err = e.msg;
+    return e.code;
+  } catch (const std::exception &e) {
+    b->err = e.what();
+    return XFDTD_ERR_INVALID_PLAN;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int xfdtd_batch_create(xfdtd_handle *const *members, int n, int flags, xfdtd_batch **out) {
+  if (!out) return XFDTD_ERR_INVALID_PLAN;
+  std::unique_ptr<xfdtd_batch> b(new xfdtd_batch());
+  b->flags = flags;
+  const int rc = [&]() -> int {
+    try {
+      if (!members || n < 1) invalid("a batch needs at least one member");
+      for (int q = 0; q < n; ++q) {
+        xfdtd_handle *h = members[q];
+        if (!h || !h->stream) invalid("batch member " + std::to_string(q) + " is not a created handle");
+        if (q == 0) {
+          b->device = h->device;
+          b->precision = h->precision;
+          b->idx_bytes = h->idx_bytes;
+        }
+        if (h->device != b->device || h->precision != b->precision || h->idx_bytes != b->idx_bytes)
+          invalid("batch members must share device, precision and material-index width");
+        if (h->host_step != 0) invalid("batch members must not have been stepped");
+        if (h->n_inj || h->n_ind || h->n_probes) invalid("batch members may not have lumped elements or monitors");
+        if (h->d.nx >= 65535 || h->d.ny >= 2040 || h->d.nz >= 8160) invalid("batch member grid too large for the tile numbering");
+        for (int r = 0; r < q; ++r)
+          if (members[r] == h) invalid("a handle appears twice in the batch");
+      }
+      XCHECK(cudaSetDevice(b->device));
+      int sms = 0;
+      XCHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+      b->n_sm = sms;
+      XCHECK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+      for (int q = 0; q < n; ++q) {
+        xfdtd_handle *h = members[q];
+        XCHECK(cudaStreamSynchronize(h->stream));
+        if (h->gexec) {   // its own graph will not run again
+          cudaGraphExecDestroy(h->gexec);
+          h->gexec = nullptr;
+        }
+        h->sweep = false;   // the batch runs the split kernels on the handle's current buffers
+        b->m.push_back(h);
+      }
+      if (b->precision == XFDTD_FP64) {
+        if (b->idx_bytes == 1) batch_setup<double, uint8_t>(b.get());
+        else batch_setup<double, uint16_t>(b.get());
+      } else {
+        if (b->idx_bytes == 1) batch_setup<float, uint8_t>(b.get());
+        else batch_setup<float, uint16_t>(b.get());
+      }
+      return XFDTD_OK;
+    } catch (const Err &e) {
+      b->err = e.msg;
+      return e.code;
+    }
+  }();
+  *out = b.release();
+  return rc;
+}
+
+int xfdtd_batch_step(xfdtd_batch *b, int64_t n) {
+  if (!b) return XFDTD_ERR_STATE;
+  return batch_guarded(b, [&] { batch_steps(b, n); });
+}
+
+int xfdtd_batch_step_timed(xfdtd_batch *b, int64_t n, double *ms) {
+  if (!b) return XFDTD_ERR_STATE;
+  return batch_guarded(b, [&] {
+    batch_lists(b);   // list uploads stay outside the timed region
+    cudaEvent_t e0, e1;
+    XCHECK(cudaEventCreate(&e0));
+    XCHECK(cudaEventCreate(&e1));
+    XCHECK(cudaEventRecord(e0, b->stream));
+    batch_steps(b, n);
+    XCHECK(cudaEventRecord(e1, b->stream));
+    XCHECK(cudaEventSynchronize(e1));
+    float f = 0;
+    XCHECK(cudaEventElapsedTime(&f, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms) *ms = f;
+  });
+}
+
+int xfdtd_batch_synchronize(xfdtd_batch *b) {
+  if (!b) return XFDTD_ERR_STATE;
+  return batch_guarded(b, [&] {
+    XCHECK(cudaStreamSynchronize(b->stream));
+    for (xfdtd_handle *h : b->m) check_status(h);
+  });
+}
+
+int xfdtd_batch_status(xfdtd_batch *b, int *n_running, int64_t *clock, int64_t *launches) {
+  if (!b) return XFDTD_ERR_STATE;
+  int r = 0;
+  for (xfdtd_handle *h : b->m) r += h->host_step < h->total ? 1 : 0;
+  if (n_running) *n_running = r;
+  if (clock) *clock = b->clock;
+  if (launches) *launches = b->launches;
+  return XFDTD_OK;
+}
+
+const char *xfdtd_batch_last_error(xfdtd_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+void xfdtd_batch_destroy(xfdtd_batch *b) {
+  if (!b) return;
+  if (b->stream) {
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+  }
+  delete b;
 }
 
 }  // extern "C"

@@ -25,7 +25,8 @@ struct AuxParams {
   int *status;
 };
 
-__global__ void k_tfsf_aux(AuxParams p) {
+// Body of the 1-D line update for one block (all of its threads).
+__device__ __forceinline__ void tfsf_aux_block(const AuxParams &p) {
   const long long t = *p.step;
   if (t >= p.total) {
     if (threadIdx.x == 0) atomicExch(p.status, 6);
@@ -72,6 +73,8 @@ __global__ void k_tfsf_aux(AuxParams p) {
   }
 }
 
+__global__ void k_tfsf_aux(AuxParams p) { tfsf_aux_block(p); }
+
 // ------------------------------------------------------------------------
 // NffftFd::update (src/nffft/nffft_fd.cpp:108-203) with the face-centre
 // interpolations of EMF (src/electromagnetic_field/linear_interpolation_emf.cpp:286-421).
@@ -95,8 +98,9 @@ struct NfParams {
   int batch;
 };
 
+// Samples face pair `face` at face coordinates (u, v) (u the fastest axis).
 template <typename T>
-__global__ void k_nffft(NfParams<T> p) {
+__device__ __forceinline__ void nffft_sample(const NfParams<T> &p, int face, int u, int v) {
   const long long t = *p.step;
   if (t >= p.total) return;
   const int li = p.lo[0], lj = p.lo[1], lk = p.lo[2], ri = p.hi[0], rj = p.hi[1], rk = p.hi[2];
@@ -108,9 +112,6 @@ __global__ void k_nffft(NfParams<T> p) {
     return f[static_cast<long long>(i) * si + static_cast<long long>(j) * sj + k];
   };
   const T half = T(0.5), quarter = T(0.25), neg = T(-1);
-  const int face = blockIdx.z;
-  const int u = blockIdx.x * blockDim.x + threadIdx.x;   // fastest face axis
-  const int v = blockIdx.y * blockDim.y + threadIdx.y;
   T val[8];
   long long cell, plane;
   int base;
@@ -165,6 +166,11 @@ __global__ void k_nffft(NfParams<T> p) {
   for (int q = 0; q < 8; ++q) buf[q * plane] = val[q];
 }
 
+template <typename T>
+__global__ void k_nffft(NfParams<T> p) {
+  nffft_sample(p, blockIdx.z, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
+
 // acc[n] += v[s] * phase[n][t0 + s] for the `count` (<= 8) buffered steps
 // ending at step *step - lag.  FP64 form: added one step at a time in step
 // order, the same additions in the same order as accumulating every step
@@ -174,12 +180,10 @@ __global__ void k_nffft(NfParams<T> p) {
 constexpr int kMaxNfBatch = 8;
 
 template <typename T>
-__global__ void k_nffft_accumulate(NfParams<T> p, int count, int lag) {
-  const int group = blockIdx.z;
+__device__ __forceinline__ void nffft_fold(const NfParams<T> &p, int group, long long cell, int count, int lag) {
   const int lo_a = group == 0 ? p.lo[1] : p.lo[0], hi_a = group == 0 ? p.hi[1] : p.hi[0];
   const int lo_b = group == 2 ? p.lo[1] : p.lo[2], hi_b = group == 2 ? p.hi[1] : p.hi[2];
   const long long plane = static_cast<long long>(hi_a - lo_a) * (hi_b - lo_b);
-  const long long cell = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
   if (cell >= plane) return;
   const long long t_last = *p.step - lag;
   const long long t0 = t_last - count + 1;
@@ -219,6 +223,11 @@ __global__ void k_nffft_accumulate(NfParams<T> p, int count, int lag) {
       *a = r;
     }
   }
+}
+
+template <typename T>
+__global__ void k_nffft_accumulate(NfParams<T> p, int count, int lag) {
+  nffft_fold(p, blockIdx.z, blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x, count, lag);
 }
 
 // ------------------------------------------------------------------------
@@ -493,11 +502,11 @@ __device__ __forceinline__ void tfsf_e_component(const TfsfSurfParams<T> &p, con
   p.F[C][b] = e;
 }
 
+// TFSF E corrections of surface cell q (surface_cell order).
 template <typename T>
-__global__ void k_tfsf_e(TfsfSurfParams<T> p) {
+__device__ __forceinline__ void tfsf_e_surface(const TfsfSurfParams<T> &p, int q) {
   const TfsfDev &tf = p.tf;
   int i, j, k;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (!surface_cell(q, tf.lo[0], tf.hi[0], tf.lo[1], tf.hi[1], tf.lo[2], tf.hi[2], i, j, k)) return;
   const auto hinc = tfsf_view<T>(tf).inc + (((*p.step) + 1) & 1) * 6 * tf.L;   // incident H of the previous step
   const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
@@ -507,11 +516,17 @@ __global__ void k_tfsf_e(TfsfSurfParams<T> p) {
 }
 
 template <typename T>
-__global__ void k_tfsf_h(TfsfSurfParams<T> p) {
+__global__ void k_tfsf_e(TfsfSurfParams<T> p) {
+  tfsf_e_surface(p, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// TFSF3D::updateH (src/tfsf/tfsf_3d.cpp:185-297) at surface cell q of the
+// box one cell larger on the low sides.
+template <typename T>
+__device__ __forceinline__ void tfsf_h_surface(const TfsfSurfParams<T> &p, int q) {
   const TfsfDev &tf = p.tf;
   const int li = tf.lo[0], ri = tf.hi[0], lj = tf.lo[1], rj = tf.hi[1], lk = tf.lo[2], rk = tf.hi[2];
   int i, j, k;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (!surface_cell(q, li - 1, ri, lj - 1, rj, lk - 1, rk, i, j, k)) return;
   const auto V = tfsf_view<T>(tf);
   using R = typename std::remove_const<typename std::remove_pointer<decltype(V.inc)>::type>::type;
@@ -583,6 +598,11 @@ __global__ void k_tfsf_h(TfsfSurfParams<T> p) {
       p.F[5][b] = h;
     }
   }
+}
+
+template <typename T>
+__global__ void k_tfsf_h(TfsfSurfParams<T> p) {
+  tfsf_h_surface(p, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Number of cells on the surface of [a0,a1]x[b0,b1]x[c0,c1] (surface_cell's range).
