@@ -229,6 +229,34 @@ void xfdtd_destroy(xfdtd_handle *h);
 const char *xfdtd_version(void);
 
 /* ---------------------------------------------------------------------
+ * Adjoint gradients.  No counterpart in the reference, which has no
+ * differentiation: the gradient of the loss
+ *   L = sum over steps t in [t_begin, t_end) and over a plane of F(t+1)^2
+ * (F = Ex, Ey or Ez after step t) with respect to eps_r and sigma of every
+ * cell of a design box, by the discrete adjoint (transpose) of the split
+ * E/H update including CPML.  Lumped sources and TFSF injection are
+ * affine and do not enter the adjoint; inductors are not supported.  The
+ * design box and its one-cell rim must lie outside the CPML.
+ * xfdtd_adjoint_forward runs all total_steps from step 0 (the handle must
+ * not have been stepped), checkpointing the state every checkpoint_every
+ * steps (0: record the design box at every step instead) and returns L.
+ * xfdtd_adjoint_backward then returns dL/d eps_r and dL/d sigma per design
+ * cell, [i][j][k] over the box (re-running each checkpoint segment once). */
+typedef struct xfdtd_adjoint_desc {
+  int64_t design_lo[3], design_hi[3];   /* cells [lo, hi) per axis                    */
+  int32_t loss_comp;                    /* 0 Ex, 1 Ey, 2 Ez                            */
+  int32_t plane_axis;                   /* axis normal to the loss plane               */
+  int64_t plane_index;                  /* its index on that axis                      */
+  int64_t plane_lo[2], plane_hi[2];     /* extents on the other two axes, in axis order */
+  int64_t t_begin, t_end;               /* loss window (steps)                         */
+  int32_t checkpoint_every;             /* K                                           */
+  int32_t reserved;
+} xfdtd_adjoint_desc;
+
+int xfdtd_adjoint_forward(xfdtd_handle *h, const xfdtd_adjoint_desc *d, double *loss);
+int xfdtd_adjoint_backward(xfdtd_handle *h, double *grad_eps, double *grad_sigma, int64_t len);
+
+/* ---------------------------------------------------------------------
  * Batches: many independent simulations of different sizes advanced
  * together.  The reference runs one Simulation at a time
  * (simulation_update.cpp:5-40); a batch runs each phase of the loop body

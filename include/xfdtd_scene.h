@@ -173,8 +173,10 @@ typedef struct xfdtd_scene_desc {
    * fastest) into voxel_materials, applied after all objects.  The grid
    * size it must match is the one the objects and PML layers produce.    */
   const xfdtd_material_desc *voxel_materials;
-  const uint16_t *voxel_index;
+  const void *voxel_index;      /* uint16_t, or uint32_t when voxel_index_bytes = 4 */
   int64_t voxel_shape[3];
+  int32_t voxel_index_bytes;    /* 2 (or 0, meaning 2) or 4                      */
+  int32_t reserved3;
 } xfdtd_scene_desc;
 
 #ifdef __cplusplus

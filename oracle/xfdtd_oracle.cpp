@@ -316,7 +316,7 @@ struct oracle_sim {
   bool has_tfsf = false, has_nffft = false;
   xfdtd_tfsf_desc tfsf_d{};
   std::vector<xfdtd_material_desc> voxel_mats;
-  std::vector<uint16_t> voxel_idx;
+  std::vector<uint32_t> voxel_idx;
   int64_t voxel_shape[3] = {0, 0, 0};
 
   std::unique_ptr<GridSpace> gs;
@@ -1432,10 +1432,16 @@ int oracle_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, oracle_si
     if (sc->voxel_index) {
       s->voxel_mats.assign(sc->voxel_materials, sc->voxel_materials + sc->n_voxel_materials);
       size_t cnt = static_cast<size_t>(sc->voxel_shape[0] * sc->voxel_shape[1] * sc->voxel_shape[2]);
-      s->voxel_idx.assign(sc->voxel_index, sc->voxel_index + cnt);
+      if (sc->voxel_index_bytes == 4) {
+        const uint32_t *v = static_cast<const uint32_t *>(sc->voxel_index);
+        s->voxel_idx.assign(v, v + cnt);
+      } else {
+        const uint16_t *v = static_cast<const uint16_t *>(sc->voxel_index);
+        s->voxel_idx.assign(v, v + cnt);
+      }
       for (int a = 0; a < 3; ++a) s->voxel_shape[a] = sc->voxel_shape[a];
-      for (uint16_t v : s->voxel_idx)
-        if (v >= sc->n_voxel_materials) throw std::invalid_argument("voxel index out of range");
+      for (uint32_t v : s->voxel_idx)
+        if (v >= static_cast<uint32_t>(sc->n_voxel_materials)) throw std::invalid_argument("voxel index out of range");
     }
     s->init();
     *out = s.release();

@@ -88,6 +88,8 @@ def libs():
         cu.xfdtd_last_error.argtypes = [C.c_void_p]
         cu.xfdtd_last_error.restype = C.c_char_p
         cu.xfdtd_version.restype = C.c_char_p
+        cu.xfdtd_adjoint_forward.argtypes = [C.c_void_p, P(AdjointDesc), dp]
+        cu.xfdtd_adjoint_backward.argtypes = [C.c_void_p, dp, dp, C.c_int64]
         cu.xfdtd_batch_create.argtypes = [P(C.c_void_p), C.c_int, C.c_int, P(C.c_void_p)]
         cu.xfdtd_batch_step.argtypes = [C.c_void_p, C.c_int64]
         cu.xfdtd_batch_step_timed.argtypes = [C.c_void_p, C.c_int64, dp]
@@ -98,6 +100,15 @@ def libs():
         cu.xfdtd_batch_destroy.argtypes = [C.c_void_p]
         _cuda, _host = cu, ho
     return _cuda, _host
+
+
+class AdjointDesc(C.Structure):
+    """ctypes mirror of xfdtd_adjoint_desc (include/xfdtd_cuda.h)."""
+    _fields_ = [("design_lo", C.c_int64 * 3), ("design_hi", C.c_int64 * 3),
+                ("loss_comp", C.c_int32), ("plane_axis", C.c_int32), ("plane_index", C.c_int64),
+                ("plane_lo", C.c_int64 * 2), ("plane_hi", C.c_int64 * 2),
+                ("t_begin", C.c_int64), ("t_end", C.c_int64),
+                ("checkpoint_every", C.c_int32), ("reserved", C.c_int32)]
 
 
 def _dp(a: np.ndarray):
@@ -250,6 +261,36 @@ class Simulation:
         n = C.c_int()
         self._check_engine(libs()[0].xfdtd_launches_per_step(self.engine, C.byref(n)))
         return n.value
+
+    def adjoint_forward(self, design_lo, design_hi, plane_axis: int, plane_index: int, plane_lo, plane_hi,
+                        t_begin: int, t_end: int, loss_comp: int = 2, checkpoint_every: int = 100) -> float:
+        """Runs every step from step 0 for an adjoint gradient (the forward
+        half of the forward/backward pair) and returns the loss: the sum,
+        over the steps t_begin .. t_end-1 and the plane plane_axis =
+        plane_index (extents plane_lo .. plane_hi on the other two axes), of
+        the squared field component loss_comp (0 Ex, 1 Ey, 2 Ez) after each
+        step.  Cell indices are grid indices (CPML included).  The state is
+        checkpointed every checkpoint_every steps (0: the design box
+        [design_lo, design_hi) is recorded at every step instead)."""
+        d = AdjointDesc()
+        d.design_lo[:] = [int(v) for v in design_lo]
+        d.design_hi[:] = [int(v) for v in design_hi]
+        d.loss_comp, d.plane_axis, d.plane_index = int(loss_comp), int(plane_axis), int(plane_index)
+        d.plane_lo[:] = [int(v) for v in plane_lo]
+        d.plane_hi[:] = [int(v) for v in plane_hi]
+        d.t_begin, d.t_end, d.checkpoint_every = int(t_begin), int(t_end), int(checkpoint_every)
+        self._adj_shape = tuple(int(b) - int(a) for a, b in zip(design_lo, design_hi))
+        loss = C.c_double()
+        self._check_engine(libs()[0].xfdtd_adjoint_forward(self.engine, C.byref(d), C.byref(loss)))
+        return loss.value
+
+    def adjoint_backward(self):
+        """dL/d eps_r and dL/d sigma of every design cell (arrays over the
+        design box), by the discrete adjoint of the step loop."""
+        ge = np.empty(self._adj_shape, dtype=np.float64)
+        gs = np.empty(self._adj_shape, dtype=np.float64)
+        self._check_engine(libs()[0].xfdtd_adjoint_backward(self.engine, _dp(ge), _dp(gs), ge.size))
+        return ge, gs
 
     def kernel_variants(self) -> dict:
         """Volume-kernel variant in use for E and H and the autotuner's trial

@@ -147,6 +147,44 @@ def batched_scatterers(n: int = 64, scale: int = 1, seed0: int = 4000, n_theta: 
     return out
 
 
+def adjoint_dipole(scale: int = 1, steps: int = 2000, seed: int = 5001):
+    """Adjoint-gradient problem: 160 x 160 x 96 interior + 10-cell CPML,
+    dx = 50 nm, a z-directed soft point current source (Gaussian-modulated
+    sine, f0 = c0 / (12 dx), bandwidth f0 / 2) 20 cells below a 64 x 64 x 32
+    design region whose eps_r is 2.5 + U[-0.5, 0.5] clamped to [1, 4]
+    (seed 5001), loss plane 20 cells above it.  `scale` divides every
+    length in cells and the step count.  Returns (Scene, total_steps, spec)
+    with spec = the design box, loss plane and window in grid indices."""
+    dl = 50e-9
+    cpml = 10
+    interior = (160 // scale, 160 // scale, 96 // scale)
+    dsz = (64 // scale, 64 // scale, 32 // scale)
+    gap = 20 // scale
+    steps = steps // scale
+    n = tuple(v + 2 * cpml for v in interior)
+    lo = (cpml + (interior[0] - dsz[0]) // 2, cpml + (interior[1] - dsz[1]) // 2, cpml + (interior[2] - dsz[2]) // 2)
+    hi = tuple(a + b for a, b in zip(lo, dsz))
+    rng = np.random.default_rng(seed)
+    eps = np.clip(2.5 + rng.uniform(-0.5, 0.5, size=dsz), 1.0, 4.0).astype(np.float32)
+    mats = [S.Material("air", 1.0, 1.0, 0.0, 0.0)] + [S.Material("d", float(e), 1.0, 0.0, 0.0) for e in eps.ravel()]
+    voxel = np.zeros(n, dtype=np.uint32)
+    voxel[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]] = (1 + np.arange(eps.size, dtype=np.uint32)).reshape(dsz)
+    objects = [S.Object("domain", S.Cube([0.0, 0.0, 0.0], [v * dl for v in interior]), S.Material("air", 1, 1, 0, 0))]
+    f0 = S.C_0 / (12 * dl)
+    tau = 2.0 / (math.pi * 0.5 * f0)
+    t0 = 4.5 * tau
+    src_cell = ((lo[0] + hi[0]) // 2 - cpml, (lo[1] + hi[1]) // 2 - cpml, lo[2] - gap - cpml)
+    src = S.CurrentSource(S.Cube([c * dl for c in src_cell], [dl, dl, dl]), S.ZP, 1e30,
+                          S.CustomWaveform(1.0, S.gaussian_modulated_sine(f0, tau, t0)))
+    sc = S.Scene(dl, objects, _six_pml(cpml), lumped_elements=[src], cfl=0.98,
+                 voxel_materials=mats, voxel_index=voxel)
+    spec = {"design_lo": lo, "design_hi": hi, "plane_axis": 2, "plane_index": hi[2] + gap,
+            "plane_lo": (lo[0], lo[1]), "plane_hi": (hi[0], hi[1]),
+            "t_begin": steps - steps // 5, "t_end": steps, "loss_comp": 2,
+            "checkpoint_every": 100 // scale, "eps": eps}
+    return sc, steps, spec
+
+
 CONFIGS = {
     "pec_sphere_rcs": pec_sphere_rcs,
     "dielectric_sphere": dielectric_sphere,

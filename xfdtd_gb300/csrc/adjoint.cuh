@@ -1,0 +1,392 @@
+// adjoint.cuh -- reverse-time (discrete adjoint) kernels of the split E/H
+// update, for gradients of a field loss with respect to per-cell eps_r and
+// sigma.
+//
+// One forward step t maps (E, H, psiE, psiH) to (E', H', psiE', psiH'):
+//   E' = c0 E + ca dH_a + cb dH_b  (+ (c dl) psiE',  psiE' = b psiE + a dH)
+//   H' = c0 H + ca dE'_a + cb dE'_b (+ (c dl) psiH', psiH' = b psiH + a dE')
+// with the masks and CPML terms of e_general / h_general (volume.cuh).  Its
+// transpose, applied to the adjoint state (lE, lH, mE, mH) of step t+1,
+// gives that of step t.  Writing W for the adjoint weight an E cell puts on
+// one of its H differences,
+//   W = [main] ca L + [slab] a (mE + c dl L),      L = lE' of that cell,
+// and U for the weight an H cell puts on one of its E differences (same
+// form with lH', mH'), the transpose is
+//   lE' += loss gradient + sum of the U of the H cells that read the cell
+//   lH  =  [main] c0 lH' + sum of the W of the E cells that read the cell
+//   mH  =  b (mH' + c dl lH')
+//   lE  =  [main] c0 lE'                mE = b (mE' + c dl lE')
+// and the parameter gradient gathers lE' dE'/dp with the forward state of
+// step t.  The sources (lumped injections, TFSF corrections) are affine and
+// drop out.  Two kernels per step, each a gather over neighbours with the
+// forward's own index ranges:
+//   k_adj_h(t):  lH(t) and mH(t) from lH', mH' and the W of lE'(t), mE'(t);
+//   k_adj_e(t):  lE(t), mE(t), the gradient of step t, then (for the step
+//                before) the loss gradient of step t-1 and the U of lH(t).
+#pragma once
+
+#include "common.cuh"
+#include "volume.cuh"
+
+namespace xg {
+
+template <typename T, typename I>
+struct AdjParams {
+  VolParams<T, I> v;          // geometry, coefficient table, CPML profiles, flags
+  T *lE[3], *lH[3];           // adjoint fields, padded layout
+  Psi<T> m;                   // adjoint psi, layout of the forward psi
+  // parameter gradient over the design box [lo, hi)
+  int dlo[3], dhi[3];
+  double *g_eps, *g_sig;      // [di][dj][dk]
+  const double *dtab;         // per table entry: dc0/deps, dc0/dsig, dc/deps / c, dc/dsig / c
+  const T *recE[3];           // E(t) over the design box
+  const T *recH[3];           // H(t) over the design box grown by one cell on the low sides
+  // loss: sum over a plane of F(comp)^2 after the steps of a window
+  int loss_comp, plane_axis, plane_index;
+  int plo[2], phi[2];         // ranges on the two other axes (in axis order)
+  const T *plane_rec;         // the loss component over the plane after step t-1 (or null)
+  int do_e_own;               // k_adj_e: the own-cell transpose and gradient of step t
+  int do_gather;              // k_adj_e: the loss and U gather of step t-1
+};
+
+// ---- weights of one E cell on its H differences ------------------------
+// which: 0 = Ex on dHy/dz, 1 = Ex on dHz/dy, 2 = Ey on dHx/dz, 3 = Ey on
+// dHz/dx, 4 = Ez on dHx/dy, 5 = Ez on dHy/dx.  Zero outside the component.
+template <typename T, typename I>
+__device__ __forceinline__ T e_weight(const AdjParams<T, I> &a, int i, int j, int k, int which) {
+  const VolParams<T, I> &p = a.v;
+  const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
+  if (i < 0 || j < 0 || k < 0 || i > nx || j > ny || k > nz) return T(0);
+  const int comp = which >> 1;
+  if ((comp == 0 && i >= nx) || (comp == 1 && j >= ny) || (comp == 2 && k >= nz)) return T(0);
+  const unsigned b = static_cast<unsigned>(i) * static_cast<unsigned>(p.d.si) +
+                     static_cast<unsigned>(j) * static_cast<unsigned>(p.d.sj) + static_cast<unsigned>(k);
+  const T L = a.lE[comp][b];
+  const T *c = p.table + static_cast<unsigned>(__ldg(p.idx + b)) * 18;
+  const int xs = p.cp[0].n_layers ? p.cp[0].slot_e[i] : -1;
+  const int ys = p.cp[1].n_layers ? p.cp[1].slot_e[j] : -1;
+  const int zs = p.cp[2].n_layers ? p.cp[2].slot_e[k] : -1;
+  const bool in_i = i >= 1 && i < nx, in_j = j >= 1 && j < ny, in_k = k >= 1 && k < nz;
+  const int Ly = p.cp[1].n_layers, Lz = p.cp[2].n_layers;
+  const unsigned nzp = static_cast<unsigned>(p.d.nzp), ny1 = static_cast<unsigned>(ny + 1);
+  T w = T(0);
+  switch (which) {
+    case 0:   // Ex, (Hy(k) - Hy(k-1)): main ca = cexhy (x 1/kappa_z), psi_ex_z
+      if (in_j && in_k) w = mul(zs >= 0 ? mul(c[1], p.cp[2].rk_e[k]) : c[1], L);
+      if (zs >= 0) {
+        const unsigned o = (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
+        w = fmad(p.cp[2].a_e[k], fmad(mul(c[1], p.dl[2]), L, a.m.ex_z[o]), w);
+      }
+      break;
+    case 1:   // Ex, (Hz(j) - Hz(j-1)): main cb = cexhz (x 1/kappa_y), psi_ex_y
+      if (in_j && in_k) w = mul(ys >= 0 ? mul(c[2], p.cp[1].rk_e[j]) : c[2], L);
+      if (ys >= 0) {
+        const unsigned o = (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
+        w = fmad(p.cp[1].a_e[j], fmad(mul(c[2], p.dl[1]), L, a.m.ex_y[o]), w);
+      }
+      break;
+    case 2:   // Ey, (Hx(k) - Hx(k-1)): main ca = ceyhx (x 1/kappa_z), psi_ey_z
+      if (in_i && in_k) w = mul(zs >= 0 ? mul(c[5], p.cp[2].rk_e[k]) : c[5], L);
+      if (zs >= 0) {
+        const unsigned o = (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
+        w = fmad(p.cp[2].a_e[k], fmad(mul(c[5], p.dl[2]), L, a.m.ey_z[o]), w);
+      }
+      break;
+    case 3:   // Ey, (Hz(i) - Hz(i-1)): main cb = ceyhz (x 1/kappa_x), psi_ey_x
+      if (in_i && in_k) w = mul(xs >= 0 ? mul(c[4], p.cp[0].rk_e[i]) : c[4], L);
+      if (xs >= 0) {
+        const unsigned o = (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
+        w = fmad(p.cp[0].a_e[i], fmad(mul(c[4], p.dl[0]), L, a.m.ey_x[o]), w);
+      }
+      break;
+    case 4:   // Ez, (Hx(j) - Hx(j-1)): main ca = cezhx (x 1/kappa_y), psi_ez_y
+      if (in_i && in_j) w = mul(ys >= 0 ? mul(c[7], p.cp[1].rk_e[j]) : c[7], L);
+      if (ys >= 0) {
+        const unsigned o = (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
+        w = fmad(p.cp[1].a_e[j], fmad(mul(c[7], p.dl[1]), L, a.m.ez_y[o]), w);
+      }
+      break;
+    default:   // Ez, (Hy(i) - Hy(i-1)): main cb = cezhy (x 1/kappa_x), psi_ez_x
+      if (in_i && in_j) w = mul(xs >= 0 ? mul(c[8], p.cp[0].rk_e[i]) : c[8], L);
+      if (xs >= 0) {
+        const unsigned o = (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
+        w = fmad(p.cp[0].a_e[i], fmad(mul(c[8], p.dl[0]), L, a.m.ez_x[o]), w);
+      }
+      break;
+  }
+  return w;
+}
+
+// ---- weights of one H cell on its E differences ------------------------
+// which: 0 = Hx on dEy/dz, 1 = Hx on dEz/dy, 2 = Hy on dEz/dx, 3 = Hy on
+// dEx/dz, 4 = Hz on dEx/dy, 5 = Hz on dEy/dx.  Zero outside the component.
+template <typename T, typename I>
+__device__ __forceinline__ T h_weight(const AdjParams<T, I> &a, int i, int j, int k, int which) {
+  const VolParams<T, I> &p = a.v;
+  const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
+  if (i < 0 || j < 0 || k < 0 || i > nx || j > ny || k > nz) return T(0);
+  const int comp = which >> 1;
+  if ((comp == 0 && (j >= ny || k >= nz)) || (comp == 1 && (i >= nx || k >= nz)) || (comp == 2 && (i >= nx || j >= ny)))
+    return T(0);
+  const unsigned b = static_cast<unsigned>(i) * static_cast<unsigned>(p.d.si) +
+                     static_cast<unsigned>(j) * static_cast<unsigned>(p.d.sj) + static_cast<unsigned>(k);
+  const T L = a.lH[comp][b];
+  const T *c = p.table + static_cast<unsigned>(__ldg(p.idx + b)) * 18 + 9;
+  const int xs = p.cp[0].n_layers ? p.cp[0].slot_h[i] : -1;
+  const int ys = p.cp[1].n_layers ? p.cp[1].slot_h[j] : -1;
+  const int zs = p.cp[2].n_layers ? p.cp[2].slot_h[k] : -1;
+  const int Ly = p.cp[1].n_layers, Lz = p.cp[2].n_layers;
+  const unsigned nzp = static_cast<unsigned>(p.d.nzp), ny1 = static_cast<unsigned>(ny + 1);
+  T w = T(0);
+  switch (which) {
+    case 0:   // Hx, (Ey(k+1) - Ey(k)): main ca = chxey (x 1/kappa_z), psi_hx_z
+      if (i < nx) w = mul(zs >= 0 ? mul(c[1], p.cp[2].rk_m[k]) : c[1], L);
+      if (zs >= 0) {
+        const unsigned o = (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
+        w = fmad(p.cp[2].a_m[k], fmad(mul(c[1], p.dl[2]), L, a.m.hx_z[o]), w);
+      }
+      break;
+    case 1:   // Hx, (Ez(j+1) - Ez(j)): main cb = chxez (x 1/kappa_y), psi_hx_y
+      if (i < nx) w = mul(ys >= 0 ? mul(c[2], p.cp[1].rk_m[j]) : c[2], L);
+      if (ys >= 0) {
+        const unsigned o = (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
+        w = fmad(p.cp[1].a_m[j], fmad(mul(c[2], p.dl[1]), L, a.m.hx_y[o]), w);
+      }
+      break;
+    case 2:   // Hy, (Ez(i+1) - Ez(i)): main ca = chyez (x 1/kappa_x), psi_hy_x
+      if (j < ny) w = mul(xs >= 0 ? mul(c[4], p.cp[0].rk_m[i]) : c[4], L);
+      if (xs >= 0) {
+        const unsigned o = (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
+        w = fmad(p.cp[0].a_m[i], fmad(mul(c[4], p.dl[0]), L, a.m.hy_x[o]), w);
+      }
+      break;
+    case 3:   // Hy, (Ex(k+1) - Ex(k)): main cb = chyex (x 1/kappa_z), psi_hy_z
+      if (j < ny) w = mul(zs >= 0 ? mul(c[5], p.cp[2].rk_m[k]) : c[5], L);
+      if (zs >= 0) {
+        const unsigned o = (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
+        w = fmad(p.cp[2].a_m[k], fmad(mul(c[5], p.dl[2]), L, a.m.hy_z[o]), w);
+      }
+      break;
+    case 4:   // Hz, (Ex(j+1) - Ex(j)): main ca = chzex (x 1/kappa_y), psi_hz_y
+      if (k < nz) w = mul(ys >= 0 ? mul(c[7], p.cp[1].rk_m[j]) : c[7], L);
+      if (ys >= 0) {
+        const unsigned o = (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
+        w = fmad(p.cp[1].a_m[j], fmad(mul(c[7], p.dl[1]), L, a.m.hz_y[o]), w);
+      }
+      break;
+    default:   // Hz, (Ey(i+1) - Ey(i)): main cb = chzey (x 1/kappa_x), psi_hz_x
+      if (k < nz) w = mul(xs >= 0 ? mul(c[8], p.cp[0].rk_m[i]) : c[8], L);
+      if (xs >= 0) {
+        const unsigned o = (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
+        w = fmad(p.cp[0].a_m[i], fmad(mul(c[8], p.dl[0]), L, a.m.hz_x[o]), w);
+      }
+      break;
+  }
+  return w;
+}
+
+// lH(t) = [main] c0 lH' + W gather;  mH(t) = b (mH' + c dl lH').
+template <typename T, typename I>
+__global__ void __launch_bounds__(256) k_adj_h(AdjParams<T, I> a) {
+  const VolParams<T, I> &p = a.v;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = blockIdx.z;
+  const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
+  if (k > nz || j > ny || i > nx) return;
+  const unsigned b = static_cast<unsigned>(i) * static_cast<unsigned>(p.d.si) +
+                     static_cast<unsigned>(j) * static_cast<unsigned>(p.d.sj) + static_cast<unsigned>(k);
+  // W gathers (E cells reading H at this cell)
+  const T gx = e_weight(a, i, j, k, 2) - e_weight(a, i, j, k + 1, 2) + e_weight(a, i, j, k, 4) - e_weight(a, i, j + 1, k, 4);
+  const T gy = e_weight(a, i, j, k, 0) - e_weight(a, i, j, k + 1, 0) + e_weight(a, i, j, k, 5) - e_weight(a, i + 1, j, k, 5);
+  const T gz = e_weight(a, i, j, k, 1) - e_weight(a, i, j + 1, k, 1) + e_weight(a, i, j, k, 3) - e_weight(a, i + 1, j, k, 3);
+  const T *c = p.table + static_cast<unsigned>(__ldg(p.idx + b)) * 18 + 9;
+  const int xs = p.cp[0].n_layers ? p.cp[0].slot_h[i] : -1;
+  const int ys = p.cp[1].n_layers ? p.cp[1].slot_h[j] : -1;
+  const int zs = p.cp[2].n_layers ? p.cp[2].slot_h[k] : -1;
+  const int Ly = p.cp[1].n_layers, Lz = p.cp[2].n_layers;
+  const unsigned nzp = static_cast<unsigned>(p.d.nzp), ny1 = static_cast<unsigned>(ny + 1);
+  // own transpose: mH = b (mH' + c dl lH'), lH = [main] c0 lH' (+ gather)
+  if (j < ny && k < nz) {   // Hx
+    const T L = a.lH[0][b];
+    if (ys >= 0) {
+      T *q = a.m.hx_y + (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
+      *q = mul(p.cp[1].b_m[j], fmad(mul(c[2], p.dl[1]), L, *q));
+    }
+    if (zs >= 0) {
+      T *q = a.m.hx_z + (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
+      *q = mul(p.cp[2].b_m[k], fmad(mul(c[1], p.dl[2]), L, *q));
+    }
+    a.lH[0][b] = (i < nx ? mul(c[0], L) : L) + gx;
+  }
+  if (i < nx && k < nz) {   // Hy
+    const T L = a.lH[1][b];
+    if (xs >= 0) {
+      T *q = a.m.hy_x + (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
+      *q = mul(p.cp[0].b_m[i], fmad(mul(c[4], p.dl[0]), L, *q));
+    }
+    if (zs >= 0) {
+      T *q = a.m.hy_z + (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
+      *q = mul(p.cp[2].b_m[k], fmad(mul(c[5], p.dl[2]), L, *q));
+    }
+    a.lH[1][b] = (j < ny ? mul(c[3], L) : L) + gy;
+  }
+  if (i < nx && j < ny) {   // Hz
+    const T L = a.lH[2][b];
+    if (xs >= 0) {
+      T *q = a.m.hz_x + (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
+      *q = mul(p.cp[0].b_m[i], fmad(mul(c[8], p.dl[0]), L, *q));
+    }
+    if (ys >= 0) {
+      T *q = a.m.hz_y + (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
+      *q = mul(p.cp[1].b_m[j], fmad(mul(c[7], p.dl[1]), L, *q));
+    }
+    a.lH[2][b] = (k < nz ? mul(c[6], L) : L) + gz;
+  }
+}
+
+// Own E transpose and gradient of step t (do_e_own), then the loss and U
+// gather of step t-1 (do_gather).
+template <typename T, typename I>
+__global__ void __launch_bounds__(256) k_adj_e(AdjParams<T, I> a) {
+  const VolParams<T, I> &p = a.v;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = blockIdx.z;
+  const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
+  if (k > nz || j > ny || i > nx) return;
+  const unsigned b = static_cast<unsigned>(i) * static_cast<unsigned>(p.d.si) +
+                     static_cast<unsigned>(j) * static_cast<unsigned>(p.d.sj) + static_cast<unsigned>(k);
+  const bool ex = i < nx, ey = j < ny, ez = k < nz;   // components present at this index
+  T L[3] = {ex ? a.lE[0][b] : T(0), ey ? a.lE[1][b] : T(0), ez ? a.lE[2][b] : T(0)};
+  if (a.do_e_own) {
+    const unsigned id = static_cast<unsigned>(__ldg(p.idx + b));
+    const T *c = p.table + id * 18;
+    // gradient of step t over the design box (interior cells: main updates, no CPML)
+    if (i >= a.dlo[0] && i < a.dhi[0] && j >= a.dlo[1] && j < a.dhi[1] && k >= a.dlo[2] && k < a.dhi[2]) {
+      const int di = i - a.dlo[0], dj = j - a.dlo[1], dk = k - a.dlo[2];
+      const int ej = a.dhi[1] - a.dlo[1], ek = a.dhi[2] - a.dlo[2];
+      const int hj = ej + 1, hk = ek + 1;
+      auto E = [&](int comp) { return static_cast<double>(a.recE[comp][(di * ej + dj) * ek + dk]); };
+      auto H = [&](int comp, int oi, int oj, int ok) {   // H(t) at (i+oi, j+oj, k+ok), o* in {-1, 0}
+        return static_cast<double>(a.recH[comp][((di + 1 + oi) * hj + (dj + 1 + oj)) * hk + (dk + 1 + ok)]);
+      };
+      const double curl[3] = {
+          static_cast<double>(c[1]) * (H(1, 0, 0, 0) - H(1, 0, 0, -1)) + static_cast<double>(c[2]) * (H(2, 0, 0, 0) - H(2, 0, -1, 0)),
+          static_cast<double>(c[5]) * (H(0, 0, 0, 0) - H(0, 0, 0, -1)) + static_cast<double>(c[4]) * (H(2, 0, 0, 0) - H(2, -1, 0, 0)),
+          static_cast<double>(c[7]) * (H(0, 0, 0, 0) - H(0, 0, -1, 0)) + static_cast<double>(c[8]) * (H(1, 0, 0, 0) - H(1, -1, 0, 0))};
+      const double *dt = a.dtab + 4 * id;
+      double ge = 0, gs = 0;
+      for (int comp = 0; comp < 3; ++comp) {
+        const double l = static_cast<double>(L[comp]);
+        ge += l * (dt[0] * E(comp) + dt[2] * curl[comp]);
+        gs += l * (dt[1] * E(comp) + dt[3] * curl[comp]);
+      }
+      const int g = (di * ej + dj) * ek + dk;
+      a.g_eps[g] += ge;
+      a.g_sig[g] += gs;
+    }
+    const int xs = p.cp[0].n_layers ? p.cp[0].slot_e[i] : -1;
+    const int ys = p.cp[1].n_layers ? p.cp[1].slot_e[j] : -1;
+    const int zs = p.cp[2].n_layers ? p.cp[2].slot_e[k] : -1;
+    const bool in_i = i >= 1 && i < nx, in_j = j >= 1 && j < ny, in_k = k >= 1 && k < nz;
+    const int Ly = p.cp[1].n_layers, Lz = p.cp[2].n_layers;
+    const unsigned nzp = static_cast<unsigned>(p.d.nzp), ny1 = static_cast<unsigned>(ny + 1);
+    if (ex) {
+      if (ys >= 0) {
+        T *q = a.m.ex_y + (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
+        *q = mul(p.cp[1].b_e[j], fmad(mul(c[2], p.dl[1]), L[0], *q));
+      }
+      if (zs >= 0) {
+        T *q = a.m.ex_z + (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
+        *q = mul(p.cp[2].b_e[k], fmad(mul(c[1], p.dl[2]), L[0], *q));
+      }
+      if (in_j && in_k) L[0] = mul(c[0], L[0]);
+    }
+    if (ey) {
+      if (xs >= 0) {
+        T *q = a.m.ey_x + (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
+        *q = mul(p.cp[0].b_e[i], fmad(mul(c[4], p.dl[0]), L[1], *q));
+      }
+      if (zs >= 0) {
+        T *q = a.m.ey_z + (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
+        *q = mul(p.cp[2].b_e[k], fmad(mul(c[5], p.dl[2]), L[1], *q));
+      }
+      if (in_i && in_k) L[1] = mul(c[3], L[1]);
+    }
+    if (ez) {
+      if (xs >= 0) {
+        T *q = a.m.ez_x + (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
+        *q = mul(p.cp[0].b_e[i], fmad(mul(c[8], p.dl[0]), L[2], *q));
+      }
+      if (ys >= 0) {
+        T *q = a.m.ez_y + (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
+        *q = mul(p.cp[1].b_e[j], fmad(mul(c[7], p.dl[1]), L[2], *q));
+      }
+      if (in_i && in_j) L[2] = mul(c[6], L[2]);
+    }
+  }
+  if (a.do_gather) {
+    // loss gradient of step t-1: d/dF sum F^2 = 2 F over the plane
+    if (a.plane_rec) {
+      const int ax = a.plane_axis;
+      const int idx3[3] = {i, j, k};
+      const int u = idx3[ax == 0 ? 1 : 0], v = idx3[ax == 2 ? 1 : 2];
+      if (idx3[ax] == a.plane_index && u >= a.plo[0] && u < a.phi[0] && v >= a.plo[1] && v < a.phi[1]) {
+        const int nv = a.phi[1] - a.plo[1];
+        L[a.loss_comp] += T(2) * a.plane_rec[(u - a.plo[0]) * nv + (v - a.plo[1])];
+      }
+    }
+    // U gathers (H cells of step t-1 reading E at this cell)
+    if (ex) L[0] += h_weight(a, i, j, k - 1, 3) - h_weight(a, i, j, k, 3) + h_weight(a, i, j - 1, k, 4) - h_weight(a, i, j, k, 4);
+    if (ey) L[1] += h_weight(a, i, j, k - 1, 0) - h_weight(a, i, j, k, 0) + h_weight(a, i - 1, j, k, 5) - h_weight(a, i, j, k, 5);
+    if (ez) L[2] += h_weight(a, i, j - 1, k, 1) - h_weight(a, i, j, k, 1) + h_weight(a, i - 1, j, k, 2) - h_weight(a, i, j, k, 2);
+  }
+  if (ex) a.lE[0][b] = L[0];
+  if (ey) a.lE[1][b] = L[1];
+  if (ez) a.lE[2][b] = L[2];
+}
+
+template <typename T>
+struct FieldPtrs {
+  const T *f[6];
+};
+
+// Copies E(t) over the design box and H(t) over the box grown by one cell
+// on the low sides into the records of step slot s.
+template <typename T>
+__global__ void k_adj_record(FieldPtrs<T> F, Dims d, int lo0, int lo1, int lo2, int n0, int n1, int n2, T *recE0,
+                             T *recE1, T *recE2, T *recH0, T *recH1, T *recH2) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;   // 0 .. n2 (H box is one larger)
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = blockIdx.z;
+  if (k > n2 || j > n1 || i > n0) return;
+  // H box cell (i, j, k) is grid cell (lo-1 + i, ...)
+  const long long gh = static_cast<long long>(lo0 - 1 + i) * d.si + static_cast<long long>(lo1 - 1 + j) * d.sj + (lo2 - 1 + k);
+  const long long h = (static_cast<long long>(i) * (n1 + 1) + j) * (n2 + 1) + k;
+  recH0[h] = F.f[3][gh];
+  recH1[h] = F.f[4][gh];
+  recH2[h] = F.f[5][gh];
+  if (i >= 1 && j >= 1 && k >= 1) {
+    const long long e = (static_cast<long long>(i - 1) * n1 + (j - 1)) * n2 + (k - 1);
+    recE0[e] = F.f[0][gh];
+    recE1[e] = F.f[1][gh];
+    recE2[e] = F.f[2][gh];
+  }
+}
+
+// Copies the loss component over the plane into rec (row-major over the two
+// other axes).
+template <typename T>
+__global__ void k_adj_plane(const T *f, Dims d, int axis, int index, int lo0, int lo1, int n0, int n1, T *rec) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const int u = blockIdx.y;
+  if (v >= n1 || u >= n0) return;
+  int ijk[3];
+  ijk[axis] = index;
+  ijk[axis == 0 ? 1 : 0] = lo0 + u;
+  ijk[axis == 2 ? 1 : 2] = lo1 + v;
+  rec[static_cast<long long>(u) * n1 + v] = f[static_cast<long long>(ijk[0]) * d.si + static_cast<long long>(ijk[1]) * d.sj + ijk[2]];
+}
+
+}  // namespace xg

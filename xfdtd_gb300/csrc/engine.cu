@@ -35,6 +35,7 @@
 
 #include "../../include/xfdtd_cuda.h"
 #include "common.cuh"
+#include "adjoint.cuh"
 #include "batch.cuh"
 #include "surface.cuh"
 #include "sweep.cuh"
@@ -64,6 +65,8 @@ const char *kKernelNames[] = {"tfsf_aux", "update_e", "lumped_e", "update_h",  "
 constexpr int kNumKernels = 11;
 
 }  // namespace
+
+struct AdjointState;
 
 struct xfdtd_handle {
   std::string err;
@@ -97,6 +100,7 @@ struct xfdtd_handle {
   uint8_t *axis_flags[3] = {};  // per-axis fast-path flags
   void *prof[3][6] = {};   // b_e a_e rk_e b_m a_m rk_m (precision T)
   void *psi[12] = {};      // ex_y ex_z ey_x ey_z ez_x ez_y hx_y hx_z hy_x hy_z hz_x hz_y
+  size_t psi_bytes[12] = {};
 
   // TFSF
   bool tfsf = false;
@@ -134,6 +138,12 @@ struct xfdtd_handle {
   long long *d_step = nullptr;
   int *d_status = nullptr;
   int *d_flag = nullptr;
+
+  // host copies kept for the adjoint: the coefficient table (FP64) and the
+  // per-axis index flags
+  std::vector<double> table_host;
+  std::vector<uint8_t> axis_flags_host[3];
+  std::shared_ptr<AdjointState> adj;   // set up by xfdtd_adjoint_forward
 
   // volume-kernel variants (autotuned)
   int var_e = 1, var_h = 1;   // L1-table variant: valid for every plan
@@ -230,6 +240,20 @@ int guarded(xfdtd_handle *h, F &&fn) {
 }
 
 void invalid(const std::string &m) { throw Err{XFDTD_ERR_INVALID_PLAN, m}; }
+
+// Calls f(T{}, I{}) with the field type and material-index type of a handle.
+template <class F>
+void with_types(int precision, int idx_bytes, F &&f) {
+  if (precision == XFDTD_FP64) {
+    if (idx_bytes == 1) f(double{}, uint8_t{});
+    else if (idx_bytes == 2) f(double{}, uint16_t{});
+    else f(double{}, uint32_t{});
+  } else {
+    if (idx_bytes == 1) f(float{}, uint8_t{});
+    else if (idx_bytes == 2) f(float{}, uint16_t{});
+    else f(float{}, uint32_t{});
+  }
+}
 
 // ------------------------------------------------------------ launches ---
 void prof_begin(xfdtd_handle *h, int id, cudaStream_t st = nullptr) {
@@ -531,13 +555,9 @@ void autotune_t(xfdtd_handle *h, int trials) {
 
 void autotune(xfdtd_handle *h, int trials) {
   if (h->host_step != 0) throw Err{XFDTD_ERR_STATE, "autotuning runs before the first step only"};
-  if (h->precision == XFDTD_FP64) {
-    if (h->idx_bytes == 1) autotune_t<double, uint8_t>(h, trials);
-    else autotune_t<double, uint16_t>(h, trials);
-  } else {
-    if (h->idx_bytes == 1) autotune_t<float, uint8_t>(h, trials);
-    else autotune_t<float, uint16_t>(h, trials);
-  }
+  with_types(h->precision, h->idx_bytes, [&](auto t, auto i) {
+    autotune_t<decltype(t), decltype(i)>(h, trials);
+  });
 }
 
 template <typename T>
@@ -754,13 +774,9 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
 
 // Enqueues the kernels of step s (s = the step's index, known on the host).
 void enqueue_step(xfdtd_handle *h, long long s) {
-  if (h->precision == XFDTD_FP64) {
-    if (h->idx_bytes == 1) enqueue_step_t<double, uint8_t>(h, s);
-    else enqueue_step_t<double, uint16_t>(h, s);
-  } else {
-    if (h->idx_bytes == 1) enqueue_step_t<float, uint8_t>(h, s);
-    else enqueue_step_t<float, uint16_t>(h, s);
-  }
+  with_types(h->precision, h->idx_bytes, [&](auto t, auto i) {
+    enqueue_step_t<decltype(t), decltype(i)>(h, s);
+  });
 }
 
 int launches_per_step(const xfdtd_handle *h) {
@@ -806,8 +822,8 @@ void comp_shape(const xfdtd_handle *h, int c, long long s[3]) {
 void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   if (pl->nx < 2 || pl->ny < 2 || pl->nz < 2) invalid("grid must have at least 2 cells per axis");
   if (pl->precision != XFDTD_FP64 && pl->precision != XFDTD_FP32) invalid("precision must be FP64 or FP32");
-  if (pl->index_bytes != 1 && pl->index_bytes != 2) invalid("index_bytes must be 1 or 2");
-  if (pl->n_materials < 1 || pl->n_materials > (pl->index_bytes == 1 ? 256 : 65536))
+  if (pl->index_bytes != 1 && pl->index_bytes != 2 && pl->index_bytes != 4) invalid("index_bytes must be 1, 2 or 4");
+  if (pl->n_materials < 1 || (pl->index_bytes < 4 && pl->n_materials > (pl->index_bytes == 1 ? 256 : 65536)))
     invalid("material count does not fit the index width");
   if (!pl->material_index || !pl->coeff_table) invalid("material index and coefficient table are required");
   if (pl->total_steps < 1) invalid("total_steps must be positive");
@@ -845,7 +861,13 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     for (long long i = 0; i < NX1; ++i)
       for (long long j = 0; j < NY1; ++j) {
         const uint8_t *row = src + ((i * NY1 + j) * NZ1) * pl->index_bytes;
-        if (pl->index_bytes == 2) {
+        if (pl->index_bytes == 4) {
+          for (long long k = 0; k < NZ1; ++k) {
+            uint32_t v;
+            std::memcpy(&v, row + 4 * k, 4);
+            if (v >= static_cast<uint32_t>(pl->n_materials)) invalid("material index out of range");
+          }
+        } else if (pl->index_bytes == 2) {
           const uint16_t *r16 = reinterpret_cast<const uint16_t *>(row);
           for (long long k = 0; k < NZ1; ++k)
             if (r16[k] >= pl->n_materials) invalid("material index out of range");
@@ -858,19 +880,14 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     h->idx = h->upload<uint8_t>(buf.data(), buf.size());
   }
   h->n_mat = pl->n_materials;
+  h->table_host.assign(pl->coeff_table, pl->coeff_table + static_cast<size_t>(pl->n_materials) * XFDTD_N_COEFF);
   h->table = h->upload_real(pl->coeff_table, static_cast<size_t>(pl->n_materials) * XFDTD_N_COEFF);
   h->smem_bytes = static_cast<size_t>(pl->n_materials) * 9 * h->esize;
   h->smem_table = h->smem_bytes <= 96 * 1024;
   if (h->smem_table && h->smem_bytes > 48 * 1024) {
     // opt in to more than 48 KB of dynamic shared memory for the table
     int bytes = static_cast<int>(h->smem_bytes);
-    if (h->precision == XFDTD_FP64) {
-      if (h->idx_bytes == 1) smem_attr<double, uint8_t>(bytes);
-      else smem_attr<double, uint16_t>(bytes);
-    } else {
-      if (h->idx_bytes == 1) smem_attr<float, uint8_t>(bytes);
-      else smem_attr<float, uint16_t>(bytes);
-    }
+    with_types(h->precision, h->idx_bytes, [&](auto t, auto i) { smem_attr<decltype(t), decltype(i)>(bytes); });
   }
 
   // CPML profiles
@@ -900,10 +917,14 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     const size_t sz = static_cast<size_t>(NX1) * NY1 * h->L[2];
     // order: ex_y ex_z ey_x ey_z ez_x ez_y hx_y hx_z hy_x hy_z hz_x hz_y
     const size_t sizes[12] = {sy, sz, sx, sz, sx, sy, sy, sz, sx, sz, sx, sy};
-    for (int q = 0; q < 12; ++q) h->psi[q] = sizes[q] ? h->alloc_bytes(sizes[q] * h->esize) : nullptr;
+    for (int q = 0; q < 12; ++q) {
+      h->psi[q] = sizes[q] ? h->alloc_bytes(sizes[q] * h->esize) : nullptr;
+      h->psi_bytes[q] = sizes[q] * h->esize;
+    }
     // the fused sweep, unless the plan asks for the split kernels or has
     // lumped elements (whose E corrections run between the E and H updates)
-    h->sweep_ok = !(pl->flags & XFDTD_FLAG_SPLIT_EH) && pl->n_injections == 0 && pl->n_inductor_cells == 0;
+    h->sweep_ok = !(pl->flags & XFDTD_FLAG_SPLIT_EH) && pl->n_injections == 0 && pl->n_inductor_cells == 0 &&
+                  pl->index_bytes < 4;
     h->sweep = h->sweep_ok && (pl->flags & XFDTD_FLAG_FUSED_EH);
     if (h->sweep_ok) {
       for (int c = 0; c < 6; ++c) h->F2[c] = h->alloc_bytes(d.cells * h->esize);
@@ -1059,6 +1080,7 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
       if (h->tfsf && (q == h->tf_lo[a] || q == h->tf_hi[a])) fl[q] |= xg::kTfsfE;
     }
     h->axis_flags[a] = h->upload<uint8_t>(fl.data(), fl.size());
+    h->axis_flags_host[a] = fl;
   }
 
   h->d_step = h->alloc<long long>(1);
@@ -1709,6 +1731,7 @@ int xfdtd_batch_create(xfdtd_handle *const *members, int n, int flags, xfdtd_bat
         }
         if (h->device != b->device || h->precision != b->precision || h->idx_bytes != b->idx_bytes)
           invalid("batch members must share device, precision and material-index width");
+        if (h->idx_bytes > 2) invalid("batch members must use 1- or 2-byte material indices");
         if (h->host_step != 0) invalid("batch members must not have been stepped");
         if (h->n_inj || h->n_ind || h->n_probes) invalid("batch members may not have lumped elements or monitors");
         if (h->d.nx >= 65535 || h->d.ny >= 2040 || h->d.nz >= 8160) invalid("batch member grid too large for the tile numbering");
@@ -1798,6 +1821,325 @@ void xfdtd_batch_destroy(xfdtd_batch *b) {
     cudaStreamSynchronize(b->stream);
   }
   delete b;
+}
+
+}  // extern "C"
+
+// ============================================================== adjoint ===
+// Gradient of a field loss with respect to eps_r and sigma of the cells of
+// a design box (adjoint.cuh).  xfdtd_adjoint_forward runs the whole step
+// loop from step 0 on the split kernels, recording the loss component over
+// the loss plane after every step of the loss window and, every K steps, a
+// checkpoint of the state (fields, psi, TFSF line).  xfdtd_adjoint_backward
+// walks the checkpoint segments from the last to the first: it restores the
+// segment's checkpoint, re-runs its K steps recording E and H over the
+// design box, then runs the K reverse steps.  With K = 0 the forward pass
+// records the design box at every step and the backward pass re-runs
+// nothing.
+
+struct AdjointState {
+  xfdtd_adjoint_desc d{};
+  int dn[3] = {0, 0, 0};                 // design box extent
+  long long nE = 0, nH = 0;              // cells of the E and H record boxes
+  int pn[2] = {0, 0};                    // loss plane extent
+  int K = 0;                             // checkpoint interval (0: record every step)
+  int slots = 0;                         // design-record slots
+  std::vector<void *> allocs;
+  void *recE[3] = {}, *recH[3] = {};     // [slots][box]
+  void *plane = nullptr;                 // [window][pn0 * pn1]
+  std::vector<void *> ck;                // checkpoints: one block each
+  size_t ck_bytes = 0;
+  void *lE[3] = {}, *lH[3] = {}, *m[12] = {};
+  double *g_eps = nullptr, *g_sig = nullptr, *dtab = nullptr;
+  double loss = 0;
+  bool forward_done = false;
+  int device = 0;
+  void *alloc(size_t bytes) {
+    void *p = nullptr;
+    XCHECK(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+    allocs.push_back(p);
+    return p;
+  }
+  ~AdjointState() {
+    cudaSetDevice(device);
+    for (void *p : allocs) cudaFree(p);
+  }
+};
+
+namespace {
+
+// Bytes of one checkpoint: fields, psi, TFSF line state and both incident buffers.
+size_t adj_checkpoint_bytes(const xfdtd_handle *h) {
+  size_t b = 6 * static_cast<size_t>(h->d.cells) * h->esize;
+  for (int q = 0; q < 12; ++q) b += h->psi_bytes[q];
+  if (h->tfsf) b += (2 * static_cast<size_t>(h->aux_len) + 1 + 12 * static_cast<size_t>(h->aux_len)) * sizeof(double) +
+                    (h->tf_incf ? 12 * static_cast<size_t>(h->aux_len) * sizeof(float) : 0);
+  return b;
+}
+
+// Copies the state into (save) or out of (restore) one checkpoint block.
+void adj_checkpoint(xfdtd_handle *h, void *block, bool save) {
+  unsigned char *p = static_cast<unsigned char *>(block);
+  auto io = [&](void *dev, size_t bytes) {
+    if (!bytes || !dev) return;
+    if (save) XCHECK(cudaMemcpyAsync(p, dev, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    else XCHECK(cudaMemcpyAsync(dev, p, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    p += bytes;
+  };
+  for (int c = 0; c < 6; ++c) io(h->F[c], static_cast<size_t>(h->d.cells) * h->esize);
+  for (int q = 0; q < 12; ++q) io(h->psi[q], h->psi_bytes[q]);
+  if (h->tfsf) {
+    io(h->tf_state, (2 * static_cast<size_t>(h->aux_len) + 1) * sizeof(double));
+    io(h->tf_inc, 12 * static_cast<size_t>(h->aux_len) * sizeof(double));
+    if (h->tf_incf) io(h->tf_incf, 12 * static_cast<size_t>(h->aux_len) * sizeof(float));
+  }
+}
+
+template <typename T>
+void adj_record_design(xfdtd_handle *h, AdjointState *a, int slot) {
+  const int n0 = a->dn[0], n1 = a->dn[1], n2 = a->dn[2];
+  T *rE[3], *rH[3];
+  for (int c = 0; c < 3; ++c) {
+    rE[c] = static_cast<T *>(a->recE[c]) + static_cast<size_t>(slot) * a->nE;
+    rH[c] = static_cast<T *>(a->recH[c]) + static_cast<size_t>(slot) * a->nH;
+  }
+  xg::FieldPtrs<T> fp;
+  for (int c = 0; c < 6; ++c) fp.f[c] = static_cast<const T *>(h->F[c]);
+  dim3 block(32, 8, 1);
+  dim3 grid((n2 + 1 + 31) / 32, (n1 + 1 + 7) / 8, n0 + 1);
+  xg::k_adj_record<T><<<grid, block, 0, h->stream>>>(fp, h->d, static_cast<int>(a->d.design_lo[0]),
+                                                      static_cast<int>(a->d.design_lo[1]), static_cast<int>(a->d.design_lo[2]),
+                                                      n0, n1, n2, rE[0], rE[1], rE[2], rH[0], rH[1], rH[2]);
+  XCHECK(cudaGetLastError());
+}
+
+template <typename T>
+void adj_record_plane(xfdtd_handle *h, AdjointState *a, long long w) {
+  T *rec = static_cast<T *>(a->plane) + static_cast<size_t>(w) * a->pn[0] * a->pn[1];
+  dim3 grid((a->pn[1] + 127) / 128, a->pn[0], 1);
+  xg::k_adj_plane<T><<<grid, 128, 0, h->stream>>>(static_cast<const T *>(h->F[a->d.loss_comp]), h->d, a->d.plane_axis,
+                                                  static_cast<int>(a->d.plane_index), static_cast<int>(a->d.plane_lo[0]),
+                                                  static_cast<int>(a->d.plane_lo[1]), a->pn[0], a->pn[1], rec);
+  XCHECK(cudaGetLastError());
+}
+
+void adj_validate(xfdtd_handle *h, const xfdtd_adjoint_desc *d) {
+  if (h->host_step != 0) throw Err{XFDTD_ERR_STATE, "the adjoint forward pass starts at step 0"};
+  if (h->n_ind) invalid("the adjoint does not cover inductors (their current is extra state)");
+  const int n[3] = {h->d.nx, h->d.ny, h->d.nz};
+  for (int a = 0; a < 3; ++a) {
+    if (d->design_lo[a] < 1 || d->design_hi[a] <= d->design_lo[a] || d->design_hi[a] > n[a] - 1)
+      invalid("design box must lie inside the grid, off the outer walls");
+    for (long long q = d->design_lo[a] - 1; q <= d->design_hi[a]; ++q)
+      if (h->axis_flags_host[a][q] & (xg::kSpecialE | xg::kSpecialH))
+        invalid("design box (and its one-cell rim) must lie outside the CPML");
+  }
+  if (d->loss_comp < 0 || d->loss_comp > 2) invalid("loss component must be Ex, Ey or Ez");
+  if (d->plane_axis < 0 || d->plane_axis > 2) invalid("plane axis must be 0, 1 or 2");
+  const int u = d->plane_axis == 0 ? 1 : 0, v = d->plane_axis == 2 ? 1 : 2;
+  if (d->plane_index < 0 || d->plane_index > n[d->plane_axis]) invalid("plane index outside the grid");
+  if (d->plane_lo[0] < 0 || d->plane_hi[0] <= d->plane_lo[0] || d->plane_hi[0] > n[u] + 1 || d->plane_lo[1] < 0 ||
+      d->plane_hi[1] <= d->plane_lo[1] || d->plane_hi[1] > n[v] + 1)
+    invalid("plane extent outside the grid");
+  if (d->t_begin < 0 || d->t_end <= d->t_begin || d->t_end > h->total) invalid("loss window outside the steps");
+  if (d->checkpoint_every < 0) invalid("checkpoint interval must be >= 0");
+}
+
+template <typename T>
+void adj_forward_t(xfdtd_handle *h, const xfdtd_adjoint_desc *d, double *loss) {
+  adj_validate(h, d);
+  auto a = std::make_shared<AdjointState>();
+  a->device = h->device;
+  a->d = *d;
+  for (int q = 0; q < 3; ++q) a->dn[q] = static_cast<int>(d->design_hi[q] - d->design_lo[q]);
+  a->nE = static_cast<long long>(a->dn[0]) * a->dn[1] * a->dn[2];
+  a->nH = static_cast<long long>(a->dn[0] + 1) * (a->dn[1] + 1) * (a->dn[2] + 1);
+  a->pn[0] = static_cast<int>(d->plane_hi[0] - d->plane_lo[0]);
+  a->pn[1] = static_cast<int>(d->plane_hi[1] - d->plane_lo[1]);
+  a->K = d->checkpoint_every;
+  const long long T_ = h->total;
+  a->slots = a->K > 0 ? a->K : static_cast<int>(T_);
+  for (int c = 0; c < 3; ++c) {
+    a->recE[c] = a->alloc(static_cast<size_t>(a->slots) * a->nE * sizeof(T));
+    a->recH[c] = a->alloc(static_cast<size_t>(a->slots) * a->nH * sizeof(T));
+  }
+  const long long win = d->t_end - d->t_begin;
+  a->plane = a->alloc(static_cast<size_t>(win) * a->pn[0] * a->pn[1] * sizeof(T));
+  if (a->K > 0) {
+    a->ck_bytes = adj_checkpoint_bytes(h);
+    const long long n_ck = (T_ + a->K - 1) / a->K + 1;   // segment starts and the final state
+    for (long long q = 0; q < n_ck; ++q) a->ck.push_back(a->alloc(a->ck_bytes));
+  }
+  h->sweep = false;   // the adjoint transposes the split kernels' arithmetic
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  for (long long t = 0; t < T_; ++t) {
+    if (a->K > 0 && t % a->K == 0) adj_checkpoint(h, a->ck[t / a->K], true);
+    if (a->K == 0) adj_record_design<T>(h, a.get(), static_cast<int>(t));
+    enqueue_step(h, t);
+    h->host_step = t + 1;
+    if (t >= d->t_begin && t < d->t_end) adj_record_plane<T>(h, a.get(), t - d->t_begin);
+  }
+  if (a->K > 0) adj_checkpoint(h, a->ck.back(), true);
+  prof_collect(h);
+  // loss = sum over the window and the plane of F^2
+  std::vector<T> pl(static_cast<size_t>(win) * a->pn[0] * a->pn[1]);
+  XCHECK(cudaMemcpyAsync(pl.data(), a->plane, pl.size() * sizeof(T), cudaMemcpyDeviceToHost, h->stream));
+  XCHECK(cudaStreamSynchronize(h->stream));
+  check_status(h);
+  double L = 0;
+  for (T v : pl) L += static_cast<double>(v) * static_cast<double>(v);
+  a->loss = L;
+  a->forward_done = true;
+  h->adj = a;
+  if (loss) *loss = L;
+}
+
+template <typename T, typename I>
+void adj_backward_t(xfdtd_handle *h, double *g_eps, double *g_sig) {
+  AdjointState *a = h->adj.get();
+  if (!a || !a->forward_done || h->host_step != h->total)
+    throw Err{XFDTD_ERR_STATE, "run xfdtd_adjoint_forward (to the last step) first"};
+  const size_t cells = static_cast<size_t>(h->d.cells);
+  for (int c = 0; c < 3; ++c) {
+    if (!a->lE[c]) a->lE[c] = a->alloc(cells * sizeof(T));
+    if (!a->lH[c]) a->lH[c] = a->alloc(cells * sizeof(T));
+    XCHECK(cudaMemsetAsync(a->lE[c], 0, cells * sizeof(T), h->stream));
+    XCHECK(cudaMemsetAsync(a->lH[c], 0, cells * sizeof(T), h->stream));
+  }
+  for (int q = 0; q < 12; ++q)
+    if (h->psi_bytes[q]) {
+      if (!a->m[q]) a->m[q] = a->alloc(h->psi_bytes[q]);
+      XCHECK(cudaMemsetAsync(a->m[q], 0, h->psi_bytes[q], h->stream));
+    }
+  if (!a->g_eps) {
+    a->g_eps = static_cast<double *>(a->alloc(a->nE * sizeof(double)));
+    a->g_sig = static_cast<double *>(a->alloc(a->nE * sizeof(double)));
+  }
+  XCHECK(cudaMemsetAsync(a->g_eps, 0, a->nE * sizeof(double), h->stream));
+  XCHECK(cudaMemsetAsync(a->g_sig, 0, a->nE * sizeof(double), h->stream));
+  if (!a->dtab) {   // coefficient derivatives per table entry, from the FP64 table
+    const double eps0 = kEps0, dt = h->dt;
+    std::vector<double> dtab(4 * static_cast<size_t>(h->n_mat), 0.0);
+    for (int q = 0; q < h->n_mat; ++q) {
+      const double c0 = h->table_host[q * XFDTD_N_COEFF + 0], c1 = h->table_host[q * XFDTD_N_COEFF + 1];
+      if (c1 == 0) continue;
+      const double D = -2 * dt / (c1 * h->dl[2]);   // cexhy = -2 dt / (D dz)
+      const double eps = D * (1 + c0) / 4, sig = D * (1 - c0) / (2 * dt);
+      dtab[4 * q + 0] = 4 * eps0 * dt * sig / (D * D);   // dc0 / deps_r
+      dtab[4 * q + 1] = -4 * dt * eps / (D * D);         // dc0 / dsigma
+      dtab[4 * q + 2] = -2 * eps0 / D;                   // (dc / deps_r) / c
+      dtab[4 * q + 3] = -dt / D;                         // (dc / dsigma) / c
+    }
+    a->dtab = static_cast<double *>(a->alloc(dtab.size() * sizeof(double)));
+    XCHECK(cudaMemcpyAsync(a->dtab, dtab.data(), dtab.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    XCHECK(cudaStreamSynchronize(h->stream));
+  }
+
+  xg::AdjParams<T, I> p{};
+  p.v = vol_params<T, I>(h);
+  for (int c = 0; c < 3; ++c) {
+    p.lE[c] = static_cast<T *>(a->lE[c]);
+    p.lH[c] = static_cast<T *>(a->lH[c]);
+  }
+  T **mp = reinterpret_cast<T **>(&p.m);
+  for (int q = 0; q < 12; ++q) mp[q] = static_cast<T *>(a->m[q]);
+  for (int q = 0; q < 3; ++q) {
+    p.dlo[q] = static_cast<int>(a->d.design_lo[q]);
+    p.dhi[q] = static_cast<int>(a->d.design_hi[q]);
+  }
+  p.g_eps = a->g_eps;
+  p.g_sig = a->g_sig;
+  p.dtab = a->dtab;
+  p.loss_comp = a->d.loss_comp;
+  p.plane_axis = a->d.plane_axis;
+  p.plane_index = static_cast<int>(a->d.plane_index);
+  for (int q = 0; q < 2; ++q) {
+    p.plo[q] = static_cast<int>(a->d.plane_lo[q]);
+    p.phi[q] = static_cast<int>(a->d.plane_hi[q]);
+  }
+  const long long T_ = h->total;
+  dim3 block(32, 8, 1);
+  dim3 grid((h->d.nz + 32) / 32, (h->d.ny + 8) / 8, h->d.nx + 1);
+  auto plane_of = [&](long long t1) -> const T * {   // loss record of the field after step t1
+    if (t1 < a->d.t_begin || t1 >= a->d.t_end) return nullptr;
+    return static_cast<const T *>(a->plane) + static_cast<size_t>(t1 - a->d.t_begin) * a->pn[0] * a->pn[1];
+  };
+  auto set_rec = [&](int slot) {
+    for (int c = 0; c < 3; ++c) {
+      p.recE[c] = static_cast<const T *>(a->recE[c]) + static_cast<size_t>(slot) * a->nE;
+      p.recH[c] = static_cast<const T *>(a->recH[c]) + static_cast<size_t>(slot) * a->nH;
+    }
+  };
+  // the loss gradient of the last step
+  p.do_e_own = 0;
+  p.do_gather = 1;
+  p.plane_rec = plane_of(T_ - 1);
+  set_rec(0);
+  xg::k_adj_e<T, I><<<grid, block, 0, h->stream>>>(p);
+  XCHECK(cudaGetLastError());
+  const bool nffft = h->nffft;
+  const int n_probes = h->n_probes;
+  const long long seg = a->K > 0 ? a->K : T_;
+  for (long long s0 = ((T_ - 1) / seg) * seg; s0 >= 0; s0 -= seg) {
+    const long long s1 = std::min(T_, s0 + seg);
+    if (a->K > 0) {   // re-run the segment from its checkpoint, recording the design box
+      adj_checkpoint(h, a->ck[s0 / a->K], false);
+      XCHECK(cudaMemcpyAsync(h->d_step, &s0, sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+      h->nffft = false;   // the NF-FF sums and probes of the forward pass are final
+      h->n_probes = 0;
+      for (long long t = s0; t < s1; ++t) {
+        adj_record_design<T>(h, a, static_cast<int>(t - s0));
+        enqueue_step(h, t);
+      }
+      h->nffft = nffft;
+      h->n_probes = n_probes;
+    }
+    for (long long t = s1 - 1; t >= s0; --t) {
+      xg::k_adj_h<T, I><<<grid, block, 0, h->stream>>>(p);
+      XCHECK(cudaGetLastError());
+      set_rec(static_cast<int>(a->K > 0 ? t - s0 : t));
+      p.do_e_own = 1;
+      p.do_gather = t >= 1 ? 1 : 0;
+      p.plane_rec = t >= 1 ? plane_of(t - 1) : nullptr;
+      xg::k_adj_e<T, I><<<grid, block, 0, h->stream>>>(p);
+      XCHECK(cudaGetLastError());
+    }
+  }
+  if (a->K > 0) {   // back to the state after the last step
+    adj_checkpoint(h, a->ck.back(), false);
+    XCHECK(cudaMemcpyAsync(h->d_step, &T_, sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+  }
+  XCHECK(cudaMemcpyAsync(g_eps, a->g_eps, a->nE * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  XCHECK(cudaMemcpyAsync(g_sig, a->g_sig, a->nE * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  XCHECK(cudaStreamSynchronize(h->stream));
+  check_status(h);
+}
+
+}  // namespace
+
+extern "C" {
+
+int xfdtd_adjoint_forward(xfdtd_handle *h, const xfdtd_adjoint_desc *d, double *loss) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    if (!d) invalid("null adjoint description");
+    if (h->precision == XFDTD_FP64) adj_forward_t<double>(h, d, loss);
+    else adj_forward_t<float>(h, d, loss);
+  });
+}
+
+int xfdtd_adjoint_backward(xfdtd_handle *h, double *grad_eps, double *grad_sigma, int64_t len) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    if (!h->adj) throw Err{XFDTD_ERR_STATE, "run xfdtd_adjoint_forward first"};
+    if (!grad_eps || !grad_sigma || len != h->adj->nE) invalid("gradient arrays must hold one value per design cell");
+    with_types(h->precision, h->idx_bytes, [&](auto t, auto i) {
+      adj_backward_t<decltype(t), decltype(i)>(h, grad_eps, grad_sigma);
+    });
+  });
 }
 
 }  // extern "C"

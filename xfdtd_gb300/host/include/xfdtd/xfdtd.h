@@ -553,6 +553,7 @@ class Simulation {
   void setFusedSweep(int mode) { _fused = mode; }
   // One material per cell, applied after all objects (see xfdtd_scene.h).
   void setVoxelMaterials(std::vector<Material> materials, std::vector<uint16_t> index, std::array<size_t, 3> shape);
+  void setVoxelMaterials(std::vector<Material> materials, std::vector<uint32_t> index, std::array<size_t, 3> shape);
   // Split run(): init once, step in pieces, read state, output at the end.
   void init(size_t total_time_steps);
   void step(size_t n);
@@ -586,7 +587,7 @@ class Simulation {
   std::shared_ptr<TFSF> _tfsf;
   std::shared_ptr<NFFFT> _nffft;
   std::vector<Material> _voxel_materials;
-  std::vector<uint16_t> _voxel_index;
+  std::vector<uint32_t> _voxel_index;
   std::array<size_t, 3> _voxel_shape{0, 0, 0};
 
   Precision _precision{Precision::FP64};

@@ -152,7 +152,16 @@ int xfdtd_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, int precis
         mats.emplace_back("voxel", m.eps_r, m.mu_r, m.sigma_e, m.sigma_m);
       }
       const size_t cnt = static_cast<size_t>(sc->voxel_shape[0] * sc->voxel_shape[1] * sc->voxel_shape[2]);
-      std::vector<uint16_t> idx(sc->voxel_index, sc->voxel_index + cnt);
+      std::vector<uint32_t> idx(cnt);
+      if (sc->voxel_index_bytes == 4) {
+        const uint32_t *v = static_cast<const uint32_t *>(sc->voxel_index);
+        std::copy(v, v + cnt, idx.begin());
+      } else if (sc->voxel_index_bytes == 2 || sc->voxel_index_bytes == 0) {
+        const uint16_t *v = static_cast<const uint16_t *>(sc->voxel_index);
+        std::copy(v, v + cnt, idx.begin());
+      } else {
+        throw std::invalid_argument("voxel_index_bytes must be 2 or 4");
+      }
       sim->setVoxelMaterials(std::move(mats), std::move(idx),
                              {static_cast<size_t>(sc->voxel_shape[0]), static_cast<size_t>(sc->voxel_shape[1]),
                               static_cast<size_t>(sc->voxel_shape[2])});

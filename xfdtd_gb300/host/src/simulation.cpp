@@ -68,8 +68,13 @@ void Simulation::addMonitor(std::shared_ptr<Monitor> m) { _monitors.push_back(st
 
 void Simulation::setVoxelMaterials(std::vector<Material> materials, std::vector<uint16_t> index,
                                    std::array<size_t, 3> shape) {
+  setVoxelMaterials(std::move(materials), std::vector<uint32_t>(index.begin(), index.end()), shape);
+}
+
+void Simulation::setVoxelMaterials(std::vector<Material> materials, std::vector<uint32_t> index,
+                                   std::array<size_t, 3> shape) {
   if (index.size() != shape[0] * shape[1] * shape[2]) throw std::invalid_argument("voxel index size mismatch");
-  for (uint16_t v : index)
+  for (uint32_t v : index)
     if (v >= materials.size()) throw std::invalid_argument("voxel index out of range");
   _voxel_materials = std::move(materials);
   _voxel_index = std::move(index);
@@ -427,16 +432,17 @@ void Simulation::init(size_t total_time_steps) {
     }
     idx32[kv.first] = id;
   }
-  if (table.size() > 65536) throw std::runtime_error("more than 65536 distinct coefficient tuples");
-  const int index_bytes = table.size() <= 256 ? 1 : 2;
+  const int index_bytes = table.size() <= 256 ? 1 : table.size() <= 65536 ? 2 : 4;
   std::vector<uint8_t> idx_bytes(idx32.size() * index_bytes);
   if (index_bytes == 1)
     for (size_t q = 0; q < idx32.size(); ++q) idx_bytes[q] = static_cast<uint8_t>(idx32[q]);
-  else
+  else if (index_bytes == 2)
     for (size_t q = 0; q < idx32.size(); ++q) {
       const uint16_t v = static_cast<uint16_t>(idx32[q]);
       std::memcpy(idx_bytes.data() + 2 * q, &v, 2);
     }
+  else
+    std::memcpy(idx_bytes.data(), idx32.data(), idx32.size() * 4);
   std::vector<double> coeff(table.size() * XFDTD_N_COEFF);
   for (size_t q = 0; q < table.size(); ++q)
     std::copy(table[q].begin(), table[q].end(), coeff.begin() + q * XFDTD_N_COEFF);

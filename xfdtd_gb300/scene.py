@@ -104,8 +104,9 @@ class SceneDesc(C.Structure):
                 ("monitors", C.POINTER(MonitorDesc)),
                 ("tfsf", TFSFDesc), ("nffft", NFFFTDesc),
                 ("voxel_materials", C.POINTER(MaterialDesc)),
-                ("voxel_index", C.POINTER(C.c_uint16)),
-                ("voxel_shape", C.c_int64 * 3)]
+                ("voxel_index", C.c_void_p),
+                ("voxel_shape", C.c_int64 * 3),
+                ("voxel_index_bytes", C.c_int32), ("reserved3", C.c_int32)]
 
 
 # ---------------------------------------------------------------- shapes ---
@@ -454,7 +455,7 @@ class Scene:
     monitors: List[_Monitor] = field(default_factory=list)
     cfl: float = 0.99
     voxel_materials: Optional[List[Material]] = None
-    voxel_index: Optional[np.ndarray] = None  # (nx, ny, nz) uint16
+    voxel_index: Optional[np.ndarray] = None  # (nx, ny, nz) material numbers
 
     def desc(self) -> SceneDesc:
         """Builds the C description.  The returned struct keeps its arrays
@@ -490,10 +491,12 @@ class Scene:
             if l.waveform is not None:
                 keep.append(l.waveform)
         if self.voxel_index is not None:
-            vi = np.ascontiguousarray(self.voxel_index, dtype=np.uint16)
+            wide = len(self.voxel_materials) > 65536
+            vi = np.ascontiguousarray(self.voxel_index, dtype=np.uint32 if wide else np.uint16)
             vm = (MaterialDesc * len(self.voxel_materials))(*[m.desc() for m in self.voxel_materials])
             keep += [vi, vm]
-            d.voxel_index = vi.ctypes.data_as(C.POINTER(C.c_uint16))
+            d.voxel_index = vi.ctypes.data
+            d.voxel_index_bytes = 4 if wide else 2
             d.voxel_materials = vm
             d.n_voxel_materials = len(self.voxel_materials)
             d.voxel_shape[:] = list(vi.shape)
