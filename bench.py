@@ -40,6 +40,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 from xfdtd_gb300 import configs  # noqa: E402
+from xfdtd_gb300 import scene as S  # noqa: E402
 
 CONFIG_NAME = "dielectric_sphere"
 METRIC = "Mcell-updates/s"
@@ -268,7 +269,7 @@ def run_batched_form(args, local):
     batch, against the same problems run one after another with the plain
     single-simulation kernels on the same GPU.  Both timed with CUDA events
     over the step loops (set-up excluded), FP32."""
-    from xfdtd_gb300 import configs
+    import xfdtd_gb300 as X
     probs = configs.batched_scatterers(n=args.batch_problems)
     members = [X.Simulation(sc, st, precision="fp32", fused=False, autotune=False, device=local) for sc, st in probs]
     cells = [m.n[0] * m.n[1] * m.n[2] for m in members]
@@ -291,6 +292,65 @@ def run_batched_form(args, local):
             "speedup_vs_sequential": ms_s / ms_b,
             "workload": "64 dielectric-sphere problems, interior U{32..160}^3 + 8-cell CPML, "
                         "steps U{500..1500}, seeds 4000+i"}
+
+
+def run_adjoint_form(args, local):
+    """The adjoint form: dL/d eps_r over a 64 x 64 x 32 design region of the
+    160 x 160 x 96 (+ 10-cell CPML) dipole problem, L = sum of Ez^2 over a
+    64 x 64 plane over the last 400 of 2000 steps, FP32 forward and reverse
+    passes with checkpoints every 100 steps.  Times: the plain FP32 forward
+    run (CUDA events), the checkpointed forward and the backward pass (wall
+    clock around the synchronous calls).  Check: central differences of the
+    FP64 forward loss (eps_r +- 1e-4, as float) at `adjoint_fd` seeded
+    design voxels."""
+    import xfdtd_gb300 as X
+    sc, st, spec = configs.adjoint_dipole()
+    keys = ("design_lo", "design_hi", "plane_axis", "plane_index", "plane_lo", "plane_hi", "t_begin", "t_end",
+            "loss_comp", "checkpoint_every")
+    sa = {q: spec[q] for q in keys}
+    plain = X.Simulation(sc, st, precision="fp32", fused=False, autotune=False, device=local)
+    fwd_ms = plain.step_timed(st)
+    cells = plain.n[0] * plain.n[1] * plain.n[2]
+    del plain
+    g = X.Simulation(sc, st, precision="fp32", fused=False, autotune=False, device=local)
+    t0 = time.perf_counter()
+    loss = g.adjoint_forward(**sa)
+    t1 = time.perf_counter()
+    ge, _ = g.adjoint_backward()
+    t2 = time.perf_counter()
+    del g
+    out = {"grid": cells, "steps": st, "design_cells": int(ge.size), "loss": loss,
+           "forward_ms": fwd_ms, "checkpointed_forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
+           "backward_over_forward": (t2 - t1) * 1e3 / fwd_ms,
+           "gradient_over_forward": (t2 - t0) * 1e3 / fwd_ms,
+           "value": cells * st / ((t2 - t1)) / 1e6, "unit": "Mcell-updates/s (reverse pass)",
+           "checkpoint_every": spec["checkpoint_every"]}
+    if args.adjoint_fd > 0:
+        import copy
+        rng = np.random.default_rng(5002)
+        dsz = ge.shape
+        picks = [tuple(int(rng.integers(0, n)) for n in dsz) for _ in range(args.adjoint_fd)]
+        sb = dict(sa, checkpoint_every=st)   # one checkpoint: the FD runs only need the loss
+
+        def loss_with(cell, eps):
+            sc2 = copy.copy(sc)
+            sc2.voxel_materials = list(sc.voxel_materials)
+            q = 1 + int(np.ravel_multi_index(cell, dsz))
+            e = float(np.float32(eps))
+            sc2.voxel_materials[q] = S.Material("d", e, 1.0, 0.0, 0.0)
+            s64 = X.Simulation(sc2, st, precision="fp64", fused=False, autotune=False, device=local)
+            return s64.adjoint_forward(**sb), e
+
+        rel = []
+        for cell in picks:
+            e0 = float(spec["eps"][cell])
+            lp, ep = loss_with(cell, e0 + 1e-4)
+            lm, em = loss_with(cell, e0 - 1e-4)
+            fd = (lp - lm) / (ep - em)
+            rel.append(abs(ge[cell] - fd) / abs(fd))
+        out["fd_check"] = {"voxels": len(picks), "h": 1e-4, "forward": "fp64",
+                           "max_rel_err": float(max(rel)), "median_rel_err": float(np.median(rel))}
+    return out
 
 
 def ours_arm(args, world, rank, local, grp):
@@ -321,14 +381,14 @@ def ours_arm(args, world, rank, local, grp):
 
     # roofline of the dominant kernel (largest share of device time)
     peak, peak_kind = _peaks()
+    # the TFSF 1-D line runs on a side stream beside update_e: its event time
+    # overlaps the main stream's and is reported apart from the shares
+    side = {k: prof.pop(k) for k in SIDE_STREAM_KERNELS if k in prof}
     dom = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_n = prof[dom]
     slabs = _slab_layers(sc)
     alg = algorithmic_bytes(n, slabs, args.precision, dom)
     achieved = alg / (dom_ms / dom_n / 1e3) / 1e9
-    # the TFSF 1-D line runs on a side stream beside update_e: its event time
-    # overlaps the main stream's and is reported apart from the shares
-    side = {k: prof.pop(k) for k in SIDE_STREAM_KERNELS if k in prof}
     total_prof = sum(v[0] for v in prof.values())
     shares = {k: round(v[0] / total_prof, 4) for k, v in prof.items()}
     shares.update({f"{k} (concurrent)": round(v[0] / total_prof, 4) for k, v in side.items()})
@@ -362,6 +422,7 @@ def ours_arm(args, world, rank, local, grp):
         del s64
 
     batched = run_batched_form(args, local) if (args.batch_problems > 0 and rank == 0) else None
+    adjoint = run_adjoint_form(args, local) if (args.adjoint and rank == 0) else None
 
     cpu = None
     if rank == 0 and world == 1 and args.cpu_sample > 0:
@@ -396,6 +457,7 @@ def ours_arm(args, world, rank, local, grp):
         "cpu_baseline": cpu,
         "fp64_form": fp64,
         "batched_form": batched,
+        "adjoint_form": adjoint,
     }
     print(json.dumps(line), flush=True)
 
@@ -411,6 +473,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=8, help="oracle steps timed for cpu_baseline (0: skip)")
     ap.add_argument("--ref-budget", type=float, default=120.0, help="seconds of oracle work for --impl reference")
     ap.add_argument("--batch-problems", type=int, default=64, help="problems of the batched form (0: skip)")
+    ap.add_argument("--adjoint", type=int, default=1, help="run the adjoint form (0: skip)")
+    ap.add_argument("--adjoint-fd", type=int, default=16, help="design voxels of the adjoint FD check (0: skip)")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.impl == "reference":

@@ -196,10 +196,29 @@ __global__ void __launch_bounds__(256) k_adj_h(AdjParams<T, I> a) {
   if (k > nz || j > ny || i > nx) return;
   const unsigned b = static_cast<unsigned>(i) * static_cast<unsigned>(p.d.si) +
                      static_cast<unsigned>(j) * static_cast<unsigned>(p.d.sj) + static_cast<unsigned>(k);
-  // W gathers (E cells reading H at this cell)
-  const T gx = e_weight(a, i, j, k, 2) - e_weight(a, i, j, k + 1, 2) + e_weight(a, i, j, k, 4) - e_weight(a, i, j + 1, k, 4);
-  const T gy = e_weight(a, i, j, k, 0) - e_weight(a, i, j, k + 1, 0) + e_weight(a, i, j, k, 5) - e_weight(a, i + 1, j, k, 5);
-  const T gz = e_weight(a, i, j, k, 1) - e_weight(a, i, j + 1, k, 1) + e_weight(a, i, j, k, 3) - e_weight(a, i + 1, j, k, 3);
+  // W gathers (E cells reading H at this cell).  When the E cells at this
+  // index and one above on each axis are plain (main update, no CPML), a
+  // weight is the E cell's curl coefficient times its lE.
+  const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
+  const bool plain = i < nx && j < ny && k < nz &&
+                     !((__ldg(p.flags[0] + i) | __ldg(p.flags[0] + i + 1) | __ldg(p.flags[1] + j) |
+                        __ldg(p.flags[1] + j + 1) | __ldg(p.flags[2] + k) | __ldg(p.flags[2] + k + 1)) &
+                       (kSpecialE | kSpecialH));
+  T gx, gy, gz;
+  if (plain) {
+    const T *c0 = p.table + static_cast<unsigned>(__ldg(p.idx + b)) * 18;
+    const T *ck = p.table + static_cast<unsigned>(__ldg(p.idx + b + 1)) * 18;
+    const T *cj = p.table + static_cast<unsigned>(__ldg(p.idx + b + usj)) * 18;
+    const T *ci = p.table + static_cast<unsigned>(__ldg(p.idx + b + usi)) * 18;
+    const T *lx = a.lE[0], *ly = a.lE[1], *lz = a.lE[2];
+    gx = mul(c0[5], ly[b]) - mul(ck[5], ly[b + 1]) + mul(c0[7], lz[b]) - mul(cj[7], lz[b + usj]);
+    gy = mul(c0[1], lx[b]) - mul(ck[1], lx[b + 1]) + mul(c0[8], lz[b]) - mul(ci[8], lz[b + usi]);
+    gz = mul(c0[2], lx[b]) - mul(cj[2], lx[b + usj]) + mul(c0[4], ly[b]) - mul(ci[4], ly[b + usi]);
+  } else {
+    gx = e_weight(a, i, j, k, 2) - e_weight(a, i, j, k + 1, 2) + e_weight(a, i, j, k, 4) - e_weight(a, i, j + 1, k, 4);
+    gy = e_weight(a, i, j, k, 0) - e_weight(a, i, j, k + 1, 0) + e_weight(a, i, j, k, 5) - e_weight(a, i + 1, j, k, 5);
+    gz = e_weight(a, i, j, k, 1) - e_weight(a, i, j + 1, k, 1) + e_weight(a, i, j, k, 3) - e_weight(a, i + 1, j, k, 3);
+  }
   const T *c = p.table + static_cast<unsigned>(__ldg(p.idx + b)) * 18 + 9;
   const int xs = p.cp[0].n_layers ? p.cp[0].slot_h[i] : -1;
   const int ys = p.cp[1].n_layers ? p.cp[1].slot_h[j] : -1;
@@ -337,10 +356,27 @@ __global__ void __launch_bounds__(256) k_adj_e(AdjParams<T, I> a) {
         L[a.loss_comp] += T(2) * a.plane_rec[(u - a.plo[0]) * nv + (v - a.plo[1])];
       }
     }
-    // U gathers (H cells of step t-1 reading E at this cell)
-    if (ex) L[0] += h_weight(a, i, j, k - 1, 3) - h_weight(a, i, j, k, 3) + h_weight(a, i, j - 1, k, 4) - h_weight(a, i, j, k, 4);
-    if (ey) L[1] += h_weight(a, i, j, k - 1, 0) - h_weight(a, i, j, k, 0) + h_weight(a, i - 1, j, k, 5) - h_weight(a, i, j, k, 5);
-    if (ez) L[2] += h_weight(a, i, j - 1, k, 1) - h_weight(a, i, j, k, 1) + h_weight(a, i - 1, j, k, 2) - h_weight(a, i, j, k, 2);
+    // U gathers (H cells of step t-1 reading E at this cell); plain H cells
+    // at this index and one below on each axis: coefficient times lH
+    const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
+    const bool plain = i >= 1 && j >= 1 && k >= 1 && i < nx && j < ny && k < nz &&
+                       !((__ldg(p.flags[0] + i) | __ldg(p.flags[0] + i - 1) | __ldg(p.flags[1] + j) |
+                          __ldg(p.flags[1] + j - 1) | __ldg(p.flags[2] + k) | __ldg(p.flags[2] + k - 1)) &
+                         (kSpecialE | kSpecialH));
+    if (plain) {
+      const T *c0 = p.table + static_cast<unsigned>(__ldg(p.idx + b)) * 18 + 9;
+      const T *ck = p.table + static_cast<unsigned>(__ldg(p.idx + b - 1)) * 18 + 9;
+      const T *cj = p.table + static_cast<unsigned>(__ldg(p.idx + b - usj)) * 18 + 9;
+      const T *ci = p.table + static_cast<unsigned>(__ldg(p.idx + b - usi)) * 18 + 9;
+      const T *hx = a.lH[0], *hy = a.lH[1], *hz = a.lH[2];
+      L[0] += mul(ck[5], hy[b - 1]) - mul(c0[5], hy[b]) + mul(cj[7], hz[b - usj]) - mul(c0[7], hz[b]);
+      L[1] += mul(ck[1], hx[b - 1]) - mul(c0[1], hx[b]) + mul(ci[8], hz[b - usi]) - mul(c0[8], hz[b]);
+      L[2] += mul(cj[2], hx[b - usj]) - mul(c0[2], hx[b]) + mul(ci[4], hy[b - usi]) - mul(c0[4], hy[b]);
+    } else {
+      if (ex) L[0] += h_weight(a, i, j, k - 1, 3) - h_weight(a, i, j, k, 3) + h_weight(a, i, j - 1, k, 4) - h_weight(a, i, j, k, 4);
+      if (ey) L[1] += h_weight(a, i, j, k - 1, 0) - h_weight(a, i, j, k, 0) + h_weight(a, i - 1, j, k, 5) - h_weight(a, i, j, k, 5);
+      if (ez) L[2] += h_weight(a, i, j - 1, k, 1) - h_weight(a, i, j, k, 1) + h_weight(a, i - 1, j, k, 2) - h_weight(a, i, j, k, 2);
+    }
   }
   if (ex) a.lE[0][b] = L[0];
   if (ey) a.lE[1][b] = L[1];
