@@ -353,6 +353,31 @@ def run_adjoint_form(args, local):
     return out
 
 
+def run_heterogeneous_form(args, local):
+    """The bandwidth-bound heterogeneous medium: 512 x 512 x 384 + 10-cell
+    CPML (532 x 532 x 404 cells), 256-entry voxel material table, soft point
+    source, 64 Ez probes, FP32; `hetero_steps` steps timed with CUDA events."""
+    import xfdtd_gb300 as X
+    sc, st = configs.heterogeneous(steps=args.hetero_steps + 3)
+    g = X.Simulation(sc, st, precision="fp32", device=local, profile=True)
+    g.step(3)
+    g.synchronize()
+    g.profile_reset()
+    ms = g.step_timed(args.hetero_steps)
+    prof = g.profile()
+    cells = g.n[0] * g.n[1] * g.n[2]
+    dom = max(prof, key=lambda k: prof[k][0])
+    slabs = _slab_layers(sc)
+    alg = algorithmic_bytes(g.n, slabs, "fp32", dom)
+    gbs = alg / (prof[dom][0] / prof[dom][1] / 1e3) / 1e9
+    peak, kind = _peaks()
+    g.check_finite()
+    return {"grid": list(g.n), "cells": cells, "steps": args.hetero_steps,
+            "value": cells * args.hetero_steps / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms / args.hetero_steps,
+            "dominant_kernel": dom, "achieved_GBs": gbs, "frac": gbs / peak, "peak_source": kind,
+            "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (cells * 4 / 1e6)}
+
+
 def ours_arm(args, world, rank, local, grp):
     import xfdtd_gb300 as X
     X.build()
@@ -423,6 +448,7 @@ def ours_arm(args, world, rank, local, grp):
 
     batched = run_batched_form(args, local) if (args.batch_problems > 0 and rank == 0) else None
     adjoint = run_adjoint_form(args, local) if (args.adjoint and rank == 0) else None
+    hetero = run_heterogeneous_form(args, local) if (args.hetero_steps > 0 and rank == 0) else None
 
     cpu = None
     if rank == 0 and world == 1 and args.cpu_sample > 0:
@@ -458,6 +484,7 @@ def ours_arm(args, world, rank, local, grp):
         "fp64_form": fp64,
         "batched_form": batched,
         "adjoint_form": adjoint,
+        "heterogeneous_form": hetero,
     }
     print(json.dumps(line), flush=True)
 
@@ -474,6 +501,7 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=120.0, help="seconds of oracle work for --impl reference")
     ap.add_argument("--batch-problems", type=int, default=64, help="problems of the batched form (0: skip)")
     ap.add_argument("--adjoint", type=int, default=1, help="run the adjoint form (0: skip)")
+    ap.add_argument("--hetero-steps", type=int, default=100, help="steps of the heterogeneous-medium form (0: skip)")
     ap.add_argument("--adjoint-fd", type=int, default=16, help="design voxels of the adjoint FD check (0: skip)")
     args = ap.parse_args()
     world, rank, local = _dist()

@@ -23,6 +23,8 @@ def main():
     ap.add_argument("--scale", type=int, default=1)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--volume", default="auto", choices=["auto", "fused", "split"],
+                    help="volume kernels: autotuned choice, the fused E/H sweep, or the split E and H kernels")
     ap.add_argument("--out", default=None)
     args = ap.parse_args()
     build()
@@ -32,14 +34,15 @@ def main():
     if args.out and sc.nffft is not None:
         sc.nffft.output_dir_path = args.out
     t0 = time.perf_counter()
-    sim = Simulation(sc, steps, precision=args.precision, graph=not args.no_graph)
+    fused = {"auto": None, "fused": True, "split": False}[args.volume]
+    sim = Simulation(sc, steps, precision=args.precision, graph=not args.no_graph, fused=fused)
     t1 = time.perf_counter()
     ms = sim.step_timed(steps)
     sim.synchronize()
     cells = sim.n[0] * sim.n[1] * sim.n[2]
     res = {"config": args.config, "grid": sim.n, "steps": steps, "precision": args.precision,
            "setup_s": t1 - t0, "ms_per_step": ms / steps, "Mcell_updates_per_s": cells * steps / ms / 1e3,
-           "device_bytes": sim.device_bytes()}
+           "device_bytes": sim.device_bytes(), "volume_kernels": sim.kernel_variants()}
     if args.out:
         os.makedirs(args.out, exist_ok=True)
         sim.output()
