@@ -383,7 +383,8 @@ def ours_arm(args, world, rank, local, grp):
     X.build()
     sc, _ = configs.dielectric_sphere()
     total = args.warmup + args.steps
-    sim = X.Simulation(sc, total, precision=args.precision, graph=False, profile=True, device=local)
+    fused = {"auto": None, "fused": True, "split": False}[args.volume]
+    sim = X.Simulation(sc, total, precision=args.precision, graph=False, profile=True, device=local, fused=fused)
     n = sim.n
     cells = n[0] * n[1] * n[2]
     sim.step(args.warmup)
@@ -422,7 +423,7 @@ def ours_arm(args, world, rank, local, grp):
     # e2e: one whole job through the public API, host scene to host results
     grp.barrier()
     t0 = time.perf_counter()
-    job = X.Simulation(sc, args.steps, precision=args.precision, graph=True, device=local)
+    job = X.Simulation(sc, args.steps, precision=args.precision, graph=True, device=local, fused=fused)
     job.step(args.steps)
     rcs = job.rcs_db()
     t1 = time.perf_counter()
@@ -466,7 +467,7 @@ def ours_arm(args, world, rank, local, grp):
                                "dx 2 mm, eps_r 4 sphere r=60 cells, TFSF x-pol +z Gaussian, NF-FF 1/2/3 GHz",
                    "cells": cells, "grid": list(n), "precision_form": args.precision,
                    "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (cells * (4 if args.precision == 'fp32' else 8) / 1e6),
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}", "volume_kernels": args.volume},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": NCU_TRAFFIC.get((dom, args.precision, tuple(n))),
@@ -500,6 +501,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=8, help="oracle steps timed for cpu_baseline (0: skip)")
     ap.add_argument("--ref-budget", type=float, default=120.0, help="seconds of oracle work for --impl reference")
     ap.add_argument("--batch-problems", type=int, default=64, help="problems of the batched form (0: skip)")
+    ap.add_argument("--volume", default="split", choices=["split", "fused", "auto"],
+                    help="volume kernels of the main workload: the split E and H kernels (the faster on this "
+                         "workload), the fused E/H sweep, or the autotuner's choice")
     ap.add_argument("--adjoint", type=int, default=1, help="run the adjoint form (0: skip)")
     ap.add_argument("--hetero-steps", type=int, default=100, help="steps of the heterogeneous-medium form (0: skip)")
     ap.add_argument("--adjoint-fd", type=int, default=16, help="design voxels of the adjoint FD check (0: skip)")

@@ -26,8 +26,13 @@ def main():
     ap.add_argument("--volume", default="auto", choices=["auto", "fused", "split"],
                     help="volume kernels: autotuned choice, the fused E/H sweep, or the split E and H kernels")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--adjoint", action="store_true",
+                    help="run the adjoint-gradient problem (forward with checkpoints, then backward) instead")
     args = ap.parse_args()
     build()
+    if args.adjoint:
+        run_adjoint(args)
+        return
     sc, steps = configs.CONFIGS[args.config](scale=args.scale)
     if args.steps is not None:
         steps = args.steps
@@ -47,6 +52,24 @@ def main():
         os.makedirs(args.out, exist_ok=True)
         sim.output()
     print(json.dumps(res))
+
+
+def run_adjoint(args):
+    sc, steps, spec = configs.adjoint_dipole(scale=args.scale)
+    if args.steps is not None:
+        steps = args.steps
+        spec["t_begin"], spec["t_end"] = steps - steps // 5, steps
+    keys = ("design_lo", "design_hi", "plane_axis", "plane_index", "plane_lo", "plane_hi", "t_begin", "t_end",
+            "loss_comp", "checkpoint_every")
+    sim = Simulation(sc, steps, precision=args.precision, fused=False, autotune=False)
+    t0 = time.perf_counter()
+    loss = sim.adjoint_forward(**{k: spec[k] for k in keys})
+    t1 = time.perf_counter()
+    ge, _ = sim.adjoint_backward()
+    t2 = time.perf_counter()
+    print(json.dumps({"config": "adjoint_dipole", "scale": args.scale, "grid": sim.n, "steps": steps,
+                      "loss": loss, "forward_s": t1 - t0, "backward_s": t2 - t1,
+                      "grad_eps_absmax": float(abs(ge).max())}))
 
 
 if __name__ == "__main__":
