@@ -8,7 +8,7 @@
 // range of the list and loading a simulation's parameters into shared
 // memory when its range crosses into the next simulation.
 // Per cell the work is that of the single-simulation split kernels
-// (e_plain / e_cell, h_plain / h_cell, tfsf_e_surface / tfsf_h_surface,
+// (e_fast / e_cell_general, h_fast / h_cell_general, tfsf_e_surface / tfsf_h_surface,
 // nffft_sample / nffft_fold, tfsf_aux_block), so a batched simulation gives
 // the same bits as the same simulation run alone.
 #pragma once
@@ -58,9 +58,17 @@ __global__ void __launch_bounds__(256, 6) k_volume_batch(const VolParams<T, I> *
   const VolParams<T, I> &p = all[it.sim];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int i = it.tile >> 16, j = ((it.tile >> 8) & 0xff) * 8 + ty, k = (it.tile & 0xff) * 32 + tx;
-  if (k > p.d.nz || j > p.d.ny) return;
-  if (E_SIDE) e_cell<T, I>(p, p.table, 18, i, j, k);
-  else h_cell<T, I>(p, p.table + 9, 18, i, j, k);
+  const bool valid = k <= p.d.nz && j <= p.d.ny;
+  const bool plain = valid && (E_SIDE ? e_plain_cell(p, i, j, k) : h_plain_cell(p, i, j, k));
+  const bool fast = __all_sync(0xffffffffu, plain || !valid);   // one path per warp (row)
+  if (!valid) return;
+  if (E_SIDE) {
+    if (fast) e_fast<T, I, 1>(p, p.table, 18, i, j, k);
+    else e_cell_general<T, I>(p, p.table, 18, i, j, k);
+  } else {
+    if (fast) h_fast<T, I, 1>(p, p.table + 9, 18, i, j, k);
+    else h_cell_general<T, I>(p, p.table + 9, 18, i, j, k);
+  }
 }
 
 // TFSF E or H corrections: tile = 256 consecutive surface cells.

@@ -24,7 +24,9 @@
 //
 // Cells whose three indices are all flagged "plain" (not an outer wall, not
 // in a CPML slab) take a fast path with only the main update, written with
-// the same expression as the general path so both give identical bits.
+// the same expression as the general path so both give identical bits.  The
+// choice is made per warp: a warp with any non-plain cell runs the general
+// path for all its cells.
 #pragma once
 
 #include "common.cuh"
@@ -271,10 +273,25 @@ __device__ __forceinline__ void h_general(const VolParams<T, I> &p, const T *c, 
   }
 }
 
-// E update of one cell of the in-place split kernel (fast path when the
-// cell is plain, else the general path).
+// Whether cell (i, j, k) is plain for the E update (no outer wall, no CPML
+// slab): then e_fast applies.  Indices are clamped to the box.
 template <typename T, typename I>
-__device__ __forceinline__ void e_cell(const VolParams<T, I> &p, const T *tab, int ts, int i, int j, int k) {
+__device__ __forceinline__ bool e_plain_cell(const VolParams<T, I> &p, int i, int j, int k) {
+  return !((__ldg(p.flags[0] + min(i, p.d.nx)) | __ldg(p.flags[1] + min(j, p.d.ny)) | __ldg(p.flags[2] + min(k, p.d.nz))) &
+           kSpecialE);
+}
+template <typename T, typename I>
+__device__ __forceinline__ bool h_plain_cell(const VolParams<T, I> &p, int i, int j, int k) {
+  return !((__ldg(p.flags[0] + min(i, p.d.nx)) | __ldg(p.flags[1] + min(j, p.d.ny)) | __ldg(p.flags[2] + min(k, p.d.nz))) &
+           kSpecialH);
+}
+
+// E update of one cell by the general path.  It serves any cell: a plain
+// cell gets the bits of the fast path (same expressions, no CPML terms).
+// The volume kernels decide per warp: a warp whose cells are not all plain
+// runs this path for all of them, so that no warp runs both paths.
+template <typename T, typename I>
+__device__ __forceinline__ void e_cell_general(const VolParams<T, I> &p, const T *tab, int ts, int i, int j, int k) {
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
   const T *__restrict__ Hx = p.H[0];
@@ -283,18 +300,6 @@ __device__ __forceinline__ void e_cell(const VolParams<T, I> &p, const T *tab, i
   T *__restrict__ Ex = p.E[0];
   T *__restrict__ Ey = p.E[1];
   T *__restrict__ Ez = p.E[2];
-  if (!((__ldg(p.flags[0] + i) | __ldg(p.flags[1] + j) | __ldg(p.flags[2] + k)) & kSpecialE)) {
-    const ECurl<T> h{__ldg(Hx + b),       __ldg(Hy + b),       __ldg(Hz + b),
-                     __ldg(Hx + b - 1),   __ldg(Hy + b - 1),   __ldg(Hx + b - usj),
-                     __ldg(Hz + b - usj), __ldg(Hy + b - usi), __ldg(Hz + b - usi)};
-    const T *c = tab + static_cast<unsigned>(__ldg(p.idx + b)) * ts;
-    T ex = Ex[b], ey = Ey[b], ez = Ez[b];
-    e_plain(c, h, ex, ey, ez);
-    Ex[b] = ex;
-    Ey[b] = ey;
-    Ez[b] = ez;
-    return;
-  }
   ECurl<T> h;
   h.hx = __ldg(Hx + b);
   h.hy = __ldg(Hy + b);
@@ -366,22 +371,25 @@ __global__ void __launch_bounds__(256, MINB) k_update_e(VolParams<T, I> p) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int i0 = (blockIdx.z * blockDim.z + threadIdx.z) * NC;
-  if (k > p.d.nz || j > p.d.ny || i0 > p.d.nx) return;
-  bool plain = !((__ldg(p.flags[1] + j) | __ldg(p.flags[2] + k)) & kSpecialE) && i0 + NC - 1 <= p.d.nx;
+  const bool valid = k <= p.d.nz && j <= p.d.ny && i0 <= p.d.nx;
+  bool plain = valid && i0 + NC - 1 <= p.d.nx;
 #pragma unroll
-  for (int q = 0; q < NC; ++q) plain = plain && !(__ldg(p.flags[0] + min(i0 + q, p.d.nx)) & kSpecialE);
-  if (plain) {
+  for (int q = 0; q < NC; ++q) plain = plain && e_plain_cell(p, i0 + q, j, k);
+  // one path per warp (blockDim.x is a multiple of 32: a warp is one row)
+  const bool fast = __all_sync(0xffffffffu, plain || !valid);
+  if (!valid) return;
+  if (fast) {
     e_fast<T, I, NC>(p, tab, ts, i0, j, k);
     return;
   }
 #pragma unroll
   for (int q = 0; q < NC; ++q)
-    if (i0 + q <= p.d.nx) e_cell<T, I>(p, tab, ts, i0 + q, j, k);
+    if (i0 + q <= p.d.nx) e_cell_general<T, I>(p, tab, ts, i0 + q, j, k);
 }
 
-// H update of one cell of the in-place split kernel.
+// H update of one cell by the general path (any cell, as e_cell_general).
 template <typename T, typename I>
-__device__ __forceinline__ void h_cell(const VolParams<T, I> &p, const T *tab, int ts, int i, int j, int k) {
+__device__ __forceinline__ void h_cell_general(const VolParams<T, I> &p, const T *tab, int ts, int i, int j, int k) {
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
@@ -391,18 +399,6 @@ __device__ __forceinline__ void h_cell(const VolParams<T, I> &p, const T *tab, i
   T *__restrict__ Hx = p.H[0];
   T *__restrict__ Hy = p.H[1];
   T *__restrict__ Hz = p.H[2];
-  if (!((__ldg(p.flags[0] + i) | __ldg(p.flags[1] + j) | __ldg(p.flags[2] + k)) & kSpecialH)) {
-    const HCurl<T> e{__ldg(Ex + b),       __ldg(Ey + b),       __ldg(Ez + b),
-                     __ldg(Ex + b + 1),   __ldg(Ey + b + 1),   __ldg(Ex + b + usj),
-                     __ldg(Ez + b + usj), __ldg(Ey + b + usi), __ldg(Ez + b + usi)};
-    const T *c = tab + static_cast<unsigned>(__ldg(p.idx + b)) * ts;
-    T hx = Hx[b], hy = Hy[b], hz = Hz[b];
-    h_plain(c, e, hx, hy, hz);
-    Hx[b] = hx;
-    Hy[b] = hy;
-    Hz[b] = hz;
-    return;
-  }
   HCurl<T> e;
   e.ex = __ldg(Ex + b);
   e.ey = __ldg(Ey + b);
@@ -470,17 +466,19 @@ __global__ void __launch_bounds__(256, MINB) k_update_h(VolParams<T, I> p) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int i0 = (blockIdx.z * blockDim.z + threadIdx.z) * NC;
-  if (k > p.d.nz || j > p.d.ny || i0 > p.d.nx) return;
-  bool plain = !((__ldg(p.flags[1] + j) | __ldg(p.flags[2] + k)) & kSpecialH) && i0 + NC - 1 <= p.d.nx;
+  const bool valid = k <= p.d.nz && j <= p.d.ny && i0 <= p.d.nx;
+  bool plain = valid && i0 + NC - 1 <= p.d.nx;
 #pragma unroll
-  for (int q = 0; q < NC; ++q) plain = plain && !(__ldg(p.flags[0] + min(i0 + q, p.d.nx)) & kSpecialH);
-  if (plain) {
+  for (int q = 0; q < NC; ++q) plain = plain && h_plain_cell(p, i0 + q, j, k);
+  const bool fast = __all_sync(0xffffffffu, plain || !valid);
+  if (!valid) return;
+  if (fast) {
     h_fast<T, I, NC>(p, tab, ts, i0, j, k);
     return;
   }
 #pragma unroll
   for (int q = 0; q < NC; ++q)
-    if (i0 + q <= p.d.nx) h_cell<T, I>(p, tab, ts, i0 + q, j, k);
+    if (i0 + q <= p.d.nx) h_cell_general<T, I>(p, tab, ts, i0 + q, j, k);
 }
 
 }  // namespace xg
