@@ -161,15 +161,18 @@ SIDE_STREAM_KERNELS = ("tfsf_aux",)
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
 # from an ncu --set full capture of that kernel on this workload
 # (python -m xfdtd_gb300.run --config dielectric_sphere --steps 24 --precision fp32 --no-graph).
-NCU_TRAFFIC = {("update_e", "fp32", (280, 280, 280)): 621.793024e6 + 318.648320e6}
+NCU_TRAFFIC = {}
 
 
-def algorithmic_bytes(n, slab_layers, precision: str, kernel: str) -> float:
-    """Bytes one launch of a volume kernel must move at least.  Split E (or
-    H) kernel: read the 3 own components and the 3 curl components, write
-    the 3 own components, read the 1-byte material index; inside CPML slabs
-    read and write one psi per (component, slab axis) pair (2 per slab
-    axis).  Fused sweep (E and H of one step): read and write all 6
+def algorithmic_bytes(n, slab_layers, precision: str, kernel: str, split=None) -> float:
+    """Bytes one launch of a volume kernel must move at least.  E (or H)
+    update: per cell read the 3 own components and the 3 curl components,
+    write the 3 own components, read the 1-byte material index; inside CPML
+    slabs read and write one psi per (component, slab axis) pair (2 per
+    slab axis).  The update runs as two kernels: the interior kernel over
+    the plain cells (split["e_interior"] / ["h_interior"]) and the shell
+    kernel over walls and slabs (["e_shell"] / ["h_shell"], all psi
+    traffic).  Fused sweep (E and H of one step): read and write all 6
     components once and the index once; psi traffic of both halves."""
     nx, ny, nz = n
     cells = nx * ny * nz
@@ -177,6 +180,10 @@ def algorithmic_bytes(n, slab_layers, precision: str, kernel: str) -> float:
     slab_cells = (slab_layers[0] * ny * nz + slab_layers[1] * nx * nz + slab_layers[2] * nx * ny)
     if kernel == "sweep_eh":
         return cells * (12 * w + 1) + slab_cells * 2 * 2 * w * 2
+    if split is not None and kernel in ("update_e", "update_h"):
+        return split[kernel[-1] + "_interior"] * (9 * w + 1)
+    if split is not None and kernel in ("update_e_shell", "update_h_shell"):
+        return split[kernel[7] + "_shell"] * (9 * w + 1) + slab_cells * 2 * 2 * w
     return cells * (9 * w + 1) + slab_cells * 2 * 2 * w
 
 
@@ -368,7 +375,7 @@ def run_heterogeneous_form(args, local):
     cells = g.n[0] * g.n[1] * g.n[2]
     dom = max(prof, key=lambda k: prof[k][0])
     slabs = _slab_layers(sc)
-    alg = algorithmic_bytes(g.n, slabs, "fp32", dom)
+    alg = algorithmic_bytes(g.n, slabs, "fp32", dom, g.volume_split())
     gbs = alg / (prof[dom][0] / prof[dom][1] / 1e3) / 1e9
     peak, kind = _peaks()
     g.check_finite()
@@ -413,7 +420,8 @@ def ours_arm(args, world, rank, local, grp):
     dom = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_n = prof[dom]
     slabs = _slab_layers(sc)
-    alg = algorithmic_bytes(n, slabs, args.precision, dom)
+    split = sim.volume_split()
+    alg = algorithmic_bytes(n, slabs, args.precision, dom, split)
     achieved = alg / (dom_ms / dom_n / 1e3) / 1e9
     total_prof = sum(v[0] for v in prof.values())
     shares = {k: round(v[0] / total_prof, 4) for k, v in prof.items()}
@@ -441,7 +449,7 @@ def ours_arm(args, world, rank, local, grp):
         ms64 = s64.step_timed(args.fp64_steps)
         p64 = s64.profile()
         d64 = max(p64, key=lambda k: p64[k][0])
-        a64 = algorithmic_bytes(n, slabs, "fp64", d64) / (p64[d64][0] / p64[d64][1] / 1e3) / 1e9
+        a64 = algorithmic_bytes(n, slabs, "fp64", d64, s64.volume_split()) / (p64[d64][0] / p64[d64][1] / 1e3) / 1e9
         fp64 = {"value": cells * args.fp64_steps / (ms64 / 1e3) / 1e6, "unit": UNIT, "steps": args.fp64_steps,
                 "ms_per_step": ms64 / args.fp64_steps, "dominant_kernel": d64,
                 "dominant_kernel_GBs": a64, "note": "GB300 FP64 is ~1/64 rate: this form is compute-bound"}
@@ -473,6 +481,7 @@ def ours_arm(args, world, rank, local, grp):
                      "traffic": NCU_TRAFFIC.get((dom, args.precision, tuple(n))),
                      "algorithmic_bytes_per_launch": alg, "launch_ms": dom_ms / dom_n},
         "kernel_shares": shares,
+        "volume_split_cells": split,
         "autotuned_variants": {"update_e": variants["e"], "update_h": variants["h"],
                                "trial_ms_e": [round(v, 4) for v in variants["trials_e"]],
                                "trial_ms_h": [round(v, 4) for v in variants["trials_h"]]},

@@ -214,6 +214,10 @@ int xfdtd_autotune(xfdtd_handle *h, int trials);
  * xfdtd_set_kernel_variant takes the same variant for both. */
 int xfdtd_kernel_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h, double *trial_ms);
 int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant);
+/* Cells of the split volume update: cells[0] / [1] the E update's interior
+ * (plain on every axis, the interior kernel) and shell (walls and CPML
+ * slabs, the shell kernel); cells[2] / [3] the same for H. */
+int xfdtd_volume_split(xfdtd_handle *h, int64_t cells[4]);
 /* Per-step kernel launches enqueued so far (graph replays included). */
 int xfdtd_launch_count(xfdtd_handle *h, int64_t *n);
 /* Kernel launches the engine enqueues per step for this plan. */

@@ -85,6 +85,7 @@ def libs():
         cu.xfdtd_autotune.argtypes = [C.c_void_p, C.c_int]
         cu.xfdtd_kernel_variants.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int), dp]
         cu.xfdtd_set_kernel_variant.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        cu.xfdtd_volume_split.argtypes = [C.c_void_p, P(C.c_int64)]
         cu.xfdtd_last_error.argtypes = [C.c_void_p]
         cu.xfdtd_last_error.restype = C.c_char_p
         cu.xfdtd_version.restype = C.c_char_p
@@ -303,6 +304,13 @@ class Simulation:
 
     def set_kernel_variant(self, e_variant: int, h_variant: int):
         self._check_engine(libs()[0].xfdtd_set_kernel_variant(self.engine, int(e_variant), int(h_variant)))
+
+    def volume_split(self) -> dict:
+        """Cells of the interior (plain) and shell (walls, CPML) kernels of
+        the E and H updates."""
+        c = (C.c_int64 * 4)()
+        self._check_engine(libs()[0].xfdtd_volume_split(self.engine, c))
+        return {"e_interior": c[0], "e_shell": c[1], "h_interior": c[2], "h_shell": c[3]}
 
     def transfer_bytes(self):
         """(host->device, device->host) bytes the engine has copied so far."""

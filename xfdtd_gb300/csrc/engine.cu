@@ -60,9 +60,10 @@ struct Err {
                 std::string(#call) + ": " + cudaGetErrorString(e_)};                    \
   } while (0)
 
-const char *kKernelNames[] = {"tfsf_aux", "update_e", "lumped_e", "update_h",  "nffft",   "probes",
-                              "advance",  "tfsf_e",   "tfsf_h",   "nffft_acc", "sweep_eh"};
-constexpr int kNumKernels = 11;
+const char *kKernelNames[] = {"tfsf_aux", "update_e", "lumped_e", "update_h",  "nffft",          "probes",
+                              "advance",  "tfsf_e",   "tfsf_h",   "nffft_acc", "sweep_eh",       "update_e_shell",
+                              "update_h_shell"};
+constexpr int kNumKernels = 13;
 
 }  // namespace
 
@@ -148,6 +149,12 @@ struct xfdtd_handle {
   // volume-kernel variants (autotuned)
   int var_e = 1, var_h = 1;   // L1-table variant: valid for every plan
   float tune_ms[2][16] = {};
+  // split volume update, per side (0 E, 1 H): the plain interior box and
+  // the shell around it, with their cell counts; shell register cap
+  xg::InteriorBox vin[2] = {};
+  xg::ShellBoxes vshell[2] = {};
+  long long vin_cells[2] = {}, vshell_cells[2] = {};
+  int shell_minb[2] = {4, 4};
 
   // fused E/H sweep (sweep.cuh): the state of step t+1 goes to the second
   // buffer set, swapped with the first after each step
@@ -351,18 +358,158 @@ constexpr Variant kVariants[] = {
     {1, 32, 4, 2, 2, false},  {1, 32, 4, 2, 1, false},  {8, 32, 4, 2, 2, false}, {6, 32, 4, 2, 1, true},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+static_assert(kNumVariants <= 16, "tune_ms holds 16 variants per side");
 
 // A shared-memory-table variant needs the table to fit (smem_table).
 bool variant_allowed(const xfdtd_handle *h, const Variant &v) { return !v.smem || h->smem_table; }
 
 template <typename T, typename I, bool S, int MB, int NC>
 void launch_vol_v(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, const Variant &v) {
-  dim3 block(v.bx, v.by, v.bz);
+  xg::InteriorBox in = h->vin[e_side ? 0 : 1];
+  in.k0 = (in.lo[2] / v.bx) * v.bx;   // rows of threads start on the block's k alignment
+  const int nk = in.hi[2] - in.k0 + 1, nj = in.hi[1] - in.lo[1] + 1, ni = in.hi[0] - in.lo[0] + 1;
   const int zc = v.bz * NC;
-  dim3 grid((h->d.nz + v.bx) / v.bx, (h->d.ny + v.by) / v.by, (h->d.nx + zc) / zc);
+  dim3 block(v.bx, v.by, v.bz);
+  dim3 grid((nk + v.bx - 1) / v.bx, (nj + v.by - 1) / v.by, (ni + zc - 1) / zc);
   const size_t smem = S ? h->smem_bytes : 0;
-  if (e_side) xg::k_update_e<T, I, S, MB, NC><<<grid, block, smem, h->stream>>>(p);
-  else xg::k_update_h<T, I, S, MB, NC><<<grid, block, smem, h->stream>>>(p);
+  if (e_side) xg::k_update_e<T, I, S, MB, NC><<<grid, block, smem, h->stream>>>(p, in);
+  else xg::k_update_h<T, I, S, MB, NC><<<grid, block, smem, h->stream>>>(p, in);
+}
+
+
+// Shell-kernel register caps the autotuner chooses from (minimum resident
+// 256-thread blocks per SM).
+constexpr int kShellMinb[] = {4, 6};
+constexpr int kNumShellVariants = 2;
+
+template <typename T, typename I>
+void launch_shell(xfdtd_handle *h, bool e_side, int minb = 0) {
+  const int side = e_side ? 0 : 1;
+  const xg::ShellBoxes &s = h->vshell[side];
+  if (s.blocks == 0) return;
+  if (minb == 0) minb = h->shell_minb[side];
+  const auto p = vol_params<T, I>(h);
+  const unsigned blocks = s.blocks;
+  if (minb == 6) {
+    if (e_side) xg::k_update_e_shell<T, I, 6><<<blocks, 256, 0, h->stream>>>(p, s);
+    else xg::k_update_h_shell<T, I, 6><<<blocks, 256, 0, h->stream>>>(p, s);
+  } else {
+    if (e_side) xg::k_update_e_shell<T, I, 4><<<blocks, 256, 0, h->stream>>>(p, s);
+    else xg::k_update_h_shell<T, I, 4><<<blocks, 256, 0, h->stream>>>(p, s);
+  }
+  XCHECK(cudaGetLastError());
+}
+
+// Multiply-shift constants for dividing n < 2^31 by d (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", 1994:
+// with l = ceil(log2 d) and sh = 31 + l, m = ceil(2^sh / d) gives
+// floor(n / d) = (n m) >> sh for every n < 2^31).
+void div_constants(unsigned d, unsigned long long &m, int &sh) {
+  int l = 0;
+  while ((1ull << l) < d) ++l;
+  sh = 31 + l;
+  m = ((1ull << sh) + d - 1) / d;
+}
+
+// The plain box of one side (kSpecialE, or kSpecialH, clear on all three
+// axes: no outer wall, no CPML slab) and the shell around it.  Per axis the
+// indices split into the plain run P and the special ones S (below and
+// above P).  Along k, P is narrowed to whole 32-byte sectors of a row, so
+// that the rows of every box start and end on sector boundaries (the cells
+// it gives up are plain cells of the shell, where the general path gives
+// the same bits).  The shell is S x P x P, P x S x P, P x P x S (faces, one
+// special axis), S x P x S, P x S x S (edges) and S x S x all (edges along
+// z with the corners); a box that is S along k numbers the cells below and
+// above P of one row together.  Without one contiguous plain run on every
+// axis there is no interior and the shell is the whole component box.
+void volume_boxes(xfdtd_handle *h, int side) {
+  const uint8_t bit = side == 0 ? xg::kSpecialE : xg::kSpecialH;
+  const int n[3] = {h->d.nx, h->d.ny, h->d.nz};
+  int lo[3], hi[3];
+  bool interior = true;
+  for (int a = 0; a < 3; ++a) {
+    const std::vector<uint8_t> &fl = h->axis_flags_host[a];
+    lo[a] = 0;
+    while (lo[a] <= n[a] && (fl[lo[a]] & bit)) ++lo[a];
+    hi[a] = n[a];
+    while (hi[a] >= lo[a] && (fl[hi[a]] & bit)) --hi[a];
+    if (lo[a] > hi[a]) interior = false;
+    for (int q = lo[a]; q <= hi[a]; ++q)
+      if (fl[q] & bit) interior = false;
+  }
+  const int sector = 32 / static_cast<int>(h->esize);   // cells per 32-byte sector
+  lo[2] = (lo[2] + sector - 1) / sector * sector;
+  hi[2] = (hi[2] + 1) / sector * sector - 1;
+  if (lo[2] > hi[2]) interior = false;
+  xg::InteriorBox &in = h->vin[side];
+  xg::ShellBoxes &s = h->vshell[side];
+  s = xg::ShellBoxes{};
+  long long total = 0;
+  unsigned blocks = 0;
+  // ranges per axis: 0 = below the plain run, 1 = the plain run, 2 = above,
+  // 3 = all, 4 = below and above (k only: the row's two parts together)
+  auto add = [&](int ri, int rj, int rk, int cls) {
+    const int r[3] = {ri, rj, rk};
+    int r0[3], ext[3], ksplit = 0, kgap = 0;
+    for (int a = 0; a < 3; ++a) {
+      if (r[a] == 0) r0[a] = 0, ext[a] = lo[a];
+      else if (r[a] == 1) r0[a] = lo[a], ext[a] = hi[a] - lo[a] + 1;
+      else if (r[a] == 2) r0[a] = hi[a] + 1, ext[a] = n[a] - hi[a];
+      else if (r[a] == 3) r0[a] = 0, ext[a] = n[a] + 1;
+      else r0[a] = 0, ext[a] = lo[a] + n[a] - hi[a];
+      if (ext[a] <= 0) return;
+    }
+    if (rk == 4) {
+      ksplit = lo[2];
+      kgap = hi[2] + 1 - lo[2];
+    } else {
+      ksplit = ext[2];
+    }
+    if (s.n == xg::kMaxShellBoxes) throw Err{XFDTD_ERR_STATE, "shell box table full"};
+    xg::ShellBox &b = s.b[s.n++];
+    long long cells = 1;
+    for (int a = 0; a < 3; ++a) {
+      b.lo[a] = r0[a];
+      b.ext[a] = ext[a];
+      cells *= ext[a];
+    }
+    if (cells >= (1ll << 31)) throw Err{XFDTD_ERR_INVALID_PLAN, "CPML shell box above 2^31 cells"};
+    b.ksplit = ksplit;
+    b.kgap = kgap;
+    b.cells = static_cast<unsigned>(cells);
+    b.cls = cls;
+    div_constants(static_cast<unsigned>(b.ext[2]), b.m2, b.sh2);
+    div_constants(static_cast<unsigned>(b.ext[1]), b.m1, b.sh1);
+    b.block0 = blocks;
+    blocks += static_cast<unsigned>((cells + 255) / 256);
+    total += cells;
+  };
+  if (!interior) {
+    for (int a = 0; a < 3; ++a) {
+      in.lo[a] = 0;
+      in.hi[a] = -1;
+    }
+    add(3, 3, 3, 7);
+    h->vin_cells[side] = 0;
+  } else {
+    for (int a = 0; a < 3; ++a) {
+      in.lo[a] = lo[a];
+      in.hi[a] = hi[a];
+    }
+    for (int r : {0, 2}) {
+      add(r, 1, 1, 1);   // x faces
+      add(1, r, 1, 2);   // y faces
+    }
+    add(1, 1, 4, 4);     // z faces
+    for (int r : {0, 2}) {
+      add(r, 1, 4, 5);   // x-z edges
+      add(1, r, 4, 6);   // y-z edges
+      for (int q : {0, 2}) add(r, q, 3, 7);   // x-y edges with the corners
+    }
+    h->vin_cells[side] = static_cast<long long>(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+  }
+  s.blocks = blocks;
+  h->vshell_cells[side] = total;
 }
 
 // Fused-sweep variants: register cap (minimum resident 256-thread blocks
@@ -466,8 +613,10 @@ void swap_state(xfdtd_handle *h) {
   h->cur_set ^= 1;
 }
 
+// Interior kernel of one side (nothing when the plan has no interior).
 template <typename T, typename I>
 void launch_volume(xfdtd_handle *h, bool e_side, int var = -1) {
+  if (h->vin_cells[e_side ? 0 : 1] == 0) return;
   auto p = vol_params<T, I>(h);
   if (var < 0) var = e_side ? h->var_e : h->var_h;
   const Variant &v = kVariants[var];
@@ -526,6 +675,26 @@ void autotune_t(xfdtd_handle *h, int trials) {
   }
   const bool forced = h->sweep && (h->flags & XFDTD_FLAG_FUSED_EH);
   for (int side = 0; side < 2 && !forced; ++side) {
+    // shell kernel: register cap
+    float best_shell = 0.f;
+    if (h->vshell_cells[side]) {
+      best_shell = 1e30f;
+      for (int v = 0; v < kNumShellVariants; ++v) {
+        launch_shell<T, I>(h, side == 0, kShellMinb[v]);
+        XCHECK(cudaEventRecord(a, h->stream));
+        for (int r = 0; r < trials; ++r) launch_shell<T, I>(h, side == 0, kShellMinb[v]);
+        XCHECK(cudaEventRecord(b, h->stream));
+        XCHECK(cudaEventSynchronize(b));
+        float ms = 0;
+        XCHECK(cudaEventElapsedTime(&ms, a, b));
+        if (ms / trials < best_shell) {
+          best_shell = ms / trials;
+          h->shell_minb[side] = kShellMinb[v];
+        }
+      }
+    }
+    best_split += best_shell;
+    if (!h->vin_cells[side]) continue;
     float best = 1e30f;
     int best_v = 0;
     for (int v = 0; v < kNumVariants; ++v) {
@@ -715,9 +884,16 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     prof_end(h);
     swap_state(h);
   } else {
-    prof_begin(h, 1);
-    launch_volume<T, I>(h, true);
-    prof_end(h);
+    if (h->vin_cells[0]) {
+      prof_begin(h, 1);
+      launch_volume<T, I>(h, true);
+      prof_end(h);
+    }
+    if (h->vshell_cells[0]) {
+      prof_begin(h, 11);
+      launch_shell<T, I>(h, true);
+      prof_end(h);
+    }
     if (h->n_inj || h->n_ind) {
       auto sp = sparse_params<T>(h);
       int n = std::max(h->n_inj, h->n_ind);
@@ -734,9 +910,16 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
       XCHECK(cudaGetLastError());
       prof_end(h);
     }
-    prof_begin(h, 3);
-    launch_volume<T, I>(h, false);
-    prof_end(h);
+    if (h->vin_cells[1]) {
+      prof_begin(h, 3);
+      launch_volume<T, I>(h, false);
+      prof_end(h);
+    }
+    if (h->vshell_cells[1]) {
+      prof_begin(h, 12);
+      launch_shell<T, I>(h, false);
+      prof_end(h);
+    }
   }
   if (h->tfsf) {
     XCHECK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
@@ -781,7 +964,9 @@ void enqueue_step(xfdtd_handle *h, long long s) {
 
 int launches_per_step(const xfdtd_handle *h) {
   if (h->sweep) return (h->tfsf ? 2 : 0) + 1 + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
-  return (h->tfsf ? 3 : 0) + 2 + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
+  const int vol = (h->vin_cells[0] ? 1 : 0) + (h->vshell_cells[0] ? 1 : 0) + (h->vin_cells[1] ? 1 : 0) +
+                  (h->vshell_cells[1] ? 1 : 0);
+  return (h->tfsf ? 3 : 0) + vol + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
 }
 
 // Captures g steps starting at a step index that is a multiple of the NF-FF
@@ -1082,6 +1267,8 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     h->axis_flags[a] = h->upload<uint8_t>(fl.data(), fl.size());
     h->axis_flags_host[a] = fl;
   }
+  volume_boxes(h, 0);
+  volume_boxes(h, 1);
 
   h->d_step = h->alloc<long long>(1);
   h->d_status = h->alloc<int>(1);
@@ -1412,6 +1599,16 @@ int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant) {
     if (h->gexec) {   // the captured graph holds the old launches
       cudaGraphExecDestroy(h->gexec);
       h->gexec = nullptr;
+    }
+  });
+}
+
+int xfdtd_volume_split(xfdtd_handle *h, int64_t cells[4]) {
+  if (!h || !cells) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    for (int side = 0; side < 2; ++side) {
+      cells[2 * side] = h->vin_cells[side];
+      cells[2 * side + 1] = h->vshell_cells[side];
     }
   });
 }

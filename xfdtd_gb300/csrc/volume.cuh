@@ -25,8 +25,9 @@
 // Cells whose three indices are all flagged "plain" (not an outer wall, not
 // in a CPML slab) take a fast path with only the main update, written with
 // the same expression as the general path so both give identical bits.  The
-// choice is made per warp: a warp with any non-plain cell runs the general
-// path for all its cells.
+// split kernels run the plain box and the rest (the shell) as two launches;
+// the batched kernels choose per warp: a warp with any non-plain cell runs
+// the general path for all its cells.
 #pragma once
 
 #include "common.cuh"
@@ -94,180 +95,248 @@ __device__ __forceinline__ void h_plain(const T *c, const HCurl<T> &e, T &hx, T 
   hz = yee(c[6], hz, c[7], e.ex_j - e.ex, c[8], e.ey_i - e.ey);
 }
 
-// One CPML recursion: psi' = b psi + a d (read from pr, written to pw when
-// `store`), returns the field term (c dl) psi'.
+// One CPML recursion: psi' = b psi + a d.  The field term is (c dl) psi'.
 template <typename T>
-__device__ __forceinline__ T psi_step(const T *pr, T *pw, bool store, T b, T a, T d, T c_dl, T f) {
-  const T s = fmad(a, d, mul(b, *pr));
-  if (store) *pw = s;
-  return fmad(c_dl, s, f);
+__device__ __forceinline__ T psi_next(T b, T a, T d, T psi) {
+  return fmad(a, d, mul(b, psi));
+}
+
+// The CPML profile values of one index on one axis (b, a, 1/kappa; 0, 0, 1
+// outside the slabs).
+template <typename T>
+struct AxisCoef {
+  T b, a, rk;
+};
+template <typename T>
+__device__ __forceinline__ AxisCoef<T> axis_coef(int slot, const T *b, const T *a, const T *rk, int n) {
+  AxisCoef<T> r{T(0), T(0), T(1)};
+  if (slot >= 0) {
+    r.b = __ldg(b + n);
+    r.a = __ldg(a + n);
+    r.rk = __ldg(rk + n);
+  }
+  return r;
 }
 
 // General E update of one cell: outer walls and CPML slabs.  E psi is read
 // from pr and, when store_psi, written to pw (SEPARATE_PSI) or back to pr
-// (in place).  w[c] reports whether component c was updated.
-template <typename T, typename I, bool SEPARATE_PSI>
+// (in place).  w[c] reports whether component c was updated.  Every operand
+// (coefficients, profiles, psi values) is loaded before the first store, so
+// that the loads are in flight together; the arithmetic is that of the
+// reference's loops, term by term.  AXES (bit 0 x, 1 y, 2 z) names the axes
+// whose index may be special (wall or CPML slab); on the others the caller
+// guarantees a plain index, and their tests and terms drop out at compile
+// time (a CPML face cell has one special axis, an edge cell two).
+template <typename T, typename I, bool SEPARATE_PSI, int AXES = 7>
 __device__ __forceinline__ void e_general(const VolParams<T, I> &p, const T *c, int i, int j, int k,
                                           const ECurl<T> &h, const Psi<T> &pr, const Psi<T> &pw_, bool store_psi,
                                           T &ex, T &ey, T &ez, bool w[3]) {
+  constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
   const Psi<T> &pw = SEPARATE_PSI ? pw_ : pr;
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
-  const int xs = p.cp[0].n_layers ? p.cp[0].slot_e[i] : -1;
-  const int ys = p.cp[1].n_layers ? p.cp[1].slot_e[j] : -1;
-  const int zs = p.cp[2].n_layers ? p.cp[2].slot_e[k] : -1;
-  const bool in_i = i >= 1 && i < nx, in_j = j >= 1 && j < ny, in_k = k >= 1 && k < nz;
-  const int Ly = p.cp[1].n_layers, Lz = p.cp[2].n_layers;
+  const int xs = SX && p.cp[0].n_layers ? __ldg(p.cp[0].slot_e + i) : -1;
+  const int ys = SY && p.cp[1].n_layers ? __ldg(p.cp[1].slot_e + j) : -1;
+  const int zs = SZ && p.cp[2].n_layers ? __ldg(p.cp[2].slot_e + k) : -1;
+  const bool in_i = !SX || (i >= 1 && i < nx), in_j = !SY || (j >= 1 && j < ny), in_k = !SZ || (k >= 1 && k < nz);
+  const bool ex_on = !SX || i < nx, ey_on = !SY || j < ny, ez_on = !SZ || k < nz;   // Ex, Ey, Ez exist here
+  const unsigned Ly = p.cp[1].n_layers, Lz = p.cp[2].n_layers;
   const unsigned nzp = static_cast<unsigned>(p.d.nzp), ny1 = static_cast<unsigned>(ny + 1);
+  const unsigned ox = (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;   // X-slab psi (Ey, Ez)
+  const unsigned oy = (static_cast<unsigned>(i) * Ly + ys) * nzp + k;    // Y-slab psi (Ex, Ez)
+  const unsigned oz = (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;    // Z-slab psi (Ex, Ey)
+  T cf[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) cf[q] = c[q];
+  const AxisCoef<T> X = axis_coef(xs, p.cp[0].b_e, p.cp[0].a_e, p.cp[0].rk_e, i);
+  const AxisCoef<T> Y = axis_coef(ys, p.cp[1].b_e, p.cp[1].a_e, p.cp[1].rk_e, j);
+  const AxisCoef<T> Z = axis_coef(zs, p.cp[2].b_e, p.cp[2].a_e, p.cp[2].rk_e, k);
+  const T s_ex_y = ex_on && ys >= 0 ? pr.ex_y[oy] : T(0);
+  const T s_ex_z = ex_on && zs >= 0 ? pr.ex_z[oz] : T(0);
+  const T s_ey_x = ey_on && xs >= 0 ? pr.ey_x[ox] : T(0);
+  const T s_ey_z = ey_on && zs >= 0 ? pr.ey_z[oz] : T(0);
+  const T s_ez_x = ez_on && xs >= 0 ? pr.ez_x[ox] : T(0);
+  const T s_ez_y = ez_on && ys >= 0 ? pr.ez_y[oy] : T(0);
   w[0] = w[1] = w[2] = false;
 
   // ---- Ex (nx, ny+1, nz+1) ----
-  if (i < nx) {
+  if (ex_on) {
     const T d_hz_y = h.hz - h.hz_j;   // Hz(j) - Hz(j-1)
     const T d_hy_z = h.hy - h.hy_k;   // Hy(k) - Hy(k-1)
     if (in_j && in_k) {
-      T ca = c[1], cb = c[2];
-      if (zs >= 0) ca = mul(ca, p.cp[2].rk_e[k]);
-      if (ys >= 0) cb = mul(cb, p.cp[1].rk_e[j]);
-      ex = yee(c[0], ex, ca, d_hy_z, cb, d_hz_y);
+      T ca = cf[1], cb = cf[2];
+      if (zs >= 0) ca = mul(ca, Z.rk);
+      if (ys >= 0) cb = mul(cb, Y.rk);
+      ex = yee(cf[0], ex, ca, d_hy_z, cb, d_hz_y);
       w[0] = true;
     }
     if (ys >= 0) {   // Y slabs: psi_eb of YN/YP, c_psi = cexhz * dy
-      const unsigned o = (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
-      ex = psi_step(pr.ex_y + o, pw.ex_y + o, store_psi, p.cp[1].b_e[j], p.cp[1].a_e[j], d_hz_y, mul(c[2], p.dl[1]), ex);
+      const T s = psi_next(Y.b, Y.a, d_hz_y, s_ex_y);
+      if (store_psi) pw.ex_y[oy] = s;
+      ex = fmad(mul(cf[2], p.dl[1]), s, ex);
       w[0] = true;
     }
     if (zs >= 0) {   // Z slabs: psi_ea of ZN/ZP, c_psi = cexhy * dz
-      const unsigned o = (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
-      ex = psi_step(pr.ex_z + o, pw.ex_z + o, store_psi, p.cp[2].b_e[k], p.cp[2].a_e[k], d_hy_z, mul(c[1], p.dl[2]), ex);
+      const T s = psi_next(Z.b, Z.a, d_hy_z, s_ex_z);
+      if (store_psi) pw.ex_z[oz] = s;
+      ex = fmad(mul(cf[1], p.dl[2]), s, ex);
       w[0] = true;
     }
   }
 
   // ---- Ey (nx+1, ny, nz+1) ----
-  if (j < ny) {
+  if (ey_on) {
     const T d_hz_x = h.hz - h.hz_i;  // Hz(i) - Hz(i-1)
     const T d_hx_z = h.hx - h.hx_k;  // Hx(k) - Hx(k-1)
     if (in_i && in_k) {
-      T ca = c[5], cb = c[4];      // ceyhx, ceyhz
-      if (zs >= 0) ca = mul(ca, p.cp[2].rk_e[k]);
-      if (xs >= 0) cb = mul(cb, p.cp[0].rk_e[i]);
-      ey = yee(c[3], ey, ca, d_hx_z, cb, d_hz_x);
+      T ca = cf[5], cb = cf[4];      // ceyhx, ceyhz
+      if (zs >= 0) ca = mul(ca, Z.rk);
+      if (xs >= 0) cb = mul(cb, X.rk);
+      ey = yee(cf[3], ey, ca, d_hx_z, cb, d_hz_x);
       w[1] = true;
     }
     if (xs >= 0) {   // X slabs: psi_ea of XN/XP, c_psi = ceyhz * dx
-      const unsigned o = (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
-      ey = psi_step(pr.ey_x + o, pw.ey_x + o, store_psi, p.cp[0].b_e[i], p.cp[0].a_e[i], d_hz_x, mul(c[4], p.dl[0]), ey);
+      const T s = psi_next(X.b, X.a, d_hz_x, s_ey_x);
+      if (store_psi) pw.ey_x[ox] = s;
+      ey = fmad(mul(cf[4], p.dl[0]), s, ey);
       w[1] = true;
     }
     if (zs >= 0) {   // Z slabs: psi_eb of ZN/ZP, c_psi = ceyhx * dz
-      const unsigned o = (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
-      ey = psi_step(pr.ey_z + o, pw.ey_z + o, store_psi, p.cp[2].b_e[k], p.cp[2].a_e[k], d_hx_z, mul(c[5], p.dl[2]), ey);
+      const T s = psi_next(Z.b, Z.a, d_hx_z, s_ey_z);
+      if (store_psi) pw.ey_z[oz] = s;
+      ey = fmad(mul(cf[5], p.dl[2]), s, ey);
       w[1] = true;
     }
   }
 
   // ---- Ez (nx+1, ny+1, nz) ----
-  if (k < nz) {
+  if (ez_on) {
     const T d_hy_x = h.hy - h.hy_i;  // Hy(i) - Hy(i-1)
     const T d_hx_y = h.hx - h.hx_j;  // Hx(j) - Hx(j-1)
     if (in_i && in_j) {
-      T ca = c[7], cb = c[8];      // cezhx, cezhy
-      if (ys >= 0) ca = mul(ca, p.cp[1].rk_e[j]);
-      if (xs >= 0) cb = mul(cb, p.cp[0].rk_e[i]);
-      ez = yee(c[6], ez, ca, d_hx_y, cb, d_hy_x);
+      T ca = cf[7], cb = cf[8];      // cezhx, cezhy
+      if (ys >= 0) ca = mul(ca, Y.rk);
+      if (xs >= 0) cb = mul(cb, X.rk);
+      ez = yee(cf[6], ez, ca, d_hx_y, cb, d_hy_x);
       w[2] = true;
     }
     if (xs >= 0) {   // X slabs: psi_eb of XN/XP, c_psi = cezhy * dx
-      const unsigned o = (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
-      ez = psi_step(pr.ez_x + o, pw.ez_x + o, store_psi, p.cp[0].b_e[i], p.cp[0].a_e[i], d_hy_x, mul(c[8], p.dl[0]), ez);
+      const T s = psi_next(X.b, X.a, d_hy_x, s_ez_x);
+      if (store_psi) pw.ez_x[ox] = s;
+      ez = fmad(mul(cf[8], p.dl[0]), s, ez);
       w[2] = true;
     }
     if (ys >= 0) {   // Y slabs: psi_ea of YN/YP, c_psi = cezhx * dy
-      const unsigned o = (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
-      ez = psi_step(pr.ez_y + o, pw.ez_y + o, store_psi, p.cp[1].b_e[j], p.cp[1].a_e[j], d_hx_y, mul(c[7], p.dl[1]), ez);
+      const T s = psi_next(Y.b, Y.a, d_hx_y, s_ez_y);
+      if (store_psi) pw.ez_y[oy] = s;
+      ez = fmad(mul(cf[7], p.dl[1]), s, ez);
       w[2] = true;
     }
   }
 }
 
-// General H update of one cell: last planes and CPML slabs (H psi in place).
-template <typename T, typename I>
+// General H update of one cell: last planes and CPML slabs (H psi in place),
+// operands first and AXES as in e_general.
+template <typename T, typename I, int AXES = 7>
 __device__ __forceinline__ void h_general(const VolParams<T, I> &p, const T *c, int i, int j, int k,
                                           const HCurl<T> &e, T &hx, T &hy, T &hz, bool w[3]) {
+  constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
-  const int xs = p.cp[0].n_layers ? p.cp[0].slot_h[i] : -1;
-  const int ys = p.cp[1].n_layers ? p.cp[1].slot_h[j] : -1;
-  const int zs = p.cp[2].n_layers ? p.cp[2].slot_h[k] : -1;
-  const int Ly = p.cp[1].n_layers, Lz = p.cp[2].n_layers;
+  const int xs = SX && p.cp[0].n_layers ? __ldg(p.cp[0].slot_h + i) : -1;
+  const int ys = SY && p.cp[1].n_layers ? __ldg(p.cp[1].slot_h + j) : -1;
+  const int zs = SZ && p.cp[2].n_layers ? __ldg(p.cp[2].slot_h + k) : -1;
+  const unsigned Ly = p.cp[1].n_layers, Lz = p.cp[2].n_layers;
   const unsigned nzp = static_cast<unsigned>(p.d.nzp), ny1 = static_cast<unsigned>(ny + 1);
+  const bool i_lt = !SX || i < nx, j_lt = !SY || j < ny, k_lt = !SZ || k < nz;
+  const bool hx_on = j_lt && k_lt, hy_on = i_lt && k_lt, hz_on = i_lt && j_lt;   // Hx, Hy, Hz exist here
+  const unsigned ox = (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;   // X-slab psi (Hy, Hz)
+  const unsigned oy = (static_cast<unsigned>(i) * Ly + ys) * nzp + k;    // Y-slab psi (Hx, Hz)
+  const unsigned oz = (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;    // Z-slab psi (Hx, Hy)
   const Psi<T> &ps = p.psi;
+  T cf[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) cf[q] = c[q];
+  const AxisCoef<T> X = axis_coef(xs, p.cp[0].b_m, p.cp[0].a_m, p.cp[0].rk_m, i);
+  const AxisCoef<T> Y = axis_coef(ys, p.cp[1].b_m, p.cp[1].a_m, p.cp[1].rk_m, j);
+  const AxisCoef<T> Z = axis_coef(zs, p.cp[2].b_m, p.cp[2].a_m, p.cp[2].rk_m, k);
+  const T s_hx_y = hx_on && ys >= 0 ? ps.hx_y[oy] : T(0);
+  const T s_hx_z = hx_on && zs >= 0 ? ps.hx_z[oz] : T(0);
+  const T s_hy_x = hy_on && xs >= 0 ? ps.hy_x[ox] : T(0);
+  const T s_hy_z = hy_on && zs >= 0 ? ps.hy_z[oz] : T(0);
+  const T s_hz_x = hz_on && xs >= 0 ? ps.hz_x[ox] : T(0);
+  const T s_hz_y = hz_on && ys >= 0 ? ps.hz_y[oy] : T(0);
   w[0] = w[1] = w[2] = false;
 
   // ---- Hx (nx+1, ny, nz) ----
-  if (j < ny && k < nz) {
+  if (hx_on) {
     const T d_ey_z = e.ey_k - e.ey;   // Ey(k+1) - Ey(k)
     const T d_ez_y = e.ez_j - e.ez;   // Ez(j+1) - Ez(j)
-    if (i < nx) {
-      T ca = c[1], cb = c[2];        // chxey, chxez
-      if (zs >= 0) ca = mul(ca, p.cp[2].rk_m[k]);
-      if (ys >= 0) cb = mul(cb, p.cp[1].rk_m[j]);
-      hx = yee(c[0], hx, ca, d_ey_z, cb, d_ez_y);
+    if (i_lt) {
+      T ca = cf[1], cb = cf[2];        // chxey, chxez
+      if (zs >= 0) ca = mul(ca, Z.rk);
+      if (ys >= 0) cb = mul(cb, Y.rk);
+      hx = yee(cf[0], hx, ca, d_ey_z, cb, d_ez_y);
       w[0] = true;
     }
     if (ys >= 0) {   // Y slabs: psi_hb of YN/YP, c_psi = chxez * dy
-      T *q = ps.hx_y + (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
-      hx = psi_step(q, q, true, p.cp[1].b_m[j], p.cp[1].a_m[j], d_ez_y, mul(c[2], p.dl[1]), hx);
+      const T s = psi_next(Y.b, Y.a, d_ez_y, s_hx_y);
+      ps.hx_y[oy] = s;
+      hx = fmad(mul(cf[2], p.dl[1]), s, hx);
       w[0] = true;
     }
     if (zs >= 0) {   // Z slabs: psi_ha of ZN/ZP, c_psi = chxey * dz
-      T *q = ps.hx_z + (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
-      hx = psi_step(q, q, true, p.cp[2].b_m[k], p.cp[2].a_m[k], d_ey_z, mul(c[1], p.dl[2]), hx);
+      const T s = psi_next(Z.b, Z.a, d_ey_z, s_hx_z);
+      ps.hx_z[oz] = s;
+      hx = fmad(mul(cf[1], p.dl[2]), s, hx);
       w[0] = true;
     }
   }
 
   // ---- Hy (nx, ny+1, nz) ----
-  if (i < nx && k < nz) {
+  if (hy_on) {
     const T d_ez_x = e.ez_i - e.ez;   // Ez(i+1) - Ez(i)
     const T d_ex_z = e.ex_k - e.ex;   // Ex(k+1) - Ex(k)
-    if (j < ny) {
-      T ca = c[4], cb = c[5];        // chyez, chyex
-      if (xs >= 0) ca = mul(ca, p.cp[0].rk_m[i]);
-      if (zs >= 0) cb = mul(cb, p.cp[2].rk_m[k]);
-      hy = yee(c[3], hy, ca, d_ez_x, cb, d_ex_z);
+    if (j_lt) {
+      T ca = cf[4], cb = cf[5];        // chyez, chyex
+      if (xs >= 0) ca = mul(ca, X.rk);
+      if (zs >= 0) cb = mul(cb, Z.rk);
+      hy = yee(cf[3], hy, ca, d_ez_x, cb, d_ex_z);
       w[1] = true;
     }
     if (xs >= 0) {   // X slabs: psi_ha of XN/XP, c_psi = chyez * dx
-      T *q = ps.hy_x + (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
-      hy = psi_step(q, q, true, p.cp[0].b_m[i], p.cp[0].a_m[i], d_ez_x, mul(c[4], p.dl[0]), hy);
+      const T s = psi_next(X.b, X.a, d_ez_x, s_hy_x);
+      ps.hy_x[ox] = s;
+      hy = fmad(mul(cf[4], p.dl[0]), s, hy);
       w[1] = true;
     }
     if (zs >= 0) {   // Z slabs: psi_hb of ZN/ZP, c_psi = chyex * dz
-      T *q = ps.hy_z + (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;
-      hy = psi_step(q, q, true, p.cp[2].b_m[k], p.cp[2].a_m[k], d_ex_z, mul(c[5], p.dl[2]), hy);
+      const T s = psi_next(Z.b, Z.a, d_ex_z, s_hy_z);
+      ps.hy_z[oz] = s;
+      hy = fmad(mul(cf[5], p.dl[2]), s, hy);
       w[1] = true;
     }
   }
 
   // ---- Hz (nx, ny, nz+1) ----
-  if (i < nx && j < ny) {
+  if (hz_on) {
     const T d_ex_y = e.ex_j - e.ex;   // Ex(j+1) - Ex(j)
     const T d_ey_x = e.ey_i - e.ey;   // Ey(i+1) - Ey(i)
-    if (k < nz) {
-      T ca = c[7], cb = c[8];        // chzex, chzey
-      if (ys >= 0) ca = mul(ca, p.cp[1].rk_m[j]);
-      if (xs >= 0) cb = mul(cb, p.cp[0].rk_m[i]);
-      hz = yee(c[6], hz, ca, d_ex_y, cb, d_ey_x);
+    if (k_lt) {
+      T ca = cf[7], cb = cf[8];        // chzex, chzey
+      if (ys >= 0) ca = mul(ca, Y.rk);
+      if (xs >= 0) cb = mul(cb, X.rk);
+      hz = yee(cf[6], hz, ca, d_ex_y, cb, d_ey_x);
       w[2] = true;
     }
     if (xs >= 0) {   // X slabs: psi_hb of XN/XP, c_psi = chzey * dx
-      T *q = ps.hz_x + (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;
-      hz = psi_step(q, q, true, p.cp[0].b_m[i], p.cp[0].a_m[i], d_ey_x, mul(c[8], p.dl[0]), hz);
+      const T s = psi_next(X.b, X.a, d_ey_x, s_hz_x);
+      ps.hz_x[ox] = s;
+      hz = fmad(mul(cf[8], p.dl[0]), s, hz);
       w[2] = true;
     }
     if (ys >= 0) {   // Y slabs: psi_ha of YN/YP, c_psi = chzex * dy
-      T *q = ps.hz_y + (static_cast<unsigned>(i) * Ly + ys) * nzp + k;
-      hz = psi_step(q, q, true, p.cp[1].b_m[j], p.cp[1].a_m[j], d_ex_y, mul(c[7], p.dl[1]), hz);
+      const T s = psi_next(Y.b, Y.a, d_ex_y, s_hz_y);
+      ps.hz_y[oy] = s;
+      hz = fmad(mul(cf[7], p.dl[1]), s, hz);
       w[2] = true;
     }
   }
@@ -288,10 +357,10 @@ __device__ __forceinline__ bool h_plain_cell(const VolParams<T, I> &p, int i, in
 
 // E update of one cell by the general path.  It serves any cell: a plain
 // cell gets the bits of the fast path (same expressions, no CPML terms).
-// The volume kernels decide per warp: a warp whose cells are not all plain
-// runs this path for all of them, so that no warp runs both paths.
-template <typename T, typename I>
+// AXES as in e_general.
+template <typename T, typename I, int AXES = 7>
 __device__ __forceinline__ void e_cell_general(const VolParams<T, I> &p, const T *tab, int ts, int i, int j, int k) {
+  constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
   const T *__restrict__ Hx = p.H[0];
@@ -304,16 +373,16 @@ __device__ __forceinline__ void e_cell_general(const VolParams<T, I> &p, const T
   h.hx = __ldg(Hx + b);
   h.hy = __ldg(Hy + b);
   h.hz = __ldg(Hz + b);
-  h.hx_k = k > 0 ? __ldg(Hx + b - 1) : T(0);
-  h.hy_k = k > 0 ? __ldg(Hy + b - 1) : T(0);
-  h.hx_j = j > 0 ? __ldg(Hx + b - usj) : T(0);
-  h.hz_j = j > 0 ? __ldg(Hz + b - usj) : T(0);
-  h.hy_i = i > 0 ? __ldg(Hy + b - usi) : T(0);
-  h.hz_i = i > 0 ? __ldg(Hz + b - usi) : T(0);
+  h.hx_k = !SZ || k > 0 ? __ldg(Hx + b - 1) : T(0);
+  h.hy_k = !SZ || k > 0 ? __ldg(Hy + b - 1) : T(0);
+  h.hx_j = !SY || j > 0 ? __ldg(Hx + b - usj) : T(0);
+  h.hz_j = !SY || j > 0 ? __ldg(Hz + b - usj) : T(0);
+  h.hy_i = !SX || i > 0 ? __ldg(Hy + b - usi) : T(0);
+  h.hz_i = !SX || i > 0 ? __ldg(Hz + b - usi) : T(0);
   const T *c = tab + static_cast<unsigned>(__ldg(p.idx + b)) * ts;
   T ex = Ex[b], ey = Ey[b], ez = Ez[b];
   bool w[3];
-  e_general<T, I, false>(p, c, i, j, k, h, p.psi, p.psi, true, ex, ey, ez, w);
+  e_general<T, I, false, AXES>(p, c, i, j, k, h, p.psi, p.psi, true, ex, ey, ez, w);
   if (w[0]) Ex[b] = ex;
   if (w[1]) Ey[b] = ey;
   if (w[2]) Ez[b] = ez;
@@ -361,35 +430,113 @@ __device__ __forceinline__ void e_fast(const VolParams<T, I> &p, const T *tab, i
   }
 }
 
+// The volume update runs as two kernels per side.  The interior kernel
+// covers the box of cells that are plain on all three axes (no flag loads,
+// no general path: its registers serve the fast path alone); the shell
+// kernel covers every other cell, one thread per cell, by the general path.
+// The two sets are disjoint and together cover the component box, so the
+// pair does what one kernel over all cells with a per-cell choice would.
+//
+// Interior box [lo, hi] (inclusive, per axis).  k0: first k of the launch
+// grid, lo[2] rounded down to the block's k extent, so that every row of
+// threads starts on the row's alignment.
+struct InteriorBox {
+  int lo[3], hi[3];
+  int k0;
+};
+
+// The shell: boxes of cells (origin, extent per axis), each covering whole
+// 256-thread blocks from block0 on, cells numbered with k fastest.  Along k
+// a box may skip a gap: its k offsets from ksplit on are shifted by kgap,
+// so that the cells below and above the interior's k range of one row are
+// numbered together (ext[2] counts both parts).  cls names the axes on
+// which the box's indices may be special (AXES of e_general): 1, 2, 4 for
+// the CPML faces, 5, 6, 7 for edges and corners.  Division by the extents
+// uses multiply-shift constants (m, sh: q = n * m >> sh, exact for n <
+// 2^31).
+struct ShellBox {
+  int lo[3];
+  int ext[3];
+  int ksplit, kgap;
+  unsigned cells;
+  int cls;
+  unsigned long long m2, m1;   // divide by ext[2], by ext[1]
+  int sh2, sh1;
+  unsigned block0;
+};
+constexpr int kMaxShellBoxes = 18;
+struct ShellBoxes {
+  int n;
+  unsigned blocks;   // total blocks
+  ShellBox b[kMaxShellBoxes];
+};
+
+__device__ __forceinline__ unsigned div_magic(unsigned n, unsigned long long m, int sh) {
+  return static_cast<unsigned>((static_cast<unsigned long long>(n) * m) >> sh);
+}
+
+// Box of this block (binary search on block0) and this thread's cell in it;
+// false past the box's last cell.
+__device__ __forceinline__ bool shell_cell(const ShellBoxes &s, int &cls, int &i, int &j, int &k) {
+  int lo = 0, hi = s.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (blockIdx.x >= s.b[mid].block0) lo = mid;
+    else hi = mid - 1;
+  }
+  const ShellBox &bx = s.b[lo];
+  const unsigned r = (blockIdx.x - bx.block0) * 256u + threadIdx.x;
+  if (r >= bx.cells) return false;
+  const unsigned t = div_magic(r, bx.m2, bx.sh2);
+  const unsigned u = div_magic(t, bx.m1, bx.sh1);
+  const int kk = static_cast<int>(r - t * static_cast<unsigned>(bx.ext[2]));
+  k = bx.lo[2] + kk + (kk >= bx.ksplit ? bx.kgap : 0);
+  j = bx.lo[1] + static_cast<int>(t - u * static_cast<unsigned>(bx.ext[1]));
+  i = bx.lo[0] + static_cast<int>(u);
+  cls = bx.cls;
+  return true;
+}
+
 // MINB: minimum resident blocks per SM requested from the register
 // allocator (1 = no cap); NC: cells per thread along i.  The autotuner in
 // engine.cu picks both (and the block shape) per plan.
 template <typename T, typename I, bool SMEM_TABLE, int MINB, int NC>
-__global__ void __launch_bounds__(256, MINB) k_update_e(VolParams<T, I> p) {
+__global__ void __launch_bounds__(256, MINB) k_update_e(VolParams<T, I> p, InteriorBox in) {
   int ts;
   const T *tab = load_table<T, I, SMEM_TABLE>(p, 0, ts);
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int i0 = (blockIdx.z * blockDim.z + threadIdx.z) * NC;
-  const bool valid = k <= p.d.nz && j <= p.d.ny && i0 <= p.d.nx;
-  bool plain = valid && i0 + NC - 1 <= p.d.nx;
-#pragma unroll
-  for (int q = 0; q < NC; ++q) plain = plain && e_plain_cell(p, i0 + q, j, k);
-  // one path per warp (blockDim.x is a multiple of 32: a warp is one row)
-  const bool fast = __all_sync(0xffffffffu, plain || !valid);
-  if (!valid) return;
-  if (fast) {
+  const int k = in.k0 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = in.lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
+  const int i0 = in.lo[0] + (blockIdx.z * blockDim.z + threadIdx.z) * NC;
+  if (k < in.lo[2] || k > in.hi[2] || j > in.hi[1] || i0 > in.hi[0]) return;
+  if (i0 + NC - 1 <= in.hi[0]) {
     e_fast<T, I, NC>(p, tab, ts, i0, j, k);
     return;
   }
 #pragma unroll
   for (int q = 0; q < NC; ++q)
-    if (i0 + q <= p.d.nx) e_cell_general<T, I>(p, tab, ts, i0 + q, j, k);
+    if (i0 + q <= in.hi[0]) e_fast<T, I, 1>(p, tab, ts, i0 + q, j, k);
+}
+
+// E update of the shell cells (coefficient table read through L1), the
+// general path specialised per box class (uniform per block).
+template <typename T, typename I, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_update_e_shell(VolParams<T, I> p, const __grid_constant__ ShellBoxes s) {
+  int cls, i, j, k;
+  if (!shell_cell(s, cls, i, j, k)) return;
+  switch (cls) {
+    case 1: e_cell_general<T, I, 1>(p, p.table, 18, i, j, k); break;
+    case 2: e_cell_general<T, I, 2>(p, p.table, 18, i, j, k); break;
+    case 4: e_cell_general<T, I, 4>(p, p.table, 18, i, j, k); break;
+    case 5: e_cell_general<T, I, 5>(p, p.table, 18, i, j, k); break;
+    case 6: e_cell_general<T, I, 6>(p, p.table, 18, i, j, k); break;
+    default: e_cell_general<T, I, 7>(p, p.table, 18, i, j, k); break;
+  }
 }
 
 // H update of one cell by the general path (any cell, as e_cell_general).
-template <typename T, typename I>
+template <typename T, typename I, int AXES = 7>
 __device__ __forceinline__ void h_cell_general(const VolParams<T, I> &p, const T *tab, int ts, int i, int j, int k) {
+  constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
@@ -403,16 +550,16 @@ __device__ __forceinline__ void h_cell_general(const VolParams<T, I> &p, const T
   e.ex = __ldg(Ex + b);
   e.ey = __ldg(Ey + b);
   e.ez = __ldg(Ez + b);
-  e.ey_i = i < nx ? __ldg(Ey + b + usi) : T(0);
-  e.ez_i = i < nx ? __ldg(Ez + b + usi) : T(0);
-  e.ex_k = k < nz ? __ldg(Ex + b + 1) : T(0);
-  e.ey_k = k < nz ? __ldg(Ey + b + 1) : T(0);
-  e.ex_j = j < ny ? __ldg(Ex + b + usj) : T(0);
-  e.ez_j = j < ny ? __ldg(Ez + b + usj) : T(0);
+  e.ey_i = !SX || i < nx ? __ldg(Ey + b + usi) : T(0);
+  e.ez_i = !SX || i < nx ? __ldg(Ez + b + usi) : T(0);
+  e.ex_k = !SZ || k < nz ? __ldg(Ex + b + 1) : T(0);
+  e.ey_k = !SZ || k < nz ? __ldg(Ey + b + 1) : T(0);
+  e.ex_j = !SY || j < ny ? __ldg(Ex + b + usj) : T(0);
+  e.ez_j = !SY || j < ny ? __ldg(Ez + b + usj) : T(0);
   const T *c = tab + static_cast<unsigned>(__ldg(p.idx + b)) * ts;
   T hx = Hx[b], hy = Hy[b], hz = Hz[b];
   bool w[3];
-  h_general(p, c, i, j, k, e, hx, hy, hz, w);
+  h_general<T, I, AXES>(p, c, i, j, k, e, hx, hy, hz, w);
   if (w[0]) Hx[b] = hx;
   if (w[1]) Hy[b] = hy;
   if (w[2]) Hz[b] = hz;
@@ -460,25 +607,35 @@ __device__ __forceinline__ void h_fast(const VolParams<T, I> &p, const T *tab, i
 }
 
 template <typename T, typename I, bool SMEM_TABLE, int MINB, int NC>
-__global__ void __launch_bounds__(256, MINB) k_update_h(VolParams<T, I> p) {
+__global__ void __launch_bounds__(256, MINB) k_update_h(VolParams<T, I> p, InteriorBox in) {
   int ts;
   const T *tab = load_table<T, I, SMEM_TABLE>(p, 1, ts);
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int i0 = (blockIdx.z * blockDim.z + threadIdx.z) * NC;
-  const bool valid = k <= p.d.nz && j <= p.d.ny && i0 <= p.d.nx;
-  bool plain = valid && i0 + NC - 1 <= p.d.nx;
-#pragma unroll
-  for (int q = 0; q < NC; ++q) plain = plain && h_plain_cell(p, i0 + q, j, k);
-  const bool fast = __all_sync(0xffffffffu, plain || !valid);
-  if (!valid) return;
-  if (fast) {
+  const int k = in.k0 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = in.lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
+  const int i0 = in.lo[0] + (blockIdx.z * blockDim.z + threadIdx.z) * NC;
+  if (k < in.lo[2] || k > in.hi[2] || j > in.hi[1] || i0 > in.hi[0]) return;
+  if (i0 + NC - 1 <= in.hi[0]) {
     h_fast<T, I, NC>(p, tab, ts, i0, j, k);
     return;
   }
 #pragma unroll
   for (int q = 0; q < NC; ++q)
-    if (i0 + q <= p.d.nx) h_cell_general<T, I>(p, tab, ts, i0 + q, j, k);
+    if (i0 + q <= in.hi[0]) h_fast<T, I, 1>(p, tab, ts, i0 + q, j, k);
+}
+
+
+template <typename T, typename I, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_update_h_shell(VolParams<T, I> p, const __grid_constant__ ShellBoxes s) {
+  int cls, i, j, k;
+  if (!shell_cell(s, cls, i, j, k)) return;
+  switch (cls) {
+    case 1: h_cell_general<T, I, 1>(p, p.table + 9, 18, i, j, k); break;
+    case 2: h_cell_general<T, I, 2>(p, p.table + 9, 18, i, j, k); break;
+    case 4: h_cell_general<T, I, 4>(p, p.table + 9, 18, i, j, k); break;
+    case 5: h_cell_general<T, I, 5>(p, p.table + 9, 18, i, j, k); break;
+    case 6: h_cell_general<T, I, 6>(p, p.table + 9, 18, i, j, k); break;
+    default: h_cell_general<T, I, 7>(p, p.table + 9, 18, i, j, k); break;
+  }
 }
 
 }  // namespace xg
