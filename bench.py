@@ -156,7 +156,13 @@ def _peaks():
 
 
 # --------------------------------------------------------------- roofline ---
-SIDE_STREAM_KERNELS = ("tfsf_aux",)
+# Entries timed on their own streams, concurrently with the main stream's:
+# the TFSF 1-D line, and the two kernels of each volume update (whose
+# main-stream entry, update_e / update_h, spans both).
+GRAPH_STEPS = 32        # steps per captured CUDA graph (4 NF-FF batches of 8)
+PROFILE_STEPS = 400     # steps of the profiled pass behind the kernel times
+
+SIDE_STREAM_KERNELS = ("tfsf_aux", "update_e_interior", "update_e_shell", "update_h_interior", "update_h_shell")
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
 # from an ncu --set full capture of that kernel on this workload
@@ -164,27 +170,37 @@ SIDE_STREAM_KERNELS = ("tfsf_aux",)
 NCU_TRAFFIC = {}
 
 
+def dominant(prof) -> str:
+    """The main-stream entry with the largest device time."""
+    return max((k for k in prof if k not in SIDE_STREAM_KERNELS), key=lambda k: prof[k][0])
+
+
 def algorithmic_bytes(n, slab_layers, precision: str, kernel: str, split=None) -> float:
-    """Bytes one launch of a volume kernel must move at least.  E (or H)
-    update: per cell read the 3 own components and the 3 curl components,
-    write the 3 own components, read the 1-byte material index; inside CPML
-    slabs read and write one psi per (component, slab axis) pair (2 per
-    slab axis).  The update runs as two kernels: the interior kernel over
-    the plain cells (split["e_interior"] / ["h_interior"]) and the shell
-    kernel over walls and slabs (["e_shell"] / ["h_shell"], all psi
-    traffic).  Fused sweep (E and H of one step): read and write all 6
-    components once and the index once; psi traffic of both halves."""
+    """Bytes one E (or H) volume update must move at least: per cell read
+    the 3 own components and the 3 curl components, write the 3 own
+    components, read the 1-byte material index; inside CPML slabs read and
+    write one psi per (component, slab axis) pair (2 per slab axis).  The
+    update runs as two concurrent kernels: the interior kernel over the
+    plain cells (split["e_interior"] / ["h_interior"]) and the shell kernel
+    over walls and slabs (["e_shell"] / ["h_shell"], all psi traffic);
+    "update_e" / "update_h" is the pair.  Fused sweep (E and H of one step):
+    read and write all 6 components once and the index once; psi traffic of
+    both halves."""
     nx, ny, nz = n
     cells = nx * ny * nz
     w = 8 if precision == "fp64" else 4
     slab_cells = (slab_layers[0] * ny * nz + slab_layers[1] * nx * nz + slab_layers[2] * nx * ny)
+    psi = slab_cells * 2 * 2 * w
     if kernel == "sweep_eh":
-        return cells * (12 * w + 1) + slab_cells * 2 * 2 * w * 2
-    if split is not None and kernel in ("update_e", "update_h"):
-        return split[kernel[-1] + "_interior"] * (9 * w + 1)
-    if split is not None and kernel in ("update_e_shell", "update_h_shell"):
-        return split[kernel[7] + "_shell"] * (9 * w + 1) + slab_cells * 2 * 2 * w
-    return cells * (9 * w + 1) + slab_cells * 2 * 2 * w
+        return cells * (12 * w + 1) + psi * 2
+    if split is not None:
+        side = kernel[7]
+        if kernel.endswith("_interior"):
+            return split[side + "_interior"] * (9 * w + 1)
+        if kernel.endswith("_shell"):
+            return split[side + "_shell"] * (9 * w + 1) + psi
+        return (split[side + "_interior"] + split[side + "_shell"]) * (9 * w + 1) + psi
+    return cells * (9 * w + 1) + psi
 
 
 def _slab_layers(sc):
@@ -373,7 +389,7 @@ def run_heterogeneous_form(args, local):
     ms = g.step_timed(args.hetero_steps)
     prof = g.profile()
     cells = g.n[0] * g.n[1] * g.n[2]
-    dom = max(prof, key=lambda k: prof[k][0])
+    dom = dominant(prof)
     slabs = _slab_layers(sc)
     alg = algorithmic_bytes(g.n, slabs, "fp32", dom, g.volume_split())
     gbs = alg / (prof[dom][0] / prof[dom][1] / 1e3) / 1e9
@@ -389,14 +405,19 @@ def ours_arm(args, world, rank, local, grp):
     import xfdtd_gb300 as X
     X.build()
     sc, _ = configs.dielectric_sphere()
-    total = args.warmup + args.steps
     fused = {"auto": None, "fused": True, "split": False}[args.volume]
-    sim = X.Simulation(sc, total, precision=args.precision, graph=False, profile=True, device=local, fused=fused)
+    # The timed run is the production path: steps replayed from CUDA graphs
+    # of GRAPH_STEPS steps, no per-kernel events.  After the warm-up the run
+    # is brought to a graph boundary and one graph is captured and replayed
+    # (setup, untimed); then exactly `steps` steps are timed.
+    setup = GRAPH_STEPS - args.warmup % GRAPH_STEPS + GRAPH_STEPS
+    total = args.warmup + setup + args.steps
+    sim = X.Simulation(sc, total, precision=args.precision, graph=True, device=local, fused=fused)
     n = sim.n
     cells = n[0] * n[1] * n[2]
     sim.step(args.warmup)
+    sim.step(setup)
     sim.synchronize()
-    sim.profile_reset()
     launches0 = sim.launch_count()
     clock = ClockSampler(local)
     clock.start()
@@ -406,27 +427,42 @@ def ours_arm(args, world, rank, local, grp):
     grp.barrier()
     clocks = clock.stop()
     max_ms = grp.max(ms)
-    prof = sim.profile()
     variants = sim.kernel_variants()
     launches = sim.launch_count() - launches0
     sim.check_finite()
+    split = sim.volume_split()
     value = aggregate_value(cells, args.steps, world, max_ms)
+    del sim
 
-    # roofline of the dominant kernel (largest share of device time)
+    # Per-kernel device times: a profiled pass over the same workload (events
+    # around every launch, no graph), after `warmup` steps.
+    prof_steps = min(args.steps, PROFILE_STEPS)
+    psim = X.Simulation(sc, args.warmup + prof_steps, precision=args.precision, graph=False, profile=True,
+                        device=local, fused=fused)
+    psim.step(args.warmup)
+    psim.synchronize()
+    psim.profile_reset()
+    prof_ms_total = psim.step_timed(prof_steps)
+    prof = psim.profile()
+    del psim
+
+    # roofline of the dominant entry (largest share of device time): the E or
+    # H volume update, whose interior and shell kernels run concurrently
     peak, peak_kind = _peaks()
-    # the TFSF 1-D line runs on a side stream beside update_e: its event time
-    # overlaps the main stream's and is reported apart from the shares
+    # entries on side streams (the TFSF 1-D line, the two kernels of each
+    # volume update) overlap the main stream's and are reported apart
     side = {k: prof.pop(k) for k in SIDE_STREAM_KERNELS if k in prof}
-    dom = max(prof, key=lambda k: prof[k][0])
+    dom = dominant(prof)
     dom_ms, dom_n = prof[dom]
     slabs = _slab_layers(sc)
-    split = sim.volume_split()
     alg = algorithmic_bytes(n, slabs, args.precision, dom, split)
     achieved = alg / (dom_ms / dom_n / 1e3) / 1e9
+    concurrent = {k: {"ms_per_launch": v[0] / max(v[1], 1),
+                      "algorithmic_GBs": algorithmic_bytes(n, slabs, args.precision, k, split) / (v[0] / max(v[1], 1) / 1e3) / 1e9}
+                  for k, v in side.items() if k.startswith("update_")}
     total_prof = sum(v[0] for v in prof.values())
     shares = {k: round(v[0] / total_prof, 4) for k, v in prof.items()}
     shares.update({f"{k} (concurrent)": round(v[0] / total_prof, 4) for k, v in side.items()})
-    del sim
 
     # e2e: one whole job through the public API, host scene to host results
     grp.barrier()
@@ -448,7 +484,7 @@ def ours_arm(args, world, rank, local, grp):
         s64.profile_reset()
         ms64 = s64.step_timed(args.fp64_steps)
         p64 = s64.profile()
-        d64 = max(p64, key=lambda k: p64[k][0])
+        d64 = dominant(p64)
         a64 = algorithmic_bytes(n, slabs, "fp64", d64, s64.volume_split()) / (p64[d64][0] / p64[d64][1] / 1e3) / 1e9
         fp64 = {"value": cells * args.fp64_steps / (ms64 / 1e3) / 1e6, "unit": UNIT, "steps": args.fp64_steps,
                 "ms_per_step": ms64 / args.fp64_steps, "dominant_kernel": d64,
@@ -475,13 +511,18 @@ def ours_arm(args, world, rank, local, grp):
                                "dx 2 mm, eps_r 4 sphere r=60 cells, TFSF x-pol +z Gaussian, NF-FF 1/2/3 GHz",
                    "cells": cells, "grid": list(n), "precision_form": args.precision,
                    "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (cells * (4 if args.precision == 'fp32' else 8) / 1e6),
-                   "parallelism": f"replicas x{world}", "volume_kernels": args.volume},
+                   "parallelism": f"replicas x{world}", "volume_kernels": args.volume,
+                   "timed_path": f"CUDA graph replay ({GRAPH_STEPS}-step graphs), after {args.warmup} warm-up steps "
+                                 f"and {setup} untimed steps to reach a graph boundary and capture the graph"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": NCU_TRAFFIC.get((dom, args.precision, tuple(n))),
-                     "algorithmic_bytes_per_launch": alg, "launch_ms": dom_ms / dom_n},
+                     "algorithmic_bytes_per_launch": alg, "launch_ms": dom_ms / dom_n,
+                     "timing": f"CUDA events around each launch in a profiled pass of {prof_steps} steps "
+                               f"({prof_ms_total / prof_steps:.4f} ms/step, no graph)"},
         "kernel_shares": shares,
         "volume_split_cells": split,
+        "volume_kernels_concurrent": concurrent,
         "autotuned_variants": {"update_e": variants["e"], "update_h": variants["h"],
                                "trial_ms_e": [round(v, 4) for v in variants["trials_e"]],
                                "trial_ms_h": [round(v, 4) for v in variants["trials_h"]]},

@@ -60,10 +60,14 @@ struct Err {
                 std::string(#call) + ": " + cudaGetErrorString(e_)};                    \
   } while (0)
 
-const char *kKernelNames[] = {"tfsf_aux", "update_e", "lumped_e", "update_h",  "nffft",          "probes",
-                              "advance",  "tfsf_e",   "tfsf_h",   "nffft_acc", "sweep_eh",       "update_e_shell",
-                              "update_h_shell"};
-constexpr int kNumKernels = 13;
+// Profile entries.  update_e / update_h time the whole E / H volume update
+// (its interior and shell kernels, which run concurrently on two streams);
+// the *_interior and *_shell entries time each kernel on its own stream.
+const char *kKernelNames[] = {"tfsf_aux",         "update_e",       "lumped_e",         "update_h",
+                              "nffft",            "probes",         "advance",          "tfsf_e",
+                              "tfsf_h",           "nffft_acc",      "sweep_eh",         "update_e_shell",
+                              "update_h_shell",   "update_e_interior", "update_h_interior"};
+constexpr int kNumKernels = 15;
 
 }  // namespace
 
@@ -84,6 +88,8 @@ struct xfdtd_handle {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;            // the TFSF 1-D line runs here, forked and joined per step
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t shell = nullptr;           // the volume shell kernels run here, beside the interior kernels
+  cudaEvent_t ev_vfork[2] = {}, ev_vjoin[2] = {};
   std::vector<void *> allocs;
   size_t bytes = 0;
   long long h2d = 0, d2h = 0;   // bytes copied host<->device
@@ -181,7 +187,12 @@ struct xfdtd_handle {
 
   // profiling
   std::vector<cudaEvent_t> ev_pool;
-  std::vector<std::pair<int, int>> ev_pending;   // (kernel id, event index of start)
+  struct ProfEntry {
+    int id;        // kernel id
+    int ev;        // event index of the start (end: ev + 1)
+    bool closed;   // end event recorded
+  };
+  std::vector<ProfEntry> ev_pending;
   double prof_ms[kNumKernels] = {};
   long long prof_n[kNumKernels] = {};
 
@@ -225,6 +236,11 @@ struct xfdtd_handle {
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     if (side) cudaStreamDestroy(side);
+    for (int q = 0; q < 2; ++q) {
+      if (ev_vfork[q]) cudaEventDestroy(ev_vfork[q]);
+      if (ev_vjoin[q]) cudaEventDestroy(ev_vjoin[q]);
+    }
+    if (shell) cudaStreamDestroy(shell);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -263,8 +279,7 @@ void with_types(int precision, int idx_bytes, F &&f) {
 }
 
 // ------------------------------------------------------------ launches ---
-void prof_begin(xfdtd_handle *h, int id, cudaStream_t st = nullptr) {
-  h->launch_count += 1;   // every per-step kernel launch passes here
+void prof_region_begin(xfdtd_handle *h, int id, cudaStream_t st = nullptr) {
   if (!(h->flags & XFDTD_FLAG_PROFILE)) return;
   size_t need = h->ev_pending.size() * 2 + 2;
   while (h->ev_pool.size() < need) {
@@ -274,21 +289,32 @@ void prof_begin(xfdtd_handle *h, int id, cudaStream_t st = nullptr) {
   }
   int s = static_cast<int>(h->ev_pending.size() * 2);
   XCHECK(cudaEventRecord(h->ev_pool[s], st ? st : h->stream));
-  h->ev_pending.push_back({id, s});
+  h->ev_pending.push_back({id, s, false});
 }
+// Ends the innermost open entry (entries nest: an entry opened after another
+// closes first).
 void prof_end(xfdtd_handle *h, cudaStream_t st = nullptr) {
   if (!(h->flags & XFDTD_FLAG_PROFILE)) return;
-  int s = h->ev_pending.back().second;
-  XCHECK(cudaEventRecord(h->ev_pool[s + 1], st ? st : h->stream));
+  for (auto it = h->ev_pending.rbegin(); it != h->ev_pending.rend(); ++it)
+    if (!it->closed) {
+      it->closed = true;
+      XCHECK(cudaEventRecord(h->ev_pool[it->ev + 1], st ? st : h->stream));
+      return;
+    }
+}
+// One kernel launch: counted, and timed under XFDTD_FLAG_PROFILE.
+void prof_begin(xfdtd_handle *h, int id, cudaStream_t st = nullptr) {
+  h->launch_count += 1;   // every per-step kernel launch passes here
+  prof_region_begin(h, id, st);
 }
 void prof_collect(xfdtd_handle *h) {
   if (h->ev_pending.empty()) return;
   XCHECK(cudaStreamSynchronize(h->stream));
   for (auto &pr : h->ev_pending) {
     float ms = 0;
-    XCHECK(cudaEventElapsedTime(&ms, h->ev_pool[pr.second], h->ev_pool[pr.second + 1]));
-    h->prof_ms[pr.first] += ms;
-    h->prof_n[pr.first] += 1;
+    XCHECK(cudaEventElapsedTime(&ms, h->ev_pool[pr.ev], h->ev_pool[pr.ev + 1]));
+    h->prof_ms[pr.id] += ms;
+    h->prof_n[pr.id] += 1;
   }
   h->ev_pending.clear();
 }
@@ -383,19 +409,20 @@ constexpr int kShellMinb[] = {4, 6};
 constexpr int kNumShellVariants = 2;
 
 template <typename T, typename I>
-void launch_shell(xfdtd_handle *h, bool e_side, int minb = 0) {
+void launch_shell(xfdtd_handle *h, bool e_side, int minb = 0, cudaStream_t st = nullptr) {
   const int side = e_side ? 0 : 1;
   const xg::ShellBoxes &s = h->vshell[side];
   if (s.blocks == 0) return;
   if (minb == 0) minb = h->shell_minb[side];
   const auto p = vol_params<T, I>(h);
   const unsigned blocks = s.blocks;
+  if (!st) st = h->stream;
   if (minb == 6) {
-    if (e_side) xg::k_update_e_shell<T, I, 6><<<blocks, 256, 0, h->stream>>>(p, s);
-    else xg::k_update_h_shell<T, I, 6><<<blocks, 256, 0, h->stream>>>(p, s);
+    if (e_side) xg::k_update_e_shell<T, I, 6><<<blocks, 256, 0, st>>>(p, s);
+    else xg::k_update_h_shell<T, I, 6><<<blocks, 256, 0, st>>>(p, s);
   } else {
-    if (e_side) xg::k_update_e_shell<T, I, 4><<<blocks, 256, 0, h->stream>>>(p, s);
-    else xg::k_update_h_shell<T, I, 4><<<blocks, 256, 0, h->stream>>>(p, s);
+    if (e_side) xg::k_update_e_shell<T, I, 4><<<blocks, 256, 0, st>>>(p, s);
+    else xg::k_update_h_shell<T, I, 4><<<blocks, 256, 0, st>>>(p, s);
   }
   XCHECK(cudaGetLastError());
 }
@@ -863,6 +890,35 @@ xg::AuxParams aux_params(xfdtd_handle *h) {
   return a;
 }
 
+// The E (or H) update of one step: the interior kernel on the main stream
+// and the shell kernel on the shell stream beside it (they write disjoint
+// cells and read only the other field), joined before what follows.
+template <typename T, typename I>
+void volume_pair(xfdtd_handle *h, bool e_side) {
+  const int side = e_side ? 0 : 1;
+  const bool in = h->vin_cells[side] != 0, sh = h->vshell_cells[side] != 0;
+  prof_region_begin(h, e_side ? 1 : 3);
+  if (in && sh) {
+    XCHECK(cudaEventRecord(h->ev_vfork[side], h->stream));
+    XCHECK(cudaStreamWaitEvent(h->shell, h->ev_vfork[side], 0));
+    prof_begin(h, e_side ? 11 : 12, h->shell);
+    launch_shell<T, I>(h, e_side, 0, h->shell);
+    prof_end(h, h->shell);
+    XCHECK(cudaEventRecord(h->ev_vjoin[side], h->shell));
+  } else if (sh) {
+    prof_begin(h, e_side ? 11 : 12);
+    launch_shell<T, I>(h, e_side);
+    prof_end(h);
+  }
+  if (in) {
+    prof_begin(h, e_side ? 13 : 14);
+    launch_volume<T, I>(h, e_side);
+    prof_end(h);
+  }
+  if (in && sh) XCHECK(cudaStreamWaitEvent(h->stream, h->ev_vjoin[side], 0));
+  prof_end(h);
+}
+
 template <typename T, typename I>
 void enqueue_step_t(xfdtd_handle *h, long long s) {
   if (h->tfsf) {
@@ -884,16 +940,7 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     prof_end(h);
     swap_state(h);
   } else {
-    if (h->vin_cells[0]) {
-      prof_begin(h, 1);
-      launch_volume<T, I>(h, true);
-      prof_end(h);
-    }
-    if (h->vshell_cells[0]) {
-      prof_begin(h, 11);
-      launch_shell<T, I>(h, true);
-      prof_end(h);
-    }
+    volume_pair<T, I>(h, true);
     if (h->n_inj || h->n_ind) {
       auto sp = sparse_params<T>(h);
       int n = std::max(h->n_inj, h->n_ind);
@@ -910,16 +957,7 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
       XCHECK(cudaGetLastError());
       prof_end(h);
     }
-    if (h->vin_cells[1]) {
-      prof_begin(h, 3);
-      launch_volume<T, I>(h, false);
-      prof_end(h);
-    }
-    if (h->vshell_cells[1]) {
-      prof_begin(h, 12);
-      launch_shell<T, I>(h, false);
-      prof_end(h);
-    }
+    volume_pair<T, I>(h, false);
   }
   if (h->tfsf) {
     XCHECK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
@@ -1037,6 +1075,11 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   XCHECK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
   XCHECK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
   XCHECK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+  XCHECK(cudaStreamCreateWithFlags(&h->shell, cudaStreamNonBlocking));
+  for (int q = 0; q < 2; ++q) {
+    XCHECK(cudaEventCreateWithFlags(&h->ev_vfork[q], cudaEventDisableTiming));
+    XCHECK(cudaEventCreateWithFlags(&h->ev_vjoin[q], cudaEventDisableTiming));
+  }
   for (int c = 0; c < 6; ++c) h->F[c] = h->alloc_bytes(d.cells * h->esize);
 
   // material index, repacked into the padded layout
