@@ -321,16 +321,19 @@ def run_adjoint_form(args, local):
     """The adjoint form: dL/d eps_r over a 64 x 64 x 32 design region of the
     160 x 160 x 96 (+ 10-cell CPML) dipole problem, L = sum of Ez^2 over a
     64 x 64 plane over the last 400 of 2000 steps, FP32 forward and reverse
-    passes with checkpoints every 100 steps.  Times: the plain FP32 forward
-    run (CUDA events), the checkpointed forward and the backward pass (wall
-    clock around the synchronous calls).  Check: central differences of the
-    FP64 forward loss (eps_r +- 1e-4, as float) at `adjoint_fd` seeded
-    design voxels."""
+    passes.  `adjoint_checkpoint` K: 0 records the design box at every step
+    (no recomputation; about 6 GB here, small beside the GPU's HBM), K > 0
+    keeps a full checkpoint every K steps and recomputes each segment in the
+    backward pass.  Times: the plain FP32 forward run (CUDA events), the
+    recording forward and the backward pass (wall clock around the
+    synchronous calls).  Check: central differences of the FP64 forward loss
+    (eps_r +- 1e-4, as float) at `adjoint_fd` seeded design voxels."""
     import xfdtd_gb300 as X
     sc, st, spec = configs.adjoint_dipole()
     keys = ("design_lo", "design_hi", "plane_axis", "plane_index", "plane_lo", "plane_hi", "t_begin", "t_end",
             "loss_comp", "checkpoint_every")
     sa = {q: spec[q] for q in keys}
+    sa["checkpoint_every"] = args.adjoint_checkpoint
     plain = X.Simulation(sc, st, precision="fp32", fused=False, autotune=False, device=local)
     fwd_ms = plain.step_timed(st)
     cells = plain.n[0] * plain.n[1] * plain.n[2]
@@ -339,15 +342,16 @@ def run_adjoint_form(args, local):
     t0 = time.perf_counter()
     loss = g.adjoint_forward(**sa)
     t1 = time.perf_counter()
+    dev_bytes = g.device_bytes()
     ge, _ = g.adjoint_backward()
     t2 = time.perf_counter()
     del g
     out = {"grid": cells, "steps": st, "design_cells": int(ge.size), "loss": loss,
-           "forward_ms": fwd_ms, "checkpointed_forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
+           "forward_ms": fwd_ms, "adjoint_forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
            "backward_over_forward": (t2 - t1) * 1e3 / fwd_ms,
            "gradient_over_forward": (t2 - t0) * 1e3 / fwd_ms,
            "value": cells * st / ((t2 - t1)) / 1e6, "unit": "Mcell-updates/s (reverse pass)",
-           "checkpoint_every": spec["checkpoint_every"]}
+           "checkpoint_every": args.adjoint_checkpoint, "device_bytes": dev_bytes}
     if args.adjoint_fd > 0:
         import copy
         rng = np.random.default_rng(5002)
@@ -557,6 +561,8 @@ def main():
     ap.add_argument("--adjoint", type=int, default=1, help="run the adjoint form (0: skip)")
     ap.add_argument("--hetero-steps", type=int, default=100, help="steps of the heterogeneous-medium form (0: skip)")
     ap.add_argument("--adjoint-fd", type=int, default=16, help="design voxels of the adjoint FD check (0: skip)")
+    ap.add_argument("--adjoint-checkpoint", type=int, default=0,
+                    help="adjoint form: checkpoint every K steps (0: record the design box at every step)")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.impl == "reference":

@@ -224,7 +224,7 @@ int xfdtd_launch_count(xfdtd_handle *h, int64_t *n);
 int xfdtd_launches_per_step(xfdtd_handle *h, int *n);
 /* Bytes copied host->device and device->host by the handle so far. */
 int xfdtd_transfer_bytes(xfdtd_handle *h, int64_t *h2d, int64_t *d2h);
-/* Device bytes held by the handle. */
+/* Device bytes held by the handle (with its adjoint state, if any). */
 int xfdtd_device_bytes(xfdtd_handle *h, int64_t *bytes);
 const char *xfdtd_last_error(xfdtd_handle *h);
 void xfdtd_destroy(xfdtd_handle *h);

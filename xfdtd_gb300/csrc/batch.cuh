@@ -7,8 +7,8 @@
 // simulation) have a fixed number of blocks, each walking a contiguous
 // range of the list and loading a simulation's parameters into shared
 // memory when its range crosses into the next simulation.
-// Per cell the work is that of the single-simulation split kernels
-// (e_fast / e_cell_general, h_fast / h_cell_general, tfsf_e_surface / tfsf_h_surface,
+// Per cell the work is that of the single-simulation kernels (e_fast /
+// e_shell_cell, h_fast / h_shell_cell, tfsf_e_surface / tfsf_h_surface,
 // nffft_sample / nffft_fold, tfsf_aux_block), so a batched simulation gives
 // the same bits as the same simulation run alone.
 #pragma once
@@ -44,31 +44,45 @@ __device__ __forceinline__ void load_params(P &dst, const P *all, int sim) {
   __syncthreads();
 }
 
-// Volume update (E or H): one block per listed tile, a tile being 32 (k) x
-// 8 (j) cells of one plane i, packed as i << 16 | j-block << 8 | k-block.
-// The block reads its simulation's parameters from the array (the same
-// addresses for every thread: served by L1); per cell the update is that of
-// the split kernels.  (A persistent form -- a fixed grid walking the list,
-// one or two tiles per block at a time -- ran at 14-21 Gcell-updates/s on
-// GB300 against 25+ for one block per tile: fewer resident warps.)
+// Volume update (E or H) of each member as in the single-simulation split
+// kernels: interior tiles by the fast path, shell cells by the general path
+// specialised per box class; the member's parameters are read from the
+// array (the same addresses for every thread: served by L1).
+//
+// Interior: one block per listed tile, a tile being 32 (k) x 8 (j) cells of
+// one plane i of the member's interior box, packed as i << 16 | j-block <<
+// 8 | k-block, blocks counted from the box's lo[1] and k0.
 template <typename T, typename I, bool E_SIDE>
-__global__ void __launch_bounds__(256, 6) k_volume_batch(const VolParams<T, I> *__restrict__ all,
-                                                          const WorkItem *__restrict__ items) {
+__global__ void __launch_bounds__(256, 8) k_interior_batch(const VolParams<T, I> *__restrict__ all,
+                                                            const InteriorBox *__restrict__ boxes,
+                                                            const WorkItem *__restrict__ items) {
   const WorkItem it = items[blockIdx.x];
   const VolParams<T, I> &p = all[it.sim];
+  const InteriorBox &in = boxes[it.sim];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int i = it.tile >> 16, j = ((it.tile >> 8) & 0xff) * 8 + ty, k = (it.tile & 0xff) * 32 + tx;
-  const bool valid = k <= p.d.nz && j <= p.d.ny;
-  const bool plain = valid && (E_SIDE ? e_plain_cell(p, i, j, k) : h_plain_cell(p, i, j, k));
-  const bool fast = __all_sync(0xffffffffu, plain || !valid);   // one path per warp (row)
-  if (!valid) return;
-  if (E_SIDE) {
-    if (fast) e_fast<T, I, 1>(p, p.table, 18, i, j, k);
-    else e_cell_general<T, I>(p, p.table, 18, i, j, k);
-  } else {
-    if (fast) h_fast<T, I, 1>(p, p.table + 9, 18, i, j, k);
-    else h_cell_general<T, I>(p, p.table + 9, 18, i, j, k);
-  }
+  const unsigned t = static_cast<unsigned>(it.tile);
+  const int i = static_cast<int>(t >> 16);
+  const int j = in.lo[1] + static_cast<int>((t >> 8) & 0xff) * 8 + ty;
+  const int k = in.k0 + static_cast<int>(t & 0xff) * 32 + tx;
+  if (k < in.lo[2] || k > in.hi[2] || j > in.hi[1]) return;
+  if (E_SIDE) e_fast<T, I, 1>(p, p.table, 18, i, j, k);
+  else h_fast<T, I, 1>(p, p.table + 9, 18, i, j, k);
+}
+
+// Shell: one block per listed (member, shell block) item; the member's
+// parameters are copied to shared memory first (the general path reads
+// many of them, which from global memory would hold registers).
+template <typename T, typename I, bool E_SIDE>
+__global__ void __launch_bounds__(256, 4) k_shell_batch(const VolParams<T, I> *__restrict__ all,
+                                                         const ShellBoxes *__restrict__ shells,
+                                                         const WorkItem *__restrict__ items) {
+  __shared__ VolParams<T, I> p;
+  const WorkItem it = items[blockIdx.x];
+  load_params(p, all, it.sim);
+  int cls, i, j, k;
+  if (!shell_cell(shells[it.sim], static_cast<unsigned>(it.tile), cls, i, j, k)) return;
+  if (E_SIDE) e_shell_cell(p, cls, i, j, k);
+  else h_shell_cell(p, cls, i, j, k);
 }
 
 // TFSF E or H corrections: tile = 256 consecutive surface cells.

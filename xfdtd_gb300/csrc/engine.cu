@@ -72,6 +72,7 @@ constexpr int kNumKernels = 15;
 }  // namespace
 
 struct AdjointState;
+size_t adjoint_bytes(const xfdtd_handle *h);   // device bytes of the handle's adjoint state
 
 struct xfdtd_handle {
   std::string err;
@@ -1677,7 +1678,7 @@ int xfdtd_transfer_bytes(xfdtd_handle *h, int64_t *h2d, int64_t *d2h) {
 
 int xfdtd_device_bytes(xfdtd_handle *h, int64_t *bytes) {
   if (!h || !bytes) return XFDTD_ERR_STATE;
-  *bytes = static_cast<int64_t>(h->bytes);
+  *bytes = static_cast<int64_t>(h->bytes + adjoint_bytes(h));
   return XFDTD_OK;
 }
 
@@ -1707,18 +1708,24 @@ struct xfdtd_batch {
   int device = 0, precision = XFDTD_FP64, idx_bytes = 1, flags = 0;
   int n_sm = 152;
   cudaStream_t stream = nullptr;
+  cudaStream_t shell = nullptr;   // shell kernels, beside the interior kernels
+  cudaEvent_t ev_fork[2] = {}, ev_join[2] = {};
   long long clock = 0;   // steps taken (every member started at step 0)
   long long nf_done = 0;
   long long launches = 0;
   std::vector<void *> allocs;
   // per-member parameter arrays (device), built once
   void *vol = nullptr, *tsurf = nullptr, *nfp = nullptr, *aux = nullptr;
+  xg::InteriorBox *vin[2] = {};   // per side: the members' interior boxes (k0 on the 32-cell tile grid)
+  xg::ShellBoxes *vshell[2] = {};  // per side: the members' shells
   int2 *nf_grid = nullptr;
   int *nf_nb = nullptr;
   // work lists of the running members (device, sized for all members)
   std::vector<int> running;
-  xg::WorkItem *it_vol = nullptr, *it_te = nullptr, *it_th = nullptr, *it_nf = nullptr, *it_fold = nullptr;
-  int n_vol = 0, n_te = 0, n_th = 0, n_nf = 0, n_fold = 0;
+  xg::WorkItem *it_in[2] = {}, *it_sh[2] = {};   // per side: interior tiles, shell blocks
+  int n_in[2] = {}, n_sh[2] = {};
+  xg::WorkItem *it_te = nullptr, *it_th = nullptr, *it_nf = nullptr, *it_fold = nullptr;
+  int n_te = 0, n_th = 0, n_nf = 0, n_fold = 0;
   int *aux_list = nullptr;
   int n_aux = 0;
   long long **step_list = nullptr;
@@ -1736,6 +1743,11 @@ struct xfdtd_batch {
   ~xfdtd_batch() {
     if (gexec) cudaGraphExecDestroy(gexec);
     for (void *p : allocs) cudaFree(p);
+    for (int q = 0; q < 2; ++q) {
+      if (ev_fork[q]) cudaEventDestroy(ev_fork[q]);
+      if (ev_join[q]) cudaEventDestroy(ev_join[q]);
+    }
+    if (shell) cudaStreamDestroy(shell);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -1753,9 +1765,17 @@ void batch_setup(xfdtd_batch *b) {
   std::vector<xg::AuxParams> ax(n);
   std::vector<int2> grid(n);
   std::vector<int> nb(n);
+  std::vector<xg::InteriorBox> vin[2];
+  std::vector<xg::ShellBoxes> vsh[2];
   for (int q = 0; q < n; ++q) {
     xfdtd_handle *h = b->m[q];
     vol[q] = vol_params<T, I>(h);
+    for (int side = 0; side < 2; ++side) {
+      xg::InteriorBox in = h->vin[side];
+      in.k0 = in.lo[2] / 32 * 32;
+      vin[side].push_back(in);
+      vsh[side].push_back(h->vshell[side]);
+    }
     if (h->tfsf) {
       ts[q] = tfsf_surf_params<T>(h);
       ax[q] = aux_params(h);
@@ -1779,6 +1799,10 @@ void batch_setup(xfdtd_batch *b) {
   b->aux = up(ax);
   b->nf_grid = up(grid);
   b->nf_nb = up(nb);
+  for (int side = 0; side < 2; ++side) {
+    b->vin[side] = up(vin[side]);
+    b->vshell[side] = up(vsh[side]);
+  }
   XCHECK(cudaStreamSynchronize(b->stream));   // the host vectors go out of scope
 }
 
@@ -1787,21 +1811,29 @@ void batch_lists(xfdtd_batch *b) {
   std::vector<int> run;
   for (int q = 0; q < static_cast<int>(b->m.size()); ++q)
     if (b->m[q]->host_step < b->m[q]->total) run.push_back(q);
-  if (run == b->running && b->it_vol) return;
+  if (run == b->running && b->it_in[0]) return;
   b->running = run;
   if (b->gexec) {
     cudaGraphExecDestroy(b->gexec);
     b->gexec = nullptr;
   }
-  std::vector<xg::WorkItem> vol, te, th, nf, fold;
+  std::vector<xg::WorkItem> vin[2], vsh[2], te, th, nf, fold;
   std::vector<int> aux;
   std::vector<long long *> steps;
   for (int q : run) {
     xfdtd_handle *h = b->m[q];
-    const int gx = (h->d.nz + 32) / 32, gy = (h->d.ny + 8) / 8;
-    for (int i = 0; i <= h->d.nx; ++i)   // packed tiles: i << 16 | j-block << 8 | k-block
-      for (int by = 0; by < gy; ++by)
-        for (int bx = 0; bx < gx; ++bx) vol.push_back({q, (i << 16) | (by << 8) | bx});
+    for (int side = 0; side < 2; ++side) {
+      const xg::InteriorBox &in = h->vin[side];
+      if (h->vin_cells[side]) {   // packed tiles: i << 16 | j-block << 8 | k-block
+        const int k0 = in.lo[2] / 32 * 32;
+        const int gx = (in.hi[2] - k0) / 32 + 1, gy = (in.hi[1] - in.lo[1]) / 8 + 1;
+        for (int i = in.lo[0]; i <= in.hi[0]; ++i)
+          for (int by = 0; by < gy; ++by)
+            for (int bx = 0; bx < gx; ++bx)
+              vin[side].push_back({q, static_cast<int>((static_cast<unsigned>(i) << 16) | (by << 8) | bx)});
+      }
+      for (unsigned t = 0; t < h->vshell[side].blocks; ++t) vsh[side].push_back({q, static_cast<int>(t)});
+    }
     if (h->tfsf) {
       aux.push_back(q);
       const long long ne = xg::surface_count(h->tf_lo[0], h->tf_hi[0], h->tf_lo[1], h->tf_hi[1], h->tf_lo[2], h->tf_hi[2]);
@@ -1825,7 +1857,10 @@ void batch_lists(xfdtd_batch *b) {
     if (!v.empty()) XCHECK(cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice, b->stream));
     return static_cast<int>(v.size());
   };
-  b->n_vol = put(vol, b->it_vol);
+  for (int side = 0; side < 2; ++side) {
+    b->n_in[side] = put(vin[side], b->it_in[side]);
+    b->n_sh[side] = put(vsh[side], b->it_sh[side]);
+  }
   b->n_te = put(te, b->it_te);
   b->n_th = put(th, b->it_th);
   b->n_nf = put(nf, b->it_nf);
@@ -1848,15 +1883,36 @@ void batch_enqueue_t(xfdtd_batch *b, long long s) {
     ++launched;
   }
   const auto *vp = static_cast<const xg::VolParams<T, I> *>(b->vol);
-  xg::k_volume_batch<T, I, true><<<b->n_vol, 256, 0, st>>>(vp, b->it_vol);
-  ++launched;
+  // one side of the volume update: the shell kernel on the shell stream
+  // beside the interior kernel, joined before what follows
+  auto volume = [&](bool e_side) {
+    const int side = e_side ? 0 : 1;
+    const bool fork = b->n_in[side] && b->n_sh[side];
+    cudaStream_t ss = fork ? b->shell : st;
+    if (fork) {
+      XCHECK(cudaEventRecord(b->ev_fork[side], st));
+      XCHECK(cudaStreamWaitEvent(b->shell, b->ev_fork[side], 0));
+    }
+    if (b->n_sh[side]) {
+      if (e_side) xg::k_shell_batch<T, I, true><<<b->n_sh[side], 256, 0, ss>>>(vp, b->vshell[side], b->it_sh[side]);
+      else xg::k_shell_batch<T, I, false><<<b->n_sh[side], 256, 0, ss>>>(vp, b->vshell[side], b->it_sh[side]);
+      ++launched;
+    }
+    if (fork) XCHECK(cudaEventRecord(b->ev_join[side], b->shell));
+    if (b->n_in[side]) {
+      if (e_side) xg::k_interior_batch<T, I, true><<<b->n_in[side], 256, 0, st>>>(vp, b->vin[side], b->it_in[side]);
+      else xg::k_interior_batch<T, I, false><<<b->n_in[side], 256, 0, st>>>(vp, b->vin[side], b->it_in[side]);
+      ++launched;
+    }
+    if (fork) XCHECK(cudaStreamWaitEvent(st, b->ev_join[side], 0));
+  };
+  volume(true);
   const auto *tp = static_cast<const xg::TfsfSurfParams<T> *>(b->tsurf);
   if (b->n_te) {
     xg::k_tfsf_batch<T, true><<<persistent_grid(b, b->n_te, 8), 256, 0, st>>>(tp, b->it_te, b->n_te);
     ++launched;
   }
-  xg::k_volume_batch<T, I, false><<<b->n_vol, 256, 0, st>>>(vp, b->it_vol);
-  ++launched;
+  volume(false);
   if (b->n_th) {
     xg::k_tfsf_batch<T, false><<<persistent_grid(b, b->n_th, 8), 256, 0, st>>>(tp, b->it_th, b->n_th);
     ++launched;
@@ -1983,6 +2039,11 @@ int xfdtd_batch_create(xfdtd_handle *const *members, int n, int flags, xfdtd_bat
       XCHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
       b->n_sm = sms;
       XCHECK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+      XCHECK(cudaStreamCreateWithFlags(&b->shell, cudaStreamNonBlocking));
+      for (int q = 0; q < 2; ++q) {
+        XCHECK(cudaEventCreateWithFlags(&b->ev_fork[q], cudaEventDisableTiming));
+        XCHECK(cudaEventCreateWithFlags(&b->ev_join[q], cudaEventDisableTiming));
+      }
       for (int q = 0; q < n; ++q) {
         xfdtd_handle *h = members[q];
         XCHECK(cudaStreamSynchronize(h->stream));
@@ -2094,10 +2155,13 @@ struct AdjointState {
   double loss = 0;
   bool forward_done = false;
   int device = 0;
-  void *alloc(size_t bytes) {
+  size_t bytes = 0;   // device bytes held
+  void *alloc(size_t nb) {
     void *p = nullptr;
-    XCHECK(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+    nb = std::max<size_t>(nb, 16);
+    XCHECK(cudaMalloc(&p, nb));
     allocs.push_back(p);
+    bytes += nb;
     return p;
   }
   ~AdjointState() {
@@ -2105,6 +2169,8 @@ struct AdjointState {
     for (void *p : allocs) cudaFree(p);
   }
 };
+
+size_t adjoint_bytes(const xfdtd_handle *h) { return h->adj ? h->adj->bytes : 0; }
 
 namespace {
 

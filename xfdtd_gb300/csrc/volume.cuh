@@ -342,19 +342,6 @@ __device__ __forceinline__ void h_general(const VolParams<T, I> &p, const T *c, 
   }
 }
 
-// Whether cell (i, j, k) is plain for the E update (no outer wall, no CPML
-// slab): then e_fast applies.  Indices are clamped to the box.
-template <typename T, typename I>
-__device__ __forceinline__ bool e_plain_cell(const VolParams<T, I> &p, int i, int j, int k) {
-  return !((__ldg(p.flags[0] + min(i, p.d.nx)) | __ldg(p.flags[1] + min(j, p.d.ny)) | __ldg(p.flags[2] + min(k, p.d.nz))) &
-           kSpecialE);
-}
-template <typename T, typename I>
-__device__ __forceinline__ bool h_plain_cell(const VolParams<T, I> &p, int i, int j, int k) {
-  return !((__ldg(p.flags[0] + min(i, p.d.nx)) | __ldg(p.flags[1] + min(j, p.d.ny)) | __ldg(p.flags[2] + min(k, p.d.nz))) &
-           kSpecialH);
-}
-
 // E update of one cell by the general path.  It serves any cell: a plain
 // cell gets the bits of the fast path (same expressions, no CPML terms).
 // AXES as in e_general.
@@ -475,17 +462,17 @@ __device__ __forceinline__ unsigned div_magic(unsigned n, unsigned long long m, 
   return static_cast<unsigned>((static_cast<unsigned long long>(n) * m) >> sh);
 }
 
-// Box of this block (binary search on block0) and this thread's cell in it;
-// false past the box's last cell.
-__device__ __forceinline__ bool shell_cell(const ShellBoxes &s, int &cls, int &i, int &j, int &k) {
+// Box of shell block `blk` (binary search on block0) and this thread's cell
+// in it; false past the box's last cell.
+__device__ __forceinline__ bool shell_cell(const ShellBoxes &s, unsigned blk, int &cls, int &i, int &j, int &k) {
   int lo = 0, hi = s.n - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (blockIdx.x >= s.b[mid].block0) lo = mid;
+    if (blk >= s.b[mid].block0) lo = mid;
     else hi = mid - 1;
   }
   const ShellBox &bx = s.b[lo];
-  const unsigned r = (blockIdx.x - bx.block0) * 256u + threadIdx.x;
+  const unsigned r = (blk - bx.block0) * 256u + threadIdx.x;
   if (r >= bx.cells) return false;
   const unsigned t = div_magic(r, bx.m2, bx.sh2);
   const unsigned u = div_magic(t, bx.m1, bx.sh1);
@@ -517,12 +504,10 @@ __global__ void __launch_bounds__(256, MINB) k_update_e(VolParams<T, I> p, Inter
     if (i0 + q <= in.hi[0]) e_fast<T, I, 1>(p, tab, ts, i0 + q, j, k);
 }
 
-// E update of the shell cells (coefficient table read through L1), the
-// general path specialised per box class (uniform per block).
-template <typename T, typename I, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_update_e_shell(VolParams<T, I> p, const __grid_constant__ ShellBoxes s) {
-  int cls, i, j, k;
-  if (!shell_cell(s, cls, i, j, k)) return;
+// E update of one shell cell of box class cls (coefficient table read
+// through L1): the general path specialised per class.
+template <typename T, typename I>
+__device__ __forceinline__ void e_shell_cell(const VolParams<T, I> &p, int cls, int i, int j, int k) {
   switch (cls) {
     case 1: e_cell_general<T, I, 1>(p, p.table, 18, i, j, k); break;
     case 2: e_cell_general<T, I, 2>(p, p.table, 18, i, j, k); break;
@@ -531,6 +516,13 @@ __global__ void __launch_bounds__(256, MINB) k_update_e_shell(VolParams<T, I> p,
     case 6: e_cell_general<T, I, 6>(p, p.table, 18, i, j, k); break;
     default: e_cell_general<T, I, 7>(p, p.table, 18, i, j, k); break;
   }
+}
+
+// E update of the shell cells, the class uniform per block.
+template <typename T, typename I, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_update_e_shell(VolParams<T, I> p, const __grid_constant__ ShellBoxes s) {
+  int cls, i, j, k;
+  if (shell_cell(s, blockIdx.x, cls, i, j, k)) e_shell_cell(p, cls, i, j, k);
 }
 
 // H update of one cell by the general path (any cell, as e_cell_general).
@@ -624,10 +616,8 @@ __global__ void __launch_bounds__(256, MINB) k_update_h(VolParams<T, I> p, Inter
 }
 
 
-template <typename T, typename I, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_update_h_shell(VolParams<T, I> p, const __grid_constant__ ShellBoxes s) {
-  int cls, i, j, k;
-  if (!shell_cell(s, cls, i, j, k)) return;
+template <typename T, typename I>
+__device__ __forceinline__ void h_shell_cell(const VolParams<T, I> &p, int cls, int i, int j, int k) {
   switch (cls) {
     case 1: h_cell_general<T, I, 1>(p, p.table + 9, 18, i, j, k); break;
     case 2: h_cell_general<T, I, 2>(p, p.table + 9, 18, i, j, k); break;
@@ -636,6 +626,12 @@ __global__ void __launch_bounds__(256, MINB) k_update_h_shell(VolParams<T, I> p,
     case 6: h_cell_general<T, I, 6>(p, p.table + 9, 18, i, j, k); break;
     default: h_cell_general<T, I, 7>(p, p.table + 9, 18, i, j, k); break;
   }
+}
+
+template <typename T, typename I, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_update_h_shell(VolParams<T, I> p, const __grid_constant__ ShellBoxes s) {
+  int cls, i, j, k;
+  if (shell_cell(s, blockIdx.x, cls, i, j, k)) h_shell_cell(p, cls, i, j, k);
 }
 
 }  // namespace xg
