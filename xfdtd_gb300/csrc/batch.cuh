@@ -46,43 +46,68 @@ __device__ __forceinline__ void load_params(P &dst, const P *all, int sim) {
 
 // Volume update (E or H) of each member as in the single-simulation split
 // kernels: interior tiles by the fast path, shell cells by the general path
-// specialised per box class; the member's parameters are read from the
-// array (the same addresses for every thread: served by L1).
-//
-// Interior: one block per listed tile, a tile being 32 (k) x 8 (j) cells of
-// one plane i of the member's interior box, packed as i << 16 | j-block <<
-// 8 | k-block, blocks counted from the box's lo[1] and k0.
+// specialised per box class.  The members' parameters travel in the
+// launch's own parameter space, up to kBatchGroup members per launch (a
+// group): read there, as in the single-simulation kernels, they take no
+// registers until used.
+constexpr int kBatchGroup = 64;
+template <typename T, typename I>
+struct VolGroup {
+  VolCore<T, I> m[kBatchGroup];
+};
+static_assert(sizeof(VolGroup<double, uint32_t>) <= 30000, "a group's parameters fit one launch");
+
+// Blocks of one volume launch per group member: member q owns blocks
+// first[q] .. first[q+1]-1 (none when it has stopped).  The member of a
+// block follows from blockIdx and these launch parameters alone, so the
+// compiler knows it is the same for the whole block.
+struct GroupBlocks {
+  int n;                          // members in the group
+  unsigned first[kBatchGroup + 1];
+};
+
+__device__ __forceinline__ int group_member(const GroupBlocks &gb) {
+  int lo = 0, hi = gb.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (blockIdx.x >= gb.first[mid]) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Interior: one block per tile of 32 (k) x 8 (j) cells of one plane i of the
+// member's interior box, tiles numbered k-block fastest, then j-block,
+// then i, counted from the box's k0, lo[1], lo[0].
 template <typename T, typename I, bool E_SIDE>
-__global__ void __launch_bounds__(256, 8) k_interior_batch(const VolParams<T, I> *__restrict__ all,
-                                                            const InteriorBox *__restrict__ boxes,
-                                                            const WorkItem *__restrict__ items) {
-  const WorkItem it = items[blockIdx.x];
-  const VolParams<T, I> &p = all[it.sim];
-  const InteriorBox &in = boxes[it.sim];
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const unsigned t = static_cast<unsigned>(it.tile);
-  const int i = static_cast<int>(t >> 16);
-  const int j = in.lo[1] + static_cast<int>((t >> 8) & 0xff) * 8 + ty;
-  const int k = in.k0 + static_cast<int>(t & 0xff) * 32 + tx;
+__global__ void __launch_bounds__(256, 8) k_interior_batch(const __grid_constant__ VolGroup<T, I> g,
+                                                            const __grid_constant__ GroupBlocks gb,
+                                                            const InteriorBox *__restrict__ boxes) {
+  const int q = group_member(gb);
+  const VolCore<T, I> &p = g.m[q];
+  const InteriorBox in = boxes[q];
+  const unsigned t = blockIdx.x - gb.first[q];
+  const unsigned gx = static_cast<unsigned>((in.hi[2] - in.k0) / 32 + 1), gy = static_cast<unsigned>((in.hi[1] - in.lo[1]) / 8 + 1);
+  const unsigned t2 = t / gx;
+  const int i = in.lo[0] + static_cast<int>(t2 / gy);
+  const int j = in.lo[1] + static_cast<int>(t2 % gy) * 8 + static_cast<int>(threadIdx.x >> 5);
+  const int k = in.k0 + static_cast<int>(t % gx) * 32 + static_cast<int>(threadIdx.x & 31);
   if (k < in.lo[2] || k > in.hi[2] || j > in.hi[1]) return;
   if (E_SIDE) e_fast<T, I, 1>(p, p.table, 18, i, j, k);
   else h_fast<T, I, 1>(p, p.table + 9, 18, i, j, k);
 }
 
-// Shell: one block per listed (member, shell block) item; the member's
-// parameters are copied to shared memory first (the general path reads
-// many of them, which from global memory would hold registers).
+// Shell: the member's shell blocks (numbered as in the single-simulation
+// shell kernel).
 template <typename T, typename I, bool E_SIDE>
-__global__ void __launch_bounds__(256, 4) k_shell_batch(const VolParams<T, I> *__restrict__ all,
-                                                         const ShellBoxes *__restrict__ shells,
-                                                         const WorkItem *__restrict__ items) {
-  __shared__ VolParams<T, I> p;
-  const WorkItem it = items[blockIdx.x];
-  load_params(p, all, it.sim);
+__global__ void __launch_bounds__(256, 6) k_shell_batch(const __grid_constant__ VolGroup<T, I> g,
+                                                         const __grid_constant__ GroupBlocks gb,
+                                                         const ShellBoxes *__restrict__ shells) {
+  const int q = group_member(gb);
   int cls, i, j, k;
-  if (!shell_cell(shells[it.sim], static_cast<unsigned>(it.tile), cls, i, j, k)) return;
-  if (E_SIDE) e_shell_cell(p, cls, i, j, k);
-  else h_shell_cell(p, cls, i, j, k);
+  if (!shell_cell(shells[q], blockIdx.x - gb.first[q], cls, i, j, k)) return;
+  if (E_SIDE) e_shell_cell(g.m[q], cls, i, j, k);
+  else h_shell_cell(g.m[q], cls, i, j, k);
 }
 
 // TFSF E or H corrections: tile = 256 consecutive surface cells.

@@ -72,8 +72,9 @@ struct Psi {
   T *hx_y, *hx_z, *hy_x, *hy_z, *hz_x, *hz_y;   // H recursions
 };
 
+// What the volume updates read: fields, material index and table, CPML.
 template <typename T, typename I>
-struct VolParams {
+struct VolCore {
   Dims d;
   T *E[3];
   T *H[3];
@@ -83,6 +84,11 @@ struct VolParams {
   CpmlAxis<T> cp[3];
   Psi<T> psi;
   T dl[3];
+};
+
+// VolCore plus what the fused sweep and the adjoint also need.
+template <typename T, typename I>
+struct VolParams : VolCore<T, I> {
   TfsfDev tf;
   const long long *step;
   const uint8_t *flags[3];   // per-axis index flags (kSpecialE / kSpecialH)

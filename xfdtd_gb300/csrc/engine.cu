@@ -1715,15 +1715,21 @@ struct xfdtd_batch {
   long long launches = 0;
   std::vector<void *> allocs;
   // per-member parameter arrays (device), built once
-  void *vol = nullptr, *tsurf = nullptr, *nfp = nullptr, *aux = nullptr;
+  void *tsurf = nullptr, *nfp = nullptr, *aux = nullptr;
+  // volume parameters of each group of up to kBatchGroup members (host
+  // bytes of an xg::VolGroup, passed by value to the volume launches)
+  std::vector<std::vector<unsigned char>> group_params;
   xg::InteriorBox *vin[2] = {};   // per side: the members' interior boxes (k0 on the 32-cell tile grid)
   xg::ShellBoxes *vshell[2] = {};  // per side: the members' shells
   int2 *nf_grid = nullptr;
   int *nf_nb = nullptr;
   // work lists of the running members (device, sized for all members)
   std::vector<int> running;
-  xg::WorkItem *it_in[2] = {}, *it_sh[2] = {};   // per side: interior tiles, shell blocks
-  int n_in[2] = {}, n_sh[2] = {};
+  bool lists_ok = false;
+  struct VolLists {   // per group and side: blocks of the interior and shell launches
+    xg::GroupBlocks in[2] = {}, sh[2] = {};
+  };
+  std::vector<VolLists> vl;
   xg::WorkItem *it_te = nullptr, *it_th = nullptr, *it_nf = nullptr, *it_fold = nullptr;
   int n_te = 0, n_th = 0, n_nf = 0, n_fold = 0;
   int *aux_list = nullptr;
@@ -1759,7 +1765,8 @@ constexpr int kBatchGraphSteps = 32;   // a multiple of the NF-FF batch
 template <typename T, typename I>
 void batch_setup(xfdtd_batch *b) {
   const int n = static_cast<int>(b->m.size());
-  std::vector<xg::VolParams<T, I>> vol(n);
+  const int groups = (n + xg::kBatchGroup - 1) / xg::kBatchGroup;
+  std::vector<xg::VolGroup<T, I>> vg(groups);
   std::vector<xg::TfsfSurfParams<T>> ts(n);
   std::vector<xg::NfParams<T>> nf(n);
   std::vector<xg::AuxParams> ax(n);
@@ -1769,7 +1776,7 @@ void batch_setup(xfdtd_batch *b) {
   std::vector<xg::ShellBoxes> vsh[2];
   for (int q = 0; q < n; ++q) {
     xfdtd_handle *h = b->m[q];
-    vol[q] = vol_params<T, I>(h);
+    vg[q / xg::kBatchGroup].m[q % xg::kBatchGroup] = vol_params<T, I>(h);
     for (int side = 0; side < 2; ++side) {
       xg::InteriorBox in = h->vin[side];
       in.k0 = in.lo[2] / 32 * 32;
@@ -1793,7 +1800,9 @@ void batch_setup(xfdtd_batch *b) {
     XCHECK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice, b->stream));
     return d;
   };
-  b->vol = up(vol);
+  b->group_params.assign(groups, std::vector<unsigned char>(sizeof(xg::VolGroup<T, I>)));
+  for (int g = 0; g < groups; ++g) std::memcpy(b->group_params[g].data(), &vg[g], sizeof(xg::VolGroup<T, I>));
+  b->vl.assign(groups, xfdtd_batch::VolLists{});
   b->tsurf = up(ts);
   b->nfp = up(nf);
   b->aux = up(ax);
@@ -1811,29 +1820,41 @@ void batch_lists(xfdtd_batch *b) {
   std::vector<int> run;
   for (int q = 0; q < static_cast<int>(b->m.size()); ++q)
     if (b->m[q]->host_step < b->m[q]->total) run.push_back(q);
-  if (run == b->running && b->it_in[0]) return;
+  if (run == b->running && b->lists_ok) return;
   b->running = run;
   if (b->gexec) {
     cudaGraphExecDestroy(b->gexec);
     b->gexec = nullptr;
   }
-  std::vector<xg::WorkItem> vin[2], vsh[2], te, th, nf, fold;
+  const int groups = static_cast<int>(b->vl.size());
+  const int nm = static_cast<int>(b->m.size());
+  std::vector<char> on(nm, 0);
+  for (int q : run) on[q] = 1;
+  for (int g = 0; g < groups; ++g)   // volume launches: blocks per member, none for stopped members
+    for (int side = 0; side < 2; ++side) {
+      xg::GroupBlocks &bi = b->vl[g].in[side], &bs = b->vl[g].sh[side];
+      bi = xg::GroupBlocks{};
+      bs = xg::GroupBlocks{};
+      bi.n = bs.n = std::min(xg::kBatchGroup, nm - g * xg::kBatchGroup);
+      for (int ql = 0; ql < bi.n; ++ql) {
+        const xfdtd_handle *h = b->m[g * xg::kBatchGroup + ql];
+        const bool r = on[g * xg::kBatchGroup + ql] != 0;
+        const xg::InteriorBox &in = h->vin[side];
+        unsigned tiles = 0;
+        if (r && h->vin_cells[side]) {
+          const int k0 = in.lo[2] / 32 * 32;
+          tiles = static_cast<unsigned>(((in.hi[2] - k0) / 32 + 1) * ((in.hi[1] - in.lo[1]) / 8 + 1) *
+                                        (in.hi[0] - in.lo[0] + 1));
+        }
+        bi.first[ql + 1] = bi.first[ql] + tiles;
+        bs.first[ql + 1] = bs.first[ql] + (r ? h->vshell[side].blocks : 0u);
+      }
+    }
+  std::vector<xg::WorkItem> te, th, nf, fold;
   std::vector<int> aux;
   std::vector<long long *> steps;
   for (int q : run) {
     xfdtd_handle *h = b->m[q];
-    for (int side = 0; side < 2; ++side) {
-      const xg::InteriorBox &in = h->vin[side];
-      if (h->vin_cells[side]) {   // packed tiles: i << 16 | j-block << 8 | k-block
-        const int k0 = in.lo[2] / 32 * 32;
-        const int gx = (in.hi[2] - k0) / 32 + 1, gy = (in.hi[1] - in.lo[1]) / 8 + 1;
-        for (int i = in.lo[0]; i <= in.hi[0]; ++i)
-          for (int by = 0; by < gy; ++by)
-            for (int bx = 0; bx < gx; ++bx)
-              vin[side].push_back({q, static_cast<int>((static_cast<unsigned>(i) << 16) | (by << 8) | bx)});
-      }
-      for (unsigned t = 0; t < h->vshell[side].blocks; ++t) vsh[side].push_back({q, static_cast<int>(t)});
-    }
     if (h->tfsf) {
       aux.push_back(q);
       const long long ne = xg::surface_count(h->tf_lo[0], h->tf_hi[0], h->tf_lo[1], h->tf_hi[1], h->tf_lo[2], h->tf_hi[2]);
@@ -1857,10 +1878,6 @@ void batch_lists(xfdtd_batch *b) {
     if (!v.empty()) XCHECK(cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice, b->stream));
     return static_cast<int>(v.size());
   };
-  for (int side = 0; side < 2; ++side) {
-    b->n_in[side] = put(vin[side], b->it_in[side]);
-    b->n_sh[side] = put(vsh[side], b->it_sh[side]);
-  }
   b->n_te = put(te, b->it_te);
   b->n_th = put(th, b->it_th);
   b->n_nf = put(nf, b->it_nf);
@@ -1868,6 +1885,7 @@ void batch_lists(xfdtd_batch *b) {
   b->n_aux = put(aux, b->aux_list);
   put(steps, b->step_list);
   XCHECK(cudaStreamSynchronize(b->stream));
+  b->lists_ok = true;
 }
 
 unsigned persistent_grid(const xfdtd_batch *b, int items, int per_sm) {
@@ -1882,29 +1900,31 @@ void batch_enqueue_t(xfdtd_batch *b, long long s) {
     xg::k_tfsf_aux_batch<<<b->n_aux, 512, 0, st>>>(static_cast<const xg::AuxParams *>(b->aux), b->aux_list);
     ++launched;
   }
-  const auto *vp = static_cast<const xg::VolParams<T, I> *>(b->vol);
-  // one side of the volume update: the shell kernel on the shell stream
-  // beside the interior kernel, joined before what follows
+  // one side of the volume update: per group of members, the shell kernel
+  // on the shell stream beside the interior kernel, joined before what
+  // follows
   auto volume = [&](bool e_side) {
     const int side = e_side ? 0 : 1;
-    const bool fork = b->n_in[side] && b->n_sh[side];
-    cudaStream_t ss = fork ? b->shell : st;
-    if (fork) {
-      XCHECK(cudaEventRecord(b->ev_fork[side], st));
-      XCHECK(cudaStreamWaitEvent(b->shell, b->ev_fork[side], 0));
+    XCHECK(cudaEventRecord(b->ev_fork[side], st));
+    XCHECK(cudaStreamWaitEvent(b->shell, b->ev_fork[side], 0));
+    for (size_t g = 0; g < b->vl.size(); ++g) {
+      const auto &vg = *reinterpret_cast<const xg::VolGroup<T, I> *>(b->group_params[g].data());
+      const xfdtd_batch::VolLists &l = b->vl[g];
+      const size_t base = g * xg::kBatchGroup;
+      const unsigned nsh = l.sh[side].first[l.sh[side].n], nin = l.in[side].first[l.in[side].n];
+      if (nsh) {
+        if (e_side) xg::k_shell_batch<T, I, true><<<nsh, 256, 0, b->shell>>>(vg, l.sh[side], b->vshell[side] + base);
+        else xg::k_shell_batch<T, I, false><<<nsh, 256, 0, b->shell>>>(vg, l.sh[side], b->vshell[side] + base);
+        ++launched;
+      }
+      if (nin) {
+        if (e_side) xg::k_interior_batch<T, I, true><<<nin, 256, 0, st>>>(vg, l.in[side], b->vin[side] + base);
+        else xg::k_interior_batch<T, I, false><<<nin, 256, 0, st>>>(vg, l.in[side], b->vin[side] + base);
+        ++launched;
+      }
     }
-    if (b->n_sh[side]) {
-      if (e_side) xg::k_shell_batch<T, I, true><<<b->n_sh[side], 256, 0, ss>>>(vp, b->vshell[side], b->it_sh[side]);
-      else xg::k_shell_batch<T, I, false><<<b->n_sh[side], 256, 0, ss>>>(vp, b->vshell[side], b->it_sh[side]);
-      ++launched;
-    }
-    if (fork) XCHECK(cudaEventRecord(b->ev_join[side], b->shell));
-    if (b->n_in[side]) {
-      if (e_side) xg::k_interior_batch<T, I, true><<<b->n_in[side], 256, 0, st>>>(vp, b->vin[side], b->it_in[side]);
-      else xg::k_interior_batch<T, I, false><<<b->n_in[side], 256, 0, st>>>(vp, b->vin[side], b->it_in[side]);
-      ++launched;
-    }
-    if (fork) XCHECK(cudaStreamWaitEvent(st, b->ev_join[side], 0));
+    XCHECK(cudaEventRecord(b->ev_join[side], b->shell));
+    XCHECK(cudaStreamWaitEvent(st, b->ev_join[side], 0));
   };
   volume(true);
   const auto *tp = static_cast<const xg::TfsfSurfParams<T> *>(b->tsurf);

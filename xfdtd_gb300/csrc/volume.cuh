@@ -35,7 +35,7 @@
 namespace xg {
 
 template <typename T, typename I, bool SMEM_TABLE>
-__device__ __forceinline__ const T *load_table(const VolParams<T, I> &p, int half, int &ts) {
+__device__ __forceinline__ const T *load_table(const VolCore<T, I> &p, int half, int &ts) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   if (!SMEM_TABLE) {
     ts = 18;
@@ -128,7 +128,7 @@ __device__ __forceinline__ AxisCoef<T> axis_coef(int slot, const T *b, const T *
 // guarantees a plain index, and their tests and terms drop out at compile
 // time (a CPML face cell has one special axis, an edge cell two).
 template <typename T, typename I, bool SEPARATE_PSI, int AXES = 7>
-__device__ __forceinline__ void e_general(const VolParams<T, I> &p, const T *c, int i, int j, int k,
+__device__ __forceinline__ void e_general(const VolCore<T, I> &p, const T *c, int i, int j, int k,
                                           const ECurl<T> &h, const Psi<T> &pr, const Psi<T> &pw_, bool store_psi,
                                           T &ex, T &ey, T &ez, bool w[3]) {
   constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
@@ -237,7 +237,7 @@ __device__ __forceinline__ void e_general(const VolParams<T, I> &p, const T *c, 
 // General H update of one cell: last planes and CPML slabs (H psi in place),
 // operands first and AXES as in e_general.
 template <typename T, typename I, int AXES = 7>
-__device__ __forceinline__ void h_general(const VolParams<T, I> &p, const T *c, int i, int j, int k,
+__device__ __forceinline__ void h_general(const VolCore<T, I> &p, const T *c, int i, int j, int k,
                                           const HCurl<T> &e, T &hx, T &hy, T &hz, bool w[3]) {
   constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
@@ -346,7 +346,7 @@ __device__ __forceinline__ void h_general(const VolParams<T, I> &p, const T *c, 
 // cell gets the bits of the fast path (same expressions, no CPML terms).
 // AXES as in e_general.
 template <typename T, typename I, int AXES = 7>
-__device__ __forceinline__ void e_cell_general(const VolParams<T, I> &p, const T *tab, int ts, int i, int j, int k) {
+__device__ __forceinline__ void e_cell_general(const VolCore<T, I> &p, const T *tab, int ts, int i, int j, int k) {
   constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
@@ -378,7 +378,7 @@ __device__ __forceinline__ void e_cell_general(const VolParams<T, I> &p, const T
 // NC plain cells (i0 .. i0+NC-1) of one (j, k) column: every load is issued
 // before any store, and the H at i-1 of cell c+1 is cell c's own.
 template <typename T, typename I, int NC>
-__device__ __forceinline__ void e_fast(const VolParams<T, I> &p, const T *tab, int ts, int i0, int j, int k) {
+__device__ __forceinline__ void e_fast(const VolCore<T, I> &p, const T *tab, int ts, int i0, int j, int k) {
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const unsigned b0 = static_cast<unsigned>(i0) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
   const T *__restrict__ Hx = p.H[0];
@@ -488,7 +488,7 @@ __device__ __forceinline__ bool shell_cell(const ShellBoxes &s, unsigned blk, in
 // allocator (1 = no cap); NC: cells per thread along i.  The autotuner in
 // engine.cu picks both (and the block shape) per plan.
 template <typename T, typename I, bool SMEM_TABLE, int MINB, int NC>
-__global__ void __launch_bounds__(256, MINB) k_update_e(VolParams<T, I> p, InteriorBox in) {
+__global__ void __launch_bounds__(256, MINB) k_update_e(VolCore<T, I> p, InteriorBox in) {
   int ts;
   const T *tab = load_table<T, I, SMEM_TABLE>(p, 0, ts);
   const int k = in.k0 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -507,7 +507,7 @@ __global__ void __launch_bounds__(256, MINB) k_update_e(VolParams<T, I> p, Inter
 // E update of one shell cell of box class cls (coefficient table read
 // through L1): the general path specialised per class.
 template <typename T, typename I>
-__device__ __forceinline__ void e_shell_cell(const VolParams<T, I> &p, int cls, int i, int j, int k) {
+__device__ __forceinline__ void e_shell_cell(const VolCore<T, I> &p, int cls, int i, int j, int k) {
   switch (cls) {
     case 1: e_cell_general<T, I, 1>(p, p.table, 18, i, j, k); break;
     case 2: e_cell_general<T, I, 2>(p, p.table, 18, i, j, k); break;
@@ -520,14 +520,14 @@ __device__ __forceinline__ void e_shell_cell(const VolParams<T, I> &p, int cls, 
 
 // E update of the shell cells, the class uniform per block.
 template <typename T, typename I, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_update_e_shell(VolParams<T, I> p, const __grid_constant__ ShellBoxes s) {
+__global__ void __launch_bounds__(256, MINB) k_update_e_shell(VolCore<T, I> p, const __grid_constant__ ShellBoxes s) {
   int cls, i, j, k;
   if (shell_cell(s, blockIdx.x, cls, i, j, k)) e_shell_cell(p, cls, i, j, k);
 }
 
 // H update of one cell by the general path (any cell, as e_cell_general).
 template <typename T, typename I, int AXES = 7>
-__device__ __forceinline__ void h_cell_general(const VolParams<T, I> &p, const T *tab, int ts, int i, int j, int k) {
+__device__ __forceinline__ void h_cell_general(const VolCore<T, I> &p, const T *tab, int ts, int i, int j, int k) {
   constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
@@ -559,7 +559,7 @@ __device__ __forceinline__ void h_cell_general(const VolParams<T, I> &p, const T
 
 // NC plain cells of one column for H: the E at i+1 of cell c is cell c+1's own.
 template <typename T, typename I, int NC>
-__device__ __forceinline__ void h_fast(const VolParams<T, I> &p, const T *tab, int ts, int i0, int j, int k) {
+__device__ __forceinline__ void h_fast(const VolCore<T, I> &p, const T *tab, int ts, int i0, int j, int k) {
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const unsigned b0 = static_cast<unsigned>(i0) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
   const T *__restrict__ Ex = p.E[0];
@@ -599,7 +599,7 @@ __device__ __forceinline__ void h_fast(const VolParams<T, I> &p, const T *tab, i
 }
 
 template <typename T, typename I, bool SMEM_TABLE, int MINB, int NC>
-__global__ void __launch_bounds__(256, MINB) k_update_h(VolParams<T, I> p, InteriorBox in) {
+__global__ void __launch_bounds__(256, MINB) k_update_h(VolCore<T, I> p, InteriorBox in) {
   int ts;
   const T *tab = load_table<T, I, SMEM_TABLE>(p, 1, ts);
   const int k = in.k0 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(256, MINB) k_update_h(VolParams<T, I> p, Inter
 
 
 template <typename T, typename I>
-__device__ __forceinline__ void h_shell_cell(const VolParams<T, I> &p, int cls, int i, int j, int k) {
+__device__ __forceinline__ void h_shell_cell(const VolCore<T, I> &p, int cls, int i, int j, int k) {
   switch (cls) {
     case 1: h_cell_general<T, I, 1>(p, p.table + 9, 18, i, j, k); break;
     case 2: h_cell_general<T, I, 2>(p, p.table + 9, 18, i, j, k); break;
@@ -629,7 +629,7 @@ __device__ __forceinline__ void h_shell_cell(const VolParams<T, I> &p, int cls, 
 }
 
 template <typename T, typename I, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_update_h_shell(VolParams<T, I> p, const __grid_constant__ ShellBoxes s) {
+__global__ void __launch_bounds__(256, MINB) k_update_h_shell(VolCore<T, I> p, const __grid_constant__ ShellBoxes s) {
   int cls, i, j, k;
   if (shell_cell(s, blockIdx.x, cls, i, j, k)) h_shell_cell(p, cls, i, j, k);
 }
