@@ -442,10 +442,11 @@ void div_constants(unsigned d, unsigned long long &m, int &sh) {
 // The plain box of one side (kSpecialE, or kSpecialH, clear on all three
 // axes: no outer wall, no CPML slab) and the shell around it.  Per axis the
 // indices split into the plain run P and the special ones S (below and
-// above P).  Along k, P is narrowed to whole 32-byte sectors of a row, so
-// that the rows of every box start and end on sector boundaries (the cells
-// it gives up are plain cells of the shell, where the general path gives
-// the same bits).  The shell is S x P x P, P x S x P, P x P x S (faces, one
+// above P).  Along k, P is narrowed to whole 128-byte lines of a row (on
+// short rows to 32-byte sectors), so that the rows of every box start on a
+// line and the interior kernel's warps each cover one line (the cells it
+// gives up are plain cells of the shell, where the general path gives the
+// same bits).  The shell is S x P x P, P x S x P, P x P x S (faces, one
 // special axis), S x P x S, P x S x S (edges) and S x S x all (edges along
 // z with the corners); a box that is S along k numbers the cells below and
 // above P of one row together.  Without one contiguous plain run on every
@@ -465,10 +466,16 @@ void volume_boxes(xfdtd_handle *h, int side) {
     for (int q = lo[a]; q <= hi[a]; ++q)
       if (fl[q] & bit) interior = false;
   }
-  const int sector = 32 / static_cast<int>(h->esize);   // cells per 32-byte sector
-  lo[2] = (lo[2] + sector - 1) / sector * sector;
-  hi[2] = (hi[2] + 1) / sector * sector - 1;
-  if (lo[2] > hi[2]) interior = false;
+  // cut on 128-byte lines, else (a short run) on 32-byte sectors, else not at all
+  for (int bytes : {128, 32}) {
+    const int q = bytes / static_cast<int>(h->esize);
+    const int l = (lo[2] + q - 1) / q * q, u = (hi[2] + 1) / q * q - 1;
+    if (l <= u) {
+      lo[2] = l;
+      hi[2] = u;
+      break;
+    }
+  }
   xg::InteriorBox &in = h->vin[side];
   xg::ShellBoxes &s = h->vshell[side];
   s = xg::ShellBoxes{};
