@@ -164,10 +164,12 @@ PROFILE_STEPS = 400     # steps of the profiled pass behind the kernel times
 
 SIDE_STREAM_KERNELS = ("tfsf_aux", "update_e_interior", "update_e_shell", "update_h_interior", "update_h_shell")
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
-# from an ncu --set full capture of that kernel on this workload
-# (python -m xfdtd_gb300.run --config dielectric_sphere --steps 24 --precision fp32 --no-graph).
-NCU_TRAFFIC = {}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one E update
+# on this workload: the ncu --set full captures of its interior kernel
+# (524.7 MB) and its shell kernel (386.2 MB), each run by
+# python -m xfdtd_gb300.run --config dielectric_sphere --steps 24 --precision fp32 --no-graph --volume split
+#     --kernel-variant 9,9
+NCU_TRAFFIC = {("update_e", "fp32", (280, 280, 280)): 524.660992e6 + 386.16576e6}
 
 
 def dominant(prof) -> str:

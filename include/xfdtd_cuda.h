@@ -245,7 +245,10 @@ const char *xfdtd_version(void);
  * not have been stepped), checkpointing the state every checkpoint_every
  * steps (0: record the design box at every step instead) and returns L.
  * xfdtd_adjoint_backward then returns dL/d eps_r and dL/d sigma per design
- * cell, [i][j][k] over the box (re-running each checkpoint segment once). */
+ * cell, [i][j][k] over the box (with K > 0 it re-runs each checkpoint
+ * segment once; with K = 0 it reads the recorded design box).  Memory: K = 0
+ * holds 6 components of the design box per step, K > 0 one full state per
+ * checkpoint (xfdtd_device_bytes reports both). */
 typedef struct xfdtd_adjoint_desc {
   int64_t design_lo[3], design_hi[3];   /* cells [lo, hi) per axis                    */
   int32_t loss_comp;                    /* 0 Ex, 1 Ey, 2 Ez                            */
@@ -264,8 +267,9 @@ int xfdtd_adjoint_backward(xfdtd_handle *h, double *grad_eps, double *grad_sigma
  * Batches: many independent simulations of different sizes advanced
  * together.  The reference runs one Simulation at a time
  * (simulation_update.cpp:5-40); a batch runs each phase of the loop body
- * for all of its members in one launch over a (member, tile) work list,
- * and replays the step loop from a CUDA graph (XFDTD_FLAG_GRAPH).  Members
+ * for all of its running members in one launch (the volume phases: an
+ * interior and a shell launch per group of up to 64 members), and replays
+ * the step loop from a CUDA graph (XFDTD_FLAG_GRAPH).  Members
  * are ordinary handles from xfdtd_create -- same device, precision and
  * material-index width, not yet stepped, without lumped elements or
  * monitors; the batch does not own them.  Each member stops at its own

@@ -25,6 +25,9 @@ def main():
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--volume", default="auto", choices=["auto", "fused", "split"],
                     help="volume kernels: autotuned choice, the fused E/H sweep, or the split E and H kernels")
+    ap.add_argument("--kernel-variant", default=None, metavar="E,H",
+                    help="interior-kernel variants of the E and H updates (after autotuning; for profiling a "
+                         "fixed variant)")
     ap.add_argument("--out", default=None)
     ap.add_argument("--adjoint", action="store_true",
                     help="run the adjoint-gradient problem (forward with checkpoints, then backward) instead")
@@ -41,6 +44,8 @@ def main():
     t0 = time.perf_counter()
     fused = {"auto": None, "fused": True, "split": False}[args.volume]
     sim = Simulation(sc, steps, precision=args.precision, graph=not args.no_graph, fused=fused)
+    if args.kernel_variant:
+        sim.set_kernel_variant(*(int(v) for v in args.kernel_variant.split(",")))
     t1 = time.perf_counter()
     ms = sim.step_timed(steps)
     sim.synchronize()
