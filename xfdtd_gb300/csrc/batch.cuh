@@ -79,7 +79,7 @@ __device__ __forceinline__ int group_member(const GroupBlocks &gb) {
 // Interior: one block per tile of 32 (k) x 8 (j) cells of one plane i of the
 // member's interior box, tiles numbered k-block fastest, then j-block,
 // then i, counted from the box's k0, lo[1], lo[0].
-template <typename T, typename I, bool E_SIDE>
+template <typename T, typename I, bool E_SIDE, bool CT>
 __global__ void __launch_bounds__(256, 8) k_interior_batch(const __grid_constant__ VolGroup<T, I> g,
                                                             const __grid_constant__ GroupBlocks gb,
                                                             const InteriorBox *__restrict__ boxes) {
@@ -93,21 +93,21 @@ __global__ void __launch_bounds__(256, 8) k_interior_batch(const __grid_constant
   const int j = in.lo[1] + static_cast<int>(t2 % gy) * 8 + static_cast<int>(threadIdx.x >> 5);
   const int k = in.k0 + static_cast<int>(t % gx) * 32 + static_cast<int>(threadIdx.x & 31);
   if (k < in.lo[2] || k > in.hi[2] || j > in.hi[1]) return;
-  if (E_SIDE) e_fast<T, I, 1>(p, p.table, 18, i, j, k);
-  else h_fast<T, I, 1>(p, p.table + 9, 18, i, j, k);
+  if (E_SIDE) e_fast<T, I, 1, CT>(p, p.table, 18, i, j, k);
+  else h_fast<T, I, 1, CT>(p, p.table + 9, 18, i, j, k);
 }
 
 // Shell: the member's shell blocks (numbered as in the single-simulation
 // shell kernel).
-template <typename T, typename I, bool E_SIDE>
+template <typename T, typename I, bool E_SIDE, bool CT>
 __global__ void __launch_bounds__(256, 6) k_shell_batch(const __grid_constant__ VolGroup<T, I> g,
                                                          const __grid_constant__ GroupBlocks gb,
                                                          const ShellBoxes *__restrict__ shells) {
   const int q = group_member(gb);
   int cls, i, j, k;
   if (!shell_cell(shells[q], blockIdx.x - gb.first[q], cls, i, j, k)) return;
-  if (E_SIDE) e_shell_cell(g.m[q], cls, i, j, k);
-  else h_shell_cell(g.m[q], cls, i, j, k);
+  if (E_SIDE) e_shell_cell<T, I, CT>(g.m[q], cls, i, j, k);
+  else h_shell_cell<T, I, CT>(g.m[q], cls, i, j, k);
 }
 
 // TFSF E or H corrections: tile = 256 consecutive surface cells.

@@ -80,6 +80,7 @@ struct VolCore {
   T *H[3];
   const I *idx;
   const T *table;      // [n_mat][18], reference coefficient order
+  const T *ctable;     // [n_mat][2][4]: compact table (compact_coefs)
   int n_mat;
   CpmlAxis<T> cp[3];
   Psi<T> psi;

@@ -98,6 +98,7 @@ struct xfdtd_handle {
   void *F[6] = {};
   void *idx = nullptr;
   void *table = nullptr;
+  void *ctable = nullptr;   // compact coefficient table (volume.cuh coefs)
   int n_mat = 0;
   bool smem_table = false;
   size_t smem_bytes = 0;
@@ -161,7 +162,7 @@ struct xfdtd_handle {
   xg::InteriorBox vin[2] = {};
   xg::ShellBoxes vshell[2] = {};
   long long vin_cells[2] = {}, vshell_cells[2] = {};
-  int shell_minb[2] = {4, 4};
+  int shell_var[2] = {0, 0};   // shell-kernel variant per side
 
   // fused E/H sweep (sweep.cuh): the state of step t+1 goes to the second
   // buffer set, swapped with the first after each step
@@ -330,6 +331,7 @@ xg::VolParams<T, I> vol_params(xfdtd_handle *h) {
   }
   p.idx = static_cast<const I *>(h->idx);
   p.table = static_cast<const T *>(h->table);
+  p.ctable = static_cast<const T *>(h->ctable);
   p.n_mat = h->n_mat;
   for (int a = 0; a < 3; ++a) {
     p.cp[a].n_layers = h->L[a];
@@ -378,11 +380,15 @@ struct Variant {
   int bx, by, bz;
   int nc;
   bool smem;
+  bool ct;   // coefficients from the compact table (volume.cuh coefs)
 };
 constexpr Variant kVariants[] = {
-    {8, 32, 4, 2, 1, true},   {8, 32, 4, 2, 1, false},  {8, 32, 8, 1, 1, false}, {8, 64, 4, 1, 1, false},
-    {8, 128, 2, 1, 1, false}, {6, 32, 4, 2, 2, false},  {6, 32, 8, 1, 2, false}, {6, 64, 4, 1, 2, false},
-    {1, 32, 4, 2, 2, false},  {1, 32, 4, 2, 1, false},  {8, 32, 4, 2, 2, false}, {6, 32, 4, 2, 1, true},
+    {8, 32, 4, 2, 1, true, false},   {8, 32, 4, 2, 1, false, false}, {8, 32, 8, 1, 1, false, false},
+    {8, 64, 4, 1, 1, false, false},  {8, 128, 2, 1, 1, false, false}, {6, 32, 4, 2, 2, false, false},
+    {6, 32, 8, 1, 2, false, false},  {6, 64, 4, 1, 2, false, false},  {1, 32, 4, 2, 2, false, false},
+    {1, 32, 4, 2, 1, false, false},  {8, 32, 4, 2, 2, false, false},  {6, 32, 4, 2, 1, true, false},
+    {8, 32, 4, 2, 1, false, true},   {8, 32, 8, 1, 1, false, true},   {1, 32, 4, 2, 1, false, true},
+    {6, 32, 4, 2, 1, true, true},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 static_assert(kNumVariants <= 16, "tune_ms holds 16 variants per side");
@@ -390,7 +396,7 @@ static_assert(kNumVariants <= 16, "tune_ms holds 16 variants per side");
 // A shared-memory-table variant needs the table to fit (smem_table).
 bool variant_allowed(const xfdtd_handle *h, const Variant &v) { return !v.smem || h->smem_table; }
 
-template <typename T, typename I, bool S, int MB, int NC>
+template <typename T, typename I, bool S, int MB, int NC, bool CT>
 void launch_vol_v(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, const Variant &v) {
   xg::InteriorBox in = h->vin[e_side ? 0 : 1];
   in.k0 = (in.lo[2] / v.bx) * v.bx;   // rows of threads start on the block's k alignment
@@ -399,33 +405,69 @@ void launch_vol_v(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, co
   dim3 block(v.bx, v.by, v.bz);
   dim3 grid((nk + v.bx - 1) / v.bx, (nj + v.by - 1) / v.by, (ni + zc - 1) / zc);
   const size_t smem = S ? h->smem_bytes : 0;
-  if (e_side) xg::k_update_e<T, I, S, MB, NC><<<grid, block, smem, h->stream>>>(p, in);
-  else xg::k_update_h<T, I, S, MB, NC><<<grid, block, smem, h->stream>>>(p, in);
+  if (e_side) xg::k_update_e<T, I, S, MB, NC, CT><<<grid, block, smem, h->stream>>>(p, in);
+  else xg::k_update_h<T, I, S, MB, NC, CT><<<grid, block, smem, h->stream>>>(p, in);
 }
 
 
-// Shell-kernel register caps the autotuner chooses from (minimum resident
-// 256-thread blocks per SM).
-constexpr int kShellMinb[] = {4, 6};
-constexpr int kNumShellVariants = 2;
+// Shell-kernel variants the autotuner chooses from: register cap (minimum
+// resident 256-thread blocks per SM) and table form (compact or full).
+struct ShellVariant {
+  int minb;
+  bool ct;
+};
+constexpr ShellVariant kShellVariants[] = {{4, false}, {6, false}, {4, true}, {6, true}};
+constexpr int kNumShellVariants = sizeof(kShellVariants) / sizeof(kShellVariants[0]);
+
+template <typename T, typename I, int MB, bool CT>
+void launch_shell_v(xfdtd_handle *h, bool e_side, cudaStream_t st) {
+  const xg::ShellBoxes &s = h->vshell[e_side ? 0 : 1];
+  const auto p = vol_params<T, I>(h);
+  if (e_side) xg::k_update_e_shell<T, I, MB, CT><<<s.blocks, 256, 0, st>>>(p, s);
+  else xg::k_update_h_shell<T, I, MB, CT><<<s.blocks, 256, 0, st>>>(p, s);
+}
 
 template <typename T, typename I>
-void launch_shell(xfdtd_handle *h, bool e_side, int minb = 0, cudaStream_t st = nullptr) {
+void launch_shell(xfdtd_handle *h, bool e_side, int var = -1, cudaStream_t st = nullptr) {
   const int side = e_side ? 0 : 1;
-  const xg::ShellBoxes &s = h->vshell[side];
-  if (s.blocks == 0) return;
-  if (minb == 0) minb = h->shell_minb[side];
-  const auto p = vol_params<T, I>(h);
-  const unsigned blocks = s.blocks;
+  if (h->vshell[side].blocks == 0) return;
+  if (var < 0) var = h->shell_var[side];
+  const ShellVariant &v = kShellVariants[var];
   if (!st) st = h->stream;
-  if (minb == 6) {
-    if (e_side) xg::k_update_e_shell<T, I, 6><<<blocks, 256, 0, st>>>(p, s);
-    else xg::k_update_h_shell<T, I, 6><<<blocks, 256, 0, st>>>(p, s);
+  if (v.minb == 6) {
+    if (v.ct) launch_shell_v<T, I, 6, true>(h, e_side, st);
+    else launch_shell_v<T, I, 6, false>(h, e_side, st);
   } else {
-    if (e_side) xg::k_update_e_shell<T, I, 4><<<blocks, 256, 0, st>>>(p, s);
-    else xg::k_update_h_shell<T, I, 4><<<blocks, 256, 0, st>>>(p, s);
+    if (v.ct) launch_shell_v<T, I, 4, true>(h, e_side, st);
+    else launch_shell_v<T, I, 4, false>(h, e_side, st);
   }
   XCHECK(cudaGetLastError());
+}
+
+// The compact coefficient table (volume.cuh coefs): per material and side
+// (E: coefficients 0..8, H: 9..17) c0, c1, c2 and a flag, 0 when the
+// side's three components share their coefficients bit for bit in the
+// field precision (c0 = c3 = c6, c1 = c4 = c7, c2 = c5 = c8), else 1.
+template <typename T>
+void *compact_table_t(xfdtd_handle *h, const double *table, int n_mat) {
+  std::vector<T> ct(static_cast<size_t>(n_mat) * 8, T(0));
+  for (int m = 0; m < n_mat; ++m)
+    for (int half = 0; half < 2; ++half) {
+      T c[9];
+      for (int q = 0; q < 9; ++q) c[q] = static_cast<T>(table[static_cast<size_t>(m) * XFDTD_N_COEFF + 9 * half + q]);
+      bool same = true;
+      for (int t = 0; t < 3; ++t)
+        same = same && std::memcmp(&c[t], &c[t + 3], sizeof(T)) == 0 && std::memcmp(&c[t], &c[t + 6], sizeof(T)) == 0;
+      T *o = ct.data() + static_cast<size_t>(m) * 8 + 4 * half;
+      o[0] = c[0];
+      o[1] = c[1];
+      o[2] = c[2];
+      o[3] = same ? T(0) : T(1);
+    }
+  return h->upload<T>(ct.data(), ct.size());
+}
+void *compact_table(xfdtd_handle *h, const double *table, int n_mat) {
+  return h->precision == XFDTD_FP64 ? compact_table_t<double>(h, table, n_mat) : compact_table_t<float>(h, table, n_mat);
 }
 
 // Multiply-shift constants for dividing n < 2^31 by d (Granlund and
@@ -655,15 +697,18 @@ void launch_volume(xfdtd_handle *h, bool e_side, int var = -1) {
   auto p = vol_params<T, I>(h);
   if (var < 0) var = e_side ? h->var_e : h->var_h;
   const Variant &v = kVariants[var];
-  const int key = v.minb * 100 + v.nc * 10 + (v.smem ? 1 : 0);
+  const int key = (v.ct ? 1000 : 0) + v.minb * 100 + v.nc * 10 + (v.smem ? 1 : 0);
   switch (key) {
-    case 811: launch_vol_v<T, I, true, 8, 1>(h, p, e_side, v); break;
-    case 810: launch_vol_v<T, I, false, 8, 1>(h, p, e_side, v); break;
-    case 820: launch_vol_v<T, I, false, 8, 2>(h, p, e_side, v); break;
-    case 620: launch_vol_v<T, I, false, 6, 2>(h, p, e_side, v); break;
-    case 611: launch_vol_v<T, I, true, 6, 1>(h, p, e_side, v); break;
-    case 120: launch_vol_v<T, I, false, 1, 2>(h, p, e_side, v); break;
-    case 110: launch_vol_v<T, I, false, 1, 1>(h, p, e_side, v); break;
+    case 811: launch_vol_v<T, I, true, 8, 1, false>(h, p, e_side, v); break;
+    case 810: launch_vol_v<T, I, false, 8, 1, false>(h, p, e_side, v); break;
+    case 820: launch_vol_v<T, I, false, 8, 2, false>(h, p, e_side, v); break;
+    case 620: launch_vol_v<T, I, false, 6, 2, false>(h, p, e_side, v); break;
+    case 611: launch_vol_v<T, I, true, 6, 1, false>(h, p, e_side, v); break;
+    case 120: launch_vol_v<T, I, false, 1, 2, false>(h, p, e_side, v); break;
+    case 110: launch_vol_v<T, I, false, 1, 1, false>(h, p, e_side, v); break;
+    case 1810: launch_vol_v<T, I, false, 8, 1, true>(h, p, e_side, v); break;
+    case 1110: launch_vol_v<T, I, false, 1, 1, true>(h, p, e_side, v); break;
+    case 1611: launch_vol_v<T, I, true, 6, 1, true>(h, p, e_side, v); break;
     default: throw Err{XFDTD_ERR_STATE, "volume-kernel variant without an instantiation"};
   }
   XCHECK(cudaGetLastError());
@@ -673,10 +718,12 @@ void launch_volume(xfdtd_handle *h, bool e_side, int var = -1) {
 // shared memory (needed above 48 KB).
 template <typename T, typename I>
 void smem_attr(int bytes) {
-  XCHECK(cudaFuncSetAttribute(xg::k_update_e<T, I, true, 8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  XCHECK(cudaFuncSetAttribute(xg::k_update_h<T, I, true, 8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  XCHECK(cudaFuncSetAttribute(xg::k_update_e<T, I, true, 6, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  XCHECK(cudaFuncSetAttribute(xg::k_update_h<T, I, true, 6, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_update_e<T, I, true, 8, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_update_h<T, I, true, 8, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_update_e<T, I, true, 6, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_update_h<T, I, true, 6, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_update_e<T, I, true, 6, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  XCHECK(cudaFuncSetAttribute(xg::k_update_h<T, I, true, 6, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
 }
 
 // Times every variant of the E and H kernels on the handle's current state
@@ -715,16 +762,16 @@ void autotune_t(xfdtd_handle *h, int trials) {
     if (h->vshell_cells[side]) {
       best_shell = 1e30f;
       for (int v = 0; v < kNumShellVariants; ++v) {
-        launch_shell<T, I>(h, side == 0, kShellMinb[v]);
+        launch_shell<T, I>(h, side == 0, v);
         XCHECK(cudaEventRecord(a, h->stream));
-        for (int r = 0; r < trials; ++r) launch_shell<T, I>(h, side == 0, kShellMinb[v]);
+        for (int r = 0; r < trials; ++r) launch_shell<T, I>(h, side == 0, v);
         XCHECK(cudaEventRecord(b, h->stream));
         XCHECK(cudaEventSynchronize(b));
         float ms = 0;
         XCHECK(cudaEventElapsedTime(&ms, a, b));
         if (ms / trials < best_shell) {
           best_shell = ms / trials;
-          h->shell_minb[side] = kShellMinb[v];
+          h->shell_var[side] = v;
         }
       }
     }
@@ -910,7 +957,7 @@ void volume_pair(xfdtd_handle *h, bool e_side) {
     XCHECK(cudaEventRecord(h->ev_vfork[side], h->stream));
     XCHECK(cudaStreamWaitEvent(h->shell, h->ev_vfork[side], 0));
     prof_begin(h, e_side ? 11 : 12, h->shell);
-    launch_shell<T, I>(h, e_side, 0, h->shell);
+    launch_shell<T, I>(h, e_side, -1, h->shell);
     prof_end(h, h->shell);
     XCHECK(cudaEventRecord(h->ev_vjoin[side], h->shell));
   } else if (sh) {
@@ -1118,6 +1165,7 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   h->n_mat = pl->n_materials;
   h->table_host.assign(pl->coeff_table, pl->coeff_table + static_cast<size_t>(pl->n_materials) * XFDTD_N_COEFF);
   h->table = h->upload_real(pl->coeff_table, static_cast<size_t>(pl->n_materials) * XFDTD_N_COEFF);
+  h->ctable = compact_table(h, pl->coeff_table, pl->n_materials);
   h->smem_bytes = static_cast<size_t>(pl->n_materials) * 9 * h->esize;
   h->smem_table = h->smem_bytes <= 96 * 1024;
   if (h->smem_table && h->smem_bytes > 48 * 1024) {
@@ -1714,6 +1762,7 @@ struct xfdtd_batch {
   std::vector<xfdtd_handle *> m;
   int device = 0, precision = XFDTD_FP64, idx_bytes = 1, flags = 0;
   int n_sm = 152;
+  bool ct = false;   // volume kernels read the compact coefficient table (members with many materials)
   cudaStream_t stream = nullptr;
   cudaStream_t shell = nullptr;   // shell kernels, beside the interior kernels
   cudaEvent_t ev_fork[2] = {}, ev_join[2] = {};
@@ -1920,13 +1969,25 @@ void batch_enqueue_t(xfdtd_batch *b, long long s) {
       const size_t base = g * xg::kBatchGroup;
       const unsigned nsh = l.sh[side].first[l.sh[side].n], nin = l.in[side].first[l.in[side].n];
       if (nsh) {
-        if (e_side) xg::k_shell_batch<T, I, true><<<nsh, 256, 0, b->shell>>>(vg, l.sh[side], b->vshell[side] + base);
-        else xg::k_shell_batch<T, I, false><<<nsh, 256, 0, b->shell>>>(vg, l.sh[side], b->vshell[side] + base);
+        const xg::ShellBoxes *sb = b->vshell[side] + base;
+        if (b->ct) {
+          if (e_side) xg::k_shell_batch<T, I, true, true><<<nsh, 256, 0, b->shell>>>(vg, l.sh[side], sb);
+          else xg::k_shell_batch<T, I, false, true><<<nsh, 256, 0, b->shell>>>(vg, l.sh[side], sb);
+        } else {
+          if (e_side) xg::k_shell_batch<T, I, true, false><<<nsh, 256, 0, b->shell>>>(vg, l.sh[side], sb);
+          else xg::k_shell_batch<T, I, false, false><<<nsh, 256, 0, b->shell>>>(vg, l.sh[side], sb);
+        }
         ++launched;
       }
       if (nin) {
-        if (e_side) xg::k_interior_batch<T, I, true><<<nin, 256, 0, st>>>(vg, l.in[side], b->vin[side] + base);
-        else xg::k_interior_batch<T, I, false><<<nin, 256, 0, st>>>(vg, l.in[side], b->vin[side] + base);
+        const xg::InteriorBox *ib = b->vin[side] + base;
+        if (b->ct) {
+          if (e_side) xg::k_interior_batch<T, I, true, true><<<nin, 256, 0, st>>>(vg, l.in[side], ib);
+          else xg::k_interior_batch<T, I, false, true><<<nin, 256, 0, st>>>(vg, l.in[side], ib);
+        } else {
+          if (e_side) xg::k_interior_batch<T, I, true, false><<<nin, 256, 0, st>>>(vg, l.in[side], ib);
+          else xg::k_interior_batch<T, I, false, false><<<nin, 256, 0, st>>>(vg, l.in[side], ib);
+        }
         ++launched;
       }
     }
@@ -2060,6 +2121,8 @@ int xfdtd_batch_create(xfdtd_handle *const *members, int n, int flags, xfdtd_bat
         if (h->d.nx >= 65535 || h->d.ny >= 2040 || h->d.nz >= 8160) invalid("batch member grid too large for the tile numbering");
         for (int r = 0; r < q; ++r)
           if (members[r] == h) invalid("a handle appears twice in the batch");
+        // many materials scatter the nine full-table loads per cell: read the compact table
+        if (h->n_mat > 16) b->ct = true;
       }
       XCHECK(cudaSetDevice(b->device));
       int sms = 0;

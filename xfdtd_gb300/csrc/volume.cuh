@@ -50,6 +50,43 @@ __device__ __forceinline__ const T *load_table(const VolCore<T, I> &p, int half,
   return st;
 }
 
+// The 9 coefficients of material m for one side (half 0: E, 1: H).  On a
+// uniform grid the three components of a side share their coefficients
+// (c0 = c3 = c6, c1 = c4 = c7, c2 = c5 = c8, bit for bit); the compact
+// table holds c0, c1, c2 and a flag per material and side, one 16-byte load
+// instead of nine gathered ones.  A material whose coefficients differ
+// (flag != 0: a lumped element's override) takes them from the full table
+// (tab: this side's half, stride ts).  CT = false reads every material
+// from the full table: for few materials its nine loads hit L1 and need no
+// second dependent load, and the autotuner keeps whichever form is faster.
+template <typename T, typename I, bool CT>
+__device__ __forceinline__ void coefs(const VolCore<T, I> &p, const T *tab, int ts, unsigned m, int half, T out[9]) {
+  if constexpr (!CT) {
+    const T *t = tab + m * static_cast<unsigned>(ts);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) out[q] = t[q];
+    return;
+  }
+  const T *cc = p.ctable + m * 8 + half * 4;
+  T a, b, c, f;
+  if constexpr (sizeof(T) == 4) {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(cc));
+    a = v.x, b = v.y, c = v.z, f = v.w;
+  } else {
+    const double2 v0 = __ldg(reinterpret_cast<const double2 *>(cc)), v1 = __ldg(reinterpret_cast<const double2 *>(cc) + 1);
+    a = v0.x, b = v0.y, c = v1.x, f = v1.y;
+  }
+  if (f == T(0)) {
+    out[0] = out[3] = out[6] = a;
+    out[1] = out[4] = out[7] = b;
+    out[2] = out[5] = out[8] = c;
+  } else {
+    const T *t = tab + m * static_cast<unsigned>(ts);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) out[q] = t[q];
+  }
+}
+
 // Rounded arithmetic with the contractions spelled out, so that every kernel
 // that updates a cell (split E/H kernels, fused sweep) gives the same bits.
 template <typename T>
@@ -345,7 +382,7 @@ __device__ __forceinline__ void h_general(const VolCore<T, I> &p, const T *c, in
 // E update of one cell by the general path.  It serves any cell: a plain
 // cell gets the bits of the fast path (same expressions, no CPML terms).
 // AXES as in e_general.
-template <typename T, typename I, int AXES = 7>
+template <typename T, typename I, int AXES = 7, bool CT = false>
 __device__ __forceinline__ void e_cell_general(const VolCore<T, I> &p, const T *tab, int ts, int i, int j, int k) {
   constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
@@ -366,7 +403,8 @@ __device__ __forceinline__ void e_cell_general(const VolCore<T, I> &p, const T *
   h.hz_j = !SY || j > 0 ? __ldg(Hz + b - usj) : T(0);
   h.hy_i = !SX || i > 0 ? __ldg(Hy + b - usi) : T(0);
   h.hz_i = !SX || i > 0 ? __ldg(Hz + b - usi) : T(0);
-  const T *c = tab + static_cast<unsigned>(__ldg(p.idx + b)) * ts;
+  T c[9];
+  coefs<T, I, CT>(p, tab, ts, static_cast<unsigned>(__ldg(p.idx + b)), 0, c);
   T ex = Ex[b], ey = Ey[b], ez = Ez[b];
   bool w[3];
   e_general<T, I, false, AXES>(p, c, i, j, k, h, p.psi, p.psi, true, ex, ey, ez, w);
@@ -377,7 +415,7 @@ __device__ __forceinline__ void e_cell_general(const VolCore<T, I> &p, const T *
 
 // NC plain cells (i0 .. i0+NC-1) of one (j, k) column: every load is issued
 // before any store, and the H at i-1 of cell c+1 is cell c's own.
-template <typename T, typename I, int NC>
+template <typename T, typename I, int NC, bool CT = false>
 __device__ __forceinline__ void e_fast(const VolCore<T, I> &p, const T *tab, int ts, int i0, int j, int k) {
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const unsigned b0 = static_cast<unsigned>(i0) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
@@ -388,7 +426,7 @@ __device__ __forceinline__ void e_fast(const VolCore<T, I> &p, const T *tab, int
   T *__restrict__ Ey = p.E[1];
   T *__restrict__ Ez = p.E[2];
   T hx[NC], hy[NC + 1], hz[NC + 1], hx_k[NC], hy_k[NC], hx_j[NC], hz_j[NC], ex[NC], ey[NC], ez[NC];
-  const T *c[NC];
+  unsigned m[NC];
   hy[0] = __ldg(Hy + b0 - usi);
   hz[0] = __ldg(Hz + b0 - usi);
 #pragma unroll
@@ -401,7 +439,7 @@ __device__ __forceinline__ void e_fast(const VolCore<T, I> &p, const T *tab, int
     hy_k[q] = __ldg(Hy + b - 1);
     hx_j[q] = __ldg(Hx + b - usj);
     hz_j[q] = __ldg(Hz + b - usj);
-    c[q] = tab + static_cast<unsigned>(__ldg(p.idx + b)) * ts;
+    m[q] = __ldg(p.idx + b);
     ex[q] = Ex[b];
     ey[q] = Ey[b];
     ez[q] = Ez[b];
@@ -410,7 +448,9 @@ __device__ __forceinline__ void e_fast(const VolCore<T, I> &p, const T *tab, int
   for (int q = 0; q < NC; ++q) {
     const unsigned b = b0 + q * usi;
     const ECurl<T> h{hx[q], hy[q + 1], hz[q + 1], hx_k[q], hy_k[q], hx_j[q], hz_j[q], hy[q], hz[q]};
-    e_plain(c[q], h, ex[q], ey[q], ez[q]);
+    T c[9];
+    coefs<T, I, CT>(p, tab, ts, m[q], 0, c);
+    e_plain(c, h, ex[q], ey[q], ez[q]);
     Ex[b] = ex[q];
     Ey[b] = ey[q];
     Ez[b] = ez[q];
@@ -487,7 +527,7 @@ __device__ __forceinline__ bool shell_cell(const ShellBoxes &s, unsigned blk, in
 // MINB: minimum resident blocks per SM requested from the register
 // allocator (1 = no cap); NC: cells per thread along i.  The autotuner in
 // engine.cu picks both (and the block shape) per plan.
-template <typename T, typename I, bool SMEM_TABLE, int MINB, int NC>
+template <typename T, typename I, bool SMEM_TABLE, int MINB, int NC, bool CT>
 __global__ void __launch_bounds__(256, MINB) k_update_e(VolCore<T, I> p, InteriorBox in) {
   int ts;
   const T *tab = load_table<T, I, SMEM_TABLE>(p, 0, ts);
@@ -496,37 +536,37 @@ __global__ void __launch_bounds__(256, MINB) k_update_e(VolCore<T, I> p, Interio
   const int i0 = in.lo[0] + (blockIdx.z * blockDim.z + threadIdx.z) * NC;
   if (k < in.lo[2] || k > in.hi[2] || j > in.hi[1] || i0 > in.hi[0]) return;
   if (i0 + NC - 1 <= in.hi[0]) {
-    e_fast<T, I, NC>(p, tab, ts, i0, j, k);
+    e_fast<T, I, NC, CT>(p, tab, ts, i0, j, k);
     return;
   }
 #pragma unroll
   for (int q = 0; q < NC; ++q)
-    if (i0 + q <= in.hi[0]) e_fast<T, I, 1>(p, tab, ts, i0 + q, j, k);
+    if (i0 + q <= in.hi[0]) e_fast<T, I, 1, CT>(p, tab, ts, i0 + q, j, k);
 }
 
 // E update of one shell cell of box class cls (coefficient table read
 // through L1): the general path specialised per class.
-template <typename T, typename I>
+template <typename T, typename I, bool CT = false>
 __device__ __forceinline__ void e_shell_cell(const VolCore<T, I> &p, int cls, int i, int j, int k) {
   switch (cls) {
-    case 1: e_cell_general<T, I, 1>(p, p.table, 18, i, j, k); break;
-    case 2: e_cell_general<T, I, 2>(p, p.table, 18, i, j, k); break;
-    case 4: e_cell_general<T, I, 4>(p, p.table, 18, i, j, k); break;
-    case 5: e_cell_general<T, I, 5>(p, p.table, 18, i, j, k); break;
-    case 6: e_cell_general<T, I, 6>(p, p.table, 18, i, j, k); break;
-    default: e_cell_general<T, I, 7>(p, p.table, 18, i, j, k); break;
+    case 1: e_cell_general<T, I, 1, CT>(p, p.table, 18, i, j, k); break;
+    case 2: e_cell_general<T, I, 2, CT>(p, p.table, 18, i, j, k); break;
+    case 4: e_cell_general<T, I, 4, CT>(p, p.table, 18, i, j, k); break;
+    case 5: e_cell_general<T, I, 5, CT>(p, p.table, 18, i, j, k); break;
+    case 6: e_cell_general<T, I, 6, CT>(p, p.table, 18, i, j, k); break;
+    default: e_cell_general<T, I, 7, CT>(p, p.table, 18, i, j, k); break;
   }
 }
 
 // E update of the shell cells, the class uniform per block.
-template <typename T, typename I, int MINB>
+template <typename T, typename I, int MINB, bool CT>
 __global__ void __launch_bounds__(256, MINB) k_update_e_shell(VolCore<T, I> p, const __grid_constant__ ShellBoxes s) {
   int cls, i, j, k;
-  if (shell_cell(s, blockIdx.x, cls, i, j, k)) e_shell_cell(p, cls, i, j, k);
+  if (shell_cell(s, blockIdx.x, cls, i, j, k)) e_shell_cell<T, I, CT>(p, cls, i, j, k);
 }
 
 // H update of one cell by the general path (any cell, as e_cell_general).
-template <typename T, typename I, int AXES = 7>
+template <typename T, typename I, int AXES = 7, bool CT = false>
 __device__ __forceinline__ void h_cell_general(const VolCore<T, I> &p, const T *tab, int ts, int i, int j, int k) {
   constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
@@ -548,7 +588,8 @@ __device__ __forceinline__ void h_cell_general(const VolCore<T, I> &p, const T *
   e.ey_k = !SZ || k < nz ? __ldg(Ey + b + 1) : T(0);
   e.ex_j = !SY || j < ny ? __ldg(Ex + b + usj) : T(0);
   e.ez_j = !SY || j < ny ? __ldg(Ez + b + usj) : T(0);
-  const T *c = tab + static_cast<unsigned>(__ldg(p.idx + b)) * ts;
+  T c[9];
+  coefs<T, I, CT>(p, tab, ts, static_cast<unsigned>(__ldg(p.idx + b)), 1, c);
   T hx = Hx[b], hy = Hy[b], hz = Hz[b];
   bool w[3];
   h_general<T, I, AXES>(p, c, i, j, k, e, hx, hy, hz, w);
@@ -558,7 +599,7 @@ __device__ __forceinline__ void h_cell_general(const VolCore<T, I> &p, const T *
 }
 
 // NC plain cells of one column for H: the E at i+1 of cell c is cell c+1's own.
-template <typename T, typename I, int NC>
+template <typename T, typename I, int NC, bool CT = false>
 __device__ __forceinline__ void h_fast(const VolCore<T, I> &p, const T *tab, int ts, int i0, int j, int k) {
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   const unsigned b0 = static_cast<unsigned>(i0) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
@@ -569,7 +610,7 @@ __device__ __forceinline__ void h_fast(const VolCore<T, I> &p, const T *tab, int
   T *__restrict__ Hy = p.H[1];
   T *__restrict__ Hz = p.H[2];
   T ex[NC], ey[NC + 1], ez[NC + 1], ex_kp[NC], ey_kp[NC], ex_jp[NC], ez_jp[NC], hx[NC], hy[NC], hz[NC];
-  const T *c[NC];
+  unsigned m[NC];
 #pragma unroll
   for (int q = 0; q < NC; ++q) {
     const unsigned b = b0 + q * usi;
@@ -580,7 +621,7 @@ __device__ __forceinline__ void h_fast(const VolCore<T, I> &p, const T *tab, int
     ey_kp[q] = __ldg(Ey + b + 1);
     ex_jp[q] = __ldg(Ex + b + usj);
     ez_jp[q] = __ldg(Ez + b + usj);
-    c[q] = tab + static_cast<unsigned>(__ldg(p.idx + b)) * ts;
+    m[q] = __ldg(p.idx + b);
     hx[q] = Hx[b];
     hy[q] = Hy[b];
     hz[q] = Hz[b];
@@ -591,14 +632,16 @@ __device__ __forceinline__ void h_fast(const VolCore<T, I> &p, const T *tab, int
   for (int q = 0; q < NC; ++q) {
     const unsigned b = b0 + q * usi;
     const HCurl<T> e{ex[q], ey[q], ez[q], ex_kp[q], ey_kp[q], ex_jp[q], ez_jp[q], ey[q + 1], ez[q + 1]};
-    h_plain(c[q], e, hx[q], hy[q], hz[q]);
+    T c[9];
+    coefs<T, I, CT>(p, tab, ts, m[q], 1, c);
+    h_plain(c, e, hx[q], hy[q], hz[q]);
     Hx[b] = hx[q];
     Hy[b] = hy[q];
     Hz[b] = hz[q];
   }
 }
 
-template <typename T, typename I, bool SMEM_TABLE, int MINB, int NC>
+template <typename T, typename I, bool SMEM_TABLE, int MINB, int NC, bool CT>
 __global__ void __launch_bounds__(256, MINB) k_update_h(VolCore<T, I> p, InteriorBox in) {
   int ts;
   const T *tab = load_table<T, I, SMEM_TABLE>(p, 1, ts);
@@ -607,31 +650,31 @@ __global__ void __launch_bounds__(256, MINB) k_update_h(VolCore<T, I> p, Interio
   const int i0 = in.lo[0] + (blockIdx.z * blockDim.z + threadIdx.z) * NC;
   if (k < in.lo[2] || k > in.hi[2] || j > in.hi[1] || i0 > in.hi[0]) return;
   if (i0 + NC - 1 <= in.hi[0]) {
-    h_fast<T, I, NC>(p, tab, ts, i0, j, k);
+    h_fast<T, I, NC, CT>(p, tab, ts, i0, j, k);
     return;
   }
 #pragma unroll
   for (int q = 0; q < NC; ++q)
-    if (i0 + q <= in.hi[0]) h_fast<T, I, 1>(p, tab, ts, i0 + q, j, k);
+    if (i0 + q <= in.hi[0]) h_fast<T, I, 1, CT>(p, tab, ts, i0 + q, j, k);
 }
 
 
-template <typename T, typename I>
+template <typename T, typename I, bool CT = false>
 __device__ __forceinline__ void h_shell_cell(const VolCore<T, I> &p, int cls, int i, int j, int k) {
   switch (cls) {
-    case 1: h_cell_general<T, I, 1>(p, p.table + 9, 18, i, j, k); break;
-    case 2: h_cell_general<T, I, 2>(p, p.table + 9, 18, i, j, k); break;
-    case 4: h_cell_general<T, I, 4>(p, p.table + 9, 18, i, j, k); break;
-    case 5: h_cell_general<T, I, 5>(p, p.table + 9, 18, i, j, k); break;
-    case 6: h_cell_general<T, I, 6>(p, p.table + 9, 18, i, j, k); break;
-    default: h_cell_general<T, I, 7>(p, p.table + 9, 18, i, j, k); break;
+    case 1: h_cell_general<T, I, 1, CT>(p, p.table + 9, 18, i, j, k); break;
+    case 2: h_cell_general<T, I, 2, CT>(p, p.table + 9, 18, i, j, k); break;
+    case 4: h_cell_general<T, I, 4, CT>(p, p.table + 9, 18, i, j, k); break;
+    case 5: h_cell_general<T, I, 5, CT>(p, p.table + 9, 18, i, j, k); break;
+    case 6: h_cell_general<T, I, 6, CT>(p, p.table + 9, 18, i, j, k); break;
+    default: h_cell_general<T, I, 7, CT>(p, p.table + 9, 18, i, j, k); break;
   }
 }
 
-template <typename T, typename I, int MINB>
+template <typename T, typename I, int MINB, bool CT>
 __global__ void __launch_bounds__(256, MINB) k_update_h_shell(VolCore<T, I> p, const __grid_constant__ ShellBoxes s) {
   int cls, i, j, k;
-  if (shell_cell(s, blockIdx.x, cls, i, j, k)) h_shell_cell(p, cls, i, j, k);
+  if (shell_cell(s, blockIdx.x, cls, i, j, k)) h_shell_cell<T, I, CT>(p, cls, i, j, k);
 }
 
 }  // namespace xg
