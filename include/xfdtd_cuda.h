@@ -214,6 +214,10 @@ int xfdtd_autotune(xfdtd_handle *h, int trials);
  * xfdtd_set_kernel_variant takes the same variant for both. */
 int xfdtd_kernel_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h, double *trial_ms);
 int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant);
+/* Variants of the shell kernels (walls and CPML slabs): how many, the ones
+ * in use for E and H; and fixing them (all give the same bits). */
+int xfdtd_shell_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h);
+int xfdtd_set_shell_variant(xfdtd_handle *h, int e_variant, int h_variant);
 /* Cells of the split volume update: cells[0] / [1] the E update's interior
  * (plain on every axis, the interior kernel) and shell (walls and CPML
  * slabs, the shell kernel); cells[2] / [3] the same for H. */

@@ -103,6 +103,60 @@ def thin_wire(steps=300):
     return S.Scene(dl, objects, boundaries, lumped_elements=le, monitors=mons, cfl=0.99), steps
 
 
+def _boxed(dims, dl, boundaries, steps, cfl=0.97):
+    """A box of `dims` cells with a dielectric block, a lossy cube and a
+    soft current source off the centre, and one voltage monitor."""
+    objects = [
+        S.Object("domain", S.Cube([0, 0, 0], [v * dl for v in dims]), S.Material("air", 1, 1, 0, 0)),
+        S.Object("block", S.Cube([v * dl * 0.3 for v in dims], [max(1, v // 3) * dl for v in dims]),
+                 S.Material("b", 3.0, 1.0, 0.0, 0.0)),
+        S.Object("lossy", S.Cube([v * dl * 0.6 for v in dims], [max(1, v // 5) * dl for v in dims]),
+                 S.Material("l", 1.5, 1.2, 0.2, 0.0)),
+    ]
+    c = [max(1, int(v * 0.45)) for v in dims]
+    src = S.CurrentSource(S.Cube([q * dl for q in c], [dl, dl, dl]), S.ZP, 1e3,
+                          S.CosineModulatedGaussianWaveform(1e-3, 30e-12, 120e-12, 8e9))
+    mon = S.VoltageMonitor(S.Cube([(q + 1) * dl for q in c], [dl, dl, dl]), S.ZP)
+    return S.Scene(dl, objects, boundaries, lumped_elements=[src], monitors=[mon], cfl=cfl), steps
+
+
+def _six(t):
+    return [S.PML(o, t) for o in (S.XN, S.XP, S.YN, S.YP, S.ZN, S.ZP)]
+
+
+def tiny_box(steps=120):
+    """10 x 9 x 8 cells inside a 4-cell CPML on every face: plain runs of 1-2
+    cells per axis, too short for the interior's line cut."""
+    return _boxed((10, 9, 8), 2e-3, _six(4), steps)
+
+
+def pec_box(steps=150):
+    """No CPML: PEC walls only, odd extents (23 x 18 x 37)."""
+    return _boxed((23, 18, 37), 2e-3, [], steps)
+
+
+def long_z(steps=120):
+    """A long z axis (14 x 12 x 90 + 5-cell CPML): several 128-byte lines per
+    row, so the interior's k range is cut on lines."""
+    return _boxed((14, 12, 90), 2e-3, _six(5), steps)
+
+
+def one_sided(steps=150):
+    """CPML on XP and ZN only, 21 x 26 x 40: the interior touches the walls on
+    the other faces."""
+    return _boxed((21, 26, 40), 2e-3, [S.PML(S.XP, 6), S.PML(S.ZN, 9)], steps)
+
+
+# Scenes for the volume split (interior box and CPML/wall shell), compared
+# against the oracle at test time (no golden fixtures).
+SPLIT_SCENES = {
+    "tiny_box": tiny_box,
+    "pec_box": pec_box,
+    "long_z": long_z,
+    "one_sided": one_sided,
+}
+
+
 def rel_err(a, b):
     """max |a - b| / max |b| (0 when both vanish)."""
     a = np.asarray(a)

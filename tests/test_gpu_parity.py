@@ -162,6 +162,53 @@ def test_invalid_plans_rejected():
         X.Simulation(sc2, st2)
 
 
+@pytest.mark.parametrize("name", list(scenes.SPLIT_SCENES))
+def test_volume_split_shapes_fp64(name):
+    """Grids that stress the split of each volume update into an interior
+    kernel and a shell kernel: no interior, PEC walls only, a long k range
+    cut on 128-byte lines, CPML on two faces.  Fields and monitor against
+    the oracle; interior and shell cells partition the component box."""
+    sc, st = scenes.SPLIT_SCENES[name]()
+    o = O.OracleSim(sc, st)
+    o.step(st)
+    for precision in ("fp64", "fp32"):
+        g = X.Simulation(sc, st, precision=precision)
+        g.step(st)
+        sp = g.volume_split()
+        n = g.n
+        total = (n[0] + 1) * (n[1] + 1) * (n[2] + 1)
+        assert sp["e_interior"] + sp["e_shell"] == total and sp["h_interior"] + sp["h_shell"] == total, sp
+        if precision == "fp32":
+            continue
+        for c in range(6):
+            e = scenes.rel_err(g.read_field(c), o.read_field(c))
+            assert e <= TOL, f"{name} component {c}: rel err {e:.3e}"
+        e = scenes.rel_err(g.read_monitor(0), o.read_monitor(0))
+        assert e <= TOL, f"{name} monitor: rel err {e:.3e}"
+
+
+@pytest.mark.parametrize("name", ["heterogeneous", "oblique"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_every_shell_variant_is_bitwise_identical(name, precision):
+    """The shell kernel's variants (register caps x full or compact
+    coefficient table), with every interior variant's table form: the
+    heterogeneous scene has random materials and a current source whose
+    coefficient override falls back to the full table."""
+    sc, st = scenes.SCENES[name](steps=40)
+    ref = X.Simulation(sc, st, precision=precision, autotune=False, fused=False)
+    ref.step(st)
+    want = [ref.read_field(c) for c in range(6)]
+    n = ref.shell_variants()["n"]
+    assert n >= 4
+    for v in range(n):
+        g = X.Simulation(sc, st, precision=precision, autotune=False, fused=False)
+        g.set_shell_variant(v, v)
+        g.set_kernel_variant(12 + v % 4, 12 + v % 4)   # the compact-table interior variants
+        g.step(st)
+        for c in range(6):
+            assert np.array_equal(g.read_field(c), want[c]), (name, precision, v, c)
+
+
 def test_every_kernel_variant_is_bitwise_identical():
     """The autotuner's variants (split kernels: register caps x block shapes
     x cells per thread x table placement; fused sweep: register caps x

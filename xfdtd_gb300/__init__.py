@@ -86,6 +86,8 @@ def libs():
         cu.xfdtd_kernel_variants.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int), dp]
         cu.xfdtd_set_kernel_variant.argtypes = [C.c_void_p, C.c_int, C.c_int]
         cu.xfdtd_volume_split.argtypes = [C.c_void_p, P(C.c_int64)]
+        cu.xfdtd_shell_variants.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int)]
+        cu.xfdtd_set_shell_variant.argtypes = [C.c_void_p, C.c_int, C.c_int]
         cu.xfdtd_last_error.argtypes = [C.c_void_p]
         cu.xfdtd_last_error.restype = C.c_char_p
         cu.xfdtd_version.restype = C.c_char_p
@@ -304,6 +306,15 @@ class Simulation:
 
     def set_kernel_variant(self, e_variant: int, h_variant: int):
         self._check_engine(libs()[0].xfdtd_set_kernel_variant(self.engine, int(e_variant), int(h_variant)))
+
+    def shell_variants(self) -> dict:
+        """Number of shell-kernel variants and the ones in use for E and H."""
+        n, ce, ch = C.c_int(), C.c_int(), C.c_int()
+        self._check_engine(libs()[0].xfdtd_shell_variants(self.engine, C.byref(n), C.byref(ce), C.byref(ch)))
+        return {"n": n.value, "e": ce.value, "h": ch.value}
+
+    def set_shell_variant(self, e_variant: int, h_variant: int):
+        self._check_engine(libs()[0].xfdtd_set_shell_variant(self.engine, int(e_variant), int(h_variant)))
 
     def volume_split(self) -> dict:
         """Cells of the interior (plain) and shell (walls, CPML) kernels of

@@ -1702,6 +1702,28 @@ int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant) {
   });
 }
 
+int xfdtd_shell_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h) {
+  if (!h) return XFDTD_ERR_STATE;
+  if (n) *n = kNumShellVariants;
+  if (current_e) *current_e = h->shell_var[0];
+  if (current_h) *current_h = h->shell_var[1];
+  return XFDTD_OK;
+}
+
+int xfdtd_set_shell_variant(xfdtd_handle *h, int e_variant, int h_variant) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    if (e_variant < 0 || e_variant >= kNumShellVariants || h_variant < 0 || h_variant >= kNumShellVariants)
+      invalid("shell-kernel variant out of range");
+    h->shell_var[0] = e_variant;
+    h->shell_var[1] = h_variant;
+    if (h->gexec) {   // the captured graph holds the old launches
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+    }
+  });
+}
+
 int xfdtd_volume_split(xfdtd_handle *h, int64_t cells[4]) {
   if (!h || !cells) return XFDTD_ERR_STATE;
   return guarded(h, [&] {
