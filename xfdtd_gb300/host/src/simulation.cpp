@@ -20,12 +20,39 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <thread>
 #include <unordered_map>
+#include <vector>
 
 #include "../../../include/xfdtd_cuda.h"
 #include "xfdtd/xfdtd.h"
 
 namespace xfdtd {
+
+namespace {
+
+// f(q) for q in [0, n), split over the host's cores in contiguous chunks;
+// every q is independent (rasterisation and index raster: one cell or one
+// plane each).
+template <typename F>
+void parallel_for(size_t n, F &&f) {
+  const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nt = std::min<size_t>(std::min<size_t>(hw, 64), n);
+  if (nt <= 1) {
+    for (size_t q = 0; q < n; ++q) f(q);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const size_t per = (n + nt - 1) / nt;
+  for (size_t t = 0; t < nt; ++t)
+    pool.emplace_back([&, t] {
+      const size_t lo = t * per, hi = std::min(n, lo + per);
+      for (size_t q = lo; q < hi; ++q) f(q);
+    });
+  for (auto &th : pool) th.join();
+}
+
+}  // namespace
 
 void checkEngine(int status, xfdtd_handle *h) {
   if (status != XFDTD_OK)
@@ -226,11 +253,14 @@ void Simulation::init(size_t total_time_steps) {
       r1[a] = static_cast<size_t>(std::upper_bound(hc.begin(), hc.end(), hi[a] + tol) - hc.begin());
     }
     const Shape &sh = o->shape();
-    for (size_t i = r0[0]; i < r1[0]; ++i)
-      for (size_t j = r0[1]; j < r1[1]; ++j)
-        for (size_t k = r0[2]; k < r1[2]; ++k)
-          if (sh.isPointInside(PointVector{gs.hNode(0, i), gs.hNode(1, j), gs.hNode(2, k)}))
-            cell_mat[(i * ny + j) * nz + k] = id;
+    if (r1[0] > r0[0])
+      parallel_for(r1[0] - r0[0], [&](size_t q) {   // planes of one object: disjoint cells
+        const size_t i = r0[0] + q;
+        for (size_t j = r0[1]; j < r1[1]; ++j)
+          for (size_t k = r0[2]; k < r1[2]; ++k)
+            if (sh.isPointInside(PointVector{gs.hNode(0, i), gs.hNode(1, j), gs.hNode(2, k)}))
+              cell_mat[(i * ny + j) * nz + k] = id;
+      });
   }
   if (!_voxel_index.empty()) {
     if (_voxel_shape[0] != nx || _voxel_shape[1] != ny || _voxel_shape[2] != nz)
@@ -241,7 +271,9 @@ void Simulation::init(size_t total_time_steps) {
       vid[q] = intern(Props{m.getPermittivityE(), m.getPermeabilityM(), m.getElectricalConductivity(),
                             m.getMagneticConductivity()});
     }
-    for (size_t q = 0; q < cell_mat.size(); ++q) cell_mat[q] = vid[_voxel_index[q]];
+    parallel_for(nx, [&](size_t i) {
+      for (size_t q = i * ny * nz; q < (i + 1) * ny * nz; ++q) cell_mat[q] = vid[_voxel_index[q]];
+    });
   }
 
   // ---- coefficient table with per-cell overrides ------------------------
@@ -417,9 +449,10 @@ void Simulation::init(size_t total_time_steps) {
   std::map<Tuple, uint32_t> tuple_ids;
   for (uint32_t q = 0; q < table.size(); ++q) tuple_ids.emplace(table[q], q);
   std::vector<uint32_t> idx32(NX1 * NY1 * NZ1);
-  for (size_t i = 0; i < NX1; ++i)
+  parallel_for(NX1, [&](size_t i) {
     for (size_t j = 0; j < NY1; ++j)
       for (size_t k = 0; k < NZ1; ++k) idx32[box_cell(i, j, k)] = base_mat(i, j, k);
+  });
   for (auto &kv : over) {
     auto it = tuple_ids.find(kv.second);
     uint32_t id;
@@ -434,13 +467,18 @@ void Simulation::init(size_t total_time_steps) {
   }
   const int index_bytes = table.size() <= 256 ? 1 : table.size() <= 65536 ? 2 : 4;
   std::vector<uint8_t> idx_bytes(idx32.size() * index_bytes);
+  const size_t plane = NY1 * NZ1;
   if (index_bytes == 1)
-    for (size_t q = 0; q < idx32.size(); ++q) idx_bytes[q] = static_cast<uint8_t>(idx32[q]);
+    parallel_for(NX1, [&](size_t i) {
+      for (size_t q = i * plane; q < (i + 1) * plane; ++q) idx_bytes[q] = static_cast<uint8_t>(idx32[q]);
+    });
   else if (index_bytes == 2)
-    for (size_t q = 0; q < idx32.size(); ++q) {
-      const uint16_t v = static_cast<uint16_t>(idx32[q]);
-      std::memcpy(idx_bytes.data() + 2 * q, &v, 2);
-    }
+    parallel_for(NX1, [&](size_t i) {
+      for (size_t q = i * plane; q < (i + 1) * plane; ++q) {
+        const uint16_t v = static_cast<uint16_t>(idx32[q]);
+        std::memcpy(idx_bytes.data() + 2 * q, &v, 2);
+      }
+    });
   else
     std::memcpy(idx_bytes.data(), idx32.data(), idx32.size() * 4);
   std::vector<double> coeff(table.size() * XFDTD_N_COEFF);

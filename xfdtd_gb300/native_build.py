@@ -41,7 +41,7 @@ def cuda_cmd(out: str = CUDA_LIB, extra=()) -> list:
 
 def host_cmd() -> list:
     srcs = sorted(glob.glob(os.path.join(HERE, "host", "src", "*.cpp")))
-    return ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-Wno-unused-variable",
+    return ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-Wall", "-Wno-unused-variable",
             "-I", os.path.join(HERE, "host", "include"), *srcs,
             "-L", LIB_DIR, "-lxfdtd_cuda", "-Wl,-rpath,$ORIGIN", "-o", HOST_LIB]
 
