@@ -209,13 +209,15 @@ def test_every_shell_variant_is_bitwise_identical(name, precision):
             assert np.array_equal(g.read_field(c), want[c]), (name, precision, v, c)
 
 
-def test_every_kernel_variant_is_bitwise_identical():
+@pytest.mark.parametrize("scene", ["oblique", "dielectric"])
+def test_every_kernel_variant_is_bitwise_identical(scene):
     """The autotuner's variants (split kernels: register caps x block shapes
-    x cells per thread x table placement; fused sweep: register caps x
-    planes per block) change only scheduling: fields after the same steps
-    are bitwise equal."""
+    x cells per thread x table placement and form x TMA-staged planes; fused
+    sweep: register caps x planes per block) change only scheduling: fields
+    after the same steps are bitwise equal."""
+    staged = 0
     for precision, fused in (("fp64", False), ("fp32", False), ("fp64", True), ("fp32", True)):
-        sc, st = scenes.oblique(steps=60)
+        sc, st = scenes.SCENES[scene](steps=60)
         ref = X.Simulation(sc, st, precision=precision, autotune=False, fused=fused)
         ref.step(st)
         want = [ref.read_field(c) for c in range(6)]
@@ -228,10 +230,13 @@ def test_every_kernel_variant_is_bitwise_identical():
             except X.EngineError:
                 continue   # not offered for this precision
             tried += 1
+            staged += (not fused) and v >= 16   # the TMA-staged interior variants
             g.step(st)
             for c in range(6):
                 assert np.array_equal(g.read_field(c), want[c]), (precision, v, c)
         assert tried >= 4
+    if scene == "dielectric":
+        assert staged >= 4   # offered on this grid (its interior starts on a 16-byte boundary)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])

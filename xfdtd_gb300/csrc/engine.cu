@@ -38,6 +38,7 @@
 #include "adjoint.cuh"
 #include "batch.cuh"
 #include "surface.cuh"
+#include "interior_tma.cuh"
 #include "sweep.cuh"
 #include "volume.cuh"
 
@@ -156,7 +157,12 @@ struct xfdtd_handle {
 
   // volume-kernel variants (autotuned)
   int var_e = 1, var_h = 1;   // L1-table variant: valid for every plan
-  float tune_ms[2][16] = {};
+  float tune_ms[2][24] = {};
+  // TMA-staged interior kernels (interior_tma.cuh): offered per side when the
+  // interior's k range starts on a 16-byte boundary for fields and index
+  bool it_ok[2] = {};
+  xg::ItMaps itm[2] = {};
+  void *itm_base = nullptr;   // E_x buffer the maps were encoded for
   // split volume update, per side (0 E, 1 H): the plain interior box and
   // the shell around it, with their cell counts; shell register cap
   xg::InteriorBox vin[2] = {};
@@ -380,7 +386,9 @@ struct Variant {
   int bx, by, bz;
   int nc;
   bool smem;
-  bool ct;   // coefficients from the compact table (volume.cuh coefs)
+  bool ct;      // coefficients from the compact table (volume.cuh coefs)
+  int stages;   // TMA-staged kernel (interior_tma.cuh): ring stages, 0 = not staged
+  int chunk;    //   and planes per block
 };
 constexpr Variant kVariants[] = {
     {8, 32, 4, 2, 1, true, false},   {8, 32, 4, 2, 1, false, false}, {8, 32, 8, 1, 1, false, false},
@@ -389,12 +397,17 @@ constexpr Variant kVariants[] = {
     {1, 32, 4, 2, 1, false, false},  {8, 32, 4, 2, 2, false, false},  {6, 32, 4, 2, 1, true, false},
     {8, 32, 4, 2, 1, false, true},   {8, 32, 8, 1, 1, false, true},   {1, 32, 4, 2, 1, false, true},
     {6, 32, 4, 2, 1, true, true},
+    {0, 32, 8, 1, 1, false, false, 4, 16}, {0, 32, 8, 1, 1, false, false, 6, 16},
+    {0, 32, 8, 1, 1, false, false, 4, 32}, {0, 32, 8, 1, 1, false, true, 4, 16},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
-static_assert(kNumVariants <= 16, "tune_ms holds 16 variants per side");
+static_assert(kNumVariants <= 24, "tune_ms holds 24 variants per side");
 
-// A shared-memory-table variant needs the table to fit (smem_table).
-bool variant_allowed(const xfdtd_handle *h, const Variant &v) { return !v.smem || h->smem_table; }
+// A shared-memory-table variant needs the table to fit (smem_table); a
+// TMA-staged one an aligned interior on both sides (it_ok).
+bool variant_allowed(const xfdtd_handle *h, const Variant &v) {
+  return (!v.smem || h->smem_table) && (!v.stages || (h->it_ok[0] && h->it_ok[1]));
+}
 
 template <typename T, typename I, bool S, int MB, int NC, bool CT>
 void launch_vol_v(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, const Variant &v) {
@@ -683,6 +696,65 @@ void sweep_setup(xfdtd_handle *h) {
   sweep_smem_attr<T, I>();
 }
 
+// Tensor maps of the TMA-staged interior kernels over the current buffers:
+// E kernel H tiles (HW x 9 rows), E and index tiles (32 x 8); H kernel E
+// tiles (EW x 9 rows), H and index tiles.
+template <typename T, typename I>
+void interior_tma_encode(xfdtd_handle *h) {
+  using G = xg::ItTiles<T, I>;
+  const CUtensorMapDataType dt = sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  const CUtensorMapDataType it = sizeof(I) == 1   ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                 : sizeof(I) == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16
+                                                  : CU_TENSOR_MAP_DATA_TYPE_UINT32;
+  for (int c = 0; c < 3; ++c) {
+    encode_map(h, &h->itm[0].a[c], h->F[3 + c], dt, sizeof(T), G::HW, xg::kItJ + 1);
+    encode_map(h, &h->itm[0].b[c], h->F[c], dt, sizeof(T), xg::kItK, xg::kItJ);
+    encode_map(h, &h->itm[1].a[c], h->F[c], dt, sizeof(T), G::EW, xg::kItJ + 1);
+    encode_map(h, &h->itm[1].b[c], h->F[3 + c], dt, sizeof(T), xg::kItK, xg::kItJ);
+  }
+  for (int side = 0; side < 2; ++side) encode_map(h, &h->itm[side].idx, h->idx, it, sizeof(I), xg::kItK, xg::kItJ);
+  h->itm_base = h->F[0];
+}
+
+// Which sides may run the TMA-staged interior kernels: the interior's first
+// k (and, for the E kernel, its H tile's first column) on a 16-byte
+// boundary for the fields and the index.
+template <typename T, typename I>
+void interior_tma_setup(xfdtd_handle *h) {
+  using G = xg::ItTiles<T, I>;
+  const int es = static_cast<int>(sizeof(T)), is = static_cast<int>(sizeof(I));
+  for (int side = 0; side < 2; ++side) {
+    const int k = h->vin[side].lo[2], kh = side == 0 ? k - G::HOFF - 1 : k;
+    h->it_ok[side] = h->vin_cells[side] > 0 && kh >= 0 && (k * es) % 16 == 0 && (kh * es) % 16 == 0 && (k * is) % 16 == 0;
+  }
+  if (!(h->it_ok[0] && h->it_ok[1])) return;
+  interior_tma_encode<T, I>(h);
+  auto attr = [](auto kern, int bytes) {
+    XCHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  };
+  attr(xg::k_interior_tma_e<T, I, 4, false>, G::template smem_e<4>());
+  attr(xg::k_interior_tma_e<T, I, 6, false>, G::template smem_e<6>());
+  attr(xg::k_interior_tma_e<T, I, 4, true>, G::template smem_e<4>());
+  attr(xg::k_interior_tma_h<T, I, 4, false>, G::template smem_h<4>());
+  attr(xg::k_interior_tma_h<T, I, 6, false>, G::template smem_h<6>());
+  attr(xg::k_interior_tma_h<T, I, 4, true>, G::template smem_h<4>());
+}
+
+template <typename T, typename I, int S, bool CT>
+void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, const Variant &v) {
+  using G = xg::ItTiles<T, I>;
+  if (h->itm_base != h->F[0]) interior_tma_encode<T, I>(h);   // the buffers were swapped
+  const xg::InteriorBox in = h->vin[e_side ? 0 : 1];
+  const int nk = in.hi[2] - in.lo[2] + 1, nj = in.hi[1] - in.lo[1] + 1, ni = in.hi[0] - in.lo[0] + 1;
+  dim3 grid((nk + xg::kItK - 1) / xg::kItK, (nj + xg::kItJ - 1) / xg::kItJ, (ni + v.chunk - 1) / v.chunk);
+  if (e_side)
+    xg::k_interior_tma_e<T, I, S, CT>
+        <<<grid, xg::kItThreads, G::template smem_e<S>(), h->stream>>>(h->itm[0], p, in, v.chunk, h->d_status);
+  else
+    xg::k_interior_tma_h<T, I, S, CT>
+        <<<grid, xg::kItThreads, G::template smem_h<S>(), h->stream>>>(h->itm[1], p, in, v.chunk, h->d_status);
+}
+
 // After a sweep the second buffer set holds step t+1: make it current.
 void swap_state(xfdtd_handle *h) {
   for (int c = 0; c < 6; ++c) std::swap(h->F[c], h->F2[c]);
@@ -697,6 +769,13 @@ void launch_volume(xfdtd_handle *h, bool e_side, int var = -1) {
   auto p = vol_params<T, I>(h);
   if (var < 0) var = e_side ? h->var_e : h->var_h;
   const Variant &v = kVariants[var];
+  if (v.stages) {
+    if (v.stages == 6) launch_vol_tma<T, I, 6, false>(h, p, e_side, v);
+    else if (v.ct) launch_vol_tma<T, I, 4, true>(h, p, e_side, v);
+    else launch_vol_tma<T, I, 4, false>(h, p, e_side, v);
+    XCHECK(cudaGetLastError());
+    return;
+  }
   const int key = (v.ct ? 1000 : 0) + v.minb * 100 + v.nc * 10 + (v.smem ? 1 : 0);
   switch (key) {
     case 811: launch_vol_v<T, I, true, 8, 1, false>(h, p, e_side, v); break;
@@ -1368,6 +1447,7 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   }
   volume_boxes(h, 0);
   volume_boxes(h, 1);
+  with_types(h->precision, h->idx_bytes, [&](auto t, auto i) { interior_tma_setup<decltype(t), decltype(i)>(h); });
 
   h->d_step = h->alloc<long long>(1);
   h->d_status = h->alloc<int>(1);

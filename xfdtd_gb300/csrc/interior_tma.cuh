@@ -1,0 +1,264 @@
+// interior_tma.cuh -- the interior E and H kernels with their planes staged
+// by TMA.
+//
+// The one-thread-per-cell interior kernels (volume.cuh) are latency-bound:
+// each warp waits for its own loads, and about 80 % of the warp slots
+// cannot keep enough bytes in flight to reach the copy bandwidth.  Here a
+// block owns a tile of 8 rows (j) x 32 cells (k) of the interior box and
+// marches along i through a chunk of planes.  One elected thread fetches
+// each plane's tiles with tiled TMA loads (cp.async.bulk.tensor) into a
+// ring of STAGES plane stages, STAGES-2 planes ahead of the one being
+// updated; an mbarrier per stage counts the bytes in.  The threads read
+// the tiles from shared memory, apply the same per-cell arithmetic as the
+// fast path (e_plain / h_plain with the same coefficients) and store the
+// updated plane straight to global memory.
+//
+//   E kernel: plane i needs H(i) on rows j0-1 .. j0+7 and columns k0-1 ..
+//   k0+31, H(i-1) on the tile (the previous stage), E(i) and the index on
+//   the tile.
+//   H kernel: plane i needs E(i) on rows j0 .. j0+8 and columns k0 ..
+//   k0+32, E(i+1) on the tile (the next stage), H(i) and the index on the
+//   tile.
+//
+// Tile rows start on 16-byte boundaries as TMA requires: the engine offers
+// these kernels only when the interior's k range starts on one (see
+// interior_tma_ok in engine.cu), and the rows of the E kernel's H tile
+// start HOFF+1 cells before k0, widened to whole 16-byte rows.  Waits on a
+// stage are bounded; a block that gives up reports XFDTD_ERR_TIMEOUT
+// through the status word and stops.
+#pragma once
+
+#include "common.cuh"
+#include "tma.cuh"
+#include "volume.cuh"
+
+namespace xg {
+
+constexpr int kItK = 32;                  // tile: 32 cells along k
+constexpr int kItJ = 8;                   //        8 rows along j
+constexpr int kItThreads = kItK * kItJ;
+constexpr int kItWaitLimit = 1 << 22;     // polls of a stage barrier before giving up
+
+// Tile geometry.  E kernel: H rows of HW columns starting at k0-HOFF-1,
+// 9 rows from j0-1; E and index tiles 32 x 8 from (k0, j0).  H kernel: E
+// rows of EW columns starting at k0, 9 rows from j0; H and index tiles
+// 32 x 8.
+template <typename T, typename I>
+struct ItTiles {
+  static constexpr int HOFF = sizeof(T) == 4 ? 3 : 1;
+  static constexpr int HW = sizeof(T) == 4 ? 40 : 36;    // covers k0-HOFF-1 .. k0+32+
+  static constexpr int EW = sizeof(T) == 4 ? 36 : 34;    // covers k0 .. k0+32+
+  static constexpr int RND = 128;
+  static constexpr int rnd(int b) { return (b + RND - 1) / RND * RND; }
+  // E kernel stage: 3 H tiles (halo), 3 E tiles, index tile
+  static constexpr int EH_TILE = rnd((kItJ + 1) * HW * int(sizeof(T)));
+  static constexpr int EE_TILE = rnd(kItJ * kItK * int(sizeof(T)));
+  static constexpr int I_TILE = rnd(kItJ * kItK * int(sizeof(I)));
+  static constexpr int E_STAGE = 3 * EH_TILE + 3 * EE_TILE + I_TILE;
+  static constexpr unsigned E_HBYTES = 3u * (kItJ + 1) * HW * sizeof(T);
+  static constexpr unsigned E_FULL = E_HBYTES + 3u * kItJ * kItK * sizeof(T) + unsigned(kItJ * kItK * sizeof(I));
+  // H kernel stage: 3 E tiles (halo), 3 H tiles, index tile
+  static constexpr int HE_TILE = rnd((kItJ + 1) * EW * int(sizeof(T)));
+  static constexpr int HH_TILE = EE_TILE;
+  static constexpr int H_STAGE = 3 * HE_TILE + 3 * HH_TILE + I_TILE;
+  static constexpr unsigned H_EBYTES = 3u * (kItJ + 1) * EW * sizeof(T);
+  static constexpr unsigned H_FULL = H_EBYTES + 3u * kItJ * kItK * sizeof(T) + unsigned(kItJ * kItK * sizeof(I));
+  template <int STAGES>
+  static constexpr int smem_e() { return STAGES * E_STAGE + STAGES * 8; }
+  template <int STAGES>
+  static constexpr int smem_h() { return STAGES * H_STAGE + STAGES * 8; }
+};
+
+// Tensor maps of one launch: a[3] the halo tiles (H for the E kernel, E for
+// the H kernel), b[3] the updated side's tiles, the index.
+struct ItMaps {
+  CUtensorMap a[3];
+  CUtensorMap b[3];
+  CUtensorMap idx;
+};
+
+// The block's planes and tile: k0, j0 of the tile, planes [ia, ib) of its
+// chunk (the interior box's k range starts on a 16-byte boundary).
+struct ItBlock {
+  int k0, j0, ia, ib;
+};
+__device__ __forceinline__ ItBlock it_block(const InteriorBox &in, int chunk) {
+  ItBlock b;
+  b.k0 = in.lo[2] + static_cast<int>(blockIdx.x) * kItK;
+  b.j0 = in.lo[1] + static_cast<int>(blockIdx.y) * kItJ;
+  b.ia = in.lo[0] + static_cast<int>(blockIdx.z) * chunk;
+  b.ib = min(b.ia + chunk, in.hi[0] + 1);
+  return b;
+}
+
+// Stage bookkeeping of one block (thread 0 issues and drains; every thread
+// waits).  A wait that gives up marks the block timed out; the block then
+// stops, and thread 0 waits (bounded) for the loads it issued before the
+// block exits, so that no copy lands in a finished block's shared memory.
+template <int STAGES>
+struct ItRing {
+  uint64_t *bar;
+  unsigned phase = 0;   // bit s: parity of the next completion of stage s
+  bool timed_out = false;
+  __device__ bool wait(int st) {
+    if (timed_out) return false;
+    if (!mbar_wait_bounded(&bar[st], (phase >> st) & 1u, kItWaitLimit)) {
+      timed_out = true;
+      return false;
+    }
+    phase ^= 1u << st;
+    return true;
+  }
+};
+
+template <typename T, typename I, int STAGES, bool CT>
+__global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
+                                                               InteriorBox in, int chunk, int *status) {
+  using G = ItTiles<T, I>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::E_STAGE)};
+  const int tid = threadIdx.x, c = tid & 31, r = tid >> 5;
+  const ItBlock blk = it_block(in, chunk);
+  if (blk.ia >= blk.ib) return;
+  auto stage_of = [&](int q) { return (q - blk.ia + 1) % STAGES; };   // plane ia-1 in stage 0
+  auto htile = [&](int st, int comp) { return reinterpret_cast<const T *>(smem + st * G::E_STAGE + comp * G::EH_TILE); };
+  auto etile = [&](int st, int comp) {
+    return reinterpret_cast<const T *>(smem + st * G::E_STAGE + 3 * G::EH_TILE + comp * G::EE_TILE);
+  };
+  auto itile = [&](int st) { return reinterpret_cast<const I *>(smem + st * G::E_STAGE + 3 * G::EH_TILE + 3 * G::EE_TILE); };
+  auto issue = [&](int q) {   // thread 0: the loads of plane q (H only for plane ia-1)
+    const int st = stage_of(q);
+    const bool full = q >= blk.ia;
+    unsigned char *base = smem + st * G::E_STAGE;
+    mbar_arrive_expect_tx(&ring.bar[st], full ? G::E_FULL : G::E_HBYTES);
+    for (int comp = 0; comp < 3; ++comp)
+      tma_load_3d(base + comp * G::EH_TILE, &maps.a[comp], blk.k0 - G::HOFF - 1, blk.j0 - 1, q, &ring.bar[st]);
+    if (full) {
+      for (int comp = 0; comp < 3; ++comp)
+        tma_load_3d(base + 3 * G::EH_TILE + comp * G::EE_TILE, &maps.b[comp], blk.k0, blk.j0, q, &ring.bar[st]);
+      tma_load_3d(base + 3 * G::EH_TILE + 3 * G::EE_TILE, &maps.idx, blk.k0, blk.j0, q, &ring.bar[st]);
+    }
+  };
+  int issued = blk.ia - 2, waited = blk.ia - 2;   // thread 0: last plane issued, last plane waited
+  if (tid == 0) {
+    for (int q = 0; q < STAGES; ++q) mbar_init(&ring.bar[q], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    issued = min(blk.ia + STAGES - 2, blk.ib - 1);
+    for (int q = blk.ia - 1; q <= issued; ++q) issue(q);
+  }
+  if (ring.wait(stage_of(blk.ia - 1))) waited = blk.ia - 1;
+  const int j = blk.j0 + r, k = blk.k0 + c;
+  const bool mine = j <= in.hi[1] && k <= in.hi[2];
+  const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
+  for (int i = blk.ia; i < blk.ib; ++i) {
+    if (ring.wait(stage_of(i))) waited = i;
+    if (mine && !ring.timed_out) {
+      const int st = stage_of(i), sm = stage_of(i - 1);
+      auto hv = [&](int s, int comp, int rr, int cc) { return htile(s, comp)[rr * G::HW + cc + G::HOFF]; };
+      // H at (j, k), (k-1), (j-1) of plane i and at (j, k) of plane i-1
+      const ECurl<T> h{hv(st, 0, r + 1, c + 1), hv(st, 1, r + 1, c + 1), hv(st, 2, r + 1, c + 1),
+                       hv(st, 0, r + 1, c),     hv(st, 1, r + 1, c),     hv(st, 0, r, c + 1),
+                       hv(st, 2, r, c + 1),     hv(sm, 1, r + 1, c + 1), hv(sm, 2, r + 1, c + 1)};
+      T ex = etile(st, 0)[r * kItK + c], ey = etile(st, 1)[r * kItK + c], ez = etile(st, 2)[r * kItK + c];
+      T cf[9];
+      coefs<T, I, CT>(p, p.table, 18, static_cast<unsigned>(itile(st)[r * kItK + c]), 0, cf);
+      e_plain(cf, h, ex, ey, ez);
+      const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
+      p.E[0][b] = ex;
+      p.E[1][b] = ey;
+      p.E[2][b] = ez;
+    }
+    if (__syncthreads_or(ring.timed_out)) break;   // the stage of plane i-1 is free
+    if (tid == 0 && i + STAGES - 1 <= blk.ib - 1) {
+      fence_proxy_async();
+      issue(i + STAGES - 1);
+      issued = i + STAGES - 1;
+    }
+  }
+  if (tid == 0) {
+    const bool failed = ring.timed_out;
+    ring.timed_out = false;
+    for (int q = waited + 1; q <= issued; ++q) ring.wait(stage_of(q));   // copies still in flight
+    if (failed || ring.timed_out) atomicExch(status, static_cast<int>(4));   // XFDTD_ERR_TIMEOUT
+  }
+}
+
+template <typename T, typename I, int STAGES, bool CT>
+__global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
+                                                               InteriorBox in, int chunk, int *status) {
+  using G = ItTiles<T, I>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::H_STAGE)};
+  const int tid = threadIdx.x, c = tid & 31, r = tid >> 5;
+  const ItBlock blk = it_block(in, chunk);
+  if (blk.ia >= blk.ib) return;
+  auto stage_of = [&](int q) { return (q - blk.ia) % STAGES; };
+  auto etile = [&](int st, int comp) { return reinterpret_cast<const T *>(smem + st * G::H_STAGE + comp * G::HE_TILE); };
+  auto htile = [&](int st, int comp) {
+    return reinterpret_cast<const T *>(smem + st * G::H_STAGE + 3 * G::HE_TILE + comp * G::HH_TILE);
+  };
+  auto itile = [&](int st) { return reinterpret_cast<const I *>(smem + st * G::H_STAGE + 3 * G::HE_TILE + 3 * G::HH_TILE); };
+  auto issue = [&](int q) {   // thread 0: the loads of plane q (E only for plane ib)
+    const int st = stage_of(q);
+    const bool full = q < blk.ib;
+    unsigned char *base = smem + st * G::H_STAGE;
+    mbar_arrive_expect_tx(&ring.bar[st], full ? G::H_FULL : G::H_EBYTES);
+    for (int comp = 0; comp < 3; ++comp)
+      tma_load_3d(base + comp * G::HE_TILE, &maps.a[comp], blk.k0, blk.j0, q, &ring.bar[st]);
+    if (full) {
+      for (int comp = 0; comp < 3; ++comp)
+        tma_load_3d(base + 3 * G::HE_TILE + comp * G::HH_TILE, &maps.b[comp], blk.k0, blk.j0, q, &ring.bar[st]);
+      tma_load_3d(base + 3 * G::HE_TILE + 3 * G::HH_TILE, &maps.idx, blk.k0, blk.j0, q, &ring.bar[st]);
+    }
+  };
+  int issued = blk.ia - 1, waited = blk.ia - 1;   // thread 0: last plane issued, last plane waited
+  if (tid == 0) {
+    for (int q = 0; q < STAGES; ++q) mbar_init(&ring.bar[q], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    issued = min(blk.ia + STAGES - 1, blk.ib);
+    for (int q = blk.ia; q <= issued; ++q) issue(q);
+  }
+  if (ring.wait(stage_of(blk.ia))) waited = blk.ia;
+  const int j = blk.j0 + r, k = blk.k0 + c;
+  const bool mine = j <= in.hi[1] && k <= in.hi[2];
+  const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
+  for (int i = blk.ia; i < blk.ib; ++i) {
+    if (ring.wait(stage_of(i + 1))) waited = i + 1;
+    if (mine && !ring.timed_out) {
+      const int st = stage_of(i), sn = stage_of(i + 1);
+      auto ev = [&](int s, int comp, int rr, int cc) { return etile(s, comp)[rr * G::EW + cc]; };
+      // E at (j, k), (k+1), (j+1) of plane i and at (j, k) of plane i+1
+      const HCurl<T> e{ev(st, 0, r, c),     ev(st, 1, r, c),     ev(st, 2, r, c),
+                       ev(st, 0, r, c + 1), ev(st, 1, r, c + 1), ev(st, 0, r + 1, c),
+                       ev(st, 2, r + 1, c), ev(sn, 1, r, c),     ev(sn, 2, r, c)};
+      T hx = htile(st, 0)[r * kItK + c], hy = htile(st, 1)[r * kItK + c], hz = htile(st, 2)[r * kItK + c];
+      T cf[9];
+      coefs<T, I, CT>(p, p.table + 9, 18, static_cast<unsigned>(itile(st)[r * kItK + c]), 1, cf);
+      h_plain(cf, e, hx, hy, hz);
+      const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
+      p.H[0][b] = hx;
+      p.H[1][b] = hy;
+      p.H[2][b] = hz;
+    }
+    if (__syncthreads_or(ring.timed_out)) break;   // the stage of plane i is free
+    if (tid == 0 && i + STAGES <= blk.ib) {
+      fence_proxy_async();
+      issue(i + STAGES);
+      issued = i + STAGES;
+    }
+  }
+  if (tid == 0) {
+    const bool failed = ring.timed_out;
+    ring.timed_out = false;
+    for (int q = waited + 1; q <= issued; ++q) ring.wait(stage_of(q));
+    if (failed || ring.timed_out) atomicExch(status, static_cast<int>(4));   // XFDTD_ERR_TIMEOUT
+  }
+}
+
+}  // namespace xg
