@@ -182,25 +182,28 @@ def algorithmic_bytes(n, slab_layers, precision: str, kernel: str, split=None) -
     the 3 own components and the 3 curl components, write the 3 own
     components, read the 1-byte material index; inside CPML slabs read and
     write one psi per (component, slab axis) pair (2 per slab axis).  The
-    update runs as two concurrent kernels: the interior kernel over the
-    plain cells (split["e_interior"] / ["h_interior"]) and the shell kernel
-    over walls and slabs (["e_shell"] / ["h_shell"], all psi traffic);
-    "update_e" / "update_h" is the pair.  Fused sweep (E and H of one step):
-    read and write all 6 components once and the index once; psi traffic of
-    both halves."""
+    update runs as two concurrent launches, an interior and a shell launch
+    (cells split["e_interior"] / ["e_shell"], likewise for H); in the narrow
+    decomposition the shell launch carries all psi traffic, in the wide one
+    (split["e_wide"]) the interior launch carries the x- and y-slab psi and
+    the shell launch the z-slab psi.  "update_e" / "update_h" is the pair.
+    Fused sweep (E and H of one step): read and write all 6 components once
+    and the index once; psi traffic of both halves."""
     nx, ny, nz = n
     cells = nx * ny * nz
     w = 8 if precision == "fp64" else 4
-    slab_cells = (slab_layers[0] * ny * nz + slab_layers[1] * nx * nz + slab_layers[2] * nx * ny)
-    psi = slab_cells * 2 * 2 * w
+    psi_xy = (slab_layers[0] * ny * nz + slab_layers[1] * nx * nz) * 2 * 2 * w
+    psi_z = slab_layers[2] * nx * ny * 2 * 2 * w
+    psi = psi_xy + psi_z
     if kernel == "sweep_eh":
         return cells * (12 * w + 1) + psi * 2
     if split is not None:
         side = kernel[7]
+        wide = split.get(side + "_wide", False)
         if kernel.endswith("_interior"):
-            return split[side + "_interior"] * (9 * w + 1)
+            return split[side + "_interior"] * (9 * w + 1) + (psi_xy if wide else 0)
         if kernel.endswith("_shell"):
-            return split[side + "_shell"] * (9 * w + 1) + psi
+            return split[side + "_shell"] * (9 * w + 1) + (psi_z if wide else psi)
         return (split[side + "_interior"] + split[side + "_shell"]) * (9 * w + 1) + psi
     return cells * (9 * w + 1) + psi
 
@@ -400,9 +403,12 @@ def run_heterogeneous_form(args, local):
     cells = n[0] * n[1] * n[2]
     split = g.volume_split()
     variants = g.kernel_variants()
+    shell_variants = g.shell_variants()
     del g
     sc, st = configs.heterogeneous(steps=3 + args.hetero_steps)
     g = X.Simulation(sc, st, precision="fp32", device=local, profile=True, graph=False)
+    g.set_kernel_variant(variants["e"], variants["h"])
+    g.set_shell_variant(shell_variants["e"], shell_variants["h"])
     g.step(3)
     g.synchronize()
     g.profile_reset()
@@ -419,7 +425,8 @@ def run_heterogeneous_form(args, local):
             "value": cells * args.hetero_steps / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms / args.hetero_steps,
             "timed_path": "CUDA graph replay", "dominant_kernel": dom, "dominant_ms": prof[dom][0] / prof[dom][1],
             "achieved_GBs": gbs, "frac": gbs / peak, "peak_source": kind, "concurrent_ms": conc,
-            "variants": {"e": variants["e"], "h": variants["h"]},
+            "variants": {"e": variants["e"], "h": variants["h"], "shell_e": shell_variants["e"],
+                         "shell_h": shell_variants["h"]},
             "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (cells * 4 / 1e6)}
 
 
@@ -450,6 +457,7 @@ def ours_arm(args, world, rank, local, grp):
     clocks = clock.stop()
     max_ms = grp.max(ms)
     variants = sim.kernel_variants()
+    shell_variants = sim.shell_variants()
     launches = sim.launch_count() - launches0
     sim.check_finite()
     split = sim.volume_split()
@@ -461,6 +469,10 @@ def ours_arm(args, world, rank, local, grp):
     prof_steps = min(args.steps, PROFILE_STEPS)
     psim = X.Simulation(sc, args.warmup + prof_steps, precision=args.precision, graph=False, profile=True,
                         device=local, fused=fused)
+    # the timed run's variants, so that the kernel times explain its number
+    psim.set_kernel_variant(variants["e"], variants["h"])
+    psim.set_shell_variant(shell_variants["e"], shell_variants["h"])
+    assert psim.volume_split() == split
     psim.step(args.warmup)
     psim.synchronize()
     psim.profile_reset()
@@ -546,6 +558,7 @@ def ours_arm(args, world, rank, local, grp):
         "volume_split_cells": split,
         "volume_kernels_concurrent": concurrent,
         "autotuned_variants": {"update_e": variants["e"], "update_h": variants["h"],
+                               "shell_e": shell_variants["e"], "shell_h": shell_variants["h"],
                                "trial_ms_e": [round(v, 4) for v in variants["trials_e"]],
                                "trial_ms_h": [round(v, 4) for v in variants["trials_h"]]},
         "e2e": {"value": cells * args.steps * world / e2e_s / 1e6, "unit": UNIT,

@@ -203,25 +203,40 @@ int xfdtd_profile(xfdtd_handle *h, int max, const char **names, double *ms, int6
 int xfdtd_profile_reset(xfdtd_handle *h);
 /* Times every variant of the volume kernels and keeps the fastest: of the
  * fused E/H sweep (register cap x planes per block), or with
- * XFDTD_FLAG_SPLIT_EH of the E and H kernels separately (register cap x
- * block shape x cells per thread x table placement).  Only before the first
- * step: the trials run on the all-zero initial state and leave it unchanged.
- * All variants compute bitwise-identical results. */
+ * XFDTD_FLAG_SPLIT_EH of the E and H updates separately.  A split update is
+ * an interior launch and a shell launch on two streams; its variants are
+ * the interior launch's (register cap x block shape x cells per thread x
+ * table placement and form, or TMA-staged planes over the narrow or the
+ * wide decomposition) paired with a shell variant, timed as the pair runs.
+ * Only before the first step: the trials run on the all-zero initial state
+ * and leave it unchanged.  All variants compute bitwise-identical results. */
 int xfdtd_autotune(xfdtd_handle *h, int trials);
-/* Number of variants, the ones in use, and the last trial times
- * (trial_ms[2*v] for E, [2*v+1] for H; 0 where not tried).  For the fused
+/* Number of variants, the ones in use, and the last trial times of the
+ * whole update with each (trial_ms[2*v] for E, [2*v+1] for H; 0 where not
+ * tried).  A variant of the wide decomposition moves the x and y slabs into
+ * the interior launch (see xfdtd_volume_decomposition).  For the fused
  * sweep both sides report the sweep's variant and time, and
  * xfdtd_set_kernel_variant takes the same variant for both. */
 int xfdtd_kernel_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h, double *trial_ms);
 int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant);
-/* Variants of the shell kernels (walls and CPML slabs): how many, the ones
- * in use for E and H; and fixing them (all give the same bits). */
+/* Variants of the shell launches (walls and CPML slabs): how many, the ones
+ * in use for E and H; and fixing them (all give the same bits).  Variants
+ * 0-3 are the shell kernel (register cap x table form); 4-6 the z-edge
+ * TMA-staged launch, offered with a wide interior variant only
+ * (XFDTD_ERR_INVALID_PLAN otherwise). */
 int xfdtd_shell_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h);
 int xfdtd_set_shell_variant(xfdtd_handle *h, int e_variant, int h_variant);
 /* Cells of the split volume update: cells[0] / [1] the E update's interior
  * (plain on every axis, the interior kernel) and shell (walls and CPML
  * slabs, the shell kernel); cells[2] / [3] the same for H. */
 int xfdtd_volume_split(xfdtd_handle *h, int64_t cells[4]);
+/* The decomposition each update runs with its current variant: wide[0]
+ * (E) and wide[1] (H) are 0 for the narrow one (the interior launch covers
+ * the cells plain on every axis, the shell launch the rest) and 1 for the
+ * wide one (the interior launch covers every plane and row over the
+ * interior's k range, x and y slabs included; the shell launch the z
+ * slabs). */
+int xfdtd_volume_decomposition(xfdtd_handle *h, int wide[2]);
 /* Per-step kernel launches enqueued so far (graph replays included). */
 int xfdtd_launch_count(xfdtd_handle *h, int64_t *n);
 /* Kernel launches the engine enqueues per step for this plan. */

@@ -199,14 +199,64 @@ def test_every_shell_variant_is_bitwise_identical(name, precision):
     ref.step(st)
     want = [ref.read_field(c) for c in range(6)]
     n = ref.shell_variants()["n"]
-    assert n >= 4
+    assert n >= 7
     for v in range(n):
         g = X.Simulation(sc, st, precision=precision, autotune=False, fused=False)
+        if v < 4:
+            g.set_kernel_variant(12 + v % 4, 12 + v % 4)   # the compact-table interior variants
+        else:
+            try:   # z-edge TMA launches: with a wide interior variant, where the grid offers one
+                g.set_kernel_variant(WIDE_VARIANTS[v % 3], WIDE_VARIANTS[v % 3])
+            except X.EngineError:
+                continue
         g.set_shell_variant(v, v)
-        g.set_kernel_variant(12 + v % 4, 12 + v % 4)   # the compact-table interior variants
         g.step(st)
         for c in range(6):
             assert np.array_equal(g.read_field(c), want[c]), (name, precision, v, c)
+
+
+# the wide decomposition's interior variants (TMA-staged, every plane and
+# row over the interior's k range) and the z-edge TMA shell variants
+WIDE_VARIANTS = (20, 21, 22)
+ZEDGE_SHELL_VARIANTS = (4, 5, 6)
+
+
+@pytest.mark.parametrize("name", ["dielectric", "heterogeneous", "oblique", "long_z", "one_sided"])
+def test_wide_decomposition_is_bitwise_identical(name):
+    """The wide decomposition (x and y slabs inside the TMA-staged interior
+    launch, the z slabs on the shell kernel or on the z-edge TMA launch)
+    gives the narrow decomposition's bits, for every pairing of its
+    interior and shell variants; its interior and shell cells partition
+    the component box."""
+    make = scenes.SCENES.get(name) or scenes.SPLIT_SCENES[name]
+    offered = 0
+    for precision in ("fp64", "fp32"):
+        sc, st = make()
+        st = min(st, 60)
+        ref = X.Simulation(sc, st, precision=precision, autotune=False, fused=False)
+        ref.step(st)
+        want = [ref.read_field(c) for c in range(6)]
+        for v in WIDE_VARIANTS:
+            for sv in (0, 1) + ZEDGE_SHELL_VARIANTS:
+                g = X.Simulation(sc, st, precision=precision, autotune=False, fused=False)
+                try:
+                    g.set_kernel_variant(v, v)
+                    g.set_shell_variant(sv, sv)
+                except X.EngineError:
+                    continue   # not offered on this grid
+                offered += 1
+                sp = g.volume_split()
+                n = g.n
+                total = (n[0] + 1) * (n[1] + 1) * (n[2] + 1)
+                assert sp["e_interior"] + sp["e_shell"] == total, sp
+                assert sp["h_interior"] + sp["h_shell"] == total, sp
+                g.step(st)
+                for c in range(6):
+                    assert np.array_equal(g.read_field(c), want[c]), (name, precision, v, sv, c)
+    if name == "dielectric":
+        # every pairing in one precision at least (the other's k range may
+        # not start on a 16-byte boundary on this small grid)
+        assert offered >= len(WIDE_VARIANTS) * (2 + len(ZEDGE_SHELL_VARIANTS))
 
 
 @pytest.mark.parametrize("scene", ["oblique", "dielectric"])

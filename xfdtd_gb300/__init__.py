@@ -86,6 +86,7 @@ def libs():
         cu.xfdtd_kernel_variants.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int), dp]
         cu.xfdtd_set_kernel_variant.argtypes = [C.c_void_p, C.c_int, C.c_int]
         cu.xfdtd_volume_split.argtypes = [C.c_void_p, P(C.c_int64)]
+        cu.xfdtd_volume_decomposition.argtypes = [C.c_void_p, P(C.c_int)]
         cu.xfdtd_shell_variants.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int)]
         cu.xfdtd_set_shell_variant.argtypes = [C.c_void_p, C.c_int, C.c_int]
         cu.xfdtd_last_error.argtypes = [C.c_void_p]
@@ -317,11 +318,17 @@ class Simulation:
         self._check_engine(libs()[0].xfdtd_set_shell_variant(self.engine, int(e_variant), int(h_variant)))
 
     def volume_split(self) -> dict:
-        """Cells of the interior (plain) and shell (walls, CPML) kernels of
-        the E and H updates."""
+        """Cells of the interior and shell launches of the E and H updates,
+        and whether each update runs the wide decomposition (x and y slabs
+        in the interior launch, z slabs in the shell launch) or the narrow
+        one (plain cells in the interior launch, walls and slabs in the
+        shell launch)."""
         c = (C.c_int64 * 4)()
         self._check_engine(libs()[0].xfdtd_volume_split(self.engine, c))
-        return {"e_interior": c[0], "e_shell": c[1], "h_interior": c[2], "h_shell": c[3]}
+        w = (C.c_int * 2)()
+        self._check_engine(libs()[0].xfdtd_volume_decomposition(self.engine, w))
+        return {"e_interior": c[0], "e_shell": c[1], "h_interior": c[2], "h_shell": c[3],
+                "e_wide": bool(w[0]), "h_wide": bool(w[1])}
 
     def transfer_bytes(self):
         """(host->device, device->host) bytes the engine has copied so far."""

@@ -31,6 +31,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/xfdtd_cuda.h"
@@ -166,6 +167,13 @@ struct xfdtd_handle {
   // split volume update, per side (0 E, 1 H): the plain interior box and
   // the shell around it, with their cell counts; shell register cap
   xg::InteriorBox vin[2] = {};
+  // wide decomposition (TMA-staged interior over every plane and row of the
+  // interior's k range; the shell keeps the z slabs)
+  xg::InteriorBox vin_w[2] = {};
+  xg::InteriorBox vin_z[2] = {};   // the z slabs of the wide decomposition as TMA tiles
+  xg::ShellBoxes vshell_w[2] = {};
+  long long vin_w_cells[2] = {}, vshell_w_cells[2] = {};
+  bool wide_ok[2] = {};
   xg::ShellBoxes vshell[2] = {};
   long long vin_cells[2] = {}, vshell_cells[2] = {};
   int shell_var[2] = {0, 0};   // shell-kernel variant per side
@@ -389,6 +397,7 @@ struct Variant {
   bool ct;      // coefficients from the compact table (volume.cuh coefs)
   int stages;   // TMA-staged kernel (interior_tma.cuh): ring stages, 0 = not staged
   int chunk;    //   and planes per block
+  bool wide;    //   over the wide decomposition (the shell keeps the z slabs only)
 };
 constexpr Variant kVariants[] = {
     {8, 32, 4, 2, 1, true, false},   {8, 32, 4, 2, 1, false, false}, {8, 32, 8, 1, 1, false, false},
@@ -399,14 +408,34 @@ constexpr Variant kVariants[] = {
     {6, 32, 4, 2, 1, true, true},
     {0, 32, 8, 1, 1, false, false, 4, 16}, {0, 32, 8, 1, 1, false, false, 6, 16},
     {0, 32, 8, 1, 1, false, false, 4, 32}, {0, 32, 8, 1, 1, false, true, 4, 16},
+    {0, 32, 8, 1, 1, false, false, 4, 16, true}, {0, 32, 8, 1, 1, false, false, 6, 16, true},
+    {0, 32, 8, 1, 1, false, true, 4, 16, true},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 static_assert(kNumVariants <= 24, "tune_ms holds 24 variants per side");
 
 // A shared-memory-table variant needs the table to fit (smem_table); a
-// TMA-staged one an aligned interior on both sides (it_ok).
+// TMA-staged one an aligned interior on both sides (it_ok), a wide one the
+// wide decomposition on both sides too.
 bool variant_allowed(const xfdtd_handle *h, const Variant &v) {
-  return (!v.smem || h->smem_table) && (!v.stages || (h->it_ok[0] && h->it_ok[1]));
+  return (!v.smem || h->smem_table) && (!v.stages || (h->it_ok[0] && h->it_ok[1])) &&
+         (!v.wide || (h->wide_ok[0] && h->wide_ok[1]));
+}
+
+// The decomposition a side runs with its current variant: narrow (the
+// interior box and the shell around it) or wide.
+bool side_wide(const xfdtd_handle *h, int side) { return kVariants[side == 0 ? h->var_e : h->var_h].wide; }
+const xg::InteriorBox &side_interior(const xfdtd_handle *h, int side, bool wide) {
+  return wide ? h->vin_w[side] : h->vin[side];
+}
+const xg::ShellBoxes &side_shell(const xfdtd_handle *h, int side, bool wide) {
+  return wide ? h->vshell_w[side] : h->vshell[side];
+}
+long long side_interior_cells(const xfdtd_handle *h, int side, bool wide) {
+  return wide ? h->vin_w_cells[side] : h->vin_cells[side];
+}
+long long side_shell_cells(const xfdtd_handle *h, int side, bool wide) {
+  return wide ? h->vshell_w_cells[side] : h->vshell_cells[side];
 }
 
 template <typename T, typename I, bool S, int MB, int NC, bool CT>
@@ -424,35 +453,55 @@ void launch_vol_v(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, co
 
 
 // Shell-kernel variants the autotuner chooses from: register cap (minimum
-// resident 256-thread blocks per SM) and table form (compact or full).
+// resident 256-thread blocks per SM) and table form (compact or full); or,
+// for the wide decomposition only, the z-edge TMA launch (interior_tma.cuh
+// mode 2) with its ring stages.
 struct ShellVariant {
   int minb;
   bool ct;
+  int stages;   // 0 = the shell kernel
 };
-constexpr ShellVariant kShellVariants[] = {{4, false}, {6, false}, {4, true}, {6, true}};
+constexpr ShellVariant kShellVariants[] = {{4, false}, {6, false}, {4, true},     {6, true},
+                                           {0, false, 4}, {0, false, 6}, {0, true, 4}};
 constexpr int kNumShellVariants = sizeof(kShellVariants) / sizeof(kShellVariants[0]);
 
+// A z-edge TMA variant runs on the wide decomposition only.
+bool shell_allowed(const xfdtd_handle *h, const ShellVariant &v, bool wide) {
+  return !v.stages || (wide && h->it_ok[0] && h->it_ok[1] && h->wide_ok[0] && h->wide_ok[1]);
+}
+
 template <typename T, typename I, int MB, bool CT>
-void launch_shell_v(xfdtd_handle *h, bool e_side, cudaStream_t st) {
-  const xg::ShellBoxes &s = h->vshell[e_side ? 0 : 1];
+void launch_shell_v(xfdtd_handle *h, bool e_side, const xg::ShellBoxes &s, cudaStream_t st) {
   const auto p = vol_params<T, I>(h);
   if (e_side) xg::k_update_e_shell<T, I, MB, CT><<<s.blocks, 256, 0, st>>>(p, s);
   else xg::k_update_h_shell<T, I, MB, CT><<<s.blocks, 256, 0, st>>>(p, s);
 }
 
+template <typename T, typename I, int S, bool CT, int MODE>
+void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, int chunk, cudaStream_t st);
+
+// The shell kernel of one side over the decomposition of its current
+// variant (wide: 0 narrow, 1 wide, -1 the current one).
 template <typename T, typename I>
-void launch_shell(xfdtd_handle *h, bool e_side, int var = -1, cudaStream_t st = nullptr) {
+void launch_shell(xfdtd_handle *h, bool e_side, int var = -1, cudaStream_t st = nullptr, int wide = -1) {
   const int side = e_side ? 0 : 1;
-  if (h->vshell[side].blocks == 0) return;
+  const xg::ShellBoxes &s = side_shell(h, side, wide < 0 ? side_wide(h, side) : wide != 0);
+  if (s.blocks == 0) return;
   if (var < 0) var = h->shell_var[side];
   const ShellVariant &v = kShellVariants[var];
   if (!st) st = h->stream;
-  if (v.minb == 6) {
-    if (v.ct) launch_shell_v<T, I, 6, true>(h, e_side, st);
-    else launch_shell_v<T, I, 6, false>(h, e_side, st);
+  if (v.stages) {
+    if (&s != &h->vshell_w[side]) throw Err{XFDTD_ERR_STATE, "z-edge TMA launch outside the wide decomposition"};
+    auto p = vol_params<T, I>(h);
+    if (v.stages == 6) launch_vol_tma<T, I, 6, false, 2>(h, p, e_side, 16, st);
+    else if (v.ct) launch_vol_tma<T, I, 4, true, 2>(h, p, e_side, 16, st);
+    else launch_vol_tma<T, I, 4, false, 2>(h, p, e_side, 16, st);
+  } else if (v.minb == 6) {
+    if (v.ct) launch_shell_v<T, I, 6, true>(h, e_side, s, st);
+    else launch_shell_v<T, I, 6, false>(h, e_side, s, st);
   } else {
-    if (v.ct) launch_shell_v<T, I, 4, true>(h, e_side, st);
-    else launch_shell_v<T, I, 4, false>(h, e_side, st);
+    if (v.ct) launch_shell_v<T, I, 4, true>(h, e_side, s, st);
+    else launch_shell_v<T, I, 4, false>(h, e_side, s, st);
   }
   XCHECK(cudaGetLastError());
 }
@@ -510,17 +559,18 @@ void volume_boxes(xfdtd_handle *h, int side) {
   const uint8_t bit = side == 0 ? xg::kSpecialE : xg::kSpecialH;
   const int n[3] = {h->d.nx, h->d.ny, h->d.nz};
   int lo[3], hi[3];
-  bool interior = true;
+  bool run[3];
   for (int a = 0; a < 3; ++a) {
     const std::vector<uint8_t> &fl = h->axis_flags_host[a];
     lo[a] = 0;
     while (lo[a] <= n[a] && (fl[lo[a]] & bit)) ++lo[a];
     hi[a] = n[a];
     while (hi[a] >= lo[a] && (fl[hi[a]] & bit)) --hi[a];
-    if (lo[a] > hi[a]) interior = false;
+    run[a] = lo[a] <= hi[a];
     for (int q = lo[a]; q <= hi[a]; ++q)
-      if (fl[q] & bit) interior = false;
+      if (fl[q] & bit) run[a] = false;
   }
+  const int px_lo = lo[0], px_hi = hi[0], py_lo = lo[1], py_hi = hi[1];
   // cut on 128-byte lines, else (a short run) on 32-byte sectors, else not at all
   for (int bytes : {128, 32}) {
     const int q = bytes / static_cast<int>(h->esize);
@@ -531,14 +581,10 @@ void volume_boxes(xfdtd_handle *h, int side) {
       break;
     }
   }
-  xg::InteriorBox &in = h->vin[side];
-  xg::ShellBoxes &s = h->vshell[side];
-  s = xg::ShellBoxes{};
-  long long total = 0;
-  unsigned blocks = 0;
+  const bool interior = run[0] && run[1] && run[2];
   // ranges per axis: 0 = below the plain run, 1 = the plain run, 2 = above,
   // 3 = all, 4 = below and above (k only: the row's two parts together)
-  auto add = [&](int ri, int rj, int rk, int cls) {
+  auto add = [&](xg::ShellBoxes &s, unsigned &blocks, long long &total, int ri, int rj, int rk, int cls) {
     const int r[3] = {ri, rj, rk};
     int r0[3], ext[3], ksplit = 0, kgap = 0;
     for (int a = 0; a < 3; ++a) {
@@ -574,32 +620,78 @@ void volume_boxes(xfdtd_handle *h, int side) {
     blocks += static_cast<unsigned>((cells + 255) / 256);
     total += cells;
   };
-  if (!interior) {
-    for (int a = 0; a < 3; ++a) {
-      in.lo[a] = 0;
-      in.hi[a] = -1;
+
+  // narrow: the interior box P x P x P, the shell around it
+  {
+    xg::InteriorBox &in = h->vin[side];
+    xg::ShellBoxes &s = h->vshell[side];
+    s = xg::ShellBoxes{};
+    long long total = 0;
+    unsigned blocks = 0;
+    in = xg::InteriorBox{};
+    if (!interior) {
+      for (int a = 0; a < 3; ++a) {
+        in.lo[a] = 0;
+        in.hi[a] = -1;
+      }
+      add(s, blocks, total, 3, 3, 3, 7);
+      h->vin_cells[side] = 0;
+    } else {
+      for (int a = 0; a < 3; ++a) {
+        in.lo[a] = lo[a];
+        in.hi[a] = hi[a];
+      }
+      in.px_lo = in.lo[0], in.px_hi = in.hi[0], in.py_lo = in.lo[1], in.py_hi = in.hi[1];
+      in.pz_lo = in.lo[2], in.pz_hi = in.hi[2];
+      for (int r : {0, 2}) {
+        add(s, blocks, total, r, 1, 1, 1);   // x faces
+        add(s, blocks, total, 1, r, 1, 2);   // y faces
+      }
+      add(s, blocks, total, 1, 1, 4, 4);     // z faces
+      for (int r : {0, 2}) {
+        add(s, blocks, total, r, 1, 4, 5);   // x-z edges
+        add(s, blocks, total, 1, r, 4, 6);   // y-z edges
+        for (int q : {0, 2}) add(s, blocks, total, r, q, 3, 7);   // x-y edges with the corners
+      }
+      h->vin_cells[side] = static_cast<long long>(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
     }
-    add(3, 3, 3, 7);
-    h->vin_cells[side] = 0;
-  } else {
-    for (int a = 0; a < 3; ++a) {
-      in.lo[a] = lo[a];
-      in.hi[a] = hi[a];
-    }
-    for (int r : {0, 2}) {
-      add(r, 1, 1, 1);   // x faces
-      add(1, r, 1, 2);   // y faces
-    }
-    add(1, 1, 4, 4);     // z faces
-    for (int r : {0, 2}) {
-      add(r, 1, 4, 5);   // x-z edges
-      add(1, r, 4, 6);   // y-z edges
-      for (int q : {0, 2}) add(r, q, 3, 7);   // x-y edges with the corners
-    }
-    h->vin_cells[side] = static_cast<long long>(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+    s.blocks = blocks;
+    h->vshell_cells[side] = total;
   }
-  s.blocks = blocks;
-  h->vshell_cells[side] = total;
+
+  // wide (TMA-staged interior only): every plane and row over the interior's
+  // k range, the plain x and y runs marking the planes and rows of the fast
+  // path; the shell keeps the z slabs, by the x and y class of their rows
+  {
+    xg::InteriorBox &in = h->vin_w[side];
+    xg::ShellBoxes &s = h->vshell_w[side];
+    s = xg::ShellBoxes{};
+    in = xg::InteriorBox{};
+    long long total = 0;
+    unsigned blocks = 0;
+    h->wide_ok[side] = interior;
+    if (interior) {
+      in.lo[0] = 0, in.hi[0] = n[0];
+      in.lo[1] = 0, in.hi[1] = n[1];
+      in.lo[2] = lo[2], in.hi[2] = hi[2];
+      in.px_lo = px_lo, in.px_hi = px_hi, in.py_lo = py_lo, in.py_hi = py_hi;
+      in.pz_lo = lo[2], in.pz_hi = hi[2];
+      // the same cells as the z slabs, for the z-edge TMA launch
+      xg::InteriorBox &z = h->vin_z[side];
+      z = in;
+      z.lo[2] = 0;
+      z.hi[2] = n[2];
+      add(s, blocks, total, 1, 1, 4, 4);     // z faces
+      for (int r : {0, 2}) {
+        add(s, blocks, total, r, 1, 4, 5);   // x-z edges
+        add(s, blocks, total, 1, r, 4, 6);   // y-z edges
+        for (int q : {0, 2}) add(s, blocks, total, r, q, 4, 7);   // corners
+      }
+      h->vin_w_cells[side] = static_cast<long long>(n[0] + 1) * (n[1] + 1) * (hi[2] - lo[2] + 1);
+    }
+    s.blocks = blocks;
+    h->vshell_w_cells[side] = total;
+  }
 }
 
 // Fused-sweep variants: register cap (minimum resident 256-thread blocks
@@ -732,27 +824,42 @@ void interior_tma_setup(xfdtd_handle *h) {
   auto attr = [](auto kern, int bytes) {
     XCHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   };
-  attr(xg::k_interior_tma_e<T, I, 4, false>, G::template smem_e<4>());
-  attr(xg::k_interior_tma_e<T, I, 6, false>, G::template smem_e<6>());
-  attr(xg::k_interior_tma_e<T, I, 4, true>, G::template smem_e<4>());
-  attr(xg::k_interior_tma_h<T, I, 4, false>, G::template smem_h<4>());
-  attr(xg::k_interior_tma_h<T, I, 6, false>, G::template smem_h<6>());
-  attr(xg::k_interior_tma_h<T, I, 4, true>, G::template smem_h<4>());
+  auto attrs = [&](auto mode) {
+    constexpr int M = decltype(mode)::value;
+    attr(xg::k_interior_tma_e<T, I, 4, false, M>, G::template smem_e<4>());
+    attr(xg::k_interior_tma_e<T, I, 6, false, M>, G::template smem_e<6>());
+    attr(xg::k_interior_tma_e<T, I, 4, true, M>, G::template smem_e<4>());
+    attr(xg::k_interior_tma_h<T, I, 4, false, M>, G::template smem_h<4>());
+    attr(xg::k_interior_tma_h<T, I, 6, false, M>, G::template smem_h<6>());
+    attr(xg::k_interior_tma_h<T, I, 4, true, M>, G::template smem_h<4>());
+  };
+  attrs(std::integral_constant<int, 0>{});
+  // the z-edge launch's upper tiles start after the interior's last k
+  for (int side = 0; side < 2; ++side) {
+    const int k = h->vin[side].hi[2] + 1, kh = side == 0 ? k - G::HOFF - 1 : k;
+    if ((k * es) % 16 || (kh * es) % 16 || (k * is) % 16) h->wide_ok[side] = false;
+  }
+  if (!(h->wide_ok[0] && h->wide_ok[1])) return;
+  attrs(std::integral_constant<int, 1>{});
+  attrs(std::integral_constant<int, 2>{});
 }
 
-template <typename T, typename I, int S, bool CT>
-void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, const Variant &v) {
+template <typename T, typename I, int S, bool CT, int MODE>
+void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, int chunk, cudaStream_t st) {
   using G = xg::ItTiles<T, I>;
   if (h->itm_base != h->F[0]) interior_tma_encode<T, I>(h);   // the buffers were swapped
-  const xg::InteriorBox in = h->vin[e_side ? 0 : 1];
-  const int nk = in.hi[2] - in.lo[2] + 1, nj = in.hi[1] - in.lo[1] + 1, ni = in.hi[0] - in.lo[0] + 1;
-  dim3 grid((nk + xg::kItK - 1) / xg::kItK, (nj + xg::kItJ - 1) / xg::kItJ, (ni + v.chunk - 1) / v.chunk);
+  const int side = e_side ? 0 : 1;
+  const xg::InteriorBox in = MODE == 2 ? h->vin_z[side] : side_interior(h, side, MODE == 1);
+  const int nj = in.hi[1] - in.lo[1] + 1, ni = in.hi[0] - in.lo[0] + 1;
+  const int nkt = MODE == 2 ? (in.pz_lo + xg::kItK - 1) / xg::kItK + (in.hi[2] - in.pz_hi + xg::kItK - 1) / xg::kItK
+                            : (in.hi[2] - in.lo[2] + xg::kItK) / xg::kItK;
+  dim3 grid(nkt, (nj + xg::kItJ - 1) / xg::kItJ, (ni + chunk - 1) / chunk);
   if (e_side)
-    xg::k_interior_tma_e<T, I, S, CT>
-        <<<grid, xg::kItThreads, G::template smem_e<S>(), h->stream>>>(h->itm[0], p, in, v.chunk, h->d_status);
+    xg::k_interior_tma_e<T, I, S, CT, MODE>
+        <<<grid, xg::kItThreads, G::template smem_e<S>(), st>>>(h->itm[0], p, in, chunk, h->d_status);
   else
-    xg::k_interior_tma_h<T, I, S, CT>
-        <<<grid, xg::kItThreads, G::template smem_h<S>(), h->stream>>>(h->itm[1], p, in, v.chunk, h->d_status);
+    xg::k_interior_tma_h<T, I, S, CT, MODE>
+        <<<grid, xg::kItThreads, G::template smem_h<S>(), st>>>(h->itm[1], p, in, chunk, h->d_status);
 }
 
 // After a sweep the second buffer set holds step t+1: make it current.
@@ -765,14 +872,20 @@ void swap_state(xfdtd_handle *h) {
 // Interior kernel of one side (nothing when the plan has no interior).
 template <typename T, typename I>
 void launch_volume(xfdtd_handle *h, bool e_side, int var = -1) {
-  if (h->vin_cells[e_side ? 0 : 1] == 0) return;
-  auto p = vol_params<T, I>(h);
   if (var < 0) var = e_side ? h->var_e : h->var_h;
   const Variant &v = kVariants[var];
+  if (side_interior_cells(h, e_side ? 0 : 1, v.wide) == 0) return;
+  auto p = vol_params<T, I>(h);
   if (v.stages) {
-    if (v.stages == 6) launch_vol_tma<T, I, 6, false>(h, p, e_side, v);
-    else if (v.ct) launch_vol_tma<T, I, 4, true>(h, p, e_side, v);
-    else launch_vol_tma<T, I, 4, false>(h, p, e_side, v);
+    if (v.wide) {
+      if (v.stages == 6) launch_vol_tma<T, I, 6, false, 1>(h, p, e_side, v.chunk, h->stream);
+      else if (v.ct) launch_vol_tma<T, I, 4, true, 1>(h, p, e_side, v.chunk, h->stream);
+      else launch_vol_tma<T, I, 4, false, 1>(h, p, e_side, v.chunk, h->stream);
+    } else {
+      if (v.stages == 6) launch_vol_tma<T, I, 6, false, 0>(h, p, e_side, v.chunk, h->stream);
+      else if (v.ct) launch_vol_tma<T, I, 4, true, 0>(h, p, e_side, v.chunk, h->stream);
+      else launch_vol_tma<T, I, 4, false, 0>(h, p, e_side, v.chunk, h->stream);
+    }
     XCHECK(cudaGetLastError());
     return;
   }
@@ -805,6 +918,9 @@ void smem_attr(int bytes) {
   XCHECK(cudaFuncSetAttribute(xg::k_update_h<T, I, true, 6, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
 }
 
+template <typename T, typename I>
+void volume_pair(xfdtd_handle *h, bool e_side);
+
 // Times every variant of the E and H kernels on the handle's current state
 // and keeps the fastest.  Run before the first step, when every field and
 // psi is zero: the volume kernels then write zeros back (the TFSF buffers
@@ -835,48 +951,62 @@ void autotune_t(xfdtd_handle *h, int trials) {
     best_sweep = best / trials;
   }
   const bool forced = h->sweep && (h->flags & XFDTD_FLAG_FUSED_EH);
+  const bool was_sweep = h->sweep;
+  const long long launches = h->launch_count;
+  h->sweep = false;
+  auto time_ms = [&](auto &&run) {
+    run();   // warm-up / module load
+    XCHECK(cudaEventRecord(a, h->stream));
+    for (int r = 0; r < trials; ++r) run();
+    XCHECK(cudaEventRecord(b, h->stream));
+    XCHECK(cudaEventSynchronize(b));
+    float ms = 0;
+    XCHECK(cudaEventElapsedTime(&ms, a, b));
+    return ms / trials;
+  };
   for (int side = 0; side < 2 && !forced; ++side) {
-    // shell kernel: register cap
-    float best_shell = 0.f;
-    if (h->vshell_cells[side]) {
-      best_shell = 1e30f;
+    // shell kernel of each decomposition: its fastest variant, timed alone
+    int shell_best[2] = {0, 0};
+    for (int w = 0; w < 2; ++w) {
+      if (w && !h->wide_ok[side]) continue;
+      if (!side_shell_cells(h, side, w != 0)) continue;
+      float best = 1e30f;
       for (int v = 0; v < kNumShellVariants; ++v) {
-        launch_shell<T, I>(h, side == 0, v);
-        XCHECK(cudaEventRecord(a, h->stream));
-        for (int r = 0; r < trials; ++r) launch_shell<T, I>(h, side == 0, v);
-        XCHECK(cudaEventRecord(b, h->stream));
-        XCHECK(cudaEventSynchronize(b));
-        float ms = 0;
-        XCHECK(cudaEventElapsedTime(&ms, a, b));
-        if (ms / trials < best_shell) {
-          best_shell = ms / trials;
-          h->shell_var[side] = v;
-        }
+        if (!shell_allowed(h, kShellVariants[v], w != 0)) continue;
+        const float ms = time_ms([&] { launch_shell<T, I>(h, side == 0, v, nullptr, w); });
+        if (ms < best) best = ms, shell_best[w] = v;
       }
     }
-    best_split += best_shell;
-    if (!h->vin_cells[side]) continue;
+    // each interior variant with its decomposition's best shell variant,
+    // timed as the step runs them: the pair on two streams
+    int &var = side == 0 ? h->var_e : h->var_h;
     float best = 1e30f;
     int best_v = 0;
     for (int v = 0; v < kNumVariants; ++v) {
       if (!variant_allowed(h, kVariants[v])) continue;
-      launch_volume<T, I>(h, side == 0, v);   // warm-up / module load
-      XCHECK(cudaEventRecord(a, h->stream));
-      for (int r = 0; r < trials; ++r) launch_volume<T, I>(h, side == 0, v);
-      XCHECK(cudaEventRecord(b, h->stream));
-      XCHECK(cudaEventSynchronize(b));
-      float ms = 0;
-      XCHECK(cudaEventElapsedTime(&ms, a, b));
-      h->tune_ms[side][v] = ms / trials;
-      if (ms < best) {
-        best = ms;
-        best_v = v;
-      }
+      var = v;
+      h->shell_var[side] = shell_best[kVariants[v].wide ? 1 : 0];
+      const float ms = time_ms([&] { volume_pair<T, I>(h, side == 0); });
+      h->tune_ms[side][v] = ms;
+      if (ms < best) best = ms, best_v = v;
     }
-    if (side == 0) h->var_e = best_v;
-    else h->var_h = best_v;
-    best_split += best / trials;
+    var = best_v;
+    h->shell_var[side] = shell_best[kVariants[best_v].wide ? 1 : 0];
+    // the shell variant fastest alone need not be fastest beside the
+    // interior launch: time the chosen interior variant with each of them
+    if (side_shell_cells(h, side, kVariants[best_v].wide))
+      for (int v = 0; v < kNumShellVariants; ++v) {
+        if (!shell_allowed(h, kShellVariants[v], kVariants[best_v].wide)) continue;
+        const int keep = h->shell_var[side];
+        h->shell_var[side] = v;
+        const float ms = time_ms([&] { volume_pair<T, I>(h, side == 0); });
+        if (ms < best) best = ms, h->tune_ms[side][best_v] = ms;
+        else h->shell_var[side] = keep;
+      }
+    best_split += best;
   }
+  h->sweep = was_sweep;
+  h->launch_count = launches;
   // without a forcing flag, the faster of the sweep and the split pair
   if (h->sweep_ok && !forced) h->sweep = best_sweep < best_split;
   cudaEventDestroy(a);
@@ -1030,7 +1160,8 @@ xg::AuxParams aux_params(xfdtd_handle *h) {
 template <typename T, typename I>
 void volume_pair(xfdtd_handle *h, bool e_side) {
   const int side = e_side ? 0 : 1;
-  const bool in = h->vin_cells[side] != 0, sh = h->vshell_cells[side] != 0;
+  const bool wide = side_wide(h, side);
+  const bool in = side_interior_cells(h, side, wide) != 0, sh = side_shell_cells(h, side, wide) != 0;
   prof_region_begin(h, e_side ? 1 : 3);
   if (in && sh) {
     XCHECK(cudaEventRecord(h->ev_vfork[side], h->stream));
@@ -1136,8 +1267,11 @@ void enqueue_step(xfdtd_handle *h, long long s) {
 
 int launches_per_step(const xfdtd_handle *h) {
   if (h->sweep) return (h->tfsf ? 2 : 0) + 1 + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
-  const int vol = (h->vin_cells[0] ? 1 : 0) + (h->vshell_cells[0] ? 1 : 0) + (h->vin_cells[1] ? 1 : 0) +
-                  (h->vshell_cells[1] ? 1 : 0);
+  int vol = 0;
+  for (int side = 0; side < 2; ++side) {
+    const bool w = side_wide(h, side);
+    vol += (side_interior_cells(h, side, w) ? 1 : 0) + (side_shell_cells(h, side, w) ? 1 : 0);
+  }
   return (h->tfsf ? 3 : 0) + vol + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
 }
 
@@ -1209,7 +1343,13 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   XCHECK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
   XCHECK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
   XCHECK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
-  XCHECK(cudaStreamCreateWithFlags(&h->shell, cudaStreamNonBlocking));
+  {
+    // the shell launch is the pair's long pole: its blocks go first as the
+    // interior's retire
+    int least = 0, greatest = 0;
+    XCHECK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    XCHECK(cudaStreamCreateWithPriority(&h->shell, cudaStreamNonBlocking, greatest));
+  }
   for (int q = 0; q < 2; ++q) {
     XCHECK(cudaEventCreateWithFlags(&h->ev_vfork[q], cudaEventDisableTiming));
     XCHECK(cudaEventCreateWithFlags(&h->ev_vjoin[q], cudaEventDisableTiming));
@@ -1775,6 +1915,8 @@ int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant) {
       invalid("kernel variant not available for this precision");
     h->var_e = e_variant;
     h->var_h = h_variant;
+    for (int side = 0; side < 2; ++side)   // a z-edge shell variant needs the wide decomposition
+      if (!shell_allowed(h, kShellVariants[h->shell_var[side]], side_wide(h, side))) h->shell_var[side] = 0;
     if (h->gexec) {   // the captured graph holds the old launches
       cudaGraphExecDestroy(h->gexec);
       h->gexec = nullptr;
@@ -1795,6 +1937,9 @@ int xfdtd_set_shell_variant(xfdtd_handle *h, int e_variant, int h_variant) {
   return guarded(h, [&] {
     if (e_variant < 0 || e_variant >= kNumShellVariants || h_variant < 0 || h_variant >= kNumShellVariants)
       invalid("shell-kernel variant out of range");
+    if (!shell_allowed(h, kShellVariants[e_variant], side_wide(h, 0)) ||
+        !shell_allowed(h, kShellVariants[h_variant], side_wide(h, 1)))
+      invalid("shell-kernel variant needs the wide decomposition (a wide kernel variant)");
     h->shell_var[0] = e_variant;
     h->shell_var[1] = h_variant;
     if (h->gexec) {   // the captured graph holds the old launches
@@ -1808,10 +1953,17 @@ int xfdtd_volume_split(xfdtd_handle *h, int64_t cells[4]) {
   if (!h || !cells) return XFDTD_ERR_STATE;
   return guarded(h, [&] {
     for (int side = 0; side < 2; ++side) {
-      cells[2 * side] = h->vin_cells[side];
-      cells[2 * side + 1] = h->vshell_cells[side];
+      const bool w = side_wide(h, side);
+      cells[2 * side] = side_interior_cells(h, side, w);
+      cells[2 * side + 1] = side_shell_cells(h, side, w);
     }
   });
+}
+
+int xfdtd_volume_decomposition(xfdtd_handle *h, int wide[2]) {
+  if (!h || !wide) return XFDTD_ERR_STATE;
+  for (int side = 0; side < 2; ++side) wide[side] = side_wide(h, side) ? 1 : 0;
+  return XFDTD_OK;
 }
 
 int xfdtd_launch_count(xfdtd_handle *h, int64_t *n) {

@@ -20,6 +20,21 @@
 //   k0+32, E(i+1) on the tile (the next stage), H(i) and the index on the
 //   tile.
 //
+// MODE selects the cells a launch covers:
+//   0  the interior box, plain on every axis;
+//   1  (wide) every plane and row, i 0 .. nx and j 0 .. ny, over the
+//      interior's k range: the CPML slabs and walls on x and y join the
+//      interior.  Planes outside the plain x run and rows outside the plain
+//      y run take the general path with x, y or both as the special axes
+//      (uniform per block plane and per warp, since a warp is one row);
+//   2  (z edges) the same planes and rows over the k tiles below and above
+//      the interior's k range, with z special too: tiles from k = 0 up to
+//      the interior's first k, and from the one after its last k up to nz.
+//      Modes 1 and 2 together cover the grid.
+// H and E beyond the grid (plane -1, row -1, plane nx+1, row ny+1, k -1)
+// arrive as TMA zeros, the values the general path puts there; E at k nz+1
+// (inside the row padding) is zeroed by hand, as the general path does.
+//
 // Tile rows start on 16-byte boundaries as TMA requires: the engine offers
 // these kernels only when the interior's k range starts on one (see
 // interior_tma_ok in engine.cu), and the rows of the E kernel's H tile
@@ -77,14 +92,26 @@ struct ItMaps {
   CUtensorMap idx;
 };
 
-// The block's planes and tile: k0, j0 of the tile, planes [ia, ib) of its
-// chunk (the interior box's k range starts on a 16-byte boundary).
+// The block's planes and tile: k0, j0 of the tile, its last k khi, planes
+// [ia, ib) of its chunk.  Every tile starts on a 16-byte boundary: the
+// interior box's k range starts on one, and mode 2's upper tiles start
+// after its last k, whose successor is on one too.
 struct ItBlock {
-  int k0, j0, ia, ib;
+  int k0, khi, j0, ia, ib;
 };
+template <int MODE>
 __device__ __forceinline__ ItBlock it_block(const InteriorBox &in, int chunk) {
   ItBlock b;
-  b.k0 = in.lo[2] + static_cast<int>(blockIdx.x) * kItK;
+  const int t = static_cast<int>(blockIdx.x);
+  if (MODE == 2) {
+    const int nlo = (in.pz_lo + kItK - 1) / kItK;
+    const bool below = t < nlo;
+    b.k0 = below ? t * kItK : in.pz_hi + 1 + (t - nlo) * kItK;
+    b.khi = below ? in.pz_lo - 1 : in.hi[2];
+  } else {
+    b.k0 = in.lo[2] + t * kItK;
+    b.khi = in.hi[2];
+  }
   b.j0 = in.lo[1] + static_cast<int>(blockIdx.y) * kItJ;
   b.ia = in.lo[0] + static_cast<int>(blockIdx.z) * chunk;
   b.ib = min(b.ia + chunk, in.hi[0] + 1);
@@ -111,14 +138,14 @@ struct ItRing {
   }
 };
 
-template <typename T, typename I, int STAGES, bool CT>
+template <typename T, typename I, int STAGES, bool CT, int MODE>
 __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
                                                                InteriorBox in, int chunk, int *status) {
   using G = ItTiles<T, I>;
   extern __shared__ __align__(128) unsigned char smem[];
   ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::E_STAGE)};
   const int tid = threadIdx.x, c = tid & 31, r = tid >> 5;
-  const ItBlock blk = it_block(in, chunk);
+  const ItBlock blk = it_block<MODE>(in, chunk);
   if (blk.ia >= blk.ib) return;
   auto stage_of = [&](int q) { return (q - blk.ia + 1) % STAGES; };   // plane ia-1 in stage 0
   auto htile = [&](int st, int comp) { return reinterpret_cast<const T *>(smem + st * G::E_STAGE + comp * G::EH_TILE); };
@@ -151,25 +178,64 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
   }
   if (ring.wait(stage_of(blk.ia - 1))) waited = blk.ia - 1;
   const int j = blk.j0 + r, k = blk.k0 + c;
-  const bool mine = j <= in.hi[1] && k <= in.hi[2];
+  const bool mine = j <= in.hi[1] && k <= blk.khi;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
+  // the CPML context of the thread's row and column, fixed over the planes
+  SlabCtx<T> cx = slab_ctx<T, I, 0>(p, 0, 0, 0, 0);
+  const bool yspec = MODE != 0 && (j < in.py_lo || j > in.py_hi);
+  if (MODE != 0 && mine) {
+    if (yspec) slab_axis(p, 1, 0, j, cx.ys, cx.Y);
+    if (MODE == 2) slab_axis(p, 2, 0, k, cx.zs, cx.Z);
+  }
   for (int i = blk.ia; i < blk.ib; ++i) {
+    // a special cell's psi operands, loaded before the wait for the plane
+    const int cls = MODE == 0 ? 0 : ((i < in.px_lo || i > in.px_hi) ? 1 : 0) | (yspec ? 2 : 0) | (MODE == 2 ? 4 : 0);
+    PsiOps<T> ps{};
+    if (MODE != 0 && mine && cls != 0) {
+      if (cls & 1) {
+        slab_axis(p, 0, 0, i, cx.xs, cx.X);
+      } else {
+        cx.xs = -1;
+        cx.X = AxisCoef<T>{T(0), T(0), T(1)};
+      }
+      ps = e_psi_load<T, I, 7>(p, cx, i, j, k, p.psi);
+    }
     if (ring.wait(stage_of(i))) waited = i;
     if (mine && !ring.timed_out) {
       const int st = stage_of(i), sm = stage_of(i - 1);
       auto hv = [&](int s, int comp, int rr, int cc) { return htile(s, comp)[rr * G::HW + cc + G::HOFF]; };
       // H at (j, k), (k-1), (j-1) of plane i and at (j, k) of plane i-1
-      const ECurl<T> h{hv(st, 0, r + 1, c + 1), hv(st, 1, r + 1, c + 1), hv(st, 2, r + 1, c + 1),
+      ECurl<T> h{hv(st, 0, r + 1, c + 1), hv(st, 1, r + 1, c + 1), hv(st, 2, r + 1, c + 1),
                        hv(st, 0, r + 1, c),     hv(st, 1, r + 1, c),     hv(st, 0, r, c + 1),
                        hv(st, 2, r, c + 1),     hv(sm, 1, r + 1, c + 1), hv(sm, 2, r + 1, c + 1)};
       T ex = etile(st, 0)[r * kItK + c], ey = etile(st, 1)[r * kItK + c], ez = etile(st, 2)[r * kItK + c];
       T cf[9];
       coefs<T, I, CT>(p, p.table, 18, static_cast<unsigned>(itile(st)[r * kItK + c]), 0, cf);
-      e_plain(cf, h, ex, ey, ez);
       const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
-      p.E[0][b] = ex;
-      p.E[1][b] = ey;
-      p.E[2][b] = ez;
+      if (MODE != 2 && cls == 0) {
+        e_plain(cf, h, ex, ey, ez);
+        p.E[0][b] = ex;
+        p.E[1][b] = ey;
+        p.E[2][b] = ez;
+      } else {
+        bool w[3];
+        if (MODE == 2) {
+          if (k == 0) h.hx_k = h.hy_k = T(0);
+          if (cls == 4) e_general_ops<T, I, 4>(p, cf, i, j, k, h, cx, ps, p.psi, true, ex, ey, ez, w);
+          else if (cls == 5) e_general_ops<T, I, 5>(p, cf, i, j, k, h, cx, ps, p.psi, true, ex, ey, ez, w);
+          else if (cls == 6) e_general_ops<T, I, 6>(p, cf, i, j, k, h, cx, ps, p.psi, true, ex, ey, ez, w);
+          else e_general_ops<T, I, 7>(p, cf, i, j, k, h, cx, ps, p.psi, true, ex, ey, ez, w);
+        } else if (cls == 1) {
+          e_general_ops<T, I, 1>(p, cf, i, j, k, h, cx, ps, p.psi, true, ex, ey, ez, w);
+        } else if (cls == 2) {
+          e_general_ops<T, I, 2>(p, cf, i, j, k, h, cx, ps, p.psi, true, ex, ey, ez, w);
+        } else {
+          e_general_ops<T, I, 3>(p, cf, i, j, k, h, cx, ps, p.psi, true, ex, ey, ez, w);
+        }
+        if (w[0]) p.E[0][b] = ex;
+        if (w[1]) p.E[1][b] = ey;
+        if (w[2]) p.E[2][b] = ez;
+      }
     }
     if (__syncthreads_or(ring.timed_out)) break;   // the stage of plane i-1 is free
     if (tid == 0 && i + STAGES - 1 <= blk.ib - 1) {
@@ -186,14 +252,14 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
   }
 }
 
-template <typename T, typename I, int STAGES, bool CT>
+template <typename T, typename I, int STAGES, bool CT, int MODE>
 __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
                                                                InteriorBox in, int chunk, int *status) {
   using G = ItTiles<T, I>;
   extern __shared__ __align__(128) unsigned char smem[];
   ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::H_STAGE)};
   const int tid = threadIdx.x, c = tid & 31, r = tid >> 5;
-  const ItBlock blk = it_block(in, chunk);
+  const ItBlock blk = it_block<MODE>(in, chunk);
   if (blk.ia >= blk.ib) return;
   auto stage_of = [&](int q) { return (q - blk.ia) % STAGES; };
   auto etile = [&](int st, int comp) { return reinterpret_cast<const T *>(smem + st * G::H_STAGE + comp * G::HE_TILE); };
@@ -226,25 +292,62 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
   }
   if (ring.wait(stage_of(blk.ia))) waited = blk.ia;
   const int j = blk.j0 + r, k = blk.k0 + c;
-  const bool mine = j <= in.hi[1] && k <= in.hi[2];
+  const bool mine = j <= in.hi[1] && k <= blk.khi;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
+  SlabCtx<T> cx = slab_ctx<T, I, 0>(p, 1, 0, 0, 0);
+  const bool yspec = MODE != 0 && (j < in.py_lo || j > in.py_hi);
+  if (MODE != 0 && mine) {
+    if (yspec) slab_axis(p, 1, 1, j, cx.ys, cx.Y);
+    if (MODE == 2) slab_axis(p, 2, 1, k, cx.zs, cx.Z);
+  }
   for (int i = blk.ia; i < blk.ib; ++i) {
+    const int cls = MODE == 0 ? 0 : ((i < in.px_lo || i > in.px_hi) ? 1 : 0) | (yspec ? 2 : 0) | (MODE == 2 ? 4 : 0);
+    PsiOps<T> pv{};
+    if (MODE != 0 && mine && cls != 0) {
+      if (cls & 1) {
+        slab_axis(p, 0, 1, i, cx.xs, cx.X);
+      } else {
+        cx.xs = -1;
+        cx.X = AxisCoef<T>{T(0), T(0), T(1)};
+      }
+      pv = h_psi_load<T, I, 7>(p, cx, i, j, k);
+    }
     if (ring.wait(stage_of(i + 1))) waited = i + 1;
     if (mine && !ring.timed_out) {
       const int st = stage_of(i), sn = stage_of(i + 1);
       auto ev = [&](int s, int comp, int rr, int cc) { return etile(s, comp)[rr * G::EW + cc]; };
       // E at (j, k), (k+1), (j+1) of plane i and at (j, k) of plane i+1
-      const HCurl<T> e{ev(st, 0, r, c),     ev(st, 1, r, c),     ev(st, 2, r, c),
+      HCurl<T> e{ev(st, 0, r, c),     ev(st, 1, r, c),     ev(st, 2, r, c),
                        ev(st, 0, r, c + 1), ev(st, 1, r, c + 1), ev(st, 0, r + 1, c),
                        ev(st, 2, r + 1, c), ev(sn, 1, r, c),     ev(sn, 2, r, c)};
       T hx = htile(st, 0)[r * kItK + c], hy = htile(st, 1)[r * kItK + c], hz = htile(st, 2)[r * kItK + c];
       T cf[9];
       coefs<T, I, CT>(p, p.table + 9, 18, static_cast<unsigned>(itile(st)[r * kItK + c]), 1, cf);
-      h_plain(cf, e, hx, hy, hz);
       const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
-      p.H[0][b] = hx;
-      p.H[1][b] = hy;
-      p.H[2][b] = hz;
+      if (MODE != 2 && cls == 0) {
+        h_plain(cf, e, hx, hy, hz);
+        p.H[0][b] = hx;
+        p.H[1][b] = hy;
+        p.H[2][b] = hz;
+      } else {
+        bool w[3];
+        if (MODE == 2) {
+          if (k >= p.d.nz) e.ex_k = e.ey_k = T(0);
+          if (cls == 4) h_general_ops<T, I, 4>(p, cf, i, j, k, e, cx, pv, hx, hy, hz, w);
+          else if (cls == 5) h_general_ops<T, I, 5>(p, cf, i, j, k, e, cx, pv, hx, hy, hz, w);
+          else if (cls == 6) h_general_ops<T, I, 6>(p, cf, i, j, k, e, cx, pv, hx, hy, hz, w);
+          else h_general_ops<T, I, 7>(p, cf, i, j, k, e, cx, pv, hx, hy, hz, w);
+        } else if (cls == 1) {
+          h_general_ops<T, I, 1>(p, cf, i, j, k, e, cx, pv, hx, hy, hz, w);
+        } else if (cls == 2) {
+          h_general_ops<T, I, 2>(p, cf, i, j, k, e, cx, pv, hx, hy, hz, w);
+        } else {
+          h_general_ops<T, I, 3>(p, cf, i, j, k, e, cx, pv, hx, hy, hz, w);
+        }
+        if (w[0]) p.H[0][b] = hx;
+        if (w[1]) p.H[1][b] = hy;
+        if (w[2]) p.H[2][b] = hz;
+      }
     }
     if (__syncthreads_or(ring.timed_out)) break;   // the stage of plane i is free
     if (tid == 0 && i + STAGES <= blk.ib) {

@@ -155,44 +155,115 @@ __device__ __forceinline__ AxisCoef<T> axis_coef(int slot, const T *b, const T *
   return r;
 }
 
-// General E update of one cell: outer walls and CPML slabs.  E psi is read
-// from pr and, when store_psi, written to pw (SEPARATE_PSI) or back to pr
-// (in place).  w[c] reports whether component c was updated.  Every operand
-// (coefficients, profiles, psi values) is loaded before the first store, so
-// that the loads are in flight together; the arithmetic is that of the
-// reference's loops, term by term.  AXES (bit 0 x, 1 y, 2 z) names the axes
-// whose index may be special (wall or CPML slab); on the others the caller
-// guarantees a plain index, and their tests and terms drop out at compile
-// time (a CPML face cell has one special axis, an edge cell two).
-template <typename T, typename I, bool SEPARATE_PSI, int AXES = 7>
-__device__ __forceinline__ void e_general(const VolCore<T, I> &p, const T *c, int i, int j, int k,
-                                          const ECurl<T> &h, const Psi<T> &pr, const Psi<T> &pw_, bool store_psi,
-                                          T &ex, T &ey, T &ez, bool w[3]) {
+// The CPML context of one cell: the slab slot on each axis (-1 outside the
+// slabs, and on the axes a caller names plain) and the profile values at
+// the cell's indices.
+template <typename T>
+struct SlabCtx {
+  int xs, ys, zs;
+  AxisCoef<T> X, Y, Z;
+};
+
+// One axis of it: the E (half 0) or H (half 1) slot and profiles of axis a
+// at index n.
+template <typename T, typename I>
+__device__ __forceinline__ void slab_axis(const VolCore<T, I> &p, int a, int half, int n, int &slot, AxisCoef<T> &c) {
+  const CpmlAxis<T> &cp = p.cp[a];
+  slot = cp.n_layers ? __ldg((half ? cp.slot_h : cp.slot_e) + n) : -1;
+  c = half ? axis_coef(slot, cp.b_m, cp.a_m, cp.rk_m, n) : axis_coef(slot, cp.b_e, cp.a_e, cp.rk_e, n);
+}
+
+template <typename T, typename I, int AXES>
+__device__ __forceinline__ SlabCtx<T> slab_ctx(const VolCore<T, I> &p, int half, int i, int j, int k) {
+  SlabCtx<T> x;
+  x.xs = x.ys = x.zs = -1;
+  x.X = x.Y = x.Z = AxisCoef<T>{T(0), T(0), T(1)};
+  if (AXES & 1) slab_axis(p, 0, half, i, x.xs, x.X);
+  if (AXES & 2) slab_axis(p, 1, half, j, x.ys, x.Y);
+  if (AXES & 4) slab_axis(p, 2, half, k, x.zs, x.Z);
+  return x;
+}
+
+// The six psi operands of one cell and side: E ex_y, ex_z, ey_x, ey_z,
+// ez_x, ez_y (H likewise), 0 where the recursion does not run.
+template <typename T>
+struct PsiOps {
+  T xy, xz, yx, yz, zx, zy;
+};
+
+// Psi offsets of one cell: X slabs (xs, j, k), Y slabs (i, ys, k), Z slabs
+// (i, j, zs), each with k (or the slot) fastest.
+template <typename T, typename I>
+__device__ __forceinline__ void psi_offsets(const VolCore<T, I> &p, const SlabCtx<T> &x, int i, int j, int k,
+                                            unsigned &ox, unsigned &oy, unsigned &oz) {
+  const unsigned Ly = p.cp[1].n_layers, Lz = p.cp[2].n_layers;
+  const unsigned nzp = static_cast<unsigned>(p.d.nzp), ny1 = static_cast<unsigned>(p.d.ny + 1);
+  ox = (static_cast<unsigned>(x.xs) * ny1 + j) * nzp + k;
+  oy = (static_cast<unsigned>(i) * Ly + x.ys) * nzp + k;
+  oz = (static_cast<unsigned>(i) * ny1 + j) * Lz + x.zs;
+}
+
+// The E psi operands of one cell (AXES as in e_general).
+template <typename T, typename I, int AXES>
+__device__ __forceinline__ PsiOps<T> e_psi_load(const VolCore<T, I> &p, const SlabCtx<T> &x, int i, int j, int k,
+                                                const Psi<T> &pr) {
   constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
-  const Psi<T> &pw = SEPARATE_PSI ? pw_ : pr;
+  const bool ex_on = !SX || i < p.d.nx, ey_on = !SY || j < p.d.ny, ez_on = !SZ || k < p.d.nz;
+  unsigned ox, oy, oz;
+  psi_offsets(p, x, i, j, k, ox, oy, oz);
+  PsiOps<T> s;
+  s.xy = ex_on && x.ys >= 0 ? pr.ex_y[oy] : T(0);
+  s.xz = ex_on && x.zs >= 0 ? pr.ex_z[oz] : T(0);
+  s.yx = ey_on && x.xs >= 0 ? pr.ey_x[ox] : T(0);
+  s.yz = ey_on && x.zs >= 0 ? pr.ey_z[oz] : T(0);
+  s.zx = ez_on && x.xs >= 0 ? pr.ez_x[ox] : T(0);
+  s.zy = ez_on && x.ys >= 0 ? pr.ez_y[oy] : T(0);
+  return s;
+}
+
+// The H psi operands of one cell (AXES as in h_general).
+template <typename T, typename I, int AXES>
+__device__ __forceinline__ PsiOps<T> h_psi_load(const VolCore<T, I> &p, const SlabCtx<T> &x, int i, int j, int k) {
+  constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
+  const bool i_lt = !SX || i < p.d.nx, j_lt = !SY || j < p.d.ny, k_lt = !SZ || k < p.d.nz;
+  const bool hx_on = j_lt && k_lt, hy_on = i_lt && k_lt, hz_on = i_lt && j_lt;
+  unsigned ox, oy, oz;
+  psi_offsets(p, x, i, j, k, ox, oy, oz);
+  const Psi<T> &ps = p.psi;
+  PsiOps<T> s;
+  s.xy = hx_on && x.ys >= 0 ? ps.hx_y[oy] : T(0);
+  s.xz = hx_on && x.zs >= 0 ? ps.hx_z[oz] : T(0);
+  s.yx = hy_on && x.xs >= 0 ? ps.hy_x[ox] : T(0);
+  s.yz = hy_on && x.zs >= 0 ? ps.hy_z[oz] : T(0);
+  s.zx = hz_on && x.xs >= 0 ? ps.hz_x[ox] : T(0);
+  s.zy = hz_on && x.ys >= 0 ? ps.hz_y[oy] : T(0);
+  return s;
+}
+
+// The arithmetic of the general E update of one cell, from its operands:
+// curl operands h, coefficients c, CPML context x and psi operands ps
+// (e_psi_load).  Psi is written to pw when store_psi.  w[c] reports whether
+// component c was updated.  The arithmetic is that of the reference's
+// loops, term by term.  AXES (bit 0 x, 1 y, 2 z) names the axes whose index
+// may be special (wall or CPML slab); on the others the caller guarantees a
+// plain index, and their tests and terms drop out at compile time (a CPML
+// face cell has one special axis, an edge cell two).
+template <typename T, typename I, int AXES>
+__device__ __forceinline__ void e_general_ops(const VolCore<T, I> &p, const T *c, int i, int j, int k,
+                                              const ECurl<T> &h, const SlabCtx<T> &x, const PsiOps<T> &ps,
+                                              const Psi<T> &pw, bool store_psi, T &ex, T &ey, T &ez, bool w[3]) {
+  constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
-  const int xs = SX && p.cp[0].n_layers ? __ldg(p.cp[0].slot_e + i) : -1;
-  const int ys = SY && p.cp[1].n_layers ? __ldg(p.cp[1].slot_e + j) : -1;
-  const int zs = SZ && p.cp[2].n_layers ? __ldg(p.cp[2].slot_e + k) : -1;
+  const int xs = SX ? x.xs : -1, ys = SY ? x.ys : -1, zs = SZ ? x.zs : -1;
   const bool in_i = !SX || (i >= 1 && i < nx), in_j = !SY || (j >= 1 && j < ny), in_k = !SZ || (k >= 1 && k < nz);
   const bool ex_on = !SX || i < nx, ey_on = !SY || j < ny, ez_on = !SZ || k < nz;   // Ex, Ey, Ez exist here
-  const unsigned Ly = p.cp[1].n_layers, Lz = p.cp[2].n_layers;
-  const unsigned nzp = static_cast<unsigned>(p.d.nzp), ny1 = static_cast<unsigned>(ny + 1);
-  const unsigned ox = (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;   // X-slab psi (Ey, Ez)
-  const unsigned oy = (static_cast<unsigned>(i) * Ly + ys) * nzp + k;    // Y-slab psi (Ex, Ez)
-  const unsigned oz = (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;    // Z-slab psi (Ex, Ey)
+  unsigned ox, oy, oz;
+  psi_offsets(p, x, i, j, k, ox, oy, oz);
+  const AxisCoef<T> &X = x.X, &Y = x.Y, &Z = x.Z;
+  const T s_ex_y = ps.xy, s_ex_z = ps.xz, s_ey_x = ps.yx, s_ey_z = ps.yz, s_ez_x = ps.zx, s_ez_y = ps.zy;
   T cf[9];
 #pragma unroll
   for (int q = 0; q < 9; ++q) cf[q] = c[q];
-  const AxisCoef<T> X = axis_coef(xs, p.cp[0].b_e, p.cp[0].a_e, p.cp[0].rk_e, i);
-  const AxisCoef<T> Y = axis_coef(ys, p.cp[1].b_e, p.cp[1].a_e, p.cp[1].rk_e, j);
-  const AxisCoef<T> Z = axis_coef(zs, p.cp[2].b_e, p.cp[2].a_e, p.cp[2].rk_e, k);
-  const T s_ex_y = ex_on && ys >= 0 ? pr.ex_y[oy] : T(0);
-  const T s_ex_z = ex_on && zs >= 0 ? pr.ex_z[oz] : T(0);
-  const T s_ey_x = ey_on && xs >= 0 ? pr.ey_x[ox] : T(0);
-  const T s_ey_z = ey_on && zs >= 0 ? pr.ey_z[oz] : T(0);
-  const T s_ez_x = ez_on && xs >= 0 ? pr.ez_x[ox] : T(0);
-  const T s_ez_y = ez_on && ys >= 0 ? pr.ez_y[oy] : T(0);
   w[0] = w[1] = w[2] = false;
 
   // ---- Ex (nx, ny+1, nz+1) ----
@@ -271,36 +342,40 @@ __device__ __forceinline__ void e_general(const VolCore<T, I> &p, const T *c, in
   }
 }
 
-// General H update of one cell: last planes and CPML slabs (H psi in place),
-// operands first and AXES as in e_general.
-template <typename T, typename I, int AXES = 7>
-__device__ __forceinline__ void h_general(const VolCore<T, I> &p, const T *c, int i, int j, int k,
-                                          const HCurl<T> &e, T &hx, T &hy, T &hz, bool w[3]) {
+// General E update of one cell: outer walls and CPML slabs.  E psi is read
+// from pr and, when store_psi, written to pw (SEPARATE_PSI) or back to pr
+// (in place).  Every operand (coefficients, profiles, psi values) is loaded
+// before the first store, so that the loads are in flight together.  AXES
+// as in e_general_ops.
+template <typename T, typename I, bool SEPARATE_PSI, int AXES = 7>
+__device__ __forceinline__ void e_general(const VolCore<T, I> &p, const T *c, int i, int j, int k,
+                                          const ECurl<T> &h, const Psi<T> &pr, const Psi<T> &pw_, bool store_psi,
+                                          T &ex, T &ey, T &ez, bool w[3]) {
+  const Psi<T> &pw = SEPARATE_PSI ? pw_ : pr;
+  const SlabCtx<T> x = slab_ctx<T, I, AXES>(p, 0, i, j, k);
+  const PsiOps<T> ps = e_psi_load<T, I, AXES>(p, x, i, j, k, pr);
+  e_general_ops<T, I, AXES>(p, c, i, j, k, h, x, ps, pw, store_psi, ex, ey, ez, w);
+}
+
+// The arithmetic of the general H update of one cell (H psi in place), as
+// e_general_ops.
+template <typename T, typename I, int AXES>
+__device__ __forceinline__ void h_general_ops(const VolCore<T, I> &p, const T *c, int i, int j, int k,
+                                              const HCurl<T> &e, const SlabCtx<T> &x, const PsiOps<T> &pv,
+                                              T &hx, T &hy, T &hz, bool w[3]) {
   constexpr bool SX = AXES & 1, SY = AXES & 2, SZ = AXES & 4;
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
-  const int xs = SX && p.cp[0].n_layers ? __ldg(p.cp[0].slot_h + i) : -1;
-  const int ys = SY && p.cp[1].n_layers ? __ldg(p.cp[1].slot_h + j) : -1;
-  const int zs = SZ && p.cp[2].n_layers ? __ldg(p.cp[2].slot_h + k) : -1;
-  const unsigned Ly = p.cp[1].n_layers, Lz = p.cp[2].n_layers;
-  const unsigned nzp = static_cast<unsigned>(p.d.nzp), ny1 = static_cast<unsigned>(ny + 1);
+  const int xs = SX ? x.xs : -1, ys = SY ? x.ys : -1, zs = SZ ? x.zs : -1;
   const bool i_lt = !SX || i < nx, j_lt = !SY || j < ny, k_lt = !SZ || k < nz;
   const bool hx_on = j_lt && k_lt, hy_on = i_lt && k_lt, hz_on = i_lt && j_lt;   // Hx, Hy, Hz exist here
-  const unsigned ox = (static_cast<unsigned>(xs) * ny1 + j) * nzp + k;   // X-slab psi (Hy, Hz)
-  const unsigned oy = (static_cast<unsigned>(i) * Ly + ys) * nzp + k;    // Y-slab psi (Hx, Hz)
-  const unsigned oz = (static_cast<unsigned>(i) * ny1 + j) * Lz + zs;    // Z-slab psi (Hx, Hy)
+  unsigned ox, oy, oz;
+  psi_offsets(p, x, i, j, k, ox, oy, oz);
   const Psi<T> &ps = p.psi;
+  const AxisCoef<T> &X = x.X, &Y = x.Y, &Z = x.Z;
+  const T s_hx_y = pv.xy, s_hx_z = pv.xz, s_hy_x = pv.yx, s_hy_z = pv.yz, s_hz_x = pv.zx, s_hz_y = pv.zy;
   T cf[9];
 #pragma unroll
   for (int q = 0; q < 9; ++q) cf[q] = c[q];
-  const AxisCoef<T> X = axis_coef(xs, p.cp[0].b_m, p.cp[0].a_m, p.cp[0].rk_m, i);
-  const AxisCoef<T> Y = axis_coef(ys, p.cp[1].b_m, p.cp[1].a_m, p.cp[1].rk_m, j);
-  const AxisCoef<T> Z = axis_coef(zs, p.cp[2].b_m, p.cp[2].a_m, p.cp[2].rk_m, k);
-  const T s_hx_y = hx_on && ys >= 0 ? ps.hx_y[oy] : T(0);
-  const T s_hx_z = hx_on && zs >= 0 ? ps.hx_z[oz] : T(0);
-  const T s_hy_x = hy_on && xs >= 0 ? ps.hy_x[ox] : T(0);
-  const T s_hy_z = hy_on && zs >= 0 ? ps.hy_z[oz] : T(0);
-  const T s_hz_x = hz_on && xs >= 0 ? ps.hz_x[ox] : T(0);
-  const T s_hz_y = hz_on && ys >= 0 ? ps.hz_y[oy] : T(0);
   w[0] = w[1] = w[2] = false;
 
   // ---- Hx (nx+1, ny, nz) ----
@@ -377,6 +452,16 @@ __device__ __forceinline__ void h_general(const VolCore<T, I> &p, const T *c, in
       w[2] = true;
     }
   }
+}
+
+// General H update of one cell: last planes and CPML slabs (H psi in place),
+// operands first and AXES as in e_general_ops.
+template <typename T, typename I, int AXES = 7>
+__device__ __forceinline__ void h_general(const VolCore<T, I> &p, const T *c, int i, int j, int k,
+                                          const HCurl<T> &e, T &hx, T &hy, T &hz, bool w[3]) {
+  const SlabCtx<T> x = slab_ctx<T, I, AXES>(p, 1, i, j, k);
+  const PsiOps<T> pv = h_psi_load<T, I, AXES>(p, x, i, j, k);
+  h_general_ops<T, I, AXES>(p, c, i, j, k, e, x, pv, hx, hy, hz, w);
 }
 
 // E update of one cell by the general path.  It serves any cell: a plain
@@ -470,6 +555,8 @@ __device__ __forceinline__ void e_fast(const VolCore<T, I> &p, const T *tab, int
 struct InteriorBox {
   int lo[3], hi[3];
   int k0;
+  int px_lo, px_hi, py_lo, py_hi;   // plain runs on x and y and the interior's k range
+  int pz_lo, pz_hi;                 //   (the wide and z-edge TMA launches of interior_tma.cuh)
 };
 
 // The shell: boxes of cells (origin, extent per axis), each covering whole

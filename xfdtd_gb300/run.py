@@ -28,6 +28,10 @@ def main():
     ap.add_argument("--kernel-variant", default=None, metavar="E,H",
                     help="interior-kernel variants of the E and H updates (after autotuning; for profiling a "
                          "fixed variant)")
+    ap.add_argument("--shell-variant", default=None, metavar="E,H",
+                    help="shell-kernel variants of the E and H updates (after the interior variants)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the autotuner's trials (with --kernel-variant, for profiling one launch per step)")
     ap.add_argument("--out", default=None)
     ap.add_argument("--adjoint", action="store_true",
                     help="run the adjoint-gradient problem (forward with checkpoints, then backward) instead")
@@ -43,9 +47,12 @@ def main():
         sc.nffft.output_dir_path = args.out
     t0 = time.perf_counter()
     fused = {"auto": None, "fused": True, "split": False}[args.volume]
-    sim = Simulation(sc, steps, precision=args.precision, graph=not args.no_graph, fused=fused)
+    sim = Simulation(sc, steps, precision=args.precision, graph=not args.no_graph, fused=fused,
+                     autotune=not args.no_autotune)
     if args.kernel_variant:
         sim.set_kernel_variant(*(int(v) for v in args.kernel_variant.split(",")))
+    if args.shell_variant:
+        sim.set_shell_variant(*(int(v) for v in args.shell_variant.split(",")))
     t1 = time.perf_counter()
     ms = sim.step_timed(steps)
     sim.synchronize()
