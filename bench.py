@@ -164,12 +164,17 @@ PROFILE_STEPS = 400     # steps of the profiled pass behind the kernel times
 
 SIDE_STREAM_KERNELS = ("tfsf_aux", "update_e_interior", "update_e_shell", "update_h_interior", "update_h_shell")
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one E update
-# on this workload: the ncu --set full captures of its interior kernel
-# (524.7 MB) and its shell kernel (386.2 MB), each run by
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one E and
+# one H update on this workload in the wide decomposition, keyed by (entry,
+# precision, grid, wide): the wide interior launch plus the z-edge launch,
+# one ncu capture of each in step 13 of
 # python -m xfdtd_gb300.run --config dielectric_sphere --steps 24 --precision fp32 --no-graph --volume split
-#     --kernel-variant 9,9
-NCU_TRAFFIC = {("update_e", "fp32", (280, 280, 280)): 524.660992e6 + 386.16576e6}
+#     --no-autotune --kernel-variant 20,20 --shell-variant 5,5
+# E: 535.4 + 193.0 MB (interior) + 219.8 + 40.7 MB (z edges); H: 504.4 + 190.5 + 187.7 + 34.3 MB.
+NCU_TRAFFIC = {
+    ("update_e", "fp32", (280, 280, 280), True): 535.400704e6 + 192.98304e6 + 219.822848e6 + 40.7488e6,
+    ("update_h", "fp32", (280, 280, 280), True): 504.384e6 + 190.464e6 + 187.740672e6 + 34.299904e6,
+}
 
 
 def dominant(prof) -> str:
@@ -442,6 +447,10 @@ def ours_arm(args, world, rank, local, grp):
     setup = GRAPH_STEPS - args.warmup % GRAPH_STEPS + GRAPH_STEPS
     total = args.warmup + setup + args.steps
     sim = X.Simulation(sc, total, precision=args.precision, graph=True, device=local, fused=fused)
+    if args.kernel_variant:
+        sim.set_kernel_variant(*(int(v) for v in args.kernel_variant.split(",")))
+    if args.shell_variant:
+        sim.set_shell_variant(*(int(v) for v in args.shell_variant.split(",")))
     n = sim.n
     cells = n[0] * n[1] * n[2]
     sim.step(args.warmup)
@@ -550,7 +559,7 @@ def ours_arm(args, world, rank, local, grp):
                                  f"and {setup} untimed steps to reach a graph boundary and capture the graph"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": NCU_TRAFFIC.get((dom, args.precision, tuple(n))),
+                     "traffic": NCU_TRAFFIC.get((dom, args.precision, tuple(n), split.get(dom[7] + "_wide"))),
                      "algorithmic_bytes_per_launch": alg, "launch_ms": dom_ms / dom_n,
                      "timing": f"CUDA events around each launch in a profiled pass of {prof_steps} steps "
                                f"({prof_ms_total / prof_steps:.4f} ms/step, no graph)"},
@@ -591,6 +600,10 @@ def main():
                          "workload), the fused E/H sweep, or the autotuner's choice")
     ap.add_argument("--adjoint", type=int, default=1, help="run the adjoint form (0: skip)")
     ap.add_argument("--hetero-steps", type=int, default=100, help="steps of the heterogeneous-medium form (0: skip)")
+    ap.add_argument("--kernel-variant", default=None, metavar="E,H",
+                    help="fix the interior variants of the headline run (after autotuning; for a launch list "
+                         "under a profiler, whose timings would mislead the autotuner)")
+    ap.add_argument("--shell-variant", default=None, metavar="E,H", help="fix the shell variants likewise")
     ap.add_argument("--adjoint-fd", type=int, default=16, help="design voxels of the adjoint FD check (0: skip)")
     ap.add_argument("--adjoint-checkpoint", type=int, default=0,
                     help="adjoint form: checkpoint every K steps (0: record the design box at every step)")

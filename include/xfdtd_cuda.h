@@ -222,7 +222,8 @@ int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant);
 /* Variants of the shell launches (walls and CPML slabs): how many, the ones
  * in use for E and H; and fixing them (all give the same bits).  Variants
  * 0-3 are the shell kernel (register cap x table form); 4-6 the z-edge
- * TMA-staged launch, offered with a wide interior variant only
+ * TMA-staged launch (ring stages x table form), offered
+ * with a wide interior variant only
  * (XFDTD_ERR_INVALID_PLAN otherwise). */
 int xfdtd_shell_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h);
 int xfdtd_set_shell_variant(xfdtd_handle *h, int e_variant, int h_variant);
