@@ -140,6 +140,21 @@ typedef struct xfdtd_probe_term {
   double weight;
 } xfdtd_probe_term;
 
+/* A series of field snapshots, what a MovieMonitor over a
+ * TimeDomainFieldMonitor records (src/monitor/movie_monitor.cpp:46-59,
+ * src/monitor/field_monitor.cpp:91-122): after each step t with
+ * t % every == 0, and after step `last` (-1: none), the values of field
+ * component comp (0..5: Ex Ey Ez Hx Hy Hz) over the box lo .. lo+n-1 of
+ * the component's array. */
+typedef struct xfdtd_snapshot_desc {
+  int32_t comp;
+  int32_t reserved;
+  int64_t lo[3];
+  int64_t n[3];
+  int64_t every;                   /* >= 1                                      */
+  int64_t last;
+} xfdtd_snapshot_desc;
+
 typedef struct xfdtd_plan_desc {
   int32_t nx, ny, nz;
   int32_t precision;               /* XFDTD_FP64 or XFDTD_FP32 (fields, psi)    */
@@ -165,6 +180,9 @@ typedef struct xfdtd_plan_desc {
   int32_t n_probe_terms;
   int32_t reserved2;
   const xfdtd_probe_term *probe_terms;
+  int32_t n_snapshots;
+  int32_t reserved3;
+  const xfdtd_snapshot_desc *snapshots;
 } xfdtd_plan_desc;
 
 typedef struct xfdtd_handle xfdtd_handle;
@@ -187,6 +205,13 @@ int xfdtd_read_field(xfdtd_handle *h, int comp, double *out, int64_t len);
 int xfdtd_write_field(xfdtd_handle *h, int comp, const double *in, int64_t len);
 /* Probe time series [n_probes * total_steps]. */
 int xfdtd_read_probes(xfdtd_handle *h, double *out, int64_t len);
+/* Frames of snapshot series s (plan order): their number, and the step
+ * after which each is taken (steps[f] for f < min(max, count); steps may be
+ * null).  A frame holds data once its step has run. */
+int xfdtd_snapshot_frames(xfdtd_handle *h, int s, int64_t *count, int64_t *steps, int64_t max);
+/* Frame f of snapshot series s, [n0][n1][n2] converted to FP64 (len =
+ * n0*n1*n2 of the series' box). */
+int xfdtd_read_snapshot(xfdtd_handle *h, int s, int64_t frame, double *out, int64_t len);
 /* NF-FF accumulator `which` = face*4 + q (faces XN XP YN YP ZN ZP; X faces
  * jy jz my mz over (ny_box, nz_box); Y faces jz jx mz mx over (nz_box,
  * nx_box); Z faces jx jy mx my over (nx_box, ny_box)), [n_freq][a][b] (re, im). */

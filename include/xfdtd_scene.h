@@ -63,7 +63,7 @@ enum {
   XFDTD_LUMPED_CAPACITOR = 3,
   XFDTD_LUMPED_INDUCTOR = 4
 };
-enum { XFDTD_MONITOR_VOLTAGE = 0, XFDTD_MONITOR_CURRENT = 1 };
+enum { XFDTD_MONITOR_VOLTAGE = 0, XFDTD_MONITOR_CURRENT = 1, XFDTD_MONITOR_FIELD = 2 };
 
 /* Field components in the order of EMF's getters. */
 enum { XFDTD_EX = 0, XFDTD_EY = 1, XFDTD_EZ = 2, XFDTD_HX = 3, XFDTD_HY = 4, XFDTD_HZ = 5 };
@@ -153,6 +153,14 @@ typedef struct xfdtd_monitor_desc {
   int32_t orientation;  /* XFDTD_XN .. XFDTD_ZP                           */
   double point[3];
   double size[3];
+  /* XFDTD_MONITOR_FIELD: TimeDomainFieldMonitor(cube, plane_type,
+   * component, ...) (src/include/monitor/field_monitor.h); with
+   * plot_step > 0 wrapped in MovieMonitor(monitor, total_time_steps,
+   * plot_step) (src/include/monitor/movie_monitor.h).                    */
+  int32_t component;    /* EMComponent: 0 EX .. 5 HZ                       */
+  int32_t plane_type;   /* PlaneType: 0 XY, 1 YZ, 2 ZX                     */
+  int64_t plot_step;
+  int64_t total_time_steps;
 } xfdtd_monitor_desc;
 
 typedef struct xfdtd_scene_desc {

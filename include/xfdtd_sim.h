@@ -43,9 +43,24 @@ int xfdtd_sim_info(xfdtd_sim *s, int64_t out_n[3], double *out_dt, int64_t *out_
 int xfdtd_sim_read_field(xfdtd_sim *s, int comp, double *out, int64_t len);
 int xfdtd_sim_write_field(xfdtd_sim *s, int comp, const double *in, int64_t len);
 int xfdtd_sim_read_monitor(xfdtd_sim *s, int index, double *out, int64_t len);
+/* A field monitor (TimeDomainFieldMonitor, or a MovieMonitor over one):
+ * its box (first index lo and shape, in the component's array), its number
+ * of frames and their steps (steps[f] for f < min(max, n_frames); may be
+ * null).  A plain field monitor has one frame,
+ * the current field, step -1; a movie monitor's frames are those of
+ * MovieMonitor::update (src/monitor/movie_monitor.cpp:46-59). */
+int xfdtd_sim_field_monitor(xfdtd_sim *s, int index, int64_t lo[3], int64_t shape[3], int64_t *n_frames,
+                            int64_t *steps, int64_t max);
+/* Frame `frame` of field monitor `index`, [n0][n1][n2]. */
+int xfdtd_sim_read_field_monitor(xfdtd_sim *s, int index, int64_t frame, double *out, int64_t len);
 int xfdtd_sim_read_nffft(xfdtd_sim *s, int which, double *out, int64_t len);
 int xfdtd_sim_far_field(xfdtd_sim *s, int which, double *out, int64_t len);
 int xfdtd_sim_incident_dft(xfdtd_sim *s, const double *freqs, int n, double *out);
+/* Output directory (and file name) of monitor `index`, or with index -1
+ * the NF-FF's output directory: the constructors' output_dir_path /
+ * output_file_name arguments, which the scene description does not
+ * carry.  An empty directory writes nothing. */
+int xfdtd_sim_set_output(xfdtd_sim *s, int index, const char *dir, const char *file);
 /* Writes the reference's .npy outputs (NF-FF into its output directory,
  * monitors into theirs). */
 int xfdtd_sim_output(xfdtd_sim *s);

@@ -46,6 +46,9 @@ def lib():
                    "oracle_sim_far_field", "oracle_sim_read_coeff"):
             getattr(L, fn).argtypes = [C.c_void_p, C.c_int, P(C.c_double), C.c_int64]
         L.oracle_sim_write_field.argtypes = [C.c_void_p, C.c_int, P(C.c_double), C.c_int64]
+        L.oracle_sim_field_monitor.argtypes = [C.c_void_p, C.c_int, P(C.c_int64), P(C.c_int64), P(C.c_int64),
+                                               P(C.c_int64), C.c_int64]
+        L.oracle_sim_read_field_monitor.argtypes = [C.c_void_p, C.c_int, C.c_int64, P(C.c_double), C.c_int64]
         L.oracle_sim_incident_dft.argtypes = [C.c_void_p, P(C.c_double), C.c_int, P(C.c_double)]
         L.oracle_set_threads.argtypes = [C.c_int]
         L.oracle_last_error.restype = C.c_char_p
@@ -118,6 +121,21 @@ class OracleSim:
     def read_monitor(self, index: int) -> np.ndarray:
         out = np.empty(self.total_steps, dtype=np.float64)
         _check(lib().oracle_sim_read_monitor(self.h, index, _dp(out), out.size))
+        return out
+
+    def field_monitor_frames(self, index: int):
+        """(lo, shape, frame steps) of field or movie monitor `index`."""
+        lo, shape = (C.c_int64 * 3)(), (C.c_int64 * 3)()
+        n = C.c_int64()
+        _check(lib().oracle_sim_field_monitor(self.h, index, lo, shape, C.byref(n), None, 0))
+        steps = (C.c_int64 * max(1, n.value))()
+        _check(lib().oracle_sim_field_monitor(self.h, index, lo, shape, C.byref(n), steps, n.value))
+        return tuple(lo), tuple(shape), [steps[f] for f in range(n.value)]
+
+    def read_field_monitor(self, index: int, frame: int = 0) -> np.ndarray:
+        _, shape, _ = self.field_monitor_frames(index)
+        out = np.empty(shape, dtype=np.float64)
+        _check(lib().oracle_sim_read_field_monitor(self.h, index, int(frame), _dp(out), out.size))
         return out
 
     def nffft_box(self):

@@ -299,6 +299,10 @@ struct Monitor {
   std::vector<double> coff, da, db;
   double positive = 1;
   std::vector<double> value;
+  // field monitors: the component view (lo, n) and a movie's frames
+  size_t lo[3] = {0, 0, 0}, n[3] = {0, 0, 0};
+  std::vector<std::vector<double>> frames;
+  std::vector<long long> frame_steps;
 };
 
 struct Sim;
@@ -389,6 +393,17 @@ struct oracle_sim {
   void lumpedE(Lumped &l);
   void nffftUpdate();
   void monitorUpdate(Monitor &m);
+  // TimeDomainFieldMonitor::outputData's view of the current field
+  // (field_monitor.cpp:102-121)
+  std::vector<double> fieldView(const Monitor &m) {
+    const A3 &f = field(m.d.component);
+    std::vector<double> v;
+    v.reserve(m.n[0] * m.n[1] * m.n[2]);
+    for (size_t i = 0; i < m.n[0]; ++i)
+      for (size_t j = 0; j < m.n[1]; ++j)
+        for (size_t k = 0; k < m.n[2]; ++k) v.push_back(f(m.lo[0] + i, m.lo[1] + j, m.lo[2] + k));
+    return v;
+  }
   void farField();
 };
 
@@ -881,6 +896,21 @@ void oracle_sim::initPML(PML &p) {
 void oracle_sim::initMonitor(Monitor &m) {
   GridBox g = gs->getGridBox(m.d.point, m.d.size);
   for (int a = 0; a < 3; ++a) { m.s[a] = g.start(a); m.e[a] = g.end(a); }
+  if (m.d.kind == XFDTD_MONITOR_FIELD) {  // TimeDomainFieldMonitor::init, field_monitor.cpp:31-82
+    if (m.d.component < 0 || m.d.component > 5) throw std::invalid_argument("bad component");
+    const int normal = m.d.plane_type == 0 ? 2 : (m.d.plane_type == 1 ? 0 : 1);   // XY, YZ, ZX
+    if (m.e[normal] - m.s[normal] > 1) throw std::runtime_error("Error: invalid grid box");
+    // outputData's view (field_monitor.cpp:105-117): extents of 0 count
+    // as 1; the range is clipped to the component's array
+    const A3 &f = field(m.d.component);
+    const size_t lim[3] = {f.n0, f.n1, f.n2};
+    for (int a = 0; a < 3; ++a) {
+      m.lo[a] = m.s[a];
+      if (m.lo[a] >= lim[a]) throw std::out_of_range("field monitor outside its component");
+      m.n[a] = std::min(std::max<size_t>(m.e[a] - m.s[a], 1), lim[a] - m.lo[a]);
+    }
+    return;
+  }
   int axis = m.d.orientation / 2;
   bool neg = m.d.orientation % 2 == 0;
   if (m.d.kind == XFDTD_MONITOR_VOLTAGE) {  // voltage_monitor.cpp:25-62
@@ -1218,6 +1248,17 @@ void oracle_sim::nffftUpdate() {  // NffftFd::update, nffft_fd.cpp:108-203
 void oracle_sim::monitorUpdate(Monitor &m) {
   size_t t = cur;
   int axis = m.d.orientation / 2;
+  if (m.d.kind == XFDTD_MONITOR_FIELD) {
+    // MovieMonitor::update (movie_monitor.cpp:46-59): a frame when t is a
+    // multiple of the plot step or the movie's last step; a plain field
+    // monitor records nothing during the run
+    if (m.d.plot_step <= 0) return;
+    const long long tt = static_cast<long long>(t);
+    if (tt % m.d.plot_step != 0 && tt != m.d.total_time_steps - 1) return;
+    m.frames.push_back(fieldView(m));
+    m.frame_steps.push_back(tt);
+    return;
+  }
   if (m.d.kind == XFDTD_MONITOR_VOLTAGE) {  // voltage_monitor.cpp:64-97
     A3 &e = field(axis);
     for (size_t i = m.s[0]; i < m.e[0]; ++i)
@@ -1484,6 +1525,42 @@ int oracle_sim_read_monitor(oracle_sim *s, int index, double *out, int64_t len) 
   return guarded([&] {
     if (index < 0 || index >= static_cast<int>(s->monitors.size())) throw std::invalid_argument("bad monitor");
     auto &v = s->monitors[index].value;
+    if (static_cast<size_t>(len) != v.size()) throw std::invalid_argument("length mismatch");
+    std::memcpy(out, v.data(), v.size() * sizeof(double));
+  });
+}
+
+int oracle_sim_field_monitor(oracle_sim *s, int index, int64_t lo[3], int64_t shape[3], int64_t *n_frames,
+                             int64_t *steps, int64_t max) {
+  return guarded([&] {
+    if (index < 0 || index >= static_cast<int>(s->monitors.size())) throw std::invalid_argument("bad monitor");
+    const Monitor &m = s->monitors[index];
+    if (m.d.kind != XFDTD_MONITOR_FIELD) throw std::invalid_argument("not a field monitor");
+    for (int a = 0; a < 3; ++a) {
+      if (lo) lo[a] = static_cast<int64_t>(m.lo[a]);
+      if (shape) shape[a] = static_cast<int64_t>(m.n[a]);
+    }
+    const bool movie = m.d.plot_step > 0;
+    const int64_t nf = movie ? static_cast<int64_t>(m.frames.size()) : 1;
+    if (n_frames) *n_frames = nf;
+    if (steps)
+      for (int64_t f = 0; f < std::min(nf, max); ++f) steps[f] = movie ? m.frame_steps[f] : -1;
+  });
+}
+
+int oracle_sim_read_field_monitor(oracle_sim *s, int index, int64_t frame, double *out, int64_t len) {
+  return guarded([&] {
+    if (index < 0 || index >= static_cast<int>(s->monitors.size())) throw std::invalid_argument("bad monitor");
+    const Monitor &m = s->monitors[index];
+    if (m.d.kind != XFDTD_MONITOR_FIELD) throw std::invalid_argument("not a field monitor");
+    std::vector<double> v;
+    if (m.d.plot_step > 0) {
+      if (frame < 0 || frame >= static_cast<int64_t>(m.frames.size())) throw std::invalid_argument("bad frame");
+      v = m.frames[frame];
+    } else {
+      if (frame != 0) throw std::invalid_argument("bad frame");
+      v = s->fieldView(m);
+    }
     if (static_cast<size_t>(len) != v.size()) throw std::invalid_argument("length mismatch");
     std::memcpy(out, v.data(), v.size() * sizeof(double));
   });

@@ -44,6 +44,13 @@ int oracle_sim_read_field(oracle_sim *sim, int comp, double *out, int64_t len);
 int oracle_sim_write_field(oracle_sim *sim, int comp, const double *in, int64_t len);
 /* Monitor time series [total_steps]. */
 int oracle_sim_read_monitor(oracle_sim *sim, int index, double *out, int64_t len);
+/* A field monitor (TimeDomainFieldMonitor, or a MovieMonitor over one,
+ * src/monitor/field_monitor.cpp, movie_monitor.cpp): its view of the
+ * component (lo, shape), its frames so far and their steps (a plain field
+ * monitor: one frame, the current field, step -1). */
+int oracle_sim_field_monitor(oracle_sim *sim, int index, int64_t lo[3], int64_t shape[3], int64_t *n_frames,
+                             int64_t *steps, int64_t max);
+int oracle_sim_read_field_monitor(oracle_sim *sim, int index, int64_t frame, double *out, int64_t len);
 /* NF-FF running-DFT accumulators, complex as (re, im) pairs.  which = face*4+q,
  * faces XN,XP,YN,YP,ZN,ZP; q: X faces jy,jz,my,mz; Y faces jz,jx,mz,mx;
  * Z faces jx,jy,mx,my (nffft_fd.cpp:117-203). */

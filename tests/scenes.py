@@ -120,6 +120,23 @@ def _boxed(dims, dl, boundaries, steps, cfl=0.97):
     return S.Scene(dl, objects, boundaries, lumped_elements=[src], monitors=[mon], cfl=cfl), steps
 
 
+def field_monitors(steps=40):
+    """A boxed scene (CPML on every face, a soft source) with field
+    monitors between its voltage monitors: a movie of Ez on an XY plane
+    (plot step 6), a plain Hy monitor on a YZ plane, a movie of Hx on a ZX
+    plane whose own total_time_steps ends before the run does (its extra
+    last frame falls between plot steps), and a second voltage monitor."""
+    dl = 2e-3
+    dims = (14, 12, 16)
+    sc, _ = _boxed(dims, dl, _six(4), steps)
+    ez = S.TimeDomainFieldMonitor(S.Cube([0, 0, 7 * dl], [dims[0] * dl, dims[1] * dl, 0]), S.PLANE_XY, S.EZ)
+    hy = S.TimeDomainFieldMonitor(S.Cube([6 * dl, 2 * dl, 3 * dl], [0, 8 * dl, 9 * dl]), S.PLANE_YZ, S.HY)
+    hx = S.TimeDomainFieldMonitor(S.Cube([dl, 5 * dl, 0], [10 * dl, 0, 12 * dl]), S.PLANE_ZX, S.HX)
+    v2 = S.VoltageMonitor(S.Cube([4 * dl, 4 * dl, 4 * dl], [dl, dl, 2 * dl]), S.ZP)
+    sc.monitors = [sc.monitors[0], S.MovieMonitor(ez, steps, 6), hy, S.MovieMonitor(hx, steps - 3, 7), v2]
+    return sc, steps
+
+
 def _six(t):
     return [S.PML(o, t) for o in (S.XN, S.XP, S.YN, S.YP, S.ZN, S.ZP)]
 

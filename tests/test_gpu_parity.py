@@ -368,3 +368,54 @@ def test_nffft_batches_flush_mid_run():
             plain.step(st)
             for w in range(24):
                 assert np.array_equal(g.read_nffft(w), plain.read_nffft(w))
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_field_and_movie_monitors(graph, tmp_path):
+    """TimeDomainFieldMonitor and MovieMonitor (field_monitor.cpp,
+    movie_monitor.cpp:46-59) on the engine: the frame steps and boxes of the
+    oracle; FP64 frames within 1e-10 of the oracle's; FP32 frames bit for
+    bit the engine's own field after each frame's step; the voltage monitors
+    around them keep their series; outputData writes one NNNN.npy per frame
+    and the plain monitor's file."""
+    sc, st = scenes.field_monitors(steps=30)
+    sc.monitors[1].output_dir_path = str(tmp_path / "movie_ez")
+    sc.monitors[2].output_dir_path = str(tmp_path / "hy")
+    sc.monitors[2].output_file_name = "hy.npy"
+    o = O.OracleSim(sc, st)
+    o.step(st)
+    for precision in ("fp64", "fp32"):
+        g = X.Simulation(sc, st, precision=precision, graph=graph)
+        g.step(st)
+        for m in (1, 2, 3):
+            lo, shape, steps = g.field_monitor_frames(m)
+            assert (lo, shape, steps) == o.field_monitor_frames(m), m
+            for f in range(len(steps)):
+                got, want = g.read_field_monitor(m, f), o.read_field_monitor(m, f)
+                assert got.shape == want.shape
+                e = scenes.rel_err(got, want)
+                assert e <= (TOL if precision == "fp64" else 1e-4), (precision, m, f, e)
+        for m in (0, 4):
+            e = scenes.rel_err(g.read_monitor(m), o.read_monitor(m))
+            assert e <= (TOL if precision == "fp64" else 1e-4), (precision, m, e)
+        if precision == "fp32":
+            # each frame is the field after its step, bit for bit
+            r = X.Simulation(sc, st, precision=precision, graph=graph)
+            frames = sorted((t, m, f) for m in (1, 3) for f, t in enumerate(g.field_monitor_frames(m)[2]))
+            done = 0
+            for t, m, f in frames:
+                if t + 1 > done:
+                    r.step(t + 1 - done)
+                    done = t + 1
+                lo, shape, _ = g.field_monitor_frames(m)
+                full = r.read_field(sc.monitors[m].component)
+                view = full[lo[0]:lo[0] + shape[0], lo[1]:lo[1] + shape[1], lo[2]:lo[2] + shape[2]]
+                assert np.array_equal(g.read_field_monitor(m, f), view), (m, f)
+        if precision == "fp64":
+            g.output()
+            _, _, steps = g.field_monitor_frames(1)
+            names = sorted(p.name for p in (tmp_path / "movie_ez").iterdir())
+            assert names == ["%04d.npy" % t for t in steps]
+            for f, t in enumerate(steps):
+                assert np.array_equal(np.load(tmp_path / "movie_ez" / ("%04d.npy" % t)), g.read_field_monitor(1, f))
+            assert np.array_equal(np.load(tmp_path / "hy" / "hy.npy"), g.read_field_monitor(2, 0))

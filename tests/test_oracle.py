@@ -152,3 +152,49 @@ def test_oracle_rejects_bad_scenes():
     sc2, _ = scenes.pec_sphere()
     with pytest.raises(RuntimeError):
         O.OracleSim(sc2, 0)
+
+
+def test_oracle_field_and_movie_monitors():
+    """TimeDomainFieldMonitor / MovieMonitor restated (field_monitor.cpp,
+    movie_monitor.cpp:46-59): a movie frame after every step t with
+    t % plot_step == 0 and after its last step, each the component's view
+    of the field after that step; a plain field monitor is the view of the
+    current field.  Checked against the oracle's own fields stepped one
+    step at a time."""
+    sc, st = scenes.field_monitors(steps=24)
+    o = O.OracleSim(sc, st)
+    o.step(st)
+    ref = O.OracleSim(sc, st)
+    views = {}
+    for t in range(st):
+        ref.step(1)
+        for m in (1, 2, 3):
+            lo, shape, _ = o.field_monitor_frames(m)
+            c = sc.monitors[m].component
+            f = ref.read_field(c)
+            views[(m, t)] = f[lo[0]:lo[0] + shape[0], lo[1]:lo[1] + shape[1], lo[2]:lo[2] + shape[2]]
+    lo, shape, steps = o.field_monitor_frames(1)
+    assert steps == [0, 6, 12, 18, 23] and shape[2] == 1 and lo[2] > 0
+    for f, t in enumerate(steps):
+        assert np.array_equal(o.read_field_monitor(1, f), views[(1, t)])
+    _, _, steps = o.field_monitor_frames(3)
+    # total_time_steps 21: its last step, 20, falls between plot steps, and
+    # the plot steps go on after it
+    assert steps == [0, 7, 14, 20, 21]
+    for f, t in enumerate(steps):
+        assert np.array_equal(o.read_field_monitor(3, f), views[(3, t)])
+    _, shape, steps = o.field_monitor_frames(2)
+    assert steps == [-1] and shape[0] == 1
+    assert np.array_equal(o.read_field_monitor(2, 0), views[(2, st - 1)])
+    # the voltage monitors keep their time series around the field monitors
+    assert np.abs(o.read_monitor(0)).max() > 0 and np.abs(o.read_monitor(4)).max() > 0
+
+
+def test_oracle_field_monitor_rejects_thick_plane():
+    """An XY field monitor more than one cell thick in z is an error
+    (field_monitor.cpp:35-38)."""
+    sc, st = scenes.field_monitors(steps=4)
+    dl = sc.cell_size
+    sc.monitors = [S.TimeDomainFieldMonitor(S.Cube([0, 0, 2 * dl], [4 * dl, 4 * dl, 3 * dl]), S.PLANE_XY, S.EX)]
+    with pytest.raises(RuntimeError):
+        O.OracleSim(sc, st)

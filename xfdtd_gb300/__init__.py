@@ -65,8 +65,12 @@ def libs():
         for fn in ("xfdtd_sim_read_field", "xfdtd_sim_read_monitor", "xfdtd_sim_read_nffft", "xfdtd_sim_far_field"):
             getattr(ho, fn).argtypes = [C.c_void_p, C.c_int, dp, C.c_int64]
         ho.xfdtd_sim_write_field.argtypes = [C.c_void_p, C.c_int, dp, C.c_int64]
+        ho.xfdtd_sim_field_monitor.argtypes = [C.c_void_p, C.c_int, P(C.c_int64), P(C.c_int64), P(C.c_int64),
+                                               P(C.c_int64), C.c_int64]
+        ho.xfdtd_sim_read_field_monitor.argtypes = [C.c_void_p, C.c_int, C.c_int64, dp, C.c_int64]
         ho.xfdtd_sim_incident_dft.argtypes = [C.c_void_p, dp, C.c_int, dp]
         ho.xfdtd_sim_output.argtypes = [C.c_void_p]
+        ho.xfdtd_sim_set_output.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_char_p]
         ho.xfdtd_sim_engine.argtypes = [C.c_void_p]
         ho.xfdtd_sim_engine.restype = C.c_void_p
         ho.xfdtd_sim_last_error.argtypes = [C.c_void_p]
@@ -153,6 +157,13 @@ class Simulation:
         self.n = tuple(int(v) for v in n)
         self.dt = dt.value
         self.engine = C.c_void_p(ho.xfdtd_sim_engine(self.h))
+        # output directories the scene description does not carry
+        if sc.nffft is not None and sc.nffft.output_dir_path:
+            self._check(ho.xfdtd_sim_set_output(self.h, -1, sc.nffft.output_dir_path.encode(), None))
+        for q, m in enumerate(sc.monitors):
+            if m.output_dir_path:
+                self._check(ho.xfdtd_sim_set_output(self.h, q, m.output_dir_path.encode(),
+                                                    (m.output_file_name or "").encode()))
 
     def close(self):
         if getattr(self, "h", None):
@@ -203,6 +214,24 @@ class Simulation:
     def read_monitor(self, index: int) -> np.ndarray:
         out = np.empty(self.total_steps, dtype=np.float64)
         self._check(libs()[1].xfdtd_sim_read_monitor(self.h, index, _dp(out), out.size))
+        return out
+
+    def field_monitor_frames(self, index: int):
+        """Box of field (or movie) monitor `index` in its component's array
+        (first index, shape) and the steps of its frames (-1: a field
+        monitor's one frame, the current field)."""
+        lo, shape = (C.c_int64 * 3)(), (C.c_int64 * 3)()
+        n = C.c_int64()
+        self._check(libs()[1].xfdtd_sim_field_monitor(self.h, index, lo, shape, C.byref(n), None, 0))
+        steps = (C.c_int64 * max(1, n.value))()
+        self._check(libs()[1].xfdtd_sim_field_monitor(self.h, index, lo, shape, C.byref(n), steps, n.value))
+        return tuple(lo), tuple(shape), [steps[f] for f in range(n.value)]
+
+    def read_field_monitor(self, index: int, frame: int = 0) -> np.ndarray:
+        """Frame `frame` of field (or movie) monitor `index`."""
+        _, shape, _ = self.field_monitor_frames(index)
+        out = np.empty(shape, dtype=np.float64)
+        self._check(libs()[1].xfdtd_sim_read_field_monitor(self.h, index, int(frame), _dp(out), out.size))
         return out
 
     def nffft_box(self):

@@ -68,8 +68,8 @@ struct Err {
 const char *kKernelNames[] = {"tfsf_aux",         "update_e",       "lumped_e",         "update_h",
                               "nffft",            "probes",         "advance",          "tfsf_e",
                               "tfsf_h",           "nffft_acc",      "sweep_eh",         "update_e_shell",
-                              "update_h_shell",   "update_e_interior", "update_h_interior"};
-constexpr int kNumKernels = 15;
+                              "update_h_shell",   "update_e_interior", "update_h_interior", "snapshots"};
+constexpr int kNumKernels = 16;
 
 }  // namespace
 
@@ -145,6 +145,10 @@ struct xfdtd_handle {
   xfdtd_probe_term *terms = nullptr;
   int *probe_off = nullptr;
   double *probe_out = nullptr;
+  // field snapshot series (host copies of the descriptors, device table)
+  std::vector<xg::SnapDev> snaps;
+  xg::SnapDev *d_snaps = nullptr;
+  long long snap_cells_max = 0;
 
   long long *d_step = nullptr;
   int *d_status = nullptr;
@@ -1254,6 +1258,18 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     XCHECK(cudaGetLastError());
     prof_end(h);
   }
+  if (!h->snaps.empty()) {
+    xg::SnapParams<T> sp{};
+    sp.d = h->d;
+    for (int c = 0; c < 6; ++c) sp.F[c] = static_cast<const T *>(h->F[c]);
+    sp.s = h->d_snaps;
+    sp.step = h->d_step;
+    const unsigned bx = static_cast<unsigned>(std::min<long long>((h->snap_cells_max + 255) / 256, 1024));
+    prof_begin(h, 15);
+    xg::k_snapshots<T><<<dim3(bx, static_cast<unsigned>(h->snaps.size())), 256, 0, h->stream>>>(sp);
+    XCHECK(cudaGetLastError());
+    prof_end(h);
+  }
   prof_begin(h, 6);
   xg::k_advance<<<1, 1, 0, h->stream>>>(h->d_step);
   XCHECK(cudaGetLastError());
@@ -1268,13 +1284,15 @@ void enqueue_step(xfdtd_handle *h, long long s) {
 }
 
 int launches_per_step(const xfdtd_handle *h) {
-  if (h->sweep) return (h->tfsf ? 2 : 0) + 1 + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
+  const int snap = h->snaps.empty() ? 0 : 1;
+  if (h->sweep) return (h->tfsf ? 2 : 0) + 1 + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + snap + 1;
   int vol = 0;
   for (int side = 0; side < 2; ++side) {
     const bool w = side_wide(h, side);
     vol += (side_interior_cells(h, side, w) ? 1 : 0) + (side_shell_cells(h, side, w) ? 1 : 0);
   }
-  return (h->tfsf ? 3 : 0) + vol + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + 1;
+  return (h->tfsf ? 3 : 0) + vol + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) +
+         snap + 1;
 }
 
 // Captures g steps starting at a step index that is a multiple of the NF-FF
@@ -1572,6 +1590,37 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     h->probe_off = h->upload<int>(off.data(), off.size());
     h->probe_out = h->alloc<double>(static_cast<size_t>(pl->n_probes) * pl->total_steps);
   }
+  if (pl->n_snapshots < 0 || (pl->n_snapshots && !pl->snapshots)) invalid("bad snapshot list");
+  if (pl->n_snapshots > 65535) invalid("at most 65535 snapshot series");
+  long long snap_bytes = 0;
+  for (int q = 0; q < pl->n_snapshots; ++q) {
+    const xfdtd_snapshot_desc &sd = pl->snapshots[q];
+    if (sd.comp < 0 || sd.comp > 5) invalid("bad field component in a snapshot series");
+    if (sd.every < 1) invalid("snapshot interval must be at least 1");
+    long long cs[3];
+    comp_shape(h, sd.comp, cs);
+    xg::SnapDev sv{};
+    sv.comp = sd.comp;
+    sv.cells = 1;
+    for (int a = 0; a < 3; ++a) {
+      if (sd.n[a] < 1 || sd.lo[a] < 0 || sd.lo[a] + sd.n[a] > cs[a]) invalid("snapshot box outside its component");
+      sv.lo[a] = sd.lo[a];
+      sv.n[a] = sd.n[a];
+      sv.cells *= sd.n[a];
+    }
+    sv.every = sd.every;
+    sv.last = sd.last;
+    sv.n_regular = pl->total_steps > 0 ? (pl->total_steps - 1) / sd.every + 1 : 0;
+    const bool extra = sd.last >= 0 && sd.last < pl->total_steps && sd.last % sd.every != 0;
+    sv.extra = extra ? 1 : 0;
+    sv.n_frames = sv.n_regular + sv.extra;
+    snap_bytes += sv.n_frames * sv.cells * static_cast<long long>(h->esize);
+    if (snap_bytes > (64ll << 30)) invalid("snapshot frames above 64 GiB");
+    sv.frames = h->alloc_bytes(static_cast<size_t>(std::max(1ll, sv.n_frames * sv.cells)) * h->esize);
+    h->snap_cells_max = std::max(h->snap_cells_max, sv.cells);
+    h->snaps.push_back(sv);
+  }
+  if (!h->snaps.empty()) h->d_snaps = h->upload<xg::SnapDev>(h->snaps.data(), h->snaps.size());
 
   // per-axis index flags for the volume kernels' fast path
   for (int a = 0; a < 3; ++a) {
@@ -1774,6 +1823,45 @@ int xfdtd_read_probes(xfdtd_handle *h, double *out, int64_t len) {
     XCHECK(cudaMemcpyAsync(out, h->probe_out, len * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     h->d2h += len * static_cast<long long>(sizeof(double));
     XCHECK(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int xfdtd_snapshot_frames(xfdtd_handle *h, int s, int64_t *count, int64_t *steps, int64_t max) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    if (s < 0 || s >= static_cast<int>(h->snaps.size())) invalid("no such snapshot series");
+    const xg::SnapDev &sv = h->snaps[s];
+    if (count) *count = sv.n_frames;
+    if (steps) {   // step order: the multiples of every, with `last` in its place
+      long long f = 0;
+      for (long long r = 0; r < sv.n_regular && f < max; ++r) {
+        if (sv.extra && r * sv.every > sv.last && (r == 0 || (r - 1) * sv.every < sv.last) && f < max)
+          steps[f++] = sv.last;
+        if (f < max) steps[f++] = r * sv.every;
+      }
+      if (sv.extra && (sv.n_regular - 1) * sv.every < sv.last && f < max) steps[f++] = sv.last;
+    }
+  });
+}
+
+int xfdtd_read_snapshot(xfdtd_handle *h, int s, int64_t frame, double *out, int64_t len) {
+  if (!h || !out) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    if (s < 0 || s >= static_cast<int>(h->snaps.size())) invalid("no such snapshot series");
+    const xg::SnapDev &sv = h->snaps[s];
+    if (frame < 0 || frame >= sv.n_frames) invalid("no such frame");
+    if (len != sv.cells) invalid("length must be the series' box cells");
+    const char *src = static_cast<const char *>(sv.frames) + static_cast<size_t>(frame * sv.cells) * h->esize;
+    if (h->precision == XFDTD_FP64) {
+      XCHECK(cudaMemcpyAsync(out, src, len * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      XCHECK(cudaStreamSynchronize(h->stream));
+    } else {
+      std::vector<float> tmp(static_cast<size_t>(len));
+      XCHECK(cudaMemcpyAsync(tmp.data(), src, len * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+      XCHECK(cudaStreamSynchronize(h->stream));
+      for (int64_t q = 0; q < len; ++q) out[q] = tmp[static_cast<size_t>(q)];
+    }
+    h->d2h += static_cast<long long>(len) * static_cast<long long>(h->esize);
   });
 }
 
@@ -2373,7 +2461,8 @@ int xfdtd_batch_create(xfdtd_handle *const *members, int n, int flags, xfdtd_bat
           invalid("batch members must share device, precision and material-index width");
         if (h->idx_bytes > 2) invalid("batch members must use 1- or 2-byte material indices");
         if (h->host_step != 0) invalid("batch members must not have been stepped");
-        if (h->n_inj || h->n_ind || h->n_probes) invalid("batch members may not have lumped elements or monitors");
+        if (h->n_inj || h->n_ind || h->n_probes || !h->snaps.empty())
+          invalid("batch members may not have lumped elements or monitors");
         if (h->d.nx >= 65535 || h->d.ny >= 2040 || h->d.nz >= 8160) invalid("batch member grid too large for the tile numbering");
         for (int r = 0; r < q; ++r)
           if (members[r] == h) invalid("a handle appears twice in the batch");

@@ -671,6 +671,45 @@ __global__ void k_probes(SparseParams<T> p) {
   p.probe_out[static_cast<long long>(q) * p.total + t] = acc;
 }
 
+// One snapshot series on the device: frames [n_frames][cells] of the
+// field type, in step order.  The steps are the multiples of `every` and,
+// when extra, the step `last` between two of them.
+struct SnapDev {
+  int comp;
+  int extra;
+  long long lo[3], n[3];
+  long long every, last, n_regular, n_frames, cells;
+  void *frames;
+};
+
+template <typename T>
+struct SnapParams {
+  Dims d;
+  const T *F[6];
+  const SnapDev *s;
+  const long long *step;
+};
+
+// MovieMonitor::update over TimeDomainFieldMonitors: blockIdx.y is the
+// series; blocks of a series that records nothing this step return.
+template <typename T>
+__global__ void k_snapshots(SnapParams<T> p) {
+  const SnapDev &s = p.s[blockIdx.y];
+  const long long t = *p.step;
+  long long slot;
+  if (t % s.every == 0) slot = t / s.every + ((s.extra && t > s.last) ? 1 : 0);
+  else if (s.extra && t == s.last) slot = s.last / s.every + 1;
+  else return;
+  if (slot >= s.n_frames) return;
+  T *out = static_cast<T *>(s.frames) + slot * s.cells;
+  const T *f = p.F[s.comp];
+  for (long long q = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; q < s.cells;
+       q += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long k = q % s.n[2], r = q / s.n[2], j = r % s.n[1], i = r / s.n[1];
+    out[q] = f[(s.lo[0] + i) * p.d.si + (s.lo[1] + j) * p.d.sj + s.lo[2] + k];
+  }
+}
+
 __global__ void k_advance(long long *step) { *step += 1; }
 
 // Non-finite scan: sets *flag when any value is NaN or Inf.

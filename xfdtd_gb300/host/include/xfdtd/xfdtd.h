@@ -57,6 +57,10 @@ using PointVector = std::array<double, 3>;
 using SpatialIndex = size_t;
 enum class Orientation { XN, XP, YN, YP, ZN, ZP };
 enum class Axis { X, Y, Z };
+// src/include/electromagnetic_field/electromagnetic_field.h:8,
+// src/include/util/type_define.h:30
+enum class EMComponent { EX, EY, EZ, HX, HY, HZ };
+enum class PlaneType { XY, YZ, ZX };
 
 // GB300 engine precision (extension).
 enum class Precision { FP64, FP32 };
@@ -328,6 +332,7 @@ class NFFFT {
     return {_distance_x, _distance_y, _distance_z};
   }
   const std::string &getOutputDirPath() const { return _output_dir_path; }
+  void setOutputDirPath(const std::string &d) { _output_dir_path = d; }
 
  private:
   SpatialIndex _distance_x, _distance_y, _distance_z;
@@ -477,6 +482,52 @@ class CurrentMonitor : public Monitor {
   Orientation _orientation;
 };
 
+// TimeDomainFieldMonitor (src/include/monitor/field_monitor.h,
+// src/monitor/field_monitor.cpp): component `component` over the cube's
+// grid box (an extent of 0 cells counts as 1), written by outputData as a
+// 3-D .npy of the field after the last step.  The plane type is checked as
+// the reference checks it (field_monitor.cpp:31-82): a monitor thicker than
+// one cell across its plane is an error.
+class TimeDomainFieldMonitor : public Monitor {
+ public:
+  TimeDomainFieldMonitor(std::unique_ptr<Cube> shape, PlaneType plane_type, EMComponent component,
+                         std::string output_dir_path, std::string output_file_name)
+      : Monitor{std::move(shape), std::move(output_dir_path), std::move(output_file_name)},
+        _plane_type{plane_type},
+        _component{component} {}
+  PlaneType getPlaneType() const { return _plane_type; }
+  EMComponent getComponent() const { return _component; }
+
+ private:
+  PlaneType _plane_type;
+  EMComponent _component;
+};
+
+// MovieMonitor (src/include/monitor/movie_monitor.h,
+// src/monitor/movie_monitor.cpp:46-59) over a TimeDomainFieldMonitor: a
+// frame of the field after every step t with t % plot_step == 0 and after
+// step total_time_steps - 1, written by outputData as <dir>/NNNN.npy (the
+// step, four digits zero-padded) in the field monitor's directory.  The
+// reference writes each frame during the run; here the frames stay in
+// device memory until outputData.  Other monitors cannot be wrapped.
+class MovieMonitor : public Monitor {
+ public:
+  MovieMonitor(std::unique_ptr<Monitor> monitor, size_t total_time_steps, size_t plot_step = 30)
+      : Monitor{std::make_unique<Cube>(monitor->cube()), monitor->getOutputPath(), monitor->getOutputFileName()},
+        _monitor{std::move(monitor)},
+        _total_time_steps{total_time_steps},
+        _plot_step{plot_step} {}
+  const Monitor &getMonitor() const { return *_monitor; }
+  size_t getTotalTimeSteps() const { return _total_time_steps; }
+  size_t getPlotStep() const { return _plot_step; }
+  void setPlotStep(size_t plot_step) { _plot_step = plot_step; }
+
+ private:
+  std::shared_ptr<Monitor> _monitor;
+  size_t _total_time_steps;
+  size_t _plot_step;
+};
+
 // -------------------------------------------------------------- grid space
 // Uniform GridSpace (src/grid/grid_space.cpp:14-757, uniform path only).
 class GridSpace {
@@ -532,6 +583,7 @@ class Simulation {
   void addTFSFSource(std::shared_ptr<TFSF> tfsf);
   void addNFFFT(std::shared_ptr<NFFFT> nffft);
   void addMonitor(std::shared_ptr<Monitor> monitor);
+  NFFFT *getNFFFT() const { return _nffft.get(); }
 
   // Simulation::run (simulation_update.cpp:5-40): init, the loop, outputData.
   void run(size_t total_time_steps);
@@ -567,6 +619,16 @@ class Simulation {
   std::vector<std::complex<double>> farField(int which) const;
   std::vector<double> farFieldPower(int which) const;
   std::vector<std::complex<double>> nffftAccumulator(int which) const;
+  // Time series of monitor m (a voltage or current monitor), one value per
+  // step.
+  std::vector<double> monitorValues(size_t m) const;
+  // A field or movie monitor m: its box shape, and the steps of its frames
+  // (a field monitor has one frame, the current field, step -1).
+  std::array<size_t, 3> fieldMonitorShape(size_t m) const;
+  std::array<size_t, 3> fieldMonitorOrigin(size_t m) const;
+  std::vector<long long> fieldMonitorSteps(size_t m) const;
+  // Frame f of field or movie monitor m, [n0][n1][n2].
+  std::vector<double> fieldMonitorFrame(size_t m, size_t f) const;
   // Bistatic RCS in dB over (frequency, theta, phi):
   // 10 log10(4 pi (|E_theta|^2 + |E_phi|^2) / |E_inc(f)|^2).
   std::vector<double> rcsDb() const;
@@ -600,7 +662,15 @@ class Simulation {
   size_t _nx{0}, _ny{0}, _nz{0};
   double _dt{0};
   xfdtd_handle *_engine{nullptr};
-  std::vector<size_t> _monitor_probe;   // probe index of each monitor
+  // per monitor: its probe index (voltage, current) or -1; its snapshot
+  // series (movie) or -1; the component and box of a field monitor
+  struct FieldBox {
+    int comp = -1;
+    size_t lo[3] = {0, 0, 0}, n[3] = {0, 0, 0};
+  };
+  std::vector<long> _monitor_probe, _monitor_series;
+  std::vector<FieldBox> _monitor_box;
+  size_t _n_probes{0};
   void release();
 };
 

@@ -139,9 +139,23 @@ int xfdtd_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, int precis
       const auto &m = sc->monitors[i];
       auto cube = std::make_unique<Cube>(pv(m.point), pv(m.size));
       std::shared_ptr<Monitor> mon;
-      if (m.kind == XFDTD_MONITOR_VOLTAGE) mon = std::make_shared<VoltageMonitor>(std::move(cube), ori(m.orientation), "", "");
-      else if (m.kind == XFDTD_MONITOR_CURRENT) mon = std::make_shared<CurrentMonitor>(std::move(cube), ori(m.orientation), "", "");
-      else throw std::invalid_argument("unknown monitor kind");
+      if (m.kind == XFDTD_MONITOR_VOLTAGE) {
+        mon = std::make_shared<VoltageMonitor>(std::move(cube), ori(m.orientation), "", "");
+      } else if (m.kind == XFDTD_MONITOR_CURRENT) {
+        mon = std::make_shared<CurrentMonitor>(std::move(cube), ori(m.orientation), "", "");
+      } else if (m.kind == XFDTD_MONITOR_FIELD) {
+        if (m.component < 0 || m.component > 5 || m.plane_type < 0 || m.plane_type > 2)
+          throw std::invalid_argument("bad field monitor component or plane type");
+        auto fm = std::make_unique<TimeDomainFieldMonitor>(std::move(cube), static_cast<PlaneType>(m.plane_type),
+                                                           static_cast<EMComponent>(m.component), "", "");
+        if (m.plot_step > 0)
+          mon = std::make_shared<MovieMonitor>(std::move(fm), static_cast<size_t>(m.total_time_steps),
+                                               static_cast<size_t>(m.plot_step));
+        else
+          mon = std::move(fm);
+      } else {
+        throw std::invalid_argument("unknown monitor kind");
+      }
       s->monitors.push_back(mon.get());
       sim->addMonitor(mon);
     }
@@ -219,9 +233,37 @@ int xfdtd_sim_read_monitor(xfdtd_sim *s, int index, double *out, int64_t len) {
     const size_t total = s->sim->getTotalTimeSteps();
     if (index < 0 || index >= static_cast<int>(s->monitors.size())) throw std::invalid_argument("bad monitor index");
     if (static_cast<size_t>(len) != total) throw std::invalid_argument("length must be total_steps");
-    std::vector<double> all(s->monitors.size() * total);
-    checkEngine(xfdtd_read_probes(s->sim->engine(), all.data(), static_cast<int64_t>(all.size())), s->sim->engine());
-    std::memcpy(out, all.data() + index * total, total * sizeof(double));
+    const auto v = s->sim->monitorValues(static_cast<size_t>(index));
+    std::memcpy(out, v.data(), total * sizeof(double));
+  });
+}
+
+int xfdtd_sim_field_monitor(xfdtd_sim *s, int index, int64_t lo[3], int64_t shape[3], int64_t *n_frames,
+                            int64_t *steps, int64_t max) {
+  if (!s || !s->sim) return XFDTD_ERR_STATE;
+  return guarded(s, [&] {
+    if (index < 0 || index >= static_cast<int>(s->monitors.size())) throw std::invalid_argument("bad monitor index");
+    const auto shp = s->sim->fieldMonitorShape(static_cast<size_t>(index));
+    const auto first = s->sim->fieldMonitorOrigin(static_cast<size_t>(index));
+    if (lo)
+      for (int a = 0; a < 3; ++a) lo[a] = static_cast<int64_t>(first[a]);
+    const auto st = s->sim->fieldMonitorSteps(static_cast<size_t>(index));
+    if (shape)
+      for (int a = 0; a < 3; ++a) shape[a] = static_cast<int64_t>(shp[a]);
+    if (n_frames) *n_frames = static_cast<int64_t>(st.size());
+    if (steps)
+      for (size_t f = 0; f < st.size() && static_cast<int64_t>(f) < max; ++f) steps[f] = st[f];
+  });
+}
+
+int xfdtd_sim_read_field_monitor(xfdtd_sim *s, int index, int64_t frame, double *out, int64_t len) {
+  if (!s || !s->sim || !out) return XFDTD_ERR_STATE;
+  return guarded(s, [&] {
+    if (index < 0 || index >= static_cast<int>(s->monitors.size())) throw std::invalid_argument("bad monitor index");
+    if (frame < 0) throw std::invalid_argument("bad frame");
+    const auto v = s->sim->fieldMonitorFrame(static_cast<size_t>(index), static_cast<size_t>(frame));
+    if (static_cast<size_t>(len) != v.size()) throw std::invalid_argument("length must be the monitor's box cells");
+    std::memcpy(out, v.data(), v.size() * sizeof(double));
   });
 }
 
@@ -260,6 +302,20 @@ int xfdtd_sim_incident_dft(xfdtd_sim *s, const double *freqs, int n, double *out
       out[2 * i] = r[i].real();
       out[2 * i + 1] = r[i].imag();
     }
+  });
+}
+
+int xfdtd_sim_set_output(xfdtd_sim *s, int index, const char *dir, const char *file) {
+  if (!s || !s->sim) return XFDTD_ERR_STATE;
+  return guarded(s, [&] {
+    if (index == -1) {
+      if (!s->sim->getNFFFT()) throw std::invalid_argument("no NF-FF in this simulation");
+      s->sim->getNFFFT()->setOutputDirPath(dir ? dir : "");
+      return;
+    }
+    if (index < 0 || index >= static_cast<int>(s->monitors.size())) throw std::invalid_argument("bad monitor index");
+    s->monitors[index]->setOutputDirPath(dir ? dir : "");
+    s->monitors[index]->setOutputFileName(file ? file : "");
   });
 }
 

@@ -1,9 +1,12 @@
 // output.cpp -- .npy outputs of the reference (NffftFd::outputData,
 // src/nffft/nffft_fd.cpp:579-634; VoltageMonitor / CurrentMonitor ::outputData,
-// src/monitor/voltage_monitor.cpp:99-120, current_monitor.cpp:117-140) and
+// src/monitor/voltage_monitor.cpp:99-120, current_monitor.cpp:117-140;
+// TimeDomainFieldMonitor::outputData, src/monitor/field_monitor.cpp:91-122;
+// MovieMonitor::update, src/monitor/movie_monitor.cpp:46-59) and
 // Simulation::checkRun (src/simulation/simulation.cpp:98-113).
 #include <cstdio>
 #include <filesystem>
+#include <iomanip>
 #include <fstream>
 #include <iostream>
 #include <sstream>
@@ -63,12 +66,14 @@ std::vector<double> linspace(double a, double b, size_t n) {
 
 void Simulation::outputData() {
   if (!_engine) throw std::runtime_error("Simulation::init has not been called");
-  // monitors: stack(time, value) -> (2, N)
-  if (!_monitors.empty()) {
-    std::vector<double> all(_monitors.size() * _total);
+  // voltage and current monitors: stack(time, value) -> (2, N)
+  if (_n_probes) {
+    std::vector<double> all(_n_probes * _total);
     checkEngine(xfdtd_read_probes(_engine, all.data(), static_cast<int64_t>(all.size())), _engine);
     for (size_t m = 0; m < _monitors.size(); ++m) {
-      std::vector<double> v(all.begin() + m * _total, all.begin() + (m + 1) * _total);
+      if (_monitor_probe[m] < 0) continue;
+      const size_t p = static_cast<size_t>(_monitor_probe[m]);
+      std::vector<double> v(all.begin() + p * _total, all.begin() + (p + 1) * _total);
       _monitors[m]->setValue(v);
       const std::string &dir = _monitors[m]->getOutputPath();
       if (dir.empty()) continue;
@@ -79,6 +84,29 @@ void Simulation::outputData() {
       std::copy(t.begin(), t.end(), st.begin());
       std::copy(v.begin(), v.end(), st.begin() + _total);
       writeNpy(std::filesystem::path(dir) / _monitors[m]->getOutputFileName(), st.data(), 8, "<f8", {2, _total});
+    }
+  }
+  // field monitors: the component over the box after the last step; movie
+  // monitors: one NNNN.npy per recorded frame
+  for (size_t m = 0; m < _monitors.size(); ++m) {
+    if (_monitor_box[m].comp < 0) continue;
+    const std::string &dir = _monitors[m]->getOutputPath();
+    if (dir.empty() || !ensureDir(dir)) continue;
+    const auto shp = fieldMonitorShape(m);
+    const std::vector<size_t> shape{shp[0], shp[1], shp[2]};
+    if (_monitor_series[m] < 0) {
+      const auto v = fieldMonitorFrame(m, 0);
+      writeNpy(std::filesystem::path(dir) / _monitors[m]->getOutputFileName(), v.data(), 8, "<f8", shape);
+      continue;
+    }
+    const auto steps = fieldMonitorSteps(m);
+    const long long done = static_cast<long long>(getCurrentTimeStep());
+    for (size_t f = 0; f < steps.size(); ++f) {
+      if (steps[f] >= done) continue;   // not run yet
+      std::ostringstream name;
+      name << std::setw(4) << std::setfill('0') << steps[f] << ".npy";
+      const auto v = fieldMonitorFrame(m, f);
+      writeNpy(std::filesystem::path(dir) / name.str(), v.data(), 8, "<f8", shape);
     }
   }
   const NffftFd *nfd = dynamic_cast<const NffftFd *>(_nffft.get());

@@ -660,11 +660,59 @@ void Simulation::init(size_t total_time_steps) {
     np.phi = nfd->getPhi().data();
   }
 
-  // ---- monitors -> probe terms -----------------------------------------
+  // ---- monitors -> probe terms and snapshot series ----------------------
   std::vector<xfdtd_probe_term> terms;
+  std::vector<xfdtd_snapshot_desc> series;
   _monitor_probe.clear();
+  _monitor_series.clear();
+  _monitor_box.clear();
   int probe = 0;
+  const size_t comp_shape[6][3] = {{nx, ny + 1, nz + 1}, {nx + 1, ny, nz + 1}, {nx + 1, ny + 1, nz},
+                                   {nx + 1, ny, nz},     {nx, ny + 1, nz},     {nx, ny, nz + 1}};
+  // the component view of a field monitor (field_monitor.cpp:31-82,
+  // 91-122): the grid box, 0 cells counting as 1, clipped to the array
+  auto field_box = [&](const TimeDomainFieldMonitor &fm) {
+    auto g = gs.gridBox(fm.cube());
+    const size_t num[3] = {g[3] - g[0], g[4] - g[1], g[5] - g[2]};
+    const int normal = fm.getPlaneType() == PlaneType::XY ? 2 : fm.getPlaneType() == PlaneType::YZ ? 0 : 1;
+    if (num[normal] > 1) throw std::runtime_error("Error: invalid grid box");
+    FieldBox b;
+    b.comp = static_cast<int>(fm.getComponent());
+    for (int a = 0; a < 3; ++a) {
+      const size_t lim = comp_shape[b.comp][a];
+      b.lo[a] = g[a];
+      if (b.lo[a] >= lim) throw std::out_of_range("field monitor outside its component");
+      b.n[a] = std::min(std::max<size_t>(num[a], 1), lim - b.lo[a]);
+    }
+    return b;
+  };
   for (auto &m : _monitors) {
+    _monitor_series.push_back(-1);
+    _monitor_box.emplace_back();
+    if (auto fm = dynamic_cast<const TimeDomainFieldMonitor *>(m.get())) {
+      _monitor_box.back() = field_box(*fm);
+      _monitor_probe.push_back(-1);
+      continue;
+    }
+    if (auto mm = dynamic_cast<const MovieMonitor *>(m.get())) {   // movie_monitor.cpp:46-59
+      auto fm = dynamic_cast<const TimeDomainFieldMonitor *>(&mm->getMonitor());
+      if (!fm) throw std::runtime_error("a MovieMonitor runs on the GPU engine over a TimeDomainFieldMonitor only");
+      if (mm->getPlotStep() == 0) throw std::invalid_argument("MovieMonitor plot step must be at least 1");
+      const FieldBox b = field_box(*fm);
+      xfdtd_snapshot_desc sd{};
+      sd.comp = b.comp;
+      for (int a = 0; a < 3; ++a) {
+        sd.lo[a] = static_cast<int64_t>(b.lo[a]);
+        sd.n[a] = static_cast<int64_t>(b.n[a]);
+      }
+      sd.every = static_cast<int64_t>(mm->getPlotStep());
+      sd.last = static_cast<int64_t>(mm->getTotalTimeSteps()) - 1;
+      _monitor_box.back() = b;
+      _monitor_series.back() = static_cast<long>(series.size());
+      _monitor_probe.push_back(-1);
+      series.push_back(sd);
+      continue;
+    }
     auto g = gs.gridBox(m->cube());
     const size_t is = g[0], js = g[1], ks = g[2], ie = g[3], je = g[4], ke = g[5];
     auto term = [&](int comp, size_t i, size_t j, size_t k, double w) {
@@ -702,11 +750,12 @@ void Simulation::init(size_t total_time_steps) {
         for (size_t j = js; j <= je; ++j) { term(4, ie, j, ks, pos * d[1]); term(4, is - 1, j, ks, -pos * d[1]); }
       }
     } else {
-      throw std::runtime_error("only voltage and current monitors run on the GPU engine");
+      throw std::runtime_error("unknown monitor type");
     }
     _monitor_probe.push_back(probe);
     ++probe;
   }
+  _n_probes = static_cast<size_t>(probe);
 
   plan.n_waveforms = n_waveforms;
   plan.waveforms = waveforms.data();
@@ -717,6 +766,8 @@ void Simulation::init(size_t total_time_steps) {
   plan.n_probes = probe;
   plan.n_probe_terms = static_cast<int32_t>(terms.size());
   plan.probe_terms = terms.data();
+  plan.n_snapshots = static_cast<int32_t>(series.size());
+  plan.snapshots = series.data();
 
   xfdtd_handle *h = nullptr;
   const int rc = xfdtd_create(&plan, &h);
@@ -747,6 +798,60 @@ std::vector<double> Simulation::readField(int comp) const {
   std::vector<double> v(s[comp][0] * s[comp][1] * s[comp][2]);
   checkEngine(xfdtd_read_field(_engine, comp, v.data(), static_cast<int64_t>(v.size())), _engine);
   return v;
+}
+
+std::vector<double> Simulation::monitorValues(size_t m) const {
+  if (!_engine) throw std::runtime_error("Simulation::init has not been called");
+  if (m >= _monitors.size() || _monitor_probe[m] < 0) throw std::invalid_argument("not a voltage or current monitor");
+  std::vector<double> all(_n_probes * _total);
+  checkEngine(xfdtd_read_probes(_engine, all.data(), static_cast<int64_t>(all.size())), _engine);
+  const size_t p = static_cast<size_t>(_monitor_probe[m]);
+  return std::vector<double>(all.begin() + p * _total, all.begin() + (p + 1) * _total);
+}
+
+std::array<size_t, 3> Simulation::fieldMonitorShape(size_t m) const {
+  if (!_engine) throw std::runtime_error("Simulation::init has not been called");
+  if (m >= _monitors.size() || _monitor_box[m].comp < 0) throw std::invalid_argument("not a field or movie monitor");
+  const FieldBox &b = _monitor_box[m];
+  return {b.n[0], b.n[1], b.n[2]};
+}
+
+std::array<size_t, 3> Simulation::fieldMonitorOrigin(size_t m) const {
+  fieldMonitorShape(m);
+  const FieldBox &b = _monitor_box[m];
+  return {b.lo[0], b.lo[1], b.lo[2]};
+}
+
+std::vector<long long> Simulation::fieldMonitorSteps(size_t m) const {
+  fieldMonitorShape(m);
+  if (_monitor_series[m] < 0) return {-1};
+  int64_t count = 0;
+  const int s = static_cast<int>(_monitor_series[m]);
+  checkEngine(xfdtd_snapshot_frames(_engine, s, &count, nullptr, 0), _engine);
+  std::vector<int64_t> st(static_cast<size_t>(count));
+  checkEngine(xfdtd_snapshot_frames(_engine, s, &count, st.data(), count), _engine);
+  return std::vector<long long>(st.begin(), st.end());
+}
+
+std::vector<double> Simulation::fieldMonitorFrame(size_t m, size_t f) const {
+  const auto shp = fieldMonitorShape(m);
+  const FieldBox &b = _monitor_box[m];
+  std::vector<double> out(shp[0] * shp[1] * shp[2]);
+  if (_monitor_series[m] >= 0) {
+    checkEngine(xfdtd_read_snapshot(_engine, static_cast<int>(_monitor_series[m]), static_cast<int64_t>(f), out.data(),
+                                    static_cast<int64_t>(out.size())),
+                _engine);
+    return out;
+  }
+  if (f != 0) throw std::invalid_argument("a field monitor has one frame");
+  const auto all = readField(b.comp);
+  const size_t s1 = b.comp == 0 || b.comp == 2 || b.comp == 4 ? _ny + 1 : _ny;
+  const size_t s2 = b.comp <= 1 || b.comp == 5 ? _nz + 1 : _nz;
+  size_t q = 0;
+  for (size_t i = 0; i < b.n[0]; ++i)
+    for (size_t j = 0; j < b.n[1]; ++j)
+      for (size_t k = 0; k < b.n[2]; ++k) out[q++] = all[((b.lo[0] + i) * s1 + b.lo[1] + j) * s2 + b.lo[2] + k];
+  return out;
 }
 
 void Simulation::writeField(int comp, const std::vector<double> &values) {

@@ -31,7 +31,7 @@ SHAPE_CUBE, SHAPE_SPHERE, SHAPE_CYLINDER = range(3)
 OBJECT_PLAIN, OBJECT_THIN_WIRE = range(2)
 WAVE_GAUSSIAN, WAVE_COS_GAUSSIAN, WAVE_SINUSOIDAL, WAVE_CUSTOM = range(4)
 LUMPED_CURRENT_SOURCE, LUMPED_VOLTAGE_SOURCE, LUMPED_RESISTOR, LUMPED_CAPACITOR, LUMPED_INDUCTOR = range(5)
-MONITOR_VOLTAGE, MONITOR_CURRENT = range(2)
+MONITOR_VOLTAGE, MONITOR_CURRENT, MONITOR_FIELD = range(3)
 
 # src/include/util/constant.h:10-29
 PI = math.pi
@@ -92,7 +92,8 @@ class LumpedDesc(C.Structure):
 
 class MonitorDesc(C.Structure):
     _fields_ = [("kind", C.c_int32), ("orientation", C.c_int32), ("point", C.c_double * 3),
-                ("size", C.c_double * 3)]
+                ("size", C.c_double * 3), ("component", C.c_int32), ("plane_type", C.c_int32),
+                ("plot_step", C.c_int64), ("total_time_steps", C.c_int64)]
 
 
 class SceneDesc(C.Structure):
@@ -421,12 +422,18 @@ class _Monitor:
     output_dir_path: str = ""
     output_file_name: str = ""
     kind: int = -1
+    component: int = 0       # field monitors: EMComponent
+    plane_type: int = 0      #                 PlaneType
+    plot_step: int = 0       # movie monitors: frame interval (0: not a movie)
+    total_time_steps: int = 0
 
     def desc(self) -> MonitorDesc:
         d = MonitorDesc()
         d.kind, d.orientation = self.kind, int(self.orientation)
         d.point[:] = list(map(float, self.cube.point))
         d.size[:] = list(map(float, self.cube.size))
+        d.component, d.plane_type = int(self.component), int(self.plane_type)
+        d.plot_step, d.total_time_steps = int(self.plot_step), int(self.total_time_steps)
         return d
 
 
@@ -438,6 +445,34 @@ def VoltageMonitor(cube: Cube, orientation: int, output_dir_path: str = "", outp
 def CurrentMonitor(cube: Cube, orientation: int, output_dir_path: str = "", output_file_name: str = "") -> _Monitor:
     """CurrentMonitor(cube, orientation, dir, file), src/monitor/current_monitor.cpp:9-16."""
     return _Monitor(cube, orientation, output_dir_path, output_file_name, MONITOR_CURRENT)
+
+
+# EMComponent (src/include/electromagnetic_field/electromagnetic_field.h:8)
+EX, EY, EZ, HX, HY, HZ = range(6)
+# PlaneType (src/include/util/type_define.h:30)
+PLANE_XY, PLANE_YZ, PLANE_ZX = range(3)
+
+
+def TimeDomainFieldMonitor(cube: Cube, plane_type: int, component: int, output_dir_path: str = "",
+                           output_file_name: str = "") -> _Monitor:
+    """TimeDomainFieldMonitor(cube, plane_type, component, dir, file),
+    src/monitor/field_monitor.cpp:15-24: the component over the cube's grid
+    box after the last step (a 3-D .npy at output)."""
+    return _Monitor(cube, 0, output_dir_path, output_file_name, MONITOR_FIELD, int(component), int(plane_type))
+
+
+def MovieMonitor(monitor: _Monitor, total_time_steps: int, plot_step: int = 30) -> _Monitor:
+    """MovieMonitor(monitor, total_time_steps, plot_step=30),
+    src/monitor/movie_monitor.cpp:6-10, over a TimeDomainFieldMonitor: a
+    frame after every step t with t % plot_step == 0 and after step
+    total_time_steps - 1 (NNNN.npy files in the field monitor's directory
+    at output)."""
+    if monitor.kind != MONITOR_FIELD:
+        raise ValueError("a MovieMonitor runs over a TimeDomainFieldMonitor")
+    if plot_step < 1:
+        raise ValueError("plot_step must be at least 1")
+    return _Monitor(monitor.cube, 0, monitor.output_dir_path, monitor.output_file_name, MONITOR_FIELD,
+                    monitor.component, monitor.plane_type, int(plot_step), int(total_time_steps))
 
 
 # ----------------------------------------------------------------- scene ---
