@@ -163,6 +163,17 @@ typedef struct xfdtd_monitor_desc {
   int64_t total_time_steps;
 } xfdtd_monitor_desc;
 
+/* Port(index, impedance, is_activated_source, voltage, current)
+ * (src/include/network/port.h): its voltage and current monitors are
+ * indices into the scene's monitor list. */
+typedef struct xfdtd_port_desc {
+  int32_t index;
+  int32_t is_activated_source;
+  double impedance_re, impedance_im;
+  int32_t voltage_monitor;
+  int32_t current_monitor;
+} xfdtd_port_desc;
+
 typedef struct xfdtd_scene_desc {
   double cell_size;     /* dx = dy = dz                                   */
   float cfl;            /* float, as in Simulation(..., float cfl)        */
@@ -185,6 +196,12 @@ typedef struct xfdtd_scene_desc {
   int64_t voxel_shape[3];
   int32_t voxel_index_bytes;    /* 2 (or 0, meaning 2) or 4                      */
   int32_t reserved3;
+  /* Optional Network(ports, frequencies, output_path)
+   * (src/include/network/network.h): n_ports = 0 for none.              */
+  int32_t n_ports;
+  int32_t n_network_freqs;
+  const xfdtd_port_desc *ports;
+  const double *network_freqs;
 } xfdtd_scene_desc;
 
 #ifdef __cplusplus

@@ -56,13 +56,21 @@ int xfdtd_sim_read_field_monitor(xfdtd_sim *s, int index, int64_t frame, double 
 int xfdtd_sim_read_nffft(xfdtd_sim *s, int which, double *out, int64_t len);
 int xfdtd_sim_far_field(xfdtd_sim *s, int which, double *out, int64_t len);
 int xfdtd_sim_incident_dft(xfdtd_sim *s, const double *freqs, int n, double *out);
-/* Output directory (and file name) of monitor `index`, or with index -1
- * the NF-FF's output directory: the constructors' output_dir_path /
- * output_file_name arguments, which the scene description does not
- * carry.  An empty directory writes nothing. */
+/* Output directory (and file name) of monitor `index`; with index -1 the
+ * NF-FF's output directory, with -2 the network's output path: the
+ * constructors' output_dir_path / output_file_name / output_path
+ * arguments, which the scene description does not carry.  An empty
+ * directory writes nothing. */
 int xfdtd_sim_set_output(xfdtd_sim *s, int index, const char *dir, const char *file);
+/* The network's S-parameters (Network::outputData's arithmetic,
+ * src/network/network.cpp:40-52) from the monitor series recorded so far:
+ * their keys (10 * j + i for port indices j and activated i, ascending;
+ * keys[q] for q < min(max, count)) and the number of frequencies. */
+int xfdtd_sim_s_parameters(xfdtd_sim *s, int32_t *keys, int64_t max, int64_t *count, int64_t *n_freq);
+/* S-parameter `key` over the network's frequencies, (re, im) pairs. */
+int xfdtd_sim_read_s_parameter(xfdtd_sim *s, int key, double *out, int64_t len);
 /* Writes the reference's .npy outputs (NF-FF into its output directory,
- * monitors into theirs). */
+ * monitors and the network into theirs). */
 int xfdtd_sim_output(xfdtd_sim *s);
 /* The engine handle behind the simulation (for timing and profiling). */
 xfdtd_handle *xfdtd_sim_engine(xfdtd_sim *s);

@@ -137,6 +137,26 @@ def field_monitors(steps=40):
     return sc, steps
 
 
+def two_port(steps=160):
+    """A boxed scene with a two-port network (Port, Network;
+    src/network/port.cpp, network.cpp): port 1 at the soft current source,
+    port 2 across the box, each a voltage monitor and a current monitor
+    around it; S-parameters at four frequencies."""
+    dl = 2e-3
+    dims = (16, 14, 12)
+    sc, _ = _boxed(dims, dl, _six(4), steps)
+    c = [max(1, int(v * 0.45)) for v in dims]   # the source cell of _boxed
+    v1 = S.VoltageMonitor(S.Cube([q * dl for q in c], [dl, dl, dl]), S.ZP)
+    c1 = S.CurrentMonitor(S.Cube([q * dl for q in c], [dl, dl, dl]), S.ZP)
+    far = [c[0] + 5, c[1] - 3, c[2]]
+    v2 = S.VoltageMonitor(S.Cube([q * dl for q in far], [dl, dl, 2 * dl]), S.ZP)
+    c2 = S.CurrentMonitor(S.Cube([q * dl for q in far], [dl, dl, dl]), S.ZP)
+    sc.monitors = [v1, sc.monitors[0], c1, v2, c2]
+    ports = [S.Port(1, 50.0, True, v1, c1), S.Port(2, 100.0 + 5.0j, False, v2, c2)]
+    sc.network = S.Network(ports, [1e9, 3e9, 6e9, 9e9])
+    return sc, steps
+
+
 def _six(t):
     return [S.PML(o, t) for o in (S.XN, S.XP, S.YN, S.YP, S.ZN, S.ZP)]
 

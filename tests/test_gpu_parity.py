@@ -419,3 +419,57 @@ def test_field_and_movie_monitors(graph, tmp_path):
             for f, t in enumerate(steps):
                 assert np.array_equal(np.load(tmp_path / "movie_ez" / ("%04d.npy" % t)), g.read_field_monitor(1, f))
             assert np.array_equal(np.load(tmp_path / "hy" / "hy.npy"), g.read_field_monitor(2, 0))
+
+
+def _s_parameters_restated(sc, series, dt):
+    """Network::outputData's arithmetic (src/network/network.cpp:40-52,
+    port.cpp:25-34, util/dft.h:11-27) in numpy, from monitor series."""
+    f = np.asarray(sc.network.frequencies, dtype=np.float64)
+
+    def dft(x):
+        t = np.arange(len(x)) * dt
+        return np.array([np.sum(x * np.exp(-2j * np.pi * fq * t)) * dt for fq in f])
+
+    ab = []
+    for p in sc.network.ports:
+        z = complex(p.impedance)
+        k = np.sqrt(z.real)
+        v = dft(series(sc.monitors.index(p.voltage)))
+        i = dft(series(sc.monitors.index(p.current)))
+        ab.append((0.5 * (v + z * i) / k, 0.5 * (v - np.conj(z) * i) / k))
+    out = {}
+    for i, pi in enumerate(sc.network.ports):
+        if not pi.is_activated_source:
+            continue
+        for j, pj in enumerate(sc.network.ports):
+            out[pj.index * 10 + pi.index] = ab[j][1] / ab[i][0]
+    return out
+
+
+def test_network_s_parameters(tmp_path):
+    """Port / Network S-parameters from the engine's monitor series (FP64)
+    against the same arithmetic restated in numpy over the oracle's series:
+    within 1e-10; outputData writes s<key>.npy as stack(frequencies, S)."""
+    sc, st = scenes.two_port(steps=160)
+    sc.network.output_path = str(tmp_path / "net")
+    o = O.OracleSim(sc, st)
+    o.step(st)
+    g = X.Simulation(sc, st, precision="fp64")
+    g.step(st)
+    got = g.s_parameters()
+    want = _s_parameters_restated(sc, o.read_monitor, g.dt)
+    assert sorted(got) == sorted(want) == [11, 21]
+    for key in want:
+        assert np.abs(want[key]).max() > 0
+        e = np.abs(got[key] - want[key]).max() / np.abs(want[key]).max()
+        assert e <= TOL, (key, e)
+    # the engine's own series through the restatement agree bit for bit in
+    # the inputs, so the C++ arithmetic is checked on its own too
+    mine = _s_parameters_restated(sc, g.read_monitor, g.dt)
+    for key in want:
+        assert np.abs(got[key] - mine[key]).max() <= 1e-12 * np.abs(mine[key]).max()
+    g.output()
+    for key in want:
+        a = np.load(tmp_path / "net" / ("s%d.npy" % key))
+        assert a.shape == (2, 4) and a.dtype == np.complex128
+        assert np.array_equal(a[0].real, np.asarray(sc.network.frequencies)) and np.array_equal(a[1], got[key])

@@ -71,6 +71,8 @@ def libs():
         ho.xfdtd_sim_incident_dft.argtypes = [C.c_void_p, dp, C.c_int, dp]
         ho.xfdtd_sim_output.argtypes = [C.c_void_p]
         ho.xfdtd_sim_set_output.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_char_p]
+        ho.xfdtd_sim_s_parameters.argtypes = [C.c_void_p, P(C.c_int32), C.c_int64, P(C.c_int64), P(C.c_int64)]
+        ho.xfdtd_sim_read_s_parameter.argtypes = [C.c_void_p, C.c_int, dp, C.c_int64]
         ho.xfdtd_sim_engine.argtypes = [C.c_void_p]
         ho.xfdtd_sim_engine.restype = C.c_void_p
         ho.xfdtd_sim_last_error.argtypes = [C.c_void_p]
@@ -160,6 +162,8 @@ class Simulation:
         # output directories the scene description does not carry
         if sc.nffft is not None and sc.nffft.output_dir_path:
             self._check(ho.xfdtd_sim_set_output(self.h, -1, sc.nffft.output_dir_path.encode(), None))
+        if sc.network is not None and sc.network.ports and sc.network.output_path:
+            self._check(ho.xfdtd_sim_set_output(self.h, -2, sc.network.output_path.encode(), None))
         for q, m in enumerate(sc.monitors):
             if m.output_dir_path:
                 self._check(ho.xfdtd_sim_set_output(self.h, q, m.output_dir_path.encode(),
@@ -214,6 +218,21 @@ class Simulation:
     def read_monitor(self, index: int) -> np.ndarray:
         out = np.empty(self.total_steps, dtype=np.float64)
         self._check(libs()[1].xfdtd_sim_read_monitor(self.h, index, _dp(out), out.size))
+        return out
+
+    def s_parameters(self) -> dict:
+        """The network's S-parameters {10 j + i: complex array over its
+        frequencies} from the monitor series recorded so far
+        (src/network/network.cpp:40-52)."""
+        n, nf = C.c_int64(), C.c_int64()
+        self._check(libs()[1].xfdtd_sim_s_parameters(self.h, None, 0, C.byref(n), C.byref(nf)))
+        keys = (C.c_int32 * max(1, n.value))()
+        self._check(libs()[1].xfdtd_sim_s_parameters(self.h, keys, n.value, C.byref(n), C.byref(nf)))
+        out = {}
+        for q in range(n.value):
+            buf = np.empty(2 * nf.value, dtype=np.float64)
+            self._check(libs()[1].xfdtd_sim_read_s_parameter(self.h, int(keys[q]), _dp(buf), buf.size))
+            out[int(keys[q])] = buf[0::2] + 1j * buf[1::2]
         return out
 
     def field_monitor_frames(self, index: int):

@@ -31,6 +31,7 @@
 #include <cstdint>
 #include <functional>
 #include <limits>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -528,6 +529,64 @@ class MovieMonitor : public Monitor {
   size_t _plot_step;
 };
 
+// ----------------------------------------------------------------- network
+// dt * sum_j x[j] exp(-i 2 pi f j dt) for each f (src/include/util/dft.h:11-27).
+std::vector<std::complex<double>> dft(const std::vector<double> &x, double dt, const std::vector<double> &frequencies);
+
+// Port (src/include/network/port.h, src/network/port.cpp): the incident and
+// reflected waves a = (V + Z I) / (2 sqrt(Re Z)), b = (V - conj(Z) I) /
+// (2 sqrt(Re Z)) from the DFTs of its monitors' series.
+class Port {
+ public:
+  Port(int index, std::complex<double> impedance, bool is_activated_source, std::shared_ptr<VoltageMonitor> voltage,
+       std::shared_ptr<CurrentMonitor> current)
+      : _index{index},
+        _impedance{impedance},
+        _is_activated_source{is_activated_source},
+        _voltage{std::move(voltage)},
+        _current{std::move(current)} {}
+  void calculateSParameter(const std::vector<double> &frequencies, double dt);
+  int getPortIndex() const { return _index; }
+  bool isActivatedSource() const { return _is_activated_source; }
+  std::complex<double> getImpedance() const { return _impedance; }
+  const std::shared_ptr<VoltageMonitor> &getVoltageMonitor() const { return _voltage; }
+  const std::shared_ptr<CurrentMonitor> &getCurrentMonitor() const { return _current; }
+  const std::vector<std::complex<double>> &getA() const { return _a; }
+  const std::vector<std::complex<double>> &getB() const { return _b; }
+
+ private:
+  int _index;
+  std::complex<double> _impedance;
+  bool _is_activated_source;
+  std::shared_ptr<VoltageMonitor> _voltage;
+  std::shared_ptr<CurrentMonitor> _current;
+  std::vector<std::complex<double>> _a, _b;
+};
+
+// Network (src/include/network/network.h, src/network/network.cpp): for
+// every activated port i and every port j, S[10 j + i] = b_j / a_i, by the
+// ports' indices; outputData writes each as s<key>.npy, the frequencies
+// stacked over the values (a complex (2, n_freq) array).
+class Network {
+ public:
+  Network(std::vector<std::unique_ptr<Port>> ports, std::vector<double> frequencies, std::string output_path)
+      : _ports{std::move(ports)}, _frequencies{std::move(frequencies)}, _output_path{std::move(output_path)} {}
+  // Computes the S-parameters from the ports' monitor series (which
+  // Simulation::outputData fills).
+  void calculate(double dt);
+  const std::vector<std::unique_ptr<Port>> &getPorts() const { return _ports; }
+  const std::vector<double> &getFrequencies() const { return _frequencies; }
+  const std::string &getOutputPath() const { return _output_path; }
+  void setOutputPath(const std::string &p) { _output_path = p; }
+  const std::map<int, std::vector<std::complex<double>>> &getSParameters() const { return _s_parameters; }
+
+ private:
+  std::vector<std::unique_ptr<Port>> _ports;
+  std::vector<double> _frequencies;
+  std::string _output_path;
+  std::map<int, std::vector<std::complex<double>>> _s_parameters;
+};
+
 // -------------------------------------------------------------- grid space
 // Uniform GridSpace (src/grid/grid_space.cpp:14-757, uniform path only).
 class GridSpace {
@@ -573,6 +632,11 @@ class Simulation {
              float cfl = DEFAULT_CFL);
   Simulation(double cell_size, std::vector<std::shared_ptr<Object>> objects,
              std::vector<std::shared_ptr<Monitor>> monitors = {}, float cfl = DEFAULT_CFL);
+  // simulation.h:46-49 (the network's ports use monitors of the list)
+  Simulation(double cell_size, std::vector<std::shared_ptr<Object>> objects,
+             std::vector<std::shared_ptr<LumpedElement>> lumped_elements,
+             std::vector<std::shared_ptr<Boundary>> boundaries, std::vector<std::shared_ptr<Monitor>> monitors,
+             std::unique_ptr<Network> network, float cfl = DEFAULT_CFL);
   ~Simulation();
   Simulation(const Simulation &) = delete;
   Simulation &operator=(const Simulation &) = delete;
@@ -584,6 +648,10 @@ class Simulation {
   void addNFFFT(std::shared_ptr<NFFFT> nffft);
   void addMonitor(std::shared_ptr<Monitor> monitor);
   NFFFT *getNFFFT() const { return _nffft.get(); }
+  void addNetwork(std::shared_ptr<Network> network) { _network = std::move(network); }
+  Network *getNetwork() const { return _network.get(); }
+  // The network's S-parameters from the monitor series recorded so far.
+  const std::map<int, std::vector<std::complex<double>>> &sParameters();
 
   // Simulation::run (simulation_update.cpp:5-40): init, the loop, outputData.
   void run(size_t total_time_steps);
@@ -648,6 +716,7 @@ class Simulation {
   std::vector<std::shared_ptr<Monitor>> _monitors;
   std::shared_ptr<TFSF> _tfsf;
   std::shared_ptr<NFFFT> _nffft;
+  std::shared_ptr<Network> _network;
   std::vector<Material> _voxel_materials;
   std::vector<uint32_t> _voxel_index;
   std::array<size_t, 3> _voxel_shape{0, 0, 0};

@@ -8,6 +8,7 @@
 struct xfdtd_sim {
   std::unique_ptr<xfdtd::Simulation> sim;
   std::vector<xfdtd::Monitor *> monitors;
+  std::vector<std::shared_ptr<xfdtd::Monitor>> monitor_ptrs;
   std::shared_ptr<xfdtd::TFSF> tfsf;
   std::vector<double> nffft_freqs;
   int64_t nffft_box[3] = {0, 0, 0};
@@ -157,7 +158,26 @@ int xfdtd_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, int precis
         throw std::invalid_argument("unknown monitor kind");
       }
       s->monitors.push_back(mon.get());
+      s->monitor_ptrs.push_back(mon);
       sim->addMonitor(mon);
+    }
+    if (sc->n_ports > 0) {   // Network(ports, frequencies, output_path)
+      if (!sc->ports || (sc->n_network_freqs > 0 && !sc->network_freqs)) throw std::invalid_argument("bad network");
+      std::vector<std::unique_ptr<Port>> ports;
+      for (int q = 0; q < sc->n_ports; ++q) {
+        const auto &p = sc->ports[q];
+        auto mon = [&](int m) {
+          if (m < 0 || m >= static_cast<int>(s->monitor_ptrs.size())) throw std::invalid_argument("bad port monitor");
+          return s->monitor_ptrs[m];
+        };
+        auto v = std::dynamic_pointer_cast<VoltageMonitor>(mon(p.voltage_monitor));
+        auto c = std::dynamic_pointer_cast<CurrentMonitor>(mon(p.current_monitor));
+        if (!v || !c) throw std::invalid_argument("a port takes a voltage monitor and a current monitor");
+        ports.push_back(std::make_unique<Port>(p.index, std::complex<double>{p.impedance_re, p.impedance_im},
+                                               p.is_activated_source != 0, v, c));
+      }
+      std::vector<double> fr(sc->network_freqs, sc->network_freqs + std::max(0, sc->n_network_freqs));
+      sim->addNetwork(std::make_shared<Network>(std::move(ports), std::move(fr), ""));
     }
     if (sc->voxel_index) {
       std::vector<Material> mats;
@@ -305,9 +325,39 @@ int xfdtd_sim_incident_dft(xfdtd_sim *s, const double *freqs, int n, double *out
   });
 }
 
+int xfdtd_sim_s_parameters(xfdtd_sim *s, int32_t *keys, int64_t max, int64_t *count, int64_t *n_freq) {
+  if (!s || !s->sim) return XFDTD_ERR_STATE;
+  return guarded(s, [&] {
+    const auto &sp = s->sim->sParameters();
+    if (count) *count = static_cast<int64_t>(sp.size());
+    if (n_freq) *n_freq = static_cast<int64_t>(s->sim->getNetwork()->getFrequencies().size());
+    int64_t q = 0;
+    for (const auto &e : sp) {
+      if (keys && q < max) keys[q] = e.first;
+      ++q;
+    }
+  });
+}
+
+int xfdtd_sim_read_s_parameter(xfdtd_sim *s, int key, double *out, int64_t len) {
+  if (!s || !s->sim || !out) return XFDTD_ERR_STATE;
+  return guarded(s, [&] {
+    const auto &sp = s->sim->sParameters();
+    auto it = sp.find(key);
+    if (it == sp.end()) throw std::invalid_argument("no such S-parameter");
+    if (static_cast<size_t>(len) != 2 * it->second.size()) throw std::invalid_argument("length must be 2 * n_freq");
+    std::memcpy(out, it->second.data(), it->second.size() * sizeof(std::complex<double>));
+  });
+}
+
 int xfdtd_sim_set_output(xfdtd_sim *s, int index, const char *dir, const char *file) {
   if (!s || !s->sim) return XFDTD_ERR_STATE;
   return guarded(s, [&] {
+    if (index == -2) {
+      if (!s->sim->getNetwork()) throw std::invalid_argument("no network in this simulation");
+      s->sim->getNetwork()->setOutputPath(dir ? dir : "");
+      return;
+    }
     if (index == -1) {
       if (!s->sim->getNFFFT()) throw std::invalid_argument("no NF-FF in this simulation");
       s->sim->getNFFFT()->setOutputDirPath(dir ? dir : "");

@@ -2,7 +2,8 @@
 // src/nffft/nffft_fd.cpp:579-634; VoltageMonitor / CurrentMonitor ::outputData,
 // src/monitor/voltage_monitor.cpp:99-120, current_monitor.cpp:117-140;
 // TimeDomainFieldMonitor::outputData, src/monitor/field_monitor.cpp:91-122;
-// MovieMonitor::update, src/monitor/movie_monitor.cpp:46-59) and
+// MovieMonitor::update, src/monitor/movie_monitor.cpp:46-59;
+// Network::outputData, src/network/network.cpp:27-60) and
 // Simulation::checkRun (src/simulation/simulation.cpp:98-113).
 #include <cstdio>
 #include <filesystem>
@@ -107,6 +108,20 @@ void Simulation::outputData() {
       name << std::setw(4) << std::setfill('0') << steps[f] << ".npy";
       const auto v = fieldMonitorFrame(m, f);
       writeNpy(std::filesystem::path(dir) / name.str(), v.data(), 8, "<f8", shape);
+    }
+  }
+  // network: s<key>.npy = stack(frequencies, S) as complex (2, n_freq)
+  if (_network && !_network->getOutputPath().empty() && ensureDir(_network->getOutputPath())) {
+    const auto &sp = sParameters();
+    const auto &fr = _network->getFrequencies();
+    for (const auto &e : sp) {
+      std::vector<std::complex<double>> st(2 * fr.size());
+      for (size_t q = 0; q < fr.size(); ++q) {
+        st[q] = {fr[q], 0.0};
+        st[fr.size() + q] = e.second[q];
+      }
+      writeNpy(std::filesystem::path(_network->getOutputPath()) / ("s" + std::to_string(e.first) + ".npy"), st.data(),
+               16, "<c16", {2, fr.size()});
     }
   }
   const NffftFd *nfd = dynamic_cast<const NffftFd *>(_nffft.get());

@@ -79,7 +79,73 @@ Simulation::Simulation(double cell_size, std::vector<std::shared_ptr<Object>> ob
 Simulation::Simulation(double cell_size, std::vector<std::shared_ptr<Object>> objects,
                        std::vector<std::shared_ptr<Monitor>> monitors, float cfl)
     : _cell_size{cell_size}, _cfl{cfl}, _objects{std::move(objects)}, _monitors{std::move(monitors)} {}
+Simulation::Simulation(double cell_size, std::vector<std::shared_ptr<Object>> objects,
+                       std::vector<std::shared_ptr<LumpedElement>> lumped_elements,
+                       std::vector<std::shared_ptr<Boundary>> boundaries, std::vector<std::shared_ptr<Monitor>> monitors,
+                       std::unique_ptr<Network> network, float cfl)
+    : _cell_size{cell_size}, _cfl{cfl}, _objects{std::move(objects)}, _boundaries{std::move(boundaries)},
+      _lumped_elements{std::move(lumped_elements)}, _monitors{std::move(monitors)}, _network{std::move(network)} {}
 Simulation::~Simulation() { release(); }
+
+// util/dft.h:11-27: the phase of sample j is 2 pi f (j dt), the sum is scaled by dt
+std::vector<std::complex<double>> dft(const std::vector<double> &x, double dt, const std::vector<double> &frequencies) {
+  using namespace std::complex_literals;
+  std::vector<std::complex<double>> r(frequencies.size());
+  for (size_t q = 0; q < frequencies.size(); ++q) {
+    std::complex<double> sum{0.0, 0.0};
+    for (size_t j = 0; j < x.size(); ++j) {
+      const double t = static_cast<double>(j) * dt;
+      sum += x[j] * std::exp(-2.0 * 1i * constant::PI * frequencies[q] * t);
+    }
+    r[q] = sum * dt;
+  }
+  return r;
+}
+
+// Port::calculateSParameter, port.cpp:25-34
+void Port::calculateSParameter(const std::vector<double> &frequencies, double dt) {
+  const std::complex<double> z = _impedance;
+  const double k = std::sqrt(std::real(z));
+  const auto v = dft(_voltage->getValue(), dt, frequencies);
+  const auto i = dft(_current->getValue(), dt, frequencies);
+  _a.resize(v.size());
+  _b.resize(v.size());
+  for (size_t q = 0; q < v.size(); ++q) {
+    _a[q] = 0.5 * (v[q] + z * i[q]) / k;
+    _b[q] = 0.5 * (v[q] - std::conj(z) * i[q]) / k;
+  }
+}
+
+// Network::outputData's arithmetic, network.cpp:40-52
+void Network::calculate(double dt) {
+  for (auto &p : _ports) p->calculateSParameter(_frequencies, dt);
+  _s_parameters.clear();
+  for (size_t i = 0; i < _ports.size(); ++i) {
+    if (!_ports[i]->isActivatedSource()) continue;
+    const auto &a = _ports[i]->getA();
+    for (size_t j = 0; j < _ports.size(); ++j) {
+      const auto &b = _ports[j]->getB();
+      std::vector<std::complex<double>> s(b.size());
+      for (size_t q = 0; q < b.size(); ++q) s[q] = b[q] / a[q];
+      _s_parameters[_ports[j]->getPortIndex() * 10 + _ports[i]->getPortIndex()] = std::move(s);
+    }
+  }
+}
+
+const std::map<int, std::vector<std::complex<double>>> &Simulation::sParameters() {
+  if (!_network) throw std::runtime_error("no network in this simulation");
+  for (const auto &p : _network->getPorts()) {
+    for (const Monitor *m : {static_cast<const Monitor *>(p->getVoltageMonitor().get()),
+                             static_cast<const Monitor *>(p->getCurrentMonitor().get())}) {
+      size_t q = 0;
+      while (q < _monitors.size() && _monitors[q].get() != m) ++q;
+      if (q == _monitors.size()) throw std::runtime_error("a port's monitor is not one of the simulation's monitors");
+      _monitors[q]->setValue(monitorValues(q));
+    }
+  }
+  _network->calculate(_dt);
+  return _network->getSParameters();
+}
 
 void Simulation::release() {
   if (_engine) xfdtd_destroy(_engine);

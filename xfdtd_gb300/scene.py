@@ -96,6 +96,11 @@ class MonitorDesc(C.Structure):
                 ("plot_step", C.c_int64), ("total_time_steps", C.c_int64)]
 
 
+class PortDesc(C.Structure):
+    _fields_ = [("index", C.c_int32), ("is_activated_source", C.c_int32), ("impedance_re", C.c_double),
+                ("impedance_im", C.c_double), ("voltage_monitor", C.c_int32), ("current_monitor", C.c_int32)]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("cell_size", C.c_double), ("cfl", C.c_float),
                 ("n_objects", C.c_int32), ("objects", C.POINTER(ObjectDesc)),
@@ -107,7 +112,9 @@ class SceneDesc(C.Structure):
                 ("voxel_materials", C.POINTER(MaterialDesc)),
                 ("voxel_index", C.c_void_p),
                 ("voxel_shape", C.c_int64 * 3),
-                ("voxel_index_bytes", C.c_int32), ("reserved3", C.c_int32)]
+                ("voxel_index_bytes", C.c_int32), ("reserved3", C.c_int32),
+                ("n_ports", C.c_int32), ("n_network_freqs", C.c_int32),
+                ("ports", C.POINTER(PortDesc)), ("network_freqs", C.POINTER(C.c_double))]
 
 
 # ---------------------------------------------------------------- shapes ---
@@ -475,6 +482,27 @@ def MovieMonitor(monitor: _Monitor, total_time_steps: int, plot_step: int = 30) 
                     monitor.component, monitor.plane_type, int(plot_step), int(total_time_steps))
 
 
+@dataclass
+class Port:
+    """Port(index, impedance, is_activated_source, voltage, current),
+    src/network/port.cpp:10-17; voltage and current are the scene's
+    VoltageMonitor and CurrentMonitor objects (they must be in
+    Scene.monitors)."""
+    index: int
+    impedance: complex
+    is_activated_source: bool
+    voltage: _Monitor
+    current: _Monitor
+
+
+@dataclass
+class Network:
+    """Network(ports, frequencies, output_path), src/network/network.cpp:10-14."""
+    ports: List[Port]
+    frequencies: Sequence[float]
+    output_path: str = ""
+
+
 # ----------------------------------------------------------------- scene ---
 @dataclass
 class Scene:
@@ -491,6 +519,7 @@ class Scene:
     cfl: float = 0.99
     voxel_materials: Optional[List[Material]] = None
     voxel_index: Optional[np.ndarray] = None  # (nx, ny, nz) material numbers
+    network: Optional[Network] = None
 
     def desc(self) -> SceneDesc:
         """Builds the C description.  The returned struct keeps its arrays
@@ -535,6 +564,23 @@ class Scene:
             d.voxel_materials = vm
             d.n_voxel_materials = len(self.voxel_materials)
             d.voxel_shape[:] = list(vi.shape)
+        if self.network is not None and self.network.ports:
+            def mon_index(m):
+                for q, x in enumerate(self.monitors):
+                    if x is m:
+                        return q
+                raise ValueError("a port's monitors must be in Scene.monitors")
+            ports = (PortDesc * len(self.network.ports))()
+            for q, p in enumerate(self.network.ports):
+                z = complex(p.impedance)
+                ports[q].index, ports[q].is_activated_source = int(p.index), int(bool(p.is_activated_source))
+                ports[q].impedance_re, ports[q].impedance_im = z.real, z.imag
+                ports[q].voltage_monitor, ports[q].current_monitor = mon_index(p.voltage), mon_index(p.current)
+            fr = np.ascontiguousarray(self.network.frequencies, dtype=np.float64)
+            keep += [ports, fr]
+            d.n_ports, d.ports = len(self.network.ports), ports
+            d.n_network_freqs = fr.size
+            d.network_freqs = fr.ctypes.data_as(C.POINTER(C.c_double))
         d._keep = keep
         return d
 
