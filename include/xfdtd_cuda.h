@@ -105,6 +105,10 @@ typedef struct xfdtd_tfsf_plan {
 } xfdtd_tfsf_plan;
 
 /* NffftFd (nffft_fd.cpp:17-203, 379-556). */
+/* enabled: 1 NffftFd (running DFT at n_freq frequencies, far field over
+ * theta x phi); 2 NffftBroadBand (src/nffft/nffft_broadband.cpp: every
+ * step's surface samples kept, n_freq and the phase tables unused, theta[0]
+ * and phi[0] the one direction). */
 typedef struct xfdtd_nffft_plan {
   int32_t enabled;
   int32_t n_freq;
@@ -216,6 +220,13 @@ int xfdtd_read_snapshot(xfdtd_handle *h, int s, int64_t frame, double *out, int6
  * jy jz my mz over (ny_box, nz_box); Y faces jz jx mz mx over (nz_box,
  * nx_box); Z faces jx jy mx my over (nx_box, ny_box)), [n_freq][a][b] (re, im). */
 int xfdtd_read_nffft(xfdtd_handle *h, int which, double *out, int64_t len);
+/* Broadband NF-FF (plan nffft.enabled = 2): the auxiliary arrays n_x, n_y,
+ * n_z, l_x, l_y, l_z of NffftBroadBand::calculateLNXYZ
+ * (src/nffft/nffft_broadband.cpp:351-464) over the N = 2*total_steps - 1
+ * fftshifted bins of linspace(-1/(2 dt), 1/(2 dt), N), as [6][N] (re, im)
+ * pairs (len = 12 N), from the samples of the steps run so far.  Uses
+ * cuFFT (libcufft), loaded at the first call. */
+int xfdtd_broadband_far_field(xfdtd_handle *h, double *out, int64_t len);
 /* Far field over (n_freq, n_theta, n_phi): which 0 e_theta 1 e_phi 2 h_theta
  * 3 h_phi 4 n_theta 5 n_phi 6 l_theta 7 l_phi (complex pairs), 8 power_theta
  * 9 power_phi (real) -- the arrays NffftFd::outputData writes. */

@@ -128,6 +128,9 @@ typedef struct xfdtd_tfsf_desc {
   xfdtd_waveform_desc waveform;
 } xfdtd_tfsf_desc;
 
+/* enabled: 1 NffftFd(dx, dy, dz, frequencies, theta, phi, path); 2
+ * NffftBroadBand(dx, dy, dz, theta[0], phi[0], path)
+ * (src/include/nffft/nffft_broadband.h), frequencies unused. */
 typedef struct xfdtd_nffft_desc {
   int32_t enabled;
   int32_t n_freq;

@@ -54,6 +54,11 @@ int xfdtd_sim_field_monitor(xfdtd_sim *s, int index, int64_t lo[3], int64_t shap
 /* Frame `frame` of field monitor `index`, [n0][n1][n2]. */
 int xfdtd_sim_read_field_monitor(xfdtd_sim *s, int index, int64_t frame, double *out, int64_t len);
 int xfdtd_sim_read_nffft(xfdtd_sim *s, int which, double *out, int64_t len);
+/* Far field: for an NffftFd over (n_freq, n_theta, n_phi), which 0 e_theta
+ * 1 e_phi 2 h_theta 3 h_phi 4 n_theta 5 n_phi 6 l_theta 7 l_phi (complex
+ * pairs), 8 power_theta 9 power_phi (real).  For an NffftBroadBand the same
+ * arrays over its N = 2*total_steps - 1 bins, and 10 the bins' frequencies
+ * (NffftBroadBand::calculateFarField, src/nffft/nffft_broadband.cpp:343-371). */
 int xfdtd_sim_far_field(xfdtd_sim *s, int which, double *out, int64_t len);
 int xfdtd_sim_incident_dft(xfdtd_sim *s, const double *freqs, int n, double *out);
 /* Output directory (and file name) of monitor `index`; with index -1 the

@@ -150,6 +150,15 @@ class OracleSim:
         return out[..., 0] + 1j * out[..., 1]
 
     def far_field(self, which: int) -> np.ndarray:
+        if type(self.scene.nffft).__name__ == "NffftBroadBand":   # over the 2T-1 bins; 10 = frequencies
+            nb = 2 * self.total_steps - 1
+            if which < 8:
+                out = np.empty((nb, 2), dtype=np.float64)
+                _check(lib().oracle_sim_far_field(self.h, which, _dp(out), out.size))
+                return out[:, 0] + 1j * out[:, 1]
+            out = np.empty(nb, dtype=np.float64)
+            _check(lib().oracle_sim_far_field(self.h, which, _dp(out), out.size))
+            return out
         f, t, p = self.scene.nffft.arrays()
         shp = (len(f), len(t), len(p))
         if which < 8:

@@ -358,6 +358,14 @@ struct oracle_sim {
     size_t ff_step = 0;
     std::vector<cplx> out[8];
     std::vector<double> power[2];
+    // NffftBroadBand (src/nffft/nffft_broadband.cpp): every step's samples
+    // of the 24 surface arrays, [which][t][a][b] in the accumulators' face
+    // layout, and the far field over the N = 2T-1 bins
+    bool broadband = false;
+    std::vector<std::vector<double>> samples;
+    std::vector<double> bb_freq;
+    std::vector<cplx> bb_out[8];
+    std::vector<double> bb_power[2];
   } nf;
 
   A3 &field(int c) {
@@ -392,6 +400,7 @@ struct oracle_sim {
   void tfsfH();
   void lumpedE(Lumped &l);
   void nffftUpdate();
+  void broadbandFarField();
   void monitorUpdate(Monitor &m);
   // TimeDomainFieldMonitor::outputData's view of the current field
   // (field_monitor.cpp:102-121)
@@ -685,6 +694,12 @@ void oracle_sim::initNFFFT() {
   f.lk = f.dist[2]; f.rk = f.lk + bn[2];
   f.bx = bn[0]; f.by = bn[1]; f.bz = bn[2];
   size_t nfq = f.freq.size();
+  if (f.broadband) {   // NffftBroadBand::init (nffft_broadband.cpp:31-95): T samples per series
+    const size_t plane[3] = {f.by * f.bz, f.bz * f.bx, f.bx * f.by};
+    f.samples.assign(24, {});
+    for (int w = 0; w < 24; ++w) f.samples[w].assign(total * plane[w / 8], 0.0);
+    return;
+  }
   // NffftFd::init, nffft_fd.cpp:17-89
   f.acc.resize(24);
   for (int q = 0; q < 8; ++q) {
@@ -1201,6 +1216,12 @@ void oracle_sim::nffftUpdate() {  // NffftFd::update, nffft_fd.cpp:108-203
     return 0.25 * (hy(i, j, k) + hy(i, j + 1, k) + hy(i, j, k - 1) + hy(i, j + 1, k - 1));
   };
   auto add = [&](int which, size_t a, size_t b, double v, bool is_j) {
+    if (f.broadband) {   // NffftBroadBand::update (nffft_broadband.cpp:97-154): keep the sample
+      const size_t db = which < 8 ? f.bz : (which < 16 ? f.bx : f.by);
+      const size_t da = which < 8 ? f.by : (which < 16 ? f.bz : f.bx);
+      f.samples[which][(nt * da + a) * db + b] = v;
+      return;
+    }
     const std::vector<cplx> &tr = is_j ? f.tj : f.tm;
     for (size_t n = 0; n < nfq; ++n) f.acc[which](n, a, b) += v * tr[n * total + nt];
   };
@@ -1300,6 +1321,117 @@ void oracle_sim::step() {  // loop body of Simulation::run, simulation_update.cp
   if (has_nffft) nffftUpdate();
   for (auto &m : monitors) monitorUpdate(m);
   ++cur;
+}
+
+// NffftBroadBand::calculateFarField / calculateLNXYZ / calculateAuxiliary
+// (nffft_broadband.cpp:343-464).  The transform of each series is its
+// N-point DFT, X[q] = sum_t x[t] exp(-2 pi i q t / N) (the definition of
+// the FFT the reference takes), zero-padded past the T samples and read in
+// fftshift order: output bin m holds X[(m + (N+1)/2) mod N] for odd N.
+void oracle_sim::broadbandFarField() {
+  using namespace std::complex_literals;
+  auto &f = nf;
+  const size_t T = total, N = 2 * total - 1;
+  const double fs = 1 / dt;
+  f.bb_freq.resize(N);
+  std::vector<double> k(N);
+  const double step = (fs / 2 - (-fs / 2)) / static_cast<double>(N - 1);   // linspace(-fs/2, fs/2, N)
+  for (size_t m = 0; m < N; ++m) {
+    f.bb_freq[m] = -fs / 2 + step * static_cast<double>(m);
+    k[m] = 2 * PI * f.bb_freq[m] / C_0;
+  }
+  std::vector<cplx> tw(N);   // exp(-2 pi i j / N)
+  for (size_t j = 0; j < N; ++j) tw[j] = std::polar(1.0, -2 * PI * static_cast<double>(j) / static_cast<double>(N));
+  auto spectrum = [&](const std::vector<double> &s, size_t cell, size_t plane, std::vector<cplx> &out) {
+    for (size_t m = 0; m < N; ++m) {
+      const size_t q = (m + (N + 1) / 2) % N;
+      cplx acc{0, 0};
+      for (size_t t = 0; t < T; ++t) acc += s[t * plane + cell] * tw[(q * t) % N];
+      out[m] = acc;
+    }
+  };
+  const double th = f.theta[0], ph = f.phi[0];
+  const double ffv[3] = {std::sin(th) * std::cos(ph), std::sin(th) * std::sin(ph), std::cos(th)};
+  const double dl3[3] = {gs->base[0], gs->base[1], gs->base[2]};   // getDx/getDy/getDz
+  const double ci = static_cast<double>(f.li + f.bx / 2), cj = static_cast<double>(f.lj + f.by / 2),
+               ck = static_cast<double>(f.lk + f.bz / 2);   // GridBox::getGridCenterIndex
+  std::vector<cplx> nx_(N), ny_(N), nz_(N), lx_(N), ly_(N), lz_(N);
+  std::vector<cplx> xa(N), xb(N), xc(N), xd(N);
+  // one face: series (ja, jb, ma, mb) = samples[w0 .. w0+3] at face cells;
+  // pos(a, b) gives the cell's (x, y, z) index offsets from the centre
+  auto face = [&](int w0, size_t da, size_t db, double ds, std::vector<cplx> &na, std::vector<cplx> &nb,
+                  std::vector<cplx> &la, std::vector<cplx> &lb, auto pos) {
+    const size_t plane = da * db;
+    for (size_t a = 0; a < da; ++a)
+      for (size_t b = 0; b < db; ++b) {
+        double x, y, z;
+        pos(a, b, x, y, z);
+        const double delay = x * ffv[0] * dl3[0] + y * ffv[1] * dl3[1] + z * ffv[2] * dl3[2];
+        const size_t cell = a * db + b;
+        spectrum(f.samples[w0], cell, plane, xa);
+        spectrum(f.samples[w0 + 1], cell, plane, xb);
+        spectrum(f.samples[w0 + 2], cell, plane, xc);
+        spectrum(f.samples[w0 + 3], cell, plane, xd);
+        for (size_t m = 0; m < N; ++m) {
+          const cplx phase = std::exp(1i * delay * k[m]);
+          na[m] += ds * phase * xa[m];
+          nb[m] += ds * phase * xb[m];
+          la[m] += ds * phase * xc[m];
+          lb[m] += ds * phase * xd[m];
+        }
+      }
+  };
+  for (int side = 0; side < 2; ++side) {   // X faces: (j, k); jy, jz, my, mz
+    const double ds = dl3[1] * dl3[2];
+    const double xf = static_cast<double>(side ? f.ri : f.li) - ci;
+    face(side * 4, f.by, f.bz, ds, ny_, nz_, ly_, lz_, [&](size_t a, size_t b, double &x, double &y, double &z) {
+      x = xf;
+      y = static_cast<double>(f.lj + a) + 0.5 - cj;
+      z = static_cast<double>(f.lk + b) + 0.5 - ck;
+    });
+  }
+  for (int side = 0; side < 2; ++side) {   // Y faces: (k, i); jz, jx, mz, mx
+    const double ds = dl3[0] * dl3[2];
+    const double yf = static_cast<double>(side ? f.rj : f.lj) - cj;
+    face(8 + side * 4, f.bz, f.bx, ds, nz_, nx_, lz_, lx_, [&](size_t a, size_t b, double &x, double &y, double &z) {
+      x = static_cast<double>(f.li + b) + 0.5 - ci;
+      y = yf;
+      z = static_cast<double>(f.lk + a) + 0.5 - ck;
+    });
+  }
+  if (f.bz > 1)
+    for (int side = 0; side < 2; ++side) {   // Z faces: (i, j); jx, jy, mx, my
+      const double ds = dl3[0] * dl3[1];
+      const double zf = static_cast<double>(side ? f.rk : f.lk) - ck;
+      face(16 + side * 4, f.bx, f.by, ds, nx_, ny_, lx_, ly_, [&](size_t a, size_t b, double &x, double &y, double &z) {
+        x = static_cast<double>(f.li + a) + 0.5 - ci;
+        y = static_cast<double>(f.lj + b) + 0.5 - cj;
+        z = zf;
+      });
+    }
+  const double ct = std::cos(th), st = std::sin(th), cp = std::cos(ph), sp = std::sin(ph);
+  for (int q = 0; q < 8; ++q) f.bb_out[q].assign(N, cplx(0, 0));
+  for (int q = 0; q < 2; ++q) f.bb_power[q].assign(N, 0.0);
+  for (size_t m = 0; m < N; ++m) {
+    const cplx n_theta = ct * cp * nx_[m] + ct * sp * ny_[m] - st * nz_[m];
+    const cplx n_phi = -sp * nx_[m] + cp * ny_[m];
+    const cplx l_theta = ct * cp * lx_[m] + ct * sp * ly_[m] - st * lz_[m];
+    const cplx l_phi = -sp * lx_[m] + cp * ly_[m];
+    const double kk = k[m];
+    f.bb_out[0][m] = (-1i * kk) * (ETA_0 * n_theta + l_phi) / (4 * PI);
+    f.bb_out[1][m] = (1i * kk) * (-ETA_0 * n_phi + l_theta) / (4 * PI);
+    f.bb_out[2][m] = (1i * kk) * (n_phi - l_theta / ETA_0) / (4 * PI);
+    f.bb_out[3][m] = (-1i * kk) * (n_theta + l_phi / ETA_0) / (4 * PI);
+    f.bb_out[4][m] = n_theta;
+    f.bb_out[5][m] = n_phi;
+    f.bb_out[6][m] = l_theta;
+    f.bb_out[7][m] = l_phi;
+    const double coff = std::pow(kk, 2) / (32 * PI * PI * ETA_0);
+    f.bb_power[0][m] = coff * std::pow(std::abs(ETA_0 * n_theta + l_phi), 2);
+    f.bb_power[1][m] = coff * std::pow(std::abs(-ETA_0 * n_phi + l_theta), 2);
+  }
+  f.ff_valid = true;
+  f.ff_step = cur;
 }
 
 void oracle_sim::farField() {  // NffftFd::calculateFarfield{,X,Y,Z}, nffft_fd.cpp:379-556
@@ -1465,6 +1597,7 @@ int oracle_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, oracle_si
     }
     if (sc->nffft.enabled) {
       s->has_nffft = true;
+      s->nf.broadband = sc->nffft.enabled == 2;
       for (int a = 0; a < 3; ++a) s->nf.dist[a] = static_cast<size_t>(sc->nffft.distance[a]);
       s->nf.freq.assign(sc->nffft.frequencies, sc->nffft.frequencies + sc->nffft.n_freq);
       s->nf.theta.assign(sc->nffft.theta, sc->nffft.theta + sc->nffft.n_theta);
@@ -1579,6 +1712,21 @@ int oracle_sim_read_nffft(oracle_sim *s, int which, double *out, int64_t len) {
 int oracle_sim_far_field(oracle_sim *s, int which, double *out, int64_t len) {
   return guarded([&] {
     if (!s->has_nffft) throw std::invalid_argument("no NFFFT");
+    if (s->nf.broadband) {
+      if (!s->nf.ff_valid || s->nf.ff_step != s->cur) s->broadbandFarField();
+      const std::vector<double> *re[3] = {&s->nf.bb_power[0], &s->nf.bb_power[1], &s->nf.bb_freq};
+      if (which >= 0 && which < 8) {
+        auto &v = s->nf.bb_out[which];
+        if (static_cast<size_t>(len) != 2 * v.size()) throw std::invalid_argument("length mismatch");
+        std::memcpy(out, v.data(), v.size() * sizeof(cplx));
+      } else if (which >= 8 && which <= 10) {
+        if (static_cast<size_t>(len) != re[which - 8]->size()) throw std::invalid_argument("length mismatch");
+        std::memcpy(out, re[which - 8]->data(), re[which - 8]->size() * sizeof(double));
+      } else {
+        throw std::invalid_argument("bad far-field output");
+      }
+      return;
+    }
     if (!s->nf.ff_valid || s->nf.ff_step != s->cur) s->farField();
     if (which >= 0 && which < 8) {
       auto &v = s->nf.out[which];

@@ -473,3 +473,43 @@ def test_network_s_parameters(tmp_path):
         a = np.load(tmp_path / "net" / ("s%d.npy" % key))
         assert a.shape == (2, 4) and a.dtype == np.complex128
         assert np.array_equal(a[0].real, np.asarray(sc.network.frequencies)) and np.array_equal(a[1], got[key])
+
+
+def _broadband_scene(steps=80):
+    """The small PEC-sphere scene with an NffftBroadBand in an oblique
+    direction in place of its NffftFd."""
+    from xfdtd_gb300 import configs
+    sc, _ = configs.pec_sphere_rcs(scale=2, steps=steps)
+    nf = sc.nffft
+    sc.nffft = S.NffftBroadBand(nf.distance_x, nf.distance_y, nf.distance_z, 0.3, 0.7)
+    return sc, steps
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_broadband_nffft_far_field(precision, tmp_path):
+    """NffftBroadBand (nffft_broadband.cpp): every step's surface samples
+    kept on the device, transformed by cuFFT and summed with their path
+    delays.  Against the oracle's restatement (direct DFT per series): the
+    bin frequencies exactly, e/h theta/phi, n/l theta/phi and the powers
+    within 1e-10 of each array's largest value in FP64 (1e-3 in the FP32
+    form); outputData writes the six arrays and far_field_parameter.dat."""
+    sc, st = _broadband_scene(steps=80)
+    sc.nffft.output_dir_path = str(tmp_path / "bb")
+    o = O.OracleSim(sc, st)
+    o.step(st)
+    g = X.Simulation(sc, st, precision=precision)
+    g.step(30)
+    g.step(st - 30)
+    assert np.array_equal(g.far_field(10), o.far_field(10))
+    tol = TOL if precision == "fp64" else 1e-3
+    for which in range(10):
+        got, want = g.far_field(which), o.far_field(which)
+        assert got.shape == (2 * st - 1,)
+        e = np.abs(got - want).max() / np.abs(want).max()
+        assert e <= tol, (precision, which, e)
+    g.output()
+    names = sorted(p.name for p in (tmp_path / "bb").iterdir())
+    assert names == sorted(["e_theta.npy", "e_phi.npy", "h_theta.npy", "h_phi.npy", "power_theta.npy",
+                            "power_phi.npy", "far_field_parameter.dat"])
+    assert np.array_equal(np.load(tmp_path / "bb" / "e_phi.npy"), g.far_field(1))
+    assert np.array_equal(np.load(tmp_path / "bb" / "power_theta.npy"), g.far_field(8))

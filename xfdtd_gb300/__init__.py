@@ -265,6 +265,18 @@ class Simulation:
         return out[..., 0] + 1j * out[..., 1]
 
     def far_field(self, which: int) -> np.ndarray:
+        """NffftFd: array `which` (0 e_theta .. 7 l_phi complex, 8/9 power)
+        over (frequency, theta, phi).  NffftBroadBand: the same arrays over
+        its 2T-1 bins, and 10 the bins' frequencies."""
+        if isinstance(self.scene.nffft, scene.NffftBroadBand):
+            nb = 2 * self.total_steps - 1
+            if which < 8:
+                out = np.empty((nb, 2), dtype=np.float64)
+                self._check(libs()[1].xfdtd_sim_far_field(self.h, which, _dp(out), out.size))
+                return out[:, 0] + 1j * out[:, 1]
+            out = np.empty(nb, dtype=np.float64)
+            self._check(libs()[1].xfdtd_sim_far_field(self.h, which, _dp(out), out.size))
+            return out
         f, t, p = self.scene.nffft.arrays()
         shp = (len(f), len(t), len(p))
         if which < 8:

@@ -23,6 +23,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+#include <cufft.h>
+#include <dlfcn.h>
 
 #include <algorithm>
 #include <functional>
@@ -38,6 +40,7 @@
 #include "common.cuh"
 #include "adjoint.cuh"
 #include "batch.cuh"
+#include "broadband.cuh"
 #include "surface.cuh"
 #include "interior_tma.cuh"
 #include "sweep.cuh"
@@ -204,6 +207,9 @@ struct xfdtd_handle {
   int nf_batch = 8;
   long long nf_done = 0;        // steps already folded
   void *nf_buf[3] = {};
+  int nf_rows = 8;              // rows of the sample buffers: nf_batch, or every step (broadband)
+  bool nf_bb = false;           // NffftBroadBand: keep every step's samples, no running DFT
+  double bb_theta = 0, bb_phi = 0;
 
   // profiling
   std::vector<cudaEvent_t> ev_pool;
@@ -1067,7 +1073,7 @@ xg::NfParams<T> nf_params(xfdtd_handle *h) {
   p.total = h->total;
   p.step = h->d_step;
   for (int g = 0; g < 3; ++g) p.buf[g] = static_cast<T *>(h->nf_buf[g]);
-  p.batch = h->nf_batch;
+  p.batch = h->nf_rows;
   return p;
 }
 
@@ -1106,7 +1112,7 @@ void launch_nffft_accumulate(xfdtd_handle *h, int count, int lag) {
 // Accumulates the NF-FF steps sampled since the last fold (before any read
 // of the accumulators or the far field).
 void nffft_flush(xfdtd_handle *h) {
-  if (!h->nffft) return;
+  if (!h->nffft || h->nf_bb) return;
   const long long pending = h->host_step - h->nf_done;
   if (pending <= 0) return;
   if (h->precision == XFDTD_FP64) launch_nffft_accumulate<double>(h, static_cast<int>(pending), 1);
@@ -1244,7 +1250,9 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     prof_begin(h, 4);
     launch_nffft<T>(h);
     prof_end(h);
-    if ((s + 1) % h->nf_batch == 0) {   // the batch is full: fold it
+    if (h->nf_bb) {   // broadband: the samples stay, one row per step
+      h->nf_done = s + 1;
+    } else if ((s + 1) % h->nf_batch == 0) {   // the batch is full: fold it
       prof_begin(h, 9);
       launch_nffft_accumulate<T>(h, static_cast<int>(s + 1 - h->nf_done), 0);
       prof_end(h);
@@ -1504,7 +1512,25 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
 
   // NF-FF
   const xfdtd_nffft_plan &np = pl->nffft;
-  if (np.enabled) {
+  if (np.enabled == 2) {   // NffftBroadBand: every step's samples, the far field at the end
+    h->nffft = true;
+    h->nf_bb = true;
+    if (np.n_theta != 1 || np.n_phi != 1 || !np.theta || !np.phi) invalid("broadband NF-FF takes one direction");
+    h->bb_theta = np.theta[0];
+    h->bb_phi = np.phi[0];
+    for (int a = 0; a < 3; ++a) {
+      if (np.lo[a] < 1 || np.hi[a] <= np.lo[a] || np.hi[a] > n_axis[a] - 1) invalid("NF-FF box outside the grid");
+      h->nf_lo[a] = static_cast<int>(np.lo[a]);
+      h->nf_hi[a] = static_cast<int>(np.hi[a]);
+    }
+    const long long bx = np.hi[0] - np.lo[0], by = np.hi[1] - np.lo[1], bz = np.hi[2] - np.lo[2];
+    const long long face[3] = {by * bz, bz * bx, bx * by};
+    h->nf_rows = static_cast<int>(std::max<long long>(1, pl->total_steps));
+    long long bytes = 0;
+    for (int g = 0; g < 3; ++g) bytes += static_cast<long long>(h->nf_rows) * 8 * face[g] * h->esize;
+    if (bytes > (96ll << 30)) invalid("broadband NF-FF samples above 96 GiB");
+    for (int g = 0; g < 3; ++g) h->nf_buf[g] = h->alloc_bytes(static_cast<size_t>(h->nf_rows) * 8 * face[g] * h->esize);
+  } else if (np.enabled) {
     h->nffft = true;
     if (np.n_freq < 1) invalid("NF-FF needs at least one frequency");
     h->nf = np.n_freq;
@@ -1686,8 +1712,138 @@ void write_comp(xfdtd_handle *h, int comp, const double *in, long long len) {
   XCHECK(cudaStreamSynchronize(h->stream));
 }
 
+// cuFFT, loaded when a broadband far field is first asked for (the rest of
+// the engine does not need it).
+struct CufftApi {
+  decltype(&cufftPlanMany) plan_many = nullptr;
+  decltype(&cufftExecZ2Z) exec_z2z = nullptr;
+  decltype(&cufftSetStream) set_stream = nullptr;
+  decltype(&cufftDestroy) destroy = nullptr;
+};
+const CufftApi &cufft_api() {
+  static const CufftApi api = [] {
+    CufftApi a;
+    void *lib = nullptr;
+    for (const char *name : {"libcufft.so.12", "libcufft.so"})
+      if (!lib) lib = dlopen(name, RTLD_NOW | RTLD_LOCAL);
+    if (!lib) return a;
+    a.plan_many = reinterpret_cast<decltype(a.plan_many)>(dlsym(lib, "cufftPlanMany"));
+    a.exec_z2z = reinterpret_cast<decltype(a.exec_z2z)>(dlsym(lib, "cufftExecZ2Z"));
+    a.set_stream = reinterpret_cast<decltype(a.set_stream)>(dlsym(lib, "cufftSetStream"));
+    a.destroy = reinterpret_cast<decltype(a.destroy)>(dlsym(lib, "cufftDestroy"));
+    return a;
+  }();
+  if (!api.plan_many || !api.exec_z2z || !api.set_stream || !api.destroy)
+    throw Err{XFDTD_ERR_STATE, "cuFFT (libcufft.so) is not available for the broadband far field"};
+  return api;
+}
+
+// NffftBroadBand::calculateLNXYZ (nffft_broadband.cpp:351-464): the six
+// auxiliary arrays n_x, n_y, n_z, l_x, l_y, l_z over the N = 2T-1 output
+// bins, from the samples of every step run so far.
+template <typename T>
+void broadband_aux(xfdtd_handle *h, std::vector<double2> &out) {
+  const CufftApi &fft = cufft_api();
+  const long long steps = h->total, N = 2 * steps - 1;
+  const int li = h->nf_lo[0], lj = h->nf_lo[1], lk = h->nf_lo[2], ri = h->nf_hi[0], rj = h->nf_hi[1],
+            rk = h->nf_hi[2];
+  const int ci = li + (ri - li) / 2, cj = lj + (rj - lj) / 2, ck = lk + (rk - lk) / 2;   // GridBox centre
+  const long long plane[3] = {static_cast<long long>(rj - lj) * (rk - lk), static_cast<long long>(ri - li) * (rk - lk),
+                              static_cast<long long>(ri - li) * (rj - lj)};
+  // buffer quantity q % 4 of each face pair -> auxiliary array (0 n_x .. 5 l_z)
+  const int target[3][4] = {{1, 2, 4, 5}, {2, 0, 5, 3}, {0, 1, 3, 4}};
+  double2 *acc = nullptr, *in = nullptr, *spec = nullptr;
+  XCHECK(cudaMalloc(&acc, sizeof(double2) * 6 * N));
+  XCHECK(cudaMemsetAsync(acc, 0, sizeof(double2) * 6 * N, h->stream));
+  const long long max_plane = std::max({plane[0], plane[1], plane[2]});
+  const int chunk = static_cast<int>(std::max<long long>(1, std::min<long long>(max_plane, (256ll << 20) / (N * 16))));
+  XCHECK(cudaMalloc(&in, sizeof(double2) * chunk * N));
+  XCHECK(cudaMalloc(&spec, sizeof(double2) * chunk * N));
+  std::vector<std::pair<int, cufftHandle>> plans;
+  auto plan_for = [&](int nb) {
+    for (auto &p : plans)
+      if (p.first == nb) return p.second;
+    cufftHandle ph;
+    int n = static_cast<int>(N);
+    if (fft.plan_many(&ph, 1, &n, nullptr, 1, n, nullptr, 1, n, CUFFT_Z2Z, nb) != CUFFT_SUCCESS)
+      throw Err{XFDTD_ERR_CUDA, "cufftPlanMany failed"};
+    fft.set_stream(ph, h->stream);
+    plans.push_back({nb, ph});
+    return ph;
+  };
+  try {
+    const double eta_dir[3] = {std::sin(h->bb_theta) * std::cos(h->bb_phi), std::sin(h->bb_theta) * std::sin(h->bb_phi),
+                               std::cos(h->bb_theta)};
+    const bool three_d = rk - lk > 1;
+    for (int g = 0; g < (three_d ? 3 : 2); ++g)
+      for (int side = 0; side < 2; ++side)
+        for (int qq = 0; qq < 4; ++qq) {
+          const int q = side * 4 + qq;
+          for (long long c0 = 0; c0 < plane[g]; c0 += chunk) {
+            const int nb = static_cast<int>(std::min<long long>(chunk, plane[g] - c0));
+            const long long elems = static_cast<long long>(nb) * N;
+            xg::k_bb_load<T><<<static_cast<unsigned>(std::min<long long>((elems + 255) / 256, 65535)), 256, 0,
+                               h->stream>>>(static_cast<const T *>(h->nf_buf[g]), q, plane[g], c0, nb, steps, N, in);
+            XCHECK(cudaGetLastError());
+            if (fft.exec_z2z(plan_for(nb), reinterpret_cast<cufftDoubleComplex *>(in),
+                             reinterpret_cast<cufftDoubleComplex *>(spec), CUFFT_FORWARD) != CUFFT_SUCCESS)
+              throw Err{XFDTD_ERR_CUDA, "cufftExecZ2Z failed"};
+            xg::BbChunk c{};
+            c.group = g;
+            c.side = side;
+            c.c0 = c0;
+            c.nb = nb;
+            if (g == 0) {
+              c.du = rk - lk;
+              c.face_coord = (side ? ri : li) - ci;
+              c.off_v = lj + 0.5 - cj;
+              c.off_u = lk + 0.5 - ck;
+              c.ds = h->dl[1] * h->dl[2];
+            } else if (g == 1) {
+              c.du = rk - lk;
+              c.face_coord = (side ? rj : lj) - cj;
+              c.off_v = li + 0.5 - ci;
+              c.off_u = lk + 0.5 - ck;
+              c.ds = h->dl[0] * h->dl[2];
+            } else {
+              c.du = rj - lj;
+              c.face_coord = (side ? rk : lk) - ck;
+              c.off_v = li + 0.5 - ci;
+              c.off_u = lj + 0.5 - cj;
+              c.ds = h->dl[0] * h->dl[1];
+            }
+            for (int a = 0; a < 3; ++a) {
+              c.dir[a] = eta_dir[a];
+              c.dl[a] = h->dl[a];
+            }
+            c.fs = 1 / h->dt;
+            c.n = static_cast<double>(N);
+            c.pi = kPi;
+            c.c_0 = std::sqrt(1 / (kEps0 * kMu0));   // constant.h C_0
+            xg::k_bb_phase_sum<<<static_cast<unsigned>(N), 256, 0, h->stream>>>(c, spec, acc + target[g][qq] * N);
+            XCHECK(cudaGetLastError());
+          }
+        }
+    out.resize(static_cast<size_t>(6 * N));
+    XCHECK(cudaMemcpyAsync(out.data(), acc, sizeof(double2) * 6 * N, cudaMemcpyDeviceToHost, h->stream));
+    XCHECK(cudaStreamSynchronize(h->stream));
+  } catch (...) {
+    for (auto &p : plans) fft.destroy(p.second);
+    cudaFree(acc);
+    cudaFree(in);
+    cudaFree(spec);
+    throw;
+  }
+  for (auto &p : plans) fft.destroy(p.second);
+  cudaFree(acc);
+  cudaFree(in);
+  cudaFree(spec);
+  h->d2h += static_cast<long long>(sizeof(double2)) * 6 * N;
+}
+
 void run_far_field(xfdtd_handle *h) {
   if (!h->nffft) throw Err{XFDTD_ERR_STATE, "the plan has no NF-FF box"};
+  if (h->nf_bb) throw Err{XFDTD_ERR_STATE, "a broadband NF-FF has its own far field (xfdtd_broadband_far_field)"};
   if (!h->ff_theta) throw Err{XFDTD_ERR_STATE, "the plan has no far-field directions"};
   if (h->ff_step == h->host_step) return;
   nffft_flush(h);
@@ -1865,10 +2021,23 @@ int xfdtd_read_snapshot(xfdtd_handle *h, int s, int64_t frame, double *out, int6
   });
 }
 
+int xfdtd_broadband_far_field(xfdtd_handle *h, double *out, int64_t len) {
+  if (!h || !out) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    if (!h->nf_bb) invalid("the plan has no broadband NF-FF");
+    const long long N = 2 * h->total - 1;
+    if (len != 12 * N) invalid("length must be 6 * (2 * total_steps - 1) complex values");
+    std::vector<double2> aux;
+    if (h->precision == XFDTD_FP64) broadband_aux<double>(h, aux);
+    else broadband_aux<float>(h, aux);
+    std::memcpy(out, aux.data(), aux.size() * sizeof(double2));
+  });
+}
+
 int xfdtd_read_nffft(xfdtd_handle *h, int which, double *out, int64_t len) {
   if (!h) return XFDTD_ERR_STATE;
   return guarded(h, [&] {
-    if (!h->nffft) throw Err{XFDTD_ERR_STATE, "the plan has no NF-FF box"};
+    if (!h->nffft || h->nf_bb) throw Err{XFDTD_ERR_STATE, "the plan has no NF-FF running DFT"};
     if (which < 0 || which >= 24) invalid("accumulator index must be 0..23");
     if (len != 2 * h->acc_len[which]) invalid("length must be 2 * n_freq * face cells");
     nffft_flush(h);
@@ -2463,6 +2632,7 @@ int xfdtd_batch_create(xfdtd_handle *const *members, int n, int flags, xfdtd_bat
         if (h->host_step != 0) invalid("batch members must not have been stepped");
         if (h->n_inj || h->n_ind || h->n_probes || !h->snaps.empty())
           invalid("batch members may not have lumped elements or monitors");
+        if (h->nf_bb) invalid("batch members may not have a broadband NF-FF");
         if (h->d.nx >= 65535 || h->d.ny >= 2040 || h->d.nz >= 8160) invalid("batch member grid too large for the tile numbering");
         for (int r = 0; r < q; ++r)
           if (members[r] == h) invalid("a handle appears twice in the batch");

@@ -358,6 +358,34 @@ class NffftFd : public NFFFT {
   std::vector<double> _frequencies, _theta, _phi;
 };
 
+// NffftBroadBand (src/include/nffft/nffft_broadband.h,
+// src/nffft/nffft_broadband.cpp): the far field in one direction (theta,
+// phi) over the whole band of the run: every step's surface samples are
+// kept, and at the end each is Fourier transformed over N = 2T-1 points
+// (zero-padded), phase-shifted by its path delay and summed.  The outputs
+// are arrays over the N fftshifted bins, labelled by linspace(-fs/2, fs/2,
+// N) with fs = 1/dt, as calculateFarField labels them.
+class NffftBroadBand : public NFFFT {
+ public:
+  NffftBroadBand(SpatialIndex distance_x, SpatialIndex distance_y, SpatialIndex distance_z, double theta, double phi,
+                 std::string output_dir_path)
+      : NFFFT(distance_x, distance_y, distance_z, std::move(output_dir_path)), _theta{theta}, _phi{phi} {}
+  double getTheta() const { return _theta; }
+  double getPhi() const { return _phi; }
+
+ private:
+  double _theta, _phi;
+};
+
+// The far field of a broadband NF-FF over its N bins
+// (NffftBroadBand::calculateFarField, nffft_broadband.cpp:343-371).
+struct BroadbandFarField {
+  std::vector<double> frequencies, wave_number;
+  std::vector<std::complex<double>> n_theta, n_phi, l_theta, l_phi;
+  std::vector<std::complex<double>> e_theta, e_phi, h_theta, h_phi;
+  std::vector<double> power_theta, power_phi;
+};
+
 // ---------------------------------------------------------- lumped element
 class LumpedElement {
  public:
@@ -697,6 +725,8 @@ class Simulation {
   std::vector<long long> fieldMonitorSteps(size_t m) const;
   // Frame f of field or movie monitor m, [n0][n1][n2].
   std::vector<double> fieldMonitorFrame(size_t m, size_t f) const;
+  // The broadband NF-FF's far field from the steps run so far.
+  BroadbandFarField broadbandFarField() const;
   // Bistatic RCS in dB over (frequency, theta, phi):
   // 10 log10(4 pi (|E_theta|^2 + |E_phi|^2) / |E_inc(f)|^2).
   std::vector<double> rcsDb() const;

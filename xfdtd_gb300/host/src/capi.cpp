@@ -102,7 +102,15 @@ int xfdtd_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, int precis
                                          static_cast<SpatialIndex>(t.distance[2]), t.e0, t.theta, t.phi, t.psi, w);
       sim->addTFSFSource(s->tfsf);
     }
-    if (sc->nffft.enabled) {
+    if (sc->nffft.enabled == 2) {   // NffftBroadBand(dx, dy, dz, theta, phi, path)
+      const auto &n = sc->nffft;
+      if (n.n_theta != 1 || n.n_phi != 1 || !n.theta || !n.phi)
+        throw std::invalid_argument("a broadband NF-FF takes one theta and one phi");
+      sim->addNFFFT(std::make_shared<NffftBroadBand>(static_cast<SpatialIndex>(n.distance[0]),
+                                                     static_cast<SpatialIndex>(n.distance[1]),
+                                                     static_cast<SpatialIndex>(n.distance[2]), n.theta[0], n.phi[0], ""));
+      for (int a = 0; a < 3; ++a) s->nffft_box[a] = n.distance[a];
+    } else if (sc->nffft.enabled) {
       const auto &n = sc->nffft;
       std::vector<double> f(n.frequencies, n.frequencies + n.n_freq);
       std::vector<double> th(n.theta, n.theta + n.n_theta), ph(n.phi, n.phi + n.n_phi);
@@ -299,6 +307,22 @@ int xfdtd_sim_read_nffft(xfdtd_sim *s, int which, double *out, int64_t len) {
 int xfdtd_sim_far_field(xfdtd_sim *s, int which, double *out, int64_t len) {
   if (!s || !s->sim) return XFDTD_ERR_STATE;
   return guarded(s, [&] {
+    if (dynamic_cast<const NffftBroadBand *>(s->sim->getNFFFT())) {
+      const auto ff = s->sim->broadbandFarField();
+      const std::vector<std::complex<double>> *cx[8] = {&ff.e_theta, &ff.e_phi, &ff.h_theta, &ff.h_phi,
+                                                       &ff.n_theta, &ff.n_phi, &ff.l_theta, &ff.l_phi};
+      const std::vector<double> *re[3] = {&ff.power_theta, &ff.power_phi, &ff.frequencies};
+      if (which >= 0 && which < 8) {
+        if (static_cast<size_t>(len) != 2 * cx[which]->size()) throw std::invalid_argument("length mismatch");
+        std::memcpy(out, cx[which]->data(), cx[which]->size() * sizeof(std::complex<double>));
+      } else if (which >= 8 && which <= 10) {
+        if (static_cast<size_t>(len) != re[which - 8]->size()) throw std::invalid_argument("length mismatch");
+        std::memcpy(out, re[which - 8]->data(), re[which - 8]->size() * sizeof(double));
+      } else {
+        throw std::invalid_argument("broadband far-field output must be 0..10");
+      }
+      return;
+    }
     if (which >= 0 && which < 8) {
       auto v = s->sim->farField(which);
       if (static_cast<size_t>(len) != 2 * v.size()) throw std::invalid_argument("length mismatch");

@@ -3,7 +3,8 @@
 // src/monitor/voltage_monitor.cpp:99-120, current_monitor.cpp:117-140;
 // TimeDomainFieldMonitor::outputData, src/monitor/field_monitor.cpp:91-122;
 // MovieMonitor::update, src/monitor/movie_monitor.cpp:46-59;
-// Network::outputData, src/network/network.cpp:27-60) and
+// Network::outputData, src/network/network.cpp:27-60;
+// NffftBroadBand::outputData, src/nffft/nffft_broadband.cpp:156-200) and
 // Simulation::checkRun (src/simulation/simulation.cpp:98-113).
 #include <cstdio>
 #include <filesystem>
@@ -123,6 +124,25 @@ void Simulation::outputData() {
       writeNpy(std::filesystem::path(_network->getOutputPath()) / ("s" + std::to_string(e.first) + ".npy"), st.data(),
                16, "<c16", {2, fr.size()});
     }
+  }
+  const NffftBroadBand *nbb = dynamic_cast<const NffftBroadBand *>(_nffft.get());
+  if (nbb && !nbb->getOutputDirPath().empty() && ensureDir(nbb->getOutputDirPath())) {
+    const std::filesystem::path out{nbb->getOutputDirPath()};
+    const auto ff = broadbandFarField();
+    const size_t N = ff.frequencies.size();
+    {   // outputFarFieldParameters (:466-476)
+      std::ofstream w{out / "far_field_parameter.dat"};
+      w << "Fs:\t" << 1 / _dt << '\n';
+      w << "number of samples:\t" << N << '\n';
+      w << "Theta:\n" << nbb->getTheta() << '\n';
+      w << "Phi:\n" << nbb->getPhi() << '\n';
+    }
+    writeNpy(out / "e_theta.npy", ff.e_theta.data(), 16, "<c16", {N});
+    writeNpy(out / "e_phi.npy", ff.e_phi.data(), 16, "<c16", {N});
+    writeNpy(out / "h_theta.npy", ff.h_theta.data(), 16, "<c16", {N});
+    writeNpy(out / "h_phi.npy", ff.h_phi.data(), 16, "<c16", {N});
+    writeNpy(out / "power_theta.npy", ff.power_theta.data(), 8, "<f8", {N});
+    writeNpy(out / "power_phi.npy", ff.power_phi.data(), 8, "<f8", {N});
   }
   const NffftFd *nfd = dynamic_cast<const NffftFd *>(_nffft.get());
   if (nfd && !nfd->getOutputDirPath().empty() && !nfd->getTheta().empty() && !nfd->getPhi().empty()) {

@@ -691,7 +691,23 @@ void Simulation::init(size_t total_time_steps) {
   // ---- NF-FF ------------------------------------------------------------
   std::vector<double> phase_j, phase_m, wave_number;
   const NffftFd *nfd = dynamic_cast<const NffftFd *>(_nffft.get());
-  if (_nffft && !nfd) throw std::runtime_error("only the frequency-domain NFFFT runs on the GPU engine");
+  const NffftBroadBand *nbb = dynamic_cast<const NffftBroadBand *>(_nffft.get());
+  const double bb_dir[2] = {nbb ? nbb->getTheta() : 0.0, nbb ? nbb->getPhi() : 0.0};
+  if (_nffft && !nfd && !nbb) throw std::runtime_error("unknown NFFFT type");
+  if (nbb) {   // NffftBroadBand::init (nffft_broadband.cpp:31-95): every step's samples
+    auto [dx_, dy_, dz_] = nbb->getDistance();
+    const size_t dist[3] = {dx_, dy_, dz_};
+    xfdtd_nffft_plan &np = plan.nffft;
+    np.enabled = 2;
+    for (int a = 0; a < 3; ++a) {
+      if (2 * dist[a] >= n_ax[a]) throw std::runtime_error("NF-FF box is empty");
+      np.lo[a] = static_cast<int64_t>(dist[a]);
+      np.hi[a] = static_cast<int64_t>(n_ax[a] - dist[a]);
+    }
+    np.n_theta = np.n_phi = 1;
+    np.theta = &bb_dir[0];
+    np.phi = &bb_dir[1];
+  }
   if (nfd) {
     auto [dx_, dy_, dz_] = nfd->getDistance();
     const size_t dist[3] = {dx_, dy_, dz_};
@@ -956,6 +972,49 @@ std::vector<std::complex<double>> Simulation::nffftAccumulator(int which) const 
   checkEngine(xfdtd_read_nffft(_engine, which, buf.data(), static_cast<int64_t>(buf.size())), _engine);
   std::vector<std::complex<double>> r(n);
   for (size_t q = 0; q < n; ++q) r[q] = {buf[2 * q], buf[2 * q + 1]};
+  return r;
+}
+
+BroadbandFarField Simulation::broadbandFarField() const {
+  const NffftBroadBand *nbb = dynamic_cast<const NffftBroadBand *>(_nffft.get());
+  if (!_engine || !nbb) throw std::runtime_error("no broadband NF-FF in this simulation");
+  const size_t N = 2 * _total - 1;
+  std::vector<std::complex<double>> aux(6 * N);
+  checkEngine(xfdtd_broadband_far_field(_engine, reinterpret_cast<double *>(aux.data()), static_cast<int64_t>(12 * N)),
+              _engine);
+  const std::complex<double> *n_x = &aux[0], *n_y = &aux[N], *n_z = &aux[2 * N], *l_x = &aux[3 * N],
+                             *l_y = &aux[4 * N], *l_z = &aux[5 * N];
+  BroadbandFarField r;
+  // calculateFarField (nffft_broadband.cpp:343-371)
+  const double fs = 1 / _dt;
+  const double step = (fs / 2 - (-fs / 2)) / static_cast<double>(N - 1);
+  r.frequencies.resize(N);
+  r.wave_number.resize(N);
+  for (size_t m = 0; m < N; ++m) {
+    r.frequencies[m] = -fs / 2 + step * static_cast<double>(m);
+    r.wave_number[m] = 2 * constant::PI * r.frequencies[m] / constant::C_0;
+  }
+  const double th = nbb->getTheta(), ph = nbb->getPhi();
+  const double ct = std::cos(th), st = std::sin(th), cp = std::cos(ph), sp = std::sin(ph);
+  using namespace std::complex_literals;
+  for (auto *v : {&r.n_theta, &r.n_phi, &r.l_theta, &r.l_phi, &r.e_theta, &r.e_phi, &r.h_theta, &r.h_phi}) v->resize(N);
+  r.power_theta.resize(N);
+  r.power_phi.resize(N);
+  const double eta = constant::ETA_0;
+  for (size_t m = 0; m < N; ++m) {
+    r.n_theta[m] = ct * cp * n_x[m] + ct * sp * n_y[m] - st * n_z[m];
+    r.n_phi[m] = -sp * n_x[m] + cp * n_y[m];
+    r.l_theta[m] = ct * cp * l_x[m] + ct * sp * l_y[m] - st * l_z[m];
+    r.l_phi[m] = -sp * l_x[m] + cp * l_y[m];
+    const double k = r.wave_number[m];
+    r.e_theta[m] = (-1i * k) * (eta * r.n_theta[m] + r.l_phi[m]) / (4 * constant::PI);
+    r.e_phi[m] = (1i * k) * (-eta * r.n_phi[m] + r.l_theta[m]) / (4 * constant::PI);
+    r.h_theta[m] = (1i * k) * (r.n_phi[m] - r.l_theta[m] / eta) / (4 * constant::PI);
+    r.h_phi[m] = (-1i * k) * (r.n_theta[m] + r.l_phi[m] / eta) / (4 * constant::PI);
+    const double coff = std::pow(k, 2) / (32 * constant::PI * constant::PI * eta);
+    r.power_theta[m] = coff * std::pow(std::abs(eta * r.n_theta[m] + r.l_phi[m]), 2);
+    r.power_phi[m] = coff * std::pow(std::abs(-eta * r.n_phi[m] + r.l_theta[m]), 2);
+  }
   return r;
 }
 

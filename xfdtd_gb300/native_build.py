@@ -36,12 +36,16 @@ def _nvcc() -> str:
 def cuda_cmd(out: str = CUDA_LIB, extra=()) -> list:
     srcs = [os.path.join(HERE, "csrc", f) for f in ("engine.cu", "nffft_noalloc.cu")]
     return [_nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-            *extra, "-o", out, *srcs]
+            *extra, "-o", out, *srcs, "-ldl"]
 
 
 def host_cmd() -> list:
     srcs = sorted(glob.glob(os.path.join(HERE, "host", "src", "*.cpp")))
-    return ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-Wall", "-Wno-unused-variable",
+    # no FMA contraction (GCC contracts by default on aarch64): the host
+    # arithmetic (coefficients, profiles, far-field post-processing) rounds
+    # as the reference's does, on either architecture
+    return ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", "-Wall",
+            "-Wno-unused-variable",
             "-I", os.path.join(HERE, "host", "include"), *srcs,
             "-L", LIB_DIR, "-lxfdtd_cuda", "-Wl,-rpath,$ORIGIN", "-o", HOST_LIB]
 

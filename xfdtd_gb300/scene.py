@@ -380,6 +380,22 @@ class NffftFd:
 
 
 @dataclass
+class NffftBroadBand:
+    """NffftBroadBand(distance_x, distance_y, distance_z, theta, phi,
+    output_dir_path), src/include/nffft/nffft_broadband.h:9-12: the far
+    field in one direction over the whole band of the run."""
+    distance_x: int
+    distance_y: int
+    distance_z: int
+    theta: float
+    phi: float
+    output_dir_path: str = ""
+
+    def arrays(self):
+        return (np.zeros(0, dtype=np.float64), np.array([float(self.theta)]), np.array([float(self.phi)]))
+
+
+@dataclass
 class _Lumped:
     cube: Cube
     orientation: int
@@ -513,7 +529,7 @@ class Scene:
     objects: List[object] = field(default_factory=list)
     boundaries: List[PML] = field(default_factory=list)
     tfsf: Optional[TFSF3D] = None
-    nffft: Optional[NffftFd] = None
+    nffft: Optional[object] = None   # NffftFd or NffftBroadBand
     lumped_elements: List[_Lumped] = field(default_factory=list)
     monitors: List[_Monitor] = field(default_factory=list)
     cfl: float = 0.99
@@ -543,7 +559,7 @@ class Scene:
         if self.nffft is not None:
             f, t, p = self.nffft.arrays()
             keep += [f, t, p]
-            d.nffft.enabled = 1
+            d.nffft.enabled = 2 if isinstance(self.nffft, NffftBroadBand) else 1
             d.nffft.distance[:] = [int(self.nffft.distance_x), int(self.nffft.distance_y),
                                    int(self.nffft.distance_z)]
             d.nffft.n_freq, d.nffft.n_theta, d.nffft.n_phi = len(f), len(t), len(p)
