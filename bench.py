@@ -157,12 +157,14 @@ def _peaks():
 
 # --------------------------------------------------------------- roofline ---
 # Entries timed on their own streams, concurrently with the main stream's:
-# the TFSF 1-D line, and the two kernels of each volume update (whose
+# the TFSF 1-D line, the NF-FF sampling (beside the TFSF H corrections when
+# its box lies inside the TFSF box), and the two kernels of each volume update (whose
 # main-stream entry, update_e / update_h, spans both).
 GRAPH_STEPS = 32        # steps per captured CUDA graph (4 NF-FF batches of 8)
 PROFILE_STEPS = 400     # steps of the profiled pass behind the kernel times
 
-SIDE_STREAM_KERNELS = ("tfsf_aux", "update_e_interior", "update_e_shell", "update_h_interior", "update_h_shell")
+SIDE_STREAM_KERNELS = ("tfsf_aux", "nffft", "update_e_interior", "update_e_shell", "update_h_interior",
+                       "update_h_shell")
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one E and
 # one H update on this workload in the wide decomposition, keyed by (entry,

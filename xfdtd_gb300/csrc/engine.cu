@@ -94,6 +94,10 @@ struct xfdtd_handle {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;            // the TFSF 1-D line runs here, forked and joined per step
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // NF-FF sampling beside the TFSF H corrections (its reads lie strictly
+  // inside the TFSF box, which the corrections' writes surround)
+  bool nf_beside_tfsf = false;
+  cudaEvent_t ev_nf_fork = nullptr, ev_nf_join = nullptr;
   cudaStream_t shell = nullptr;           // the volume shell kernels run here, beside the interior kernels
   cudaEvent_t ev_vfork[2] = {}, ev_vjoin[2] = {};
   std::vector<void *> allocs;
@@ -260,6 +264,8 @@ struct xfdtd_handle {
     for (auto e : ev_pool) cudaEventDestroy(e);
     for (void *p : allocs) cudaFree(p);
     if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_nf_fork) cudaEventDestroy(ev_nf_fork);
+    if (ev_nf_join) cudaEventDestroy(ev_nf_join);
     if (ev_join) cudaEventDestroy(ev_join);
     if (side) cudaStreamDestroy(side);
     for (int q = 0; q < 2; ++q) {
@@ -1092,9 +1098,9 @@ long long nffft_fold_blocks(const xfdtd_handle *h) {
 }
 
 template <typename T>
-void launch_nffft(xfdtd_handle *h) {
+void launch_nffft(xfdtd_handle *h, cudaStream_t st = nullptr) {
   const auto p = nf_params<T>(h);
-  xg::k_nffft<T><<<nffft_grid(h), dim3(32, 8, 1), 0, h->stream>>>(p);
+  xg::k_nffft<T><<<nffft_grid(h), dim3(32, 8, 1), 0, st ? st : h->stream>>>(p);
   XCHECK(cudaGetLastError());
 }
 
@@ -1236,6 +1242,17 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     }
     volume_pair<T, I>(h, false);
   }
+  // NF-FF sampling on the side stream beside the TFSF H corrections when
+  // their cells are disjoint; joined before the samples are folded
+  const bool nf_side = h->nffft && h->tfsf && h->nf_beside_tfsf;
+  if (nf_side) {
+    XCHECK(cudaEventRecord(h->ev_nf_fork, h->stream));
+    XCHECK(cudaStreamWaitEvent(h->side, h->ev_nf_fork, 0));
+    prof_begin(h, 4, h->side);
+    launch_nffft<T>(h, h->side);
+    prof_end(h, h->side);
+    XCHECK(cudaEventRecord(h->ev_nf_join, h->side));
+  }
   if (h->tfsf) {
     XCHECK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
     const auto sp = tfsf_surf_params<T>(h);
@@ -1247,9 +1264,13 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     prof_end(h);
   }
   if (h->nffft) {
-    prof_begin(h, 4);
-    launch_nffft<T>(h);
-    prof_end(h);
+    if (nf_side) {
+      XCHECK(cudaStreamWaitEvent(h->stream, h->ev_nf_join, 0));
+    } else {
+      prof_begin(h, 4);
+      launch_nffft<T>(h);
+      prof_end(h);
+    }
     if (h->nf_bb) {   // broadband: the samples stay, one row per step
       h->nf_done = s + 1;
     } else if ((s + 1) % h->nf_batch == 0) {   // the batch is full: fold it
@@ -1371,6 +1392,8 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   XCHECK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
   XCHECK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
   XCHECK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+  XCHECK(cudaEventCreateWithFlags(&h->ev_nf_fork, cudaEventDisableTiming));
+  XCHECK(cudaEventCreateWithFlags(&h->ev_nf_join, cudaEventDisableTiming));
   {
     // the shell launch is the pair's long pole: its blocks go first as the
     // interior's retire
@@ -1570,6 +1593,12 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
       for (int q = 0; q < 2; ++q) h->ff_power[q] = h->alloc<double>(dirs);
     }
   }
+
+  // the NF-FF samples read [lo-1, hi] per axis; the TFSF H corrections write
+  // cells on the surface of [lo-1, hi] of the TFSF box
+  h->nf_beside_tfsf = h->nffft && h->tfsf;
+  for (int a = 0; a < 3 && h->nf_beside_tfsf; ++a)
+    if (!(h->nf_lo[a] > h->tf_lo[a] && h->nf_hi[a] < h->tf_hi[a])) h->nf_beside_tfsf = false;
 
   // sparse work
   h->n_waveforms = pl->n_waveforms;
