@@ -36,11 +36,12 @@
 // (inside the row padding) is zeroed by hand, as the general path does.
 //
 // Tile rows start on 16-byte boundaries as TMA requires: the engine offers
-// these kernels only when the interior's k range starts on one (see
-// interior_tma_ok in engine.cu), and the rows of the E kernel's H tile
-// start HOFF+1 cells before k0, widened to whole 16-byte rows.  Waits on a
-// stage are bounded; a block that gives up reports XFDTD_ERR_TIMEOUT
-// through the status word and stops.
+// these kernels only when the interior's k range starts on one, and (for
+// modes 1 and 2) when the k after its last does too (interior_tma_setup in
+// engine.cu); the rows of the E kernel's H tile start HOFF+1 cells before
+// k0, widened to whole 16-byte rows.  Waits on a stage are bounded; a block
+// that gives up reports XFDTD_ERR_TIMEOUT through the status word and
+// stops.
 #pragma once
 
 #include "common.cuh"
