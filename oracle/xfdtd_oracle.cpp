@@ -1356,22 +1356,30 @@ void oracle_sim::broadbandFarField() {
   const double ci = static_cast<double>(f.li + f.bx / 2), cj = static_cast<double>(f.lj + f.by / 2),
                ck = static_cast<double>(f.lk + f.bz / 2);   // GridBox::getGridCenterIndex
   std::vector<cplx> nx_(N), ny_(N), nz_(N), lx_(N), ly_(N), lz_(N);
-  std::vector<cplx> xa(N), xb(N), xc(N), xd(N);
   // one face: series (ja, jb, ma, mb) = samples[w0 .. w0+3] at face cells;
-  // pos(a, b) gives the cell's (x, y, z) index offsets from the centre
+  // pos(a, b) gives the cell's (x, y, z) index offsets from the centre.
+  // The spectra are taken in parallel; the sums run in the reference's
+  // cell order.
   auto face = [&](int w0, size_t da, size_t db, double ds, std::vector<cplx> &na, std::vector<cplx> &nb,
                   std::vector<cplx> &la, std::vector<cplx> &lb, auto pos) {
     const size_t plane = da * db;
+    std::vector<cplx> spec(plane * 4 * N);
+#pragma omp parallel for schedule(dynamic)
+    for (long long c = 0; c < static_cast<long long>(plane); ++c) {
+      std::vector<cplx> tmp(N);
+      for (int q = 0; q < 4; ++q) {
+        spectrum(f.samples[w0 + q], static_cast<size_t>(c), plane, tmp);
+        std::copy(tmp.begin(), tmp.end(), spec.begin() + (static_cast<size_t>(c) * 4 + q) * N);
+      }
+    }
     for (size_t a = 0; a < da; ++a)
       for (size_t b = 0; b < db; ++b) {
         double x, y, z;
         pos(a, b, x, y, z);
         const double delay = x * ffv[0] * dl3[0] + y * ffv[1] * dl3[1] + z * ffv[2] * dl3[2];
         const size_t cell = a * db + b;
-        spectrum(f.samples[w0], cell, plane, xa);
-        spectrum(f.samples[w0 + 1], cell, plane, xb);
-        spectrum(f.samples[w0 + 2], cell, plane, xc);
-        spectrum(f.samples[w0 + 3], cell, plane, xd);
+        const cplx *xa = &spec[(cell * 4 + 0) * N], *xb = &spec[(cell * 4 + 1) * N], *xc = &spec[(cell * 4 + 2) * N],
+                   *xd = &spec[(cell * 4 + 3) * N];
         for (size_t m = 0; m < N; ++m) {
           const cplx phase = std::exp(1i * delay * k[m]);
           na[m] += ds * phase * xa[m];
