@@ -157,6 +157,15 @@ def two_port(steps=160):
     return sc, steps
 
 
+def broadband(steps=80):
+    """The small PEC-sphere scene with an NffftBroadBand in an oblique
+    direction in place of its NffftFd."""
+    sc, _ = configs.pec_sphere_rcs(scale=2, steps=steps)
+    nf = sc.nffft
+    sc.nffft = S.NffftBroadBand(nf.distance_x, nf.distance_y, nf.distance_z, 0.3, 0.7)
+    return sc, steps
+
+
 def _six(t):
     return [S.PML(o, t) for o in (S.XN, S.XP, S.YN, S.YP, S.ZN, S.ZP)]
 
@@ -191,6 +200,14 @@ SPLIT_SCENES = {
     "pec_box": pec_box,
     "long_z": long_z,
     "one_sided": one_sided,
+}
+
+
+# scenes of the output formats (field and movie monitors, the broadband NF-FF),
+# with golden vectors of their own
+OUTPUT_SCENES = {
+    "field_monitors": field_monitors,
+    "broadband": broadband,
 }
 
 

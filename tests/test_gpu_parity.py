@@ -475,16 +475,6 @@ def test_network_s_parameters(tmp_path):
         assert np.array_equal(a[0].real, np.asarray(sc.network.frequencies)) and np.array_equal(a[1], got[key])
 
 
-def _broadband_scene(steps=80):
-    """The small PEC-sphere scene with an NffftBroadBand in an oblique
-    direction in place of its NffftFd."""
-    from xfdtd_gb300 import configs
-    sc, _ = configs.pec_sphere_rcs(scale=2, steps=steps)
-    nf = sc.nffft
-    sc.nffft = S.NffftBroadBand(nf.distance_x, nf.distance_y, nf.distance_z, 0.3, 0.7)
-    return sc, steps
-
-
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_broadband_nffft_far_field(precision, tmp_path):
     """NffftBroadBand (nffft_broadband.cpp): every step's surface samples
@@ -493,7 +483,7 @@ def test_broadband_nffft_far_field(precision, tmp_path):
     bin frequencies exactly, e/h theta/phi, n/l theta/phi and the powers
     within 1e-10 of each array's largest value in FP64 (1e-3 in the FP32
     form); outputData writes the six arrays and far_field_parameter.dat."""
-    sc, st = _broadband_scene(steps=80)
+    sc, st = scenes.broadband(steps=80)
     sc.nffft.output_dir_path = str(tmp_path / "bb")
     o = O.OracleSim(sc, st)
     o.step(st)

@@ -158,6 +158,27 @@ def test_oracle_matches_golden(name):
             np.testing.assert_allclose(o.far_field(w), g[f"ff{w}"], rtol=1e-10, atol=1e-30)
 
 
+@pytest.mark.parametrize("name", sorted(scenes.OUTPUT_SCENES))
+def test_oracle_output_formats_match_golden(name):
+    """Every frame of the field and movie monitors and the broadband far
+    field against their golden vectors."""
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    sc, _ = scenes.OUTPUT_SCENES[name]()
+    steps = int(g["steps"])
+    o = O.OracleSim(sc, steps)
+    o.step(steps)
+    for m, mon in enumerate(sc.monitors):
+        if mon.kind != S.MONITOR_FIELD:
+            continue
+        _, _, frames = o.field_monitor_frames(m)
+        assert frames == list(g[f"steps{m}"])
+        for f in range(len(frames)):
+            np.testing.assert_allclose(o.read_field_monitor(m, f), g[f"mon{m}_{f}"], rtol=1e-12, atol=1e-30)
+    if sc.nffft is not None:
+        for w in (0, 1, 8, 10):
+            np.testing.assert_allclose(o.far_field(w), g[f"ff{w}"], rtol=1e-10, atol=1e-30)
+
+
 def test_scene_description_round_trip():
     sc, st = scenes.lumped(steps=3)
     d = sc.desc()
