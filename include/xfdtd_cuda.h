@@ -263,6 +263,18 @@ int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant);
  * (XFDTD_ERR_INVALID_PLAN otherwise). */
 int xfdtd_shell_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h);
 int xfdtd_set_shell_variant(xfdtd_handle *h, int e_variant, int h_variant);
+/* Failure detection of the TMA-staged volume launches.  No counterpart in
+ * the reference (a single-threaded CPU loop has no device waits).  Each
+ * block of those launches waits on an mbarrier for every plane its loads
+ * bring in, polling at most `polls` times (default and maximum 2^22);
+ * a block that gives up stops, waits (with the full 2^22 polls) for the
+ * copies it issued, and sets XFDTD_ERR_TIMEOUT in the handle's status word,
+ * which the next xfdtd_synchronize returns.  The fields are then not
+ * advanced consistently and the handle should be destroyed; the device
+ * context stays usable.  polls = 0 makes every plane wait give up at once
+ * (the failure path's test).  Applies to launches enqueued after the call
+ * (a captured step graph is recaptured). */
+int xfdtd_set_wait_limit(xfdtd_handle *h, int64_t polls);
 /* Cells of the split volume update: cells[0] / [1] the E update's interior
  * (plain on every axis, the interior kernel) and shell (walls and CPML
  * slabs, the shell kernel); cells[2] / [3] the same for H. */
@@ -357,16 +369,25 @@ void xfdtd_batch_destroy(xfdtd_batch *b);
  * allocation and call no allocating library.
  *
  * Call xfdtd_nffft_noalloc_setup(device) once per device before the first
- * operator call and before any stream capture begins: it makes the device
- * current and looks up the scratch address.  Each operator call samples
- * step `step` (fields as they stand after that step's H update) into slot
- * step % batch and, if fold_count > 0, folds steps step-fold_count+1 ..
- * step (all sampled earlier through this operator on this device) into
- * acc[].  The accumulators must start at zero.  The scratch is shared by
- * all calls on a device: calls that overlap in time race on it.  A batch
- * larger than the scratch (batch * 24 * largest face * element size) is
- * rejected with XFDTD_ERR_INVALID_PLAN.  Launches are asynchronous on
- * `stream`; errors: xfdtd_nffft_noalloc_last_error(). */
+ * operator call and before any stream capture begins: it looks up the
+ * scratch address and leaves `device` current; an operator call before it
+ * returns XFDTD_ERR_STATE.  Each operator call makes op->device current for
+ * its launches only and puts the caller's current device back before it
+ * returns.  It samples step `step` (fields as they stand after that step's
+ * H update) into slot step % batch and, if fold_count > 0, folds steps
+ * step-fold_count+1 .. step into acc[].  Those steps must have been
+ * sampled through this operator on this device, one call per step in an
+ * unbroken run, with the same batch, box and precision: a call that
+ * changes any of them, or skips a step, starts a new run, and a fold that
+ * reaches back before its run's first step is rejected with
+ * XFDTD_ERR_INVALID_PLAN.  The accumulators must start at zero.  The
+ * scratch is one array shared by all calls on a device, resident on every
+ * device that loads this library: calls that overlap in time on a device
+ * race on it, so callers serialise them.  A batch larger than the scratch
+ * (batch * 24 * largest face * element size), a grid axis above 2^30
+ * cells or a box edge above 524,280 cells is rejected with
+ * XFDTD_ERR_INVALID_PLAN before any device call.  Launches are asynchronous
+ * on `stream`; errors: xfdtd_nffft_noalloc_last_error(). */
 typedef struct xfdtd_nffft_operator {
   int32_t precision;        /* XFDTD_FP64 or XFDTD_FP32: element type of fields */
   int32_t device;           /* CUDA device ordinal the pointers live on         */

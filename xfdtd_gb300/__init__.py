@@ -95,6 +95,7 @@ def libs():
         cu.xfdtd_volume_decomposition.argtypes = [C.c_void_p, P(C.c_int)]
         cu.xfdtd_shell_variants.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int)]
         cu.xfdtd_set_shell_variant.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        cu.xfdtd_set_wait_limit.argtypes = [C.c_void_p, C.c_int64]
         cu.xfdtd_last_error.argtypes = [C.c_void_p]
         cu.xfdtd_last_error.restype = C.c_char_p
         cu.xfdtd_version.restype = C.c_char_p
@@ -376,6 +377,11 @@ class Simulation:
 
     def set_shell_variant(self, e_variant: int, h_variant: int):
         self._check_engine(libs()[0].xfdtd_set_shell_variant(self.engine, int(e_variant), int(h_variant)))
+
+    def set_wait_limit(self, polls: int):
+        """Polls of each TMA plane wait before a block gives up and reports a
+        timeout (default and maximum 2^22; 0 gives up at once)."""
+        self._check_engine(libs()[0].xfdtd_set_wait_limit(self.engine, int(polls)))
 
     def volume_split(self) -> dict:
         """Cells of the interior and shell launches of the E and H updates,

@@ -159,6 +159,7 @@ struct xfdtd_handle {
 
   long long *d_step = nullptr;
   int *d_status = nullptr;
+  int wait_polls = xg::kItWaitLimit;   // polls of a TMA plane wait before a block gives up
   int *d_flag = nullptr;
 
   // host copies kept for the adjoint: the coefficient table (FP64) and the
@@ -874,10 +875,10 @@ void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, 
   dim3 grid(nkt, (nj + xg::kItJ - 1) / xg::kItJ, (ni + chunk - 1) / chunk);
   if (e_side)
     xg::k_interior_tma_e<T, I, S, CT, MODE>
-        <<<grid, xg::kItThreads, G::template smem_e<S>(), st>>>(h->itm[0], p, in, chunk, h->d_status);
+        <<<grid, xg::kItThreads, G::template smem_e<S>(), st>>>(h->itm[0], p, in, chunk, h->d_status, h->wait_polls);
   else
     xg::k_interior_tma_h<T, I, S, CT, MODE>
-        <<<grid, xg::kItThreads, G::template smem_h<S>(), st>>>(h->itm[1], p, in, chunk, h->d_status);
+        <<<grid, xg::kItThreads, G::template smem_h<S>(), st>>>(h->itm[1], p, in, chunk, h->d_status, h->wait_polls);
 }
 
 // After a sweep the second buffer set holds step t+1: make it current.
@@ -1365,7 +1366,7 @@ void check_status(xfdtd_handle *h) {
   int st = 0;
   XCHECK(cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   XCHECK(cudaStreamSynchronize(h->stream));
-  if (st == XFDTD_ERR_TIMEOUT) throw Err{XFDTD_ERR_TIMEOUT, "a bounded wait of the fused sweep gave up"};
+  if (st == XFDTD_ERR_TIMEOUT) throw Err{XFDTD_ERR_TIMEOUT, "a bounded device wait gave up (TMA plane stage)"};
   if (st != 0) throw Err{XFDTD_ERR_DEVICE_CHECK, "device status " + std::to_string(st) + " (step index past the plan)"};
 }
 
@@ -2225,6 +2226,18 @@ int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant) {
     for (int side = 0; side < 2; ++side)   // a z-edge shell variant needs the wide decomposition
       if (!shell_allowed(h, kShellVariants[h->shell_var[side]], side_wide(h, side))) h->shell_var[side] = 0;
     if (h->gexec) {   // the captured graph holds the old launches
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+    }
+  });
+}
+
+int xfdtd_set_wait_limit(xfdtd_handle *h, int64_t polls) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    if (polls < 0 || polls > xg::kItWaitLimit) invalid("wait limit out of range (0 .. 2^22 polls)");
+    h->wait_polls = static_cast<int>(polls);
+    if (h->gexec) {   // the captured graph holds the old launch parameters
       cudaGraphExecDestroy(h->gexec);
       h->gexec = nullptr;
     }

@@ -123,14 +123,20 @@ __device__ __forceinline__ ItBlock it_block(const InteriorBox &in, int chunk) {
 // waits).  A wait that gives up marks the block timed out; the block then
 // stops, and thread 0 waits (bounded) for the loads it issued before the
 // block exits, so that no copy lands in a finished block's shared memory.
+//
+// The plane waits poll at most `limit` times (kItWaitLimit unless the handle
+// lowered it, xfdtd_set_wait_limit; 0 gives up at once, which is how the
+// failure path is tested).  The drain of copies in flight always polls up
+// to kItWaitLimit.
 template <int STAGES>
 struct ItRing {
   uint64_t *bar;
+  int limit = kItWaitLimit;
   unsigned phase = 0;   // bit s: parity of the next completion of stage s
   bool timed_out = false;
   __device__ bool wait(int st) {
     if (timed_out) return false;
-    if (!mbar_wait_bounded(&bar[st], (phase >> st) & 1u, kItWaitLimit)) {
+    if (!mbar_wait_bounded(&bar[st], (phase >> st) & 1u, limit)) {
       timed_out = true;
       return false;
     }
@@ -141,10 +147,11 @@ struct ItRing {
 
 template <typename T, typename I, int STAGES, bool CT, int MODE>
 __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
-                                                               InteriorBox in, int chunk, int *status) {
+                                                               InteriorBox in, int chunk, int *status,
+                                                               int wait_limit) {
   using G = ItTiles<T, I>;
   extern __shared__ __align__(128) unsigned char smem[];
-  ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::E_STAGE)};
+  ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::E_STAGE), wait_limit};
   const int tid = threadIdx.x, c = tid & 31, r = tid >> 5;
   const ItBlock blk = it_block<MODE>(in, chunk);
   if (blk.ia >= blk.ib) return;
@@ -248,6 +255,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
   if (tid == 0) {
     const bool failed = ring.timed_out;
     ring.timed_out = false;
+    ring.limit = kItWaitLimit;
     for (int q = waited + 1; q <= issued; ++q) ring.wait(stage_of(q));   // copies still in flight
     if (failed || ring.timed_out) atomicExch(status, static_cast<int>(4));   // XFDTD_ERR_TIMEOUT
   }
@@ -255,10 +263,11 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
 
 template <typename T, typename I, int STAGES, bool CT, int MODE>
 __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
-                                                               InteriorBox in, int chunk, int *status) {
+                                                               InteriorBox in, int chunk, int *status,
+                                                               int wait_limit) {
   using G = ItTiles<T, I>;
   extern __shared__ __align__(128) unsigned char smem[];
-  ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::H_STAGE)};
+  ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::H_STAGE), wait_limit};
   const int tid = threadIdx.x, c = tid & 31, r = tid >> 5;
   const ItBlock blk = it_block<MODE>(in, chunk);
   if (blk.ia >= blk.ib) return;
@@ -360,6 +369,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
   if (tid == 0) {
     const bool failed = ring.timed_out;
     ring.timed_out = false;
+    ring.limit = kItWaitLimit;
     for (int q = waited + 1; q <= issued; ++q) ring.wait(stage_of(q));
     if (failed || ring.timed_out) atomicExch(status, static_cast<int>(4));   // XFDTD_ERR_TIMEOUT
   }

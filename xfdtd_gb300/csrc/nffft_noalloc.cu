@@ -41,7 +41,25 @@ constexpr size_t kScratchBytes = 64ull << 20;
 static __device__ __align__(256) unsigned char g_nffft_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
+
+// What the slots of a device's scratch were written with: the batch, the
+// box and the element size fix where each step's samples sit.  `first` is
+// the earliest step sampled with this layout in an unbroken run of steps
+// and `last` the latest; a fold may only reach back to `first`.
+struct Layout {
+  int batch = 0, esize = 0;
+  long long lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  long long first = -1, last = -1;
+  bool same(int b, int e, const long long *l, const long long *h) const {
+    if (b != batch || e != esize) return false;
+    for (int a = 0; a < 3; ++a)
+      if (l[a] != lo[a] || h[a] != hi[a]) return false;
+    return true;
+  }
+};
+
 void *g_scratch_ptr[kMaxDevices] = {};
+Layout g_layout[kMaxDevices];
 std::mutex g_scratch_mu;
 thread_local char g_err[256];
 
@@ -53,7 +71,7 @@ int fail(int code, const char *msg) {
 
 // Device address of the scratch array on `dev`, looked up once per device
 // with that device current (host code must not use the symbol itself: on
-// the host it is only a stand-in).
+// the host it is only a stand-in).  Leaves `dev` current.
 int scratch_on_device(int dev, void **out) {
   if (dev < 0 || dev >= kMaxDevices) return fail(XFDTD_ERR_INVALID_PLAN, "device ordinal out of range");
   if (cudaSetDevice(dev) != cudaSuccess) return fail(XFDTD_ERR_CUDA, "cudaSetDevice failed");
@@ -67,6 +85,48 @@ int scratch_on_device(int dev, void **out) {
   *out = g_scratch_ptr[dev];
   return XFDTD_OK;
 }
+
+// Records that `step` is sampled with this layout on `dev` and checks that
+// the fold's steps (fold_count of them, ending at `step`) were all sampled
+// with it, in an unbroken run.  A call with another batch, box or precision
+// starts a new run: the slots written before it hold another layout.
+int claim_layout(int dev, int batch, int esize, const long long *lo, const long long *hi, long long step,
+                 int fold_count) {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  Layout &L = g_layout[dev];
+  if (!L.same(batch, esize, lo, hi) || step != L.last + 1) {
+    if (fold_count > 1)
+      return fail(XFDTD_ERR_INVALID_PLAN,
+                  "fold reaches steps not sampled with this batch, box and precision in an unbroken run");
+    L.batch = batch;
+    L.esize = esize;
+    for (int a = 0; a < 3; ++a) L.lo[a] = lo[a], L.hi[a] = hi[a];
+    L.first = step;
+  } else if (step - fold_count + 1 < L.first) {
+    return fail(XFDTD_ERR_INVALID_PLAN,
+                "fold reaches steps not sampled with this batch, box and precision in an unbroken run");
+  }
+  L.last = step;
+  return XFDTD_OK;
+}
+
+// Makes `dev` current for the launches and puts the caller's device back on
+// every exit path.
+struct DeviceScope {
+  int prev = -1;
+  bool changed = false;
+  int enter(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) return fail(XFDTD_ERR_CUDA, "cudaGetDevice failed");
+    if (prev != dev) {
+      if (cudaSetDevice(dev) != cudaSuccess) return fail(XFDTD_ERR_CUDA, "cudaSetDevice failed");
+      changed = true;
+    }
+    return XFDTD_OK;
+  }
+  ~DeviceScope() {
+    if (changed) cudaSetDevice(prev);
+  }
+};
 
 template <typename T>
 struct OpParams {
@@ -190,6 +250,10 @@ template <typename T>
 int run(const xfdtd_nffft_operator *op) {
   OpParams<T> p{};
   const long long n[3] = {op->nx, op->ny, op->nz};
+  // the kernels index planes, rows and columns with int, and the sample
+  // launch covers the box's longest edge with 8 rows per block on grid.y
+  for (int a = 0; a < 3; ++a)
+    if (n[a] < 3 || n[a] > (1ll << 30)) return fail(XFDTD_ERR_INVALID_PLAN, "grid size out of range (3 .. 2^30 cells per axis)");
   for (int a = 0; a < 3; ++a) {
     if (op->lo[a] < 1 || op->hi[a] <= op->lo[a] || op->hi[a] > n[a] - 1)
       return fail(XFDTD_ERR_INVALID_PLAN, "NF-FF box outside the grid");
@@ -211,6 +275,8 @@ int run(const xfdtd_nffft_operator *op) {
   p.plane[2] = bx * by;
   p.max_plane = p.plane[0] > p.plane[1] ? p.plane[0] : p.plane[1];
   if (p.plane[2] > p.max_plane) p.max_plane = p.plane[2];
+  const long long m = bx > by ? (bx > bz ? bx : bz) : (by > bz ? by : bz);
+  if (m > 8ll * 65535) return fail(XFDTD_ERR_INVALID_PLAN, "NF-FF box edge above 524,280 cells");
   if (op->batch < 1 || op->n_freq < 1 || op->total_steps < 1 || op->step < 0 || op->step >= op->total_steps)
     return fail(XFDTD_ERR_INVALID_PLAN, "batch, n_freq, total_steps and step must be positive and in range");
   if (op->fold_count < 0 || op->fold_count > op->batch || op->fold_count > op->step + 1)
@@ -229,13 +295,22 @@ int run(const xfdtd_nffft_operator *op) {
   p.total = op->total_steps;
   p.batch = op->batch;
   p.step = op->step;
+  if (op->device < 0 || op->device >= kMaxDevices) return fail(XFDTD_ERR_INVALID_PLAN, "device ordinal out of range");
   void *scratch = nullptr;
-  const int rc = scratch_on_device(op->device, &scratch);
+  {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    scratch = g_scratch_ptr[op->device];
+  }
+  if (!scratch) return fail(XFDTD_ERR_STATE, "call xfdtd_nffft_noalloc_setup(device) before the first operator call");
+  const long long lo[3] = {op->lo[0], op->lo[1], op->lo[2]}, hi[3] = {op->hi[0], op->hi[1], op->hi[2]};
+  int rc = claim_layout(op->device, op->batch, static_cast<int>(sizeof(T)), lo, hi, op->step, op->fold_count);
+  if (rc != XFDTD_OK) return rc;
+  DeviceScope scope;
+  rc = scope.enter(op->device);
   if (rc != XFDTD_OK) return rc;
   p.buf = static_cast<T *>(scratch);
   cudaStream_t st = static_cast<cudaStream_t>(op->stream);
   // face 0 spans (k, j), face 1 (i, k), face 2 (j, i): cover the longest edge on both grid axes
-  const long long m = bx > by ? (bx > bz ? bx : bz) : (by > bz ? by : bz);
   dim3 block(32, 8, 1);
   dim3 grid(static_cast<unsigned>((m + 31) / 32), static_cast<unsigned>((m + 7) / 8), 3);
   k_sample<T><<<grid, block, 0, st>>>(p);
