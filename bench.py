@@ -14,10 +14,19 @@ flush is needed between steps.
 
 A step is one time step of the loop body over the whole grid.  value =
 (cells x steps x ranks) / max-over-ranks device time of the K timed steps
-(CUDA events on the engine's stream).  e2e = the same metric over one whole
-job through the public API (host scene -> plan -> upload, K steps, far field
-and RCS copied back), wall clock.  With --gpus N > 1 (torchrun), every rank
-runs an independent replica of the workload (the path has no exchange).
+(CUDA events on the engine's stream).  e2e = the same metric over the
+config's whole job (2000 steps) through the public API -- host scene ->
+plan lowering -> device allocation and upload -> autotuning -> steps -> far
+field and RCS copied back to the host -- wall clock, with each phase's
+time.  With --gpus N > 1 (torchrun), every rank runs an independent replica
+of the workload (the path has no exchange).
+
+The same line carries the FP64 form (the reference's arithmetic) of the
+same workload, the heterogeneous-medium configuration (532 x 532 x 404
+cells) in FP32 and FP64, the batched and the adjoint forms, each with its
+own roofline and (where it is a whole job) end-to-end figures, and the
+FP32 form's error against the FP64 form on the same jobs.  GPU clocks are
+sampled by nvidia-smi over the whole run.
 
 --impl reference times the reference's algorithm on the host cores: the
 reference cannot be built here (xtensor, xtensor-blas, xtensor-fftw, FFTW3,
@@ -392,150 +401,239 @@ def run_adjoint_form(args, local):
     return out
 
 
+def _timed(sc, precision, steps, warmup, local, grp=None, fused=False, variants=None):
+    """The production path over `steps` timed steps: after `warmup` steps
+    the run is brought to a graph boundary (untimed steps, one graph
+    captured and replayed), then exactly `steps` steps are timed with CUDA
+    events on the engine's stream (graph replays of GRAPH_STEPS steps,
+    single launches for the rest).  Returns the run's facts."""
+    import xfdtd_gb300 as X
+    setup = GRAPH_STEPS - warmup % GRAPH_STEPS + GRAPH_STEPS
+    sim = X.Simulation(sc, warmup + setup + steps, precision=precision, graph=True, device=local, fused=fused)
+    if variants:
+        sim.set_kernel_variant(*variants[0])
+        sim.set_shell_variant(*variants[1])
+    n = sim.n
+    sim.step(warmup)
+    sim.step(setup)
+    sim.synchronize()
+    l0 = sim.launch_count()
+    if grp is not None:
+        grp.barrier()
+    ms = sim.step_timed(steps)
+    sim.synchronize()
+    if grp is not None:
+        grp.barrier()
+    out = {"n": tuple(n), "cells": n[0] * n[1] * n[2], "ms": ms, "launches": sim.launch_count() - l0,
+           "variants": sim.kernel_variants(), "shell_variants": sim.shell_variants(), "split": sim.volume_split(),
+           "setup_steps": setup,
+           "timed_path": f"{steps // GRAPH_STEPS} CUDA graph replays of {GRAPH_STEPS} steps + "
+                         f"{steps % GRAPH_STEPS} single steps, after {warmup} warm-up steps and {setup} untimed "
+                         f"steps to reach a graph boundary and capture the graph"}
+    sim.check_finite()
+    del sim
+    return out
+
+
+def _profiled(sc, precision, steps, warmup, local, run, fused=False):
+    """Per-kernel device times of `steps` steps with CUDA events around every
+    launch (no graph), with the timed run's variants, and the roofline of
+    the dominant main-stream entry (algorithmic bytes / its mean time)."""
+    import xfdtd_gb300 as X
+    psim = X.Simulation(sc, warmup + steps, precision=precision, graph=False, profile=True, device=local,
+                        fused=fused)
+    psim.set_kernel_variant(run["variants"]["e"], run["variants"]["h"])
+    psim.set_shell_variant(run["shell_variants"]["e"], run["shell_variants"]["h"])
+    assert psim.volume_split() == run["split"]
+    psim.step(warmup)
+    psim.synchronize()
+    psim.profile_reset()
+    total_ms = psim.step_timed(steps)
+    prof = psim.profile()
+    del psim
+    side = {k: prof.pop(k) for k in SIDE_STREAM_KERNELS if k in prof}
+    dom = dominant(prof)
+    dom_ms, dom_n = prof[dom]
+    slabs = _slab_layers(sc)
+    n, split = run["n"], run["split"]
+    alg = algorithmic_bytes(n, slabs, precision, dom, split)
+    peak, peak_kind = _peaks()
+    achieved = alg / (dom_ms / dom_n / 1e3) / 1e9
+    total_prof = sum(v[0] for v in prof.values())
+    shares = {k: round(v[0] / total_prof, 4) for k, v in prof.items()}
+    shares.update({f"{k} (concurrent)": round(v[0] / total_prof, 4) for k, v in side.items()})
+    concurrent = {k: {"ms_per_launch": v[0] / max(v[1], 1),
+                      "algorithmic_GBs": algorithmic_bytes(n, slabs, precision, k, split) / (v[0] / max(v[1], 1) / 1e3) / 1e9}
+                  for k, v in side.items() if k.startswith("update_")}
+    # both volume updates over the whole profiled step: 2 x the pair's bytes
+    # per step over the step time (the small surface launches included)
+    pair = algorithmic_bytes(n, slabs, precision, "update_e", split) + algorithmic_bytes(n, slabs, precision, "update_h", split)
+    step_frac = pair / (total_ms / steps / 1e3) / 1e9 / peak
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind,
+            "traffic": NCU_TRAFFIC.get((dom, precision, tuple(n), split.get(dom[7] + "_wide"))),
+            "algorithmic_bytes_per_launch": alg, "launch_ms": dom_ms / dom_n,
+            "step_frac": step_frac,
+            "timing": f"CUDA events around each launch in a profiled pass of {steps} steps "
+                      f"({total_ms / steps:.4f} ms/step, no graph)"}
+    return roof, shares, concurrent
+
+
+def _e2e(sc, precision, steps, local, fused=False, readout="rcs"):
+    """One whole job through the public API (the reference's
+    Simulation(...); run(steps); outputs): host scene -> plan (lowering on
+    the host) -> engine create (device allocation, upload, autotuning) ->
+    `steps` steps -> far field / monitors copied back to the host.  Wall
+    clock per phase."""
+    import xfdtd_gb300 as X
+    t0 = time.perf_counter()
+    job = X.Simulation(sc, steps, precision=precision, graph=True, device=local, fused=fused)
+    t1 = time.perf_counter()
+    ct = job.create_times()
+    job.step(steps)
+    job.synchronize()
+    t2 = time.perf_counter()
+    if readout == "rcs":
+        result = job.rcs_db()
+    else:
+        result = np.stack([job.read_monitor(m) for m in range(len(sc.monitors))])
+    t3 = time.perf_counter()
+    h2d, d2h = job.transfer_bytes()
+    n = job.n
+    del job
+    assert np.isfinite(result).all()
+    cells = n[0] * n[1] * n[2]
+    wall = t3 - t0
+    create_s = t1 - t0
+    phases = {"lowering_s": create_s - (ct["alloc_upload_ms"] + ct["autotune_ms"]) / 1e3,
+              "alloc_upload_s": ct["alloc_upload_ms"] / 1e3, "autotune_s": ct["autotune_ms"] / 1e3,
+              "steps_s": t2 - t1, "readout_s": t3 - t2}
+    e2e = {"value": cells * steps / wall / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d / steps,
+           "d2h_bytes_per_step": d2h / steps, "wall_s": wall, "steps": steps, "phases": phases,
+           "scope": "host scene -> plan lowering -> device allocation and upload -> autotuning -> "
+                    f"{steps} steps (CUDA graph replay) -> "
+                    + ("far field and RCS copied to the host" if readout == "rcs" else "probe series copied to the host")}
+    return e2e, result
+
+
+def _rcs_err(a, b):
+    d = np.abs(a - b)
+    return {"rcs_db_max": float(d.max()), "rcs_db_median": float(np.median(d))}
+
+
+def _probe_err(a, b):
+    rel = np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+    return {"probe_l2_max": float(rel.max()), "probe_l2_median": float(np.median(rel))}
+
+
+def run_fp64_form(args, local, sc, steps, fp32_rcs):
+    """The FP64 form (the reference's arithmetic) on the same workload:
+    timed steps, kernel roofline at 146 B per cell-update, a whole job end
+    to end, and the FP32 form's RCS error against it."""
+    run = _timed(sc, "fp64", args.fp64_steps, args.warmup, local)
+    roof, shares, _ = _profiled(sc, "fp64", min(args.fp64_steps, PROFILE_STEPS), args.warmup, local, run)
+    e2e, rcs64 = _e2e(sc, "fp64", steps, local)
+    return {"value": run["cells"] * args.fp64_steps / (run["ms"] / 1e3) / 1e6, "unit": UNIT,
+            "steps": args.fp64_steps, "ms_per_step": run["ms"] / args.fp64_steps, "dtype": "f64",
+            "timed_path": run["timed_path"], "roofline": roof, "kernel_shares": shares, "e2e": e2e,
+            "fp32_form_error": dict(_rcs_err(fp32_rcs, rcs64), against="this FP64 form, same job",
+                                    steps=steps) if fp32_rcs is not None else None,
+            "note": "GB300 runs FP64 at 1/64 of the FP32 rate: the FP64 volume kernels are bound by "
+                    "the FP64 pipe, not by HBM (frac is of the copy bandwidth)"}
+
+
 def run_heterogeneous_form(args, local):
     """The bandwidth-bound heterogeneous medium: 512 x 512 x 384 + 10-cell
     CPML (532 x 532 x 404 cells), 256-entry voxel material table, soft point
-    source, 64 Ez probes, FP32.  `hetero_steps` steps timed with CUDA events
-    through graph replay (after warm-up and graph capture), then a profiled
-    pass of the same steps for the kernel times."""
-    import xfdtd_gb300 as X
-    setup = 3 + GRAPH_STEPS - 3 % GRAPH_STEPS + GRAPH_STEPS
-    sc, st = configs.heterogeneous(steps=setup + args.hetero_steps)
-    g = X.Simulation(sc, st, precision="fp32", device=local)
-    g.step(setup)
-    g.synchronize()
-    ms = g.step_timed(args.hetero_steps)
-    g.check_finite()
-    n = tuple(g.n)
-    cells = n[0] * n[1] * n[2]
-    split = g.volume_split()
-    variants = g.kernel_variants()
-    shell_variants = g.shell_variants()
-    del g
-    sc, st = configs.heterogeneous(steps=3 + args.hetero_steps)
-    g = X.Simulation(sc, st, precision="fp32", device=local, profile=True, graph=False)
-    g.set_kernel_variant(variants["e"], variants["h"])
-    g.set_shell_variant(shell_variants["e"], shell_variants["h"])
-    g.step(3)
-    g.synchronize()
-    g.profile_reset()
-    g.step_timed(args.hetero_steps)
-    prof = g.profile()
-    del g
-    dom = dominant(prof)
-    slabs = _slab_layers(sc)
-    alg = algorithmic_bytes(n, slabs, "fp32", dom, split)
-    gbs = alg / (prof[dom][0] / prof[dom][1] / 1e3) / 1e9
-    peak, kind = _peaks()
-    conc = {k: round(v[0] / max(v[1], 1), 4) for k, v in prof.items() if k in SIDE_STREAM_KERNELS}
-    return {"grid": list(n), "cells": cells, "steps": args.hetero_steps,
-            "value": cells * args.hetero_steps / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms / args.hetero_steps,
-            "timed_path": "CUDA graph replay", "dominant_kernel": dom, "dominant_ms": prof[dom][0] / prof[dom][1],
-            "achieved_GBs": gbs, "frac": gbs / peak, "peak_source": kind, "concurrent_ms": conc,
-            "variants": {"e": variants["e"], "h": variants["h"], "shell_e": shell_variants["e"],
-                         "shell_h": shell_variants["h"]},
-            "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (cells * 4 / 1e6)}
+    source, 64 Ez probes.  FP32: `hetero_steps` steps timed through graph
+    replay, a profiled pass for the kernel times and roofline, and the
+    config's whole 1000-step job end to end; FP64 likewise (fewer timed
+    steps), with the FP32 probes' error against the FP64 job's."""
+    e2e_steps = args.hetero_e2e_steps
+    sc, _ = configs.heterogeneous(steps=e2e_steps)
+    run = _timed(sc, "fp32", args.hetero_steps, 3, local, fused=None)
+    roof, shares, conc = _profiled(sc, "fp32", args.hetero_steps, 3, local, run, fused=None)
+    out = {"grid": list(run["n"]), "cells": run["cells"], "steps": args.hetero_steps,
+           "value": run["cells"] * args.hetero_steps / (run["ms"] / 1e3) / 1e6, "unit": UNIT,
+           "ms_per_step": run["ms"] / args.hetero_steps, "dtype": "f32", "timed_path": run["timed_path"],
+           "roofline": roof, "kernel_shares": shares, "volume_kernels_concurrent": conc,
+           "variants": {"e": run["variants"]["e"], "h": run["variants"]["h"],
+                        "shell_e": run["shell_variants"]["e"], "shell_h": run["shell_variants"]["h"]},
+           "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (run["cells"] * 4 / 1e6)}
+    if e2e_steps > 0:
+        e2e, p32 = _e2e(sc, "fp32", e2e_steps, local, fused=None, readout="probes")
+        out["e2e"] = e2e
+    if args.hetero_fp64_steps > 0:
+        r64 = _timed(sc, "fp64", args.hetero_fp64_steps, 3, local, fused=None)
+        roof64, _, _ = _profiled(sc, "fp64", args.hetero_fp64_steps, 3, local, r64, fused=None)
+        f64 = {"value": r64["cells"] * args.hetero_fp64_steps / (r64["ms"] / 1e3) / 1e6, "unit": UNIT,
+               "steps": args.hetero_fp64_steps, "ms_per_step": r64["ms"] / args.hetero_fp64_steps, "dtype": "f64",
+               "roofline": roof64}
+        if e2e_steps > 0:
+            e64, p64 = _e2e(sc, "fp64", e2e_steps, local, fused=None, readout="probes")
+            f64["e2e"] = e64
+            out["fp32_form_error"] = dict(_probe_err(p32, p64), against="the FP64 form, same job",
+                                          steps=e2e_steps, probes=int(p64.shape[0]))
+        out["fp64_form"] = f64
+    return out
+
+
+def _cpu_info():
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k = line.split(":")[0].strip().lower()
+                if k in ("model name", "cpu model", "hardware") and ":" in line:
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if not model:
+        try:
+            r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+            for line in r.stdout.splitlines():
+                if line.lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
+    import platform
+    return {"cpu_model": model or platform.processor() or platform.machine(), "nproc": os.cpu_count(),
+            "machine": platform.machine()}
 
 
 def ours_arm(args, world, rank, local, grp):
     import xfdtd_gb300 as X
     X.build()
-    sc, _ = configs.dielectric_sphere()
-    fused = {"auto": None, "fused": True, "split": False}[args.volume]
-    # The timed run is the production path: steps replayed from CUDA graphs
-    # of GRAPH_STEPS steps, no per-kernel events.  After the warm-up the run
-    # is brought to a graph boundary and one graph is captured and replayed
-    # (setup, untimed); then exactly `steps` steps are timed.
-    setup = GRAPH_STEPS - args.warmup % GRAPH_STEPS + GRAPH_STEPS
-    total = args.warmup + setup + args.steps
-    sim = X.Simulation(sc, total, precision=args.precision, graph=True, device=local, fused=fused)
-    if args.kernel_variant:
-        sim.set_kernel_variant(*(int(v) for v in args.kernel_variant.split(",")))
-    if args.shell_variant:
-        sim.set_shell_variant(*(int(v) for v in args.shell_variant.split(",")))
-    n = sim.n
-    cells = n[0] * n[1] * n[2]
-    sim.step(args.warmup)
-    sim.step(setup)
-    sim.synchronize()
-    launches0 = sim.launch_count()
     clock = ClockSampler(local)
     clock.start()
-    grp.barrier()
-    ms = sim.step_timed(args.steps)
-    sim.synchronize()
-    grp.barrier()
-    clocks = clock.stop()
-    max_ms = grp.max(ms)
-    variants = sim.kernel_variants()
-    shell_variants = sim.shell_variants()
-    launches = sim.launch_count() - launches0
-    sim.check_finite()
-    split = sim.volume_split()
+    sc, config_steps = configs.dielectric_sphere()
+    fused = {"auto": None, "fused": True, "split": False}[args.volume]
+    fixed = None
+    if args.kernel_variant or args.shell_variant:
+        fixed = (tuple(int(v) for v in (args.kernel_variant or "0,0").split(",")),
+                 tuple(int(v) for v in (args.shell_variant or "0,0").split(",")))
+    # the headline: the FP32 form of the dielectric-sphere workload, timed
+    # steps through the production path
+    run = _timed(sc, args.precision, args.steps, args.warmup, local, grp=grp, fused=fused, variants=fixed)
+    n, cells, split = run["n"], run["cells"], run["split"]
+    max_ms = grp.max(run["ms"])
     value = aggregate_value(cells, args.steps, world, max_ms)
-    del sim
+    roof, shares, concurrent = _profiled(sc, args.precision, min(args.steps, PROFILE_STEPS), args.warmup, local, run,
+                                         fused=fused)
 
-    # Per-kernel device times: a profiled pass over the same workload (events
-    # around every launch, no graph), after `warmup` steps.
-    prof_steps = min(args.steps, PROFILE_STEPS)
-    psim = X.Simulation(sc, args.warmup + prof_steps, precision=args.precision, graph=False, profile=True,
-                        device=local, fused=fused)
-    # the timed run's variants, so that the kernel times explain its number
-    psim.set_kernel_variant(variants["e"], variants["h"])
-    psim.set_shell_variant(shell_variants["e"], shell_variants["h"])
-    assert psim.volume_split() == split
-    psim.step(args.warmup)
-    psim.synchronize()
-    psim.profile_reset()
-    prof_ms_total = psim.step_timed(prof_steps)
-    prof = psim.profile()
-    del psim
-
-    # roofline of the dominant entry (largest share of device time): the E or
-    # H volume update, whose interior and shell kernels run concurrently
-    peak, peak_kind = _peaks()
-    # entries on side streams (the TFSF 1-D line, the two kernels of each
-    # volume update) overlap the main stream's and are reported apart
-    side = {k: prof.pop(k) for k in SIDE_STREAM_KERNELS if k in prof}
-    dom = dominant(prof)
-    dom_ms, dom_n = prof[dom]
-    slabs = _slab_layers(sc)
-    alg = algorithmic_bytes(n, slabs, args.precision, dom, split)
-    achieved = alg / (dom_ms / dom_n / 1e3) / 1e9
-    concurrent = {k: {"ms_per_launch": v[0] / max(v[1], 1),
-                      "algorithmic_GBs": algorithmic_bytes(n, slabs, args.precision, k, split) / (v[0] / max(v[1], 1) / 1e3) / 1e9}
-                  for k, v in side.items() if k.startswith("update_")}
-    total_prof = sum(v[0] for v in prof.values())
-    shares = {k: round(v[0] / total_prof, 4) for k, v in prof.items()}
-    shares.update({f"{k} (concurrent)": round(v[0] / total_prof, 4) for k, v in side.items()})
-
-    # e2e: one whole job through the public API, host scene to host results
+    # e2e: the config's whole job through the public API, host scene to host RCS
     grp.barrier()
-    t0 = time.perf_counter()
-    job = X.Simulation(sc, args.steps, precision=args.precision, graph=True, device=local, fused=fused)
-    job.step(args.steps)
-    rcs = job.rcs_db()
-    t1 = time.perf_counter()
-    h2d, d2h = job.transfer_bytes()
-    assert np.isfinite(rcs).all()
-    e2e_s = grp.max(t1 - t0)
-    del job
+    e2e, rcs32 = _e2e(sc, args.precision, args.e2e_steps or config_steps, local, fused=fused)
+    e2e_wall = grp.max(e2e["wall_s"])
+    e2e["value"] = cells * e2e["steps"] * world / e2e_wall / 1e6
+    e2e["wall_s"] = e2e_wall
 
-    # FP64 form on the same workload (fewer steps)
     fp64 = None
     if args.fp64_steps > 0 and rank == 0:
-        s64 = X.Simulation(sc, args.warmup + args.fp64_steps, precision="fp64", graph=False, profile=True, device=local)
-        s64.step(args.warmup)
-        s64.profile_reset()
-        ms64 = s64.step_timed(args.fp64_steps)
-        p64 = s64.profile()
-        d64 = dominant(p64)
-        a64 = algorithmic_bytes(n, slabs, "fp64", d64, s64.volume_split()) / (p64[d64][0] / p64[d64][1] / 1e3) / 1e9
-        fp64 = {"value": cells * args.fp64_steps / (ms64 / 1e3) / 1e6, "unit": UNIT, "steps": args.fp64_steps,
-                "ms_per_step": ms64 / args.fp64_steps, "dominant_kernel": d64,
-                "dominant_kernel_GBs": a64, "note": "GB300 FP64 is ~1/64 rate: this form is compute-bound"}
-        del s64
-
+        fp64 = run_fp64_form(args, local, sc, args.e2e_steps or config_steps,
+                             rcs32 if args.precision == "fp32" else None)
     batched = run_batched_form(args, local) if (args.batch_problems > 0 and rank == 0) else None
     adjoint = run_adjoint_form(args, local) if (args.adjoint and rank == 0) else None
     hetero = run_heterogeneous_form(args, local) if (args.hetero_steps > 0 and rank == 0) else None
@@ -543,10 +641,13 @@ def ours_arm(args, world, rank, local, grp):
     cpu = None
     if rank == 0 and world == 1 and args.cpu_sample > 0:
         v, cores, sample = run_cpu_oracle(1, args.cpu_sample)
-        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        cpu = dict({"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}, **_cpu_info())
+    clocks = clock.stop()
 
     if rank != 0:
         return
+    v = run["variants"]
+    sv = run["shell_variants"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
@@ -557,27 +658,23 @@ def ours_arm(args, world, rank, local, grp):
                    "cells": cells, "grid": list(n), "precision_form": args.precision,
                    "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (cells * (4 if args.precision == 'fp32' else 8) / 1e6),
                    "parallelism": f"replicas x{world}", "volume_kernels": args.volume,
-                   "timed_path": f"CUDA graph replay ({GRAPH_STEPS}-step graphs), after {args.warmup} warm-up steps "
-                                 f"and {setup} untimed steps to reach a graph boundary and capture the graph"},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": NCU_TRAFFIC.get((dom, args.precision, tuple(n), split.get(dom[7] + "_wide"))),
-                     "algorithmic_bytes_per_launch": alg, "launch_ms": dom_ms / dom_n,
-                     "timing": f"CUDA events around each launch in a profiled pass of {prof_steps} steps "
-                               f"({prof_ms_total / prof_steps:.4f} ms/step, no graph)"},
+                   "timed_path": run["timed_path"]},
+        "roofline": roof,
         "kernel_shares": shares,
         "volume_split_cells": split,
         "volume_kernels_concurrent": concurrent,
-        "autotuned_variants": {"update_e": variants["e"], "update_h": variants["h"],
-                               "shell_e": shell_variants["e"], "shell_h": shell_variants["h"],
-                               "trial_ms_e": [round(v, 4) for v in variants["trials_e"]],
-                               "trial_ms_h": [round(v, 4) for v in variants["trials_h"]]},
-        "e2e": {"value": cells * args.steps * world / e2e_s / 1e6, "unit": UNIT,
-                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-                "wall_s": e2e_s, "scope": "scene lowering + upload + steps + far field + RCS readback"},
-        "gpu_launches": launches,
+        "autotuned_variants": {"update_e": v["e"], "update_h": v["h"], "shell_e": sv["e"], "shell_h": sv["h"],
+                               "trial_ms_e": [round(q, 4) for q in v["trials_e"]],
+                               "trial_ms_h": [round(q, 4) for q in v["trials_h"]]},
+        "e2e": e2e,
+        "gpu_launches": run["launches"],
         "clocks": clocks,
         "cpu_baseline": cpu,
+        "accuracy": {
+            "fp32_vs_fp64_engine": (fp64 or {}).get("fp32_form_error"),
+            "against_oracle": "tests/test_gpu_fullsize.py compares the FP64 form with the CPU oracle at every "
+                              "config's full grid (1e-10) and bounds the FP32 form's errors against it",
+        },
         "fp64_form": fp64,
         "batched_form": batched,
         "adjoint_form": adjoint,
@@ -602,12 +699,18 @@ def main():
                          "workload), the fused E/H sweep, or the autotuner's choice")
     ap.add_argument("--adjoint", type=int, default=1, help="run the adjoint form (0: skip)")
     ap.add_argument("--hetero-steps", type=int, default=100, help="steps of the heterogeneous-medium form (0: skip)")
+    ap.add_argument("--hetero-fp64-steps", type=int, default=20,
+                    help="timed steps of the heterogeneous medium's FP64 form (0: skip)")
+    ap.add_argument("--hetero-e2e-steps", type=int, default=1000,
+                    help="steps of the heterogeneous medium's whole job end to end (0: skip)")
+    ap.add_argument("--e2e-steps", type=int, default=0,
+                    help="steps of the headline's whole job end to end (0: the config's 2000)")
     ap.add_argument("--kernel-variant", default=None, metavar="E,H",
                     help="fix the interior variants of the headline run (after autotuning; for a launch list "
                          "under a profiler, whose timings would mislead the autotuner)")
     ap.add_argument("--shell-variant", default=None, metavar="E,H", help="fix the shell variants likewise")
     ap.add_argument("--adjoint-fd", type=int, default=16, help="design voxels of the adjoint FD check (0: skip)")
-    ap.add_argument("--adjoint-checkpoint", type=int, default=0,
+    ap.add_argument("--adjoint-checkpoint", type=int, default=100,
                     help="adjoint form: checkpoint every K steps (0: record the design box at every step)")
     args = ap.parse_args()
     world, rank, local = _dist()

@@ -292,6 +292,10 @@ int xfdtd_launch_count(xfdtd_handle *h, int64_t *n);
 int xfdtd_launches_per_step(xfdtd_handle *h, int *n);
 /* Bytes copied host->device and device->host by the handle so far. */
 int xfdtd_transfer_bytes(xfdtd_handle *h, int64_t *h2d, int64_t *d2h);
+/* Wall time of xfdtd_create, in ms: ms[0] validation, device allocation
+ * and upload of the tables; ms[1] autotuning (0 without
+ * XFDTD_FLAG_AUTOTUNE).  No counterpart in the reference. */
+int xfdtd_create_times(xfdtd_handle *h, double ms[2]);
 /* Device bytes held by the handle (with its adjoint state, if any). */
 int xfdtd_device_bytes(xfdtd_handle *h, int64_t *bytes);
 const char *xfdtd_last_error(xfdtd_handle *h);

@@ -117,6 +117,9 @@ typedef struct xfdtd_pml_desc {
   double kappa_max;     /* default 10                                    */
 } xfdtd_pml_desc;
 
+/* enabled: 1 TFSF3D(distance x, y, z, e0, theta, phi, psi, waveform);
+ * 2 TFSF2D(distance x, y, phi, e0, waveform) (src/include/tfsf/tfsf_2d.h:8-10)
+ * on a 2-D grid (nz = 1): theta = pi / 2, psi = 0, distance[2] = 0. */
 typedef struct xfdtd_tfsf_desc {
   int32_t enabled;
   int32_t reserved;

@@ -140,6 +140,7 @@ struct GridSpace {  // src/grid/grid_space.cpp (uniform construction only)
   double base[3];
   double mn[3], mx[3];
   size_t n[3] = {0, 0, 0};
+  int dim = 0;   // 3 or 2 (GridSpace::Dimension, grid_space.h)
   bool ready = false;
   std::vector<double> ec[3], hc[3], es[3], hs[3];
 
@@ -180,8 +181,12 @@ struct GridSpace {  // src/grid/grid_space.cpp (uniform construction only)
   void generateUniformGridSpace() {  // :501-536, :625-638, :679-689, :737-757
     if (ready) throw std::runtime_error("GridSpace is ready");
     for (int a = 0; a < 3; ++a) n[a] = std::max<size_t>(n[a], 1);
-    if (!(n[0] > 1 && n[1] > 1 && n[2] > 1))
-      throw std::runtime_error("only three-dimensional grids are restated");
+    // :513-533: all three axes extended is 3-D; x extended (the reference
+    // tests `extended_x && extended_x`) is 2-D.  Restated: the 3-D grid and
+    // the 2-D grid of the TMz path, x and y extended with nz = 1.
+    if (n[0] > 1 && n[1] > 1 && n[2] > 1) dim = 3;
+    else if (n[0] > 1 && n[1] > 1 && n[2] == 1) dim = 2;
+    else throw std::runtime_error("only the 3-D grid and the 2-D (nz = 1) grid are restated");
     for (int a = 0; a < 3; ++a) {
       ec[a].resize(n[a] + 1);
       for (size_t i = 0; i <= n[a]; ++i) ec[a][i] = mn[a] + static_cast<double>(i) * base[a];
@@ -335,6 +340,7 @@ struct oracle_sim {
 
   // TFSF3D (src/tfsf/tfsf_3d.cpp)
   struct {
+    bool two_d = false;   // TFSF2D (src/tfsf/tfsf_2d.cpp)
     size_t dist[3];
     double e0, theta, phi, psi;
     double k[3], te[3], th[3];
@@ -398,6 +404,8 @@ struct oracle_sim {
   void tfsfIncident(size_t t);
   void tfsfE();
   void tfsfH();
+  void tfsf2dE();
+  void tfsf2dH();
   void lumpedE(Lumped &l);
   void nffftUpdate();
   void broadbandFarField();
@@ -441,8 +449,11 @@ void oracle_sim::init() {
 
   // FDTDBasicCoff::init, fdtd_basic_coff.cpp:11-29, :313-354
   double cfl_d = static_cast<double>(cfl);
-  dt = cfl_d / (C_0 * std::sqrt(1.0 / (gs->base[0] * gs->base[0]) + 1.0 / (gs->base[1] * gs->base[1]) +
-                                 1.0 / (gs->base[2] * gs->base[2])));
+  if (nz <= 1)   // :19-21, calculateDeltaT(cfl, dx, dy), :348-351
+    dt = cfl_d / (C_0 * std::sqrt(1.0 / (gs->base[0] * gs->base[0]) + 1.0 / (gs->base[1] * gs->base[1])));
+  else
+    dt = cfl_d / (C_0 * std::sqrt(1.0 / (gs->base[0] * gs->base[0]) + 1.0 / (gs->base[1] * gs->base[1]) +
+                                   1.0 / (gs->base[2] * gs->base[2])));
   eps[0].init(nx, ny + 1, nz + 1, EPSILON_0);
   eps[1].init(nx + 1, ny, nz + 1, EPSILON_0);
   eps[2].init(nx + 1, ny + 1, nz, EPSILON_0);
@@ -512,7 +523,9 @@ void oracle_sim::initObjects() {
       for (size_t j = 0; j < ny; ++j) {
         q[1] = gs->hc[1][j];
         for (size_t k = 0; k < nz; ++k) {
-          q[2] = gs->hc[2][k];
+          // getShapeMask (grid_space.cpp:274-291): the 2-D mask takes the
+          // cell centre at z = 0 (getGridCenterZ returns 0 there)
+          q[2] = gs->dim == 2 ? 0.0 : gs->hc[2][k];
           if (!s.inside(q)) continue;
           for (int a = 0; a < 3; ++a) {
             eps[a](i, j, k) = e; mu[a](i, j, k) = m;
@@ -639,7 +652,9 @@ void oracle_sim::initTFSF() {
   double sps = std::sin(t.psi), cps = std::cos(t.psi);
   t.k[0] = st * cp; t.k[1] = st * sp; t.k[2] = ct;
   // TFSF3D ctor, tfsf_3d.cpp:18-31: transform_e = U . (sin psi, cos psi, 0),
-  // transform_h = k x transform_e
+  // transform_h = k x transform_e.  TFSF2D (tfsf_2d.cpp:7-23) is the same
+  // with theta = pi / 2 and psi = 0; its k_e lists two of three entries,
+  // the third taken as 0.
   double u[3][3] = {{-sp, ct * cp, st * cp}, {cp, ct * sp, st * sp}, {0, -st, ct}};
   double ke[3] = {sps, cps, 0};
   for (int r = 0; r < 3; ++r) t.te[r] = u[r][0] * ke[0] + u[r][1] * ke[1] + u[r][2] * ke[2];
@@ -660,7 +675,10 @@ void oracle_sim::initTFSF() {
   double ratio_delta = 1 / std::sqrt(std::pow(std::sin(t.theta), 4) *
                                          (std::pow(std::cos(t.phi), 4) + std::pow(std::sin(t.phi), 4)) +
                                      std::pow(std::cos(t.theta), 4));
-  double diagonal_length = std::sqrt(std::pow(bn[0], 2) + std::pow(bn[1], 2) + std::pow(bn[2], 2)) * ratio_delta;
+  // TFSF2D::init (tfsf_2d.cpp:44-46) takes sqrt(nz^2) where TFSF3D takes nz^2
+  double diagonal_length =
+      t.two_d ? std::sqrt(std::pow(bn[0], 2) + std::pow(bn[1], 2) + std::sqrt(std::pow(bn[2], 2))) * ratio_delta
+              : std::sqrt(std::pow(bn[0], 2) + std::pow(bn[1], 2) + std::pow(bn[2], 2)) * ratio_delta;
   t.L = static_cast<size_t>(std::ceil(diagonal_length)) + 4 + 1;
   t.e_inc.assign(t.L, 0.0); t.exi.assign(t.L, 0.0); t.eyi.assign(t.L, 0.0); t.ezi.assign(t.L, 0.0);
   t.h_inc.assign(t.L - 1, 0.0); t.hxi.assign(t.L - 1, 0.0); t.hyi.assign(t.L - 1, 0.0); t.hzi.assign(t.L - 1, 0.0);
@@ -670,6 +688,7 @@ void oracle_sim::initTFSF() {
   double hi[3] = {static_cast<double>(t.ri), static_cast<double>(t.rj), static_cast<double>(t.rk)};
   double orig[3];
   for (int a = 0; a < 3; ++a) orig[a] = (t.k[a] >= 0 ? lo[a] : hi[a]) - extra[a];
+  if (t.two_d) orig[2] = 0.0 - extra[2];   // tfsf_2d.cpp:55-75: the corner's z is 0
   size_t start[3] = {t.li, t.lj, t.lk};
   std::vector<double> *full[3] = {&t.px_f, &t.py_f, &t.pz_f};
   std::vector<double> *half[3] = {&t.px_h, &t.py_h, &t.pz_h};
@@ -1090,6 +1109,7 @@ inline double interp(const std::vector<double> &v, double projection) {  // tfsf
 
 void oracle_sim::tfsfH() {  // TFSF3D::updateH, tfsf_3d.cpp:185-297
   auto &f = tf;
+  if (f.two_d) return tfsf2dH();
   const size_t li = f.li, ri = f.ri, lj = f.lj, rj = f.rj, lk = f.lk, rk = f.rk;
   double cbx = dt / (MU_0 * gs->base[0]), cby = dt / (MU_0 * gs->base[1]), cbz = dt / (MU_0 * gs->base[2]);
   auto Ex = [&](size_t i, size_t j, size_t k) {
@@ -1127,8 +1147,38 @@ void oracle_sim::tfsfH() {  // TFSF3D::updateH, tfsf_3d.cpp:185-297
     for (size_t j = lj; j < rj; ++j) hx(i, j, rk) += cbz * Ey(i, j, rk);
 }
 
+void oracle_sim::tfsf2dH() {  // TFSF2D::updateH, tfsf_2d.cpp:150-190 (Hy on x faces, Hx on y faces)
+  auto &f = tf;
+  const size_t li = f.li, ri = f.ri, lj = f.lj, rj = f.rj;
+  double cbx = dt / (MU_0 * gs->base[0]), cby = dt / (MU_0 * gs->base[1]);
+  auto Ez = [&](size_t i, size_t j) {   // getIncidentEz, tfsf_2d.cpp:230-238
+    return interp(f.ezi, f.px_f[i - li] + f.py_f[j - lj]);
+  };
+  for (size_t j = lj; j < rj + 1; ++j) hy(li - 1, j, 0) -= cbx * Ez(li, j);
+  for (size_t j = lj; j < rj + 1; ++j) hy(ri, j, 0) += cbx * Ez(ri, j);
+  for (size_t i = li; i < ri + 1; ++i) hx(i, lj - 1, 0) += cby * Ez(i, lj);
+  for (size_t i = li; i < ri + 1; ++i) hx(i, rj, 0) -= cby * Ez(i, rj);
+}
+
+void oracle_sim::tfsf2dE() {  // TFSF2D::updateE, tfsf_2d.cpp:192-228 (Ez on x and y faces)
+  auto &f = tf;
+  const size_t li = f.li, ri = f.ri, lj = f.lj, rj = f.rj;
+  double cax = dt / (EPSILON_0 * gs->base[0]), cay = dt / (EPSILON_0 * gs->base[1]);
+  auto Hx = [&](size_t i, size_t j) {   // getIncidentHx, tfsf_2d.cpp:240-248
+    return interp(f.hxi, f.px_f[i - li] + f.py_h[j - lj + 1] - 0.5);
+  };
+  auto Hy = [&](size_t i, size_t j) {   // getIncidentHy, tfsf_2d.cpp:250-258
+    return interp(f.hyi, f.px_h[i - li + 1] + f.py_f[j - lj] - 0.5);
+  };
+  for (size_t j = lj; j < rj + 1; ++j) ez(li, j, 0) -= cax * Hy(li - 1, j);
+  for (size_t j = lj; j < rj + 1; ++j) ez(ri, j, 0) += cax * Hy(ri, j);
+  for (size_t i = li; i < ri + 1; ++i) ez(i, lj, 0) += cay * Hx(i, lj - 1);
+  for (size_t i = li; i < ri + 1; ++i) ez(i, rj, 0) -= cay * Hx(i, rj);
+}
+
 void oracle_sim::tfsfE() {  // TFSF3D::updateE, tfsf_3d.cpp:299-411
   auto &f = tf;
+  if (f.two_d) return tfsf2dE();
   const size_t li = f.li, ri = f.ri, lj = f.lj, rj = f.rj, lk = f.lk, rk = f.rk;
   double cax = dt / (EPSILON_0 * gs->base[0]), cay = dt / (EPSILON_0 * gs->base[1]),
          caz = dt / (EPSILON_0 * gs->base[2]);
@@ -1595,6 +1645,7 @@ int oracle_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, oracle_si
     if (sc->tfsf.enabled) {
       s->has_tfsf = true;
       s->tfsf_d = sc->tfsf;
+      s->tf.two_d = sc->tfsf.enabled == 2;
       for (int a = 0; a < 3; ++a) s->tf.dist[a] = static_cast<size_t>(sc->tfsf.distance[a]);
       s->tf.e0 = sc->tfsf.e0;
       s->tf.theta = sc->tfsf.theta;

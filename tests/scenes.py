@@ -221,7 +221,15 @@ def rel_err(a, b):
     return float(np.abs(a - b).max() / scale)
 
 
+def cylinder_2d(steps=300):
+    """The 2-D (nz = 1) TMz cylinder scatter of the reference's example at a
+    fifth of its size: 70 x 60 cells + 10-cell CPML on x and y, PEC
+    cylinder, TFSF2D at phi = pi / 4."""
+    return configs.cylinder_2d(scale=5, steps=steps)
+
+
 SCENES = {
+    "cylinder_2d": cylinder_2d,
     "pec_sphere": pec_sphere,
     "dielectric": dielectric,
     "heterogeneous": heterogeneous,

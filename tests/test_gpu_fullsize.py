@@ -16,10 +16,16 @@ grid sizes, through the C-ABI.
   C5  the 180 x 180 x 116 adjoint problem's forward run, 300 steps: FP64
       fields within 1e-10; FP32 errors.
 
-Tolerance for FP64: max |gpu - oracle| / max |oracle| per array, 1e-10
-(rounding differences only).  The FP32 form's errors are asserted against
-generous bounds and recorded: with XFDTD_ACCURACY_OUT set, each test
-appends one JSON line per config to that file.
+Tolerance for FP64: max |gpu - oracle| over an array, divided by the
+largest |oracle| value of the field it belongs to -- the three E
+components, the three H components, or the 24 NF-FF accumulators -- 1e-10
+(rounding differences only).  At these sizes a component can carry only
+cross-polarised scattering and rounding residue (Ey and Hz of the
+x-polarised dielectric-sphere run after 200 steps, the accumulators of a
+face the pulse has not reached), and its own maximum is no scale for a
+rounding error.  The FP32 form's errors are asserted against generous
+bounds and recorded: with XFDTD_ACCURACY_OUT set, each test appends one
+JSON line per config to that file.
 """
 import json
 import os
@@ -50,30 +56,38 @@ def _record(**kw):
             f.write(json.dumps(kw) + "\n")
 
 
-def _l2(a, b):
-    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
-
-
 def _fields_vs(g, o, tol=None):
-    """Per component: (max-norm relative error, L2 relative error)."""
+    """Per component: max |gpu - oracle| over the largest |oracle| of its
+    field (E or H), and ||gpu - oracle|| over the L2 norm of its field."""
     out = []
-    for c in range(6):
-        a, b = g.read_field(c), o.read_field(c)
-        e = scenes.rel_err(a, b)
-        if tol is not None:
-            assert e <= tol, f"component {c}: rel err {e:.3e}"
-        out.append((e, _l2(a, b)))
+    for side in (range(0, 3), range(3, 6)):
+        diff, scale, dn, norm2 = [], 0.0, [], 0.0
+        for c in side:
+            a, b = g.read_field(c), o.read_field(c)
+            diff.append(float(np.abs(a - b).max()))
+            scale = max(scale, float(np.abs(b).max()))
+            dn.append(float(np.linalg.norm(a - b)))
+            norm2 += float(np.linalg.norm(b)) ** 2
+        norm = max(np.sqrt(norm2), 1e-300)
+        for c, d, q in zip(side, diff, dn):
+            e = d / scale if scale > 0 else d
+            if tol is not None:
+                assert e <= tol, f"component {c}: rel err {e:.3e}"
+            out.append((e, q / norm))
     return out
 
 
 def _nffft_vs(g, o, tol=None):
-    worst = 0.0
+    """Max |gpu - oracle| over the 24 accumulators, over their largest |oracle|."""
+    diff, scale = 0.0, 0.0
     for w in range(24):
-        e = scenes.rel_err(g.read_nffft(w), o.read_nffft(w))
-        if tol is not None:
-            assert e <= tol, f"accumulator {w}: rel err {e:.3e}"
-        worst = max(worst, e)
-    return worst
+        a, b = g.read_nffft(w), o.read_nffft(w)
+        diff = max(diff, float(np.abs(a - b).max()))
+        scale = max(scale, float(np.abs(b).max()))
+    e = diff / scale if scale > 0 else diff
+    if tol is not None:
+        assert e <= tol, f"accumulators: rel err {e:.3e}"
+    return e
 
 
 def test_c1_pec_sphere_fp32_rcs_against_oracle():

@@ -46,6 +46,33 @@ def test_grid_space_matches_reference_test_grid():
             assert np.all(np.abs(sizes[key] - dl) <= 10 * np.finfo(float).eps), key
 
 
+def test_2d_grid_time_step_and_tfsf2d_cancellation():
+    """The 2-D (nz = 1) TMz path: a zero-thickness domain gives nz = 1 and
+    the 2-D time step cfl / (c0 sqrt(1/dx^2 + 1/dy^2))
+    (fdtd_basic_coff.cpp:19-21, 348-351); TFSF2D at phi = pi / 4 with
+    dx = dy leaves the scattered-field region empty to rounding (the
+    1-D line's numerical dispersion matches the grid's along the diagonal),
+    carries the plane wave (|Ez| ~ e0) inside the box, and the TE
+    components stay exactly zero."""
+    sc, st = configs.cylinder_2d(scale=5, steps=200)
+    sc.objects = sc.objects[:1]
+    o = O.OracleSim(sc, st)
+    assert o.n == (90, 80, 1)
+    dx = sc.cell_size
+    want_dt = float(np.float32(0.8)) / (S.C_0 * math.sqrt(2.0 / (dx * dx)))
+    assert o.dt == pytest.approx(want_dt, rel=1e-15)
+    o.step(st)
+    ez = o.read_field(S.EZ)[:, :, 0]
+    d = sc.tfsf.distance_x
+    inside = np.abs(ez[d + 2:-d - 2, d + 2:-d - 2]).max()
+    m = ez.copy()
+    m[d - 1:-d + 1, d - 1:-d + 1] = 0
+    assert 0.9 < inside < 1.1, inside
+    assert np.abs(m).max() < 1e-12 * inside
+    for c in (S.EX, S.EY, S.HZ):
+        assert not np.any(o.read_field(c)), c
+
+
 def test_tfsf_normal_incidence_cancels_outside_box():
     sc, _ = configs.pec_sphere_rcs(scale=2, steps=260)
     sc.objects = sc.objects[:1]

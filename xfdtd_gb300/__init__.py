@@ -20,7 +20,7 @@ from .scene import (  # noqa: F401  (re-exported: the reference's scene API)
     AXIS_X, AXIS_Y, AXIS_Z, EX, EY, EZ, HX, HY, HZ, XN, XP, YN, YP, ZN, ZP,
     Capacitor, CosineModulatedGaussianWaveform, CurrentMonitor, CurrentSource, Cube,
     CustomWaveform, Cylinder, GaussianWaveform, Inductor, Material, NffftFd, Object, PML,
-    Resistor, Scene, SinusoidalWaveform, Sphere, TFSF3D, ThinWire, VoltageMonitor,
+    Resistor, Scene, SinusoidalWaveform, Sphere, TFSF2D, TFSF3D, ThinWire, VoltageMonitor,
     VoltageSource,
 )
 
@@ -96,6 +96,7 @@ def libs():
         cu.xfdtd_shell_variants.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int)]
         cu.xfdtd_set_shell_variant.argtypes = [C.c_void_p, C.c_int, C.c_int]
         cu.xfdtd_set_wait_limit.argtypes = [C.c_void_p, C.c_int64]
+        cu.xfdtd_create_times.argtypes = [C.c_void_p, dp]
         cu.xfdtd_last_error.argtypes = [C.c_void_p]
         cu.xfdtd_last_error.restype = C.c_char_p
         cu.xfdtd_version.restype = C.c_char_p
@@ -377,6 +378,13 @@ class Simulation:
 
     def set_shell_variant(self, e_variant: int, h_variant: int):
         self._check_engine(libs()[0].xfdtd_set_shell_variant(self.engine, int(e_variant), int(h_variant)))
+
+    def create_times(self) -> dict:
+        """Wall time of the engine's create, ms: allocation and upload of the
+        plan's tables, and autotuning."""
+        ms = (C.c_double * 2)()
+        self._check_engine(libs()[0].xfdtd_create_times(self.engine, ms))
+        return {"alloc_upload_ms": ms[0], "autotune_ms": ms[1]}
 
     def set_wait_limit(self, polls: int):
         """Polls of each TMA plane wait before a block gives up and reports a

@@ -185,6 +185,32 @@ def adjoint_dipole(scale: int = 1, steps: int = 2000, seed: int = 5001):
     return sc, steps, spec
 
 
+def cylinder_2d(scale: int = 1, steps: int = 1400, pec: bool = True):
+    """The reference's 2-D example (examples/2d_cylinder_scatter.cpp:29-98):
+    a 350 x 300-cell TMz grid (nz = 1) plus a 10-cell CPML on the four x and
+    y faces, dx = (c / 20 GHz) / 20, a cylinder of radius 0.03 m (40 cells)
+    along z at the centre (PEC as sigma = 1e24, or eps_r = 3 with `pec`
+    False), TFSF2D 50 cells from the domain edge at phi = pi / 4 with a
+    cosine-modulated Gaussian (12 GHz, tau = 1.7 / 8 GHz, t0 = 0.8 tau),
+    cfl 0.8, 1400 steps.  `scale` divides the cell counts, the radius in
+    cells and the TFSF offset beyond the CPML."""
+    dx = (3e8 / 20e9) / 20
+    nx, ny = 350 // scale, 300 // scale
+    pml = 10
+    tau = 1.7 / (20e9 - 12e9)
+    t0 = 0.8 * tau
+    radius = (0.03 / dx) // scale * dx
+    objects = [
+        S.Object("free_space", S.Cube([0.0, 0.0, 0.0], [nx * dx, ny * dx, 0.0]), S.Material("air", 1, 1, 0, 0)),
+        S.Object("objectA", S.Cylinder(S.AXIS_Z, [nx * 0.5 * dx, ny * 0.5 * dx, 0.0], radius, 0.0),
+                 S.Material("pec", 1, 1, 1e24, 0) if pec else S.Material("d", 3.0, 1, 0, 0)),
+    ]
+    boundaries = [S.PML(o, pml) for o in (S.XN, S.XP, S.YN, S.YP)]
+    d_tfsf = pml + max(40 // scale, 4)
+    tfsf = S.TFSF2D(d_tfsf, d_tfsf, math.pi * 0.25, 1.0, S.CosineModulatedGaussianWaveform(1.0, tau, t0, 12e9))
+    return S.Scene(dx, objects, boundaries, tfsf=tfsf, cfl=0.8), steps
+
+
 CONFIGS = {
     "pec_sphere_rcs": pec_sphere_rcs,
     "dielectric_sphere": dielectric_sphere,

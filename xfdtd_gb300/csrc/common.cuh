@@ -1,7 +1,8 @@
 // common.cuh -- device-side data layout shared by the engine's kernels.
 //
 // Fields live in one uniform padded box per component: (nx+1) x (ny+1) x NZP
-// with NZP = nz+1 rounded up to 32, i.e. index (i*(ny+1) + j)*NZP + k.  Every
+// with NZP = nz+1 rounded up to 32 (4 on the 2-D grid, nz = 1), i.e. index
+// (i*(ny+1) + j)*NZP + k.  Every
 // component of the reference (Ex (nx,ny+1,nz+1) ... Hz (nx,ny,nz+1),
 // src/simulation/simulation_init.cpp:28-35) fits in that box at the same
 // (i, j, k); the cells a component does not have stay zero and are never
@@ -34,6 +35,8 @@ struct CpmlAxis {
 // stored with stride aux_len).
 struct TfsfDev {
   int enabled;
+  int two_d;   // TFSF2D (src/tfsf/tfsf_2d.cpp:150-228): Ez on the x and y faces, Hy on the x faces,
+               // Hx on the y faces; the z projection tables are zero
   int L;
   int lo[3], hi[3];
   const double *pf[3], *ph[3];

@@ -27,6 +27,7 @@
 #include <dlfcn.h>
 
 #include <algorithm>
+#include <chrono>
 #include <functional>
 #include <cmath>
 #include <cstdio>
@@ -160,6 +161,7 @@ struct xfdtd_handle {
   long long *d_step = nullptr;
   int *d_status = nullptr;
   int wait_polls = xg::kItWaitLimit;   // polls of a TMA plane wait before a block gives up
+  double create_ms[2] = {0, 0};         // xfdtd_create: allocation and upload; autotuning
   int *d_flag = nullptr;
 
   // host copies kept for the adjoint: the coefficient table (FP64) and the
@@ -193,6 +195,7 @@ struct xfdtd_handle {
   // fused E/H sweep (sweep.cuh): the state of step t+1 goes to the second
   // buffer set, swapped with the first after each step
   bool sweep_ok = false;   // the plan allows the sweep (buffers allocated)
+  bool tf_two_d = false;   // TFSF2D: Ez, Hx, Hy corrections on the x and y faces only
   bool sweep = false;      // the sweep runs
   int cur_set = 0;         // which buffer set (0: allocated as F, 1: as F2) is current
   CUtensorMap tm_h[2][3], tm_e[2][3], tm_idx;   // TMA maps of both sets and the index
@@ -379,6 +382,7 @@ xg::VolParams<T, I> vol_params(xfdtd_handle *h) {
   T **ps = reinterpret_cast<T **>(&p.psi);
   for (int q = 0; q < 12; ++q) ps[q] = static_cast<T *>(h->psi[q]);
   p.tf.enabled = h->tfsf ? 1 : 0;
+  p.tf.two_d = h->tf_two_d ? 1 : 0;
   p.tf.L = h->aux_len;
   for (int a = 0; a < 3; ++a) {
     p.tf.lo[a] = h->tf_lo[a];
@@ -600,7 +604,10 @@ void volume_boxes(xfdtd_handle *h, int side) {
       break;
     }
   }
-  const bool interior = run[0] && run[1] && run[2];
+  // the 2-D grid (nz = 1) runs as shell boxes only: their cells are
+  // numbered k fastest over the short rows, where an interior launch would
+  // give each 32-wide row of threads one cell
+  const bool interior = run[0] && run[1] && run[2] && n[2] > 1;
   // ranges per axis: 0 = below the plain run, 1 = the plain run, 2 = above,
   // 3 = all, 4 = below and above (k only: the row's two parts together)
   auto add = [&](xg::ShellBoxes &s, unsigned &blocks, long long &total, int ri, int rj, int rk, int cls) {
@@ -1152,6 +1159,7 @@ xg::TfsfSurfParams<T> tfsf_surf_params(xfdtd_handle *h) {
   p.d = h->d;
   for (int c = 0; c < 6; ++c) p.F[c] = static_cast<T *>(h->F[c]);
   p.tf.enabled = 1;
+  p.tf.two_d = h->tf_two_d ? 1 : 0;
   p.tf.L = h->aux_len;
   for (int a = 0; a < 3; ++a) {
     p.tf.lo[a] = h->tf_lo[a];
@@ -1379,8 +1387,17 @@ void comp_shape(const xfdtd_handle *h, int c, long long s[3]) {
 }
 
 // ----------------------------------------------------------- creation ---
+double ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
 void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
-  if (pl->nx < 2 || pl->ny < 2 || pl->nz < 2) invalid("grid must have at least 2 cells per axis");
+  const auto t_begin = std::chrono::steady_clock::now();
+  // the 3-D grid, or the 2-D grid of the TMz path (nz = 1, simulation_update.cpp:157-168)
+  if (pl->nx < 2 || pl->ny < 2 || pl->nz < 1) invalid("grid must have at least 2 cells on x and y and 1 on z");
+  if (pl->tfsf.enabled == 2 && pl->nz != 1) invalid("the 2-D plane wave (TFSF2D) needs nz = 1");
+  if (pl->nz == 1 && pl->tfsf.enabled == 1) invalid("a 2-D grid (nz = 1) takes the 2-D plane wave (TFSF2D)");
+  if (pl->nz == 1 && pl->nffft.enabled) invalid("the 2-D grid (nz = 1) carries no NF-FF box");
   if (pl->precision != XFDTD_FP64 && pl->precision != XFDTD_FP32) invalid("precision must be FP64 or FP32");
   if (pl->index_bytes != 1 && pl->index_bytes != 2 && pl->index_bytes != 4) invalid("index_bytes must be 1, 2 or 4");
   if (pl->n_materials < 1 || (pl->index_bytes < 4 && pl->n_materials > (pl->index_bytes == 1 ? 256 : 65536)))
@@ -1402,7 +1419,9 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   d.nx = pl->nx;
   d.ny = pl->ny;
   d.nz = pl->nz;
-  d.nzp = ((pl->nz + 1) + 31) / 32 * 32;
+  // rows of whole 128-byte lines; the 2-D grid's rows hold k = 0, 1 and the
+  // k = 2 the general path reads past the last E, in 16 (FP32) or 32 bytes
+  d.nzp = pl->nz == 1 ? 4 : ((pl->nz + 1) + 31) / 32 * 32;
   d.sj = d.nzp;
   d.si = static_cast<long long>(pl->ny + 1) * d.nzp;
   d.cells = static_cast<long long>(pl->nx + 1) * d.si;
@@ -1498,7 +1517,7 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     // the fused sweep, unless the plan asks for the split kernels or has
     // lumped elements (whose E corrections run between the E and H updates)
     h->sweep_ok = !(pl->flags & XFDTD_FLAG_SPLIT_EH) && pl->n_injections == 0 && pl->n_inductor_cells == 0 &&
-                  pl->index_bytes < 4;
+                  pl->index_bytes < 4 && pl->nz > 1;
     h->sweep = h->sweep_ok && (pl->flags & XFDTD_FLAG_FUSED_EH);
     if (h->sweep_ok) {
       for (int c = 0; c < 6; ++c) h->F2[c] = h->alloc_bytes(d.cells * h->esize);
@@ -1512,8 +1531,13 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     h->tfsf = true;
     if (tp.aux_len < 6) invalid("TFSF auxiliary grid too short");
     h->aux_len = tp.aux_len;
+    h->tf_two_d = tp.enabled == 2;
     for (int a = 0; a < 3; ++a) {
-      if (tp.lo[a] < 1 || tp.hi[a] <= tp.lo[a] || tp.hi[a] > n_axis[a] - 1) invalid("TFSF box outside the grid");
+      if (h->tf_two_d && a == 2) {   // TFSF2D: the box spans the one z cell
+        if (tp.lo[2] != 0 || tp.hi[2] != 1) invalid("the 2-D TFSF box spans k = 0 .. 1");
+      } else if (tp.lo[a] < 1 || tp.hi[a] <= tp.lo[a] || tp.hi[a] > n_axis[a] - 1) {
+        invalid("TFSF box outside the grid");
+      }
       h->tf_lo[a] = static_cast<int>(tp.lo[a]);
       h->tf_hi[a] = static_cast<int>(tp.hi[a]);
       const long long bn = tp.hi[a] - tp.lo[a];
@@ -1728,7 +1752,10 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     }
   }
   XCHECK(cudaStreamSynchronize(h->stream));
+  h->create_ms[0] = ms_since(t_begin);
+  const auto t_tune = std::chrono::steady_clock::now();
   if (pl->flags & XFDTD_FLAG_AUTOTUNE) autotune(h, 3);
+  h->create_ms[1] = ms_since(t_tune);
 }
 
 template <typename T>
@@ -2305,6 +2332,13 @@ int xfdtd_transfer_bytes(xfdtd_handle *h, int64_t *h2d, int64_t *d2h) {
   return XFDTD_OK;
 }
 
+int xfdtd_create_times(xfdtd_handle *h, double ms[2]) {
+  if (!h || !ms) return XFDTD_ERR_STATE;
+  ms[0] = h->create_ms[0];
+  ms[1] = h->create_ms[1];
+  return XFDTD_OK;
+}
+
 int xfdtd_device_bytes(xfdtd_handle *h, int64_t *bytes) {
   if (!h || !bytes) return XFDTD_ERR_STATE;
   *bytes = static_cast<int64_t>(h->bytes + adjoint_bytes(h));
@@ -2694,6 +2728,7 @@ int xfdtd_batch_create(xfdtd_handle *const *members, int n, int flags, xfdtd_bat
         if (h->n_inj || h->n_ind || h->n_probes || !h->snaps.empty())
           invalid("batch members may not have lumped elements or monitors");
         if (h->nf_bb) invalid("batch members may not have a broadband NF-FF");
+        if (h->d.nz < 2) invalid("batch members must be 3-D grids");
         if (h->d.nx >= 65535 || h->d.ny >= 2040 || h->d.nz >= 8160) invalid("batch member grid too large for the tile numbering");
         for (int r = 0; r < q; ++r)
           if (members[r] == h) invalid("a handle appears twice in the batch");

@@ -510,8 +510,10 @@ __device__ __forceinline__ void tfsf_e_surface(const TfsfSurfParams<T> &p, int q
   if (!surface_cell(q, tf.lo[0], tf.hi[0], tf.lo[1], tf.hi[1], tf.lo[2], tf.hi[2], i, j, k)) return;
   const auto hinc = tfsf_view<T>(tf).inc + (((*p.step) + 1) & 1) * 6 * tf.L;   // incident H of the previous step
   const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
-  tfsf_e_component<0>(p, hinc, i, j, k, b);
-  tfsf_e_component<1>(p, hinc, i, j, k, b);
+  if (!tf.two_d) {   // TFSF2D::updateE corrects Ez only (tfsf_2d.cpp:192-228)
+    tfsf_e_component<0>(p, hinc, i, j, k, b);
+    tfsf_e_component<1>(p, hinc, i, j, k, b);
+  }
   tfsf_e_component<2>(p, hinc, i, j, k, b);
 }
 
@@ -534,9 +536,12 @@ __device__ __forceinline__ void tfsf_h_surface(const TfsfSurfParams<T> &p, int q
   const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
   // Hx: y faces (j = lj-1: += cby Ez_inc(i, lj, k); j = rj: -= cby Ez_inc(i, rj, k)),
   //     z faces (k = lk-1: -= cbz Ey_inc(i, j, lk); k = rk: += cbz Ey_inc(i, j, rk))
+  // TFSF2D::updateH (tfsf_2d.cpp:150-190) keeps the x- and y-face terms of
+  // Hx and Hy: no z faces, no Hz
+  const bool two_d = tf.two_d != 0;
   {
     const bool w1 = (j == lj - 1 || j == rj) && k >= lk && k < rk && i >= li && i <= ri;
-    const bool w2 = (k == lk - 1 || k == rk) && i >= li && i <= ri && j >= lj && j < rj;
+    const bool w2 = !two_d && (k == lk - 1 || k == rk) && i >= li && i <= ri && j >= lj && j < rj;
     if (w1 || w2) {
       T h = p.F[3][b];
       if (w1) {
@@ -558,7 +563,7 @@ __device__ __forceinline__ void tfsf_h_surface(const TfsfSurfParams<T> &p, int q
   //     z faces (k = lk-1: += cbz Ex_inc(i, j, lk); k = rk: -= cbz Ex_inc(i, j, rk))
   {
     const bool w1 = (i == li - 1 || i == ri) && j >= lj && j <= rj && k >= lk && k < rk;
-    const bool w2 = (k == lk - 1 || k == rk) && i >= li && i < ri && j >= lj && j <= rj;
+    const bool w2 = !two_d && (k == lk - 1 || k == rk) && i >= li && i < ri && j >= lj && j <= rj;
     if (w1 || w2) {
       T h = p.F[4][b];
       if (w1) {
@@ -578,7 +583,7 @@ __device__ __forceinline__ void tfsf_h_surface(const TfsfSurfParams<T> &p, int q
   }
   // Hz: x faces (i = li-1: += cbx Ey_inc(li, j, k); i = ri: -= cbx Ey_inc(ri, j, k)),
   //     y faces (j = lj-1: -= cby Ex_inc(i, lj, k); j = rj: += cby Ex_inc(i, rj, k))
-  {
+  if (!two_d) {
     const bool w1 = (i == li - 1 || i == ri) && j >= lj && j < rj && k >= lk && k <= rk;
     const bool w2 = (j == lj - 1 || j == rj) && k >= lk && k <= rk && i >= li && i < ri;
     if (w1 || w2) {

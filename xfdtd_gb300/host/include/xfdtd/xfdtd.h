@@ -322,6 +322,16 @@ class TFSF3D : public TFSF {
       : TFSF(distance_x, distance_y, distance_z, e_0, theta_inc, phi_inc, psi, std::move(waveform)) {}
 };
 
+// The plane wave of the 2-D (nz = 1) TMz grid (src/include/tfsf/tfsf_2d.h:8-10,
+// src/tfsf/tfsf_2d.cpp:7-10): the TFSF base with theta = pi / 2, psi = 0
+// and no z offset; Ez, Hx and Hy corrections on the x and y faces only.
+class TFSF2D : public TFSF {
+ public:
+  TFSF2D(SpatialIndex distance_x, SpatialIndex distance_y, double phi_inc, double ez_i0,
+         std::shared_ptr<Waveform> waveform)
+      : TFSF(distance_x, distance_y, 0, ez_i0, constant::PI / 2, phi_inc, 0, std::move(waveform)) {}
+};
+
 // ------------------------------------------------------------------ NF-FF
 class NFFFT {
  public:
@@ -624,6 +634,9 @@ class GridSpace {
   void extendBoundary(Orientation o, double size);
   void generateUniformGridSpace();
   size_t n(int axis) const { return _n[axis]; }
+  // 3 or 2 (GridSpace::Dimension, grid_space.cpp:513-533): the 2-D grid
+  // has x and y extended and nz = 1
+  int dim() const { return _dim; }
   double base(int axis) const { return _base[axis]; }
   double eNode(int axis, size_t i) const { return _ec[axis][i]; }
   double hNode(int axis, size_t i) const { return _hc[axis][i]; }
@@ -638,6 +651,7 @@ class GridSpace {
   double _base[3];
   double _mn[3], _mx[3];
   size_t _n[3] = {0, 0, 0};
+  int _dim = 0;
   bool _ready = false;
   std::vector<double> _ec[3], _hc[3];
   void resize(const double *mn, const double *mx);

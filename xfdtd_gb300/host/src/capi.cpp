@@ -98,7 +98,11 @@ int xfdtd_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, int precis
     if (sc->tfsf.enabled) {
       const auto &t = sc->tfsf;
       std::shared_ptr<Waveform> w = makeWaveform(t.waveform);
-      s->tfsf = std::make_shared<TFSF3D>(static_cast<SpatialIndex>(t.distance[0]), static_cast<SpatialIndex>(t.distance[1]),
+      if (t.enabled == 2)   // TFSF2D(distance_x, distance_y, phi, e0, waveform)
+        s->tfsf = std::make_shared<TFSF2D>(static_cast<SpatialIndex>(t.distance[0]),
+                                           static_cast<SpatialIndex>(t.distance[1]), t.phi, t.e0, w);
+      else
+        s->tfsf = std::make_shared<TFSF3D>(static_cast<SpatialIndex>(t.distance[0]), static_cast<SpatialIndex>(t.distance[1]),
                                          static_cast<SpatialIndex>(t.distance[2]), t.e0, t.theta, t.phi, t.psi, w);
       sim->addTFSFSource(s->tfsf);
     }

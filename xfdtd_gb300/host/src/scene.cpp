@@ -208,8 +208,11 @@ void GridSpace::extendBoundary(Orientation o, double size) {  // extendBoundary{
 void GridSpace::generateUniformGridSpace() {  // :501-538, :625-638, :737-757
   if (_ready) throw std::runtime_error("GridSpace is ready");
   for (int a = 0; a < 3; ++a) _n[a] = std::max<size_t>(_n[a], 1);
-  if (!(_n[0] > 1 && _n[1] > 1 && _n[2] > 1))
-    throw std::runtime_error("the GPU engine runs three-dimensional grids only");
+  // :513-533: three extended axes make the 3-D grid; the 2-D grid of the
+  // TMz path has x and y extended and nz = 1 (the 1-D grid is not built)
+  if (_n[0] > 1 && _n[1] > 1 && _n[2] > 1) _dim = 3;
+  else if (_n[0] > 1 && _n[1] > 1 && _n[2] == 1) _dim = 2;
+  else throw std::runtime_error("the GPU engine runs the 3-D grid and the 2-D (nz = 1) grid only");
   for (int a = 0; a < 3; ++a) {
     _ec[a].resize(_n[a] + 1);
     for (size_t i = 0; i <= _n[a]; ++i) _ec[a][i] = _mn[a] + static_cast<double>(i) * _base[a];

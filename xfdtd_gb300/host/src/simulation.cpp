@@ -272,7 +272,29 @@ void Simulation::init(size_t total_time_steps) {
   _nz = gs.n(2);
   const size_t nx = _nx, ny = _ny, nz = _nz;
   const double d[3] = {gs.base(0), gs.base(1), gs.base(2)};
-  _dt = static_cast<double>(_cfl) / (constant::C_0 * std::sqrt(1.0 / (d[0] * d[0]) + 1.0 / (d[1] * d[1]) + 1.0 / (d[2] * d[2])));
+  const bool two_d = gs.dim() == 2;
+  if (two_d)   // FDTDBasicCoff::init, fdtd_basic_coff.cpp:19-21: calculateDeltaT(cfl, dx, dy)
+    _dt = static_cast<double>(_cfl) / (constant::C_0 * std::sqrt(1.0 / (d[0] * d[0]) + 1.0 / (d[1] * d[1])));
+  else
+    _dt = static_cast<double>(_cfl) / (constant::C_0 * std::sqrt(1.0 / (d[0] * d[0]) + 1.0 / (d[1] * d[1]) + 1.0 / (d[2] * d[2])));
+  if (two_d && _tfsf && !dynamic_cast<const TFSF2D *>(_tfsf.get()))
+    throw std::runtime_error("a 2-D grid (nz = 1) takes TFSF2D");
+  if (!two_d && _tfsf && dynamic_cast<const TFSF2D *>(_tfsf.get()))
+    throw std::runtime_error("TFSF2D needs a 2-D grid (nz = 1)");
+  if (two_d) {
+    // The 2-D path carries what the reference's 2-D example uses: objects,
+    // the x and y CPML, TFSF2D and field (movie) monitors.  Its 2-D far
+    // field is a debug output (nffft_broadband.cpp:173-180), and its
+    // lumped elements and voltage/current monitors divide by the z cell
+    // size, which a 2-D GridSpace reports as 0 (grid_space.cpp:180-186).
+    if (_nffft) throw std::runtime_error("the 2-D grid (nz = 1) carries no NF-FF box");
+    if (!_lumped_elements.empty()) throw std::runtime_error("the 2-D grid (nz = 1) carries no lumped elements");
+    for (auto &o : _objects)
+      if (o->isThinWire()) throw std::runtime_error("the 2-D grid (nz = 1) carries no thin wires");
+    for (auto &m : _monitors)
+      if (dynamic_cast<const VoltageMonitor *>(m.get()) || dynamic_cast<const CurrentMonitor *>(m.get()))
+        throw std::runtime_error("the 2-D grid (nz = 1) carries field monitors only");
+  }
   const double dt = _dt;
   if (_tfsf) _tfsf->bindTimeStep(dt);
 
@@ -318,13 +340,17 @@ void Simulation::init(size_t total_time_steps) {
       r0[a] = static_cast<size_t>(std::lower_bound(hc.begin(), hc.end(), lo[a] - tol) - hc.begin());
       r1[a] = static_cast<size_t>(std::upper_bound(hc.begin(), hc.end(), hi[a] + tol) - hc.begin());
     }
+    // the 2-D mask takes the cell centre at z = 0 (GridSpace::getShapeMask
+    // and getGridCenterZ, grid_space.cpp:241-247, 284-291): its one k plane
+    // is a candidate whatever the z of the centre node
+    if (two_d) r0[2] = 0, r1[2] = 1;
     const Shape &sh = o->shape();
     if (r1[0] > r0[0])
       parallel_for(r1[0] - r0[0], [&](size_t q) {   // planes of one object: disjoint cells
         const size_t i = r0[0] + q;
         for (size_t j = r0[1]; j < r1[1]; ++j)
           for (size_t k = r0[2]; k < r1[2]; ++k)
-            if (sh.isPointInside(PointVector{gs.hNode(0, i), gs.hNode(1, j), gs.hNode(2, k)}))
+            if (sh.isPointInside(PointVector{gs.hNode(0, i), gs.hNode(1, j), two_d ? 0.0 : gs.hNode(2, k)}))
               cell_mat[(i * ny + j) * nz + k] = id;
       });
   }
@@ -649,17 +675,25 @@ void Simulation::init(size_t total_time_steps) {
     // tfsf_3d.cpp:47-57
     const double ratio_delta = 1 / std::sqrt(std::pow(std::sin(th), 4) * (std::pow(std::cos(phi), 4) + std::pow(std::sin(phi), 4)) +
                                              std::pow(std::cos(th), 4));
-    const double diagonal = std::sqrt(std::pow(bn[0], 2) + std::pow(bn[1], 2) + std::pow(bn[2], 2)) * ratio_delta;
+    // TFSF2D::init (tfsf_2d.cpp:44-46) takes sqrt(nz^2) where TFSF3D takes nz^2
+    const double diagonal =
+        two_d ? std::sqrt(std::pow(bn[0], 2) + std::pow(bn[1], 2) + std::sqrt(std::pow(bn[2], 2))) * ratio_delta
+              : std::sqrt(std::pow(bn[0], 2) + std::pow(bn[1], 2) + std::pow(bn[2], 2)) * ratio_delta;
     const size_t L = static_cast<size_t>(std::ceil(diagonal)) + 4 + 1;
-    // origin = box corner on the incoming side - 2 k / ratio_delta (:66-109)
+    // origin = box corner on the incoming side - 2 k / ratio_delta (:66-109;
+    // 2-D: tfsf_2d.cpp:55-75, corner z = 0)
     double orig[3];
     for (int a = 0; a < 3; ++a)
       orig[a] = (k[a] >= 0 ? static_cast<double>(lo[a]) : static_cast<double>(hi[a])) - 2 * k[a] / ratio_delta;
+    if (two_d) orig[2] = 0.0 - 2 * k[2] / ratio_delta;
     for (int a = 0; a < 3; ++a) {
       pf[a].resize(bn[a] + 1);
       ph[a].resize(bn[a] + 2);
-      for (size_t i = 0; i < bn[a] + 1; ++i) pf[a][i] = ((i + lo[a]) - orig[a]) * k[a] * ratio_delta;
-      for (size_t i = 0; i < bn[a] + 2; ++i) ph[a][i] = ((i + lo[a]) - orig[a] - 0.5) * k[a] * ratio_delta;
+      // the 2-D incident fields carry no z projection term (tfsf_2d.cpp:230-258):
+      // zero tables add nothing to the 3-D projection sums
+      const double kz = (two_d && a == 2) ? 0.0 : k[a];
+      for (size_t i = 0; i < bn[a] + 1; ++i) pf[a][i] = ((i + lo[a]) - orig[a]) * kz * ratio_delta;
+      for (size_t i = 0; i < bn[a] + 2; ++i) ph[a][i] = ((i + lo[a]) - orig[a] - 0.5) * kz * ratio_delta;
     }
     const double scaled_dl = d[0] / ratio_delta;
     // the incident wave: e0 * w(t dt), tfsf.cpp:51-52, 80-82
@@ -669,7 +703,7 @@ void Simulation::init(size_t total_time_steps) {
     source.resize(_total);
     for (size_t q = 0; q < _total; ++q) source[q] = t.getIncidentFieldAmplitude() * t.waveform()(q);
     xfdtd_tfsf_plan &tp = plan.tfsf;
-    tp.enabled = 1;
+    tp.enabled = two_d ? 2 : 1;
     tp.aux_len = static_cast<int32_t>(L);
     for (int a = 0; a < 3; ++a) {
       tp.lo[a] = static_cast<int64_t>(lo[a]);

@@ -362,6 +362,28 @@ class TFSF3D:
 
 
 @dataclass
+class TFSF2D:
+    """TFSF2D(distance_x, distance_y, phi_inc, ez_i0, waveform),
+    src/include/tfsf/tfsf_2d.h:8-10: the plane wave of the 2-D (nz = 1)
+    TMz grid, travelling in the x-y plane at angle phi_inc with Ez
+    polarisation.  It is the TFSF base with theta = pi / 2, psi = 0 and no
+    z offset (src/tfsf/tfsf_2d.cpp:8-10)."""
+    distance_x: int
+    distance_y: int
+    phi: float
+    e_0: float
+    waveform: Waveform
+
+    def desc(self) -> TFSFDesc:
+        d = TFSFDesc()
+        d.enabled = 2
+        d.distance[:] = [int(self.distance_x), int(self.distance_y), 0]
+        d.e0, d.theta, d.phi, d.psi = float(self.e_0), math.pi / 2, float(self.phi), 0.0
+        d.waveform = self.waveform.desc()
+        return d
+
+
+@dataclass
 class NffftFd:
     """NffftFd(distance_x, distance_y, distance_z, frequencies, theta, phi,
     output_dir_path), src/include/nffft/nffft_fd.h:39-50."""
@@ -528,7 +550,7 @@ class Scene:
     cell_size: float
     objects: List[object] = field(default_factory=list)
     boundaries: List[PML] = field(default_factory=list)
-    tfsf: Optional[TFSF3D] = None
+    tfsf: Optional[object] = None   # TFSF3D or TFSF2D
     nffft: Optional[object] = None   # NffftFd or NffftBroadBand
     lumped_elements: List[_Lumped] = field(default_factory=list)
     monitors: List[_Monitor] = field(default_factory=list)
