@@ -30,6 +30,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <functional>
+#include <iostream>   // the reference's headers bring it in, and its drivers print with std::cout
 #include <limits>
 #include <map>
 #include <memory>
@@ -56,6 +57,18 @@ inline constexpr double TOLERABLE_EPSILON{10 * std::numeric_limits<double>::epsi
 
 using PointVector = std::array<double, 3>;
 using SpatialIndex = size_t;
+
+// The angle lists the reference's drivers build with xt::linspace(start,
+// stop, num, endpoint) (examples/3d_pec_sphere_bistatic_rcs.cpp:78), as a
+// std::vector: element i is start + i * step, step = (stop - start) /
+// (num - 1) with the end point and (stop - start) / num without it.
+inline std::vector<double> linspace(double start, double stop, size_t num, bool endpoint = true) {
+  std::vector<double> v(num);
+  const size_t div = endpoint ? (num > 1 ? num - 1 : 1) : num;
+  const double step = num ? (stop - start) / static_cast<double>(div) : 0.0;
+  for (size_t i = 0; i < num; ++i) v[i] = start + static_cast<double>(i) * step;
+  return v;
+}
 enum class Orientation { XN, XP, YN, YP, ZN, ZP };
 enum class Axis { X, Y, Z };
 // src/include/electromagnetic_field/electromagnetic_field.h:8,

@@ -57,12 +57,6 @@ bool ensureDir(const std::filesystem::path &p) {
   return true;
 }
 
-std::vector<double> linspace(double a, double b, size_t n) {
-  std::vector<double> v(n);
-  const double step = n > 1 ? (b - a) / static_cast<double>(n - 1) : 0.0;
-  for (size_t i = 0; i < n; ++i) v[i] = a + static_cast<double>(i) * step;
-  return v;
-}
 
 }  // namespace
 

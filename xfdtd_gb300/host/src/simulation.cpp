@@ -208,16 +208,6 @@ Tuple coefficients(const Props &p, double dt, const double d[3]) {
   return c;
 }
 
-std::vector<double> linspace(double a, double b, size_t n) {  // xt::linspace with endpoint
-  std::vector<double> v(n);
-  if (n == 1) {
-    v[0] = a;
-    return v;
-  }
-  const double step = (b - a) / static_cast<double>(n - 1);
-  for (size_t i = 0; i < n; ++i) v[i] = a + static_cast<double>(i) * step;
-  return v;
-}
 
 struct CpmlProfile {
   std::vector<int> slot_e, slot_h;
