@@ -176,7 +176,8 @@ struct xfdtd_handle {
   // TMA-staged interior kernels (interior_tma.cuh): offered per side when the
   // interior's k range starts on a 16-byte boundary for fields and index
   bool it_ok[2] = {};
-  xg::ItMaps itm[2] = {};
+  xg::ItMaps itm[2] = {};     // interior launches (32 x 8 tiles), E and H side
+  xg::ItMaps itm_z[2] = {};   // z-edge launch (16 x 16 tiles)
   void *itm_base = nullptr;   // E_x buffer the maps were encoded for
   // split volume update, per side (0 E, 1 H): the plain interior box and
   // the shell around it, with their cell counts; shell register cap
@@ -594,6 +595,16 @@ void volume_boxes(xfdtd_handle *h, int side) {
       if (fl[q] & bit) run[a] = false;
   }
   const int px_lo = lo[0], px_hi = hi[0], py_lo = lo[1], py_hi = hi[1];
+  // the wide decomposition's k range: the plain run cut on 16-byte
+  // boundaries (TMA's alignment), so that the z-edge launch keeps only the
+  // CPML slabs and walls
+  int wk_lo = lo[2], wk_hi = hi[2];
+  {
+    const int q = 16 / static_cast<int>(h->esize);
+    const int l = (lo[2] + q - 1) / q * q, u = (hi[2] + 1) / q * q - 1;
+    wk_lo = l;
+    wk_hi = u;
+  }
   // cut on 128-byte lines, else (a short run) on 32-byte sectors, else not at all
   for (int bytes : {128, 32}) {
     const int q = bytes / static_cast<int>(h->esize);
@@ -695,8 +706,10 @@ void volume_boxes(xfdtd_handle *h, int side) {
     in = xg::InteriorBox{};
     long long total = 0;
     unsigned blocks = 0;
-    h->wide_ok[side] = interior;
-    if (interior) {
+    h->wide_ok[side] = interior && wk_lo <= wk_hi;
+    lo[2] = wk_lo;   // the shell boxes below follow the wide k range
+    hi[2] = wk_hi;
+    if (h->wide_ok[side]) {
       in.lo[0] = 0, in.hi[0] = n[0];
       in.lo[1] = 0, in.hi[1] = n[1];
       in.lo[2] = lo[2], in.hi[2] = hi[2];
@@ -817,75 +830,86 @@ void sweep_setup(xfdtd_handle *h) {
 // Tensor maps of the TMA-staged interior kernels over the current buffers:
 // E kernel H tiles (HW x 9 rows), E and index tiles (32 x 8); H kernel E
 // tiles (EW x 9 rows), H and index tiles.
+// The maps of the interior launches (32 x 8 tiles: itm) and of the z-edge
+// launch (16 x 16 tiles: itm_z).
 template <typename T, typename I>
 void interior_tma_encode(xfdtd_handle *h) {
-  using G = xg::ItTiles<T, I>;
   const CUtensorMapDataType dt = sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-  const CUtensorMapDataType it = sizeof(I) == 1   ? CU_TENSOR_MAP_DATA_TYPE_UINT8
-                                 : sizeof(I) == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16
-                                                  : CU_TENSOR_MAP_DATA_TYPE_UINT32;
-  for (int c = 0; c < 3; ++c) {
-    encode_map(h, &h->itm[0].a[c], h->F[3 + c], dt, sizeof(T), G::HW, xg::kItJ + 1);
-    encode_map(h, &h->itm[0].b[c], h->F[c], dt, sizeof(T), xg::kItK, xg::kItJ);
-    encode_map(h, &h->itm[1].a[c], h->F[c], dt, sizeof(T), G::EW, xg::kItJ + 1);
-    encode_map(h, &h->itm[1].b[c], h->F[3 + c], dt, sizeof(T), xg::kItK, xg::kItJ);
-  }
-  for (int side = 0; side < 2; ++side) encode_map(h, &h->itm[side].idx, h->idx, it, sizeof(I), xg::kItK, xg::kItJ);
+  auto encode = [&](xg::ItMaps *m, auto geom) {
+    using G = decltype(geom);
+    constexpr unsigned KT = static_cast<unsigned>(xg::kItThreads / G::J);
+    for (int c = 0; c < 3; ++c) {
+      encode_map(h, &m[0].a[c], h->F[3 + c], dt, sizeof(T), G::HW, G::J + 1);
+      encode_map(h, &m[0].b[c], h->F[c], dt, sizeof(T), KT, G::J);
+      encode_map(h, &m[1].a[c], h->F[c], dt, sizeof(T), G::EW, G::J + 1);
+      encode_map(h, &m[1].b[c], h->F[3 + c], dt, sizeof(T), KT, G::J);
+    }
+  };
+  encode(h->itm, xg::ItTiles<T, xg::kItK>{});
+  encode(h->itm_z, xg::ItTiles<T, xg::kItKz>{});
   h->itm_base = h->F[0];
 }
 
 // Which sides may run the TMA-staged interior kernels: the interior's first
 // k (and, for the E kernel, its H tile's first column) on a 16-byte
-// boundary for the fields and the index.
+// boundary for the fields; for the wide decomposition, the same of its k
+// range and of the k after its last (where the z-edge launch's upper tiles
+// start).  The material index is read with plain loads.
 template <typename T, typename I>
 void interior_tma_setup(xfdtd_handle *h) {
-  using G = xg::ItTiles<T, I>;
-  const int es = static_cast<int>(sizeof(T)), is = static_cast<int>(sizeof(I));
+  using G = xg::ItTiles<T, xg::kItK>;
+  using Gz = xg::ItTiles<T, xg::kItKz>;
+  const int es = static_cast<int>(sizeof(T));
   for (int side = 0; side < 2; ++side) {
     const int k = h->vin[side].lo[2], kh = side == 0 ? k - G::HOFF - 1 : k;
-    h->it_ok[side] = h->vin_cells[side] > 0 && kh >= 0 && (k * es) % 16 == 0 && (kh * es) % 16 == 0 && (k * is) % 16 == 0;
+    h->it_ok[side] = h->vin_cells[side] > 0 && kh >= 0 && (k * es) % 16 == 0 && (kh * es) % 16 == 0;
   }
   if (!(h->it_ok[0] && h->it_ok[1])) return;
   interior_tma_encode<T, I>(h);
   auto attr = [](auto kern, int bytes) {
     XCHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   };
-  auto attrs = [&](auto mode) {
+  auto attrs = [&](auto mode, auto kt) {
     constexpr int M = decltype(mode)::value;
-    attr(xg::k_interior_tma_e<T, I, 4, false, M>, G::template smem_e<4>());
-    attr(xg::k_interior_tma_e<T, I, 6, false, M>, G::template smem_e<6>());
-    attr(xg::k_interior_tma_e<T, I, 4, true, M>, G::template smem_e<4>());
-    attr(xg::k_interior_tma_h<T, I, 4, false, M>, G::template smem_h<4>());
-    attr(xg::k_interior_tma_h<T, I, 6, false, M>, G::template smem_h<6>());
-    attr(xg::k_interior_tma_h<T, I, 4, true, M>, G::template smem_h<4>());
+    constexpr int KT = decltype(kt)::value;
+    using GG = xg::ItTiles<T, KT>;
+    attr(xg::k_interior_tma_e<T, I, 4, false, M, KT>, GG::template smem_e<4>());
+    attr(xg::k_interior_tma_e<T, I, 6, false, M, KT>, GG::template smem_e<6>());
+    attr(xg::k_interior_tma_e<T, I, 4, true, M, KT>, GG::template smem_e<4>());
+    attr(xg::k_interior_tma_h<T, I, 4, false, M, KT>, GG::template smem_h<4>());
+    attr(xg::k_interior_tma_h<T, I, 6, false, M, KT>, GG::template smem_h<6>());
+    attr(xg::k_interior_tma_h<T, I, 4, true, M, KT>, GG::template smem_h<4>());
   };
-  attrs(std::integral_constant<int, 0>{});
-  // the z-edge launch's upper tiles start after the interior's last k
+  attrs(std::integral_constant<int, 0>{}, std::integral_constant<int, xg::kItK>{});
   for (int side = 0; side < 2; ++side) {
-    const int k = h->vin[side].hi[2] + 1, kh = side == 0 ? k - G::HOFF - 1 : k;
-    if ((k * es) % 16 || (kh * es) % 16 || (k * is) % 16) h->wide_ok[side] = false;
+    if (!h->wide_ok[side]) continue;
+    const int k = h->vin_w[side].lo[2], kh = side == 0 ? k - G::HOFF - 1 : k;
+    const int ku = h->vin_w[side].hi[2] + 1, kuh = side == 0 ? ku - Gz::HOFF - 1 : ku;
+    if (kh < 0 || (k * es) % 16 || (kh * es) % 16 || (ku * es) % 16 || (kuh * es) % 16) h->wide_ok[side] = false;
   }
   if (!(h->wide_ok[0] && h->wide_ok[1])) return;
-  attrs(std::integral_constant<int, 1>{});
-  attrs(std::integral_constant<int, 2>{});
+  attrs(std::integral_constant<int, 1>{}, std::integral_constant<int, xg::kItK>{});
+  attrs(std::integral_constant<int, 2>{}, std::integral_constant<int, xg::kItKz>{});
 }
 
 template <typename T, typename I, int S, bool CT, int MODE>
 void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, int chunk, cudaStream_t st) {
-  using G = xg::ItTiles<T, I>;
+  constexpr int KT = MODE == 2 ? xg::kItKz : xg::kItK;
+  using G = xg::ItTiles<T, KT>;
   if (h->itm_base != h->F[0]) interior_tma_encode<T, I>(h);   // the buffers were swapped
   const int side = e_side ? 0 : 1;
   const xg::InteriorBox in = MODE == 2 ? h->vin_z[side] : side_interior(h, side, MODE == 1);
   const int nj = in.hi[1] - in.lo[1] + 1, ni = in.hi[0] - in.lo[0] + 1;
-  const int nkt = MODE == 2 ? (in.pz_lo + xg::kItK - 1) / xg::kItK + (in.hi[2] - in.pz_hi + xg::kItK - 1) / xg::kItK
-                            : (in.hi[2] - in.lo[2] + xg::kItK) / xg::kItK;
-  dim3 grid(nkt, (nj + xg::kItJ - 1) / xg::kItJ, (ni + chunk - 1) / chunk);
+  const int nkt = MODE == 2 ? (in.pz_lo + KT - 1) / KT + (in.hi[2] - in.pz_hi + KT - 1) / KT
+                            : (in.hi[2] - in.lo[2] + KT) / KT;
+  dim3 grid(nkt, (nj + G::J - 1) / G::J, (ni + chunk - 1) / chunk);
+  const xg::ItMaps *maps = MODE == 2 ? h->itm_z : h->itm;
   if (e_side)
-    xg::k_interior_tma_e<T, I, S, CT, MODE>
-        <<<grid, xg::kItThreads, G::template smem_e<S>(), st>>>(h->itm[0], p, in, chunk, h->d_status, h->wait_polls);
+    xg::k_interior_tma_e<T, I, S, CT, MODE, KT>
+        <<<grid, xg::kItThreads, G::template smem_e<S>(), st>>>(maps[0], p, in, chunk, h->d_status, h->wait_polls);
   else
-    xg::k_interior_tma_h<T, I, S, CT, MODE>
-        <<<grid, xg::kItThreads, G::template smem_h<S>(), st>>>(h->itm[1], p, in, chunk, h->d_status, h->wait_polls);
+    xg::k_interior_tma_h<T, I, S, CT, MODE, KT>
+        <<<grid, xg::kItThreads, G::template smem_h<S>(), st>>>(maps[1], p, in, chunk, h->d_status, h->wait_polls);
 }
 
 // After a sweep the second buffer set holds step t+1: make it current.

@@ -11,14 +11,20 @@
 // updated; an mbarrier per stage counts the bytes in.  The threads read
 // the tiles from shared memory, apply the same per-cell arithmetic as the
 // fast path (e_plain / h_plain with the same coefficients) and store the
-// updated plane straight to global memory.
+// updated plane straight to global memory.  The 1-byte (or 2-, 4-byte)
+// material index is read with plain loads, issued before the wait for the
+// plane: a tile of it is 8 to 32 bytes a row, and its rows need no 16-byte
+// alignment that way.
 //
-//   E kernel: plane i needs H(i) on rows j0-1 .. j0+7 and columns k0-1 ..
-//   k0+31, H(i-1) on the tile (the previous stage), E(i) and the index on
-//   the tile.
-//   H kernel: plane i needs E(i) on rows j0 .. j0+8 and columns k0 ..
-//   k0+32, E(i+1) on the tile (the next stage), H(i) and the index on the
-//   tile.
+// The tile is KT cells along k by 256 / KT rows along j: 32 x 8 for the
+// interior launches, 16 x 16 for the z-edge launch, whose k runs (the CPML
+// slabs and walls below and above the interior's k range) are 10 to 16
+// cells long.
+//
+//   E kernel: plane i needs H(i) on rows j0-1 .. j0+J-1 and columns k0-1
+//   .. k0+KT-1, H(i-1) on the tile (the previous stage), E(i) on the tile.
+//   H kernel: plane i needs E(i) on rows j0 .. j0+J and columns k0 ..
+//   k0+KT, E(i+1) on the tile (the next stage), H(i) on the tile.
 //
 // MODE selects the cells a launch covers:
 //   0  the interior box, plain on every axis;
@@ -50,35 +56,37 @@
 
 namespace xg {
 
-constexpr int kItK = 32;                  // tile: 32 cells along k
-constexpr int kItJ = 8;                   //        8 rows along j
-constexpr int kItThreads = kItK * kItJ;
+constexpr int kItThreads = 256;
+constexpr int kItK = 32;                  // interior launches' tile: 32 cells along k
+constexpr int kItKz = 16;                 // z-edge launch's tile: 16 cells along k
 constexpr int kItWaitLimit = 1 << 22;     // polls of a stage barrier before giving up
 
-// Tile geometry.  E kernel: H rows of HW columns starting at k0-HOFF-1,
-// 9 rows from j0-1; E and index tiles 32 x 8 from (k0, j0).  H kernel: E
-// rows of EW columns starting at k0, 9 rows from j0; H and index tiles
-// 32 x 8.
-template <typename T, typename I>
+// Tile geometry of a KT-wide tile (J = 256 / KT rows).  E kernel: H rows of
+// HW columns starting at k0-HOFF-1, J+1 rows from j0-1; E tiles KT x J from
+// (k0, j0).  H kernel: E rows of EW columns starting at k0, J+1 rows from
+// j0; H tiles KT x J.  HW and EW are whole 16-byte rows.
+template <typename T, int KT>
 struct ItTiles {
+  static constexpr int J = kItThreads / KT;
   static constexpr int HOFF = sizeof(T) == 4 ? 3 : 1;
-  static constexpr int HW = sizeof(T) == 4 ? 40 : 36;    // covers k0-HOFF-1 .. k0+32+
-  static constexpr int EW = sizeof(T) == 4 ? 36 : 34;    // covers k0 .. k0+32+
+  static constexpr int HW = KT == 32 ? (sizeof(T) == 4 ? 40 : 36)    // covers k0-HOFF-1 .. k0+KT-1
+                                     : (sizeof(T) == 4 ? 20 : 18);
+  static constexpr int EW = KT == 32 ? (sizeof(T) == 4 ? 36 : 34)    // covers k0 .. k0+KT
+                                     : (sizeof(T) == 4 ? 20 : 18);
   static constexpr int RND = 128;
   static constexpr int rnd(int b) { return (b + RND - 1) / RND * RND; }
-  // E kernel stage: 3 H tiles (halo), 3 E tiles, index tile
-  static constexpr int EH_TILE = rnd((kItJ + 1) * HW * int(sizeof(T)));
-  static constexpr int EE_TILE = rnd(kItJ * kItK * int(sizeof(T)));
-  static constexpr int I_TILE = rnd(kItJ * kItK * int(sizeof(I)));
-  static constexpr int E_STAGE = 3 * EH_TILE + 3 * EE_TILE + I_TILE;
-  static constexpr unsigned E_HBYTES = 3u * (kItJ + 1) * HW * sizeof(T);
-  static constexpr unsigned E_FULL = E_HBYTES + 3u * kItJ * kItK * sizeof(T) + unsigned(kItJ * kItK * sizeof(I));
-  // H kernel stage: 3 E tiles (halo), 3 H tiles, index tile
-  static constexpr int HE_TILE = rnd((kItJ + 1) * EW * int(sizeof(T)));
+  // E kernel stage: 3 H tiles (halo), 3 E tiles
+  static constexpr int EH_TILE = rnd((J + 1) * HW * int(sizeof(T)));
+  static constexpr int EE_TILE = rnd(J * KT * int(sizeof(T)));
+  static constexpr int E_STAGE = 3 * EH_TILE + 3 * EE_TILE;
+  static constexpr unsigned E_HBYTES = 3u * (J + 1) * HW * sizeof(T);
+  static constexpr unsigned E_FULL = E_HBYTES + 3u * J * KT * sizeof(T);
+  // H kernel stage: 3 E tiles (halo), 3 H tiles
+  static constexpr int HE_TILE = rnd((J + 1) * EW * int(sizeof(T)));
   static constexpr int HH_TILE = EE_TILE;
-  static constexpr int H_STAGE = 3 * HE_TILE + 3 * HH_TILE + I_TILE;
-  static constexpr unsigned H_EBYTES = 3u * (kItJ + 1) * EW * sizeof(T);
-  static constexpr unsigned H_FULL = H_EBYTES + 3u * kItJ * kItK * sizeof(T) + unsigned(kItJ * kItK * sizeof(I));
+  static constexpr int H_STAGE = 3 * HE_TILE + 3 * HH_TILE;
+  static constexpr unsigned H_EBYTES = 3u * (J + 1) * EW * sizeof(T);
+  static constexpr unsigned H_FULL = H_EBYTES + 3u * J * KT * sizeof(T);
   template <int STAGES>
   static constexpr int smem_e() { return STAGES * E_STAGE + STAGES * 8; }
   template <int STAGES>
@@ -86,11 +94,10 @@ struct ItTiles {
 };
 
 // Tensor maps of one launch: a[3] the halo tiles (H for the E kernel, E for
-// the H kernel), b[3] the updated side's tiles, the index.
+// the H kernel), b[3] the updated side's tiles.
 struct ItMaps {
   CUtensorMap a[3];
   CUtensorMap b[3];
-  CUtensorMap idx;
 };
 
 // The block's planes and tile: k0, j0 of the tile, its last k khi, planes
@@ -100,20 +107,20 @@ struct ItMaps {
 struct ItBlock {
   int k0, khi, j0, ia, ib;
 };
-template <int MODE>
+template <int MODE, int KT>
 __device__ __forceinline__ ItBlock it_block(const InteriorBox &in, int chunk) {
   ItBlock b;
   const int t = static_cast<int>(blockIdx.x);
   if (MODE == 2) {
-    const int nlo = (in.pz_lo + kItK - 1) / kItK;
+    const int nlo = (in.pz_lo + KT - 1) / KT;
     const bool below = t < nlo;
-    b.k0 = below ? t * kItK : in.pz_hi + 1 + (t - nlo) * kItK;
+    b.k0 = below ? t * KT : in.pz_hi + 1 + (t - nlo) * KT;
     b.khi = below ? in.pz_lo - 1 : in.hi[2];
   } else {
-    b.k0 = in.lo[2] + t * kItK;
+    b.k0 = in.lo[2] + t * KT;
     b.khi = in.hi[2];
   }
-  b.j0 = in.lo[1] + static_cast<int>(blockIdx.y) * kItJ;
+  b.j0 = in.lo[1] + static_cast<int>(blockIdx.y) * (kItThreads / KT);
   b.ia = in.lo[0] + static_cast<int>(blockIdx.z) * chunk;
   b.ib = min(b.ia + chunk, in.hi[0] + 1);
   return b;
@@ -145,22 +152,21 @@ struct ItRing {
   }
 };
 
-template <typename T, typename I, int STAGES, bool CT, int MODE>
+template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK>
 __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
                                                                InteriorBox in, int chunk, int *status,
                                                                int wait_limit) {
-  using G = ItTiles<T, I>;
+  using G = ItTiles<T, KT>;
   extern __shared__ __align__(128) unsigned char smem[];
   ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::E_STAGE), wait_limit};
-  const int tid = threadIdx.x, c = tid & 31, r = tid >> 5;
-  const ItBlock blk = it_block<MODE>(in, chunk);
+  const int tid = threadIdx.x, c = tid % KT, r = tid / KT;
+  const ItBlock blk = it_block<MODE, KT>(in, chunk);
   if (blk.ia >= blk.ib) return;
   auto stage_of = [&](int q) { return (q - blk.ia + 1) % STAGES; };   // plane ia-1 in stage 0
   auto htile = [&](int st, int comp) { return reinterpret_cast<const T *>(smem + st * G::E_STAGE + comp * G::EH_TILE); };
   auto etile = [&](int st, int comp) {
     return reinterpret_cast<const T *>(smem + st * G::E_STAGE + 3 * G::EH_TILE + comp * G::EE_TILE);
   };
-  auto itile = [&](int st) { return reinterpret_cast<const I *>(smem + st * G::E_STAGE + 3 * G::EH_TILE + 3 * G::EE_TILE); };
   auto issue = [&](int q) {   // thread 0: the loads of plane q (H only for plane ia-1)
     const int st = stage_of(q);
     const bool full = q >= blk.ia;
@@ -171,7 +177,6 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
     if (full) {
       for (int comp = 0; comp < 3; ++comp)
         tma_load_3d(base + 3 * G::EH_TILE + comp * G::EE_TILE, &maps.b[comp], blk.k0, blk.j0, q, &ring.bar[st]);
-      tma_load_3d(base + 3 * G::EH_TILE + 3 * G::EE_TILE, &maps.idx, blk.k0, blk.j0, q, &ring.bar[st]);
     }
   };
   int issued = blk.ia - 2, waited = blk.ia - 2;   // thread 0: last plane issued, last plane waited
@@ -208,6 +213,8 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
       }
       ps = e_psi_load<T, I, 7>(p, cx, i, j, k, p.psi);
     }
+    const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
+    const unsigned m = mine ? static_cast<unsigned>(__ldg(p.idx + b)) : 0u;
     if (ring.wait(stage_of(i))) waited = i;
     if (mine && !ring.timed_out) {
       const int st = stage_of(i), sm = stage_of(i - 1);
@@ -216,10 +223,9 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
       ECurl<T> h{hv(st, 0, r + 1, c + 1), hv(st, 1, r + 1, c + 1), hv(st, 2, r + 1, c + 1),
                        hv(st, 0, r + 1, c),     hv(st, 1, r + 1, c),     hv(st, 0, r, c + 1),
                        hv(st, 2, r, c + 1),     hv(sm, 1, r + 1, c + 1), hv(sm, 2, r + 1, c + 1)};
-      T ex = etile(st, 0)[r * kItK + c], ey = etile(st, 1)[r * kItK + c], ez = etile(st, 2)[r * kItK + c];
+      T ex = etile(st, 0)[r * KT + c], ey = etile(st, 1)[r * KT + c], ez = etile(st, 2)[r * KT + c];
       T cf[9];
-      coefs<T, I, CT>(p, p.table, 18, static_cast<unsigned>(itile(st)[r * kItK + c]), 0, cf);
-      const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
+      coefs<T, I, CT>(p, p.table, 18, m, 0, cf);
       if (MODE != 2 && cls == 0) {
         e_plain(cf, h, ex, ey, ez);
         p.E[0][b] = ex;
@@ -261,22 +267,21 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
   }
 }
 
-template <typename T, typename I, int STAGES, bool CT, int MODE>
+template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK>
 __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
                                                                InteriorBox in, int chunk, int *status,
                                                                int wait_limit) {
-  using G = ItTiles<T, I>;
+  using G = ItTiles<T, KT>;
   extern __shared__ __align__(128) unsigned char smem[];
   ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::H_STAGE), wait_limit};
-  const int tid = threadIdx.x, c = tid & 31, r = tid >> 5;
-  const ItBlock blk = it_block<MODE>(in, chunk);
+  const int tid = threadIdx.x, c = tid % KT, r = tid / KT;
+  const ItBlock blk = it_block<MODE, KT>(in, chunk);
   if (blk.ia >= blk.ib) return;
   auto stage_of = [&](int q) { return (q - blk.ia) % STAGES; };
   auto etile = [&](int st, int comp) { return reinterpret_cast<const T *>(smem + st * G::H_STAGE + comp * G::HE_TILE); };
   auto htile = [&](int st, int comp) {
     return reinterpret_cast<const T *>(smem + st * G::H_STAGE + 3 * G::HE_TILE + comp * G::HH_TILE);
   };
-  auto itile = [&](int st) { return reinterpret_cast<const I *>(smem + st * G::H_STAGE + 3 * G::HE_TILE + 3 * G::HH_TILE); };
   auto issue = [&](int q) {   // thread 0: the loads of plane q (E only for plane ib)
     const int st = stage_of(q);
     const bool full = q < blk.ib;
@@ -287,7 +292,6 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
     if (full) {
       for (int comp = 0; comp < 3; ++comp)
         tma_load_3d(base + 3 * G::HE_TILE + comp * G::HH_TILE, &maps.b[comp], blk.k0, blk.j0, q, &ring.bar[st]);
-      tma_load_3d(base + 3 * G::HE_TILE + 3 * G::HH_TILE, &maps.idx, blk.k0, blk.j0, q, &ring.bar[st]);
     }
   };
   int issued = blk.ia - 1, waited = blk.ia - 1;   // thread 0: last plane issued, last plane waited
@@ -322,6 +326,8 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
       }
       pv = h_psi_load<T, I, 7>(p, cx, i, j, k);
     }
+    const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
+    const unsigned m = mine ? static_cast<unsigned>(__ldg(p.idx + b)) : 0u;
     if (ring.wait(stage_of(i + 1))) waited = i + 1;
     if (mine && !ring.timed_out) {
       const int st = stage_of(i), sn = stage_of(i + 1);
@@ -330,10 +336,9 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
       HCurl<T> e{ev(st, 0, r, c),     ev(st, 1, r, c),     ev(st, 2, r, c),
                        ev(st, 0, r, c + 1), ev(st, 1, r, c + 1), ev(st, 0, r + 1, c),
                        ev(st, 2, r + 1, c), ev(sn, 1, r, c),     ev(sn, 2, r, c)};
-      T hx = htile(st, 0)[r * kItK + c], hy = htile(st, 1)[r * kItK + c], hz = htile(st, 2)[r * kItK + c];
+      T hx = htile(st, 0)[r * KT + c], hy = htile(st, 1)[r * KT + c], hz = htile(st, 2)[r * KT + c];
       T cf[9];
-      coefs<T, I, CT>(p, p.table + 9, 18, static_cast<unsigned>(itile(st)[r * kItK + c]), 1, cf);
-      const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
+      coefs<T, I, CT>(p, p.table + 9, 18, m, 1, cf);
       if (MODE != 2 && cls == 0) {
         h_plain(cf, e, hx, hy, hz);
         p.H[0][b] = hx;
