@@ -258,7 +258,8 @@ int xfdtd_set_kernel_variant(xfdtd_handle *h, int e_variant, int h_variant);
 /* Variants of the shell launches (walls and CPML slabs): how many, the ones
  * in use for E and H; and fixing them (all give the same bits).  Variants
  * 0-3 are the shell kernel (register cap x table form); 4-6 the z-edge
- * TMA-staged launch (ring stages x table form), offered
+ * TMA-staged launch in 32 x 8 tiles and 7-9 in 16 x 16 tiles (ring stages
+ * x table form), offered
  * with a wide interior variant only
  * (XFDTD_ERR_INVALID_PLAN otherwise). */
 int xfdtd_shell_variants(xfdtd_handle *h, int *n, int *current_e, int *current_h);
@@ -292,6 +293,18 @@ int xfdtd_launch_count(xfdtd_handle *h, int64_t *n);
 int xfdtd_launches_per_step(xfdtd_handle *h, int *n);
 /* Bytes copied host->device and device->host by the handle so far. */
 int xfdtd_transfer_bytes(xfdtd_handle *h, int64_t *h2d, int64_t *d2h);
+/* The TFSF surface corrections folded into the wide TMA launches.  Where
+ * the plane wave's box lies in the wide decomposition's k range and the plan
+ * has no lumped element, the E (H) launch applies TFSF3D::updateE's
+ * (updateH's) corrections to the cells of the box's surface
+ * (src/tfsf/tfsf_3d.cpp:185-411), with the arithmetic of the separate
+ * k_tfsf_e / k_tfsf_h launches, and those launches are left out.  The
+ * autotuner keeps the faster of the two forms per side; set_tfsf_fusion
+ * allows (1) or forbids (0) the folded form, and xfdtd_tfsf_fusion reports
+ * whether each side uses it with its current variant.  Both give the same
+ * bits.  No counterpart in the reference. */
+int xfdtd_set_tfsf_fusion(xfdtd_handle *h, int e_on, int h_on);
+int xfdtd_tfsf_fusion(xfdtd_handle *h, int active[2]);
 /* Wall time of xfdtd_create, in ms: ms[0] validation, device allocation
  * and upload of the tables; ms[1] autotuning (0 without
  * XFDTD_FLAG_AUTOTUNE).  No counterpart in the reference. */

@@ -218,7 +218,7 @@ def test_every_shell_variant_is_bitwise_identical(name, precision):
 # the wide decomposition's interior variants (TMA-staged, every plane and
 # row over the interior's k range) and the z-edge TMA shell variants
 WIDE_VARIANTS = (20, 21, 22)
-ZEDGE_SHELL_VARIANTS = (4, 5, 6)
+ZEDGE_SHELL_VARIANTS = (4, 5, 6, 7, 8, 9)
 
 
 @pytest.mark.parametrize("name", ["dielectric", "heterogeneous", "oblique", "long_z", "one_sided"])
@@ -257,6 +257,40 @@ def test_wide_decomposition_is_bitwise_identical(name):
         # every pairing in one precision at least (the other's k range may
         # not start on a 16-byte boundary on this small grid)
         assert offered >= len(WIDE_VARIANTS) * (2 + len(ZEDGE_SHELL_VARIANTS))
+
+
+@pytest.mark.parametrize("name", ["dielectric", "oblique", "pec_sphere"])
+def test_tfsf_folded_into_the_wide_launch_is_bitwise_identical(name):
+    """The TFSF surface corrections applied inside the wide TMA launches
+    (E and H) give the bits of the separate k_tfsf_e / k_tfsf_h launches,
+    with every wide interior variant, through graph replay, in both
+    precisions; and the folded form is in use where the grid allows it."""
+    sc, st = scenes.SCENES[name]()
+    st = min(st, 120)
+    used = 0
+    for precision in ("fp64", "fp32"):
+        for v in WIDE_VARIANTS:
+            runs = []
+            for fold in (True, False):
+                g = X.Simulation(sc, st, precision=precision, autotune=False, fused=False)
+                try:
+                    g.set_kernel_variant(v, v)
+                    g.set_shell_variant(ZEDGE_SHELL_VARIANTS[0], ZEDGE_SHELL_VARIANTS[0])
+                except X.EngineError:
+                    break   # not offered on this grid
+                g.set_tfsf_fusion(fold, fold)
+                active = g.tfsf_fusion()
+                if fold:
+                    used += sum(active)
+                else:
+                    assert active == (False, False)
+                g.step(st)
+                runs.append([g.read_field(c) for c in range(6)] + [g.read_nffft(w) for w in (0, 9, 20)])
+            if len(runs) == 2:
+                for a, b in zip(*runs):
+                    assert np.array_equal(a, b), (name, precision, v)
+    if name == "dielectric":
+        assert used > 0
 
 
 @pytest.mark.parametrize("scene", ["oblique", "dielectric"])

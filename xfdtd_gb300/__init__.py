@@ -97,6 +97,8 @@ def libs():
         cu.xfdtd_set_shell_variant.argtypes = [C.c_void_p, C.c_int, C.c_int]
         cu.xfdtd_set_wait_limit.argtypes = [C.c_void_p, C.c_int64]
         cu.xfdtd_create_times.argtypes = [C.c_void_p, dp]
+        cu.xfdtd_set_tfsf_fusion.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        cu.xfdtd_tfsf_fusion.argtypes = [C.c_void_p, P(C.c_int)]
         cu.xfdtd_last_error.argtypes = [C.c_void_p]
         cu.xfdtd_last_error.restype = C.c_char_p
         cu.xfdtd_version.restype = C.c_char_p
@@ -385,6 +387,17 @@ class Simulation:
         ms = (C.c_double * 2)()
         self._check_engine(libs()[0].xfdtd_create_times(self.engine, ms))
         return {"alloc_upload_ms": ms[0], "autotune_ms": ms[1]}
+
+    def set_tfsf_fusion(self, e_on: bool, h_on: bool):
+        """Allow or forbid the TFSF corrections inside the wide TMA launches."""
+        self._check_engine(libs()[0].xfdtd_set_tfsf_fusion(self.engine, int(bool(e_on)), int(bool(h_on))))
+
+    def tfsf_fusion(self) -> tuple:
+        """Whether the E and H updates apply the TFSF corrections in their
+        wide launch with the current variants."""
+        a = (C.c_int * 2)()
+        self._check_engine(libs()[0].xfdtd_tfsf_fusion(self.engine, a))
+        return bool(a[0]), bool(a[1])
 
     def set_wait_limit(self, polls: int):
         """Polls of each TMA plane wait before a block gives up and reports a

@@ -197,6 +197,11 @@ struct xfdtd_handle {
   // buffer set, swapped with the first after each step
   bool sweep_ok = false;   // the plan allows the sweep (buffers allocated)
   bool tf_two_d = false;   // TFSF2D: Ez, Hx, Hy corrections on the x and y faces only
+  // the TFSF corrections may run inside the wide TMA launch (E, H): the
+  // surface lies in its k range and no lumped element corrects E first
+  bool tf_fuse_ok[2] = {false, false};
+  bool tf_fuse_on[2] = {true, true};   // the autotuner's choice between fused and separate corrections
+  float tf_fuse_ms[2][2] = {{0, 0}, {0, 0}};   // its trials: fused, separate (ms per pair)
   bool sweep = false;      // the sweep runs
   int cur_set = 0;         // which buffer set (0: allocated as F, 1: as F2) is current
   CUtensorMap tm_h[2][3], tm_e[2][3], tm_idx;   // TMA maps of both sets and the index
@@ -460,6 +465,14 @@ long long side_shell_cells(const xfdtd_handle *h, int side, bool wide) {
   return wide ? h->vshell_w_cells[side] : h->vshell_cells[side];
 }
 
+// Whether the side's TFSF corrections run inside its wide TMA launch this
+// step: the plan allows it (tf_fuse_ok, set at create) and the side runs
+// the wide decomposition with the split kernels.
+bool tfsf_fused(const xfdtd_handle *h, int side) {
+  return h->tfsf && h->tf_fuse_ok[side] && h->tf_fuse_on[side] && !h->sweep && side_wide(h, side) &&
+         kVariants[side == 0 ? h->var_e : h->var_h].stages != 0;
+}
+
 template <typename T, typename I, bool S, int MB, int NC, bool CT>
 void launch_vol_v(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, const Variant &v) {
   xg::InteriorBox in = h->vin[e_side ? 0 : 1];
@@ -483,10 +496,13 @@ struct ShellVariant {
   bool ct;
   int stages;   // 0 = the shell kernel
   int chunk;
+  int kt;       // tile width along k of the z-edge launch: 32 (x 8 rows) or 16 (x 16 rows)
 };
 // (8 and 4 planes per block measured slower on the 280^3 dielectric sphere.)
-constexpr ShellVariant kShellVariants[] = {{4, false},        {6, false},        {4, true},        {6, true},
-                                           {0, false, 4, 16}, {0, false, 6, 16}, {0, true, 4, 16}};
+constexpr ShellVariant kShellVariants[] = {{4, false},           {6, false},           {4, true},
+                                           {6, true},            {0, false, 4, 16, 32}, {0, false, 6, 16, 32},
+                                           {0, true, 4, 16, 32}, {0, false, 4, 16, 16}, {0, false, 6, 16, 16},
+                                           {0, true, 4, 16, 16}};
 constexpr int kNumShellVariants = sizeof(kShellVariants) / sizeof(kShellVariants[0]);
 
 // A z-edge TMA variant runs on the wide decomposition only.
@@ -501,7 +517,7 @@ void launch_shell_v(xfdtd_handle *h, bool e_side, const xg::ShellBoxes &s, cudaS
   else xg::k_update_h_shell<T, I, MB, CT><<<s.blocks, 256, 0, st>>>(p, s);
 }
 
-template <typename T, typename I, int S, bool CT, int MODE>
+template <typename T, typename I, int S, bool CT, int MODE, int KT = xg::kItK>
 void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, int chunk, cudaStream_t st);
 
 // The shell kernel of one side over the decomposition of its current
@@ -517,9 +533,15 @@ void launch_shell(xfdtd_handle *h, bool e_side, int var = -1, cudaStream_t st = 
   if (v.stages) {
     if (&s != &h->vshell_w[side]) throw Err{XFDTD_ERR_STATE, "z-edge TMA launch outside the wide decomposition"};
     auto p = vol_params<T, I>(h);
-    if (v.stages == 6) launch_vol_tma<T, I, 6, false, 2>(h, p, e_side, v.chunk, st);
-    else if (v.ct) launch_vol_tma<T, I, 4, true, 2>(h, p, e_side, v.chunk, st);
-    else launch_vol_tma<T, I, 4, false, 2>(h, p, e_side, v.chunk, st);
+    if (v.kt == xg::kItKz) {
+      if (v.stages == 6) launch_vol_tma<T, I, 6, false, 2, xg::kItKz>(h, p, e_side, v.chunk, st);
+      else if (v.ct) launch_vol_tma<T, I, 4, true, 2, xg::kItKz>(h, p, e_side, v.chunk, st);
+      else launch_vol_tma<T, I, 4, false, 2, xg::kItKz>(h, p, e_side, v.chunk, st);
+    } else {
+      if (v.stages == 6) launch_vol_tma<T, I, 6, false, 2>(h, p, e_side, v.chunk, st);
+      else if (v.ct) launch_vol_tma<T, I, 4, true, 2>(h, p, e_side, v.chunk, st);
+      else launch_vol_tma<T, I, 4, false, 2>(h, p, e_side, v.chunk, st);
+    }
   } else if (v.minb == 6) {
     if (v.ct) launch_shell_v<T, I, 6, true>(h, e_side, s, st);
     else launch_shell_v<T, I, 6, false>(h, e_side, s, st);
@@ -595,16 +617,6 @@ void volume_boxes(xfdtd_handle *h, int side) {
       if (fl[q] & bit) run[a] = false;
   }
   const int px_lo = lo[0], px_hi = hi[0], py_lo = lo[1], py_hi = hi[1];
-  // the wide decomposition's k range: the plain run cut on 16-byte
-  // boundaries (TMA's alignment), so that the z-edge launch keeps only the
-  // CPML slabs and walls
-  int wk_lo = lo[2], wk_hi = hi[2];
-  {
-    const int q = 16 / static_cast<int>(h->esize);
-    const int l = (lo[2] + q - 1) / q * q, u = (hi[2] + 1) / q * q - 1;
-    wk_lo = l;
-    wk_hi = u;
-  }
   // cut on 128-byte lines, else (a short run) on 32-byte sectors, else not at all
   for (int bytes : {128, 32}) {
     const int q = bytes / static_cast<int>(h->esize);
@@ -706,10 +718,8 @@ void volume_boxes(xfdtd_handle *h, int side) {
     in = xg::InteriorBox{};
     long long total = 0;
     unsigned blocks = 0;
-    h->wide_ok[side] = interior && wk_lo <= wk_hi;
-    lo[2] = wk_lo;   // the shell boxes below follow the wide k range
-    hi[2] = wk_hi;
-    if (h->wide_ok[side]) {
+    h->wide_ok[side] = interior;
+    if (interior) {
       in.lo[0] = 0, in.hi[0] = n[0];
       in.lo[1] = 0, in.hi[1] = n[1];
       in.lo[2] = lo[2], in.hi[2] = hi[2];
@@ -835,6 +845,9 @@ void sweep_setup(xfdtd_handle *h) {
 template <typename T, typename I>
 void interior_tma_encode(xfdtd_handle *h) {
   const CUtensorMapDataType dt = sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  const CUtensorMapDataType it = sizeof(I) == 1   ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                 : sizeof(I) == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16
+                                                  : CU_TENSOR_MAP_DATA_TYPE_UINT32;
   auto encode = [&](xg::ItMaps *m, auto geom) {
     using G = decltype(geom);
     constexpr unsigned KT = static_cast<unsigned>(xg::kItThreads / G::J);
@@ -844,9 +857,11 @@ void interior_tma_encode(xfdtd_handle *h) {
       encode_map(h, &m[1].a[c], h->F[c], dt, sizeof(T), G::EW, G::J + 1);
       encode_map(h, &m[1].b[c], h->F[3 + c], dt, sizeof(T), KT, G::J);
     }
+    if (G::IDX)
+      for (int side = 0; side < 2; ++side) encode_map(h, &m[side].idx, h->idx, it, sizeof(I), KT, G::J);
   };
-  encode(h->itm, xg::ItTiles<T, xg::kItK>{});
-  encode(h->itm_z, xg::ItTiles<T, xg::kItKz>{});
+  encode(h->itm, xg::ItTiles<T, I, xg::kItK>{});
+  encode(h->itm_z, xg::ItTiles<T, I, xg::kItKz>{});
   h->itm_base = h->F[0];
 }
 
@@ -857,12 +872,13 @@ void interior_tma_encode(xfdtd_handle *h) {
 // start).  The material index is read with plain loads.
 template <typename T, typename I>
 void interior_tma_setup(xfdtd_handle *h) {
-  using G = xg::ItTiles<T, xg::kItK>;
-  using Gz = xg::ItTiles<T, xg::kItKz>;
-  const int es = static_cast<int>(sizeof(T));
+  using G = xg::ItTiles<T, I, xg::kItK>;
+  using Gz = xg::ItTiles<T, I, xg::kItKz>;
+  const int es = static_cast<int>(sizeof(T)), is = static_cast<int>(sizeof(I));
   for (int side = 0; side < 2; ++side) {
     const int k = h->vin[side].lo[2], kh = side == 0 ? k - G::HOFF - 1 : k;
-    h->it_ok[side] = h->vin_cells[side] > 0 && kh >= 0 && (k * es) % 16 == 0 && (kh * es) % 16 == 0;
+    h->it_ok[side] = h->vin_cells[side] > 0 && kh >= 0 && (k * es) % 16 == 0 && (kh * es) % 16 == 0 &&
+                     (k * is) % 16 == 0;
   }
   if (!(h->it_ok[0] && h->it_ok[1])) return;
   interior_tma_encode<T, I>(h);
@@ -872,30 +888,41 @@ void interior_tma_setup(xfdtd_handle *h) {
   auto attrs = [&](auto mode, auto kt) {
     constexpr int M = decltype(mode)::value;
     constexpr int KT = decltype(kt)::value;
-    using GG = xg::ItTiles<T, KT>;
+    using GG = xg::ItTiles<T, I, KT>;
     attr(xg::k_interior_tma_e<T, I, 4, false, M, KT>, GG::template smem_e<4>());
     attr(xg::k_interior_tma_e<T, I, 6, false, M, KT>, GG::template smem_e<6>());
     attr(xg::k_interior_tma_e<T, I, 4, true, M, KT>, GG::template smem_e<4>());
     attr(xg::k_interior_tma_h<T, I, 4, false, M, KT>, GG::template smem_h<4>());
     attr(xg::k_interior_tma_h<T, I, 6, false, M, KT>, GG::template smem_h<6>());
     attr(xg::k_interior_tma_h<T, I, 4, true, M, KT>, GG::template smem_h<4>());
+    if constexpr (M == 1) {   // the wide launch with the TFSF corrections
+      attr(xg::k_interior_tma_e<T, I, 4, false, M, KT, true>, GG::template smem_e<4>());
+      attr(xg::k_interior_tma_e<T, I, 6, false, M, KT, true>, GG::template smem_e<6>());
+      attr(xg::k_interior_tma_e<T, I, 4, true, M, KT, true>, GG::template smem_e<4>());
+      attr(xg::k_interior_tma_h<T, I, 4, false, M, KT, true>, GG::template smem_h<4>());
+      attr(xg::k_interior_tma_h<T, I, 6, false, M, KT, true>, GG::template smem_h<6>());
+      attr(xg::k_interior_tma_h<T, I, 4, true, M, KT, true>, GG::template smem_h<4>());
+    }
   };
   attrs(std::integral_constant<int, 0>{}, std::integral_constant<int, xg::kItK>{});
   for (int side = 0; side < 2; ++side) {
     if (!h->wide_ok[side]) continue;
+    // the z-edge launch's upper tiles start after the interior's last k
     const int k = h->vin_w[side].lo[2], kh = side == 0 ? k - G::HOFF - 1 : k;
     const int ku = h->vin_w[side].hi[2] + 1, kuh = side == 0 ? ku - Gz::HOFF - 1 : ku;
-    if (kh < 0 || (k * es) % 16 || (kh * es) % 16 || (ku * es) % 16 || (kuh * es) % 16) h->wide_ok[side] = false;
+    if (kh < 0 || (k * es) % 16 || (kh * es) % 16 || (k * is) % 16 || (ku * es) % 16 || (kuh * es) % 16 ||
+        (ku * is) % 16)
+      h->wide_ok[side] = false;
   }
   if (!(h->wide_ok[0] && h->wide_ok[1])) return;
   attrs(std::integral_constant<int, 1>{}, std::integral_constant<int, xg::kItK>{});
+  attrs(std::integral_constant<int, 2>{}, std::integral_constant<int, xg::kItK>{});
   attrs(std::integral_constant<int, 2>{}, std::integral_constant<int, xg::kItKz>{});
 }
 
-template <typename T, typename I, int S, bool CT, int MODE>
+template <typename T, typename I, int S, bool CT, int MODE, int KT>
 void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, int chunk, cudaStream_t st) {
-  constexpr int KT = MODE == 2 ? xg::kItKz : xg::kItK;
-  using G = xg::ItTiles<T, KT>;
+  using G = xg::ItTiles<T, I, KT>;
   if (h->itm_base != h->F[0]) interior_tma_encode<T, I>(h);   // the buffers were swapped
   const int side = e_side ? 0 : 1;
   const xg::InteriorBox in = MODE == 2 ? h->vin_z[side] : side_interior(h, side, MODE == 1);
@@ -903,13 +930,32 @@ void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, 
   const int nkt = MODE == 2 ? (in.pz_lo + KT - 1) / KT + (in.hi[2] - in.pz_hi + KT - 1) / KT
                             : (in.hi[2] - in.lo[2] + KT) / KT;
   dim3 grid(nkt, (nj + G::J - 1) / G::J, (ni + chunk - 1) / chunk);
-  const xg::ItMaps *maps = MODE == 2 ? h->itm_z : h->itm;
-  if (e_side)
-    xg::k_interior_tma_e<T, I, S, CT, MODE, KT>
-        <<<grid, xg::kItThreads, G::template smem_e<S>(), st>>>(maps[0], p, in, chunk, h->d_status, h->wait_polls);
-  else
-    xg::k_interior_tma_h<T, I, S, CT, MODE, KT>
-        <<<grid, xg::kItThreads, G::template smem_h<S>(), st>>>(maps[1], p, in, chunk, h->d_status, h->wait_polls);
+  const xg::ItMaps *maps = KT == xg::kItKz ? h->itm_z : h->itm;
+  xg::TfsfFuse fz{};
+  if (MODE == 1 && tfsf_fused(h, side)) {
+    fz.tf = p.tf;
+    fz.step = h->d_step;
+    fz.on = 1;
+  }
+  const unsigned smem = e_side ? G::template smem_e<S>() : G::template smem_h<S>();
+  if constexpr (MODE == 1) {
+    if (fz.on) {
+      if (e_side)
+        xg::k_interior_tma_e<T, I, S, CT, MODE, KT, true><<<grid, xg::kItThreads, smem, st>>>(
+            maps[0], p, in, chunk, h->d_status, h->wait_polls, fz);
+      else
+        xg::k_interior_tma_h<T, I, S, CT, MODE, KT, true><<<grid, xg::kItThreads, smem, st>>>(
+            maps[1], p, in, chunk, h->d_status, h->wait_polls, fz);
+      return;
+    }
+  }
+  if (e_side) {
+    xg::k_interior_tma_e<T, I, S, CT, MODE, KT><<<grid, xg::kItThreads, smem, st>>>(maps[0], p, in, chunk, h->d_status,
+                                                                                  h->wait_polls, fz);
+  } else {
+    xg::k_interior_tma_h<T, I, S, CT, MODE, KT><<<grid, xg::kItThreads, smem, st>>>(maps[1], p, in, chunk, h->d_status,
+                                                                                  h->wait_polls, fz);
+  }
 }
 
 // After a sweep the second buffer set holds step t+1: make it current.
@@ -975,6 +1021,22 @@ void volume_pair(xfdtd_handle *h, bool e_side);
 // and keeps the fastest.  Run before the first step, when every field and
 // psi is zero: the volume kernels then write zeros back (the TFSF buffers
 // they read are zero too), so the trials leave the simulation unchanged.
+template <typename T>
+xg::TfsfSurfParams<T> tfsf_surf_params(xfdtd_handle *h);
+
+// The TFSF surface corrections of one side as their own launch (k_tfsf_e
+// over the E box's surface, k_tfsf_h over the H box's) on the main stream.
+template <typename T>
+void launch_tfsf_side(xfdtd_handle *h, bool e_side) {
+  const auto sp = tfsf_surf_params<T>(h);
+  const int d = e_side ? 0 : 1;
+  const long long n = xg::surface_count(h->tf_lo[0] - d, h->tf_hi[0], h->tf_lo[1] - d, h->tf_hi[1],
+                                        h->tf_lo[2] - d, h->tf_hi[2]);
+  if (e_side) xg::k_tfsf_e<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, h->stream>>>(sp);
+  else xg::k_tfsf_h<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, h->stream>>>(sp);
+  XCHECK(cudaGetLastError());
+}
+
 template <typename T, typename I>
 void autotune_t(xfdtd_handle *h, int trials) {
   cudaEvent_t a, b;
@@ -1072,6 +1134,20 @@ void autotune_t(xfdtd_handle *h, int trials) {
     var = best_v;
     h->shell_var[side] = best_sv;
     h->tune_ms[side][best_v] = best;
+    // the TFSF corrections inside the wide launch, or as their own launch
+    // after the pair: whichever is faster
+    if (h->tf_fuse_ok[side] && kVariants[best_v].wide) {
+      h->tf_fuse_on[side] = true;
+      const float fused = time_n([&] { volume_pair<T, I>(h, side == 0); }, 3 * trials);
+      h->tf_fuse_on[side] = false;
+      const float apart = time_n([&] {
+        volume_pair<T, I>(h, side == 0);
+        launch_tfsf_side<T>(h, side == 0);
+      }, 3 * trials);
+      h->tf_fuse_on[side] = fused <= apart;
+      h->tf_fuse_ms[side][0] = fused;
+      h->tf_fuse_ms[side][1] = apart;
+    }
     best_split += best;
   }
   h->sweep = was_sweep;
@@ -1284,7 +1360,7 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
       XCHECK(cudaGetLastError());
       prof_end(h);
     }
-    if (h->tfsf) {
+    if (h->tfsf && !tfsf_fused(h, 0)) {
       const auto sp = tfsf_surf_params<T>(h);
       const long long n = xg::surface_count(h->tf_lo[0], h->tf_hi[0], h->tf_lo[1], h->tf_hi[1], h->tf_lo[2], h->tf_hi[2]);
       prof_begin(h, 7);
@@ -1292,6 +1368,9 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
       XCHECK(cudaGetLastError());
       prof_end(h);
     }
+    // the H launch that applies the TFSF H corrections reads this step's
+    // incident E: the 1-D line joins before it
+    if (h->tfsf && tfsf_fused(h, 1)) XCHECK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
     volume_pair<T, I>(h, false);
   }
   // NF-FF sampling on the side stream beside the TFSF H corrections when
@@ -1305,7 +1384,7 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     prof_end(h, h->side);
     XCHECK(cudaEventRecord(h->ev_nf_join, h->side));
   }
-  if (h->tfsf) {
+  if (h->tfsf && (h->sweep || !tfsf_fused(h, 1))) {
     XCHECK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
     const auto sp = tfsf_surf_params<T>(h);
     const long long n = xg::surface_count(h->tf_lo[0] - 1, h->tf_hi[0], h->tf_lo[1] - 1, h->tf_hi[1],
@@ -1372,8 +1451,8 @@ int launches_per_step(const xfdtd_handle *h) {
     const bool w = side_wide(h, side);
     vol += (side_interior_cells(h, side, w) ? 1 : 0) + (side_shell_cells(h, side, w) ? 1 : 0);
   }
-  return (h->tfsf ? 3 : 0) + vol + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) +
-         snap + 1;
+  const int tf = h->tfsf ? 3 - (tfsf_fused(h, 0) ? 1 : 0) - (tfsf_fused(h, 1) ? 1 : 0) : 0;
+  return tf + vol + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + snap + 1;
 }
 
 // Captures g steps starting at a step index that is a multiple of the NF-FF
@@ -1774,6 +1853,13 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
       if (h->idx_bytes == 1) sweep_setup<float, uint8_t>(h);
       else sweep_setup<float, uint16_t>(h);
     }
+  }
+  // the TFSF corrections inside the wide TMA launches: 3-D plane wave, no
+  // lumped element, the E surface [lo, hi] and the H surface [lo-1, hi]
+  // within the wide launches' k ranges (they cover every i and j)
+  if (h->tfsf && !h->tf_two_d && h->n_inj == 0 && h->n_ind == 0) {
+    h->tf_fuse_ok[0] = h->wide_ok[0] && h->vin_w[0].lo[2] <= h->tf_lo[2] && h->tf_hi[2] <= h->vin_w[0].hi[2];
+    h->tf_fuse_ok[1] = h->wide_ok[1] && h->vin_w[1].lo[2] <= h->tf_lo[2] - 1 && h->tf_hi[2] <= h->vin_w[1].hi[2];
   }
   XCHECK(cudaStreamSynchronize(h->stream));
   h->create_ms[0] = ms_since(t_begin);
@@ -2353,6 +2439,24 @@ int xfdtd_transfer_bytes(xfdtd_handle *h, int64_t *h2d, int64_t *d2h) {
   if (!h) return XFDTD_ERR_STATE;
   if (h2d) *h2d = h->h2d;
   if (d2h) *d2h = h->d2h;
+  return XFDTD_OK;
+}
+
+int xfdtd_set_tfsf_fusion(xfdtd_handle *h, int e_on, int h_on) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    h->tf_fuse_on[0] = e_on != 0;
+    h->tf_fuse_on[1] = h_on != 0;
+    if (h->gexec) {   // the captured graph holds the old launches
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+    }
+  });
+}
+
+int xfdtd_tfsf_fusion(xfdtd_handle *h, int active[2]) {
+  if (!h || !active) return XFDTD_ERR_STATE;
+  for (int side = 0; side < 2; ++side) active[side] = tfsf_fused(h, side) ? 1 : 0;
   return XFDTD_OK;
 }
 

@@ -11,10 +11,11 @@
 // updated; an mbarrier per stage counts the bytes in.  The threads read
 // the tiles from shared memory, apply the same per-cell arithmetic as the
 // fast path (e_plain / h_plain with the same coefficients) and store the
-// updated plane straight to global memory.  The 1-byte (or 2-, 4-byte)
-// material index is read with plain loads, issued before the wait for the
-// plane: a tile of it is 8 to 32 bytes a row, and its rows need no 16-byte
-// alignment that way.
+// updated plane straight to global memory.  The material index comes with
+// the tiles in the 32-wide launches; the 16-wide z-edge launch reads it with
+// plain loads issued before the wait for the plane (its upper tiles start
+// after the interior's last k, which need not lie on a 16-byte boundary of
+// a 1-byte index).
 //
 // The tile is KT cells along k by 256 / KT rows along j: 32 x 8 for the
 // interior launches, 16 x 16 for the z-edge launch, whose k runs (the CPML
@@ -51,10 +52,37 @@
 #pragma once
 
 #include "common.cuh"
+#include "surface.cuh"
 #include "tma.cuh"
 #include "volume.cuh"
 
 namespace xg {
+
+// The TFSF corrections folded into the wide launch (mode 1): when `on`,
+// the cells of the TFSF box's surface get TFSF3D::updateE's (E kernel) or
+// updateH's (H kernel) corrections after their update, with the same
+// arithmetic as k_tfsf_e / k_tfsf_h (surface.cuh), before the store.  The
+// engine turns it on when the whole surface lies in the wide launch's k
+// range and no lumped element's correction would have to come first.
+struct TfsfFuse {
+  TfsfDev tf;
+  const long long *step;
+  int on;
+};
+
+// Out-of-line calls into the TFSF corrections: only the few warps on the
+// box's surface take them, and kept out of line they leave the launch's
+// register budget to the per-cell update.
+template <typename T>
+__device__ __noinline__ void tfsf_e_fused_call(const TfsfDev &tf, const decltype(tfsf_view<T>(tf).inc) hinc, int i,
+                                               int j, int k, T &ex, T &ey, T &ez, bool *w) {
+  tfsf_e_fused<T>(tf, hinc, i, j, k, ex, ey, ez, w);
+}
+template <typename T>
+__device__ __noinline__ void tfsf_h_cell_call(const TfsfDev &tf, const decltype(tfsf_view<T>(tf).inc) einc, int i,
+                                              int j, int k, T &hx, T &hy, T &hz, bool *w) {
+  tfsf_h_cell<T>(tf, einc, i, j, k, hx, hy, hz, w);
+}
 
 constexpr int kItThreads = 256;
 constexpr int kItK = 32;                  // interior launches' tile: 32 cells along k
@@ -65,9 +93,10 @@ constexpr int kItWaitLimit = 1 << 22;     // polls of a stage barrier before giv
 // HW columns starting at k0-HOFF-1, J+1 rows from j0-1; E tiles KT x J from
 // (k0, j0).  H kernel: E rows of EW columns starting at k0, J+1 rows from
 // j0; H tiles KT x J.  HW and EW are whole 16-byte rows.
-template <typename T, int KT>
+template <typename T, typename I, int KT>
 struct ItTiles {
   static constexpr int J = kItThreads / KT;
+  static constexpr bool IDX = KT == kItK;   // the index tile comes by TMA
   static constexpr int HOFF = sizeof(T) == 4 ? 3 : 1;
   static constexpr int HW = KT == 32 ? (sizeof(T) == 4 ? 40 : 36)    // covers k0-HOFF-1 .. k0+KT-1
                                      : (sizeof(T) == 4 ? 20 : 18);
@@ -75,18 +104,20 @@ struct ItTiles {
                                      : (sizeof(T) == 4 ? 20 : 18);
   static constexpr int RND = 128;
   static constexpr int rnd(int b) { return (b + RND - 1) / RND * RND; }
-  // E kernel stage: 3 H tiles (halo), 3 E tiles
+  // E kernel stage: 3 H tiles (halo), 3 E tiles, the index tile
   static constexpr int EH_TILE = rnd((J + 1) * HW * int(sizeof(T)));
   static constexpr int EE_TILE = rnd(J * KT * int(sizeof(T)));
-  static constexpr int E_STAGE = 3 * EH_TILE + 3 * EE_TILE;
+  static constexpr int I_TILE = IDX ? rnd(J * KT * int(sizeof(I))) : 0;
+  static constexpr unsigned I_BYTES = IDX ? unsigned(J * KT * sizeof(I)) : 0u;
+  static constexpr int E_STAGE = 3 * EH_TILE + 3 * EE_TILE + I_TILE;
   static constexpr unsigned E_HBYTES = 3u * (J + 1) * HW * sizeof(T);
-  static constexpr unsigned E_FULL = E_HBYTES + 3u * J * KT * sizeof(T);
-  // H kernel stage: 3 E tiles (halo), 3 H tiles
+  static constexpr unsigned E_FULL = E_HBYTES + 3u * J * KT * sizeof(T) + I_BYTES;
+  // H kernel stage: 3 E tiles (halo), 3 H tiles, the index tile
   static constexpr int HE_TILE = rnd((J + 1) * EW * int(sizeof(T)));
   static constexpr int HH_TILE = EE_TILE;
-  static constexpr int H_STAGE = 3 * HE_TILE + 3 * HH_TILE;
+  static constexpr int H_STAGE = 3 * HE_TILE + 3 * HH_TILE + I_TILE;
   static constexpr unsigned H_EBYTES = 3u * (J + 1) * EW * sizeof(T);
-  static constexpr unsigned H_FULL = H_EBYTES + 3u * J * KT * sizeof(T);
+  static constexpr unsigned H_FULL = H_EBYTES + 3u * J * KT * sizeof(T) + I_BYTES;
   template <int STAGES>
   static constexpr int smem_e() { return STAGES * E_STAGE + STAGES * 8; }
   template <int STAGES>
@@ -94,10 +125,11 @@ struct ItTiles {
 };
 
 // Tensor maps of one launch: a[3] the halo tiles (H for the E kernel, E for
-// the H kernel), b[3] the updated side's tiles.
+// the H kernel), b[3] the updated side's tiles, the index (32-wide tiles).
 struct ItMaps {
   CUtensorMap a[3];
   CUtensorMap b[3];
+  CUtensorMap idx;
 };
 
 // The block's planes and tile: k0, j0 of the tile, its last k khi, planes
@@ -152,11 +184,11 @@ struct ItRing {
   }
 };
 
-template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK>
+template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK, bool TF = false>
 __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
                                                                InteriorBox in, int chunk, int *status,
-                                                               int wait_limit) {
-  using G = ItTiles<T, KT>;
+                                                               int wait_limit, const __grid_constant__ TfsfFuse fz) {
+  using G = ItTiles<T, I, KT>;
   extern __shared__ __align__(128) unsigned char smem[];
   ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::E_STAGE), wait_limit};
   const int tid = threadIdx.x, c = tid % KT, r = tid / KT;
@@ -177,6 +209,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
     if (full) {
       for (int comp = 0; comp < 3; ++comp)
         tma_load_3d(base + 3 * G::EH_TILE + comp * G::EE_TILE, &maps.b[comp], blk.k0, blk.j0, q, &ring.bar[st]);
+      if (G::IDX) tma_load_3d(base + 3 * G::EH_TILE + 3 * G::EE_TILE, &maps.idx, blk.k0, blk.j0, q, &ring.bar[st]);
     }
   };
   int issued = blk.ia - 2, waited = blk.ia - 2;   // thread 0: last plane issued, last plane waited
@@ -200,6 +233,8 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
     if (yspec) slab_axis(p, 1, 0, j, cx.ys, cx.Y);
     if (MODE == 2) slab_axis(p, 2, 0, k, cx.zs, cx.Z);
   }
+  // the incident H arrays of the previous step (the 1-D line's other buffer)
+  const auto hinc = (MODE == 1 && TF) ? tfsf_view<T>(fz.tf).inc + ((*fz.step + 1) & 1) * 6 * fz.tf.L : nullptr;
   for (int i = blk.ia; i < blk.ib; ++i) {
     // a special cell's psi operands, loaded before the wait for the plane
     const int cls = MODE == 0 ? 0 : ((i < in.px_lo || i > in.px_hi) ? 1 : 0) | (yspec ? 2 : 0) | (MODE == 2 ? 4 : 0);
@@ -214,7 +249,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
       ps = e_psi_load<T, I, 7>(p, cx, i, j, k, p.psi);
     }
     const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
-    const unsigned m = mine ? static_cast<unsigned>(__ldg(p.idx + b)) : 0u;
+    const unsigned m_plain = (!G::IDX && mine) ? static_cast<unsigned>(__ldg(p.idx + b)) : 0u;
     if (ring.wait(stage_of(i))) waited = i;
     if (mine && !ring.timed_out) {
       const int st = stage_of(i), sm = stage_of(i - 1);
@@ -224,10 +259,18 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
                        hv(st, 0, r + 1, c),     hv(st, 1, r + 1, c),     hv(st, 0, r, c + 1),
                        hv(st, 2, r, c + 1),     hv(sm, 1, r + 1, c + 1), hv(sm, 2, r + 1, c + 1)};
       T ex = etile(st, 0)[r * KT + c], ey = etile(st, 1)[r * KT + c], ez = etile(st, 2)[r * KT + c];
+      const unsigned m =
+          G::IDX ? static_cast<unsigned>(reinterpret_cast<const I *>(smem + st * G::E_STAGE + 3 * G::EH_TILE +
+                                                                     3 * G::EE_TILE)[r * KT + c])
+                 : m_plain;
       T cf[9];
       coefs<T, I, CT>(p, p.table, 18, m, 0, cf);
       if (MODE != 2 && cls == 0) {
         e_plain(cf, h, ex, ey, ez);
+        if (MODE == 1 && TF && tfsf_on_e_surface(fz.tf, i, j, k)) {
+          bool w[3];
+          tfsf_e_fused_call<T>(fz.tf, hinc, i, j, k, ex, ey, ez, w);
+        }
         p.E[0][b] = ex;
         p.E[1][b] = ey;
         p.E[2][b] = ez;
@@ -245,6 +288,11 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
           e_general_ops<T, I, 2>(p, cf, i, j, k, h, cx, ps, p.psi, true, ex, ey, ez, w);
         } else {
           e_general_ops<T, I, 3>(p, cf, i, j, k, h, cx, ps, p.psi, true, ex, ey, ez, w);
+        }
+        if (MODE == 1 && TF && tfsf_on_e_surface(fz.tf, i, j, k)) {
+          bool wt[3];
+          tfsf_e_fused_call<T>(fz.tf, hinc, i, j, k, ex, ey, ez, wt);
+          for (int q = 0; q < 3; ++q) w[q] = w[q] || wt[q];
         }
         if (w[0]) p.E[0][b] = ex;
         if (w[1]) p.E[1][b] = ey;
@@ -267,11 +315,11 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
   }
 }
 
-template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK>
+template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK, bool TF = false>
 __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
                                                                InteriorBox in, int chunk, int *status,
-                                                               int wait_limit) {
-  using G = ItTiles<T, KT>;
+                                                               int wait_limit, const __grid_constant__ TfsfFuse fz) {
+  using G = ItTiles<T, I, KT>;
   extern __shared__ __align__(128) unsigned char smem[];
   ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::H_STAGE), wait_limit};
   const int tid = threadIdx.x, c = tid % KT, r = tid / KT;
@@ -292,6 +340,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
     if (full) {
       for (int comp = 0; comp < 3; ++comp)
         tma_load_3d(base + 3 * G::HE_TILE + comp * G::HH_TILE, &maps.b[comp], blk.k0, blk.j0, q, &ring.bar[st]);
+      if (G::IDX) tma_load_3d(base + 3 * G::HE_TILE + 3 * G::HH_TILE, &maps.idx, blk.k0, blk.j0, q, &ring.bar[st]);
     }
   };
   int issued = blk.ia - 1, waited = blk.ia - 1;   // thread 0: last plane issued, last plane waited
@@ -314,6 +363,8 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
     if (yspec) slab_axis(p, 1, 1, j, cx.ys, cx.Y);
     if (MODE == 2) slab_axis(p, 2, 1, k, cx.zs, cx.Z);
   }
+  // the incident E arrays of this step (written by the 1-D line beside the E update)
+  const auto einc = (MODE == 1 && TF) ? tfsf_view<T>(fz.tf).inc + (*fz.step & 1) * 6 * fz.tf.L : nullptr;
   for (int i = blk.ia; i < blk.ib; ++i) {
     const int cls = MODE == 0 ? 0 : ((i < in.px_lo || i > in.px_hi) ? 1 : 0) | (yspec ? 2 : 0) | (MODE == 2 ? 4 : 0);
     PsiOps<T> pv{};
@@ -327,7 +378,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
       pv = h_psi_load<T, I, 7>(p, cx, i, j, k);
     }
     const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
-    const unsigned m = mine ? static_cast<unsigned>(__ldg(p.idx + b)) : 0u;
+    const unsigned m_plain = (!G::IDX && mine) ? static_cast<unsigned>(__ldg(p.idx + b)) : 0u;
     if (ring.wait(stage_of(i + 1))) waited = i + 1;
     if (mine && !ring.timed_out) {
       const int st = stage_of(i), sn = stage_of(i + 1);
@@ -337,10 +388,18 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
                        ev(st, 0, r, c + 1), ev(st, 1, r, c + 1), ev(st, 0, r + 1, c),
                        ev(st, 2, r + 1, c), ev(sn, 1, r, c),     ev(sn, 2, r, c)};
       T hx = htile(st, 0)[r * KT + c], hy = htile(st, 1)[r * KT + c], hz = htile(st, 2)[r * KT + c];
+      const unsigned m =
+          G::IDX ? static_cast<unsigned>(reinterpret_cast<const I *>(smem + st * G::H_STAGE + 3 * G::HE_TILE +
+                                                                     3 * G::HH_TILE)[r * KT + c])
+                 : m_plain;
       T cf[9];
       coefs<T, I, CT>(p, p.table + 9, 18, m, 1, cf);
       if (MODE != 2 && cls == 0) {
         h_plain(cf, e, hx, hy, hz);
+        if (MODE == 1 && TF && tfsf_h_terms(fz.tf, i, j, k)) {
+          bool w[3];
+          tfsf_h_cell_call<T>(fz.tf, einc, i, j, k, hx, hy, hz, w);
+        }
         p.H[0][b] = hx;
         p.H[1][b] = hy;
         p.H[2][b] = hz;
@@ -358,6 +417,11 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
           h_general_ops<T, I, 2>(p, cf, i, j, k, e, cx, pv, hx, hy, hz, w);
         } else {
           h_general_ops<T, I, 3>(p, cf, i, j, k, e, cx, pv, hx, hy, hz, w);
+        }
+        if (MODE == 1 && TF && tfsf_h_terms(fz.tf, i, j, k)) {
+          bool wt[3];
+          tfsf_h_cell_call<T>(fz.tf, einc, i, j, k, hx, hy, hz, wt);
+          for (int q = 0; q < 3; ++q) w[q] = w[q] || wt[q];
         }
         if (w[0]) p.H[0][b] = hx;
         if (w[1]) p.H[1][b] = hy;

@@ -419,6 +419,22 @@ __device__ __forceinline__ bool surface_cell(int q, int a0, int a1, int b0, int 
   return false;
 }
 
+// Whether (i, j, k) lies on the surface of the TFSF E box [lo, hi] (the
+// cells TFSF3D::updateE may correct) or of the H box [lo-1, hi].
+__device__ __forceinline__ bool tfsf_on_e_surface(const TfsfDev &tf, int i, int j, int k) {
+  return i >= tf.lo[0] && i <= tf.hi[0] && j >= tf.lo[1] && j <= tf.hi[1] && k >= tf.lo[2] && k <= tf.hi[2] &&
+         (i == tf.lo[0] || i == tf.hi[0] || j == tf.lo[1] || j == tf.hi[1] || k == tf.lo[2] || k == tf.hi[2]);
+}
+__device__ __forceinline__ bool tfsf_h_terms(const TfsfDev &tf, int i, int j, int k) {
+  if (tf.two_d)   // TFSF2D: the x and y faces of the one z cell
+    return k >= tf.lo[2] && k < tf.hi[2] && i >= tf.lo[0] - 1 && i <= tf.hi[0] && j >= tf.lo[1] - 1 &&
+           j <= tf.hi[1] && (i == tf.lo[0] - 1 || i == tf.hi[0] || j == tf.lo[1] - 1 || j == tf.hi[1]);
+  return i >= tf.lo[0] - 1 && i <= tf.hi[0] && j >= tf.lo[1] - 1 && j <= tf.hi[1] && k >= tf.lo[2] - 1 &&
+         k <= tf.hi[2] &&
+         (i == tf.lo[0] - 1 || i == tf.hi[0] || j == tf.lo[1] - 1 || j == tf.hi[1] || k == tf.lo[2] - 1 ||
+          k == tf.hi[2]);
+}
+
 // TFSF3D::updateE (src/tfsf/tfsf_3d.cpp:299-411) for one cell and one E
 // component C: which of the component's two face corrections apply at
 // (i, j, k) (bit 0: the first face pair, bit 1: the second) ...
@@ -492,6 +508,20 @@ __device__ __forceinline__ void tfsf_e_add(const TfsfDev &tf, const decltype(tfs
   }
 }
 
+// The E corrections of one cell, on its values in registers; w[c] tells
+// which components have a term.
+template <typename T>
+__device__ __forceinline__ void tfsf_e_fused(const TfsfDev &tf, const decltype(tfsf_view<T>(tf).inc) hinc, int i,
+                                             int j, int k, T &ex, T &ey, T &ez, bool w[3]) {
+  const int t0 = tfsf_e_terms<0>(tf, i, j, k), t1 = tfsf_e_terms<1>(tf, i, j, k), t2 = tfsf_e_terms<2>(tf, i, j, k);
+  if (t0) tfsf_e_add<0>(tf, hinc, i, j, k, t0, ex);
+  if (t1) tfsf_e_add<1>(tf, hinc, i, j, k, t1, ey);
+  if (t2) tfsf_e_add<2>(tf, hinc, i, j, k, t2, ez);
+  w[0] = t0 != 0;
+  w[1] = t1 != 0;
+  w[2] = t2 != 0;
+}
+
 template <int C, typename T>
 __device__ __forceinline__ void tfsf_e_component(const TfsfSurfParams<T> &p, const decltype(tfsf_view<T>(p.tf).inc) hinc,
                                                  int i, int j, int k, long long b) {
@@ -522,18 +552,18 @@ __global__ void k_tfsf_e(TfsfSurfParams<T> p) {
   tfsf_e_surface(p, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// TFSF3D::updateH (src/tfsf/tfsf_3d.cpp:185-297) at surface cell q of the
-// box one cell larger on the low sides.
+// TFSF3D::updateH (src/tfsf/tfsf_3d.cpp:185-297) at one cell (i, j, k) of
+// the surface of the box one cell larger on the low sides: the corrections
+// of its H components, added to hx, hy, hz (the values the cell holds after
+// the H update); w[c] tells which components have a term.  einc: the
+// incident E arrays of this step.
 template <typename T>
-__device__ __forceinline__ void tfsf_h_surface(const TfsfSurfParams<T> &p, int q) {
-  const TfsfDev &tf = p.tf;
+__device__ __forceinline__ void tfsf_h_cell(const TfsfDev &tf, const decltype(tfsf_view<T>(tf).inc) einc, int i,
+                                            int j, int k, T &hx, T &hy, T &hz, bool w[3]) {
   const int li = tf.lo[0], ri = tf.hi[0], lj = tf.lo[1], rj = tf.hi[1], lk = tf.lo[2], rk = tf.hi[2];
-  int i, j, k;
-  if (!surface_cell(q, li - 1, ri, lj - 1, rj, lk - 1, rk, i, j, k)) return;
   const auto V = tfsf_view<T>(tf);
   using R = typename std::remove_const<typename std::remove_pointer<decltype(V.inc)>::type>::type;
-  const R *einc = V.inc + ((*p.step) & 1) * 6 * tf.L;   // incident E of this step
-  const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
+  w[0] = w[1] = w[2] = false;
   // Hx: y faces (j = lj-1: += cby Ez_inc(i, lj, k); j = rj: -= cby Ez_inc(i, rj, k)),
   //     z faces (k = lk-1: -= cbz Ey_inc(i, j, lk); k = rk: += cbz Ey_inc(i, j, rk))
   // TFSF2D::updateH (tfsf_2d.cpp:150-190) keeps the x- and y-face terms of
@@ -542,67 +572,76 @@ __device__ __forceinline__ void tfsf_h_surface(const TfsfSurfParams<T> &p, int q
   {
     const bool w1 = (j == lj - 1 || j == rj) && k >= lk && k < rk && i >= li && i <= ri;
     const bool w2 = !two_d && (k == lk - 1 || k == rk) && i >= li && i <= ri && j >= lj && j < rj;
-    if (w1 || w2) {
-      T h = p.F[3][b];
-      if (w1) {
-        const int jj = j == rj ? rj : lj;
-        const R pr = V.pf[0][i - li] + V.pf[1][jj - lj] + V.ph[2][k - lk + 1];
-        const R v = V.cb[1] * tfsf_interp(einc + 2 * tf.L, pr);
-        add_corr(h, j == rj ? -v : v);
-      }
-      if (w2) {
-        const int kk = k == rk ? rk : lk;
-        const R pr = V.pf[0][i - li] + V.ph[1][j - lj + 1] + V.pf[2][kk - lk];
-        const R v = V.cb[2] * tfsf_interp(einc + 1 * tf.L, pr);
-        add_corr(h, k == rk ? v : -v);
-      }
-      p.F[3][b] = h;
+    if (w1) {
+      const int jj = j == rj ? rj : lj;
+      const R pr = V.pf[0][i - li] + V.pf[1][jj - lj] + V.ph[2][k - lk + 1];
+      const R v = V.cb[1] * tfsf_interp(einc + 2 * tf.L, pr);
+      add_corr(hx, j == rj ? -v : v);
     }
+    if (w2) {
+      const int kk = k == rk ? rk : lk;
+      const R pr = V.pf[0][i - li] + V.ph[1][j - lj + 1] + V.pf[2][kk - lk];
+      const R v = V.cb[2] * tfsf_interp(einc + 1 * tf.L, pr);
+      add_corr(hx, k == rk ? v : -v);
+    }
+    w[0] = w1 || w2;
   }
   // Hy: x faces (i = li-1: -= cbx Ez_inc(li, j, k); i = ri: += cbx Ez_inc(ri, j, k)),
   //     z faces (k = lk-1: += cbz Ex_inc(i, j, lk); k = rk: -= cbz Ex_inc(i, j, rk))
   {
     const bool w1 = (i == li - 1 || i == ri) && j >= lj && j <= rj && k >= lk && k < rk;
     const bool w2 = !two_d && (k == lk - 1 || k == rk) && i >= li && i < ri && j >= lj && j <= rj;
-    if (w1 || w2) {
-      T h = p.F[4][b];
-      if (w1) {
-        const int ii = i == ri ? ri : li;
-        const R pr = V.pf[0][ii - li] + V.pf[1][j - lj] + V.ph[2][k - lk + 1];
-        const R v = V.cb[0] * tfsf_interp(einc + 2 * tf.L, pr);
-        add_corr(h, i == ri ? v : -v);
-      }
-      if (w2) {
-        const int kk = k == rk ? rk : lk;
-        const R pr = V.ph[0][i - li + 1] + V.pf[1][j - lj] + V.pf[2][kk - lk];
-        const R v = V.cb[2] * tfsf_interp(einc + 0 * tf.L, pr);
-        add_corr(h, k == rk ? -v : v);
-      }
-      p.F[4][b] = h;
+    if (w1) {
+      const int ii = i == ri ? ri : li;
+      const R pr = V.pf[0][ii - li] + V.pf[1][j - lj] + V.ph[2][k - lk + 1];
+      const R v = V.cb[0] * tfsf_interp(einc + 2 * tf.L, pr);
+      add_corr(hy, i == ri ? v : -v);
     }
+    if (w2) {
+      const int kk = k == rk ? rk : lk;
+      const R pr = V.ph[0][i - li + 1] + V.pf[1][j - lj] + V.pf[2][kk - lk];
+      const R v = V.cb[2] * tfsf_interp(einc + 0 * tf.L, pr);
+      add_corr(hy, k == rk ? -v : v);
+    }
+    w[1] = w1 || w2;
   }
   // Hz: x faces (i = li-1: += cbx Ey_inc(li, j, k); i = ri: -= cbx Ey_inc(ri, j, k)),
   //     y faces (j = lj-1: -= cby Ex_inc(i, lj, k); j = rj: += cby Ex_inc(i, rj, k))
   if (!two_d) {
     const bool w1 = (i == li - 1 || i == ri) && j >= lj && j < rj && k >= lk && k <= rk;
     const bool w2 = (j == lj - 1 || j == rj) && k >= lk && k <= rk && i >= li && i < ri;
-    if (w1 || w2) {
-      T h = p.F[5][b];
-      if (w1) {
-        const int ii = i == ri ? ri : li;
-        const R pr = V.pf[0][ii - li] + V.ph[1][j - lj + 1] + V.pf[2][k - lk];
-        const R v = V.cb[0] * tfsf_interp(einc + 1 * tf.L, pr);
-        add_corr(h, i == ri ? -v : v);
-      }
-      if (w2) {
-        const int jj = j == rj ? rj : lj;
-        const R pr = V.ph[0][i - li + 1] + V.pf[1][jj - lj] + V.pf[2][k - lk];
-        const R v = V.cb[1] * tfsf_interp(einc + 0 * tf.L, pr);
-        add_corr(h, j == rj ? v : -v);
-      }
-      p.F[5][b] = h;
+    if (w1) {
+      const int ii = i == ri ? ri : li;
+      const R pr = V.pf[0][ii - li] + V.ph[1][j - lj + 1] + V.pf[2][k - lk];
+      const R v = V.cb[0] * tfsf_interp(einc + 1 * tf.L, pr);
+      add_corr(hz, i == ri ? -v : v);
     }
+    if (w2) {
+      const int jj = j == rj ? rj : lj;
+      const R pr = V.ph[0][i - li + 1] + V.pf[1][jj - lj] + V.pf[2][k - lk];
+      const R v = V.cb[1] * tfsf_interp(einc + 0 * tf.L, pr);
+      add_corr(hz, j == rj ? v : -v);
+    }
+    w[2] = w1 || w2;
   }
+}
+
+// The H corrections at surface cell q of the box one cell larger on the low
+// sides, read from and written back to the fields.
+template <typename T>
+__device__ __forceinline__ void tfsf_h_surface(const TfsfSurfParams<T> &p, int q) {
+  const TfsfDev &tf = p.tf;
+  int i, j, k;
+  if (!surface_cell(q, tf.lo[0] - 1, tf.hi[0], tf.lo[1] - 1, tf.hi[1], tf.lo[2] - 1, tf.hi[2], i, j, k)) return;
+  const auto einc = tfsf_view<T>(tf).inc + ((*p.step) & 1) * 6 * tf.L;   // incident E of this step
+  const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
+  if (!tfsf_h_terms(tf, i, j, k)) return;
+  T hx = p.F[3][b], hy = p.F[4][b], hz = p.F[5][b];
+  bool w[3];
+  tfsf_h_cell<T>(tf, einc, i, j, k, hx, hy, hz, w);
+  if (w[0]) p.F[3][b] = hx;
+  if (w[1]) p.F[4][b] = hy;
+  if (w[2]) p.F[5][b] = hz;
 }
 
 template <typename T>
