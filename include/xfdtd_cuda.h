@@ -293,9 +293,10 @@ int xfdtd_launch_count(xfdtd_handle *h, int64_t *n);
 int xfdtd_launches_per_step(xfdtd_handle *h, int *n);
 /* Bytes copied host->device and device->host by the handle so far. */
 int xfdtd_transfer_bytes(xfdtd_handle *h, int64_t *h2d, int64_t *d2h);
-/* The TFSF surface corrections folded into the wide TMA launches.  Where
- * the plane wave's box lies in the wide decomposition's k range and the plan
- * has no lumped element, the E (H) launch applies TFSF3D::updateE's
+/* The TFSF surface corrections folded into the wide decomposition's TMA
+ * launches.  Where a side runs the wide decomposition on its two TMA
+ * launches (the wide interior launch and the z-edge launch) and the plan
+ * has no lumped element, those launches apply TFSF3D::updateE's
  * (updateH's) corrections to the cells of the box's surface
  * (src/tfsf/tfsf_3d.cpp:185-411), with the arithmetic of the separate
  * k_tfsf_e / k_tfsf_h launches, and those launches are left out.  The

@@ -99,6 +99,12 @@ struct xfdtd_handle {
   // inside the TFSF box, which the corrections' writes surround)
   bool nf_beside_tfsf = false;
   cudaEvent_t ev_nf_fork = nullptr, ev_nf_join = nullptr;
+  // split NF-FF sampling (enqueue_step_t): its stream, fork event, the
+  // events after the H half (+ fold) and after the E half, and whether the
+  // H half of the last stepped step is still to be taken
+  cudaStream_t nfs = nullptr;
+  cudaEvent_t ev_nfs_fork = nullptr, ev_nfh = nullptr, ev_nfe = nullptr;
+  bool nf_pending = false;
   cudaStream_t shell = nullptr;           // the volume shell kernels run here, beside the interior kernels
   cudaEvent_t ev_vfork[2] = {}, ev_vjoin[2] = {};
   std::vector<void *> allocs;
@@ -276,8 +282,12 @@ struct xfdtd_handle {
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_nf_fork) cudaEventDestroy(ev_nf_fork);
     if (ev_nf_join) cudaEventDestroy(ev_nf_join);
+    if (ev_nfs_fork) cudaEventDestroy(ev_nfs_fork);
+    if (ev_nfh) cudaEventDestroy(ev_nfh);
+    if (ev_nfe) cudaEventDestroy(ev_nfe);
     if (ev_join) cudaEventDestroy(ev_join);
     if (side) cudaStreamDestroy(side);
+    if (nfs) cudaStreamDestroy(nfs);
     for (int q = 0; q < 2; ++q) {
       if (ev_vfork[q]) cudaEventDestroy(ev_vfork[q]);
       if (ev_vjoin[q]) cudaEventDestroy(ev_vjoin[q]);
@@ -465,14 +475,6 @@ long long side_shell_cells(const xfdtd_handle *h, int side, bool wide) {
   return wide ? h->vshell_w_cells[side] : h->vshell_cells[side];
 }
 
-// Whether the side's TFSF corrections run inside its wide TMA launch this
-// step: the plan allows it (tf_fuse_ok, set at create) and the side runs
-// the wide decomposition with the split kernels.
-bool tfsf_fused(const xfdtd_handle *h, int side) {
-  return h->tfsf && h->tf_fuse_ok[side] && h->tf_fuse_on[side] && !h->sweep && side_wide(h, side) &&
-         kVariants[side == 0 ? h->var_e : h->var_h].stages != 0;
-}
-
 template <typename T, typename I, bool S, int MB, int NC, bool CT>
 void launch_vol_v(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, const Variant &v) {
   xg::InteriorBox in = h->vin[e_side ? 0 : 1];
@@ -509,6 +511,18 @@ constexpr int kNumShellVariants = sizeof(kShellVariants) / sizeof(kShellVariants
 bool shell_allowed(const xfdtd_handle *h, const ShellVariant &v, bool wide) {
   return !v.stages || (wide && h->it_ok[0] && h->it_ok[1] && h->wide_ok[0] && h->wide_ok[1]);
 }
+
+// Whether the side's TFSF corrections run inside its wide decomposition's
+// launches this step: the plan allows it (tf_fuse_ok, set at create), the
+// autotuner kept it (tf_fuse_on) and the side runs the wide decomposition
+// with the split kernels.
+bool tfsf_fused(const xfdtd_handle *h, int side) {
+  if (!(h->tfsf && h->tf_fuse_ok[side] && h->tf_fuse_on[side] && !h->sweep && side_wide(h, side))) return false;
+  // both launches of the wide decomposition are TMA-staged: the interior
+  // launch and, where there are z slabs, the z-edge launch
+  return side_shell_cells(h, side, true) == 0 || kShellVariants[h->shell_var[side]].stages != 0;
+}
+
 
 template <typename T, typename I, int MB, bool CT>
 void launch_shell_v(xfdtd_handle *h, bool e_side, const xg::ShellBoxes &s, cudaStream_t st) {
@@ -895,7 +909,7 @@ void interior_tma_setup(xfdtd_handle *h) {
     attr(xg::k_interior_tma_h<T, I, 4, false, M, KT>, GG::template smem_h<4>());
     attr(xg::k_interior_tma_h<T, I, 6, false, M, KT>, GG::template smem_h<6>());
     attr(xg::k_interior_tma_h<T, I, 4, true, M, KT>, GG::template smem_h<4>());
-    if constexpr (M == 1) {   // the wide launch with the TFSF corrections
+    if constexpr (M != 0) {   // the wide decomposition's launches with the TFSF corrections
       attr(xg::k_interior_tma_e<T, I, 4, false, M, KT, true>, GG::template smem_e<4>());
       attr(xg::k_interior_tma_e<T, I, 6, false, M, KT, true>, GG::template smem_e<6>());
       attr(xg::k_interior_tma_e<T, I, 4, true, M, KT, true>, GG::template smem_e<4>());
@@ -932,13 +946,13 @@ void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, 
   dim3 grid(nkt, (nj + G::J - 1) / G::J, (ni + chunk - 1) / chunk);
   const xg::ItMaps *maps = KT == xg::kItKz ? h->itm_z : h->itm;
   xg::TfsfFuse fz{};
-  if (MODE == 1 && tfsf_fused(h, side)) {
+  if (MODE != 0 && tfsf_fused(h, side)) {
     fz.tf = p.tf;
     fz.step = h->d_step;
     fz.on = 1;
   }
   const unsigned smem = e_side ? G::template smem_e<S>() : G::template smem_h<S>();
-  if constexpr (MODE == 1) {
+  if constexpr (MODE != 0) {
     if (fz.on) {
       if (e_side)
         xg::k_interior_tma_e<T, I, S, CT, MODE, KT, true><<<grid, xg::kItThreads, smem, st>>>(
@@ -1134,9 +1148,10 @@ void autotune_t(xfdtd_handle *h, int trials) {
     var = best_v;
     h->shell_var[side] = best_sv;
     h->tune_ms[side][best_v] = best;
-    // the TFSF corrections inside the wide launch, or as their own launch
-    // after the pair: whichever is faster
-    if (h->tf_fuse_ok[side] && kVariants[best_v].wide) {
+    // the TFSF corrections inside the wide decomposition's launches, or as
+    // their own launch after the pair: whichever is faster
+    if (h->tf_fuse_ok[side] && kVariants[best_v].wide &&
+        (side_shell_cells(h, side, true) == 0 || kShellVariants[best_sv].stages != 0)) {
       h->tf_fuse_on[side] = true;
       const float fused = time_n([&] { volume_pair<T, I>(h, side == 0); }, 3 * trials);
       h->tf_fuse_on[side] = false;
@@ -1224,10 +1239,12 @@ long long nffft_fold_blocks(const xfdtd_handle *h) {
   return (most + 255) / 256;
 }
 
+// The NF-FF samples of step *step - lag (part 0: all, 1: the E half, 2: the
+// H half; nffft_sample in surface.cuh).
 template <typename T>
-void launch_nffft(xfdtd_handle *h, cudaStream_t st = nullptr) {
+void launch_nffft(xfdtd_handle *h, cudaStream_t st = nullptr, int part = 0, int lag = 0) {
   const auto p = nf_params<T>(h);
-  xg::k_nffft<T><<<nffft_grid(h), dim3(32, 8, 1), 0, st ? st : h->stream>>>(p);
+  xg::k_nffft<T><<<nffft_grid(h), dim3(32, 8, 1), 0, st ? st : h->stream>>>(p, part, lag);
   XCHECK(cudaGetLastError());
 }
 
@@ -1235,22 +1252,41 @@ void launch_nffft(xfdtd_handle *h, cudaStream_t st = nullptr) {
 // a step (the device step counter points at the last sampled step), 1 after
 // it (the counter has advanced past it).
 template <typename T>
-void launch_nffft_accumulate(xfdtd_handle *h, int count, int lag) {
+void launch_nffft_accumulate(xfdtd_handle *h, int count, int lag, cudaStream_t st = nullptr) {
   const auto p = nf_params<T>(h);
   dim3 grid(static_cast<unsigned>(nffft_fold_blocks(h)), 1, 3);
-  xg::k_nffft_accumulate<T><<<grid, 256, 0, h->stream>>>(p, count, lag);
+  xg::k_nffft_accumulate<T><<<grid, 256, 0, st ? st : h->stream>>>(p, count, lag);
   XCHECK(cudaGetLastError());
+}
+
+// The split NF-FF sampling leaves the H half of the last stepped step
+// pending: the next step takes it (and folds a full batch) on the NF-FF
+// stream beside its E update.  Before a read of the accumulators or the far
+// field, and before a captured graph is replayed, it is taken here on the
+// main stream, with the fold of every step sampled since the last one.
+template <typename T>
+void nffft_catch_up_t(xfdtd_handle *h) {
+  if (h->nf_pending) {
+    prof_begin(h, 4);
+    launch_nffft<T>(h, h->stream, 2, 1);
+    prof_end(h);
+    h->nf_pending = false;
+  }
+  const long long pending = h->host_step - h->nf_done;
+  if (pending > 0) {
+    prof_begin(h, 9);
+    launch_nffft_accumulate<T>(h, static_cast<int>(pending), 1);
+    prof_end(h);
+    h->nf_done = h->host_step;
+  }
 }
 
 // Accumulates the NF-FF steps sampled since the last fold (before any read
 // of the accumulators or the far field).
 void nffft_flush(xfdtd_handle *h) {
   if (!h->nffft || h->nf_bb) return;
-  const long long pending = h->host_step - h->nf_done;
-  if (pending <= 0) return;
-  if (h->precision == XFDTD_FP64) launch_nffft_accumulate<double>(h, static_cast<int>(pending), 1);
-  else launch_nffft_accumulate<float>(h, static_cast<int>(pending), 1);
-  h->nf_done = h->host_step;
+  if (h->precision == XFDTD_FP64) nffft_catch_up_t<double>(h);
+  else nffft_catch_up_t<float>(h);
 }
 
 template <typename T>
@@ -1331,7 +1367,29 @@ void volume_pair(xfdtd_handle *h, bool e_side) {
 }
 
 template <typename T, typename I>
-void enqueue_step_t(xfdtd_handle *h, long long s) {
+void enqueue_step_t(xfdtd_handle *h, long long s, bool pre) {
+  // The NF-FF samples of a step are taken in two halves on their own stream
+  // (nfs): the E half beside this step's H update, the H half beside the
+  // next step's E update; a full batch is folded there too, after the H half
+  // of its last step.  (Broadband NF-FF and the fused sweep keep one launch.)
+  const bool split = h->nffft && !h->nf_bb && !h->sweep;
+  bool wait_nfh = false;
+  if (h->nffft && !h->nf_bb && h->nf_pending && pre) {
+    XCHECK(cudaEventRecord(h->ev_nfs_fork, h->stream));
+    XCHECK(cudaStreamWaitEvent(h->nfs, h->ev_nfs_fork, 0));
+    prof_begin(h, 4, h->nfs);
+    launch_nffft<T>(h, h->nfs, 2, 1);
+    prof_end(h, h->nfs);
+    if (s % h->nf_batch == 0 && s > h->nf_done) {
+      prof_begin(h, 9, h->nfs);
+      launch_nffft_accumulate<T>(h, static_cast<int>(s - h->nf_done), 1, h->nfs);
+      prof_end(h, h->nfs);
+      h->nf_done = s;
+    }
+    XCHECK(cudaEventRecord(h->ev_nfh, h->nfs));
+    h->nf_pending = false;
+    wait_nfh = true;
+  }
   if (h->tfsf) {
     const xg::AuxParams a = aux_params(h);
     // The 1-D line of step t runs on a side stream, beside the E update: it
@@ -1368,14 +1426,28 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
       XCHECK(cudaGetLastError());
       prof_end(h);
     }
+    // E is final for this step: its NF-FF half is taken beside the H update
+    if (split) {
+      XCHECK(cudaEventRecord(h->ev_nfs_fork, h->stream));
+      XCHECK(cudaStreamWaitEvent(h->nfs, h->ev_nfs_fork, 0));
+      prof_begin(h, 4, h->nfs);
+      launch_nffft<T>(h, h->nfs, 1, 0);
+      prof_end(h, h->nfs);
+      XCHECK(cudaEventRecord(h->ev_nfe, h->nfs));
+    }
     // the H launch that applies the TFSF H corrections reads this step's
-    // incident E: the 1-D line joins before it
+    // incident E: the 1-D line joins before it; the H half of the previous
+    // step's NF-FF samples must be taken before H changes
     if (h->tfsf && tfsf_fused(h, 1)) XCHECK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
+    if (wait_nfh) XCHECK(cudaStreamWaitEvent(h->stream, h->ev_nfh, 0));
+    wait_nfh = false;
     volume_pair<T, I>(h, false);
   }
-  // NF-FF sampling on the side stream beside the TFSF H corrections when
-  // their cells are disjoint; joined before the samples are folded
-  const bool nf_side = h->nffft && h->tfsf && h->nf_beside_tfsf;
+  if (wait_nfh) XCHECK(cudaStreamWaitEvent(h->stream, h->ev_nfh, 0));
+  // NF-FF sampling in one launch (broadband, or the fused sweep) on the side
+  // stream beside the TFSF H corrections when their cells are disjoint;
+  // joined before the samples are folded
+  const bool nf_side = !split && h->nffft && h->tfsf && h->nf_beside_tfsf;
   if (nf_side) {
     XCHECK(cudaEventRecord(h->ev_nf_fork, h->stream));
     XCHECK(cudaStreamWaitEvent(h->side, h->ev_nf_fork, 0));
@@ -1394,7 +1466,7 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     XCHECK(cudaGetLastError());
     prof_end(h);
   }
-  if (h->nffft) {
+  if (h->nffft && !split) {
     if (nf_side) {
       XCHECK(cudaStreamWaitEvent(h->stream, h->ev_nf_join, 0));
     } else {
@@ -1430,6 +1502,11 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
     XCHECK(cudaGetLastError());
     prof_end(h);
   }
+  // the E half reads the step counter: it joins before the counter moves
+  if (split) {
+    XCHECK(cudaStreamWaitEvent(h->stream, h->ev_nfe, 0));
+    h->nf_pending = true;
+  }
   prof_begin(h, 6);
   xg::k_advance<<<1, 1, 0, h->stream>>>(h->d_step);
   XCHECK(cudaGetLastError());
@@ -1437,9 +1514,12 @@ void enqueue_step_t(xfdtd_handle *h, long long s) {
 }
 
 // Enqueues the kernels of step s (s = the step's index, known on the host).
-void enqueue_step(xfdtd_handle *h, long long s) {
+// pre: also take the pending H half of the previous step's NF-FF samples
+// (and fold a finished batch) first; a captured graph's first step leaves
+// that to a catch-up before the replay.
+void enqueue_step(xfdtd_handle *h, long long s, bool pre = true) {
   with_types(h->precision, h->idx_bytes, [&](auto t, auto i) {
-    enqueue_step_t<decltype(t), decltype(i)>(h, s);
+    enqueue_step_t<decltype(t), decltype(i)>(h, s, pre);
   });
 }
 
@@ -1461,11 +1541,13 @@ int launches_per_step(const xfdtd_handle *h) {
 void build_graph(xfdtd_handle *h, int g) {
   cudaGraph_t graph;
   const long long nf_done = h->nf_done, launches = h->launch_count;
+  const bool nf_pending = h->nf_pending;
   XCHECK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  for (int s = 0; s < g; ++s) enqueue_step(h, h->host_step + s);
+  for (int s = 0; s < g; ++s) enqueue_step(h, h->host_step + s, s > 0);
   XCHECK(cudaStreamEndCapture(h->stream, &graph));
   h->graph_launches = h->launch_count - launches;
   h->nf_done = nf_done;   // capture only recorded the launches
+  h->nf_pending = nf_pending;
   h->launch_count = launches;
   cudaError_t e = cudaGraphInstantiate(&h->gexec, graph, 0);
   cudaGraphDestroy(graph);
@@ -1536,6 +1618,10 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   XCHECK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
   XCHECK(cudaEventCreateWithFlags(&h->ev_nf_fork, cudaEventDisableTiming));
   XCHECK(cudaEventCreateWithFlags(&h->ev_nf_join, cudaEventDisableTiming));
+  XCHECK(cudaStreamCreateWithFlags(&h->nfs, cudaStreamNonBlocking));
+  XCHECK(cudaEventCreateWithFlags(&h->ev_nfs_fork, cudaEventDisableTiming));
+  XCHECK(cudaEventCreateWithFlags(&h->ev_nfh, cudaEventDisableTiming));
+  XCHECK(cudaEventCreateWithFlags(&h->ev_nfe, cudaEventDisableTiming));
   {
     // the shell launch is the pair's long pole: its blocks go first as the
     // interior's retire
@@ -1854,13 +1940,10 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
       else sweep_setup<float, uint16_t>(h);
     }
   }
-  // the TFSF corrections inside the wide TMA launches: 3-D plane wave, no
-  // lumped element, the E surface [lo, hi] and the H surface [lo-1, hi]
-  // within the wide launches' k ranges (they cover every i and j)
-  if (h->tfsf && !h->tf_two_d && h->n_inj == 0 && h->n_ind == 0) {
-    h->tf_fuse_ok[0] = h->wide_ok[0] && h->vin_w[0].lo[2] <= h->tf_lo[2] && h->tf_hi[2] <= h->vin_w[0].hi[2];
-    h->tf_fuse_ok[1] = h->wide_ok[1] && h->vin_w[1].lo[2] <= h->tf_lo[2] - 1 && h->tf_hi[2] <= h->vin_w[1].hi[2];
-  }
+  // the TFSF corrections inside the wide decomposition's TMA launches (they
+  // cover every cell): 3-D plane wave, no lumped element
+  if (h->tfsf && !h->tf_two_d && h->n_inj == 0 && h->n_ind == 0)
+    for (int side = 0; side < 2; ++side) h->tf_fuse_ok[side] = h->wide_ok[side];
   XCHECK(cudaStreamSynchronize(h->stream));
   h->create_ms[0] = ms_since(t_begin);
   const auto t_tune = std::chrono::steady_clock::now();
@@ -2064,14 +2147,21 @@ void do_steps(xfdtd_handle *h, long long n) {
   const int B = h->nf_batch;
   // single steps up to a batch boundary, whole graphs, then single steps
   while (h->host_step < end) {
-    const bool aligned = h->host_step % B == 0 && (!h->nffft || h->nf_done == h->host_step);
+    const bool aligned = h->host_step % B == 0;
     const long long graph_len = h->gexec ? h->graph_steps : 4 * B;
     if (graph && aligned && end - h->host_step >= graph_len) {
+      // the graph's steps fold whole batches from its first step on
+      nffft_flush(h);
       if (!h->gexec) build_graph(h, static_cast<int>(graph_len));
       XCHECK(cudaGraphLaunch(h->gexec, h->stream));
       h->host_step += h->graph_steps;
       h->launch_count += h->graph_launches;
-      if (h->nffft) h->nf_done = h->host_step;
+      if (h->nffft && !h->nf_bb && !h->sweep) {   // split sampling: the last batch and H half wait
+        h->nf_done = h->host_step - B;
+        h->nf_pending = true;
+      } else if (h->nffft) {
+        h->nf_done = h->host_step;
+      }
       continue;
     }
     enqueue_step(h, h->host_step);

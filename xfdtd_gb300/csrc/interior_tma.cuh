@@ -58,12 +58,13 @@
 
 namespace xg {
 
-// The TFSF corrections folded into the wide launch (mode 1): when `on`,
+// The TFSF corrections folded into the wide decomposition's launches
+// (modes 1 and 2, which together cover every cell): when `on`,
 // the cells of the TFSF box's surface get TFSF3D::updateE's (E kernel) or
 // updateH's (H kernel) corrections after their update, with the same
 // arithmetic as k_tfsf_e / k_tfsf_h (surface.cuh), before the store.  The
-// engine turns it on when the whole surface lies in the wide launch's k
-// range and no lumped element's correction would have to come first.
+// engine turns it on when the wide decomposition runs on its two TMA
+// launches and no lumped element's correction would have to come first.
 struct TfsfFuse {
   TfsfDev tf;
   const long long *step;
@@ -234,7 +235,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
     if (MODE == 2) slab_axis(p, 2, 0, k, cx.zs, cx.Z);
   }
   // the incident H arrays of the previous step (the 1-D line's other buffer)
-  const auto hinc = (MODE == 1 && TF) ? tfsf_view<T>(fz.tf).inc + ((*fz.step + 1) & 1) * 6 * fz.tf.L : nullptr;
+  const auto hinc = (MODE != 0 && TF) ? tfsf_view<T>(fz.tf).inc + ((*fz.step + 1) & 1) * 6 * fz.tf.L : nullptr;
   for (int i = blk.ia; i < blk.ib; ++i) {
     // a special cell's psi operands, loaded before the wait for the plane
     const int cls = MODE == 0 ? 0 : ((i < in.px_lo || i > in.px_hi) ? 1 : 0) | (yspec ? 2 : 0) | (MODE == 2 ? 4 : 0);
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
       coefs<T, I, CT>(p, p.table, 18, m, 0, cf);
       if (MODE != 2 && cls == 0) {
         e_plain(cf, h, ex, ey, ez);
-        if (MODE == 1 && TF && tfsf_on_e_surface(fz.tf, i, j, k)) {
+        if (MODE != 0 && TF && tfsf_on_e_surface(fz.tf, i, j, k)) {
           bool w[3];
           tfsf_e_fused_call<T>(fz.tf, hinc, i, j, k, ex, ey, ez, w);
         }
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
         } else {
           e_general_ops<T, I, 3>(p, cf, i, j, k, h, cx, ps, p.psi, true, ex, ey, ez, w);
         }
-        if (MODE == 1 && TF && tfsf_on_e_surface(fz.tf, i, j, k)) {
+        if (MODE != 0 && TF && tfsf_on_e_surface(fz.tf, i, j, k)) {
           bool wt[3];
           tfsf_e_fused_call<T>(fz.tf, hinc, i, j, k, ex, ey, ez, wt);
           for (int q = 0; q < 3; ++q) w[q] = w[q] || wt[q];
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
     if (MODE == 2) slab_axis(p, 2, 1, k, cx.zs, cx.Z);
   }
   // the incident E arrays of this step (written by the 1-D line beside the E update)
-  const auto einc = (MODE == 1 && TF) ? tfsf_view<T>(fz.tf).inc + (*fz.step & 1) * 6 * fz.tf.L : nullptr;
+  const auto einc = (MODE != 0 && TF) ? tfsf_view<T>(fz.tf).inc + (*fz.step & 1) * 6 * fz.tf.L : nullptr;
   for (int i = blk.ia; i < blk.ib; ++i) {
     const int cls = MODE == 0 ? 0 : ((i < in.px_lo || i > in.px_hi) ? 1 : 0) | (yspec ? 2 : 0) | (MODE == 2 ? 4 : 0);
     PsiOps<T> pv{};
@@ -396,7 +397,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
       coefs<T, I, CT>(p, p.table + 9, 18, m, 1, cf);
       if (MODE != 2 && cls == 0) {
         h_plain(cf, e, hx, hy, hz);
-        if (MODE == 1 && TF && tfsf_h_terms(fz.tf, i, j, k)) {
+        if (MODE != 0 && TF && tfsf_h_terms(fz.tf, i, j, k)) {
           bool w[3];
           tfsf_h_cell_call<T>(fz.tf, einc, i, j, k, hx, hy, hz, w);
         }
@@ -418,7 +419,7 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_cons
         } else {
           h_general_ops<T, I, 3>(p, cf, i, j, k, e, cx, pv, hx, hy, hz, w);
         }
-        if (MODE == 1 && TF && tfsf_h_terms(fz.tf, i, j, k)) {
+        if (MODE != 0 && TF && tfsf_h_terms(fz.tf, i, j, k)) {
           bool wt[3];
           tfsf_h_cell_call<T>(fz.tf, einc, i, j, k, hx, hy, hz, wt);
           for (int q = 0; q < 3; ++q) w[q] = w[q] || wt[q];

@@ -98,11 +98,17 @@ struct NfParams {
   int batch;
 };
 
-// Samples face pair `face` at face coordinates (u, v) (u the fastest axis).
+// Samples face pair `face` at face coordinates (u, v) (u the fastest axis)
+// for step *step - lag.  part 0 takes all eight values of a face pair; part
+// 1 the four from E (the M currents), part 2 the four from H (the J
+// currents): E is final once the step's E update and corrections are done,
+// H once its H update is, so each half can be taken while the other field
+// is still being updated.
 template <typename T>
-__device__ __forceinline__ void nffft_sample(const NfParams<T> &p, int face, int u, int v) {
-  const long long t = *p.step;
-  if (t >= p.total) return;
+__device__ __forceinline__ void nffft_sample(const NfParams<T> &p, int face, int u, int v, int part = 0,
+                                             int lag = 0) {
+  const long long t = *p.step - lag;
+  if (t < 0 || t >= p.total) return;
   const int li = p.lo[0], lj = p.lo[1], lk = p.lo[2], ri = p.hi[0], rj = p.hi[1], rk = p.hi[2];
   const long long si = p.d.si, sj = p.d.sj;
   const T *ex = p.E[0], *ey = p.E[1], *ez = p.E[2], *hx = p.H[0], *hy = p.H[1], *hz = p.H[2];
@@ -112,63 +118,69 @@ __device__ __forceinline__ void nffft_sample(const NfParams<T> &p, int face, int
     return f[static_cast<long long>(i) * si + static_cast<long long>(j) * sj + k];
   };
   const T half = T(0.5), quarter = T(0.25), neg = T(-1);
-  T val[8];
+  const bool want_e = part != 2, want_h = part != 1;
+  T val[8] = {};
   long long cell, plane;
   int base;
   if (face == 0) {  // X faces: j in [lj, rj), k in [lk, rk); jy, jz, my, mz
     const int k = lk + u, j = lj + v;
     if (k >= rk || j >= rj) return;
     // M = -/+ E face centres, J = +/- H face centres
-    val[2] = neg * (half * (at(ez, li, j, k) + at(ez, li, j + 1, k)));            // my_xn
-    val[3] = half * (at(ey, li, j, k) + at(ey, li, j, k + 1));                   // mz_xn
-    val[0] = quarter * (at(hz, li, j, k) + at(hz, li, j, k + 1) + at(hz, li - 1, j, k) + at(hz, li - 1, j, k + 1));
-    val[1] = neg * (quarter * (at(hy, li, j, k) + at(hy, li, j + 1, k) + at(hy, li - 1, j, k) + at(hy, li - 1, j + 1, k)));
-    val[6] = half * (at(ez, ri, j, k) + at(ez, ri, j + 1, k));                   // my_xp
-    val[7] = neg * (half * (at(ey, ri, j, k) + at(ey, ri, j, k + 1)));            // mz_xp
-    val[4] = neg * (quarter * (at(hz, ri, j, k) + at(hz, ri, j, k + 1) + at(hz, ri - 1, j, k) + at(hz, ri - 1, j, k + 1)));
-    val[5] = quarter * (at(hy, ri, j, k) + at(hy, ri, j + 1, k) + at(hy, ri - 1, j, k) + at(hy, ri - 1, j + 1, k));
+    if (want_e) val[2] = neg * (half * (at(ez, li, j, k) + at(ez, li, j + 1, k)));            // my_xn
+    if (want_e) val[3] = half * (at(ey, li, j, k) + at(ey, li, j, k + 1));                   // mz_xn
+    if (want_h) val[0] = quarter * (at(hz, li, j, k) + at(hz, li, j, k + 1) + at(hz, li - 1, j, k) + at(hz, li - 1, j, k + 1));
+    if (want_h) val[1] = neg * (quarter * (at(hy, li, j, k) + at(hy, li, j + 1, k) + at(hy, li - 1, j, k) + at(hy, li - 1, j + 1, k)));
+    if (want_e) val[6] = half * (at(ez, ri, j, k) + at(ez, ri, j + 1, k));                   // my_xp
+    if (want_e) val[7] = neg * (half * (at(ey, ri, j, k) + at(ey, ri, j, k + 1)));            // mz_xp
+    if (want_h) val[4] = neg * (quarter * (at(hz, ri, j, k) + at(hz, ri, j, k + 1) + at(hz, ri - 1, j, k) + at(hz, ri - 1, j, k + 1)));
+    if (want_h) val[5] = quarter * (at(hy, ri, j, k) + at(hy, ri, j + 1, k) + at(hy, ri - 1, j, k) + at(hy, ri - 1, j + 1, k));
     cell = static_cast<long long>(j - lj) * (rk - lk) + (k - lk);
     plane = static_cast<long long>(rj - lj) * (rk - lk);
     base = 0;
   } else if (face == 1) {  // Y faces: k in [lk, rk), i in [li, ri); jz, jx, mz, mx
     const int k = lk + u, i = li + v;
     if (k >= rk || i >= ri) return;
-    val[2] = neg * (half * (at(ex, i, lj, k) + at(ex, i, lj + 1, k)));            // mz_yn
-    val[3] = half * (at(ez, i, lj, k) + at(ez, i + 1, lj, k));                   // mx_yn
-    val[0] = quarter * (at(hx, i + 1, lj, k) + at(hx, i, lj, k) + at(hx, i + 1, lj - 1, k) + at(hx, i, lj - 1, k));
-    val[1] = neg * (quarter * (at(hz, i, lj, k) + at(hz, i, lj, k + 1) + at(hz, i, lj - 1, k) + at(hz, i, lj - 1, k + 1)));
-    val[6] = half * (at(ex, i, rj, k) + at(ex, i, rj + 1, k));                   // mz_yp
-    val[7] = neg * (half * (at(ez, i, rj, k) + at(ez, i + 1, rj, k)));            // mx_yp
-    val[4] = neg * (quarter * (at(hx, i + 1, rj, k) + at(hx, i, rj, k) + at(hx, i + 1, rj - 1, k) + at(hx, i, rj - 1, k)));
-    val[5] = quarter * (at(hz, i, rj, k) + at(hz, i, rj, k + 1) + at(hz, i, rj - 1, k) + at(hz, i, rj - 1, k + 1));
+    if (want_e) val[2] = neg * (half * (at(ex, i, lj, k) + at(ex, i, lj + 1, k)));            // mz_yn
+    if (want_e) val[3] = half * (at(ez, i, lj, k) + at(ez, i + 1, lj, k));                   // mx_yn
+    if (want_h) val[0] = quarter * (at(hx, i + 1, lj, k) + at(hx, i, lj, k) + at(hx, i + 1, lj - 1, k) + at(hx, i, lj - 1, k));
+    if (want_h) val[1] = neg * (quarter * (at(hz, i, lj, k) + at(hz, i, lj, k + 1) + at(hz, i, lj - 1, k) + at(hz, i, lj - 1, k + 1)));
+    if (want_e) val[6] = half * (at(ex, i, rj, k) + at(ex, i, rj + 1, k));                   // mz_yp
+    if (want_e) val[7] = neg * (half * (at(ez, i, rj, k) + at(ez, i + 1, rj, k)));            // mx_yp
+    if (want_h) val[4] = neg * (quarter * (at(hx, i + 1, rj, k) + at(hx, i, rj, k) + at(hx, i + 1, rj - 1, k) + at(hx, i, rj - 1, k)));
+    if (want_h) val[5] = quarter * (at(hz, i, rj, k) + at(hz, i, rj, k + 1) + at(hz, i, rj - 1, k) + at(hz, i, rj - 1, k + 1));
     cell = static_cast<long long>(i - li) * (rk - lk) + (k - lk);
     plane = static_cast<long long>(ri - li) * (rk - lk);
     base = 8;
   } else {  // Z faces: i in [li, ri), j in [lj, rj); jx, jy, mx, my
     const int j = lj + u, i = li + v;
     if (j >= rj || i >= ri) return;
-    val[2] = neg * (half * (at(ey, i, j, lk) + at(ey, i + 1, j, lk)));            // mx_zn
-    val[3] = half * (at(ex, i, j, lk) + at(ex, i, j, lk + 1));                   // my_zn
-    val[0] = quarter * (at(hy, i, j, lk) + at(hy, i, j + 1, lk) + at(hy, i, j, lk - 1) + at(hy, i, j + 1, lk - 1));
-    val[1] = neg * (quarter * (at(hx, i + 1, j, lk) + at(hx, i, j, lk) + at(hx, i + 1, j, lk - 1) + at(hx, i, j, lk - 1)));
-    val[6] = half * (at(ey, i, j, rk) + at(ey, i + 1, j, rk));                   // mx_zp
-    val[7] = neg * (half * (at(ex, i, j, rk) + at(ex, i, j, rk + 1)));            // my_zp
-    val[4] = neg * (quarter * (at(hy, i, j, rk) + at(hy, i, j + 1, rk) + at(hy, i, j, rk - 1) + at(hy, i, j + 1, rk - 1)));
-    val[5] = quarter * (at(hx, i + 1, j, rk) + at(hx, i, j, rk) + at(hx, i + 1, j, rk - 1) + at(hx, i, j, rk - 1));
+    if (want_e) val[2] = neg * (half * (at(ey, i, j, lk) + at(ey, i + 1, j, lk)));            // mx_zn
+    if (want_e) val[3] = half * (at(ex, i, j, lk) + at(ex, i, j, lk + 1));                   // my_zn
+    if (want_h) val[0] = quarter * (at(hy, i, j, lk) + at(hy, i, j + 1, lk) + at(hy, i, j, lk - 1) + at(hy, i, j + 1, lk - 1));
+    if (want_h) val[1] = neg * (quarter * (at(hx, i + 1, j, lk) + at(hx, i, j, lk) + at(hx, i + 1, j, lk - 1) + at(hx, i, j, lk - 1)));
+    if (want_e) val[6] = half * (at(ey, i, j, rk) + at(ey, i + 1, j, rk));                   // mx_zp
+    if (want_e) val[7] = neg * (half * (at(ex, i, j, rk) + at(ex, i, j, rk + 1)));            // my_zp
+    if (want_h) val[4] = neg * (quarter * (at(hy, i, j, rk) + at(hy, i, j + 1, rk) + at(hy, i, j, rk - 1) + at(hy, i, j + 1, rk - 1)));
+    if (want_h) val[5] = quarter * (at(hx, i + 1, j, rk) + at(hx, i, j, rk) + at(hx, i + 1, j, rk - 1) + at(hx, i, j, rk - 1));
     cell = static_cast<long long>(i - li) * (rj - lj) + (j - lj);
     plane = static_cast<long long>(ri - li) * (rj - lj);
     base = 16;
   }
   // store the step's surface values in slot t % batch; k_nffft_accumulate
-  // folds a whole batch into the FP64 accumulators
+  // folds a whole batch into the FP64 accumulators (values 0, 1, 4, 5 come
+  // from H, 2, 3, 6, 7 from E)
   T *buf = p.buf[base / 8] + (static_cast<long long>(t % p.batch) * 8) * plane + cell;
 #pragma unroll
-  for (int q = 0; q < 8; ++q) buf[q * plane] = val[q];
+  for (int q = 0; q < 8; ++q) {
+    const bool from_e = (q & 2) != 0;
+    if (part == 0 || (part == 1) == from_e) buf[q * plane] = val[q];
+  }
 }
 
 template <typename T>
-__global__ void k_nffft(NfParams<T> p) {
-  nffft_sample(p, blockIdx.z, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+__global__ void k_nffft(NfParams<T> p, int part, int lag) {
+  nffft_sample(p, blockIdx.z, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y, part,
+               lag);
 }
 
 // acc[n] += v[s] * phase[n][t0 + s] for the `count` (<= 8) buffered steps
