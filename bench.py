@@ -166,14 +166,15 @@ def _peaks():
 
 # --------------------------------------------------------------- roofline ---
 # Entries timed on their own streams, concurrently with the main stream's:
-# the TFSF 1-D line, the NF-FF sampling (beside the TFSF H corrections when
-# its box lies inside the TFSF box), and the two kernels of each volume update (whose
+# the TFSF 1-D line, the NF-FF sampling and batch folds (the E half of a
+# step's samples beside its H update, the H half and the folds beside the
+# next step's E update), and the two kernels of each volume update (whose
 # main-stream entry, update_e / update_h, spans both).
 GRAPH_STEPS = 32        # steps per captured CUDA graph (4 NF-FF batches of 8)
 PROFILE_STEPS = 400     # steps of the profiled pass behind the kernel times
 
-SIDE_STREAM_KERNELS = ("tfsf_aux", "nffft", "update_e_interior", "update_e_shell", "update_h_interior",
-                       "update_h_shell")
+SIDE_STREAM_KERNELS = ("tfsf_aux", "nffft", "nffft_acc", "update_e_interior", "update_e_shell",
+                       "update_h_interior", "update_h_shell")
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one E and
 # one H update on this workload in the wide decomposition, keyed by (entry,
@@ -426,6 +427,7 @@ def _timed(sc, precision, steps, warmup, local, grp=None, fused=False, variants=
         grp.barrier()
     out = {"n": tuple(n), "cells": n[0] * n[1] * n[2], "ms": ms, "launches": sim.launch_count() - l0,
            "variants": sim.kernel_variants(), "shell_variants": sim.shell_variants(), "split": sim.volume_split(),
+           "tfsf_folded": sim.tfsf_fusion(),
            "setup_steps": setup,
            "timed_path": f"{steps // GRAPH_STEPS} CUDA graph replays of {GRAPH_STEPS} steps + "
                          f"{steps % GRAPH_STEPS} single steps, after {warmup} warm-up steps and {setup} untimed "
@@ -444,7 +446,9 @@ def _profiled(sc, precision, steps, warmup, local, run, fused=False):
                         fused=fused)
     psim.set_kernel_variant(run["variants"]["e"], run["variants"]["h"])
     psim.set_shell_variant(run["shell_variants"]["e"], run["shell_variants"]["h"])
+    psim.set_tfsf_fusion(*run["tfsf_folded"])
     assert psim.volume_split() == run["split"]
+    assert psim.tfsf_fusion() == run["tfsf_folded"]
     psim.step(warmup)
     psim.synchronize()
     psim.profile_reset()
@@ -664,6 +668,7 @@ def ours_arm(args, world, rank, local, grp):
         "volume_split_cells": split,
         "volume_kernels_concurrent": concurrent,
         "autotuned_variants": {"update_e": v["e"], "update_h": v["h"], "shell_e": sv["e"], "shell_h": sv["h"],
+                               "tfsf_folded": {"e": run["tfsf_folded"][0], "h": run["tfsf_folded"][1]},
                                "trial_ms_e": [round(q, 4) for q in v["trials_e"]],
                                "trial_ms_h": [round(q, 4) for q in v["trials_h"]]},
         "e2e": e2e,
