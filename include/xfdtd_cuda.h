@@ -159,6 +159,27 @@ typedef struct xfdtd_snapshot_desc {
   int64_t last;
 } xfdtd_snapshot_desc;
 
+/* A linear dispersive medium's E recursion, LorentzMedium /
+ * DrudeMedium / DebyMedium::updateE{x,y,z} (src/material/dispersive_material.cpp):
+ * kind 1 Lorentz, 2 Drude, 3 Debye, with the coefficients their init
+ * computes (Lorentz: ca cb cc alpha xi gamma; Drude and Debye: ca cb k
+ * beta).  The reference throws on dispersive objects at Object::init
+ * (object.cpp:109-110); the engine runs them. */
+typedef struct xfdtd_dispersive_medium {
+  int32_t kind;
+  int32_t reserved;
+  double ca, cb, cc, alpha, xi, gamma;
+  double k, beta;
+} xfdtd_dispersive_medium;
+
+/* One E component (comp 0..2) at (i, j, k) whose update is its medium's
+ * recursion instead of the Yee update; its table entry leaves E as it is. */
+typedef struct xfdtd_dispersive_cell {
+  int32_t comp;
+  int32_t medium;
+  int64_t i, j, k;
+} xfdtd_dispersive_cell;
+
 typedef struct xfdtd_plan_desc {
   int32_t nx, ny, nz;
   int32_t precision;               /* XFDTD_FP64 or XFDTD_FP32 (fields, psi)    */
@@ -187,6 +208,11 @@ typedef struct xfdtd_plan_desc {
   int32_t n_snapshots;
   int32_t reserved3;
   const xfdtd_snapshot_desc *snapshots;
+  int32_t n_disp_media;            /* linear dispersive media (above)         */
+  int32_t n_disp_cells;
+  const xfdtd_dispersive_medium *disp_media;
+  const xfdtd_dispersive_cell *disp_cells;
+  double disp_dl;                  /* the uniform cell size of their recursions */
 } xfdtd_plan_desc;
 
 typedef struct xfdtd_handle xfdtd_handle;

@@ -77,11 +77,31 @@ typedef struct xfdtd_shape_desc {
   double height;     /* cylinder                                         */
 } xfdtd_shape_desc;
 
+/* dispersion: 0 for a plain Material.  The reference's linear dispersive
+ * media (src/include/material/dispersive_material.h) take their E update
+ * from the auxiliary-differential-equation recursions of their
+ * updateEx/Ey/Ez (src/material/dispersive_material.cpp), with eps_r = mu_r
+ * = 1 and the conductivities in sigma_e, sigma_m:
+ *   1 LorentzMedium(eps_s, eps_inf, omega_p, nv)  p = {eps_s, eps_inf, omega_p, nv}
+ *   2 DrudeMedium(eps_inf, omega_p, nv)           p = {eps_inf, omega_p, nv, 0}
+ *   3 DebyMedium(eps_s, eps_inf, tau)             p = {eps_s, eps_inf, tau, 0}
+ * The reference throws on them at Object::init (object.cpp:109-110); here
+ * they run, as objects outside the CPML. */
+enum {
+  XFDTD_DISPERSION_NONE = 0,
+  XFDTD_DISPERSION_LORENTZ = 1,
+  XFDTD_DISPERSION_DRUDE = 2,
+  XFDTD_DISPERSION_DEBYE = 3
+};
+
 typedef struct xfdtd_material_desc {
   float eps_r;       /* float, as in the reference's Material ctor       */
   float mu_r;
   double sigma_e;    /* S/m; a PEC is sigma_e = 1e10                     */
   double sigma_m;
+  int32_t dispersion;   /* XFDTD_DISPERSION_*                            */
+  int32_t reserved;
+  double p[4];          /* the dispersive medium's parameters (above)    */
 } xfdtd_material_desc;
 
 typedef struct xfdtd_object_desc {

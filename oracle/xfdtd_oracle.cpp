@@ -334,6 +334,19 @@ struct oracle_sim {
   size_t total = 0, cur = 0;
 
   A3 eps[3], mu[3], sig[3], sigm[3];
+  // Linear dispersive media (src/material/dispersive_material.cpp): the
+  // object index of each cell whose object is dispersive (-1 none), the
+  // media's recursion coefficients, and the per-component state: J, and for
+  // Lorentz media also the previous E and J (EMF::allocate*Prev, allocateJ*,
+  // simulation_init.cpp:49-59).
+  struct Disp {
+    int kind;
+    double ca, cb, cc, alpha, xi, gamma, kk, beta;
+  };
+  std::vector<Disp> disp;        // per object (kind 0: not dispersive)
+  std::vector<int32_t> disp_id;  // [nx][ny][nz]
+  bool has_disp = false;
+  A3 jx, jy, jz, jxp, jyp, jzp, exp_, eyp, ezp;
   A3 cexe, cexhy, cexhz, ceye, ceyhz, ceyhx, ceze, cezhx, cezhy;
   A3 chxh, chxey, chxez, chyh, chyez, chyex, chzh, chzex, chzey;
   A3 ex, ey, ez, hx, hy, hz;
@@ -398,6 +411,8 @@ struct oracle_sim {
   void initMonitor(Monitor &m);
   void step();
   void updateE();
+  void initDispersion();
+  void dispE(int comp, size_t i, size_t j, size_t k);
   void updateH();
   void pmlE(PML &p);
   void pmlH(PML &p);
@@ -475,7 +490,11 @@ void oracle_sim::init() {
   hy.init(nx, ny + 1, nz);
   hz.init(nx, ny, nz + 1);
 
+  for (auto &o : objects)
+    if (o.material.dispersion) has_disp = true;
+  if (has_disp) disp_id.assign(nx * ny * nz, -1);
   initObjects();
+  if (has_disp) initDispersion();
   if (has_tfsf) initTFSF();
   if (has_nffft) initNFFFT();
   for (auto &l : lumped) initLumpedElement(l);
@@ -515,6 +534,13 @@ void oracle_sim::initObjects() {
     double e = static_cast<double>(o.material.eps_r) * EPSILON_0;  // material.cpp:7-16
     double m = static_cast<double>(o.material.mu_r) * MU_0;
     double se = o.material.sigma_e, sm = o.material.sigma_m;
+    // a dispersive medium is a Material(name, 1, 1, sigma_e, sigma_m)
+    // (dispersive_material.h:21-24); its cells carry its object index
+    const int32_t did = o.material.dispersion ? static_cast<int32_t>(&o - objects.data()) : -1;
+    if (did >= 0) {
+      e = EPSILON_0;
+      m = MU_0;
+    }
 #pragma omp parallel for schedule(static)
     for (long long ii = 0; ii < static_cast<long long>(nx); ++ii) {
       size_t i = static_cast<size_t>(ii);
@@ -527,6 +553,7 @@ void oracle_sim::initObjects() {
           // cell centre at z = 0 (getGridCenterZ returns 0 there)
           q[2] = gs->dim == 2 ? 0.0 : gs->hc[2][k];
           if (!s.inside(q)) continue;
+          if (!disp_id.empty()) disp_id[(i * ny + j) * nz + k] = did;
           for (int a = 0; a < 3; ++a) {
             eps[a](i, j, k) = e; mu[a](i, j, k) = m;
             sig[a](i, j, k) = se; sigm[a](i, j, k) = sm;
@@ -546,6 +573,7 @@ void oracle_sim::initObjects() {
       for (size_t j = 0; j < ny; ++j)
         for (size_t k = 0; k < nz; ++k) {
           const xfdtd_material_desc &md = voxel_mats[voxel_idx[(i * ny + j) * nz + k]];
+          if (!disp_id.empty()) disp_id[(i * ny + j) * nz + k] = -1;   // voxel materials are plain
           double e = static_cast<double>(md.eps_r) * EPSILON_0;
           double m = static_cast<double>(md.mu_r) * MU_0;
           for (int a = 0; a < 3; ++a) {
@@ -967,7 +995,134 @@ void oracle_sim::initMonitor(Monitor &m) {
 }
 
 // ------------------------------------------------------------ time loop ---
+// The linear dispersive media (src/material/dispersive_material.cpp):
+// recursion coefficients from LorentzMedium::init (:17-36), DrudeMedium::init
+// (:126-142) and DebyMedium::init (:195-210); dl is the uniform cell size
+// (LinearDispersiveMaterial::init, dispersive_material.h:30-43).
+void oracle_sim::initDispersion() {
+  const double dl = gs->base[0];
+  if (gs->base[1] != dl || gs->base[2] != dl) throw std::runtime_error("The condition (dx == dy == dz) is required");
+  disp.assign(objects.size(), Disp{});
+  for (size_t q = 0; q < objects.size(); ++q) {
+    const xfdtd_material_desc &m = objects[q].material;
+    Disp &d = disp[q];
+    d.kind = m.dispersion;
+    const double eps_0 = EPSILON_0, sigma_e = m.sigma_e;
+    if (m.dispersion == XFDTD_DISPERSION_LORENTZ) {
+      const double eps_s = m.p[0], eps_inf = m.p[1], omega_p = m.p[2], nv = m.p[3];
+      const double delta_eps = eps_s - eps_inf;
+      const double temp_coff_0 = nv * dt + 1;
+      d.alpha = (2 - omega_p * omega_p * dt * dt) / temp_coff_0;
+      d.xi = (nv * dt - 1) / temp_coff_0;
+      d.gamma = (eps_0 * delta_eps * omega_p * omega_p * dt * dt) / temp_coff_0;
+      const double temp_coff_1 = 4 * eps_0 * eps_inf + d.gamma + 2 * sigma_e * dt;
+      d.ca = (4 * eps_0 * eps_inf - 2 * sigma_e * dt) / (temp_coff_1);
+      d.cb = (d.gamma) / (temp_coff_1);
+      d.cc = (4 * dt) / (temp_coff_1 * dl);
+    } else if (m.dispersion == XFDTD_DISPERSION_DRUDE) {
+      const double eps_inf = m.p[0], omega_p = m.p[1], nv = m.p[2];
+      d.kk = (2 - nv * dt) / (2 + nv * dt);
+      d.beta = (omega_p * omega_p * eps_0 * dt) / (2 + nv * dt);
+      const double temp_coff_1 = 2 * eps_0 * eps_inf + d.beta * dt + sigma_e * dt;
+      d.ca = (2 * eps_0 * eps_inf - d.beta * dt - sigma_e * dt) / (temp_coff_1);
+      d.cb = 2 * dt / (temp_coff_1 * dl);
+    } else if (m.dispersion == XFDTD_DISPERSION_DEBYE) {
+      const double eps_s = m.p[0], eps_inf = m.p[1], tau = m.p[2];
+      const double delta_eps = eps_s - eps_inf;
+      d.kk = (2 * tau - dt) / (2 * tau + dt);
+      d.beta = (2 * delta_eps * eps_0 * dt) / (2 * tau + dt);
+      const double temp_coff_1 = 2 * eps_0 * eps_inf + d.beta + sigma_e * dt;
+      d.ca = (2 * eps_0 * eps_inf + d.beta - sigma_e * dt) / (temp_coff_1);
+      d.cb = (2 * dt) / ((temp_coff_1)*dl);
+    } else if (m.dispersion != XFDTD_DISPERSION_NONE) {
+      throw std::runtime_error("unknown dispersive medium");
+    }
+  }
+  jx.init(nx, ny + 1, nz + 1); jy.init(nx + 1, ny, nz + 1); jz.init(nx + 1, ny + 1, nz);
+  jxp.init(nx, ny + 1, nz + 1); jyp.init(nx + 1, ny, nz + 1); jzp.init(nx + 1, ny + 1, nz);
+  exp_.init(nx, ny + 1, nz + 1); eyp.init(nx + 1, ny, nz + 1); ezp.init(nx + 1, ny + 1, nz);
+}
+
+// LorentzMedium / DrudeMedium / DebyMedium::updateE{x,y,z} at (i, j, k),
+// dispersive_material.cpp:38-113, 144-196, 212-275 (the curl terms in
+// their order: the component's first minus its second H difference).
+void oracle_sim::dispE(int comp, size_t i, size_t j, size_t k) {
+  const Disp &d = disp[disp_id[(i * ny + j) * nz + k]];
+  const double dl = gs->base[0];
+  A3 &e = comp == 0 ? ex : (comp == 1 ? ey : ez);
+  A3 &jj = comp == 0 ? jx : (comp == 1 ? jy : jz);
+  A3 &jp = comp == 0 ? jxp : (comp == 1 ? jyp : jzp);
+  A3 &ep = comp == 0 ? exp_ : (comp == 1 ? eyp : ezp);
+  double curl;
+  if (comp == 0) curl = -(hy(i, j, k) - hy(i, j, k - 1)) + (hz(i, j, k) - hz(i, j - 1, k));
+  else if (comp == 1) curl = -(hz(i, j, k) - hz(i - 1, j, k)) + (hx(i, j, k) - hx(i, j, k - 1));
+  else curl = -(hx(i, j, k) - hx(i, j - 1, k)) + (hy(i, j, k) - hy(i - 1, j, k));
+  double &E = e(i, j, k);
+  double &J = jj(i, j, k);
+  const double e_old = E;
+  if (d.kind == XFDTD_DISPERSION_LORENTZ) {
+    double &Jp = jp(i, j, k);
+    double &Ep = ep(i, j, k);
+    const double j_old = J;
+    double j_sum = 0;
+    j_sum += 0.5 * dl * ((1 + d.alpha) * J + d.xi * Jp);
+    E = d.ca * E + d.cb * Ep + d.cc * (curl - j_sum);
+    J = d.alpha * J + d.xi * Jp + d.gamma * (E - Ep) / (2 * dt);
+    Ep = e_old;
+    Jp = j_old;
+  } else {
+    double j_sum = 0;
+    j_sum += 0.5 * dl * ((1 + d.kk) * J);
+    E = d.ca * E + d.cb * (curl - j_sum);
+    if (d.kind == XFDTD_DISPERSION_DRUDE) J = d.kk * J + d.beta * (E + e_old);
+    else J = d.kk * J + d.beta * (E - e_old) / dt;
+  }
+}
+
 void oracle_sim::updateE() {  // Simulation::updateE, simulation_update.cpp:170-196
+  if (has_disp) {   // Simulation::updateEWithDispersiveMaterial, simulation_update.cpp:221-280
+    auto dispersive = [&](size_t i, size_t j, size_t k) { return disp_id[(i * ny + j) * nz + k] >= 0; };
+#pragma omp parallel for schedule(static)
+    for (long long ii = 0; ii < static_cast<long long>(nx); ++ii) {
+      size_t i = static_cast<size_t>(ii);
+      for (size_t j = 1; j < ny; ++j)
+        for (size_t k = 1; k < nz; ++k) {
+          if (dispersive(i, j, k)) {
+            dispE(0, i, j, k);
+            continue;
+          }
+          ex(i, j, k) = cexe(i, j, k) * ex(i, j, k) + cexhy(i, j, k) * (hy(i, j, k) - hy(i, j, k - 1)) +
+                        cexhz(i, j, k) * (hz(i, j, k) - hz(i, j - 1, k));
+        }
+    }
+#pragma omp parallel for schedule(static)
+    for (long long jj = 0; jj < static_cast<long long>(ny); ++jj) {
+      size_t j = static_cast<size_t>(jj);
+      for (size_t k = 1; k < nz; ++k)
+        for (size_t i = 1; i < nx; ++i) {
+          if (dispersive(i, j, k)) {
+            dispE(1, i, j, k);
+            continue;
+          }
+          ey(i, j, k) = ceye(i, j, k) * ey(i, j, k) + ceyhx(i, j, k) * (hx(i, j, k) - hx(i, j, k - 1)) +
+                        ceyhz(i, j, k) * (hz(i, j, k) - hz(i - 1, j, k));
+        }
+    }
+#pragma omp parallel for schedule(static)
+    for (long long kk = 0; kk < static_cast<long long>(nz); ++kk) {
+      size_t k = static_cast<size_t>(kk);
+      for (size_t i = 1; i < nx; ++i)
+        for (size_t j = 1; j < ny; ++j) {
+          if (dispersive(i, j, k)) {
+            dispE(2, i, j, k);
+            continue;
+          }
+          ez(i, j, k) = ceze(i, j, k) * ez(i, j, k) + cezhx(i, j, k) * (hx(i, j, k) - hx(i, j - 1, k)) +
+                        cezhy(i, j, k) * (hy(i, j, k) - hy(i - 1, j, k));
+        }
+    }
+    return;
+  }
 #pragma omp parallel for schedule(static)
   for (long long ii = 0; ii < static_cast<long long>(nx); ++ii) {
     size_t i = static_cast<size_t>(ii);

@@ -221,6 +221,25 @@ def rel_err(a, b):
     return float(np.abs(a - b).max() / scale)
 
 
+def dispersive(kind="drude", steps=200, limit=False):
+    """The dielectric-sphere scene at 1/8 scale with a dispersive sphere:
+    Lorentz (eps_s 4, eps_inf 2, pole at 3e10 rad/s, damping 1e9 1/s),
+    Drude (eps_inf 1.5, plasma 5e10 rad/s, collisions 2e9 1/s) or Debye
+    (eps_s 6, eps_inf 2.5, tau 20 ps), with sigma_e 0.01 S/m.  limit=True
+    takes each medium's parameters to the plain dielectric eps_r = 2.5
+    (no pole, no plasma, eps_s = eps_inf), which the E recursion must then
+    reproduce."""
+    sc, st = dielectric(steps=steps)
+    if kind == "lorentz":
+        m = S.LorentzMedium("l", 2.5 if limit else 4.0, 2.5 if limit else 2.0, 0.0 if limit else 3e10, 1e9, 0.01)
+    elif kind == "drude":
+        m = S.DrudeMedium("d", 2.5 if limit else 1.5, 0.0 if limit else 5e10, 2e9, 0.01)
+    else:
+        m = S.DebyMedium("b", 2.5 if limit else 6.0, 2.5, 20e-12, 0.01)
+    sc.objects[1] = S.Object(sc.objects[1].name, sc.objects[1].shape, m)
+    return sc, st
+
+
 def cylinder_2d(steps=300):
     """The 2-D (nz = 1) TMz cylinder scatter of the reference's example at a
     fifth of its size: 70 x 60 cells + 10-cell CPML on x and y, PEC

@@ -73,6 +73,30 @@ def test_2d_grid_time_step_and_tfsf2d_cancellation():
         assert not np.any(o.read_field(c)), c
 
 
+@pytest.mark.parametrize("kind", ["lorentz", "drude", "debye"])
+def test_dispersive_media_reduce_to_the_plain_dielectric(kind):
+    """The linear dispersive media's E recursions
+    (src/material/dispersive_material.cpp) with no pole (Lorentz omega_p =
+    0, Drude omega_p = 0, Debye eps_s = eps_inf) give the fields of a plain
+    sphere of eps_r = eps_inf (to rounding: the recursions group the terms
+    otherwise); with a pole they differ from it."""
+    sc, st = scenes.dispersive(kind, steps=120, limit=True)
+    o = O.OracleSim(sc, st)
+    o.step(st)
+    sc_p, _ = scenes.dispersive(kind, steps=120, limit=True)
+    sc_p.objects[1] = S.Object("p", sc_p.objects[1].shape, S.Material("p", 2.5, 1, 0.01, 0))
+    p = O.OracleSim(sc_p, st)
+    p.step(st)
+    scale = max(np.abs(p.read_field(c)).max() for c in range(3))
+    for c in range(6):
+        assert np.abs(o.read_field(c) - p.read_field(c)).max() <= 1e-12 * scale, c
+    sc_d, _ = scenes.dispersive(kind, steps=120)
+    d = O.OracleSim(sc_d, st)
+    d.step(st)
+    assert np.abs(d.read_field(S.EX) - p.read_field(S.EX)).max() > 1e-3 * scale
+    assert all(np.isfinite(d.read_field(c)).all() for c in range(6))
+
+
 def test_tfsf_normal_incidence_cancels_outside_box():
     sc, _ = configs.pec_sphere_rcs(scale=2, steps=260)
     sc.objects = sc.objects[:1]

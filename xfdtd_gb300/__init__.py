@@ -19,7 +19,7 @@ from . import scene
 from .scene import (  # noqa: F401  (re-exported: the reference's scene API)
     AXIS_X, AXIS_Y, AXIS_Z, EX, EY, EZ, HX, HY, HZ, XN, XP, YN, YP, ZN, ZP,
     Capacitor, CosineModulatedGaussianWaveform, CurrentMonitor, CurrentSource, Cube,
-    CustomWaveform, Cylinder, GaussianWaveform, Inductor, Material, NffftFd, Object, PML,
+    CustomWaveform, Cylinder, DebyMedium, DrudeMedium, GaussianWaveform, Inductor, LorentzMedium, Material, NffftFd, Object, PML,
     Resistor, Scene, SinusoidalWaveform, Sphere, TFSF2D, TFSF3D, ThinWire, VoltageMonitor,
     VoltageSource,
 )
@@ -309,11 +309,11 @@ class Simulation:
 
     def profile(self) -> dict:
         """Per-kernel device time (ms) and launches recorded under profile=True."""
-        names = (C.c_char_p * 16)()
-        ms = (C.c_double * 16)()
-        cnt = (C.c_int64 * 16)()
+        names = (C.c_char_p * 32)()
+        ms = (C.c_double * 32)()
+        cnt = (C.c_int64 * 32)()
         n = C.c_int()
-        self._check_engine(libs()[0].xfdtd_profile(self.engine, 16, names, ms, cnt, C.byref(n)))
+        self._check_engine(libs()[0].xfdtd_profile(self.engine, 32, names, ms, cnt, C.byref(n)))
         return {names[i].decode(): (ms[i], int(cnt[i])) for i in range(n.value)}
 
     def profile_reset(self):

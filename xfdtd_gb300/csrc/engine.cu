@@ -72,8 +72,9 @@ struct Err {
 const char *kKernelNames[] = {"tfsf_aux",         "update_e",       "lumped_e",         "update_h",
                               "nffft",            "probes",         "advance",          "tfsf_e",
                               "tfsf_h",           "nffft_acc",      "sweep_eh",         "update_e_shell",
-                              "update_h_shell",   "update_e_interior", "update_h_interior", "snapshots"};
-constexpr int kNumKernels = 16;
+                              "update_h_shell",   "update_e_interior", "update_h_interior", "snapshots",
+                              "dispersive_e"};
+constexpr int kNumKernels = 17;
 
 }  // namespace
 
@@ -152,6 +153,13 @@ struct xfdtd_handle {
 
   // sparse
   int n_inj = 0, n_ind = 0, n_probes = 0, n_waveforms = 0;
+  // linear dispersive media: the listed E components, their media (in the
+  // field precision) and their recursion state J, previous J, previous E
+  int n_disp = 0;
+  xg::DispCell *disp_cells = nullptr;
+  void *disp_media = nullptr;
+  void *disp_j = nullptr, *disp_jp = nullptr, *disp_ep = nullptr;
+  double disp_dl = 0;
   xfdtd_injection *inj = nullptr;
   xfdtd_inductor_cell *ind = nullptr;
   double *ind_j = nullptr;
@@ -1131,8 +1139,13 @@ void autotune_t(xfdtd_handle *h, int trials) {
           break;
         }
     }
+    // Each candidate is timed with this side's TFSF corrections: inside the
+    // wide decomposition's TMA launches where it can take them, else as
+    // their own launch after the pair, so that the forms compare on the same
+    // work.
     best = 1e30f;
     int best_sv = shell_best[kVariants[best_v].wide ? 1 : 0];
+    bool best_fold = false;
     for (int q = 0; q < 3 && top[q] >= 0; ++q) {
       const int v = top[q];
       var = v;
@@ -1141,28 +1154,24 @@ void autotune_t(xfdtd_handle *h, int trials) {
         if (!shell_allowed(h, kShellVariants[sv], wide)) continue;
         if (!side_shell_cells(h, side, wide) && sv != shell_best[wide ? 1 : 0]) continue;
         h->shell_var[side] = sv;
-        const float ms = time_n([&] { volume_pair<T, I>(h, side == 0); }, 3 * trials);
-        if (ms < best) best = ms, best_v = v, best_sv = sv;
+        for (int fold = 0; fold < 2; ++fold) {
+          h->tf_fuse_on[side] = fold != 0;
+          if (fold && !tfsf_fused(h, side)) continue;
+          const bool apart = h->tfsf && !tfsf_fused(h, side);
+          const float ms = time_n([&] {
+            volume_pair<T, I>(h, side == 0);
+            if (apart) launch_tfsf_side<T>(h, side == 0);
+          }, 3 * trials);
+          if (fold) h->tf_fuse_ms[side][0] = ms;
+          else if (h->tf_fuse_ok[side] && wide) h->tf_fuse_ms[side][1] = ms;
+          if (ms < best) best = ms, best_v = v, best_sv = sv, best_fold = fold != 0;
+        }
       }
     }
     var = best_v;
     h->shell_var[side] = best_sv;
+    h->tf_fuse_on[side] = best_fold;
     h->tune_ms[side][best_v] = best;
-    // the TFSF corrections inside the wide decomposition's launches, or as
-    // their own launch after the pair: whichever is faster
-    if (h->tf_fuse_ok[side] && kVariants[best_v].wide &&
-        (side_shell_cells(h, side, true) == 0 || kShellVariants[best_sv].stages != 0)) {
-      h->tf_fuse_on[side] = true;
-      const float fused = time_n([&] { volume_pair<T, I>(h, side == 0); }, 3 * trials);
-      h->tf_fuse_on[side] = false;
-      const float apart = time_n([&] {
-        volume_pair<T, I>(h, side == 0);
-        launch_tfsf_side<T>(h, side == 0);
-      }, 3 * trials);
-      h->tf_fuse_on[side] = fused <= apart;
-      h->tf_fuse_ms[side][0] = fused;
-      h->tf_fuse_ms[side][1] = apart;
-    }
     best_split += best;
   }
   h->sweep = was_sweep;
@@ -1410,6 +1419,26 @@ void enqueue_step_t(xfdtd_handle *h, long long s, bool pre) {
     swap_state(h);
   } else {
     volume_pair<T, I>(h, true);
+    if (h->n_disp) {
+      xg::DispParams<T> dp{};
+      dp.d = h->d;
+      for (int c = 0; c < 3; ++c) {
+        dp.E[c] = static_cast<T *>(h->F[c]);
+        dp.H[c] = static_cast<const T *>(h->F[3 + c]);
+      }
+      dp.cells = h->disp_cells;
+      dp.media = static_cast<const xg::DispMedium<T> *>(h->disp_media);
+      dp.j = static_cast<T *>(h->disp_j);
+      dp.jp = static_cast<T *>(h->disp_jp);
+      dp.ep = static_cast<T *>(h->disp_ep);
+      dp.n = h->n_disp;
+      dp.dl = static_cast<T>(h->disp_dl);
+      dp.dt = static_cast<T>(h->dt);
+      prof_begin(h, 16);
+      xg::k_dispersive_e<T><<<(h->n_disp + 255) / 256, 256, 0, h->stream>>>(dp);
+      XCHECK(cudaGetLastError());
+      prof_end(h);
+    }
     if (h->n_inj || h->n_ind) {
       auto sp = sparse_params<T>(h);
       int n = std::max(h->n_inj, h->n_ind);
@@ -1532,7 +1561,8 @@ int launches_per_step(const xfdtd_handle *h) {
     vol += (side_interior_cells(h, side, w) ? 1 : 0) + (side_shell_cells(h, side, w) ? 1 : 0);
   }
   const int tf = h->tfsf ? 3 - (tfsf_fused(h, 0) ? 1 : 0) - (tfsf_fused(h, 1) ? 1 : 0) : 0;
-  return tf + vol + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->nffft ? 1 : 0) + (h->n_probes ? 1 : 0) + snap + 1;
+  return tf + vol + ((h->n_inj || h->n_ind) ? 1 : 0) + (h->n_disp ? 1 : 0) + (h->nffft ? 1 : 0) +
+         (h->n_probes ? 1 : 0) + snap + 1;
 }
 
 // Captures g steps starting at a step index that is a multiple of the NF-FF
@@ -1600,6 +1630,9 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   h->total = pl->total_steps;
   h->dt = pl->dt;
   for (int a = 0; a < 3; ++a) h->dl[a] = pl->dl[a];
+  if (pl->n_disp_cells < 0 || pl->n_disp_media < 0 || (pl->n_disp_cells && (!pl->disp_cells || !pl->disp_media)))
+    invalid("dispersive cells and media are required together");
+  h->n_disp = pl->n_disp_cells;
   xg::Dims &d = h->d;
   d.nx = pl->nx;
   d.ny = pl->ny;
@@ -1618,7 +1651,11 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   XCHECK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
   XCHECK(cudaEventCreateWithFlags(&h->ev_nf_fork, cudaEventDisableTiming));
   XCHECK(cudaEventCreateWithFlags(&h->ev_nf_join, cudaEventDisableTiming));
-  XCHECK(cudaStreamCreateWithFlags(&h->nfs, cudaStreamNonBlocking));
+  {   // the NF-FF halves are small: scheduled ahead of the volume launches they run beside
+    int lo_prio = 0, hi_prio = 0;
+    XCHECK(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+    XCHECK(cudaStreamCreateWithPriority(&h->nfs, cudaStreamNonBlocking, hi_prio));
+  }
   XCHECK(cudaEventCreateWithFlags(&h->ev_nfs_fork, cudaEventDisableTiming));
   XCHECK(cudaEventCreateWithFlags(&h->ev_nfh, cudaEventDisableTiming));
   XCHECK(cudaEventCreateWithFlags(&h->ev_nfe, cudaEventDisableTiming));
@@ -1706,7 +1743,7 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     // the fused sweep, unless the plan asks for the split kernels or has
     // lumped elements (whose E corrections run between the E and H updates)
     h->sweep_ok = !(pl->flags & XFDTD_FLAG_SPLIT_EH) && pl->n_injections == 0 && pl->n_inductor_cells == 0 &&
-                  pl->index_bytes < 4 && pl->nz > 1;
+                  pl->index_bytes < 4 && pl->nz > 1 && pl->n_disp_cells == 0;
     h->sweep = h->sweep_ok && (pl->flags & XFDTD_FLAG_FUSED_EH);
     if (h->sweep_ok) {
       for (int c = 0; c < 6; ++c) h->F2[c] = h->alloc_bytes(d.cells * h->esize);
@@ -1852,6 +1889,38 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
     }
     h->inj = h->upload<xfdtd_injection>(pl->injections, pl->n_injections);
   }
+  if (h->n_disp) {   // dispersive media (xfdtd_dispersive_medium / _cell)
+    if (!(pl->disp_dl > 0)) invalid("dispersive media need the cell size");
+    std::vector<xg::DispCell> cells(static_cast<size_t>(h->n_disp));
+    for (int q = 0; q < h->n_disp; ++q) {
+      const auto &c = pl->disp_cells[q];
+      if (c.comp < 0 || c.comp > 2) invalid("dispersive cells are E components");
+      check_cell(c.comp, c.i, c.j, c.k);
+      if (c.i < 1 && c.comp != 0) invalid("dispersive cell on an outer wall");
+      if (c.j < 1 && c.comp != 1) invalid("dispersive cell on an outer wall");
+      if (c.k < 1 && c.comp != 2) invalid("dispersive cell on an outer wall");
+      if (c.medium < 0 || c.medium >= pl->n_disp_media) invalid("dispersive medium index out of range");
+      if (pl->disp_media[c.medium].kind < 1 || pl->disp_media[c.medium].kind > 3) invalid("unknown dispersive medium");
+      cells[q] = xg::DispCell{c.i * h->d.si + c.j * h->d.sj + c.k, c.comp, c.medium};
+    }
+    h->disp_cells = h->upload<xg::DispCell>(cells.data(), cells.size());
+    h->disp_dl = pl->disp_dl;
+    auto media = [&](auto zero) {
+      using R = decltype(zero);
+      std::vector<xg::DispMedium<R>> m(static_cast<size_t>(pl->n_disp_media));
+      for (int q = 0; q < pl->n_disp_media; ++q) {
+        const auto &s0 = pl->disp_media[q];
+        m[q] = xg::DispMedium<R>{s0.kind, R(s0.ca), R(s0.cb), R(s0.cc), R(s0.alpha), R(s0.xi), R(s0.gamma), R(s0.k),
+                                 R(s0.beta)};
+      }
+      h->disp_media = h->upload<xg::DispMedium<R>>(m.data(), m.size());
+    };
+    if (h->precision == XFDTD_FP64) media(0.0);
+    else media(0.0f);
+    h->disp_j = h->alloc_bytes(static_cast<size_t>(h->n_disp) * h->esize);
+    h->disp_jp = h->alloc_bytes(static_cast<size_t>(h->n_disp) * h->esize);
+    h->disp_ep = h->alloc_bytes(static_cast<size_t>(h->n_disp) * h->esize);
+  }
   h->n_ind = pl->n_inductor_cells;
   if (pl->n_inductor_cells) {
     for (int q = 0; q < pl->n_inductor_cells; ++q) {
@@ -1942,7 +2011,7 @@ void create(const xfdtd_plan_desc *pl, xfdtd_handle *h) {
   }
   // the TFSF corrections inside the wide decomposition's TMA launches (they
   // cover every cell): 3-D plane wave, no lumped element
-  if (h->tfsf && !h->tf_two_d && h->n_inj == 0 && h->n_ind == 0)
+  if (h->tfsf && !h->tf_two_d && h->n_inj == 0 && h->n_ind == 0 && h->n_disp == 0)
     for (int side = 0; side < 2; ++side) h->tf_fuse_ok[side] = h->wide_ok[side];
   XCHECK(cudaStreamSynchronize(h->stream));
   h->create_ms[0] = ms_since(t_begin);
@@ -2947,6 +3016,7 @@ int xfdtd_batch_create(xfdtd_handle *const *members, int n, int flags, xfdtd_bat
           invalid("batch members may not have lumped elements or monitors");
         if (h->nf_bb) invalid("batch members may not have a broadband NF-FF");
         if (h->d.nz < 2) invalid("batch members must be 3-D grids");
+        if (h->n_disp) invalid("batch members may not have dispersive media");
         if (h->d.nx >= 65535 || h->d.ny >= 2040 || h->d.nz >= 8160) invalid("batch member grid too large for the tile numbering");
         for (int r = 0; r < q; ++r)
           if (members[r] == h) invalid("a handle appears twice in the batch");
@@ -3151,6 +3221,7 @@ void adj_record_plane(xfdtd_handle *h, AdjointState *a, long long w) {
 void adj_validate(xfdtd_handle *h, const xfdtd_adjoint_desc *d) {
   if (h->host_step != 0) throw Err{XFDTD_ERR_STATE, "the adjoint forward pass starts at step 0"};
   if (h->n_ind) invalid("the adjoint does not cover inductors (their current is extra state)");
+  if (h->n_disp) invalid("the adjoint does not cover dispersive media (their currents are extra state)");
   const int n[3] = {h->d.nx, h->d.ny, h->d.nz};
   for (int a = 0; a < 3; ++a) {
     if (d->design_lo[a] < 1 || d->design_hi[a] <= d->design_lo[a] || d->design_hi[a] > n[a] - 1)

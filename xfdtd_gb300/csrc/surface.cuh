@@ -692,6 +692,68 @@ __device__ __forceinline__ long long sp_index(const Dims &d, long long i, long l
   return i * d.si + j * d.sj + k;
 }
 
+// ------------------------------------------------------------------------
+// Linear dispersive media: the E components of their cells, whose volume
+// update left E as it was (identity table entry), get the medium's
+// recursion -- LorentzMedium / DrudeMedium / DebyMedium::updateE{x,y,z},
+// src/material/dispersive_material.cpp:38-113, 144-196, 212-275 -- in the
+// field precision, with the terms in the reference's order.  State per
+// listed component: J, and for Lorentz media the previous E and J.
+template <typename T>
+struct DispMedium {
+  int kind;
+  T ca, cb, cc, alpha, xi, gamma, k, beta;
+};
+struct DispCell {
+  long long b;   // padded index of (i, j, k)
+  int comp, medium;
+};
+template <typename T>
+struct DispParams {
+  Dims d;
+  T *E[3];
+  const T *H[3];
+  const DispCell *cells;
+  const DispMedium<T> *media;
+  T *j, *jp, *ep;   // [n]
+  int n;
+  T dl, dt;
+};
+
+template <typename T>
+__global__ void k_dispersive_e(DispParams<T> p) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= p.n) return;
+  const DispCell c = p.cells[q];
+  const DispMedium<T> m = p.media[c.medium];
+  const long long b = c.b, sj = p.d.sj, si = p.d.si;
+  const T *hx = p.H[0], *hy = p.H[1], *hz = p.H[2];
+  T curl;
+  if (c.comp == 0) curl = -(hy[b] - hy[b - 1]) + (hz[b] - hz[b - sj]);
+  else if (c.comp == 1) curl = -(hz[b] - hz[b - si]) + (hx[b] - hx[b - 1]);
+  else curl = -(hx[b] - hx[b - sj]) + (hy[b] - hy[b - si]);
+  T *E = p.E[c.comp] + b;
+  const T e_old = *E;
+  T J = p.j[q];
+  const T half = T(0.5), one = T(1), two = T(2);
+  if (m.kind == 1) {   // Lorentz
+    const T Jp = p.jp[q], Ep = p.ep[q];
+    T j_sum = T(0);
+    j_sum += half * p.dl * ((one + m.alpha) * J + m.xi * Jp);
+    const T e = m.ca * e_old + m.cb * Ep + m.cc * (curl - j_sum);
+    *E = e;
+    p.j[q] = m.alpha * J + m.xi * Jp + m.gamma * (e - Ep) / (two * p.dt);
+    p.ep[q] = e_old;
+    p.jp[q] = J;
+  } else {   // Drude (2), Debye (3)
+    T j_sum = T(0);
+    j_sum += half * p.dl * ((one + m.k) * J);
+    const T e = m.ca * e_old + m.cb * (curl - j_sum);
+    *E = e;
+    p.j[q] = m.kind == 2 ? m.k * J + m.beta * (e + e_old) : m.k * J + m.beta * (e - e_old) / p.dt;
+  }
+}
+
 // CurrentSource / VoltageSource ::correctE and Inductor::correctE, in list order.
 template <typename T>
 __global__ void k_lumped_e(SparseParams<T> p) {

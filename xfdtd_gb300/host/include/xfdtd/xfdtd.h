@@ -159,12 +159,60 @@ class Material {
   float getEpsR() const { return _eps_r; }
   float getMuR() const { return _mu_r; }
   const std::string &getName() const { return _name; }
+  // A linear dispersive medium's kind (0 none, 1 Lorentz, 2 Drude, 3 Debye)
+  // and parameters, kept in the base so that an Object's copy keeps them.
+  int dispersionKind() const { return _disp_kind; }
+  const std::array<double, 4> &dispersionParams() const { return _disp_p; }
+
+ protected:
+  void setDispersion(int kind, std::array<double, 4> p) {
+    _disp_kind = kind;
+    _disp_p = p;
+  }
 
  private:
   std::string _name;
   float _eps_r, _mu_r;
   double _eps, _mu, _sigma_e, _sigma_m;
   bool _is_dispersion;
+  int _disp_kind = 0;
+  std::array<double, 4> _disp_p{0, 0, 0, 0};
+};
+
+// Linear dispersive media (src/include/material/dispersive_material.h):
+// eps_r = mu_r = 1, the frequency dependence in an E recursion per medium
+// (src/material/dispersive_material.cpp).  Uniform grids with dx = dy = dz
+// only, and outside the CPML.  The reference throws on them at
+// Object::init (object.cpp:109-110); the GPU engine runs them.
+class LinearDispersiveMaterial : public Material {
+ public:
+  explicit LinearDispersiveMaterial(std::string_view name, float eps_r = 1, float mu_r = 1, double sigma_e = 0,
+                                    double sigma_m = 0)
+      : Material(name, eps_r, mu_r, sigma_e, sigma_m, true) {}
+};
+class LorentzMedium : public LinearDispersiveMaterial {
+ public:
+  LorentzMedium(std::string_view name, double eps_s, double eps_inf, double omega_p, double nv, double sigma_e = 0,
+                double sigma_m = 0)
+      : LinearDispersiveMaterial(name, 1, 1, sigma_e, sigma_m) {
+    setDispersion(1, {eps_s, eps_inf, omega_p, nv});
+  }
+};
+class DrudeMedium : public LinearDispersiveMaterial {
+ public:
+  DrudeMedium(std::string_view name, double eps_inf, double pole_omega, double nv, double sigma_e = 0,
+              double sigma_m = 0)
+      : LinearDispersiveMaterial(name, 1, 1, sigma_e, sigma_m) {
+    setDispersion(2, {eps_inf, pole_omega, nv, 0});
+  }
+};
+class DebyMedium : public LinearDispersiveMaterial {
+ public:
+  DebyMedium(std::string_view name, double eps_s, double eps_inf, double tau, double sigma_e = 0,
+             double sigma_m = 0)
+      : LinearDispersiveMaterial(name, 1, 1, sigma_e, sigma_m) {
+    setDispersion(3, {eps_s, eps_inf, tau, 0});
+  }
 };
 
 // ----------------------------------------------------------------- object

@@ -19,6 +19,22 @@ namespace {
 
 using namespace xfdtd;
 
+// A Material of the description, or the dispersive medium it names.
+std::unique_ptr<Material> makeMaterial(const xfdtd_material_desc &m) {
+  switch (m.dispersion) {
+    case XFDTD_DISPERSION_NONE:
+      return std::make_unique<Material>("material", m.eps_r, m.mu_r, m.sigma_e, m.sigma_m);
+    case XFDTD_DISPERSION_LORENTZ:
+      return std::make_unique<LorentzMedium>("lorentz", m.p[0], m.p[1], m.p[2], m.p[3], m.sigma_e, m.sigma_m);
+    case XFDTD_DISPERSION_DRUDE:
+      return std::make_unique<DrudeMedium>("drude", m.p[0], m.p[1], m.p[2], m.sigma_e, m.sigma_m);
+    case XFDTD_DISPERSION_DEBYE:
+      return std::make_unique<DebyMedium>("debye", m.p[0], m.p[1], m.p[2], m.sigma_e, m.sigma_m);
+    default:
+      throw std::invalid_argument("unknown dispersive medium kind");
+  }
+}
+
 PointVector pv(const double *p) { return PointVector{p[0], p[1], p[2]}; }
 
 std::unique_ptr<Shape> makeShape(const xfdtd_shape_desc &d) {
@@ -85,9 +101,7 @@ int xfdtd_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, int precis
         auto cy = std::make_unique<Cylinder>(axis(o.shape.axis), pv(o.shape.point), o.shape.radius, o.shape.height);
         sim->addObject(std::make_shared<ThinWire>("thin_wire", std::move(cy)));
       } else {
-        sim->addObject(std::make_shared<Object>(
-            "object", makeShape(o.shape),
-            Material("material", o.material.eps_r, o.material.mu_r, o.material.sigma_e, o.material.sigma_m)));
+        sim->addObject(std::make_shared<Object>("object", makeShape(o.shape), makeMaterial(o.material)));
       }
     }
     for (int i = 0; i < sc->n_pml; ++i) {
@@ -195,6 +209,7 @@ int xfdtd_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, int precis
       std::vector<Material> mats;
       for (int q = 0; q < sc->n_voxel_materials; ++q) {
         const auto &m = sc->voxel_materials[q];
+        if (m.dispersion) throw std::invalid_argument("voxel materials are plain materials (no dispersive media)");
         mats.emplace_back("voxel", m.eps_r, m.mu_r, m.sigma_e, m.sigma_m);
       }
       const size_t cnt = static_cast<size_t>(sc->voxel_shape[0] * sc->voxel_shape[1] * sc->voxel_shape[2]);

@@ -180,8 +180,9 @@ using Tuple = std::array<double, XFDTD_N_COEFF>;
 
 struct Props {
   double eps, mu, se, sm;
+  bool disp = false;   // a dispersive medium's cell: its E comes from the medium's recursion
   bool operator<(const Props &o) const {
-    return std::tie(eps, mu, se, sm) < std::tie(o.eps, o.mu, o.se, o.sm);
+    return std::tie(eps, mu, se, sm, disp) < std::tie(o.eps, o.mu, o.se, o.sm, o.disp);
   }
 };
 
@@ -205,7 +206,49 @@ Tuple coefficients(const Props &p, double dt, const double d[3]) {
   h(d[1], d[2], c[9], c[10], c[11]);   // Hx: da = dy, db = dz
   h(d[2], d[0], c[12], c[13], c[14]);  // Hy: da = dz, db = dx
   h(d[0], d[1], c[15], c[16], c[17]);  // Hz: da = dx, db = dy
+  if (p.disp)   // the volume update leaves E of a dispersive cell as it is
+    for (int q = 0; q < 9; ++q) c[q] = q % 3 == 0 ? 1.0 : 0.0;
   return c;
+}
+
+// The E recursion coefficients of a linear dispersive medium, as
+// LorentzMedium::init (dispersive_material.cpp:17-36), DrudeMedium::init
+// (:126-142) and DebyMedium::init (:195-210) compute them.
+xfdtd_dispersive_medium dispersiveMedium(const Material &m, double dt, double dl) {
+  xfdtd_dispersive_medium d{};
+  d.kind = m.dispersionKind();
+  const auto &p = m.dispersionParams();
+  const double eps_0 = constant::EPSILON_0, sigma_e = m.getElectricalConductivity();
+  if (d.kind == 1) {
+    const double eps_s = p[0], eps_inf = p[1], omega_p = p[2], nv = p[3];
+    const double delta_eps = eps_s - eps_inf;
+    const double temp_coff_0 = nv * dt + 1;
+    d.alpha = (2 - omega_p * omega_p * dt * dt) / temp_coff_0;
+    d.xi = (nv * dt - 1) / temp_coff_0;
+    d.gamma = (eps_0 * delta_eps * omega_p * omega_p * dt * dt) / temp_coff_0;
+    const double temp_coff_1 = 4 * eps_0 * eps_inf + d.gamma + 2 * sigma_e * dt;
+    d.ca = (4 * eps_0 * eps_inf - 2 * sigma_e * dt) / (temp_coff_1);
+    d.cb = (d.gamma) / (temp_coff_1);
+    d.cc = (4 * dt) / (temp_coff_1 * dl);
+  } else if (d.kind == 2) {
+    const double eps_inf = p[0], omega_p = p[1], nv = p[2];
+    d.k = (2 - nv * dt) / (2 + nv * dt);
+    d.beta = (omega_p * omega_p * eps_0 * dt) / (2 + nv * dt);
+    const double temp_coff_1 = 2 * eps_0 * eps_inf + d.beta * dt + sigma_e * dt;
+    d.ca = (2 * eps_0 * eps_inf - d.beta * dt - sigma_e * dt) / (temp_coff_1);
+    d.cb = 2 * dt / (temp_coff_1 * dl);
+  } else if (d.kind == 3) {
+    const double eps_s = p[0], eps_inf = p[1], tau = p[2];
+    const double delta_eps = eps_s - eps_inf;
+    d.k = (2 * tau - dt) / (2 * tau + dt);
+    d.beta = (2 * delta_eps * eps_0 * dt) / (2 * tau + dt);
+    const double temp_coff_1 = 2 * eps_0 * eps_inf + d.beta + sigma_e * dt;
+    d.ca = (2 * eps_0 * eps_inf + d.beta - sigma_e * dt) / (temp_coff_1);
+    d.cb = (2 * dt) / ((temp_coff_1)*dl);
+  } else {
+    throw std::runtime_error("unknown dispersive medium");
+  }
+  return d;
 }
 
 
@@ -301,8 +344,16 @@ void Simulation::init(size_t total_time_steps) {
   };
   intern(Props{constant::EPSILON_0, constant::MU_0, 0.0, 0.0});   // background, fdtd_basic_coff.cpp:313-339
   std::vector<uint32_t> cell_mat(nx * ny * nz, 0);
+  // dispersive media: per cell the index of its dispersive medium (-1 none)
+  std::vector<xfdtd_dispersive_medium> disp_media;
+  std::vector<int32_t> cell_disp;
+  for (auto &o : _objects)
+    if (o->isDispersion() && cell_disp.empty()) {
+      // LinearDispersiveMaterial::init (dispersive_material.h:30-43)
+      if (two_d || d[0] != d[1] || d[1] != d[2]) throw std::runtime_error("The condition (dx == dy == dz) is required");
+      cell_disp.assign(nx * ny * nz, -1);
+    }
   for (auto &o : _objects) {
-    if (o->isDispersion()) throw std::runtime_error("Dispersion is not supported yet.");   // object.cpp:109-110
     if (o->isThinWire()) {   // thin_wire.cpp:17-37: checks only
       const Cylinder *cy = dynamic_cast<const Cylinder *>(&o->shape());
       if (!cy) throw std::runtime_error("ThinWire only support Cylinder shape");
@@ -317,7 +368,12 @@ void Simulation::init(size_t total_time_steps) {
     gs.gridBox(o->shape());   // Object::init computes the grid box first; it throws out of range
     const Material &m = o->material();
     const uint32_t id = intern(Props{m.getPermittivityE(), m.getPermeabilityM(), m.getElectricalConductivity(),
-                                     m.getMagneticConductivity()});
+                                     m.getMagneticConductivity(), m.isDispersion()});
+    int32_t did = -1;
+    if (m.isDispersion()) {
+      did = static_cast<int32_t>(disp_media.size());
+      disp_media.push_back(dispersiveMedium(m, dt, d[0]));
+    }
     // candidate index range: cell centres within the wrapped box (plus tolerance)
     auto w = o->getWrappedBox();
     const Cube *c = dynamic_cast<const Cube *>(w.get());
@@ -340,8 +396,10 @@ void Simulation::init(size_t total_time_steps) {
         const size_t i = r0[0] + q;
         for (size_t j = r0[1]; j < r1[1]; ++j)
           for (size_t k = r0[2]; k < r1[2]; ++k)
-            if (sh.isPointInside(PointVector{gs.hNode(0, i), gs.hNode(1, j), two_d ? 0.0 : gs.hNode(2, k)}))
+            if (sh.isPointInside(PointVector{gs.hNode(0, i), gs.hNode(1, j), two_d ? 0.0 : gs.hNode(2, k)})) {
               cell_mat[(i * ny + j) * nz + k] = id;
+              if (!cell_disp.empty()) cell_disp[(i * ny + j) * nz + k] = did;
+            }
       });
   }
   if (!_voxel_index.empty()) {
@@ -356,6 +414,7 @@ void Simulation::init(size_t total_time_steps) {
     parallel_for(nx, [&](size_t i) {
       for (size_t q = i * ny * nz; q < (i + 1) * ny * nz; ++q) cell_mat[q] = vid[_voxel_index[q]];
     });
+    std::fill(cell_disp.begin(), cell_disp.end(), -1);   // voxel materials are plain
   }
 
   // ---- coefficient table with per-cell overrides ------------------------
@@ -874,6 +933,43 @@ void Simulation::init(size_t total_time_steps) {
   plan.probe_terms = terms.data();
   plan.n_snapshots = static_cast<int32_t>(series.size());
   plan.snapshots = series.data();
+
+  // ---- dispersive media: the E components their recursions update --------
+  // Simulation::updateEWithDispersiveMaterial (simulation_update.cpp:221-280):
+  // each component over its main-update range, in the cells whose object is
+  // a dispersive medium.  Outside the CPML only (the reference's PML would
+  // add its psi terms with the cell's free-space coefficients), and with no
+  // lumped element on them (its coefficients would override the medium's).
+  std::vector<xfdtd_dispersive_cell> disp_cells;
+  if (!cell_disp.empty()) {
+    auto in_slab = [&](int a, size_t q) { return prof[a].layers && prof[a].slot_e[q] >= 0; };
+    for (size_t i = 0; i < nx; ++i)
+      for (size_t j = 0; j < ny; ++j)
+        for (size_t k = 0; k < nz; ++k) {
+          const int32_t m = cell_disp[(i * ny + j) * nz + k];
+          if (m < 0) continue;
+          if (in_slab(0, i) || in_slab(1, j) || in_slab(2, k))
+            throw std::runtime_error("dispersive media must lie outside the CPML");
+          const bool on[3] = {j >= 1 && k >= 1, i >= 1 && k >= 1, i >= 1 && j >= 1};
+          for (int c = 0; c < 3; ++c)
+            if (on[c])
+              disp_cells.push_back(xfdtd_dispersive_cell{c, m, static_cast<int64_t>(i), static_cast<int64_t>(j),
+                                                         static_cast<int64_t>(k)});
+        }
+    auto disp_at = [&](int64_t i, int64_t j, int64_t k) {
+      return i >= 0 && j >= 0 && k >= 0 && static_cast<size_t>(i) < nx && static_cast<size_t>(j) < ny &&
+             static_cast<size_t>(k) < nz && cell_disp[(i * ny + j) * nz + k] >= 0;
+    };
+    for (const auto &c : injections)
+      if (disp_at(c.i, c.j, c.k)) throw std::runtime_error("a lumped element lies in a dispersive medium");
+    for (const auto &c : inductors)
+      if (disp_at(c.i, c.j, c.k)) throw std::runtime_error("a lumped element lies in a dispersive medium");
+  }
+  plan.n_disp_media = static_cast<int32_t>(disp_media.size());
+  plan.disp_media = disp_media.data();
+  plan.n_disp_cells = static_cast<int32_t>(disp_cells.size());
+  plan.disp_cells = disp_cells.data();
+  plan.disp_dl = d[0];
 
   xfdtd_handle *h = nullptr;
   const int rc = xfdtd_create(&plan, &h);

@@ -49,7 +49,11 @@ class ShapeDesc(C.Structure):
 
 class MaterialDesc(C.Structure):
     _fields_ = [("eps_r", C.c_float), ("mu_r", C.c_float), ("sigma_e", C.c_double),
-                ("sigma_m", C.c_double)]
+                ("sigma_m", C.c_double), ("dispersion", C.c_int32), ("reserved", C.c_int32),
+                ("p", C.c_double * 4)]
+
+
+DISPERSION_NONE, DISPERSION_LORENTZ, DISPERSION_DRUDE, DISPERSION_DEBYE = 0, 1, 2, 3
 
 
 class ObjectDesc(C.Structure):
@@ -187,6 +191,40 @@ class Material:
         d.eps_r, d.mu_r = float(self.eps_r), float(self.mu_r)
         d.sigma_e, d.sigma_m = float(self.sigma_e), float(self.sigma_m)
         return d
+
+
+class LorentzMedium(Material):
+    """LorentzMedium(name, eps_s, eps_inf, omega_p, nv, sigma_e=0, sigma_m=0),
+    src/include/material/dispersive_material.h:58-73: a Lorentz pole pair of
+    strength eps_s - eps_inf at omega_p, damping nv; eps_r = mu_r = 1."""
+
+    def __init__(self, name, eps_s, eps_inf, omega_p, nv, sigma_e=0.0, sigma_m=0.0):
+        super().__init__(name, 1, 1, sigma_e, sigma_m)
+        self.kind, self.params = DISPERSION_LORENTZ, (eps_s, eps_inf, omega_p, nv)
+
+    def desc(self) -> MaterialDesc:
+        d = super().desc()
+        d.dispersion = self.kind
+        d.p[:] = [float(v) for v in self.params]
+        return d
+
+
+class DrudeMedium(LorentzMedium):
+    """DrudeMedium(name, eps_inf, omega_p, nv, sigma_e=0, sigma_m=0),
+    dispersive_material.h:106-118."""
+
+    def __init__(self, name, eps_inf, omega_p, nv, sigma_e=0.0, sigma_m=0.0):
+        Material.__init__(self, name, 1, 1, sigma_e, sigma_m)
+        self.kind, self.params = DISPERSION_DRUDE, (eps_inf, omega_p, nv, 0.0)
+
+
+class DebyMedium(LorentzMedium):
+    """DebyMedium(name, eps_s, eps_inf, tau, sigma_e=0, sigma_m=0),
+    dispersive_material.h:138-141 (the reference's spelling)."""
+
+    def __init__(self, name, eps_s, eps_inf, tau, sigma_e=0.0, sigma_m=0.0):
+        Material.__init__(self, name, 1, 1, sigma_e, sigma_m)
+        self.kind, self.params = DISPERSION_DEBYE, (eps_s, eps_inf, tau, 0.0)
 
 
 @dataclass
