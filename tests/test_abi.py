@@ -80,6 +80,8 @@ int main(void) {
          sizeof(xfdtd_waveform_desc), sizeof(xfdtd_pml_desc), sizeof(xfdtd_tfsf_desc),
          sizeof(xfdtd_nffft_desc), sizeof(xfdtd_lumped_desc), sizeof(xfdtd_monitor_desc),
          sizeof(xfdtd_port_desc));
+  printf("%zu %zu %zu\n", sizeof(xfdtd_material_desc), offsetof(xfdtd_material_desc, dispersion),
+         offsetof(xfdtd_material_desc, p));
   printf("%zu %zu %zu %zu %zu %zu %zu\n", offsetof(xfdtd_monitor_desc, component),
          offsetof(xfdtd_monitor_desc, plot_step), offsetof(xfdtd_monitor_desc, total_time_steps),
          offsetof(xfdtd_scene_desc, n_ports), offsetof(xfdtd_scene_desc, ports),
@@ -95,6 +97,7 @@ int main(void) {
         sizes = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     mine = [C.sizeof(t) for t in (S.SceneDesc, S.ObjectDesc, S.WaveformDesc, S.PMLDesc, S.TFSFDesc,
                                   S.NFFFTDesc, S.LumpedDesc, S.MonitorDesc, S.PortDesc)]
+    mine += [C.sizeof(S.MaterialDesc), S.MaterialDesc.dispersion.offset, S.MaterialDesc.p.offset]
     mine += [S.MonitorDesc.component.offset, S.MonitorDesc.plot_step.offset, S.MonitorDesc.total_time_steps.offset,
              S.SceneDesc.n_ports.offset, S.SceneDesc.ports.offset, S.SceneDesc.network_freqs.offset,
              S.PortDesc.voltage_monitor.offset]

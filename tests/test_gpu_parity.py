@@ -218,7 +218,7 @@ def test_every_shell_variant_is_bitwise_identical(name, precision):
 # the wide decomposition's interior variants (TMA-staged, every plane and
 # row over the interior's k range) and the z-edge TMA shell variants
 WIDE_VARIANTS = (20, 21, 22)
-ZEDGE_SHELL_VARIANTS = (4, 5, 6, 7, 8, 9)
+ZEDGE_SHELL_VARIANTS = (4, 5, 6, 7, 8, 9, 10, 11)
 
 
 @pytest.mark.parametrize("name", ["dielectric", "heterogeneous", "oblique", "long_z", "one_sided"])

@@ -509,10 +509,12 @@ struct ShellVariant {
   int kt;       // tile width along k of the z-edge launch: 32 (x 8 rows) or 16 (x 16 rows)
 };
 // (8 and 4 planes per block measured slower on the 280^3 dielectric sphere.)
+// The z-edge variants with minb 5 cap the launch at 5 blocks per SM (48
+// registers a thread).
 constexpr ShellVariant kShellVariants[] = {{4, false},           {6, false},           {4, true},
                                            {6, true},            {0, false, 4, 16, 32}, {0, false, 6, 16, 32},
                                            {0, true, 4, 16, 32}, {0, false, 4, 16, 16}, {0, false, 6, 16, 16},
-                                           {0, true, 4, 16, 16}};
+                                           {0, true, 4, 16, 16}, {5, false, 4, 16, 32}, {5, false, 4, 16, 16}};
 constexpr int kNumShellVariants = sizeof(kShellVariants) / sizeof(kShellVariants[0]);
 
 // A z-edge TMA variant runs on the wide decomposition only.
@@ -539,7 +541,7 @@ void launch_shell_v(xfdtd_handle *h, bool e_side, const xg::ShellBoxes &s, cudaS
   else xg::k_update_h_shell<T, I, MB, CT><<<s.blocks, 256, 0, st>>>(p, s);
 }
 
-template <typename T, typename I, int S, bool CT, int MODE, int KT = xg::kItK>
+template <typename T, typename I, int S, bool CT, int MODE, int KT = xg::kItK, int MINB = 1>
 void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, int chunk, cudaStream_t st);
 
 // The shell kernel of one side over the decomposition of its current
@@ -555,7 +557,10 @@ void launch_shell(xfdtd_handle *h, bool e_side, int var = -1, cudaStream_t st = 
   if (v.stages) {
     if (&s != &h->vshell_w[side]) throw Err{XFDTD_ERR_STATE, "z-edge TMA launch outside the wide decomposition"};
     auto p = vol_params<T, I>(h);
-    if (v.kt == xg::kItKz) {
+    if (v.minb == 5) {
+      if (v.kt == xg::kItKz) launch_vol_tma<T, I, 4, false, 2, xg::kItKz, 5>(h, p, e_side, v.chunk, st);
+      else launch_vol_tma<T, I, 4, false, 2, xg::kItK, 5>(h, p, e_side, v.chunk, st);
+    } else if (v.kt == xg::kItKz) {
       if (v.stages == 6) launch_vol_tma<T, I, 6, false, 2, xg::kItKz>(h, p, e_side, v.chunk, st);
       else if (v.ct) launch_vol_tma<T, I, 4, true, 2, xg::kItKz>(h, p, e_side, v.chunk, st);
       else launch_vol_tma<T, I, 4, false, 2, xg::kItKz>(h, p, e_side, v.chunk, st);
@@ -925,6 +930,12 @@ void interior_tma_setup(xfdtd_handle *h) {
       attr(xg::k_interior_tma_h<T, I, 6, false, M, KT, true>, GG::template smem_h<6>());
       attr(xg::k_interior_tma_h<T, I, 4, true, M, KT, true>, GG::template smem_h<4>());
     }
+    if constexpr (M == 2) {   // the capped z-edge launches
+      attr(xg::k_interior_tma_e<T, I, 4, false, M, KT, false, 5>, GG::template smem_e<4>());
+      attr(xg::k_interior_tma_h<T, I, 4, false, M, KT, false, 5>, GG::template smem_h<4>());
+      attr(xg::k_interior_tma_e<T, I, 4, false, M, KT, true, 5>, GG::template smem_e<4>());
+      attr(xg::k_interior_tma_h<T, I, 4, false, M, KT, true, 5>, GG::template smem_h<4>());
+    }
   };
   attrs(std::integral_constant<int, 0>{}, std::integral_constant<int, xg::kItK>{});
   for (int side = 0; side < 2; ++side) {
@@ -942,7 +953,7 @@ void interior_tma_setup(xfdtd_handle *h) {
   attrs(std::integral_constant<int, 2>{}, std::integral_constant<int, xg::kItKz>{});
 }
 
-template <typename T, typename I, int S, bool CT, int MODE, int KT>
+template <typename T, typename I, int S, bool CT, int MODE, int KT, int MINB>
 void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, int chunk, cudaStream_t st) {
   using G = xg::ItTiles<T, I, KT>;
   if (h->itm_base != h->F[0]) interior_tma_encode<T, I>(h);   // the buffers were swapped
@@ -963,20 +974,20 @@ void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, 
   if constexpr (MODE != 0) {
     if (fz.on) {
       if (e_side)
-        xg::k_interior_tma_e<T, I, S, CT, MODE, KT, true><<<grid, xg::kItThreads, smem, st>>>(
+        xg::k_interior_tma_e<T, I, S, CT, MODE, KT, true, MINB><<<grid, xg::kItThreads, smem, st>>>(
             maps[0], p, in, chunk, h->d_status, h->wait_polls, fz);
       else
-        xg::k_interior_tma_h<T, I, S, CT, MODE, KT, true><<<grid, xg::kItThreads, smem, st>>>(
+        xg::k_interior_tma_h<T, I, S, CT, MODE, KT, true, MINB><<<grid, xg::kItThreads, smem, st>>>(
             maps[1], p, in, chunk, h->d_status, h->wait_polls, fz);
       return;
     }
   }
   if (e_side) {
-    xg::k_interior_tma_e<T, I, S, CT, MODE, KT><<<grid, xg::kItThreads, smem, st>>>(maps[0], p, in, chunk, h->d_status,
-                                                                                  h->wait_polls, fz);
+    xg::k_interior_tma_e<T, I, S, CT, MODE, KT, false, MINB><<<grid, xg::kItThreads, smem, st>>>(
+        maps[0], p, in, chunk, h->d_status, h->wait_polls, fz);
   } else {
-    xg::k_interior_tma_h<T, I, S, CT, MODE, KT><<<grid, xg::kItThreads, smem, st>>>(maps[1], p, in, chunk, h->d_status,
-                                                                                  h->wait_polls, fz);
+    xg::k_interior_tma_h<T, I, S, CT, MODE, KT, false, MINB><<<grid, xg::kItThreads, smem, st>>>(
+        maps[1], p, in, chunk, h->d_status, h->wait_polls, fz);
   }
 }
 

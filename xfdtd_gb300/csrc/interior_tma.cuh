@@ -185,8 +185,8 @@ struct ItRing {
   }
 };
 
-template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK, bool TF = false>
-__global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
+template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK, bool TF = false, int MINB = 1>
+__global__ void __launch_bounds__(kItThreads, MINB) k_interior_tma_e(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
                                                                InteriorBox in, int chunk, int *status,
                                                                int wait_limit, const __grid_constant__ TfsfFuse fz) {
   using G = ItTiles<T, I, KT>;
@@ -316,8 +316,8 @@ __global__ void __launch_bounds__(kItThreads) k_interior_tma_e(const __grid_cons
   }
 }
 
-template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK, bool TF = false>
-__global__ void __launch_bounds__(kItThreads) k_interior_tma_h(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
+template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK, bool TF = false, int MINB = 1>
+__global__ void __launch_bounds__(kItThreads, MINB) k_interior_tma_h(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
                                                                InteriorBox in, int chunk, int *status,
                                                                int wait_limit, const __grid_constant__ TfsfFuse fz) {
   using G = ItTiles<T, I, KT>;
