@@ -65,10 +65,12 @@ enum {
   XFDTD_FLAG_PROFILE = 2,    /* time every kernel launch with CUDA events        */
   XFDTD_FLAG_AUTOTUNE = 4,   /* pick the volume kernels and their variants by timing at create */
   XFDTD_FLAG_SPLIT_EH = 8,   /* always the separate in-place E and H kernels            */
-  XFDTD_FLAG_FUSED_EH = 16   /* always the fused E/H sweep (unless the plan has lumped
+  XFDTD_FLAG_FUSED_EH = 16,  /* always the fused E/H sweep (unless the plan has lumped
                                 elements, which run the split kernels).  With neither
                                 flag the autotuner picks the faster of the two, and
                                 without autotuning the split kernels run. */
+  XFDTD_FLAG_PLAIN_VOLUME = 32  /* xfdtd_batch_create: the one-thread-per-cell volume
+                                   kernels for every member, none TMA-staged */
 };
 
 /* The 18 coefficients of one table entry, in this order (the reference's
@@ -380,7 +382,8 @@ int xfdtd_adjoint_backward(xfdtd_handle *h, double *grad_eps, double *grad_sigma
  * together.  The reference runs one Simulation at a time
  * (simulation_update.cpp:5-40); a batch runs each phase of the loop body
  * for all of its running members in one launch (the volume phases: an
- * interior and a shell launch per group of up to 64 members), and replays
+ * interior and a shell launch per group of up to 64 members, TMA-staged
+ * for the members whose grids allow it), and replays
  * the step loop from a CUDA graph (XFDTD_FLAG_GRAPH).  Members
  * are ordinary handles from xfdtd_create -- same device, precision and
  * material-index width, not yet stepped, without lumped elements or
@@ -400,6 +403,12 @@ int xfdtd_batch_step_timed(xfdtd_batch *b, int64_t n, double *ms);
 int xfdtd_batch_synchronize(xfdtd_batch *b);
 /* Members with steps left, batch steps taken, kernel launches enqueued. */
 int xfdtd_batch_status(xfdtd_batch *b, int *n_running, int64_t *clock, int64_t *launches);
+/* Members whose volume phases run on the TMA-staged launches of the wide
+ * decomposition (every member whose grid gives those launches aligned
+ * tiles, unless the batch was made with XFDTD_FLAG_PLAIN_VOLUME); the
+ * others run the one-thread-per-cell kernels.  No counterpart in the
+ * reference. */
+int xfdtd_batch_tma_members(xfdtd_batch *b, int *n);
 const char *xfdtd_batch_last_error(xfdtd_batch *b);
 void xfdtd_batch_destroy(xfdtd_batch *b);
 

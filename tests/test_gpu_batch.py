@@ -50,3 +50,34 @@ def test_batch_rejects_bad_members():
         X.Batch([a, c])
     with pytest.raises(X.EngineError, match="twice"):
         X.Batch([c, c])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_tma_launches_match_plain_and_alone(precision):
+    """Members whose grids allow the wide decomposition's TMA-staged launches
+    run them inside the batch (batch.cuh k_tma_batch); the others run the
+    one-thread-per-cell kernels in the same phases.  Both give the bits of
+    the member stepped alone, and of the batch with every member on the
+    plain kernels."""
+    probs = [(sc, 40 + 9 * q) for q, (sc, _) in enumerate(configs.batched_scatterers(n=4, seed0=4200))]
+    probs += _problems(2, [44, 31])   # half-size members
+    runs = {}
+    for plain in (False, True):
+        members = [X.Simulation(sc, st, precision=precision, fused=False, autotune=False) for sc, st in probs]
+        b = X.Batch(members, graph=True, plain=plain)
+        if plain:
+            assert b.tma_members() == 0
+        else:
+            assert b.tma_members() >= 1
+        b.step(100)
+        b.synchronize()
+        runs[plain] = [[m.read_field(c) for c in range(6)] + [m.read_nffft(w) for w in (0, 7, 13, 22)]
+                       for m in members]
+        del b
+    for q, (sc, st) in enumerate(probs):
+        a = X.Simulation(sc, st, precision=precision, fused=False, autotune=False)
+        a.step(st)
+        alone = [a.read_field(c) for c in range(6)] + [a.read_nffft(w) for w in (0, 7, 13, 22)]
+        for x, y, z in zip(runs[False][q], runs[True][q], alone):
+            assert np.array_equal(x, z), q
+            assert np.array_equal(y, z), q

@@ -26,6 +26,7 @@ from .scene import (  # noqa: F401  (re-exported: the reference's scene API)
 
 FP64, FP32 = 0, 1
 FLAG_GRAPH, FLAG_PROFILE, FLAG_AUTOTUNE, FLAG_SPLIT_EH, FLAG_FUSED_EH = 1, 2, 4, 8, 16
+FLAG_PLAIN_VOLUME = 32
 STATUS = {0: "ok", 1: "invalid plan", 2: "CUDA error", 3: "out of device memory", 4: "timeout",
           5: "non-finite value", 6: "device check", 7: "bad state"}
 
@@ -109,6 +110,7 @@ def libs():
         cu.xfdtd_batch_step_timed.argtypes = [C.c_void_p, C.c_int64, dp]
         cu.xfdtd_batch_synchronize.argtypes = [C.c_void_p]
         cu.xfdtd_batch_status.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int64), P(C.c_int64)]
+        cu.xfdtd_batch_tma_members.argtypes = [C.c_void_p, P(C.c_int)]
         cu.xfdtd_batch_last_error.argtypes = [C.c_void_p]
         cu.xfdtd_batch_last_error.restype = C.c_char_p
         cu.xfdtd_batch_destroy.argtypes = [C.c_void_p]
@@ -439,14 +441,17 @@ class Batch:
     still running, the step loop replayed from a CUDA graph.  Members are
     `Simulation`s created with fused=False, not yet stepped, without lumped
     elements or monitors; each stops at its own total_steps.  Read them with
-    their own methods after `synchronize()`."""
+    their own methods after `synchronize()`.  The volume phases run on the
+    TMA-staged launches for the members whose grids allow them, unless
+    `plain` (every member on the one-thread-per-cell kernels)."""
 
-    def __init__(self, members: list, graph: bool = True):
+    def __init__(self, members: list, graph: bool = True, plain: bool = False):
         cu, _ = libs()
         self.members = list(members)
         arr = (C.c_void_p * len(self.members))(*[m.engine.value for m in self.members])
         b = C.c_void_p()
-        rc = cu.xfdtd_batch_create(arr, len(self.members), FLAG_GRAPH if graph else 0, C.byref(b))
+        flags = (FLAG_GRAPH if graph else 0) | (FLAG_PLAIN_VOLUME if plain else 0)
+        rc = cu.xfdtd_batch_create(arr, len(self.members), flags, C.byref(b))
         self.b = b
         if rc != 0:
             msg = cu.xfdtd_batch_last_error(b).decode()
@@ -473,6 +478,13 @@ class Batch:
         r, clock, launches = C.c_int(), C.c_int64(), C.c_int64()
         self._check(libs()[0].xfdtd_batch_status(self.b, C.byref(r), C.byref(clock), C.byref(launches)))
         return {"running": r.value, "clock": clock.value, "launches": launches.value}
+
+    def tma_members(self) -> int:
+        """Members on the TMA-staged volume launches (the rest run the
+        one-thread-per-cell kernels)."""
+        n = C.c_int()
+        self._check(libs()[0].xfdtd_batch_tma_members(self.b, C.byref(n)))
+        return n.value
 
     def __del__(self):
         if getattr(self, "b", None) and _cuda is not None:

@@ -2,11 +2,10 @@
 //
 // A batch (engine.cu, xfdtd_batch_*) drives several engine handles of
 // different grid sizes.  Each phase of a step is one launch over a work
-// list of (simulation, tile) items for all simulations still running.  The
-// volume phases run one block per item; the surface phases (few items per
-// simulation) have a fixed number of blocks, each walking a contiguous
-// range of the list and loading a simulation's parameters into shared
-// memory when its range crosses into the next simulation.
+// list of (simulation, tile) items for all simulations still running, one
+// block per item.  The volume phases find a block's member from block
+// offsets in the launch's parameters; the surface phases read the item
+// from a list and load its simulation's parameters into shared memory.
 // Per cell the work is that of the single-simulation kernels (e_fast /
 // e_shell_cell, h_fast / h_shell_cell, tfsf_e_surface / tfsf_h_surface,
 // nffft_sample / nffft_fold, tfsf_aux_block), so a batched simulation gives
@@ -14,6 +13,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "interior_tma.cuh"
 #include "surface.cuh"
 #include "volume.cuh"
 
@@ -25,13 +25,6 @@ struct WorkItem {
   int sim;
   int tile;
 };
-
-// Range of work items of this block: contiguous, equal shares.
-__device__ __forceinline__ void item_range(int n_items, int &lo, int &hi) {
-  const int per = (n_items + gridDim.x - 1) / gridDim.x;
-  lo = blockIdx.x * per;
-  hi = min(lo + per, n_items);
-}
 
 // Copies the parameter struct of simulation `sim` into shared memory (all
 // threads; returns after a barrier).
@@ -110,67 +103,82 @@ __global__ void __launch_bounds__(256, 6) k_shell_batch(const __grid_constant__ 
   else h_shell_cell<T, I, CT>(g.m[q], cls, i, j, k);
 }
 
-// TFSF E or H corrections: tile = 256 consecutive surface cells.
+// The wide decomposition's TMA-staged launches (interior_tma.cuh) over the
+// members whose grids allow them: MODE 1 every plane and row over the
+// member's interior k range, MODE 2 its z edges, with the single-simulation
+// launches' tiles and arithmetic, so the same bits.  The block's tile is
+// block t of the member's own launch grid (k tiles fastest, then j tiles,
+// then chunks of `chunk` planes; grids[q] = k tiles, j tiles).  The
+// members' tensor maps lie in global memory, written by the host when the
+// batch is made; the thread that issues the copies acquires them first.
+template <typename T, typename I, int STAGES, bool CT, int MODE, bool E_SIDE>
+__global__ void __launch_bounds__(kItThreads) k_tma_batch(const __grid_constant__ VolGroup<T, I> g,
+                                                          const __grid_constant__ GroupBlocks gb,
+                                                          const ItMaps *__restrict__ maps,
+                                                          const InteriorBox *__restrict__ boxes,
+                                                          const int2 *__restrict__ grids, int *const *__restrict__ status,
+                                                          int chunk) {
+  const int q = group_member(gb);
+  const unsigned t = blockIdx.x - gb.first[q];
+  const int2 gd = grids[q];
+  const unsigned nk = static_cast<unsigned>(gd.x), nj = static_cast<unsigned>(gd.y);
+  const uint3 bid = make_uint3(t % nk, (t / nk) % nj, t / (nk * nj));
+  const ItMaps &m = maps[q];
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < 3; ++c) {
+      fence_tensormap_acquire(&m.a[c]);
+      fence_tensormap_acquire(&m.b[c]);
+    }
+    if (ItTiles<T, I, kItK>::IDX) fence_tensormap_acquire(&m.idx);
+  }
+  const InteriorBox in = boxes[q];
+  const TfsfFuse fz{};
+  if (E_SIDE)
+    it_e_block<T, I, STAGES, CT, MODE, kItK, false>(m, g.m[q], in, chunk, status[q], kItWaitLimit, fz, bid);
+  else
+    it_h_block<T, I, STAGES, CT, MODE, kItK, false>(m, g.m[q], in, chunk, status[q], kItWaitLimit, fz, bid);
+}
+
+// TFSF E or H corrections: one block per work item, tile = 256 consecutive
+// surface cells of the item's simulation.
 template <typename T, bool E_SIDE>
 __global__ void __launch_bounds__(256) k_tfsf_batch(const TfsfSurfParams<T> *__restrict__ all,
-                                                    const WorkItem *__restrict__ items, int n_items) {
+                                                    const WorkItem *__restrict__ items) {
   __shared__ TfsfSurfParams<T> p;
-  int lo, hi;
-  item_range(n_items, lo, hi);
-  int cur = -1;
-  for (int w = lo; w < hi; ++w) {
-    const WorkItem it = items[w];
-    if (it.sim != cur) {
-      load_params(p, all, it.sim);
-      cur = it.sim;
-    }
-    const int q = it.tile * 256 + threadIdx.x;
-    if (E_SIDE) tfsf_e_surface(p, q);
-    else tfsf_h_surface(p, q);
-  }
+  const WorkItem it = items[blockIdx.x];
+  load_params(p, all, it.sim);
+  const int q = it.tile * 256 + threadIdx.x;
+  if (E_SIDE) tfsf_e_surface(p, q);
+  else tfsf_h_surface(p, q);
 }
 
-// NF-FF surface samples: tile = (face, 32 x 8 face block), numbered
-// u-block fastest, then v-block, then face; the grid of a simulation is
-// that of k_nffft, given by gu x gv per face (ints 0, 1 of the tile).
+// NF-FF surface samples: one block per work item, tile = (face, 32 x 8
+// face block), numbered u-block fastest, then v-block, then face; the grid
+// of a simulation is that of k_nffft, given by gu x gv per face (ints 0, 1
+// of the tile).
 template <typename T>
 __global__ void __launch_bounds__(256) k_nffft_batch(const NfParams<T> *__restrict__ all, const int2 *__restrict__ grid,
-                                                     const WorkItem *__restrict__ items, int n_items) {
+                                                     const WorkItem *__restrict__ items) {
   __shared__ NfParams<T> p;
-  int lo, hi;
-  item_range(n_items, lo, hi);
-  int cur = -1;
+  const WorkItem it = items[blockIdx.x];
+  load_params(p, all, it.sim);
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  for (int w = lo; w < hi; ++w) {
-    const WorkItem it = items[w];
-    if (it.sim != cur) {
-      load_params(p, all, it.sim);
-      cur = it.sim;
-    }
-    const int2 g = grid[it.sim];
-    const int bu = it.tile % g.x, bv = (it.tile / g.x) % g.y, face = it.tile / (g.x * g.y);
-    nffft_sample(p, face, bu * 32 + tx, bv * 8 + ty);
-  }
+  const int2 g = grid[it.sim];
+  const int bu = it.tile % g.x, bv = (it.tile / g.x) % g.y, face = it.tile / (g.x * g.y);
+  nffft_sample(p, face, bu * 32 + tx, bv * 8 + ty);
 }
 
-// NF-FF fold of `count` buffered steps: tile = (group, 256 face cells),
-// numbered cell block fastest; per simulation nb blocks per group.
+// NF-FF fold of `count` buffered steps: one block per work item, tile =
+// (group, 256 face cells), numbered cell block fastest; per simulation nb
+// blocks per group.
 template <typename T>
 __global__ void __launch_bounds__(256) k_nffft_fold_batch(const NfParams<T> *__restrict__ all, const int *__restrict__ nb,
-                                                          const WorkItem *__restrict__ items, int n_items, int count) {
+                                                          const WorkItem *__restrict__ items, int count) {
   __shared__ NfParams<T> p;
-  int lo, hi;
-  item_range(n_items, lo, hi);
-  int cur = -1;
-  for (int w = lo; w < hi; ++w) {
-    const WorkItem it = items[w];
-    if (it.sim != cur) {
-      load_params(p, all, it.sim);
-      cur = it.sim;
-    }
-    const int n = nb[it.sim];
-    nffft_fold(p, it.tile / n, static_cast<long long>(it.tile % n) * 256 + threadIdx.x, count, 0);
-  }
+  const WorkItem it = items[blockIdx.x];
+  load_params(p, all, it.sim);
+  const int n = nb[it.sim];
+  nffft_fold(p, it.tile / n, static_cast<long long>(it.tile % n) * 256 + threadIdx.x, count, 0);
 }
 
 // The 1-D incident lines: one block per listed simulation.

@@ -187,6 +187,7 @@ struct xfdtd_handle {
   // volume-kernel variants (autotuned)
   int var_e = 1, var_h = 1;   // L1-table variant: valid for every plan
   float tune_ms[2][24] = {};
+  float tune_step_ms = 0.f;   // the autotuner's last round: the kept pairing's trial step
   // TMA-staged interior kernels (interior_tma.cuh): offered per side when the
   // interior's k range starts on a 16-byte boundary for fields and index
   bool it_ok[2] = {};
@@ -1070,6 +1071,17 @@ void launch_tfsf_side(xfdtd_handle *h, bool e_side) {
   XCHECK(cudaGetLastError());
 }
 
+// One candidate of the autotuner's last rounds: a side's interior and shell
+// variants, whether its TFSF corrections are folded into them, and its time.
+struct TuneCand {
+  float ms;
+  int v, sv;
+  bool fold;
+};
+
+template <typename T, typename I>
+void trial_step(xfdtd_handle *h);
+
 template <typename T, typename I>
 void autotune_t(xfdtd_handle *h, int trials) {
   cudaEvent_t a, b;
@@ -1110,17 +1122,20 @@ void autotune_t(xfdtd_handle *h, int trials) {
     return ms / n;
   };
   auto time_ms = [&](auto &&run) { return time_n(run, trials); };
+  std::vector<TuneCand> cands[2];
   for (int side = 0; side < 2 && !forced; ++side) {
     // shell kernel of each decomposition: its fastest variant, timed alone
     int shell_best[2] = {0, 0};
+    float shell_alone[2][kNumShellVariants], shell_alone_best[2] = {1e30f, 1e30f};
     for (int w = 0; w < 2; ++w) {
+      for (int v = 0; v < kNumShellVariants; ++v) shell_alone[w][v] = 1e30f;
       if (w && !h->wide_ok[side]) continue;
       if (!side_shell_cells(h, side, w != 0)) continue;
-      float best = 1e30f;
       for (int v = 0; v < kNumShellVariants; ++v) {
         if (!shell_allowed(h, kShellVariants[v], w != 0)) continue;
         const float ms = time_ms([&] { launch_shell<T, I>(h, side == 0, v, nullptr, w); });
-        if (ms < best) best = ms, shell_best[w] = v;
+        shell_alone[w][v] = ms;
+        if (ms < shell_alone_best[w]) shell_alone_best[w] = ms, shell_best[w] = v;
       }
     }
     // each interior variant with its decomposition's best shell variant,
@@ -1137,9 +1152,10 @@ void autotune_t(xfdtd_handle *h, int trials) {
       if (ms < best) best = ms, best_v = v;
     }
     // the three fastest interior variants, each with every shell variant
-    // its decomposition allows (the shell variant fastest alone need not be
-    // fastest beside the interior launch), timed again over three times
-    // the trials, so that timing noise does not pick the pair
+    // its decomposition allows that is within 20 % of the fastest alone
+    // (the shell variant fastest alone need not be fastest beside the
+    // interior launch), timed again over three times the trials, so that
+    // timing noise does not pick the pair
     int top[3] = {-1, -1, -1};
     for (int v = 0; v < kNumVariants; ++v) {
       if (!variant_allowed(h, kVariants[v])) continue;
@@ -1157,6 +1173,7 @@ void autotune_t(xfdtd_handle *h, int trials) {
     best = 1e30f;
     int best_sv = shell_best[kVariants[best_v].wide ? 1 : 0];
     bool best_fold = false;
+    std::vector<TuneCand> &cand = cands[side];
     for (int q = 0; q < 3 && top[q] >= 0; ++q) {
       const int v = top[q];
       var = v;
@@ -1164,6 +1181,10 @@ void autotune_t(xfdtd_handle *h, int trials) {
       for (int sv = 0; sv < kNumShellVariants; ++sv) {
         if (!shell_allowed(h, kShellVariants[sv], wide)) continue;
         if (!side_shell_cells(h, side, wide) && sv != shell_best[wide ? 1 : 0]) continue;
+        // shell variants more than 20 % slower alone than the fastest are
+        // not retried beside the interior launch
+        if (side_shell_cells(h, side, wide) && shell_alone[wide ? 1 : 0][sv] > 1.2f * shell_alone_best[wide ? 1 : 0])
+          continue;
         h->shell_var[side] = sv;
         for (int fold = 0; fold < 2; ++fold) {
           h->tf_fuse_on[side] = fold != 0;
@@ -1175,6 +1196,7 @@ void autotune_t(xfdtd_handle *h, int trials) {
           }, 3 * trials);
           if (fold) h->tf_fuse_ms[side][0] = ms;
           else if (h->tf_fuse_ok[side] && wide) h->tf_fuse_ms[side][1] = ms;
+          cand.push_back({ms, v, sv, fold != 0});
           if (ms < best) best = ms, best_v = v, best_sv = sv, best_fold = fold != 0;
         }
       }
@@ -1184,6 +1206,40 @@ void autotune_t(xfdtd_handle *h, int trials) {
     h->tf_fuse_on[side] = best_fold;
     h->tune_ms[side][best_v] = best;
     best_split += best;
+  }
+  // Last round: the two fastest candidates of each side, paired, timed as
+  // the step runs them (the E side, then the H side, with the NF-FF
+  // sampling halves beside them on their stream), twice in turn; the
+  // fastest pairing is kept.  Each side's time alone misses how its
+  // launches share the GPU with the other side's neighbours and with the
+  // sampling stream.
+  if (!forced && !cands[0].empty() && !cands[1].empty()) {
+    for (auto &c : cands) {
+      std::stable_sort(c.begin(), c.end(), [](const TuneCand &x, const TuneCand &y) { return x.ms < y.ms; });
+      if (c.size() > 2) c.resize(2);
+    }
+    auto apply = [&](int side, const TuneCand &c) {
+      (side == 0 ? h->var_e : h->var_h) = c.v;
+      h->shell_var[side] = c.sv;
+      h->tf_fuse_on[side] = c.fold;
+    };
+    float t[2][2] = {{1e30f, 1e30f}, {1e30f, 1e30f}};
+    for (int pass = 0; pass < 2; ++pass)
+      for (size_t e = 0; e < cands[0].size(); ++e)
+        for (size_t hh = 0; hh < cands[1].size(); ++hh) {
+          apply(0, cands[0][e]);
+          apply(1, cands[1][hh]);
+          t[e][hh] = std::min(t[e][hh], time_n([&] { trial_step<T, I>(h); }, 2 * trials));
+        }
+    size_t be = 0, bh = 0;
+    for (size_t e = 0; e < cands[0].size(); ++e)
+      for (size_t hh = 0; hh < cands[1].size(); ++hh)
+        if (t[e][hh] < t[be][bh]) be = e, bh = hh;
+    apply(0, cands[0][be]);
+    apply(1, cands[1][bh]);
+    h->tune_step_ms = t[be][bh];
+    h->tune_ms[0][cands[0][be].v] = cands[0][be].ms;
+    h->tune_ms[1][cands[1][bh].v] = cands[1][bh].ms;
   }
   h->sweep = was_sweep;
   h->launch_count = launches;
@@ -1384,6 +1440,36 @@ void volume_pair(xfdtd_handle *h, bool e_side) {
   }
   if (in && sh) XCHECK(cudaStreamWaitEvent(h->stream, h->ev_vjoin[side], 0));
   prof_end(h);
+}
+
+// The volume work of one step as the step runs it, for the autotuner: the
+// E pair and its TFSF corrections (folded or apart), then the H pair and
+// its corrections, with the two NF-FF sampling halves on their stream
+// beside them.  Nothing else of a step runs: no 1-D incident line, sources,
+// fold or step counter.  On the all-zero state before the first step it
+// writes zeros where there were zeros (the samples of step 0 are taken
+// again, from the fields, by the first step).
+template <typename T, typename I>
+void trial_step(xfdtd_handle *h) {
+  const bool split = h->nffft && !h->nf_bb;
+  if (split) {
+    XCHECK(cudaEventRecord(h->ev_nfs_fork, h->stream));
+    XCHECK(cudaStreamWaitEvent(h->nfs, h->ev_nfs_fork, 0));
+    launch_nffft<T>(h, h->nfs, 2, 0);
+    XCHECK(cudaEventRecord(h->ev_nfh, h->nfs));
+  }
+  volume_pair<T, I>(h, true);
+  if (h->tfsf && !tfsf_fused(h, 0)) launch_tfsf_side<T>(h, true);
+  if (split) {
+    XCHECK(cudaEventRecord(h->ev_nfs_fork, h->stream));
+    XCHECK(cudaStreamWaitEvent(h->nfs, h->ev_nfs_fork, 0));
+    launch_nffft<T>(h, h->nfs, 1, 0);
+    XCHECK(cudaEventRecord(h->ev_nfe, h->nfs));
+    XCHECK(cudaStreamWaitEvent(h->stream, h->ev_nfh, 0));
+  }
+  volume_pair<T, I>(h, false);
+  if (h->tfsf && !tfsf_fused(h, 1)) launch_tfsf_side<T>(h, false);
+  if (split) XCHECK(cudaStreamWaitEvent(h->stream, h->ev_nfe, 0));
 }
 
 template <typename T, typename I>
@@ -2690,8 +2776,20 @@ struct xfdtd_batch {
   bool lists_ok = false;
   struct VolLists {   // per group and side: blocks of the interior and shell launches
     xg::GroupBlocks in[2] = {}, sh[2] = {};
+    xg::GroupBlocks tw[2] = {}, tz[2] = {};   // the TMA-staged wide and z-edge launches
   };
   std::vector<VolLists> vl;
+  // members on the wide decomposition's TMA-staged launches (batch.cuh
+  // k_tma_batch): per member the flag; per side their tensor maps, the
+  // wide (MODE 1) and z-edge (MODE 2) boxes and tile grids (device); the
+  // members' status words
+  std::vector<char> tma_m;
+  int n_tma = 0;
+  xg::ItMaps *tmaps[2] = {};
+  xg::InteriorBox *tbox[2][2] = {};   // [side][mode - 1]
+  int2 *tgrid[2][2] = {};
+  std::vector<unsigned> ttiles[2][2];   // host: tiles per member
+  int **status_list = nullptr;
   xg::WorkItem *it_te = nullptr, *it_th = nullptr, *it_nf = nullptr, *it_fold = nullptr;
   int n_te = 0, n_th = 0, n_nf = 0, n_fold = 0;
   int *aux_list = nullptr;
@@ -2723,6 +2821,7 @@ struct xfdtd_batch {
 namespace {
 
 constexpr int kBatchGraphSteps = 32;   // a multiple of the NF-FF batch
+constexpr int kBatchChunk = 16;        // planes per block of the TMA-staged launches
 
 template <typename T, typename I>
 void batch_setup(xfdtd_batch *b) {
@@ -2762,6 +2861,49 @@ void batch_setup(xfdtd_batch *b) {
     XCHECK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice, b->stream));
     return d;
   };
+  // the members on the TMA-staged launches, their maps, boxes and tile grids
+  b->tma_m.assign(n, 0);
+  b->n_tma = 0;
+  std::vector<xg::ItMaps> tm[2];
+  std::vector<xg::InteriorBox> tb[2][2];
+  std::vector<int2> tg[2][2];
+  for (int q = 0; q < n; ++q) {
+    xfdtd_handle *h = b->m[q];
+    const bool ok = !(b->flags & XFDTD_FLAG_PLAIN_VOLUME) && h->it_ok[0] && h->it_ok[1] && h->wide_ok[0] &&
+                    h->wide_ok[1];
+    if (ok && h->itm_base != h->F[0]) interior_tma_encode<T, I>(h);   // maps of the current buffers
+    b->tma_m[q] = ok ? 1 : 0;
+    b->n_tma += ok ? 1 : 0;
+    for (int side = 0; side < 2; ++side) {
+      tm[side].push_back(h->itm[side]);
+      for (int mode = 1; mode <= 2; ++mode) {
+        const xg::InteriorBox in = mode == 2 ? h->vin_z[side] : h->vin_w[side];
+        const int nj = in.hi[1] - in.lo[1] + 1, ni = in.hi[0] - in.lo[0] + 1;
+        const int K = xg::kItK, J = xg::kItThreads / xg::kItK;
+        int nk = mode == 2 ? (in.pz_lo + K - 1) / K + (in.hi[2] - in.pz_hi + K - 1) / K : (in.hi[2] - in.lo[2] + K) / K;
+        const bool cells = mode == 2 ? h->vshell_w_cells[side] > 0 : h->vin_w_cells[side] > 0;
+        if (!ok || !cells || nj <= 0 || ni <= 0) nk = 0;
+        const int gj = nj > 0 ? (nj + J - 1) / J : 0, gi = ni > 0 ? (ni + kBatchChunk - 1) / kBatchChunk : 0;
+        tb[side][mode - 1].push_back(in);
+        tg[side][mode - 1].push_back(make_int2(std::max(nk, 1), std::max(gj, 1)));
+        b->ttiles[side][mode - 1].push_back(static_cast<unsigned>(nk) * gj * gi);
+      }
+    }
+  }
+  if (b->n_tma) {   // dynamic shared memory of the TMA-staged launches (above 48 KB in FP64)
+    const int se = xg::ItTiles<T, I, xg::kItK>::template smem_e<4>(), sh = xg::ItTiles<T, I, xg::kItK>::template smem_h<4>();
+    auto attr = [](auto kern, int bytes) {
+      XCHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    };
+    attr(xg::k_tma_batch<T, I, 4, false, 1, true>, se);
+    attr(xg::k_tma_batch<T, I, 4, false, 2, true>, se);
+    attr(xg::k_tma_batch<T, I, 4, true, 1, true>, se);
+    attr(xg::k_tma_batch<T, I, 4, true, 2, true>, se);
+    attr(xg::k_tma_batch<T, I, 4, false, 1, false>, sh);
+    attr(xg::k_tma_batch<T, I, 4, false, 2, false>, sh);
+    attr(xg::k_tma_batch<T, I, 4, true, 1, false>, sh);
+    attr(xg::k_tma_batch<T, I, 4, true, 2, false>, sh);
+  }
   b->group_params.assign(groups, std::vector<unsigned char>(sizeof(xg::VolGroup<T, I>)));
   for (int g = 0; g < groups; ++g) std::memcpy(b->group_params[g].data(), &vg[g], sizeof(xg::VolGroup<T, I>));
   b->vl.assign(groups, xfdtd_batch::VolLists{});
@@ -2773,7 +2915,15 @@ void batch_setup(xfdtd_batch *b) {
   for (int side = 0; side < 2; ++side) {
     b->vin[side] = up(vin[side]);
     b->vshell[side] = up(vsh[side]);
+    b->tmaps[side] = up(tm[side]);
+    for (int mode = 0; mode < 2; ++mode) {
+      b->tbox[side][mode] = up(tb[side][mode]);
+      b->tgrid[side][mode] = up(tg[side][mode]);
+    }
   }
+  std::vector<int *> st(n);
+  for (int q = 0; q < n; ++q) st[q] = b->m[q]->d_status;
+  b->status_list = up(st);
   XCHECK(cudaStreamSynchronize(b->stream));   // the host vectors go out of scope
 }
 
@@ -2795,21 +2945,28 @@ void batch_lists(xfdtd_batch *b) {
   for (int g = 0; g < groups; ++g)   // volume launches: blocks per member, none for stopped members
     for (int side = 0; side < 2; ++side) {
       xg::GroupBlocks &bi = b->vl[g].in[side], &bs = b->vl[g].sh[side];
+      xg::GroupBlocks &tw = b->vl[g].tw[side], &tz = b->vl[g].tz[side];
       bi = xg::GroupBlocks{};
       bs = xg::GroupBlocks{};
-      bi.n = bs.n = std::min(xg::kBatchGroup, nm - g * xg::kBatchGroup);
+      tw = xg::GroupBlocks{};
+      tz = xg::GroupBlocks{};
+      bi.n = bs.n = tw.n = tz.n = std::min(xg::kBatchGroup, nm - g * xg::kBatchGroup);
       for (int ql = 0; ql < bi.n; ++ql) {
-        const xfdtd_handle *h = b->m[g * xg::kBatchGroup + ql];
-        const bool r = on[g * xg::kBatchGroup + ql] != 0;
+        const int q = g * xg::kBatchGroup + ql;
+        const xfdtd_handle *h = b->m[q];
+        const bool t = b->tma_m[q] != 0;
+        const bool r = on[q] != 0;
+        tw.first[ql + 1] = tw.first[ql] + (r && t ? b->ttiles[side][0][q] : 0u);
+        tz.first[ql + 1] = tz.first[ql] + (r && t ? b->ttiles[side][1][q] : 0u);
         const xg::InteriorBox &in = h->vin[side];
         unsigned tiles = 0;
-        if (r && h->vin_cells[side]) {
+        if (r && !t && h->vin_cells[side]) {
           const int k0 = in.lo[2] / 32 * 32;
           tiles = static_cast<unsigned>(((in.hi[2] - k0) / 32 + 1) * ((in.hi[1] - in.lo[1]) / 8 + 1) *
                                         (in.hi[0] - in.lo[0] + 1));
         }
         bi.first[ql + 1] = bi.first[ql] + tiles;
-        bs.first[ql + 1] = bs.first[ql] + (r ? h->vshell[side].blocks : 0u);
+        bs.first[ql + 1] = bs.first[ql] + (r && !t ? h->vshell[side].blocks : 0u);
       }
     }
   std::vector<xg::WorkItem> te, th, nf, fold;
@@ -2850,10 +3007,6 @@ void batch_lists(xfdtd_batch *b) {
   b->lists_ok = true;
 }
 
-unsigned persistent_grid(const xfdtd_batch *b, int items, int per_sm) {
-  return static_cast<unsigned>(std::max(1, std::min(items, b->n_sm * per_sm)));
-}
-
 template <typename T, typename I>
 void batch_enqueue_t(xfdtd_batch *b, long long s) {
   cudaStream_t st = b->stream;
@@ -2874,6 +3027,39 @@ void batch_enqueue_t(xfdtd_batch *b, long long s) {
       const xfdtd_batch::VolLists &l = b->vl[g];
       const size_t base = g * xg::kBatchGroup;
       const unsigned nsh = l.sh[side].first[l.sh[side].n], nin = l.in[side].first[l.in[side].n];
+      const unsigned ntw = l.tw[side].first[l.tw[side].n], ntz = l.tz[side].first[l.tz[side].n];
+      const xg::ItMaps *mp = b->tmaps[side] + base;
+      int *const *stl = b->status_list + base;
+      // the TMA-staged members: the z edges on the shell stream, the wide
+      // launch on the main stream
+      if (ntz) {
+        const xg::InteriorBox *bx = b->tbox[side][1] + base;
+        const int2 *gr = b->tgrid[side][1] + base;
+        const unsigned sm = e_side ? xg::ItTiles<T, I, xg::kItK>::template smem_e<4>()
+                                   : xg::ItTiles<T, I, xg::kItK>::template smem_h<4>();
+        if (b->ct) {
+          if (e_side) xg::k_tma_batch<T, I, 4, true, 2, true><<<ntz, xg::kItThreads, sm, b->shell>>>(vg, l.tz[side], mp, bx, gr, stl, kBatchChunk);
+          else xg::k_tma_batch<T, I, 4, true, 2, false><<<ntz, xg::kItThreads, sm, b->shell>>>(vg, l.tz[side], mp, bx, gr, stl, kBatchChunk);
+        } else {
+          if (e_side) xg::k_tma_batch<T, I, 4, false, 2, true><<<ntz, xg::kItThreads, sm, b->shell>>>(vg, l.tz[side], mp, bx, gr, stl, kBatchChunk);
+          else xg::k_tma_batch<T, I, 4, false, 2, false><<<ntz, xg::kItThreads, sm, b->shell>>>(vg, l.tz[side], mp, bx, gr, stl, kBatchChunk);
+        }
+        ++launched;
+      }
+      if (ntw) {
+        const xg::InteriorBox *bx = b->tbox[side][0] + base;
+        const int2 *gr = b->tgrid[side][0] + base;
+        const unsigned sm = e_side ? xg::ItTiles<T, I, xg::kItK>::template smem_e<4>()
+                                   : xg::ItTiles<T, I, xg::kItK>::template smem_h<4>();
+        if (b->ct) {
+          if (e_side) xg::k_tma_batch<T, I, 4, true, 1, true><<<ntw, xg::kItThreads, sm, st>>>(vg, l.tw[side], mp, bx, gr, stl, kBatchChunk);
+          else xg::k_tma_batch<T, I, 4, true, 1, false><<<ntw, xg::kItThreads, sm, st>>>(vg, l.tw[side], mp, bx, gr, stl, kBatchChunk);
+        } else {
+          if (e_side) xg::k_tma_batch<T, I, 4, false, 1, true><<<ntw, xg::kItThreads, sm, st>>>(vg, l.tw[side], mp, bx, gr, stl, kBatchChunk);
+          else xg::k_tma_batch<T, I, 4, false, 1, false><<<ntw, xg::kItThreads, sm, st>>>(vg, l.tw[side], mp, bx, gr, stl, kBatchChunk);
+        }
+        ++launched;
+      }
       if (nsh) {
         const xg::ShellBoxes *sb = b->vshell[side] + base;
         if (b->ct) {
@@ -2903,21 +3089,21 @@ void batch_enqueue_t(xfdtd_batch *b, long long s) {
   volume(true);
   const auto *tp = static_cast<const xg::TfsfSurfParams<T> *>(b->tsurf);
   if (b->n_te) {
-    xg::k_tfsf_batch<T, true><<<persistent_grid(b, b->n_te, 8), 256, 0, st>>>(tp, b->it_te, b->n_te);
+    xg::k_tfsf_batch<T, true><<<b->n_te, 256, 0, st>>>(tp, b->it_te);
     ++launched;
   }
   volume(false);
   if (b->n_th) {
-    xg::k_tfsf_batch<T, false><<<persistent_grid(b, b->n_th, 8), 256, 0, st>>>(tp, b->it_th, b->n_th);
+    xg::k_tfsf_batch<T, false><<<b->n_th, 256, 0, st>>>(tp, b->it_th);
     ++launched;
   }
   const auto *np = static_cast<const xg::NfParams<T> *>(b->nfp);
   if (b->n_nf) {
-    xg::k_nffft_batch<T><<<persistent_grid(b, b->n_nf, 8), 256, 0, st>>>(np, b->nf_grid, b->it_nf, b->n_nf);
+    xg::k_nffft_batch<T><<<b->n_nf, 256, 0, st>>>(np, b->nf_grid, b->it_nf);
     ++launched;
     if ((s + 1) % xg::kMaxNfBatch == 0) {
-      xg::k_nffft_fold_batch<T><<<persistent_grid(b, b->n_fold, 8), 256, 0, st>>>(
-          np, b->nf_nb, b->it_fold, b->n_fold, static_cast<int>(s + 1 - b->nf_done));
+      xg::k_nffft_fold_batch<T><<<b->n_fold, 256, 0, st>>>(np, b->nf_nb, b->it_fold,
+                                                           static_cast<int>(s + 1 - b->nf_done));
       ++launched;
       b->nf_done = s + 1;
     }
@@ -3110,6 +3296,12 @@ int xfdtd_batch_status(xfdtd_batch *b, int *n_running, int64_t *clock, int64_t *
   if (n_running) *n_running = r;
   if (clock) *clock = b->clock;
   if (launches) *launches = b->launches;
+  return XFDTD_OK;
+}
+
+int xfdtd_batch_tma_members(xfdtd_batch *b, int *n) {
+  if (!b) return XFDTD_ERR_STATE;
+  if (n) *n = b->n_tma;
   return XFDTD_OK;
 }
 

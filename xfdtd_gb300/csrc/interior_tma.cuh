@@ -141,9 +141,9 @@ struct ItBlock {
   int k0, khi, j0, ia, ib;
 };
 template <int MODE, int KT>
-__device__ __forceinline__ ItBlock it_block(const InteriorBox &in, int chunk) {
+__device__ __forceinline__ ItBlock it_block(const InteriorBox &in, int chunk, uint3 bid) {
   ItBlock b;
-  const int t = static_cast<int>(blockIdx.x);
+  const int t = static_cast<int>(bid.x);
   if (MODE == 2) {
     const int nlo = (in.pz_lo + KT - 1) / KT;
     const bool below = t < nlo;
@@ -153,8 +153,8 @@ __device__ __forceinline__ ItBlock it_block(const InteriorBox &in, int chunk) {
     b.k0 = in.lo[2] + t * KT;
     b.khi = in.hi[2];
   }
-  b.j0 = in.lo[1] + static_cast<int>(blockIdx.y) * (kItThreads / KT);
-  b.ia = in.lo[0] + static_cast<int>(blockIdx.z) * chunk;
+  b.j0 = in.lo[1] + static_cast<int>(bid.y) * (kItThreads / KT);
+  b.ia = in.lo[0] + static_cast<int>(bid.z) * chunk;
   b.ib = min(b.ia + chunk, in.hi[0] + 1);
   return b;
 }
@@ -185,15 +185,17 @@ struct ItRing {
   }
 };
 
-template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK, bool TF = false, int MINB = 1>
-__global__ void __launch_bounds__(kItThreads, MINB) k_interior_tma_e(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
-                                                               InteriorBox in, int chunk, int *status,
-                                                               int wait_limit, const __grid_constant__ TfsfFuse fz) {
+// The E update of one block: tile `bid` (k tile, j tile, chunk of planes)
+// of the launch over box `in`.  `maps` may lie in the launch's parameter
+// space or in global memory (the batched launches).
+template <typename T, typename I, int STAGES, bool CT, int MODE, int KT, bool TF>
+__device__ __forceinline__ void it_e_block(const ItMaps &maps, const VolCore<T, I> &p, const InteriorBox &in,
+                                           int chunk, int *status, int wait_limit, const TfsfFuse &fz, uint3 bid) {
   using G = ItTiles<T, I, KT>;
   extern __shared__ __align__(128) unsigned char smem[];
   ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::E_STAGE), wait_limit};
   const int tid = threadIdx.x, c = tid % KT, r = tid / KT;
-  const ItBlock blk = it_block<MODE, KT>(in, chunk);
+  const ItBlock blk = it_block<MODE, KT>(in, chunk, bid);
   if (blk.ia >= blk.ib) return;
   auto stage_of = [&](int q) { return (q - blk.ia + 1) % STAGES; };   // plane ia-1 in stage 0
   auto htile = [&](int st, int comp) { return reinterpret_cast<const T *>(smem + st * G::E_STAGE + comp * G::EH_TILE); };
@@ -316,15 +318,15 @@ __global__ void __launch_bounds__(kItThreads, MINB) k_interior_tma_e(const __gri
   }
 }
 
-template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK, bool TF = false, int MINB = 1>
-__global__ void __launch_bounds__(kItThreads, MINB) k_interior_tma_h(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
-                                                               InteriorBox in, int chunk, int *status,
-                                                               int wait_limit, const __grid_constant__ TfsfFuse fz) {
+// The H update of one block (as it_e_block).
+template <typename T, typename I, int STAGES, bool CT, int MODE, int KT, bool TF>
+__device__ __forceinline__ void it_h_block(const ItMaps &maps, const VolCore<T, I> &p, const InteriorBox &in,
+                                           int chunk, int *status, int wait_limit, const TfsfFuse &fz, uint3 bid) {
   using G = ItTiles<T, I, KT>;
   extern __shared__ __align__(128) unsigned char smem[];
   ItRing<STAGES> ring{reinterpret_cast<uint64_t *>(smem + STAGES * G::H_STAGE), wait_limit};
   const int tid = threadIdx.x, c = tid % KT, r = tid / KT;
-  const ItBlock blk = it_block<MODE, KT>(in, chunk);
+  const ItBlock blk = it_block<MODE, KT>(in, chunk, bid);
   if (blk.ia >= blk.ib) return;
   auto stage_of = [&](int q) { return (q - blk.ia) % STAGES; };
   auto etile = [&](int st, int comp) { return reinterpret_cast<const T *>(smem + st * G::H_STAGE + comp * G::HE_TILE); };
@@ -443,6 +445,20 @@ __global__ void __launch_bounds__(kItThreads, MINB) k_interior_tma_h(const __gri
     for (int q = waited + 1; q <= issued; ++q) ring.wait(stage_of(q));
     if (failed || ring.timed_out) atomicExch(status, static_cast<int>(4));   // XFDTD_ERR_TIMEOUT
   }
+}
+
+template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK, bool TF = false, int MINB = 1>
+__global__ void __launch_bounds__(kItThreads, MINB) k_interior_tma_e(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
+                                                                     InteriorBox in, int chunk, int *status,
+                                                                     int wait_limit, const __grid_constant__ TfsfFuse fz) {
+  it_e_block<T, I, STAGES, CT, MODE, KT, TF>(maps, p, in, chunk, status, wait_limit, fz, blockIdx);
+}
+
+template <typename T, typename I, int STAGES, bool CT, int MODE, int KT = kItK, bool TF = false, int MINB = 1>
+__global__ void __launch_bounds__(kItThreads, MINB) k_interior_tma_h(const __grid_constant__ ItMaps maps, VolCore<T, I> p,
+                                                                     InteriorBox in, int chunk, int *status,
+                                                                     int wait_limit, const __grid_constant__ TfsfFuse fz) {
+  it_h_block<T, I, STAGES, CT, MODE, KT, TF>(maps, p, in, chunk, status, wait_limit, fz, blockIdx);
 }
 
 }  // namespace xg

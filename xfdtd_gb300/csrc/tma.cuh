@@ -1,6 +1,6 @@
-// tma.cuh -- the few sm_90+/sm_100 asynchronous-copy primitives the fused
-// sweep uses, as inline PTX: mbarrier transaction barriers and tiled
-// cp.async.bulk.tensor loads from a CUtensorMap into shared memory.
+// tma.cuh -- the few sm_90+/sm_100 asynchronous-copy primitives the
+// TMA-staged kernels use, as inline PTX: mbarrier transaction barriers and
+// tiled cp.async.bulk.tensor loads from a CUtensorMap into shared memory.
 #pragma once
 
 #include <cuda.h>
@@ -23,6 +23,13 @@ __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier
 // Orders this thread's earlier generic-proxy shared-memory accesses before
 // later asynchronous-proxy ones (a TMA write into a buffer just read).
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Acquires a tensor map that lies in global memory, written there by the
+// host (cudaMemcpy) before the launch, for this thread's later TMA copies
+// through it.
+__device__ __forceinline__ void fence_tensormap_acquire(const void *map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(map) : "memory");
+}
 
 // One arrival that also announces `bytes` of transactions to come.
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes) {
