@@ -334,6 +334,21 @@ int xfdtd_transfer_bytes(xfdtd_handle *h, int64_t *h2d, int64_t *d2h);
  * bits.  No counterpart in the reference. */
 int xfdtd_set_tfsf_fusion(xfdtd_handle *h, int e_on, int h_on);
 int xfdtd_tfsf_fusion(xfdtd_handle *h, int active[2]);
+/* The schedule of the NF-FF running DFT's sampling
+ * (src/nffft/nffft_fd.cpp:108-203 samples E and H on the Huygens box after
+ * every step).  Split (1): the E half of step t's samples runs on its own
+ * stream beside step t's H update, the H half beside step t+1's E update,
+ * with the fold of each batch of 8 steps.  One launch (0): the samples in
+ * one launch after the H update (beside the TFSF H corrections where their
+ * cells are disjoint), the fold on the engine's stream.  The autotuner
+ * times both with the kept volume kernels and keeps the faster;
+ * set_nffft_split fixes one (taking any pending samples first).
+ * xfdtd_nffft_split reports the schedule in use and, in ms[2] (may be
+ * null), the autotuner's trial step times of the split and one-launch
+ * forms (0 when not timed).  Both give the same bits.  No counterpart in
+ * the reference. */
+int xfdtd_set_nffft_split(xfdtd_handle *h, int on);
+int xfdtd_nffft_split(xfdtd_handle *h, int *on, float ms[2]);
 /* Wall time of xfdtd_create, in ms: ms[0] validation, device allocation
  * and upload of the tables; ms[1] autotuning (0 without
  * XFDTD_FLAG_AUTOTUNE).  No counterpart in the reference. */

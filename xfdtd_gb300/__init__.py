@@ -100,6 +100,8 @@ def libs():
         cu.xfdtd_create_times.argtypes = [C.c_void_p, dp]
         cu.xfdtd_set_tfsf_fusion.argtypes = [C.c_void_p, C.c_int, C.c_int]
         cu.xfdtd_tfsf_fusion.argtypes = [C.c_void_p, P(C.c_int)]
+        cu.xfdtd_set_nffft_split.argtypes = [C.c_void_p, C.c_int]
+        cu.xfdtd_nffft_split.argtypes = [C.c_void_p, P(C.c_int), P(C.c_float)]
         cu.xfdtd_last_error.argtypes = [C.c_void_p]
         cu.xfdtd_last_error.restype = C.c_char_p
         cu.xfdtd_version.restype = C.c_char_p
@@ -400,6 +402,19 @@ class Simulation:
         a = (C.c_int * 2)()
         self._check_engine(libs()[0].xfdtd_tfsf_fusion(self.engine, a))
         return bool(a[0]), bool(a[1])
+
+    def set_nffft_split(self, on: bool):
+        """Fix the NF-FF sampling schedule: split halves beside the volume
+        updates (True) or one launch after the H update (False)."""
+        self._check_engine(libs()[0].xfdtd_set_nffft_split(self.engine, int(bool(on))))
+
+    def nffft_split(self) -> dict:
+        """The NF-FF sampling schedule in use and the autotuner's trial step
+        times of the split and one-launch forms (ms; 0 = not timed)."""
+        on = C.c_int()
+        ms = (C.c_float * 2)()
+        self._check_engine(libs()[0].xfdtd_nffft_split(self.engine, C.byref(on), ms))
+        return {"split": bool(on.value), "trial_ms_split": ms[0], "trial_ms_one_launch": ms[1]}
 
     def set_wait_limit(self, polls: int):
         """Polls of each TMA plane wait before a block gives up and reports a

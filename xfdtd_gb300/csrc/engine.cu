@@ -106,6 +106,11 @@ struct xfdtd_handle {
   cudaStream_t nfs = nullptr;
   cudaEvent_t ev_nfs_fork = nullptr, ev_nfh = nullptr, ev_nfe = nullptr;
   bool nf_pending = false;
+  // the split NF-FF schedule (two sampling halves and the batch folds on
+  // nfs, beside the volume updates); else one sampling launch after the H
+  // update, with the fold on the main stream.  Chosen by the autotuner.
+  bool nf_split = true;
+  float nf_sched_ms[2] = {0.f, 0.f};   // trial step time split / one launch (0 = not timed)
   cudaStream_t shell = nullptr;           // the volume shell kernels run here, beside the interior kernels
   cudaEvent_t ev_vfork[2] = {}, ev_vjoin[2] = {};
   std::vector<void *> allocs;
@@ -931,6 +936,12 @@ void interior_tma_setup(xfdtd_handle *h) {
       attr(xg::k_interior_tma_h<T, I, 6, false, M, KT, true>, GG::template smem_h<6>());
       attr(xg::k_interior_tma_h<T, I, 4, true, M, KT, true>, GG::template smem_h<4>());
     }
+    if constexpr (M == 1 && sizeof(T) == 4) {   // the wide launches capped at 5 blocks per SM (FP32)
+      attr(xg::k_interior_tma_e<T, I, 4, false, M, KT, false, 5>, GG::template smem_e<4>());
+      attr(xg::k_interior_tma_h<T, I, 4, false, M, KT, false, 5>, GG::template smem_h<4>());
+      attr(xg::k_interior_tma_e<T, I, 4, true, M, KT, false, 5>, GG::template smem_e<4>());
+      attr(xg::k_interior_tma_h<T, I, 4, true, M, KT, false, 5>, GG::template smem_h<4>());
+    }
     if constexpr (M == 2) {   // the capped z-edge launches
       attr(xg::k_interior_tma_e<T, I, 4, false, M, KT, false, 5>, GG::template smem_e<4>());
       attr(xg::k_interior_tma_h<T, I, 4, false, M, KT, false, 5>, GG::template smem_h<4>());
@@ -973,12 +984,15 @@ void launch_vol_tma(xfdtd_handle *h, const xg::VolParams<T, I> &p, bool e_side, 
   }
   const unsigned smem = e_side ? G::template smem_e<S>() : G::template smem_h<S>();
   if constexpr (MODE != 0) {
+    // the launches with the TFSF corrections folded in keep their registers
+    // in the wide interior launch (capped, the out-of-line calls would spill)
+    constexpr int MB = MODE == 1 ? 1 : MINB;
     if (fz.on) {
       if (e_side)
-        xg::k_interior_tma_e<T, I, S, CT, MODE, KT, true, MINB><<<grid, xg::kItThreads, smem, st>>>(
+        xg::k_interior_tma_e<T, I, S, CT, MODE, KT, true, MB><<<grid, xg::kItThreads, smem, st>>>(
             maps[0], p, in, chunk, h->d_status, h->wait_polls, fz);
       else
-        xg::k_interior_tma_h<T, I, S, CT, MODE, KT, true, MINB><<<grid, xg::kItThreads, smem, st>>>(
+        xg::k_interior_tma_h<T, I, S, CT, MODE, KT, true, MB><<<grid, xg::kItThreads, smem, st>>>(
             maps[1], p, in, chunk, h->d_status, h->wait_polls, fz);
       return;
     }
@@ -1008,9 +1022,12 @@ void launch_volume(xfdtd_handle *h, bool e_side, int var = -1) {
   auto p = vol_params<T, I>(h);
   if (v.stages) {
     if (v.wide) {
+      // FP32: the 4-stage launches capped at 5 resident blocks per SM (48
+      // registers, no spills; their shared memory allows 5)
+      constexpr int MB = sizeof(T) == 4 ? 5 : 1;
       if (v.stages == 6) launch_vol_tma<T, I, 6, false, 1>(h, p, e_side, v.chunk, h->stream);
-      else if (v.ct) launch_vol_tma<T, I, 4, true, 1>(h, p, e_side, v.chunk, h->stream);
-      else launch_vol_tma<T, I, 4, false, 1>(h, p, e_side, v.chunk, h->stream);
+      else if (v.ct) launch_vol_tma<T, I, 4, true, 1, xg::kItK, MB>(h, p, e_side, v.chunk, h->stream);
+      else launch_vol_tma<T, I, 4, false, 1, xg::kItK, MB>(h, p, e_side, v.chunk, h->stream);
     } else {
       if (v.stages == 6) launch_vol_tma<T, I, 6, false, 0>(h, p, e_side, v.chunk, h->stream);
       else if (v.ct) launch_vol_tma<T, I, 4, true, 0>(h, p, e_side, v.chunk, h->stream);
@@ -1080,7 +1097,7 @@ struct TuneCand {
 };
 
 template <typename T, typename I>
-void trial_step(xfdtd_handle *h);
+void trial_step(xfdtd_handle *h, bool nf_split = true);
 
 template <typename T, typename I>
 void autotune_t(xfdtd_handle *h, int trials) {
@@ -1240,6 +1257,20 @@ void autotune_t(xfdtd_handle *h, int trials) {
     h->tune_step_ms = t[be][bh];
     h->tune_ms[0][cands[0][be].v] = cands[0][be].ms;
     h->tune_ms[1][cands[1][bh].v] = cands[1][bh].ms;
+  }
+  // The NF-FF schedule: the split sampling halves beside the volume
+  // updates, or one sampling launch after the H update (beside the TFSF H
+  // corrections where it can), timed with the kept pairing, twice in turn.
+  // Beside a bandwidth-bound volume launch the halves can cost it more
+  // than they save.
+  if (!forced && h->nffft && !h->nf_bb) {
+    float ts[2] = {1e30f, 1e30f};
+    for (int pass = 0; pass < 2; ++pass)
+      for (int sp = 0; sp < 2; ++sp)
+        ts[sp] = std::min(ts[sp], time_n([&] { trial_step<T, I>(h, sp == 0); }, 2 * trials));
+    h->nf_sched_ms[0] = ts[0];
+    h->nf_sched_ms[1] = ts[1];
+    h->nf_split = ts[0] <= ts[1];
   }
   h->sweep = was_sweep;
   h->launch_count = launches;
@@ -1450,8 +1481,8 @@ void volume_pair(xfdtd_handle *h, bool e_side) {
 // writes zeros where there were zeros (the samples of step 0 are taken
 // again, from the fields, by the first step).
 template <typename T, typename I>
-void trial_step(xfdtd_handle *h) {
-  const bool split = h->nffft && !h->nf_bb;
+void trial_step(xfdtd_handle *h, bool nf_split) {
+  const bool split = h->nffft && !h->nf_bb && nf_split;
   if (split) {
     XCHECK(cudaEventRecord(h->ev_nfs_fork, h->stream));
     XCHECK(cudaStreamWaitEvent(h->nfs, h->ev_nfs_fork, 0));
@@ -1468,7 +1499,19 @@ void trial_step(xfdtd_handle *h) {
     XCHECK(cudaStreamWaitEvent(h->stream, h->ev_nfh, 0));
   }
   volume_pair<T, I>(h, false);
+  // the one-launch schedule: the samples beside the TFSF H corrections on
+  // the side stream when their cells are disjoint, else after them
+  const bool one = h->nffft && !h->nf_bb && !split;
+  const bool beside = one && h->tfsf && h->nf_beside_tfsf;
+  if (beside) {
+    XCHECK(cudaEventRecord(h->ev_nf_fork, h->stream));
+    XCHECK(cudaStreamWaitEvent(h->side, h->ev_nf_fork, 0));
+    launch_nffft<T>(h, h->side);
+    XCHECK(cudaEventRecord(h->ev_nf_join, h->side));
+  }
   if (h->tfsf && !tfsf_fused(h, 1)) launch_tfsf_side<T>(h, false);
+  if (beside) XCHECK(cudaStreamWaitEvent(h->stream, h->ev_nf_join, 0));
+  else if (one) launch_nffft<T>(h);
   if (split) XCHECK(cudaStreamWaitEvent(h->stream, h->ev_nfe, 0));
 }
 
@@ -1478,7 +1521,7 @@ void enqueue_step_t(xfdtd_handle *h, long long s, bool pre) {
   // (nfs): the E half beside this step's H update, the H half beside the
   // next step's E update; a full batch is folded there too, after the H half
   // of its last step.  (Broadband NF-FF and the fused sweep keep one launch.)
-  const bool split = h->nffft && !h->nf_bb && !h->sweep;
+  const bool split = h->nffft && !h->nf_bb && !h->sweep && h->nf_split;
   bool wait_nfh = false;
   if (h->nffft && !h->nf_bb && h->nf_pending && pre) {
     XCHECK(cudaEventRecord(h->ev_nfs_fork, h->stream));
@@ -2322,7 +2365,7 @@ void do_steps(xfdtd_handle *h, long long n) {
       XCHECK(cudaGraphLaunch(h->gexec, h->stream));
       h->host_step += h->graph_steps;
       h->launch_count += h->graph_launches;
-      if (h->nffft && !h->nf_bb && !h->sweep) {   // split sampling: the last batch and H half wait
+      if (h->nffft && !h->nf_bb && !h->sweep && h->nf_split) {   // split sampling: the last batch and H half wait
         h->nf_done = h->host_step - B;
         h->nf_pending = true;
       } else if (h->nffft) {
@@ -2708,6 +2751,28 @@ int xfdtd_set_tfsf_fusion(xfdtd_handle *h, int e_on, int h_on) {
       h->gexec = nullptr;
     }
   });
+}
+
+int xfdtd_set_nffft_split(xfdtd_handle *h, int on) {
+  if (!h) return XFDTD_ERR_STATE;
+  return guarded(h, [&] {
+    nffft_flush(h);   // no H half left pending across the switch
+    h->nf_split = on != 0;
+    if (h->gexec) {   // the captured graph holds the old launches
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+    }
+  });
+}
+
+int xfdtd_nffft_split(xfdtd_handle *h, int *on, float ms[2]) {
+  if (!h || !on) return XFDTD_ERR_STATE;
+  *on = (h->nffft && !h->nf_bb && h->nf_split) ? 1 : 0;
+  if (ms) {
+    ms[0] = h->nf_sched_ms[0];
+    ms[1] = h->nf_sched_ms[1];
+  }
+  return XFDTD_OK;
 }
 
 int xfdtd_tfsf_fusion(xfdtd_handle *h, int active[2]) {
@@ -3344,6 +3409,12 @@ struct AdjointState {
   size_t ck_bytes = 0;
   void *lE[3] = {}, *lH[3] = {}, *m[12] = {};
   double *g_eps = nullptr, *g_sig = nullptr, *dtab = nullptr;
+  void *sc = nullptr, *isc = nullptr;    // per table entry: s and 1/s of the six components (adjoint.cuh)
+  uint8_t *aflags_x = nullptr;           // x-axis flags with kAdjGeneral on the planes that need it
+  // the reverse steps run on their own stream, beside the re-run of the
+  // segment before on the engine's stream (two record buffers)
+  cudaStream_t rs = nullptr;
+  cudaEvent_t ev_ready = nullptr, ev_rec[2] = {nullptr, nullptr}, ev_rev[2] = {nullptr, nullptr};
   double loss = 0;
   bool forward_done = false;
   int device = 0;
@@ -3358,6 +3429,12 @@ struct AdjointState {
   }
   ~AdjointState() {
     cudaSetDevice(device);
+    if (rs) {
+      cudaStreamSynchronize(rs);
+      cudaStreamDestroy(rs);
+    }
+    for (cudaEvent_t e : {ev_ready, ev_rec[0], ev_rec[1], ev_rev[0], ev_rev[1]})
+      if (e) cudaEventDestroy(e);
     for (void *p : allocs) cudaFree(p);
   }
 };
@@ -3457,7 +3534,7 @@ void adj_forward_t(xfdtd_handle *h, const xfdtd_adjoint_desc *d, double *loss) {
   a->pn[1] = static_cast<int>(d->plane_hi[1] - d->plane_lo[1]);
   a->K = d->checkpoint_every;
   const long long T_ = h->total;
-  a->slots = a->K > 0 ? a->K : static_cast<int>(T_);
+  a->slots = a->K > 0 ? 2 * a->K : static_cast<int>(T_);   // two record buffers of K steps each
   for (int c = 0; c < 3; ++c) {
     a->recE[c] = a->alloc(static_cast<size_t>(a->slots) * a->nE * sizeof(T));
     a->recH[c] = a->alloc(static_cast<size_t>(a->slots) * a->nH * sizeof(T));
@@ -3474,12 +3551,24 @@ void adj_forward_t(xfdtd_handle *h, const xfdtd_adjoint_desc *d, double *loss) {
     cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
   }
-  for (long long t = 0; t < T_; ++t) {
+  // Steps that record nothing (between checkpoints, before the loss
+  // window) go through do_steps, which replays captured graphs where it can;
+  // the others one at a time with their records.
+  for (long long t = 0; t < T_;) {
     if (a->K > 0 && t % a->K == 0) adj_checkpoint(h, a->ck[t / a->K], true);
-    if (a->K == 0) adj_record_design<T>(h, a.get(), static_cast<int>(t));
-    enqueue_step(h, t);
-    h->host_step = t + 1;
-    if (t >= d->t_begin && t < d->t_end) adj_record_plane<T>(h, a.get(), t - d->t_begin);
+    const bool plane = t >= d->t_begin && t < d->t_end;
+    if (a->K == 0 || plane) {
+      if (a->K == 0) adj_record_design<T>(h, a.get(), static_cast<int>(t));
+      enqueue_step(h, t);
+      h->host_step = t + 1;
+      if (plane) adj_record_plane<T>(h, a.get(), t - d->t_begin);
+      ++t;
+      continue;
+    }
+    long long next = std::min(T_, (t / a->K + 1) * a->K);
+    if (d->t_begin > t) next = std::min<long long>(next, d->t_begin);
+    do_steps(h, next - t);
+    t = next;
   }
   if (a->K > 0) adj_checkpoint(h, a->ck.back(), true);
   prof_collect(h);
@@ -3537,8 +3626,60 @@ void adj_backward_t(xfdtd_handle *h, double *g_eps, double *g_sig) {
     XCHECK(cudaStreamSynchronize(h->stream));
   }
 
+  if (!a->sc) {   // scales of the stored adjoint fields and the planes that need the general path
+    const size_t nm = static_cast<size_t>(h->n_mat);
+    std::vector<T> sc(6 * nm), isc(6 * nm);
+    std::vector<uint8_t> nc(nm, 0);
+    for (size_t q = 0; q < nm; ++q)
+      for (int side = 0; side < 2; ++side) {
+        const double *c = h->table_host.data() + q * XFDTD_N_COEFF + 9 * side;
+        T t[9];
+        for (int r = 0; r < 9; ++r) t[r] = static_cast<T>(c[r]);
+        // the shape the fast path assumes: c0 = c3 = c6, c1 = c4 = c7 = -s, c2 = c5 = c8 = s, s != 0
+        const bool fast = t[2] != T(0) && t[1] == -t[2] && t[0] == t[3] && t[0] == t[6] && t[1] == t[4] &&
+                           t[1] == t[7] && t[2] == t[5] && t[2] == t[8];
+        if (!fast) nc[q] = 1;
+        for (int comp = 0; comp < 3; ++comp) {
+          const T s = t[2 + 3 * comp] != T(0) ? t[2 + 3 * comp] : T(1);
+          sc[6 * q + 3 * side + comp] = s;
+          isc[6 * q + 3 * side + comp] = T(1) / s;
+        }
+      }
+    a->sc = a->alloc(sc.size() * sizeof(T));
+    a->isc = a->alloc(isc.size() * sizeof(T));
+    XCHECK(cudaMemcpyAsync(a->sc, sc.data(), sc.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+    XCHECK(cudaMemcpyAsync(a->isc, isc.data(), isc.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+    const int nx = h->d.nx;
+    std::vector<uint8_t> fl = h->axis_flags_host[0];
+    if (std::find(nc.begin(), nc.end(), uint8_t(1)) != nc.end()) {
+      auto *d_nc = static_cast<uint8_t *>(a->alloc(nm));
+      auto *d_mark = static_cast<int *>(a->alloc((nx + 1) * sizeof(int)));
+      XCHECK(cudaMemcpyAsync(d_nc, nc.data(), nm, cudaMemcpyHostToDevice, h->stream));
+      XCHECK(cudaMemsetAsync(d_mark, 0, (nx + 1) * sizeof(int), h->stream));
+      dim3 block(32, 8, 1), grid((h->d.nz + 32) / 32, (h->d.ny + 8) / 8, nx + 1);
+      xg::k_adj_mark<I><<<grid, block, 0, h->stream>>>(static_cast<const I *>(h->idx), h->d, d_nc, d_mark);
+      XCHECK(cudaGetLastError());
+      std::vector<int> mark(nx + 1);
+      XCHECK(cudaMemcpyAsync(mark.data(), d_mark, mark.size() * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+      XCHECK(cudaStreamSynchronize(h->stream));
+      for (int q = 0; q <= nx; ++q)
+        if (mark[q]) fl[q] |= xg::kAdjGeneral;
+    }
+    a->aflags_x = static_cast<uint8_t *>(a->alloc(fl.size()));
+    XCHECK(cudaMemcpyAsync(a->aflags_x, fl.data(), fl.size(), cudaMemcpyHostToDevice, h->stream));
+    XCHECK(cudaStreamCreateWithFlags(&a->rs, cudaStreamNonBlocking));
+    XCHECK(cudaEventCreateWithFlags(&a->ev_ready, cudaEventDisableTiming));
+    for (int q = 0; q < 2; ++q) {
+      XCHECK(cudaEventCreateWithFlags(&a->ev_rec[q], cudaEventDisableTiming));
+      XCHECK(cudaEventCreateWithFlags(&a->ev_rev[q], cudaEventDisableTiming));
+    }
+  }
+
   xg::AdjParams<T, I> p{};
   p.v = vol_params<T, I>(h);
+  p.v.flags[0] = a->aflags_x;
+  p.sc = static_cast<const T *>(a->sc);
+  p.isc = static_cast<const T *>(a->isc);
   for (int c = 0; c < 3; ++c) {
     p.lE[c] = static_cast<T *>(a->lE[c]);
     p.lH[c] = static_cast<T *>(a->lH[c]);
@@ -3560,8 +3701,38 @@ void adj_backward_t(xfdtd_handle *h, double *g_eps, double *g_sig) {
     p.phi[q] = static_cast<int>(a->d.plane_hi[q]);
   }
   const long long T_ = h->total;
+  // k tiling per kernel (adjoint.cuh adj_k): the k whose gather reaches no
+  // special index (k_adj_h: k and k+1; k_adj_e: k and k-1, k >= 1)
+  const int nz = h->d.nz;
+  auto k_tiles = [&](bool e_side, xg::AdjParams<T, I> &q) {
+    const std::vector<uint8_t> &fz = h->axis_flags_host[2];
+    const uint8_t bits = xg::kSpecialE | xg::kSpecialH;
+    int lo = nz + 1, hi = nz;
+    for (int k = 0; k < nz; ++k) {
+      const bool ok = e_side ? (k >= 1 && !((fz[k] | fz[k - 1]) & bits)) : !((fz[k] | fz[k + 1]) & bits);
+      if (!ok) continue;
+      if (lo > nz) lo = k;
+      hi = k;
+    }
+    if (lo > nz) lo = 0, hi = -1;   // no plain k: one range over all k
+    q.kp_lo = lo;
+    q.kp_hi = hi;
+    q.kt_n0 = (lo + 31) / 32;
+    q.kt_n1 = (hi - lo + 1 + 31) / 32;
+    return static_cast<unsigned>(q.kt_n0 + q.kt_n1 + (nz - hi + 31) / 32);
+  };
+  xg::AdjParams<T, I> pe = p;
+  const unsigned gx_h = k_tiles(false, p), gx_e = k_tiles(true, pe);
+  const int kt_e[4] = {pe.kp_lo, pe.kp_hi, pe.kt_n0, pe.kt_n1};
+  const int kt_h[4] = {p.kp_lo, p.kp_hi, p.kt_n0, p.kt_n1};
+  auto use = [&](const int *kt) {
+    p.kp_lo = kt[0];
+    p.kp_hi = kt[1];
+    p.kt_n0 = kt[2];
+    p.kt_n1 = kt[3];
+  };
   dim3 block(32, 8, 1);
-  dim3 grid((h->d.nz + 32) / 32, (h->d.ny + 8) / 8, h->d.nx + 1);
+  dim3 grid_h(gx_h, (h->d.ny + 8) / 8, h->d.nx + 1), grid_e(gx_e, (h->d.ny + 8) / 8, h->d.nx + 1);
   auto plane_of = [&](long long t1) -> const T * {   // loss record of the field after step t1
     if (t1 < a->d.t_begin || t1 >= a->d.t_end) return nullptr;
     return static_cast<const T *>(a->plane) + static_cast<size_t>(t1 - a->d.t_begin) * a->pn[0] * a->pn[1];
@@ -3572,41 +3743,63 @@ void adj_backward_t(xfdtd_handle *h, double *g_eps, double *g_sig) {
       p.recH[c] = static_cast<const T *>(a->recH[c]) + static_cast<size_t>(slot) * a->nH;
     }
   };
+  const long long seg = a->K > 0 ? a->K : T_;
+  const long long n_seg = (T_ + seg - 1) / seg;
+  // Segment q covers steps [q seg, min(T, (q+1) seg)); with K > 0 its
+  // re-run records the design box into buffer q % 2.  The re-run of segment
+  // q-1 (engine stream) runs beside the reverse steps of segment q (rs): it
+  // waits for the reverse steps of segment q+1, the last reader of its
+  // buffer, and the reverse steps of segment q-1 wait for it.
+  const bool nffft = h->nffft;
+  const int n_probes = h->n_probes;
+  h->nffft = false;   // the NF-FF sums and probes of the forward pass are final
+  h->n_probes = 0;
+  auto rerun = [&](long long q) {
+    const long long s0 = q * seg, s1 = std::min(T_, s0 + seg);
+    if (q + 2 < n_seg) XCHECK(cudaStreamWaitEvent(h->stream, a->ev_rev[q % 2], 0));   // reverse(q + 2) done
+    adj_checkpoint(h, a->ck[q], false);
+    XCHECK(cudaMemcpyAsync(h->d_step, &s0, sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+    for (long long t = s0; t < s1; ++t) {
+      adj_record_design<T>(h, a, static_cast<int>((q % 2) * a->K + (t - s0)));
+      enqueue_step(h, t);
+    }
+    XCHECK(cudaEventRecord(a->ev_rec[q % 2], h->stream));
+  };
+  XCHECK(cudaEventRecord(a->ev_ready, h->stream));   // zeroed adjoint state, tables, flags
+  XCHECK(cudaStreamWaitEvent(a->rs, a->ev_ready, 0));
+  if (a->K > 0) rerun(n_seg - 1);
   // the loss gradient of the last step
   p.do_e_own = 0;
   p.do_gather = 1;
   p.plane_rec = plane_of(T_ - 1);
   set_rec(0);
-  xg::k_adj_e<T, I><<<grid, block, 0, h->stream>>>(p);
+  use(kt_e);
+  xg::k_adj_e<T, I><<<grid_e, block, 0, a->rs>>>(p);
   XCHECK(cudaGetLastError());
-  const bool nffft = h->nffft;
-  const int n_probes = h->n_probes;
-  const long long seg = a->K > 0 ? a->K : T_;
-  for (long long s0 = ((T_ - 1) / seg) * seg; s0 >= 0; s0 -= seg) {
-    const long long s1 = std::min(T_, s0 + seg);
-    if (a->K > 0) {   // re-run the segment from its checkpoint, recording the design box
-      adj_checkpoint(h, a->ck[s0 / a->K], false);
-      XCHECK(cudaMemcpyAsync(h->d_step, &s0, sizeof(long long), cudaMemcpyHostToDevice, h->stream));
-      h->nffft = false;   // the NF-FF sums and probes of the forward pass are final
-      h->n_probes = 0;
-      for (long long t = s0; t < s1; ++t) {
-        adj_record_design<T>(h, a, static_cast<int>(t - s0));
-        enqueue_step(h, t);
-      }
-      h->nffft = nffft;
-      h->n_probes = n_probes;
+  for (long long q = n_seg - 1; q >= 0; --q) {
+    const long long s0 = q * seg, s1 = std::min(T_, s0 + seg);
+    if (a->K > 0) {
+      XCHECK(cudaStreamWaitEvent(a->rs, a->ev_rec[q % 2], 0));
+      if (q >= 1) rerun(q - 1);
     }
     for (long long t = s1 - 1; t >= s0; --t) {
-      xg::k_adj_h<T, I><<<grid, block, 0, h->stream>>>(p);
+      use(kt_h);
+      xg::k_adj_h<T, I><<<grid_h, block, 0, a->rs>>>(p);
       XCHECK(cudaGetLastError());
-      set_rec(static_cast<int>(a->K > 0 ? t - s0 : t));
+      set_rec(static_cast<int>(a->K > 0 ? (q % 2) * a->K + (t - s0) : t));
       p.do_e_own = 1;
       p.do_gather = t >= 1 ? 1 : 0;
       p.plane_rec = t >= 1 ? plane_of(t - 1) : nullptr;
-      xg::k_adj_e<T, I><<<grid, block, 0, h->stream>>>(p);
+      use(kt_e);
+      xg::k_adj_e<T, I><<<grid_e, block, 0, a->rs>>>(p);
       XCHECK(cudaGetLastError());
     }
+    XCHECK(cudaEventRecord(a->ev_rev[q % 2], a->rs));
   }
+  h->nffft = nffft;
+  h->n_probes = n_probes;
+  XCHECK(cudaEventRecord(a->ev_ready, a->rs));
+  XCHECK(cudaStreamWaitEvent(h->stream, a->ev_ready, 0));
   if (a->K > 0) {   // back to the state after the last step
     adj_checkpoint(h, a->ck.back(), false);
     XCHECK(cudaMemcpyAsync(h->d_step, &T_, sizeof(long long), cudaMemcpyHostToDevice, h->stream));

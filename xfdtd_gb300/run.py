@@ -32,6 +32,11 @@ def main():
                     help="shell-kernel variants of the E and H updates (after the interior variants)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the autotuner's trials (with --kernel-variant, for profiling one launch per step)")
+    ap.add_argument("--tfsf-fusion", default="auto", choices=["auto", "on", "off"],
+                    help="TFSF corrections inside the wide TMA launches: the autotuner's choice, or fixed")
+    ap.add_argument("--nffft-split", default="auto", choices=["auto", "on", "off"],
+                    help="NF-FF sampling schedule: the autotuner's choice, split halves beside the volume "
+                         "updates (on) or one launch after the H update (off)")
     ap.add_argument("--out", default=None)
     ap.add_argument("--adjoint", action="store_true",
                     help="run the adjoint-gradient problem (forward with checkpoints, then backward) instead")
@@ -53,13 +58,18 @@ def main():
         sim.set_kernel_variant(*(int(v) for v in args.kernel_variant.split(",")))
     if args.shell_variant:
         sim.set_shell_variant(*(int(v) for v in args.shell_variant.split(",")))
+    if args.tfsf_fusion != "auto":
+        sim.set_tfsf_fusion(args.tfsf_fusion == "on", args.tfsf_fusion == "on")
+    if args.nffft_split != "auto":
+        sim.set_nffft_split(args.nffft_split == "on")
     t1 = time.perf_counter()
     ms = sim.step_timed(steps)
     sim.synchronize()
     cells = sim.n[0] * sim.n[1] * sim.n[2]
     res = {"config": args.config, "grid": sim.n, "steps": steps, "precision": args.precision,
            "setup_s": t1 - t0, "ms_per_step": ms / steps, "Mcell_updates_per_s": cells * steps / ms / 1e3,
-           "device_bytes": sim.device_bytes(), "volume_kernels": sim.kernel_variants()}
+           "device_bytes": sim.device_bytes(), "volume_kernels": sim.kernel_variants(),
+           "shell_variants": sim.shell_variants(), "tfsf_folded": sim.tfsf_fusion(), "nffft_schedule": sim.nffft_split()}
     if args.out:
         os.makedirs(args.out, exist_ok=True)
         sim.output()
