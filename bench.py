@@ -1,31 +1,35 @@
 """Benchmark of the FDTD step loop on GB300: Mcell-updates/s and the HBM
 roofline fraction of the dominant kernel, beside the CPU oracle.
 
-Workload: the dielectric-sphere scattering configuration -- 256^3 interior
-plus a 12-cell CPML per face (280^3 = 21,952,000 cells), dx = 2 mm, eps_r = 4
-sphere of radius 60 cells, TFSF x-polarised +z Gaussian plane wave
-(tau = 40 dt), NF-FF running DFT at 1, 2 and 3 GHz, 2000 steps -- in the FP32
-form (fields and CPML in FP32; TFSF 1-D grid, NF-FF accumulators and
-far-field integration in FP64).  Synthetic inputs of that shape (there is no
-dataset).  The fields (6 x 87.8 MB) are far larger than the 129 MB L2, so no
-flush is needed between steps.
+Workload (the headline): the bandwidth-bound heterogeneous medium, the
+largest benchmark configuration -- 512 x 512 x 384 interior plus a 10-cell
+CPML per face (532 x 532 x 404 = 114,341,696 cells), dx = 1 mm, voxel
+materials drawn from a seeded 256-entry table (eps_r U[1, 6], sigma
+U[0, 0.01] S/m), a z-directed soft point current source at the centre
+(Gaussian-modulated sine, f0 = 10 GHz, 5 GHz bandwidth), Ez probes at 64
+seeded cells, 1000 steps -- in its FP32 form (fields and CPML in FP32,
+probe series copied out in FP32), the form the configuration names, with
+the FP64 oracle as the check.  Synthetic inputs of that shape (there is no
+dataset).  Each field component (456 MB) is far larger than the 129 MB L2,
+so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 A step is one time step of the loop body over the whole grid.  value =
 (cells x steps x ranks) / max-over-ranks device time of the K timed steps
 (CUDA events on the engine's stream).  e2e = the same metric over the
-config's whole job (2000 steps) through the public API -- host scene ->
-plan lowering -> device allocation and upload -> autotuning -> steps -> far
-field and RCS copied back to the host -- wall clock, with each phase's
-time.  With --gpus N > 1 (torchrun), every rank runs an independent replica
-of the workload (the path has no exchange).
+configuration's whole job (1000 steps) through the public API -- host scene
+-> plan lowering -> device allocation and upload -> autotuning -> steps ->
+probe series copied back to the host -- wall clock, with each phase's time.
+With --gpus N > 1 (torchrun), every rank runs an independent replica of the
+workload (the path has no exchange).
 
-The same line carries the FP64 form (the reference's arithmetic) of the
-same workload, the heterogeneous-medium configuration (532 x 532 x 404
-cells) in FP32 and FP64, the batched and the adjoint forms, each with its
-own roofline and (where it is a whole job) end-to-end figures, and the
-FP32 form's error against the FP64 form on the same jobs.  GPU clocks are
+The same line carries the FP64 form of the headline (the reference's
+arithmetic: its e2e against the reference arm is the precision-matched
+ratio), the dielectric-sphere configuration (280^3 cells, TFSF, NF-FF and
+RCS) in FP32 and FP64, the batched and the adjoint forms, each with its own
+roofline and (where it is a whole job) end-to-end figures, and the FP32
+forms' errors against the FP64 forms on the same jobs.  GPU clocks are
 sampled by nvidia-smi over the whole run.
 
 --impl reference times the reference's algorithm on the host cores: the
@@ -51,7 +55,9 @@ sys.path.insert(0, ROOT)
 from xfdtd_gb300 import configs  # noqa: E402
 from xfdtd_gb300 import scene as S  # noqa: E402
 
-CONFIG_NAME = "dielectric_sphere"
+WORKLOAD = ("heterogeneous medium: 512 x 512 x 384 interior + 10-cell CPML (532 x 532 x 404 cells), dx 1 mm, "
+            "voxel materials from a seeded 256-entry table (eps_r U[1,6], sigma U[0,0.01] S/m), z-directed soft "
+            "point current source (Gaussian-modulated sine, 10 GHz, 5 GHz bandwidth), 64 Ez probes")
 METRIC = "Mcell-updates/s"
 UNIT = "Mcell-updates/s"
 
@@ -233,49 +239,51 @@ def _slab_layers(sc):
 
 
 # -------------------------------------------------------------------- arms ---
-def run_cpu_oracle(threads: int, sample_steps: int, scale: int = 1):
-    """FP64 CPU oracle on the same workload: init untimed, `sample_steps`
-    steps timed.  Returns (Mcell-updates/s, cores, sample description)."""
+def headline_config(world: int) -> dict:
+    """The workload both arms report on (the same dict on both lines)."""
+    return {"workload": WORKLOAD, "cells": 532 * 532 * 404, "grid": [532, 532, 404], "steps_per_job": 1000,
+            "l2": "no flush: inputs larger than L2 (each field component 456 MB in FP32, 912 MB in FP64, "
+                  "against the 129 MB L2)",
+            "parallelism": f"replicas x{world}"}
+
+
+def run_cpu_oracle(threads: int, sample_steps: int, scale: int = 2):
+    """FP64 CPU oracle on the headline workload at 1/`scale` per axis (the
+    same scene family and per-cell arithmetic): init untimed,
+    `sample_steps` steps timed.  Returns (Mcell-updates/s, cores, sample
+    description)."""
     import oracle
     oracle.build()
     cores = oracle.set_threads(threads)
-    sc, _ = configs.dielectric_sphere(scale=scale)
+    sc, _ = configs.heterogeneous(scale=scale)
     o = oracle.OracleSim(sc, sample_steps + 1)
     o.step(1)   # first touch
     t0 = time.perf_counter()
     o.step(sample_steps)
     dt = time.perf_counter() - t0
     cells = o.n[0] * o.n[1] * o.n[2]
+    grid = "x".join(str(v) for v in o.n)
     del o
-    return cells * sample_steps / dt / 1e6, cores, f"{sample_steps} steps of the {o_n(sc)} grid, {cores} thread(s), {dt:.1f} s"
-
-
-def o_n(sc):
-    return "x".join(str(v) for v in _grid_n(sc))
-
-
-def _grid_n(sc):
-    half = round(sc.objects[0].shape.size[0] / sc.cell_size)
-    t = sc.boundaries[0].thickness
-    return (half + 2 * t,) * 3
+    return cells * sample_steps / dt / 1e6, cores, (f"{sample_steps} steps of the {grid} grid (the heterogeneous "
+                                                    f"medium at 1/{scale} per axis), {cores} thread(s), {dt:.1f} s")
 
 
 def reference_arm(args, world, rank):
+    """The reference's algorithm (its FP64 CPU step loop, restated in
+    oracle/: the reference itself does not build here) on all host threads,
+    on the headline workload.  Each bench step is one oracle time step of
+    the heterogeneous-medium scene on a grid sized so that the whole
+    --warmup W --steps K run stays within about --ref-budget seconds."""
     base = {"metric": METRIC, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "dielectric sphere, 280^3 cells incl. 12-cell CPML, TFSF, NF-FF 3 freq",
-                       "cells": 280 ** 3}}
+            "dtype": "f64", "data": "synthetic", "config": headline_config(world)}
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     import oracle
     oracle.build()
     cores = oracle.set_threads(threads)
-    # Each bench step is one oracle time step of the same scene family on a
-    # grid sized so that the whole --warmup W --steps K run stays within
-    # about args.ref_budget seconds (calibrated on the 1/4-scale grid).
-    cal, _ = configs.dielectric_sphere(scale=4)
+    cal, _ = configs.heterogeneous(scale=8)   # calibration: seconds per cell-update
     oc = oracle.OracleSim(cal, 6)
     oc.step(1)
     t0 = time.perf_counter()
@@ -284,11 +292,12 @@ def reference_arm(args, world, rank):
     del oc
     budget_step = args.ref_budget / (args.warmup + args.steps)
     scale = 1
-    for s in (1, 2, 4):
+    for s in (1, 2, 4, 8):
         scale = s
-        if _grid_n(configs.dielectric_sphere(scale=s)[0])[0] ** 3 * per_cell <= budget_step:
+        nx, ny, nz = 512 // s + 20, 512 // s + 20, 384 // s + 20
+        if nx * ny * nz * per_cell <= budget_step:
             break
-    sc, _ = configs.dielectric_sphere(scale=scale)
+    sc, _ = configs.heterogeneous(scale=scale)
     o = oracle.OracleSim(sc, args.warmup + args.steps + 1)
     cells = o.n[0] * o.n[1] * o.n[2]
     o.step(1)
@@ -297,14 +306,16 @@ def reference_arm(args, world, rank):
     o.step(args.steps)
     tot = time.perf_counter() - t0
     v = cells * args.steps / tot / 1e6
+    grid = "x".join(map(str, o.n))
     line = dict(base)
-    line["config"] = dict(base["config"], sample_grid=list(o.n), sample_scale=scale)
     line.update({"value": v, "ms_per_step": 1e3 * tot / args.steps,
-                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                                  "sample": f"{args.steps} oracle steps of the {'x'.join(map(str, o.n))} grid "
-                                            f"(scale 1/{scale} of the workload), {cores} threads"},
+                 "cpu_baseline": dict({"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                       "sample": f"{args.steps} oracle steps (after {args.warmup} warm-up steps) of "
+                                                 f"the {grid} grid: the headline workload at 1/{scale} per axis, "
+                                                 f"{cores} threads"}, **_cpu_info()),
                  "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                 "note": "the reference does not build here; its FP64 algorithm is restated in oracle/"})
+                 "note": "the reference does not build here (xtensor, xtensor-blas, xtensor-fftw, FFTW3, BLAS and "
+                         "LAPACK are absent); its FP64 step loop is restated in oracle/"})
     print(json.dumps(line), flush=True)
 
 
@@ -429,7 +440,7 @@ def _timed(sc, precision, steps, warmup, local, grp=None, fused=False, variants=
         grp.barrier()
     out = {"n": tuple(n), "cells": n[0] * n[1] * n[2], "ms": ms, "launches": sim.launch_count() - l0,
            "variants": sim.kernel_variants(), "shell_variants": sim.shell_variants(), "split": sim.volume_split(),
-           "tfsf_folded": sim.tfsf_fusion(),
+           "tfsf_folded": sim.tfsf_fusion(), "nffft_schedule": sim.nffft_split(),
            "setup_steps": setup,
            "timed_path": f"{steps // GRAPH_STEPS} CUDA graph replays of {GRAPH_STEPS} steps + "
                          f"{steps % GRAPH_STEPS} single steps, after {warmup} warm-up steps and {setup} untimed "
@@ -449,6 +460,7 @@ def _profiled(sc, precision, steps, warmup, local, run, fused=False):
     psim.set_kernel_variant(run["variants"]["e"], run["variants"]["h"])
     psim.set_shell_variant(run["shell_variants"]["e"], run["shell_variants"]["h"])
     psim.set_tfsf_fusion(*run["tfsf_folded"])
+    psim.set_nffft_split(run["nffft_schedule"]["split"])
     assert psim.volume_split() == run["split"]
     assert psim.tfsf_fusion() == run["tfsf_folded"]
     psim.step(warmup)
@@ -532,55 +544,56 @@ def _probe_err(a, b):
     return {"probe_l2_max": float(rel.max()), "probe_l2_median": float(np.median(rel))}
 
 
-def run_fp64_form(args, local, sc, steps, fp32_rcs):
-    """The FP64 form (the reference's arithmetic) on the same workload:
-    timed steps, kernel roofline at 146 B per cell-update, a whole job end
-    to end, and the FP32 form's RCS error against it."""
-    run = _timed(sc, "fp64", args.fp64_steps, args.warmup, local)
-    roof, shares, _ = _profiled(sc, "fp64", min(args.fp64_steps, PROFILE_STEPS), args.warmup, local, run)
-    e2e, rcs64 = _e2e(sc, "fp64", steps, local)
-    return {"value": run["cells"] * args.fp64_steps / (run["ms"] / 1e3) / 1e6, "unit": UNIT,
-            "steps": args.fp64_steps, "ms_per_step": run["ms"] / args.fp64_steps, "dtype": "f64",
+def run_fp64_form(args, local, sc, timed_steps, job_steps, fp32_out, readout, fused):
+    """The FP64 form (the reference's arithmetic) of a workload: timed steps
+    through graph replay, the dominant kernel's roofline at 146 B per
+    cell-update, the whole job end to end, and the FP32 form's error
+    against it (probe series or RCS of the same job)."""
+    run = _timed(sc, "fp64", timed_steps, args.warmup, local, fused=fused)
+    roof, shares, _ = _profiled(sc, "fp64", min(timed_steps, PROFILE_STEPS), args.warmup, local, run, fused=fused)
+    e2e, out64 = _e2e(sc, "fp64", job_steps, local, fused=fused, readout=readout)
+    err = None
+    if fp32_out is not None:
+        err = dict(_rcs_err(fp32_out, out64) if readout == "rcs" else _probe_err(fp32_out, out64),
+                   against="this FP64 form, same job", steps=job_steps)
+    return {"value": run["cells"] * timed_steps / (run["ms"] / 1e3) / 1e6, "unit": UNIT,
+            "steps": timed_steps, "ms_per_step": run["ms"] / timed_steps, "dtype": "f64",
             "timed_path": run["timed_path"], "roofline": roof, "kernel_shares": shares, "e2e": e2e,
-            "fp32_form_error": dict(_rcs_err(fp32_rcs, rcs64), against="this FP64 form, same job",
-                                    steps=steps) if fp32_rcs is not None else None,
+            "fp32_form_error": err,
             "note": "GB300 runs FP64 at 1/64 of the FP32 rate: the FP64 volume kernels are bound by "
                     "the FP64 pipe, not by HBM (frac is of the copy bandwidth)"}
 
 
-def run_heterogeneous_form(args, local):
-    """The bandwidth-bound heterogeneous medium: 512 x 512 x 384 + 10-cell
-    CPML (532 x 532 x 404 cells), 256-entry voxel material table, soft point
-    source, 64 Ez probes.  FP32: `hetero_steps` steps timed through graph
-    replay, a profiled pass for the kernel times and roofline, and the
-    config's whole 1000-step job end to end; FP64 likewise (fewer timed
-    steps), with the FP32 probes' error against the FP64 job's."""
-    e2e_steps = args.hetero_e2e_steps
-    sc, _ = configs.heterogeneous(steps=e2e_steps)
-    run = _timed(sc, "fp32", args.hetero_steps, 3, local, fused=None)
-    roof, shares, conc = _profiled(sc, "fp32", args.hetero_steps, 3, local, run, fused=None)
-    out = {"grid": list(run["n"]), "cells": run["cells"], "steps": args.hetero_steps,
-           "value": run["cells"] * args.hetero_steps / (run["ms"] / 1e3) / 1e6, "unit": UNIT,
-           "ms_per_step": run["ms"] / args.hetero_steps, "dtype": "f32", "timed_path": run["timed_path"],
-           "roofline": roof, "kernel_shares": shares, "volume_kernels_concurrent": conc,
-           "variants": {"e": run["variants"]["e"], "h": run["variants"]["h"],
-                        "shell_e": run["shell_variants"]["e"], "shell_h": run["shell_variants"]["h"]},
-           "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (run["cells"] * 4 / 1e6)}
-    if e2e_steps > 0:
-        e2e, p32 = _e2e(sc, "fp32", e2e_steps, local, fused=None, readout="probes")
-        out["e2e"] = e2e
-    if args.hetero_fp64_steps > 0:
-        r64 = _timed(sc, "fp64", args.hetero_fp64_steps, 3, local, fused=None)
-        roof64, _, _ = _profiled(sc, "fp64", args.hetero_fp64_steps, 3, local, r64, fused=None)
-        f64 = {"value": r64["cells"] * args.hetero_fp64_steps / (r64["ms"] / 1e3) / 1e6, "unit": UNIT,
-               "steps": args.hetero_fp64_steps, "ms_per_step": r64["ms"] / args.hetero_fp64_steps, "dtype": "f64",
-               "roofline": roof64}
-        if e2e_steps > 0:
-            e64, p64 = _e2e(sc, "fp64", e2e_steps, local, fused=None, readout="probes")
-            f64["e2e"] = e64
-            out["fp32_form_error"] = dict(_probe_err(p32, p64), against="the FP64 form, same job",
-                                          steps=e2e_steps, probes=int(p64.shape[0]))
-        out["fp64_form"] = f64
+def run_dielectric_form(args, local):
+    """The dielectric-sphere scattering configuration: 256^3 interior +
+    12-cell CPML (280^3 cells), eps_r 4 sphere of radius 60 cells, TFSF
+    x-polarised +z Gaussian plane wave (tau = 40 dt), NF-FF DFT at 1, 2 and
+    3 GHz, bistatic RCS at 181 angles in two planes, 2000 steps.  FP32 form
+    (the benchmark spec's 70 % target): timed steps, roofline, the whole job end
+    to end; FP64 form likewise, with the FP32 RCS error against it."""
+    sc, job_steps = configs.dielectric_sphere()
+    fused = False   # the split E and H kernels (the fused sweep is slower on this grid)
+    run = _timed(sc, "fp32", args.dielectric_steps, args.warmup, local, fused=fused)
+    roof, shares, conc = _profiled(sc, "fp32", min(args.dielectric_steps, PROFILE_STEPS), args.warmup, local, run,
+                                   fused=fused)
+    e2e, rcs32 = _e2e(sc, "fp32", job_steps, local, fused=fused, readout="rcs")
+    v, sv = run["variants"], run["shell_variants"]
+    out = {"workload": "dielectric sphere scattering: 256^3 interior + 12-cell CPML (280^3 cells), dx 2 mm, "
+                       "eps_r 4 sphere r=60 cells, TFSF x-pol +z Gaussian, NF-FF 1/2/3 GHz",
+           "grid": list(run["n"]), "cells": run["cells"], "steps": args.dielectric_steps,
+           "value": run["cells"] * args.dielectric_steps / (run["ms"] / 1e3) / 1e6, "unit": UNIT,
+           "ms_per_step": run["ms"] / args.dielectric_steps, "dtype": "f32", "timed_path": run["timed_path"],
+           "launches": run["launches"], "roofline": roof, "kernel_shares": shares,
+           "volume_split_cells": run["split"], "volume_kernels_concurrent": conc,
+           "autotuned_variants": {"update_e": v["e"], "update_h": v["h"], "shell_e": sv["e"], "shell_h": sv["h"],
+                                  "tfsf_folded": {"e": run["tfsf_folded"][0], "h": run["tfsf_folded"][1]},
+                                  "nffft_schedule": run["nffft_schedule"],
+                                  "trial_ms_e": [round(q, 4) for q in v["trials_e"]],
+                                  "trial_ms_h": [round(q, 4) for q in v["trials_h"]]},
+           "e2e": e2e, "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (run["cells"] * 4 / 1e6)}
+    if args.dielectric_fp64_steps > 0:
+        out["fp64_form"] = run_fp64_form(args, local, sc, args.dielectric_fp64_steps, job_steps, rcs32, "rcs", fused)
+        out["fp32_form_error"] = out["fp64_form"]["fp32_form_error"]
     return out
 
 
@@ -614,35 +627,34 @@ def ours_arm(args, world, rank, local, grp):
     X.build()
     clock = ClockSampler(local)
     clock.start()
-    sc, config_steps = configs.dielectric_sphere()
+    sc, job_steps = configs.heterogeneous()
     fused = {"auto": None, "fused": True, "split": False}[args.volume]
     fixed = None
     if args.kernel_variant or args.shell_variant:
         fixed = (tuple(int(v) for v in (args.kernel_variant or "0,0").split(",")),
                  tuple(int(v) for v in (args.shell_variant or "0,0").split(",")))
-    # the headline: the FP32 form of the dielectric-sphere workload, timed
-    # steps through the production path
-    run = _timed(sc, args.precision, args.steps, args.warmup, local, grp=grp, fused=fused, variants=fixed)
+    # the headline: the FP32 form of the heterogeneous medium, timed steps
+    # through the production path
+    run = _timed(sc, "fp32", args.steps, args.warmup, local, grp=grp, fused=fused, variants=fixed)
     n, cells, split = run["n"], run["cells"], run["split"]
     max_ms = grp.max(run["ms"])
     value = aggregate_value(cells, args.steps, world, max_ms)
-    roof, shares, concurrent = _profiled(sc, args.precision, min(args.steps, PROFILE_STEPS), args.warmup, local, run,
+    roof, shares, concurrent = _profiled(sc, "fp32", min(args.steps, PROFILE_STEPS), args.warmup, local, run,
                                          fused=fused)
 
-    # e2e: the config's whole job through the public API, host scene to host RCS
+    # e2e: the config's whole job through the public API, host scene to host probe series
     grp.barrier()
-    e2e, rcs32 = _e2e(sc, args.precision, args.e2e_steps or config_steps, local, fused=fused)
+    e2e, p32 = _e2e(sc, "fp32", args.e2e_steps or job_steps, local, fused=fused, readout="probes")
     e2e_wall = grp.max(e2e["wall_s"])
     e2e["value"] = cells * e2e["steps"] * world / e2e_wall / 1e6
     e2e["wall_s"] = e2e_wall
 
     fp64 = None
     if args.fp64_steps > 0 and rank == 0:
-        fp64 = run_fp64_form(args, local, sc, args.e2e_steps or config_steps,
-                             rcs32 if args.precision == "fp32" else None)
+        fp64 = run_fp64_form(args, local, sc, args.fp64_steps, args.e2e_steps or job_steps, p32, "probes", fused)
+    dielectric = run_dielectric_form(args, local) if (args.dielectric_steps > 0 and rank == 0) else None
     batched = run_batched_form(args, local) if (args.batch_problems > 0 and rank == 0) else None
     adjoint = run_adjoint_form(args, local) if (args.adjoint and rank == 0) else None
-    hetero = run_heterogeneous_form(args, local) if (args.hetero_steps > 0 and rank == 0) else None
 
     cpu = None
     if rank == 0 and world == 1 and args.cpu_sample > 0:
@@ -657,14 +669,9 @@ def ours_arm(args, world, rank, local, grp):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
-        "data": "synthetic",
-        "config": {"workload": "dielectric sphere scattering: 256^3 interior + 12-cell CPML (280^3 cells), "
-                               "dx 2 mm, eps_r 4 sphere r=60 cells, TFSF x-pol +z Gaussian, NF-FF 1/2/3 GHz",
-                   "cells": cells, "grid": list(n), "precision_form": args.precision,
-                   "l2": "no flush: fields 6 x %.0f MB > 129 MB L2" % (cells * (4 if args.precision == 'fp32' else 8) / 1e6),
-                   "parallelism": f"replicas x{world}", "volume_kernels": args.volume,
-                   "timed_path": run["timed_path"]},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": headline_config(world),
+        "timed_path": run["timed_path"],
         "roofline": roof,
         "kernel_shares": shares,
         "volume_split_cells": split,
@@ -683,9 +690,9 @@ def ours_arm(args, world, rank, local, grp):
                               "config's full grid (1e-10) and bounds the FP32 form's errors against it",
         },
         "fp64_form": fp64,
+        "dielectric_form": dielectric,
         "batched_form": batched,
         "adjoint_form": adjoint,
-        "heterogeneous_form": hetero,
     }
     print(json.dumps(line), flush=True)
 
@@ -693,32 +700,30 @@ def ours_arm(args, world, rank, local, grp):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
-    ap.add_argument("--fp64-steps", type=int, default=200)
-    ap.add_argument("--cpu-sample", type=int, default=8, help="oracle steps timed for cpu_baseline (0: skip)")
-    ap.add_argument("--ref-budget", type=float, default=120.0, help="seconds of oracle work for --impl reference")
-    ap.add_argument("--batch-problems", type=int, default=64, help="problems of the batched form (0: skip)")
-    ap.add_argument("--volume", default="split", choices=["split", "fused", "auto"],
-                    help="volume kernels of the main workload: the split E and H kernels (the faster on this "
-                         "workload), the fused E/H sweep, or the autotuner's choice")
-    ap.add_argument("--adjoint", type=int, default=1, help="run the adjoint form (0: skip)")
-    ap.add_argument("--hetero-steps", type=int, default=100, help="steps of the heterogeneous-medium form (0: skip)")
-    ap.add_argument("--hetero-fp64-steps", type=int, default=20,
-                    help="timed steps of the heterogeneous medium's FP64 form (0: skip)")
-    ap.add_argument("--hetero-e2e-steps", type=int, default=1000,
-                    help="steps of the heterogeneous medium's whole job end to end (0: skip)")
+    ap.add_argument("--fp64-steps", type=int, default=100, help="timed steps of the headline's FP64 form (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=0,
-                    help="steps of the headline's whole job end to end (0: the config's 2000)")
+                    help="steps of the headline's whole job end to end (0: the config's 1000)")
+    ap.add_argument("--cpu-sample", type=int, default=10, help="oracle steps timed for cpu_baseline (0: skip)")
+    ap.add_argument("--ref-budget", type=float, default=120.0, help="seconds of oracle work for --impl reference")
+    ap.add_argument("--volume", default="auto", choices=["split", "fused", "auto"],
+                    help="volume kernels of the headline: the split E and H kernels, the fused E/H sweep, or the "
+                         "autotuner's choice")
+    ap.add_argument("--dielectric-steps", type=int, default=2000,
+                    help="timed steps of the dielectric-sphere form (0: skip)")
+    ap.add_argument("--dielectric-fp64-steps", type=int, default=200,
+                    help="timed steps of the dielectric-sphere FP64 form (0: skip)")
+    ap.add_argument("--batch-problems", type=int, default=64, help="problems of the batched form (0: skip)")
+    ap.add_argument("--adjoint", type=int, default=1, help="run the adjoint form (0: skip)")
+    ap.add_argument("--adjoint-fd", type=int, default=16, help="design voxels of the adjoint FD check (0: skip)")
+    ap.add_argument("--adjoint-checkpoint", type=int, default=100,
+                    help="adjoint form: checkpoint every K steps (0: record the design box at every step)")
     ap.add_argument("--kernel-variant", default=None, metavar="E,H",
                     help="fix the interior variants of the headline run (after autotuning; for a launch list "
                          "under a profiler, whose timings would mislead the autotuner)")
     ap.add_argument("--shell-variant", default=None, metavar="E,H", help="fix the shell variants likewise")
-    ap.add_argument("--adjoint-fd", type=int, default=16, help="design voxels of the adjoint FD check (0: skip)")
-    ap.add_argument("--adjoint-checkpoint", type=int, default=100,
-                    help="adjoint form: checkpoint every K steps (0: record the design box at every step)")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.impl == "reference":
