@@ -7,9 +7,11 @@
                     (host/include/xfdtd/xfdtd.h) and its C-ABI
                     (include/xfdtd_sim.h), linked against libxfdtd_cuda.so.
 
-The engine's device code is compiled by as many parallel nvcc jobs as there
-are host cores (--split-compile=0), about two minutes on 8 cores; nvcc
-cross-compiles, so the build also runs on a machine without a GPU.
+The engine is one nvcc job (about three minutes); its device code is not
+split across parallel jobs (--split-compile), which optimises parts of the
+module apart and left device functions the kernels inline out of line,
+12-20 % slower TMA volume launches.  nvcc cross-compiles, so the build
+also runs on a machine without a GPU.
 """
 from __future__ import annotations
 
@@ -36,8 +38,8 @@ def _nvcc() -> str:
 
 def cuda_cmd(out: str = CUDA_LIB, extra=()) -> list:
     srcs = [os.path.join(HERE, "csrc", f) for f in ("engine.cu", "nffft_noalloc.cu")]
-    return [_nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "--split-compile=0", "-Xcompiler", "-fPIC",
-            "-shared", *extra, "-o", out, *srcs, "-ldl"]
+    return [_nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", *extra, "-o", out,
+            *srcs, "-ldl"]
 
 
 def host_cmd() -> list:
