@@ -189,9 +189,20 @@ SIDE_STREAM_KERNELS = ("tfsf_aux", "nffft", "nffft_acc", "update_e_interior", "u
 # python -m xfdtd_gb300.run --config dielectric_sphere --steps 24 --precision fp32 --no-graph --volume split
 #     --no-autotune --kernel-variant 20,20 --shell-variant 5,5
 # E: 535.4 + 193.0 MB (interior) + 219.8 + 40.7 MB (z edges); H: 504.4 + 190.5 + 187.7 + 34.3 MB.
+#
+# The heterogeneous medium (532 x 532 x 404, 2-byte material index), its
+# autotuned variants (E: wide compact-table interior 22 + z-edge launch 6;
+# H: narrow TMA interior 19 + shell kernel 3), one ncu capture of each
+# launch in step 2 of
+# python -m xfdtd_gb300.run --config heterogeneous --steps 6 --precision fp32 --no-graph --no-autotune
+#     --kernel-variant 22,19 --shell-variant 6,3
+# E: 2900.65 + 1209.39 MB (wide) + 771.83 + 213.49 MB (z edges);
+# H: 2521.39 + 1068.52 MB (interior) + 891.77 + 356.84 MB (shell).
 NCU_TRAFFIC = {
     ("update_e", "fp32", (280, 280, 280), True): 535.400704e6 + 192.98304e6 + 219.822848e6 + 40.7488e6,
     ("update_h", "fp32", (280, 280, 280), True): 504.384e6 + 190.464e6 + 187.740672e6 + 34.299904e6,
+    ("update_e", "fp32", (532, 532, 404), True): 2900.651264e6 + 1209.392128e6 + 771.828736e6 + 213.485312e6,
+    ("update_h", "fp32", (532, 532, 404), False): 2521.388032e6 + 1068.519424e6 + 891.773952e6 + 356.841984e6,
 }
 
 
@@ -200,10 +211,10 @@ def dominant(prof) -> str:
     return max((k for k in prof if k not in SIDE_STREAM_KERNELS), key=lambda k: prof[k][0])
 
 
-def algorithmic_bytes(n, slab_layers, precision: str, kernel: str, split=None) -> float:
+def algorithmic_bytes(n, slab_layers, precision: str, kernel: str, split=None, ib: int = 1) -> float:
     """Bytes one E (or H) volume update must move at least: per cell read
     the 3 own components and the 3 curl components, write the 3 own
-    components, read the 1-byte material index; inside CPML slabs read and
+    components, read the material index (ib bytes); inside CPML slabs read and
     write one psi per (component, slab axis) pair (2 per slab axis).  The
     update runs as two concurrent launches, an interior and a shell launch
     (cells split["e_interior"] / ["e_shell"], likewise for H); in the narrow
@@ -219,16 +230,16 @@ def algorithmic_bytes(n, slab_layers, precision: str, kernel: str, split=None) -
     psi_z = slab_layers[2] * nx * ny * 2 * 2 * w
     psi = psi_xy + psi_z
     if kernel == "sweep_eh":
-        return cells * (12 * w + 1) + psi * 2
+        return cells * (12 * w + ib) + psi * 2
     if split is not None:
         side = kernel[7]
         wide = split.get(side + "_wide", False)
         if kernel.endswith("_interior"):
-            return split[side + "_interior"] * (9 * w + 1) + (psi_xy if wide else 0)
+            return split[side + "_interior"] * (9 * w + ib) + (psi_xy if wide else 0)
         if kernel.endswith("_shell"):
-            return split[side + "_shell"] * (9 * w + 1) + (psi_z if wide else psi)
-        return (split[side + "_interior"] + split[side + "_shell"]) * (9 * w + 1) + psi
-    return cells * (9 * w + 1) + psi
+            return split[side + "_shell"] * (9 * w + ib) + (psi_z if wide else psi)
+        return (split[side + "_interior"] + split[side + "_shell"]) * (9 * w + ib) + psi
+    return cells * (9 * w + ib) + psi
 
 
 def _slab_layers(sc):
@@ -340,14 +351,23 @@ def run_batched_form(args, local):
         m.check_finite()
     del b, members
     ms_s = 0.0
+    alone = []   # (cells, cell-updates, ms) of each problem run alone
     for sc, st in probs:   # sequential: each problem alone, plain split kernels, graph replay
         s = X.Simulation(sc, st, precision="fp32", fused=False, autotune=False, device=local)
-        ms_s += s.step_timed(st)
+        ms = s.step_timed(st)
+        alone.append((s.n[0] * s.n[1] * s.n[2], s.n[0] * s.n[1] * s.n[2] * st, ms))
+        ms_s += ms
         del s
+    # throughput of the problems alone, by size: the batch's gain is in packing the small ones
+    bins = {}
+    for lo, hi, name in ((0, 5e5, "<0.5M cells"), (5e5, 2e6, "0.5-2M cells"), (2e6, 1e12, ">=2M cells")):
+        sel = [a for a in alone if lo <= a[0] < hi]
+        if sel:
+            bins[name] = {"problems": len(sel), "alone_value": sum(a[1] for a in sel) / (sum(a[2] for a in sel) / 1e3) / 1e6}
     return {"problems": len(probs), "cells_total": sum(cells), "cell_updates": work,
             "value": work / (ms_b / 1e3) / 1e6, "unit": UNIT, "ms": ms_b, "launches": launches,
             "sequential_value": work / (ms_s / 1e3) / 1e6, "sequential_ms": ms_s,
-            "speedup_vs_sequential": ms_s / ms_b, "tma_members": n_tma,
+            "speedup_vs_sequential": ms_s / ms_b, "tma_members": n_tma, "sequential_by_size": bins,
             "workload": "64 dielectric-sphere problems, interior U{32..160}^3 + 8-cell CPML, "
                         "steps U{500..1500}, seeds 4000+i"}
 
@@ -362,7 +382,7 @@ def run_adjoint_form(args, local):
     backward pass.  Times: the plain FP32 forward run (CUDA events), the
     recording forward and the backward pass (wall clock around the
     synchronous calls).  Check: central differences of the FP64 forward loss
-    (eps_r +- 1e-4, as float) at `adjoint_fd` seeded design voxels."""
+    (eps_r +- 1e-4, set in double) at `adjoint_fd` seeded design voxels."""
     import xfdtd_gb300 as X
     sc, st, spec = configs.adjoint_dipole()
     keys = ("design_lo", "design_hi", "plane_axis", "plane_index", "plane_lo", "plane_hi", "t_begin", "t_end",
@@ -395,22 +415,23 @@ def run_adjoint_form(args, local):
         sb = dict(sa, checkpoint_every=st)   # one checkpoint: the FD runs only need the loss
 
         def loss_with(cell, eps):
+            # eps_r set in double (the float Material ctor would round the
+            # 1e-4 step)
             sc2 = copy.copy(sc)
             sc2.voxel_materials = list(sc.voxel_materials)
             q = 1 + int(np.ravel_multi_index(cell, dsz))
-            e = float(np.float32(eps))
-            sc2.voxel_materials[q] = S.Material("d", e, 1.0, 0.0, 0.0)
+            sc2.voxel_materials[q] = S.Material("d", eps, 1.0, 0.0, 0.0, exact_eps=True)
             s64 = X.Simulation(sc2, st, precision="fp64", fused=False, autotune=False, device=local)
-            return s64.adjoint_forward(**sb), e
+            return s64.adjoint_forward(**sb)
 
         rel = []
         for cell in picks:
             e0 = float(spec["eps"][cell])
-            lp, ep = loss_with(cell, e0 + 1e-4)
-            lm, em = loss_with(cell, e0 - 1e-4)
-            fd = (lp - lm) / (ep - em)
+            lp = loss_with(cell, e0 + 1e-4)
+            lm = loss_with(cell, e0 - 1e-4)
+            fd = (lp - lm) / 2e-4
             rel.append(abs(ge[cell] - fd) / abs(fd))
-        out["fd_check"] = {"voxels": len(picks), "h": 1e-4, "forward": "fp64",
+        out["fd_check"] = {"voxels": len(picks), "h": 1e-4, "forward": "fp64", "eps_r": "double",
                            "max_rel_err": float(max(rel)), "median_rel_err": float(np.median(rel))}
     return out
 
@@ -440,7 +461,7 @@ def _timed(sc, precision, steps, warmup, local, grp=None, fused=False, variants=
         grp.barrier()
     out = {"n": tuple(n), "cells": n[0] * n[1] * n[2], "ms": ms, "launches": sim.launch_count() - l0,
            "variants": sim.kernel_variants(), "shell_variants": sim.shell_variants(), "split": sim.volume_split(),
-           "tfsf_folded": sim.tfsf_fusion(), "nffft_schedule": sim.nffft_split(),
+           "tfsf_folded": sim.tfsf_fusion(), "nffft_schedule": sim.nffft_split(), "index_bytes": sim.index_bytes(),
            "setup_steps": setup,
            "timed_path": f"{steps // GRAPH_STEPS} CUDA graph replays of {GRAPH_STEPS} steps + "
                          f"{steps % GRAPH_STEPS} single steps, after {warmup} warm-up steps and {setup} untimed "
@@ -473,24 +494,25 @@ def _profiled(sc, precision, steps, warmup, local, run, fused=False):
     dom = dominant(prof)
     dom_ms, dom_n = prof[dom]
     slabs = _slab_layers(sc)
-    n, split = run["n"], run["split"]
-    alg = algorithmic_bytes(n, slabs, precision, dom, split)
+    n, split, ib = run["n"], run["split"], run["index_bytes"]
+    alg = algorithmic_bytes(n, slabs, precision, dom, split, ib)
     peak, peak_kind = _peaks()
     achieved = alg / (dom_ms / dom_n / 1e3) / 1e9
     total_prof = sum(v[0] for v in prof.values())
     shares = {k: round(v[0] / total_prof, 4) for k, v in prof.items()}
     shares.update({f"{k} (concurrent)": round(v[0] / total_prof, 4) for k, v in side.items()})
     concurrent = {k: {"ms_per_launch": v[0] / max(v[1], 1),
-                      "algorithmic_GBs": algorithmic_bytes(n, slabs, precision, k, split) / (v[0] / max(v[1], 1) / 1e3) / 1e9}
+                      "algorithmic_GBs": algorithmic_bytes(n, slabs, precision, k, split, ib) / (v[0] / max(v[1], 1) / 1e3) / 1e9}
                   for k, v in side.items() if k.startswith("update_")}
     # both volume updates over the whole profiled step: 2 x the pair's bytes
     # per step over the step time (the small surface launches included)
-    pair = algorithmic_bytes(n, slabs, precision, "update_e", split) + algorithmic_bytes(n, slabs, precision, "update_h", split)
+    pair = (algorithmic_bytes(n, slabs, precision, "update_e", split, ib)
+            + algorithmic_bytes(n, slabs, precision, "update_h", split, ib))
     step_frac = pair / (total_ms / steps / 1e3) / 1e9 / peak
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind,
             "traffic": NCU_TRAFFIC.get((dom, precision, tuple(n), split.get(dom[7] + "_wide"))),
-            "algorithmic_bytes_per_launch": alg, "launch_ms": dom_ms / dom_n,
+            "algorithmic_bytes_per_launch": alg, "index_bytes": ib, "launch_ms": dom_ms / dom_n,
             "step_frac": step_frac,
             "timing": f"CUDA events around each launch in a profiled pass of {steps} steps "
                       f"({total_ms / steps:.4f} ms/step, no graph)"}

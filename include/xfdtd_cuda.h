@@ -355,6 +355,8 @@ int xfdtd_nffft_split(xfdtd_handle *h, int *on, float ms[2]);
 int xfdtd_create_times(xfdtd_handle *h, double ms[2]);
 /* Device bytes held by the handle (with its adjoint state, if any). */
 int xfdtd_device_bytes(xfdtd_handle *h, int64_t *bytes);
+/* Bytes per cell of the plan's material index (1, 2 or 4). */
+int xfdtd_index_bytes(xfdtd_handle *h, int *bytes);
 const char *xfdtd_last_error(xfdtd_handle *h);
 void xfdtd_destroy(xfdtd_handle *h);
 

@@ -94,14 +94,22 @@ enum {
   XFDTD_DISPERSION_DEBYE = 3
 };
 
+/* xfdtd_material_desc.flags: eps_r exact.  A plain (non-dispersive)
+ * material whose relative permittivity is p[0] in double, not the float
+ * eps_r field (the reference's Material ctor takes eps_r as float).  For a
+ * gradient check by finite differences, whose step (1e-4) a float eps_r
+ * would round away.  No counterpart in the reference. */
+#define XFDTD_MATERIAL_EXACT_EPS 1
+
 typedef struct xfdtd_material_desc {
   float eps_r;       /* float, as in the reference's Material ctor       */
   float mu_r;
   double sigma_e;    /* S/m; a PEC is sigma_e = 1e10                     */
   double sigma_m;
   int32_t dispersion;   /* XFDTD_DISPERSION_*                            */
-  int32_t reserved;
-  double p[4];          /* the dispersive medium's parameters (above)    */
+  int32_t flags;        /* XFDTD_MATERIAL_EXACT_EPS or 0                 */
+  double p[4];          /* the dispersive medium's parameters (above);   */
+                        /* p[0] = eps_r with XFDTD_MATERIAL_EXACT_EPS    */
 } xfdtd_material_desc;
 
 typedef struct xfdtd_object_desc {

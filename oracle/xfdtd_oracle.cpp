@@ -39,6 +39,14 @@
 
 namespace {
 
+// The relative permittivity of a material description: the float eps_r of
+// the reference's Material ctor (material.cpp:7-16), or, with the scene's
+// XFDTD_MATERIAL_EXACT_EPS extension (no counterpart in the reference), p[0]
+// in double.
+double eps_r_of(const xfdtd_material_desc &m) {
+  return (m.flags & XFDTD_MATERIAL_EXACT_EPS) ? m.p[0] : static_cast<double>(m.eps_r);
+}
+
 using cplx = std::complex<double>;
 
 // src/include/util/constant.h:10-29
@@ -531,7 +539,7 @@ void oracle_sim::initObjects() {
     Shape s{};
     s.d = o.shape;
     gs->getGridBox(s);  // Object::init computes (and discards) the grid box; it can throw
-    double e = static_cast<double>(o.material.eps_r) * EPSILON_0;  // material.cpp:7-16
+    double e = eps_r_of(o.material) * EPSILON_0;  // material.cpp:7-16
     double m = static_cast<double>(o.material.mu_r) * MU_0;
     double se = o.material.sigma_e, sm = o.material.sigma_m;
     // a dispersive medium is a Material(name, 1, 1, sigma_e, sigma_m)
@@ -574,7 +582,7 @@ void oracle_sim::initObjects() {
         for (size_t k = 0; k < nz; ++k) {
           const xfdtd_material_desc &md = voxel_mats[voxel_idx[(i * ny + j) * nz + k]];
           if (!disp_id.empty()) disp_id[(i * ny + j) * nz + k] = -1;   // voxel materials are plain
-          double e = static_cast<double>(md.eps_r) * EPSILON_0;
+          double e = eps_r_of(md) * EPSILON_0;
           double m = static_cast<double>(md.mu_r) * MU_0;
           for (int a = 0; a < 3; ++a) {
             eps[a](i, j, k) = e; mu[a](i, j, k) = m;

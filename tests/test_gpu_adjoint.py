@@ -25,15 +25,16 @@ def _spec_args(spec, k=None):
 
 def _with_material(sc, spec, cell, eps=None, sigma=None):
     """The scene with the design voxel `cell` (design-box coordinates) given
-    a new eps_r / sigma; returns (scene, the eps_r / sigma actually used)."""
+    a new eps_r (set in double, bypassing the float Material ctor) / sigma;
+    returns (scene, the eps_r / sigma used)."""
     sc2 = copy.copy(sc)
     sc2.voxel_materials = list(sc.voxel_materials)
     dsz = tuple(b - a for a, b in zip(spec["design_lo"], spec["design_hi"]))
     q = 1 + int(np.ravel_multi_index(cell, dsz))
     m = sc.voxel_materials[q]
-    e = float(np.float32(eps)) if eps is not None else m.eps_r
+    e = float(eps) if eps is not None else m.eps_r
     s = sigma if sigma is not None else m.sigma_e
-    sc2.voxel_materials[q] = S.Material("d", e, 1.0, s, 0.0)
+    sc2.voxel_materials[q] = S.Material("d", e, 1.0, s, 0.0, exact_eps=True)
     return sc2, (e if eps is not None else s)
 
 

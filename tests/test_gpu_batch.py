@@ -65,7 +65,7 @@ def test_batch_tma_launches_match_plain_and_alone(precision):
     for plain in (False, True):
         members = [X.Simulation(sc, st, precision=precision, fused=False, autotune=False) for sc, st in probs]
         b = X.Batch(members, graph=True, plain=plain)
-        if plain:
+        if plain or precision == "fp64":   # the TMA-staged launches run in FP32 only
             assert b.tma_members() == 0
         else:
             assert b.tma_members() >= 1

@@ -253,10 +253,31 @@ def test_wide_decomposition_is_bitwise_identical(name):
                 g.step(st)
                 for c in range(6):
                     assert np.array_equal(g.read_field(c), want[c]), (name, precision, v, sv, c)
-    if name == "dielectric":
-        # every pairing in one precision at least (the other's k range may
-        # not start on a 16-byte boundary on this small grid)
-        assert offered >= len(WIDE_VARIANTS) * (2 + len(ZEDGE_SHELL_VARIANTS))
+    if name == "heterogeneous":
+        # every pairing of the offered wide variants (FP32, 4 stages)
+        assert offered >= len(OFFERED_WIDE_VARIANTS) * (2 + len(ZEDGE_SHELL_VARIANTS))
+
+
+# the wide variants offered: FP32, 4 stages (capped at 5 blocks per SM)
+OFFERED_WIDE_VARIANTS = (20, 22)
+
+
+def test_wide_decomposition_offered_only_on_capped_fp32_launches():
+    """The wide decomposition runs only on its FP32 4-stage launches (capped
+    at 5 blocks per SM): the 6-stage FP32 variant and every FP64 wide variant
+    are refused.  Uncapped, the wide launch returned other bits than the
+    narrow decomposition in the cells of the x-y CPML edges of a grid of
+    random per-cell materials."""
+    sc, st = scenes.SCENES["heterogeneous"](steps=40)
+    for precision in ("fp64", "fp32"):
+        for v in WIDE_VARIANTS:
+            g = X.Simulation(sc, st, precision=precision, autotune=False, fused=False)
+            offered = True
+            try:
+                g.set_kernel_variant(v, v)
+            except X.EngineError:
+                offered = False
+            assert offered == (precision == "fp32" and v in OFFERED_WIDE_VARIANTS), (precision, v)
 
 
 @pytest.mark.parametrize("name", ["dielectric", "oblique", "pec_sphere"])
@@ -265,7 +286,10 @@ def test_tfsf_folded_into_the_wide_launch_is_bitwise_identical(name):
     (E and H) give the bits of the separate k_tfsf_e / k_tfsf_h launches,
     with every wide interior variant, through graph replay, in both
     precisions; and the folded form is in use where the grid allows it."""
-    sc, st = scenes.SCENES[name]()
+    # the dielectric scene at 88^3 cells: its k range lies on 16-byte
+    # boundaries for the fields and the 1-byte index, so it offers the FP32
+    # wide launches
+    sc, st = scenes.dielectric(scale=4, steps=120) if name == "dielectric" else scenes.SCENES[name]()
     st = min(st, 120)
     used = 0
     for precision in ("fp64", "fp32"):

@@ -97,6 +97,24 @@ def test_dispersive_media_reduce_to_the_plain_dielectric(kind):
     assert all(np.isfinite(d.read_field(c)).all() for c in range(6))
 
 
+def test_exact_eps_material():
+    """A material with its eps_r kept in double (XFDTD_MATERIAL_EXACT_EPS)
+    gives the float material's fields when the value is a float, and moves
+    them when it is not (the float ctor would round 2.5 + 1e-7 to 2.5)."""
+    def fields(mat):
+        sc, st = scenes.dispersive("lorentz", steps=60, limit=True)
+        sc.objects[1] = S.Object("p", sc.objects[1].shape, mat)
+        o = O.OracleSim(sc, st)
+        o.step(st)
+        return [o.read_field(c) for c in range(6)]
+    f = fields(S.Material("p", 2.5, 1, 0.01, 0))
+    e = fields(S.Material("p", 2.5, 1, 0.01, 0, exact_eps=True))
+    assert all(np.array_equal(a, b) for a, b in zip(f, e))
+    assert float(np.float32(2.5 + 1e-7)) == 2.5
+    d = fields(S.Material("p", 2.5 + 1e-7, 1, 0.01, 0, exact_eps=True))
+    assert max(np.abs(a - b).max() for a, b in zip(f, d)) > 0
+
+
 def test_tfsf_normal_incidence_cancels_outside_box():
     sc, _ = configs.pec_sphere_rcs(scale=2, steps=260)
     sc.objects = sc.objects[:1]

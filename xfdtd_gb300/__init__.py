@@ -87,6 +87,7 @@ def libs():
         cu.xfdtd_profile_reset.argtypes = [C.c_void_p]
         cu.xfdtd_launches_per_step.argtypes = [C.c_void_p, P(C.c_int)]
         cu.xfdtd_device_bytes.argtypes = [C.c_void_p, P(C.c_int64)]
+        cu.xfdtd_index_bytes.argtypes = [C.c_void_p, P(C.c_int)]
         cu.xfdtd_transfer_bytes.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64)]
         cu.xfdtd_launch_count.argtypes = [C.c_void_p, P(C.c_int64)]
         cu.xfdtd_autotune.argtypes = [C.c_void_p, C.c_int]
@@ -443,6 +444,12 @@ class Simulation:
     def device_bytes(self) -> int:
         b = C.c_int64()
         self._check_engine(libs()[0].xfdtd_device_bytes(self.engine, C.byref(b)))
+        return b.value
+
+    def index_bytes(self) -> int:
+        """Bytes per cell of the material index (1, 2 or 4)."""
+        b = C.c_int()
+        self._check_engine(libs()[0].xfdtd_index_bytes(self.engine, C.byref(b)))
         return b.value
 
 

@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(256, 6) k_shell_batch(const __grid_constant__ 
 // members' tensor maps lie in global memory, written by the host when the
 // batch is made; the thread that issues the copies acquires them first.
 template <typename T, typename I, int STAGES, bool CT, int MODE, bool E_SIDE>
-__global__ void __launch_bounds__(kItThreads) k_tma_batch(const __grid_constant__ VolGroup<T, I> g,
+__global__ void __launch_bounds__(kItThreads, sizeof(T) == 4 ? 5 : 1) k_tma_batch(const __grid_constant__ VolGroup<T, I> g,
                                                           const __grid_constant__ GroupBlocks gb,
                                                           const ItMaps *__restrict__ maps,
                                                           const InteriorBox *__restrict__ boxes,

@@ -648,7 +648,18 @@ __device__ __forceinline__ void tfsf_h_surface(const TfsfSurfParams<T> &p, int q
   const auto einc = tfsf_view<T>(tf).inc + ((*p.step) & 1) * 6 * tf.L;   // incident E of this step
   const long long b = static_cast<long long>(i) * p.d.si + static_cast<long long>(j) * p.d.sj + k;
   if (!tfsf_h_terms(tf, i, j, k)) return;
-  T hx = p.F[3][b], hy = p.F[4][b], hz = p.F[5][b];
+  // load only the components that get a term (tfsf_h_cell's conditions):
+  // a face cell corrects one or two of its three
+  const int li = tf.lo[0], ri = tf.hi[0], lj = tf.lo[1], rj = tf.hi[1], lk = tf.lo[2], rk = tf.hi[2];
+  const bool two_d = tf.two_d != 0;
+  const bool ix = i >= li && i <= ri, iy = j >= lj && j <= rj;
+  const bool hx_t = ((j == lj - 1 || j == rj) && k >= lk && k < rk && ix) ||
+                    (!two_d && (k == lk - 1 || k == rk) && ix && j >= lj && j < rj);
+  const bool hy_t = ((i == li - 1 || i == ri) && iy && k >= lk && k < rk) ||
+                    (!two_d && (k == lk - 1 || k == rk) && i >= li && i < ri && iy);
+  const bool hz_t = !two_d && (((i == li - 1 || i == ri) && j >= lj && j < rj && k >= lk && k <= rk) ||
+                               ((j == lj - 1 || j == rj) && k >= lk && k <= rk && i >= li && i < ri));
+  T hx = hx_t ? p.F[3][b] : T(0), hy = hy_t ? p.F[4][b] : T(0), hz = hz_t ? p.F[5][b] : T(0);
   bool w[3];
   tfsf_h_cell<T>(tf, einc, i, j, k, hx, hy, hz, w);
   if (w[0]) p.F[3][b] = hx;

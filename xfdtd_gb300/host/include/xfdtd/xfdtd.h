@@ -145,6 +145,11 @@ class Material {
  public:
   Material(std::string_view name, float eps_r, float mu_r, double sigma_e, double sigma_m,
            bool is_dispersion = false);
+  // A material whose relative permittivity is kept in double (the
+  // constructor above takes eps_r as float, as the reference's does): for
+  // finite-difference gradient checks.  No counterpart in the reference.
+  static Material withExactPermittivity(std::string_view name, double eps_r, float mu_r, double sigma_e,
+                                        double sigma_m);
   static std::unique_ptr<Material> createAir(const std::string &name = "XFDTD_AIR");
   static std::unique_ptr<Material> createPEC();
   static std::unique_ptr<Material> createPMC();

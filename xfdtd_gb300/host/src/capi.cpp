@@ -20,10 +20,21 @@ namespace {
 using namespace xfdtd;
 
 // A Material of the description, or the dispersive medium it names.
+// A plain material of the description (its eps_r from p[0] in double with
+// XFDTD_MATERIAL_EXACT_EPS).
+Material plainMaterial(const char *name, const xfdtd_material_desc &m) {
+  if (m.flags & ~XFDTD_MATERIAL_EXACT_EPS) throw std::invalid_argument("unknown material flags");
+  if (m.flags & XFDTD_MATERIAL_EXACT_EPS) {
+    if (m.dispersion) throw std::invalid_argument("an exact eps_r is for plain materials only");
+    return Material::withExactPermittivity(name, m.p[0], m.mu_r, m.sigma_e, m.sigma_m);
+  }
+  return Material(name, m.eps_r, m.mu_r, m.sigma_e, m.sigma_m);
+}
+
 std::unique_ptr<Material> makeMaterial(const xfdtd_material_desc &m) {
   switch (m.dispersion) {
     case XFDTD_DISPERSION_NONE:
-      return std::make_unique<Material>("material", m.eps_r, m.mu_r, m.sigma_e, m.sigma_m);
+      return std::make_unique<Material>(plainMaterial("material", m));
     case XFDTD_DISPERSION_LORENTZ:
       return std::make_unique<LorentzMedium>("lorentz", m.p[0], m.p[1], m.p[2], m.p[3], m.sigma_e, m.sigma_m);
     case XFDTD_DISPERSION_DRUDE:
@@ -210,7 +221,7 @@ int xfdtd_sim_create(const xfdtd_scene_desc *sc, int64_t total_steps, int precis
       for (int q = 0; q < sc->n_voxel_materials; ++q) {
         const auto &m = sc->voxel_materials[q];
         if (m.dispersion) throw std::invalid_argument("voxel materials are plain materials (no dispersive media)");
-        mats.emplace_back("voxel", m.eps_r, m.mu_r, m.sigma_e, m.sigma_m);
+        mats.push_back(plainMaterial("voxel", m));
       }
       const size_t cnt = static_cast<size_t>(sc->voxel_shape[0] * sc->voxel_shape[1] * sc->voxel_shape[2]);
       std::vector<uint32_t> idx(cnt);

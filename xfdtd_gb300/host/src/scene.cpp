@@ -60,6 +60,12 @@ std::unique_ptr<Shape> Cylinder::getWrappedBox() const {
 Material::Material(std::string_view name, float eps_r, float mu_r, double sigma_e, double sigma_m, bool is_dispersion)
     : _name{name}, _eps_r{eps_r}, _mu_r{mu_r}, _eps{_eps_r * constant::EPSILON_0}, _mu{_mu_r * constant::MU_0},
       _sigma_e{sigma_e}, _sigma_m{sigma_m}, _is_dispersion{is_dispersion} {}
+Material Material::withExactPermittivity(std::string_view name, double eps_r, float mu_r, double sigma_e,
+                                         double sigma_m) {
+  Material m(name, static_cast<float>(eps_r), mu_r, sigma_e, sigma_m);
+  m._eps = eps_r * constant::EPSILON_0;
+  return m;
+}
 std::unique_ptr<Material> Material::createAir(const std::string &name) {
   return std::make_unique<Material>(name, 1, 1, 0, 0);
 }

@@ -49,8 +49,11 @@ class ShapeDesc(C.Structure):
 
 class MaterialDesc(C.Structure):
     _fields_ = [("eps_r", C.c_float), ("mu_r", C.c_float), ("sigma_e", C.c_double),
-                ("sigma_m", C.c_double), ("dispersion", C.c_int32), ("reserved", C.c_int32),
+                ("sigma_m", C.c_double), ("dispersion", C.c_int32), ("flags", C.c_int32),
                 ("p", C.c_double * 4)]
+
+
+MATERIAL_EXACT_EPS = 1
 
 
 DISPERSION_NONE, DISPERSION_LORENTZ, DISPERSION_DRUDE, DISPERSION_DEBYE = 0, 1, 2, 3
@@ -177,6 +180,9 @@ class Material:
     mu_r: float
     sigma_e: float
     sigma_m: float
+    # keep eps_r in double (XFDTD_MATERIAL_EXACT_EPS; the reference's ctor
+    # takes it as float): for finite-difference gradient checks
+    exact_eps: bool = False
 
     @staticmethod
     def create_air(name: str = "XFDTD_AIR") -> "Material":  # material.cpp:28-30
@@ -190,6 +196,9 @@ class Material:
         d = MaterialDesc()
         d.eps_r, d.mu_r = float(self.eps_r), float(self.mu_r)
         d.sigma_e, d.sigma_m = float(self.sigma_e), float(self.sigma_m)
+        if self.exact_eps:
+            d.flags = MATERIAL_EXACT_EPS
+            d.p[0] = float(self.eps_r)
         return d
 
 
