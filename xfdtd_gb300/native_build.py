@@ -7,11 +7,12 @@
                     (host/include/xfdtd/xfdtd.h) and its C-ABI
                     (include/xfdtd_sim.h), linked against libxfdtd_cuda.so.
 
-The engine is one nvcc job (about three minutes); its device code is not
+The engine is one nvcc job (two to three minutes); its device code is not
 split across parallel jobs (--split-compile), which optimises parts of the
-module apart and left device functions the kernels inline out of line,
-12-20 % slower TMA volume launches.  nvcc cross-compiles, so the build
-also runs on a machine without a GPU.
+module apart: built that way, the 280^3 dielectric-sphere step took 0.445
+ms instead of 0.427 ms with the same kernel variants, and the adjoint's
+reverse kernels executed 30 % more instructions.  nvcc cross-compiles, so
+the build also runs on a machine without a GPU.
 """
 from __future__ import annotations
 
