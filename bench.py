@@ -407,6 +407,20 @@ def run_adjoint_form(args, local):
            "gradient_over_forward": (t2 - t0) * 1e3 / fwd_ms,
            "value": cells * st / ((t2 - t1)) / 1e6, "unit": "Mcell-updates/s (reverse pass)",
            "checkpoint_every": args.adjoint_checkpoint, "device_bytes": dev_bytes}
+    if args.adjoint_checkpoint > 0:
+        # the same gradient with the design box recorded at every step (no
+        # re-run of the segments; the records fit GB300's HBM many times over)
+        g0 = X.Simulation(sc, st, precision="fp32", fused=False, autotune=False, device=local)
+        t0 = time.perf_counter()
+        g0.adjoint_forward(**dict(sa, checkpoint_every=0))
+        t1 = time.perf_counter()
+        ge0, _ = g0.adjoint_backward()
+        t2 = time.perf_counter()
+        out["record_every_step"] = {"adjoint_forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
+                                    "gradient_over_forward": (t2 - t0) * 1e3 / fwd_ms,
+                                    "device_bytes": g0.device_bytes(),
+                                    "same_gradient": bool(np.array_equal(ge0, ge))}
+        del g0
     if args.adjoint_fd > 0:
         import copy
         rng = np.random.default_rng(5002)

@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(256) k_adj_h(AdjParams<T, I> a) {
 // Own E transpose and gradient of step t (do_e_own), then the loss and U
 // gather of step t-1 (do_gather); the three paths of k_adj_h.
 template <typename T, typename I>
-__global__ void __launch_bounds__(256) k_adj_e(AdjParams<T, I> a) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 8 : 6) k_adj_e(AdjParams<T, I> a) {
   const VolParams<T, I> &p = a.v;
   const int nx = p.d.nx, ny = p.d.ny, nz = p.d.nz;
   const int k = adj_k(a, nz);
