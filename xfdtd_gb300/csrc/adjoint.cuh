@@ -686,15 +686,30 @@ struct FieldPtrs {
   const T *f[6];
 };
 
-// Copies E(t) over the design box and H(t) over the box grown by one cell
-// on the low sides into the records of step slot s.
+// The design-box records: E over the box and H over the box grown by one
+// cell on the low sides, one slot per step.  With checkpoints every K
+// steps, two buffers of K slots: step t goes to slot ((t / K) % 2) K + t % K;
+// with K = 0, slot t.
 template <typename T>
-__global__ void k_adj_record(FieldPtrs<T> F, Dims d, int lo0, int lo1, int lo2, int n0, int n1, int n2, T *recE0,
-                             T *recE1, T *recE2, T *recH0, T *recH1, T *recH2) {
+struct AdjRecords {
+  T *recE[3], *recH[3];   // slot 0
+  long long nE, nH;       // cells of a slot
+  int K;
+};
+
+// Copies E(t) and H(t) into the records of step t = *step (the step about
+// to run), so that the same launch serves every step of a captured graph.
+template <typename T>
+__global__ void k_adj_record(FieldPtrs<T> F, Dims d, int lo0, int lo1, int lo2, int n0, int n1, int n2,
+                             AdjRecords<T> r, const long long *step) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;   // 0 .. n2 (H box is one larger)
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int i = blockIdx.z;
   if (k > n2 || j > n1 || i > n0) return;
+  const long long t = *step;
+  const long long slot = r.K > 0 ? ((t / r.K) % 2) * r.K + t % r.K : t;
+  T *recE0 = r.recE[0] + slot * r.nE, *recE1 = r.recE[1] + slot * r.nE, *recE2 = r.recE[2] + slot * r.nE;
+  T *recH0 = r.recH[0] + slot * r.nH, *recH1 = r.recH[1] + slot * r.nH, *recH2 = r.recH[2] + slot * r.nH;
   // H box cell (i, j, k) is grid cell (lo-1 + i, ...)
   const long long gh = static_cast<long long>(lo0 - 1 + i) * d.si + static_cast<long long>(lo1 - 1 + j) * d.sj + (lo2 - 1 + k);
   const long long h = (static_cast<long long>(i) * (n1 + 1) + j) * (n2 + 1) + k;
@@ -709,13 +724,18 @@ __global__ void k_adj_record(FieldPtrs<T> F, Dims d, int lo0, int lo1, int lo2, 
   }
 }
 
-// Copies the loss component over the plane into rec (row-major over the two
-// other axes).
+// Copies the loss component over the plane after step t = *step - 1 (the
+// step that just ran) into its record, row-major over the two other axes,
+// when t lies in the loss window [t_begin, t_end); nothing otherwise.
 template <typename T>
-__global__ void k_adj_plane(const T *f, Dims d, int axis, int index, int lo0, int lo1, int n0, int n1, T *rec) {
+__global__ void k_adj_plane(const T *f, Dims d, int axis, int index, int lo0, int lo1, int n0, int n1, T *rec,
+                            const long long *step, long long t_begin, long long t_end) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   const int u = blockIdx.y;
   if (v >= n1 || u >= n0) return;
+  const long long t = *step - 1;
+  if (t < t_begin || t >= t_end) return;
+  rec += (t - t_begin) * n0 * n1;
   int ijk[3];
   ijk[axis] = index;
   ijk[axis == 0 ? 1 : 0] = lo0 + u;

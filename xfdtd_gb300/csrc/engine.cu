@@ -3490,32 +3490,95 @@ void adj_checkpoint(xfdtd_handle *h, void *block, bool save) {
   }
 }
 
+// The design-box record of the step about to run (its slot from the device
+// step counter, adjoint.cuh AdjRecords).
 template <typename T>
-void adj_record_design(xfdtd_handle *h, AdjointState *a, int slot) {
+void adj_record_design(xfdtd_handle *h, AdjointState *a) {
   const int n0 = a->dn[0], n1 = a->dn[1], n2 = a->dn[2];
-  T *rE[3], *rH[3];
+  xg::AdjRecords<T> r{};
   for (int c = 0; c < 3; ++c) {
-    rE[c] = static_cast<T *>(a->recE[c]) + static_cast<size_t>(slot) * a->nE;
-    rH[c] = static_cast<T *>(a->recH[c]) + static_cast<size_t>(slot) * a->nH;
+    r.recE[c] = static_cast<T *>(a->recE[c]);
+    r.recH[c] = static_cast<T *>(a->recH[c]);
   }
+  r.nE = a->nE;
+  r.nH = a->nH;
+  r.K = a->K;
   xg::FieldPtrs<T> fp;
   for (int c = 0; c < 6; ++c) fp.f[c] = static_cast<const T *>(h->F[c]);
   dim3 block(32, 8, 1);
   dim3 grid((n2 + 1 + 31) / 32, (n1 + 1 + 7) / 8, n0 + 1);
   xg::k_adj_record<T><<<grid, block, 0, h->stream>>>(fp, h->d, static_cast<int>(a->d.design_lo[0]),
                                                       static_cast<int>(a->d.design_lo[1]), static_cast<int>(a->d.design_lo[2]),
-                                                      n0, n1, n2, rE[0], rE[1], rE[2], rH[0], rH[1], rH[2]);
+                                                      n0, n1, n2, r, h->d_step);
   XCHECK(cudaGetLastError());
+  ++h->launch_count;
 }
 
+// The loss plane's record of the step that just ran, when it lies in the
+// loss window.
 template <typename T>
-void adj_record_plane(xfdtd_handle *h, AdjointState *a, long long w) {
-  T *rec = static_cast<T *>(a->plane) + static_cast<size_t>(w) * a->pn[0] * a->pn[1];
+void adj_record_plane(xfdtd_handle *h, AdjointState *a) {
   dim3 grid((a->pn[1] + 127) / 128, a->pn[0], 1);
   xg::k_adj_plane<T><<<grid, 128, 0, h->stream>>>(static_cast<const T *>(h->F[a->d.loss_comp]), h->d, a->d.plane_axis,
                                                   static_cast<int>(a->d.plane_index), static_cast<int>(a->d.plane_lo[0]),
-                                                  static_cast<int>(a->d.plane_lo[1]), a->pn[0], a->pn[1], rec);
+                                                  static_cast<int>(a->d.plane_lo[1]), a->pn[0], a->pn[1],
+                                                  static_cast<T *>(a->plane), h->d_step, a->d.t_begin, a->d.t_end);
   XCHECK(cudaGetLastError());
+  ++h->launch_count;
+}
+
+// A captured run of g steps of the adjoint's forward or re-run passes: each
+// step with its records (adj_steps).
+struct AdjGraph {
+  cudaGraphExec_t exec = nullptr;
+  long long launches = 0;   // kernel launches in the graph
+  ~AdjGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+// Runs the steps [t0, t1) with `each` (one step and the records around it)
+// as CUDA graph replays of g steps where the handle replays graphs and the
+// step sequence is the same for every step (no NF-FF, no snapshots: their
+// host bookkeeping follows the step index; the records take their slots
+// from the device step counter), single steps for the rest.  The graph is
+// captured on its first use.
+template <typename F>
+void adj_steps(xfdtd_handle *h, long long t0, long long t1, int g, AdjGraph &gr, F &&each) {
+  const bool graph = (h->flags & XFDTD_FLAG_GRAPH) && !(h->flags & XFDTD_FLAG_PROFILE) && !h->nffft &&
+                     h->snaps.empty();
+  long long t = t0;
+  while (t < t1) {
+    if (graph && g > 1 && t1 - t >= g) {
+      if (!gr.exec) {
+        cudaGraph_t cg;
+        const long long launches = h->launch_count;
+        XCHECK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        for (int s = 0; s < g; ++s) each(t + s);
+        XCHECK(cudaStreamEndCapture(h->stream, &cg));
+        gr.launches = h->launch_count - launches;
+        h->launch_count = launches;
+        const cudaError_t e = cudaGraphInstantiate(&gr.exec, cg, 0);
+        cudaGraphDestroy(cg);
+        XCHECK(e);
+      }
+      XCHECK(cudaGraphLaunch(gr.exec, h->stream));
+      h->launch_count += gr.launches;
+      t += g;
+      continue;
+    }
+    each(t);
+    ++t;
+  }
+}
+
+// Steps per captured graph: a divisor of the checkpoint interval K (graphs
+// never cross a checkpoint), at most 64; 50 without checkpoints.
+int adj_graph_steps(int K) {
+  if (K <= 0) return 50;
+  int g = std::min(K, 64);
+  while (K % g) --g;
+  return g;
 }
 
 void adj_validate(xfdtd_handle *h, const xfdtd_adjoint_desc *d) {
@@ -3571,24 +3634,26 @@ void adj_forward_t(xfdtd_handle *h, const xfdtd_adjoint_desc *d, double *loss) {
     cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
   }
-  // Steps that record nothing (between checkpoints, before the loss
-  // window) go through do_steps, which replays captured graphs where it can;
-  // the others one at a time with their records.
-  for (long long t = 0; t < T_;) {
-    if (a->K > 0 && t % a->K == 0) adj_checkpoint(h, a->ck[t / a->K], true);
-    const bool plane = t >= d->t_begin && t < d->t_end;
-    if (a->K == 0 || plane) {
-      if (a->K == 0) adj_record_design<T>(h, a.get(), static_cast<int>(t));
+  // Every step: the design-box record (K = 0), the step, the loss plane's
+  // record (a no-op outside the window); as graph replays between
+  // checkpoints.
+  {
+    AdjGraph gr;
+    const int g = adj_graph_steps(a->K);
+    AdjointState *ap = a.get();
+    auto each = [&](long long t) {
+      if (ap->K == 0) adj_record_design<T>(h, ap);
       enqueue_step(h, t);
       h->host_step = t + 1;
-      if (plane) adj_record_plane<T>(h, a.get(), t - d->t_begin);
-      ++t;
-      continue;
+      adj_record_plane<T>(h, ap);
+    };
+    const long long span = a->K > 0 ? a->K : T_;
+    for (long long t = 0; t < T_; t += span) {
+      if (a->K > 0) adj_checkpoint(h, a->ck[t / a->K], true);
+      adj_steps(h, t, std::min(T_, t + span), g, gr, each);
     }
-    long long next = std::min(T_, (t / a->K + 1) * a->K);
-    if (d->t_begin > t) next = std::min<long long>(next, d->t_begin);
-    do_steps(h, next - t);
-    t = next;
+    XCHECK(cudaStreamSynchronize(h->stream));   // the graph's last replay before it is destroyed
+    h->host_step = T_;
   }
   if (a->K > 0) adj_checkpoint(h, a->ck.back(), true);
   prof_collect(h);
@@ -3774,15 +3839,18 @@ void adj_backward_t(xfdtd_handle *h, double *g_eps, double *g_sig) {
   const int n_probes = h->n_probes;
   h->nffft = false;   // the NF-FF sums and probes of the forward pass are final
   h->n_probes = 0;
+  AdjGraph rerun_graph;   // the re-run's steps with their design-box records
+  const int rerun_g = adj_graph_steps(a->K);
+  auto rerun_each = [&](long long t) {
+    adj_record_design<T>(h, a);
+    enqueue_step(h, t);
+  };
   auto rerun = [&](long long q) {
     const long long s0 = q * seg, s1 = std::min(T_, s0 + seg);
     if (q + 2 < n_seg) XCHECK(cudaStreamWaitEvent(h->stream, a->ev_rev[q % 2], 0));   // reverse(q + 2) done
     adj_checkpoint(h, a->ck[q], false);
     XCHECK(cudaMemcpyAsync(h->d_step, &s0, sizeof(long long), cudaMemcpyHostToDevice, h->stream));
-    for (long long t = s0; t < s1; ++t) {
-      adj_record_design<T>(h, a, static_cast<int>((q % 2) * a->K + (t - s0)));
-      enqueue_step(h, t);
-    }
+    adj_steps(h, s0, s1, rerun_g, rerun_graph, rerun_each);
     XCHECK(cudaEventRecord(a->ev_rec[q % 2], h->stream));
   };
   XCHECK(cudaEventRecord(a->ev_ready, h->stream));   // zeroed adjoint state, tables, flags
