@@ -63,8 +63,8 @@ def test_plane_wait_timeout_is_reported_and_the_context_survives(wide):
     reports XFDTD_ERR_TIMEOUT, which synchronize returns.  The context stays
     usable: a fresh handle on the same device then steps to the bits of a
     handle that never timed out."""
-    # the wide launches run in FP32 on a grid whose k range lies on 16-byte
-    # boundaries for the fields and the 1-byte index (88^3 cells)
+    # the wide launches need a grid whose k range lies on 16-byte boundaries
+    # for the fields and the 1-byte index (88^3 cells)
     sc, st = scenes.dielectric(scale=4 if wide else 8, steps=10)
     ran = 0
     for precision in ("fp32", "fp64"):

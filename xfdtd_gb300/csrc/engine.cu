@@ -468,19 +468,9 @@ static_assert(kNumVariants <= 24, "tune_ms holds 24 variants per side");
 // A shared-memory-table variant needs the table to fit (smem_table); a
 // TMA-staged one an aligned interior on both sides (it_ok), a wide one the
 // wide decomposition on both sides too.
-// The wide decomposition is offered in FP32 on its 4-stage launches, which
-// run capped at 5 blocks per SM.  Built without that cap (the FP64 and the
-// 6-stage FP32 wide launches), the wide launch drops the x CPML terms of
-// the cells in both an x and a y CPML slab: compared in the kernel with its
-// operands read from global memory, their x slot comes out -1 and their x
-// profile the identity, at any number of resident blocks and with no other
-// launch beside it, in both precisions.  The same source built with the
-// cap gives the narrow decomposition's bits, and a rewrite of the context
-// with the same meaning moved the failure to other grids of the uncapped
-// builds, so those launches are not offered.
 bool variant_allowed(const xfdtd_handle *h, const Variant &v) {
   return (!v.smem || h->smem_table) && (!v.stages || (h->it_ok[0] && h->it_ok[1])) &&
-         (!v.wide || (h->wide_ok[0] && h->wide_ok[1] && h->precision == XFDTD_FP32 && v.stages == 4));
+         (!v.wide || (h->wide_ok[0] && h->wide_ok[1]));
 }
 
 // The decomposition a side runs with its current variant: narrow (the

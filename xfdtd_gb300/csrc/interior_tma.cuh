@@ -159,6 +159,26 @@ __device__ __forceinline__ ItBlock it_block(const InteriorBox &in, int chunk, ui
   return b;
 }
 
+// The CPML context of plane i for the thread's cells: the row's y and z
+// context `cyz` with the x slot and profile values of index i (E half 0,
+// H half 1).  Plane i is the same for every thread of the block, so every
+// thread loads them, unconditionally (on the plain x planes the slot is
+// -1, as no CPML index lies in the plain run, and the profile stays the
+// identity).  Loaded only for the cells whose class has the x bit, through
+// references into a per-thread context, the x part was lost in the builds
+// without the 5-block cap for the cells in both an x and a y slab.
+template <typename T, typename I, int MODE>
+__device__ __forceinline__ SlabCtx<T> it_plane_ctx(const VolCore<T, I> &p, int half, int i, const SlabCtx<T> &cyz) {
+  SlabCtx<T> cx = cyz;
+  if constexpr (MODE != 0) {
+    const CpmlAxis<T> &ax = p.cp[0];
+    const int xs = ax.n_layers ? __ldg((half ? ax.slot_h : ax.slot_e) + i) : -1;
+    cx.xs = xs;
+    cx.X = half ? axis_coef(xs, ax.b_m, ax.a_m, ax.rk_m, i) : axis_coef(xs, ax.b_e, ax.a_e, ax.rk_e, i);
+  }
+  return cx;
+}
+
 // Stage bookkeeping of one block (thread 0 issues and drains; every thread
 // waits).  A wait that gives up marks the block timed out; the block then
 // stops, and thread 0 waits (bounded) for the loads it issued before the
@@ -230,27 +250,20 @@ __device__ __forceinline__ void it_e_block(const ItMaps &maps, const VolCore<T, 
   const bool mine = j <= in.hi[1] && k <= blk.khi;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
   // the CPML context of the thread's row and column, fixed over the planes
-  SlabCtx<T> cx = slab_ctx<T, I, 0>(p, 0, 0, 0, 0);
+  SlabCtx<T> cyz = slab_ctx<T, I, 0>(p, 0, 0, 0, 0);
   const bool yspec = MODE != 0 && (j < in.py_lo || j > in.py_hi);
   if (MODE != 0 && mine) {
-    if (yspec) slab_axis(p, 1, 0, j, cx.ys, cx.Y);
-    if (MODE == 2) slab_axis(p, 2, 0, k, cx.zs, cx.Z);
+    if (yspec) slab_axis(p, 1, 0, j, cyz.ys, cyz.Y);
+    if (MODE == 2) slab_axis(p, 2, 0, k, cyz.zs, cyz.Z);
   }
   // the incident H arrays of the previous step (the 1-D line's other buffer)
   const auto hinc = (MODE != 0 && TF) ? tfsf_view<T>(fz.tf).inc + ((*fz.step + 1) & 1) * 6 * fz.tf.L : nullptr;
   for (int i = blk.ia; i < blk.ib; ++i) {
     // a special cell's psi operands, loaded before the wait for the plane
     const int cls = MODE == 0 ? 0 : ((i < in.px_lo || i > in.px_hi) ? 1 : 0) | (yspec ? 2 : 0) | (MODE == 2 ? 4 : 0);
+    const SlabCtx<T> cx = it_plane_ctx<T, I, MODE>(p, 0, i, cyz);
     PsiOps<T> ps{};
-    if (MODE != 0 && mine && cls != 0) {
-      if (cls & 1) {
-        slab_axis(p, 0, 0, i, cx.xs, cx.X);
-      } else {
-        cx.xs = -1;
-        cx.X = AxisCoef<T>{T(0), T(0), T(1)};
-      }
-      ps = e_psi_load<T, I, 7>(p, cx, i, j, k, p.psi);
-    }
+    if (MODE != 0 && mine && cls != 0) ps = e_psi_load<T, I, 7>(p, cx, i, j, k, p.psi);
     const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
     const unsigned m_plain = (!G::IDX && mine) ? static_cast<unsigned>(__ldg(p.idx + b)) : 0u;
     if (ring.wait(stage_of(i))) waited = i;
@@ -360,26 +373,19 @@ __device__ __forceinline__ void it_h_block(const ItMaps &maps, const VolCore<T, 
   const int j = blk.j0 + r, k = blk.k0 + c;
   const bool mine = j <= in.hi[1] && k <= blk.khi;
   const unsigned usj = static_cast<unsigned>(p.d.sj), usi = static_cast<unsigned>(p.d.si);
-  SlabCtx<T> cx = slab_ctx<T, I, 0>(p, 1, 0, 0, 0);
+  SlabCtx<T> cyz = slab_ctx<T, I, 0>(p, 1, 0, 0, 0);
   const bool yspec = MODE != 0 && (j < in.py_lo || j > in.py_hi);
   if (MODE != 0 && mine) {
-    if (yspec) slab_axis(p, 1, 1, j, cx.ys, cx.Y);
-    if (MODE == 2) slab_axis(p, 2, 1, k, cx.zs, cx.Z);
+    if (yspec) slab_axis(p, 1, 1, j, cyz.ys, cyz.Y);
+    if (MODE == 2) slab_axis(p, 2, 1, k, cyz.zs, cyz.Z);
   }
   // the incident E arrays of this step (written by the 1-D line beside the E update)
   const auto einc = (MODE != 0 && TF) ? tfsf_view<T>(fz.tf).inc + (*fz.step & 1) * 6 * fz.tf.L : nullptr;
   for (int i = blk.ia; i < blk.ib; ++i) {
     const int cls = MODE == 0 ? 0 : ((i < in.px_lo || i > in.px_hi) ? 1 : 0) | (yspec ? 2 : 0) | (MODE == 2 ? 4 : 0);
+    const SlabCtx<T> cx = it_plane_ctx<T, I, MODE>(p, 1, i, cyz);
     PsiOps<T> pv{};
-    if (MODE != 0 && mine && cls != 0) {
-      if (cls & 1) {
-        slab_axis(p, 0, 1, i, cx.xs, cx.X);
-      } else {
-        cx.xs = -1;
-        cx.X = AxisCoef<T>{T(0), T(0), T(1)};
-      }
-      pv = h_psi_load<T, I, 7>(p, cx, i, j, k);
-    }
+    if (MODE != 0 && mine && cls != 0) pv = h_psi_load<T, I, 7>(p, cx, i, j, k);
     const unsigned b = static_cast<unsigned>(i) * usi + static_cast<unsigned>(j) * usj + static_cast<unsigned>(k);
     const unsigned m_plain = (!G::IDX && mine) ? static_cast<unsigned>(__ldg(p.idx + b)) : 0u;
     if (ring.wait(stage_of(i + 1))) waited = i + 1;
