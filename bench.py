@@ -605,7 +605,7 @@ def run_dielectric_form(args, local):
     12-cell CPML (280^3 cells), eps_r 4 sphere of radius 60 cells, TFSF
     x-polarised +z Gaussian plane wave (tau = 40 dt), NF-FF DFT at 1, 2 and
     3 GHz, bistatic RCS at 181 angles in two planes, 2000 steps.  FP32 form
-    (the benchmark spec's 70 % target): timed steps, roofline, the whole job end
+    (its update's target: 70 % of the copy bandwidth): timed steps, roofline, the whole job end
     to end; FP64 form likewise, with the FP32 RCS error against it."""
     sc, job_steps = configs.dielectric_sphere()
     fused = False   # the split E and H kernels (the fused sweep is slower on this grid)
