@@ -1,4 +1,4 @@
-"""TEST INFRASTRUCTURE ONLY -- the CPU checker for the GPU engine.
+"""TEST INFRASTRUCTURE ONLY -- the CPU oracle the GPU engine is tested against.
 
 ctypes binding of the FP64 CPU restatement of the reference XFDTD step loop
 (oracle/xfdtd_oracle.cpp).  Only the tests, the smoke check and the

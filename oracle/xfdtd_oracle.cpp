@@ -1,4 +1,4 @@
-// xfdtd_oracle.cpp -- TEST INFRASTRUCTURE ONLY (the checker, never the product).
+// xfdtd_oracle.cpp -- TEST INFRASTRUCTURE ONLY (the oracle, never the product).
 //
 // Plain C++17 FP64 restatement of the reference XFDTD step loop and its setup,
 // following the reference sources line by line (citations are paths inside

@@ -2,7 +2,7 @@
  * xfdtd_oracle.h -- TEST INFRASTRUCTURE ONLY.
  *
  * CPU restatement, in plain C++17 FP64, of the reference XFDTD time-stepping
- * path (Mrwatermolen/XFDTD).  It is the checker the GPU engine is compared
+ * path (Mrwatermolen/XFDTD).  It is the oracle the GPU engine is compared
  * with; nothing in the product links or calls it.  Only the tests, the smoke
  * check and the benchmark's CPU-baseline leg load it.
  *

@@ -1,5 +1,5 @@
-"""Pins the CPU oracle (FP64 restatement of the reference) before it is
-trusted as the GPU engine's checker.
+"""Pins the CPU oracle (FP64 restatement of the reference) before the GPU
+engine is tested against it.
 
 * test/test_grid.cpp of the reference, restated: uniform GridSpace counts
   and node sizes for seeded random cubes.

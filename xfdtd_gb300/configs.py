@@ -2,7 +2,7 @@
 
 Every builder returns (Scene, total_steps).  `scale` shrinks the interior
 (cell counts are divided by it, CPML and TFSF / NF-FF offsets are kept) so
-that the same scene family can be run at sizes a CPU checker finishes in
+that the same scene family can be run at sizes the CPU oracle finishes in
 seconds.
 
   pec_sphere_rcs      3-D PEC sphere bistatic RCS: 40^3 interior + 8-cell
